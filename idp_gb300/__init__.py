@@ -1,0 +1,257 @@
+"""GB300 implementation of IDP's injective-deformation Newton step.
+
+The compute path is the C-ABI library ``libidp_gb300.so`` (hand-written
+sm_103a CUDA kernels + C++ host driver, declared in ``include/idp_gb300.h``).
+This package only binds it (ctypes) and mirrors the reference's Python-facing
+interface. There is no CPU fallback: importing the bindings without the
+library raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libidp_gb300.so")
+
+IDP_OK = 0
+IDP_ERR_INVALID_ARG = 1
+IDP_ERR_CUDA = 2
+IDP_ERR_CAPACITY = 3
+IDP_ERR_INVERTED = 4
+IDP_ERR_NOT_CONVERGED = 5
+IDP_ERR_ZERO_STEP = 6
+IDP_ERR_NONPOSITIVE_DIST = 7
+IDP_ERR_STATE = 8
+IDP_WARN_ITER_CAP = 9
+MODE_FP64 = 0
+MODE_MIXED = 1
+
+# every entry point include/idp_gb300.h declares
+EXPORTS = [
+    "idp_default_params", "idp_create", "idp_destroy", "idp_status_str", "idp_add_instance", "idp_set_velocity",
+    "idp_set_positions", "idp_commit", "idp_advance", "idp_get_state", "idp_instance_info", "idp_get_surface",
+    "idp_eval_energy", "idp_eval_gradient", "idp_constraint_set", "idp_ccd_stepsize", "idp_hessian_apply",
+    "idp_newton_direction",
+]
+
+
+class Params(C.Structure):
+    _fields_ = [("h", C.c_double), ("newton_tol", C.c_double), ("max_newton", C.c_int), ("mode", C.c_int),
+                ("pcg_rel_tol", C.c_double), ("pcg_max_iters", C.c_int), ("thickness", C.c_double),
+                ("device", C.c_int)]
+
+
+class Result(C.Structure):
+    _fields_ = [("status", C.c_int), ("newton_iters", C.c_int), ("pcg_iters", C.c_int), ("ls_trials", C.c_int),
+                ("num_constraints", C.c_int), ("energy", C.c_double), ("kappa", C.c_double),
+                ("residual", C.c_double), ("min_alpha", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class IDPError(RuntimeError):
+    def __init__(self, code, where=""):
+        self.code = code
+        super().__init__(f"{where}: {status_str(code)} ({code})")
+
+
+_lib = None
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int32)
+
+
+def load(path: str | None = None):
+    """Load the C-ABI library; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise ImportError(f"{p} not found: build it with `python -c 'import __graft_entry__ as g; g.build()'` "
+                          "(there is no CPU fallback)")
+    L = C.CDLL(p)
+    L.idp_create.restype = C.c_void_p
+    L.idp_create.argtypes = [C.POINTER(Params), C.POINTER(C.c_int)]
+    L.idp_destroy.argtypes = [C.c_void_p]
+    L.idp_status_str.restype = C.c_char_p
+    L.idp_default_params.argtypes = [C.POINTER(Params)]
+    L.idp_add_instance.argtypes = [C.c_void_p, C.c_int, _dp, _dp, C.c_int, _ip, _dp, _dp, _dp, C.c_int, _ip,
+                                   C.c_double, C.c_double, C.c_double]
+    L.idp_set_velocity.argtypes = [C.c_void_p, C.c_int, _dp]
+    L.idp_set_positions.argtypes = [C.c_void_p, C.c_int, _dp]
+    L.idp_commit.argtypes = [C.c_void_p]
+    L.idp_advance.argtypes = [C.c_void_p, C.POINTER(Result)]
+    L.idp_get_state.argtypes = [C.c_void_p, C.c_int, _dp, _dp, _dp]
+    L.idp_instance_info.argtypes = [C.c_void_p, C.c_int] + [C.POINTER(C.c_int)] * 5
+    L.idp_get_surface.argtypes = [C.c_void_p, C.c_int, _ip, _ip, _ip]
+    L.idp_eval_energy.argtypes = [C.c_void_p, C.c_int, _dp, _dp, _dp, _dp]
+    L.idp_eval_gradient.argtypes = [C.c_void_p, C.c_int, _dp, _dp]
+    L.idp_constraint_set.argtypes = [C.c_void_p, C.c_int, _dp, C.c_int, _ip, C.POINTER(C.c_int)]
+    L.idp_ccd_stepsize.argtypes = [C.c_void_p, C.c_int, _dp, _dp, _dp]
+    L.idp_hessian_apply.argtypes = [C.c_void_p, C.c_int, _dp, _dp, _dp]
+    L.idp_newton_direction.argtypes = [C.c_void_p, C.c_int, _dp, _dp, C.POINTER(C.c_int), _dp]
+    _lib = L
+    return L
+
+
+def status_str(code: int) -> str:
+    try:
+        return load().idp_status_str(int(code)).decode()
+    except ImportError:
+        return str(code)
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def _pd(a):
+    return a.ctypes.data_as(_dp)
+
+
+def _pi(a):
+    return a.ctypes.data_as(_ip)
+
+
+def default_params(**kw) -> Params:
+    p = Params()
+    load().idp_default_params(C.byref(p))
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+class Context:
+    """One device arena holding any number of mesh instances."""
+
+    def __init__(self, **params):
+        L = load()
+        self.params = default_params(**params)
+        st = C.c_int()
+        self._h = L.idp_create(C.byref(self.params), C.byref(st))
+        if not self._h:
+            raise IDPError(st.value, "idp_create")
+        self._V = []
+        self.committed = False
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().idp_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc, where, ok=(IDP_OK,)):
+        if rc not in ok:
+            raise IDPError(rc, where)
+        return rc
+
+    def add_instance(self, X, tets, mass, lam, mu, dHat2, kappa, kappa_max, X0=None, dbc_idx=None):
+        X, tets, mass = _f64(X).reshape(-1, 3), _i32(tets).reshape(-1, 4), _f64(mass)
+        V, T = X.shape[0], tets.shape[0]
+        lam = _f64(np.broadcast_to(lam, (T,)))
+        mu = _f64(np.broadcast_to(mu, (T,)))
+        X0 = X if X0 is None else _f64(X0).reshape(-1, 3)
+        dbc = _i32(np.zeros(0) if dbc_idx is None else dbc_idx)
+        r = load().idp_add_instance(self._h, V, _pd(X), _pd(X0), T, _pi(tets), _pd(mass), _pd(lam), _pd(mu),
+                                    dbc.size, _pi(dbc), float(dHat2), float(kappa), float(kappa_max))
+        if r < 0:
+            raise IDPError(-r, "idp_add_instance")
+        self._V.append(V)
+        return r
+
+    def set_velocity(self, i, v):
+        v = _f64(v)
+        self._check(load().idp_set_velocity(self._h, i, _pd(v)), "idp_set_velocity")
+
+    def set_positions(self, i, X):
+        X = _f64(X)
+        self._check(load().idp_set_positions(self._h, i, _pd(X)), "idp_set_positions")
+
+    def commit(self):
+        self._check(load().idp_commit(self._h), "idp_commit")
+        self.committed = True
+
+    def advance(self, check=True):
+        res = (Result * len(self._V))()
+        rc = load().idp_advance(self._h, res)
+        out = [r.as_dict() for r in res]
+        if check:
+            self._check(rc, "idp_advance", ok=(IDP_OK, IDP_WARN_ITER_CAP))
+        return rc, out
+
+    def state(self, i):
+        V = self._V[i]
+        X, v, k = np.zeros((V, 3)), np.zeros((V, 3)), np.zeros(3)
+        self._check(load().idp_get_state(self._h, i, _pd(X), _pd(v), _pd(k)), "idp_get_state")
+        return X, v, k
+
+    def surface(self, i):
+        a = [C.c_int() for _ in range(5)]
+        self._check(load().idp_instance_info(self._h, i, *[C.byref(x) for x in a]), "idp_instance_info")
+        nn, ne, nt = a[2].value, a[3].value, a[4].value
+        nodes, edges, tris = np.zeros(nn, np.int32), np.zeros((ne, 2), np.int32), np.zeros((nt, 3), np.int32)
+        self._check(load().idp_get_surface(self._h, i, _pi(nodes), _pi(edges), _pi(tris)), "idp_get_surface")
+        return dict(nodes=nodes, edges=edges, tris=tris)
+
+    # ---- sub-steps (tests and callers that drive their own loop)
+    def energy(self, i, X):
+        X = _f64(X)
+        e = [C.c_double() for _ in range(3)]
+        rc = load().idp_eval_energy(self._h, i, _pd(X), *[C.byref(x) for x in e])
+        if rc == IDP_ERR_INVERTED:
+            return None
+        self._check(rc, "idp_eval_energy")
+        return tuple(x.value for x in e)
+
+    def gradient(self, i, X):
+        X = _f64(X)
+        g = np.zeros(X.size)
+        self._check(load().idp_eval_gradient(self._h, i, _pd(X), _pd(g)), "idp_eval_gradient")
+        return g
+
+    def constraint_set(self, i, X, cap=None):
+        X = _f64(X)
+        n = C.c_int()
+        cap = cap or max(4096, 16 * self._V[i])
+        while True:
+            buf = np.zeros((cap, 4), np.int32)
+            rc = load().idp_constraint_set(self._h, i, _pd(X), cap, _pi(buf), C.byref(n))
+            if rc == IDP_ERR_CAPACITY:
+                cap = n.value + 16
+                continue
+            self._check(rc, "idp_constraint_set")
+            return buf[: n.value].copy()
+
+    def ccd_stepsize(self, i, X, d, alpha=1.0):
+        X, d = _f64(X), _f64(d)
+        a = C.c_double(alpha)
+        rc = load().idp_ccd_stepsize(self._h, i, _pd(X), _pd(d), C.byref(a))
+        self._check(rc, "idp_ccd_stepsize", ok=(IDP_OK, IDP_WARN_ITER_CAP))
+        return a.value, rc
+
+    def hessian_apply(self, i, X, x):
+        X, x = _f64(X), _f64(x)
+        y = np.zeros(x.size)
+        self._check(load().idp_hessian_apply(self._h, i, _pd(X), _pd(x), _pd(y)), "idp_hessian_apply")
+        return y
+
+    def newton_direction(self, i, X):
+        X = _f64(X)
+        p = np.zeros(X.size)
+        it, rel = C.c_int(), C.c_double()
+        self._check(load().idp_newton_direction(self._h, i, _pd(X), _pd(p), C.byref(it), C.byref(rel)),
+                    "idp_newton_direction")
+        return p, it.value, rel.value

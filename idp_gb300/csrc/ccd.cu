@@ -1,0 +1,562 @@
+// Intersection-free step size (compiled with --fmad=false): GPU restatement
+// of Compute_Intersection_Free_StepSize, 3D tet-surface branch
+// (FEM/IPC.h:1879-2244), with the CCD spatial hash of Grid/SPATIAL_HASH.h:432-622
+// and additive CCD of Math/Distance/CCD.h:279-395.
+//
+// The reference's hash changes the result (its span cap lowers the starting
+// step, and pairs whose voxel boxes do not overlap are never tested), so the
+// voxel grid is replicated exactly: voxel size = mean surface-edge length,
+// span cap = alpha * mean|dir| / voxel size, grid corner = min over x and
+// x + alpha*dir minus thickness/2, floor((p - corner) / voxel) per axis. The
+// two means are fixed-order sums (prims.cuh det_sum order) so the oracle can
+// reproduce them bit for bit. A pair is tested iff the integer boxes overlap.
+//
+// Every pair's ACCD result is independent of the order pairs are visited (a
+// pair either finishes below the bound with its own toc, or is discarded), so
+// alpha = min(capped alpha, min over pairs) is exact. ACCD loops carry an
+// iteration cap; a capped pair reports its accumulated (still safe) toc.
+#include "engine.hpp"
+#include "grid.cuh"
+#include "geom.cuh"
+#include "prims.cuh"
+
+namespace idp {
+
+using namespace geo;
+
+namespace {
+
+constexpr int ACCD_MAX_ITERS = 200000;
+
+// fixed-order sum by one CTA of 256 threads (same tiling as det_sum)
+__device__ double cta_det_sum(const double* x, long n, double* scratch) {
+    __shared__ double a[256];
+    if (n <= 0) return 0.0;
+    const double* in = x;
+    long m = n;
+    double* out = scratch;
+    while (true) {
+        long tiles = (m + 2047) / 2048;
+        for (long k = 0; k < tiles; ++k) {
+            double s = 0.0;
+            for (int r = 0; r < 8; ++r) {
+                long i = k * 2048 + r * 256 + threadIdx.x;
+                if (i < m) s += in[i];
+            }
+            a[threadIdx.x] = s;
+            __syncthreads();
+            for (int st = 128; st > 0; st >>= 1) {
+                if (threadIdx.x < st) a[threadIdx.x] += a[threadIdx.x + st];
+                __syncthreads();
+            }
+            if (threadIdx.x == 0) out[k] = a[0];
+            __syncthreads();
+        }
+        if (tiles == 1) {
+            double r = out[0];
+            __syncthreads();
+            return r;
+        }
+        in = out;
+        out = out + tiles;
+        m = tiles;
+    }
+}
+
+__global__ void k_edge_len(long nE, const int2* __restrict__ e, const double* __restrict__ X, double* __restrict__ len) {
+    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nE) return;
+    int2 v = e[i];
+    len[i] = sqrt(sqn(ld3(X, v.x) - ld3(X, v.y)));
+}
+
+__global__ void k_abs_dir(long nN, const int* __restrict__ nodes, const double* __restrict__ dir, double* __restrict__ out) {
+    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nN) return;
+    int v = nodes[i];
+    out[3 * i] = fabs(dir[3 * v]);
+    out[3 * i + 1] = fabs(dir[3 * v + 1]);
+    out[3 * i + 2] = fabs(dir[3 * v + 2]);
+}
+
+// per instance: voxel size, span cap (SPATIAL_HASH.h:455-482)
+__global__ void k_span_cap(int nI, const unsigned char* __restrict__ active, const int* __restrict__ se_off,
+                           const int* __restrict__ sn_off, const double* __restrict__ len,
+                           const double* __restrict__ absdir, double* __restrict__ scratch, double* __restrict__ alpha,
+                           double* __restrict__ voxel_size) {
+    int i = blockIdx.x;
+    if (!active[i]) return;
+    long ne = se_off[i + 1] - se_off[i], nn = sn_off[i + 1] - sn_off[i];
+    double* sc = scratch + 2 * ((long)se_off[i] + 3 * (long)sn_off[i]) / 1024 + 8 * (long)i;
+    double vsz = 1.0;
+    if (ne) {
+        double s = cta_det_sum(len + se_off[i], ne, sc);
+        vsz *= s / (double)ne;
+    }
+    double ps = cta_det_sum(absdir + 3 * (long)sn_off[i], 3 * nn, sc);
+    if (threadIdx.x == 0) {
+        double pSize = ps / (double)(nn * 3);
+        double a = alpha[i];
+        double spanSize = a * pSize / vsz;
+        if (spanSize > 1) a /= spanSize;
+        alpha[i] = a;
+        voxel_size[i] = vsz;
+    }
+}
+
+__global__ void k_ccd_bbox(long nN, const int* __restrict__ nodes, const int* __restrict__ ninst,
+                           const unsigned char* __restrict__ active, const double* __restrict__ X,
+                           const double* __restrict__ dir, const double* __restrict__ alpha,
+                           unsigned long long* __restrict__ bb) {
+    long s = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nN) return;
+    int inst = ninst[s];
+    if (!active[inst]) return;
+    int v = nodes[s];
+    double a = alpha[inst];
+    double p[3] = {X[3 * v], X[3 * v + 1], X[3 * v + 2]};
+    double q[3] = {X[3 * v] + a * dir[3 * v], X[3 * v + 1] + a * dir[3 * v + 1], X[3 * v + 2] + a * dir[3 * v + 2]};
+    unsigned long long* b = bb + 6 * inst;
+    for (int d = 0; d < 3; ++d) {
+        atomicMin(b + d, ord_enc(fmin(p[d], q[d])));
+        atomicMax(b + 3 + d, ord_enc(fmax(p[d], q[d])));
+    }
+}
+
+__global__ void k_bb_init(int nI, unsigned long long* bb) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 6 * nI) return;
+    bb[i] = (i % 6) < 3 ? 0xffffffffffffffffull : 0ull;
+}
+
+// SPATIAL_HASH.h:502-519
+__global__ void k_ccd_grid(int nI, const unsigned char* __restrict__ active, const unsigned long long* __restrict__ bb,
+                           const double* __restrict__ thick, const double* __restrict__ voxel_size,
+                           GridP* __restrict__ gp) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nI) return;
+    GridP g;
+    if (!active[i]) {
+        for (int d = 0; d < 3; ++d) { g.lo[d] = 0; g.n[d] = 1; }
+        g.inv = 1;
+        g.s1 = 2;
+        g.s2 = 4;
+        gp[i] = g;
+        return;
+    }
+    double ht = thick[i] / 2;
+    double lo[3], range[3];
+    for (int d = 0; d < 3; ++d) {
+        lo[d] = ord_dec(bb[6 * i + d]) - ht;
+        double hi = ord_dec(bb[6 * i + 3 + d]) + ht;
+        range[d] = hi - lo[d];
+    }
+    double vs = voxel_size[i];
+    double inv = 1.0 / vs;
+    long vcl[3];
+    for (int d = 0; d < 3; ++d) {
+        long c = (long)ceil(range[d] * inv);
+        vcl[d] = c > 1 ? c : 1;
+    }
+    long amt = vcl[0] * vcl[1] * vcl[2];
+    if (amt > 1e9) {
+        vs *= pow((double)amt / 1.0e9, 1.0 / 3);
+        inv = 1.0 / vs;
+    }
+    int vc[3];
+    for (int d = 0; d < 3; ++d) {
+        int c = (int)ceil(range[d] * inv);
+        vc[d] = c > 1 ? c : 1;
+    }
+    if (vc[0] <= 0 || vc[1] <= 0 || vc[2] <= 0) {
+        double rmax = fmax(range[0], fmax(range[1], range[2]));
+        inv = 1.0 / (rmax * 1.01);
+        vc[0] = vc[1] = vc[2] = 1;
+    }
+    for (int d = 0; d < 3; ++d) { g.lo[d] = lo[d]; g.n[d] = vc[d]; }
+    g.inv = inv;
+    g.s1 = (long)vc[0] + 1;
+    g.s2 = g.s1 * ((long)vc[1] + 1);
+    gp[i] = g;
+}
+
+// swept voxel box of every surface node (SPATIAL_HASH.h:525-533)
+__global__ void k_node_box(long nN, const int* __restrict__ nodes, const int* __restrict__ ninst,
+                           const unsigned char* __restrict__ active, const double* __restrict__ X,
+                           const double* __restrict__ dir, const double* __restrict__ alpha,
+                           const double* __restrict__ thick, const GridP* __restrict__ gp, BoxI* __restrict__ nbox) {
+    long s = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nN) return;
+    int inst = ninst[s];
+    BoxI b;
+    if (!active[inst]) {
+        for (int d = 0; d < 3; ++d) { b.lo[d] = 1; b.hi[d] = 0; }
+        nbox[s] = b;
+        return;
+    }
+    GridP g = gp[inst];
+    int v = nodes[s];
+    double a = alpha[inst], ht = thick[inst] / 2;
+    for (int d = 0; d < 3; ++d) {
+        double p = X[3 * v + d], q = X[3 * v + d] + a * dir[3 * v + d];
+        double mn = fmin(p, q) - ht, mx = fmax(p, q) + ht;
+        b.lo[d] = (int)floor((mn - g.lo[d]) * g.inv);
+        b.hi[d] = (int)floor((mx - g.lo[d]) * g.inv);
+    }
+    nbox[s] = b;
+}
+
+template <int K>
+__global__ void k_prim_box_from_nodes(long n, const int* __restrict__ verts, const int* __restrict__ v2s,
+                                      const BoxI* __restrict__ nbox, BoxI* __restrict__ out) {
+    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    BoxI b = nbox[v2s[verts[K * i]]];
+    for (int k = 1; k < K; ++k) {
+        BoxI c = nbox[v2s[verts[K * i + k]]];
+        for (int d = 0; d < 3; ++d) {
+            b.lo[d] = min(b.lo[d], c.lo[d]);
+            b.hi[d] = max(b.hi[d], c.hi[d]);
+        }
+    }
+    out[i] = b;
+}
+
+struct CCand {
+    int a, b;
+};
+
+__device__ __forceinline__ bool swept_far(const double* lo_a, const double* hi_a, const double* lo_b,
+                                          const double* hi_b, double dist) {
+    for (int d = 0; d < 3; ++d)
+        if (lo_a[d] - hi_b[d] > dist || lo_b[d] - hi_a[d] > dist) return true;
+    return false;
+}
+
+__global__ void k_ccd_query_pt(long nN, const int* __restrict__ nodes, const int* __restrict__ ninst,
+                               const unsigned char* __restrict__ active, const double* __restrict__ X,
+                               const double* __restrict__ dir, const unsigned char* __restrict__ dbc,
+                               const int* __restrict__ tris, const BoxI* __restrict__ nbox,
+                               const BoxI* __restrict__ tbox, const GridP* __restrict__ gp,
+                               const double* __restrict__ thick, const uint64_t* __restrict__ ckey,
+                               const uint32_t* __restrict__ cstart, int ncell, const uint32_t* __restrict__ entries,
+                               CCand* __restrict__ out, unsigned int* counter, long cap) {
+    long s = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    bool more = s < nN;
+    int inst = 0, vI = 0;
+    Cursor q;
+    GridP g;
+    double plo[3], phi[3], th = 0;
+    if (more) {
+        inst = ninst[s];
+        more = active[inst] != 0;
+    }
+    if (more) {
+        vI = nodes[s];
+        g = gp[inst];
+        th = thick[inst];
+        cursor_init(q, nbox[s]);
+        for (int d = 0; d < 3; ++d) {
+            double p = X[3 * vI + d], pe = p + dir[3 * vI + d];
+            plo[d] = fmin(p, pe);
+            phi[d] = fmax(p, pe);
+        }
+    }
+    while (__any_sync(0xffffffffu, more)) {
+        bool emit = false;
+        CCand c = {0, 0};
+        if (more) {
+            uint32_t e;
+            if (cursor_next(q, inst, g, ckey, cstart, ncell, e)) {
+                int f = (int)entries[e];
+                if (first_shared_cell(q, tbox[f])) {
+                    int t0 = tris[3 * f], t1 = tris[3 * f + 1], t2 = tris[3 * f + 2];
+                    if (!(vI == t0 || vI == t1 || vI == t2) && !(dbc[vI] && dbc[t0] && dbc[t1] && dbc[t2])) {
+                        double tlo[3], thi[3];
+                        int tv[3] = {t0, t1, t2};
+                        for (int d = 0; d < 3; ++d) {
+                            double mn = X[3 * t0 + d], mx = mn;
+                            for (int k = 0; k < 3; ++k) {
+                                double a = X[3 * tv[k] + d], b = a + dir[3 * tv[k] + d];
+                                mn = fmin(mn, fmin(a, b));
+                                mx = fmax(mx, fmax(a, b));
+                            }
+                            tlo[d] = mn;
+                            thi[d] = mx;
+                        }
+                        if (!swept_far(plo, phi, tlo, thi, th)) { emit = true; c = {(int)s, f}; }
+                    }
+                }
+            } else {
+                more = false;
+            }
+        }
+        warp_emit(emit, c, out, counter, cap);
+    }
+}
+
+__global__ void k_ccd_query_ee(long nE, const int2* __restrict__ edges, const int* __restrict__ einst,
+                               const unsigned char* __restrict__ active, const double* __restrict__ X,
+                               const double* __restrict__ dir, const unsigned char* __restrict__ dbc,
+                               const BoxI* __restrict__ ebox, const GridP* __restrict__ gp,
+                               const double* __restrict__ thick, const uint64_t* __restrict__ ckey,
+                               const uint32_t* __restrict__ cstart, int ncell, const uint32_t* __restrict__ entries,
+                               CCand* __restrict__ out, unsigned int* counter, long cap) {
+    long eI = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    bool more = eI < nE;
+    int inst = 0;
+    int2 mi = {0, 0};
+    Cursor q;
+    GridP g;
+    double alo[3], ahi[3], th = 0;
+    if (more) {
+        inst = einst[eI];
+        more = active[inst] != 0;
+    }
+    if (more) {
+        mi = edges[eI];
+        g = gp[inst];
+        th = thick[inst];
+        cursor_init(q, ebox[eI]);
+        int av[2] = {mi.x, mi.y};
+        for (int d = 0; d < 3; ++d) {
+            double mn = X[3 * mi.x + d], mx = mn;
+            for (int k = 0; k < 2; ++k) {
+                double a = X[3 * av[k] + d], b = a + dir[3 * av[k] + d];
+                mn = fmin(mn, fmin(a, b));
+                mx = fmax(mx, fmax(a, b));
+            }
+            alo[d] = mn;
+            ahi[d] = mx;
+        }
+    }
+    while (__any_sync(0xffffffffu, more)) {
+        bool emit = false;
+        CCand c = {0, 0};
+        if (more) {
+            uint32_t e;
+            if (cursor_next(q, inst, g, ckey, cstart, ncell, e)) {
+                int eJ = (int)entries[e];
+                if (eJ > eI && first_shared_cell(q, ebox[eJ])) {
+                    int2 mj = edges[eJ];
+                    if (!(mi.x == mj.x || mi.x == mj.y || mi.y == mj.x || mi.y == mj.y) &&
+                        !(dbc[mi.x] && dbc[mi.y] && dbc[mj.x] && dbc[mj.y])) {
+                        double blo[3], bhi[3];
+                        int bv[2] = {mj.x, mj.y};
+                        for (int d = 0; d < 3; ++d) {
+                            double mn = X[3 * mj.x + d], mx = mn;
+                            for (int k = 0; k < 2; ++k) {
+                                double a = X[3 * bv[k] + d], b = a + dir[3 * bv[k] + d];
+                                mn = fmin(mn, fmin(a, b));
+                                mx = fmax(mx, fmax(a, b));
+                            }
+                            blo[d] = mn;
+                            bhi[d] = mx;
+                        }
+                        if (!swept_far(alo, ahi, blo, bhi, th)) { emit = true; c = {(int)eI, eJ}; }
+                    }
+                }
+            } else {
+                more = false;
+            }
+        }
+        warp_emit(emit, c, out, counter, cap);
+    }
+}
+
+// ---- ACCD (CCD.h:279-328, 330-395)
+__device__ int accd_pt(D3 p, D3 t0, D3 t1, D3 t2, D3 dp, D3 dt0, D3 dt1, D3 dt2, double eta, double thickness,
+                       double& toc) {
+    D3 mov = 0.25 * (((dt0 + dt1) + dt2) + dp);
+    dt0 = dt0 - mov; dt1 = dt1 - mov; dt2 = dt2 - mov; dp = dp - mov;
+    double m2 = fmax(sqn(dt0), fmax(sqn(dt1), sqn(dt2)));
+    double maxDispMag = sqrt(sqn(dp)) + sqrt(m2);
+    if (maxDispMag == 0) return 0;
+    double th2 = thickness * thickness;
+    double dist2_cur = d_PT_unclassified(p, t0, t1, t2);
+    double dist_cur = sqrt(dist2_cur);
+    double gap = eta * (dist2_cur - th2) / (dist_cur + thickness);
+    double toc_prev = toc;
+    toc = 0;
+    for (int it = 0; it < ACCD_MAX_ITERS; ++it) {
+        double tocLB = (1 - eta) * (dist2_cur - th2) / ((dist_cur + thickness) * maxDispMag);
+        p = p + tocLB * dp; t0 = t0 + tocLB * dt0; t1 = t1 + tocLB * dt1; t2 = t2 + tocLB * dt2;
+        dist2_cur = d_PT_unclassified(p, t0, t1, t2);
+        dist_cur = sqrt(dist2_cur);
+        if (toc != 0 && ((dist2_cur - th2) / (dist_cur + thickness) < gap)) return 1;
+        toc += tocLB;
+        if (toc > toc_prev) return 0;
+    }
+    return 2;
+}
+
+__device__ __forceinline__ void ee_eval(D3 ea0, D3 ea1, D3 eb0, D3 eb1, double th2, double& d2, double& dF) {
+    d2 = d_EE_unclassified(ea0, ea1, eb0, eb1);
+    dF = d2 - th2;
+    if (dF <= 0) {
+        d2 = fmin(fmin(sqn(ea0 - eb0), sqn(ea0 - eb1)), fmin(sqn(ea1 - eb0), sqn(ea1 - eb1)));
+        dF = d2 - th2;
+    }
+}
+
+__device__ int accd_ee(D3 ea0, D3 ea1, D3 eb0, D3 eb1, D3 dea0, D3 dea1, D3 deb0, D3 deb1, double eta,
+                       double thickness, double& toc) {
+    D3 mov = 0.25 * (((dea0 + dea1) + deb0) + deb1);
+    dea0 = dea0 - mov; dea1 = dea1 - mov; deb0 = deb0 - mov; deb1 = deb1 - mov;
+    double maxDispMag = sqrt(fmax(sqn(dea0), sqn(dea1))) + sqrt(fmax(sqn(deb0), sqn(deb1)));
+    if (maxDispMag == 0) return 0;
+    double th2 = thickness * thickness;
+    double dist2_cur, dFunc;
+    ee_eval(ea0, ea1, eb0, eb1, th2, dist2_cur, dFunc);
+    double dist_cur = sqrt(dist2_cur);
+    double gap = eta * dFunc / (dist_cur + thickness);
+    double toc_prev = toc;
+    toc = 0;
+    for (int it = 0; it < ACCD_MAX_ITERS; ++it) {
+        double tocLB = (1 - eta) * dFunc / ((dist_cur + thickness) * maxDispMag);
+        ea0 = ea0 + tocLB * dea0; ea1 = ea1 + tocLB * dea1; eb0 = eb0 + tocLB * deb0; eb1 = eb1 + tocLB * deb1;
+        ee_eval(ea0, ea1, eb0, eb1, th2, dist2_cur, dFunc);
+        dist_cur = sqrt(dist2_cur);
+        if (toc != 0 && (dFunc / (dist_cur + thickness) < gap)) return 1;
+        toc += tocLB;
+        if (toc > toc_prev) return 0;
+    }
+    return 2;
+}
+
+// flags per instance: bit 0 = an ACCD hit its cap, bit 1 = zero step
+__global__ void k_accd(long npt, long nee, const CCand* __restrict__ cand, const int* __restrict__ nodes,
+                       const int* __restrict__ ninst, const int* __restrict__ tris, const int2* __restrict__ edges,
+                       const int* __restrict__ einst, const double* __restrict__ X, const double* __restrict__ dir,
+                       const double* __restrict__ thick, const double* __restrict__ alpha_cap,
+                       double* __restrict__ alpha_min, int* __restrict__ flags) {
+    long k = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= npt + nee) return;
+    CCand c = cand[k];
+    int inst;
+    double toc;
+    int r;
+    if (k < npt) {
+        int v = nodes[c.a];
+        inst = ninst[c.a];
+        int t0 = tris[3 * c.b], t1 = tris[3 * c.b + 1], t2 = tris[3 * c.b + 2];
+        toc = alpha_cap[inst];
+        r = accd_pt(ld3(X, v), ld3(X, t0), ld3(X, t1), ld3(X, t2), ld3(dir, v), ld3(dir, t0), ld3(dir, t1),
+                    ld3(dir, t2), 0.1, thick[inst], toc);
+        if (toc == 0) atomicOr(flags + inst, 2);
+    } else {
+        int2 mi = edges[c.a], mj = edges[c.b];
+        inst = einst[c.a];
+        toc = alpha_cap[inst];
+        r = accd_ee(ld3(X, mi.x), ld3(X, mi.y), ld3(X, mj.x), ld3(X, mj.y), ld3(dir, mi.x), ld3(dir, mi.y),
+                    ld3(dir, mj.x), ld3(dir, mj.y), 0.1, thick[inst], toc);
+    }
+    if (r == 2) atomicOr(flags + inst, 1);
+    if (r != 0) atomic_min_nonneg(alpha_min + inst, toc);
+}
+
+__global__ void k_alpha_final(int nI, const unsigned char* __restrict__ active, const double* __restrict__ amin,
+                              double* __restrict__ alpha) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nI || !active[i]) return;
+    alpha[i] = fmin(alpha[i], amin[i]);
+}
+
+__global__ void k_fill(int n, double v, double* a) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) a[i] = v;
+}
+
+}  // namespace
+
+int ccd_stepsize(Arena& A, Work& W, const double* X, const double* dir, double* alpha, int* flags, cudaStream_t s) {
+    const int nI = A.nI;
+    long Se = A.Se > 0 ? A.Se : 1, Sn = A.Sn > 0 ? A.Sn : 1;
+    // scratch layout (doubles): len[Se] | absdir[3Sn] | sum scratch | voxel[nI] | amin[nI]
+    long nsum = 2 * (A.Se + 3 * A.Sn) / 1024 + 16 * (long)nI + 64;
+    if (W[W_CCD_TMP].ensure(sizeof(double) * (Se + 3 * Sn + nsum + 2 * nI + 8))) return IDP_ERR_CUDA;
+    double* len = W[W_CCD_TMP].as<double>();
+    double* absdir = len + Se;
+    double* sumsc = absdir + 3 * Sn;
+    double* vsz = sumsc + nsum;
+    double* amin = vsz + nI;
+    if (W[W_MISC2].ensure(sizeof(int) * (nI + 1) * 2)) return IDP_ERR_CUDA;
+    int* d_se_off = W[W_MISC2].as<int>();
+    int* d_sn_off = d_se_off + nI + 1;
+    IDP_CUDA_TRY(cudaMemcpyAsync(d_se_off, A.se_off.data(), sizeof(int) * (nI + 1), cudaMemcpyHostToDevice, s));
+    IDP_CUDA_TRY(cudaMemcpyAsync(d_sn_off, A.sn_off.data(), sizeof(int) * (nI + 1), cudaMemcpyHostToDevice, s));
+    if (A.Se) k_edge_len<<<grid_for(A.Se), kBlock, 0, s>>>(A.Se, A.sedge, X, len);
+    if (A.Sn) k_abs_dir<<<grid_for(A.Sn), kBlock, 0, s>>>(A.Sn, A.snode, dir, absdir);
+    k_span_cap<<<nI, 256, 0, s>>>(nI, A.active, d_se_off, d_sn_off, len, absdir, sumsc, alpha, vsz);
+    // grid
+    if (W[W_BBOX].ensure(sizeof(unsigned long long) * 6 * nI) || W[W_GRIDP].ensure(sizeof(GridP) * nI))
+        return IDP_ERR_CUDA;
+    unsigned long long* bb = W[W_BBOX].as<unsigned long long>();
+    GridP* gp = W[W_GRIDP].as<GridP>();
+    k_bb_init<<<grid_for(6 * nI), kBlock, 0, s>>>(nI, bb);
+    if (A.Sn) k_ccd_bbox<<<grid_for(A.Sn), kBlock, 0, s>>>(A.Sn, A.snode, A.sn_inst, A.active, X, dir, alpha, bb);
+    k_ccd_grid<<<grid_for(nI), kBlock, 0, s>>>(nI, A.active, bb, A.thickness, vsz, gp);
+    long St = A.St > 0 ? A.St : 1;
+    if (W[W_BOX_A].ensure(sizeof(BoxI) * (St + Se + Sn))) return IDP_ERR_CUDA;
+    BoxI* tbox = W[W_BOX_A].as<BoxI>();
+    BoxI* ebox = tbox + St;
+    BoxI* nbox = ebox + Se;
+    if (A.Sn)
+        k_node_box<<<grid_for(A.Sn), kBlock, 0, s>>>(A.Sn, A.snode, A.sn_inst, A.active, X, dir, alpha, A.thickness, gp,
+                                                     nbox);
+    extern int* g_v2s_hack;
+    (void)0;
+    // triangle / edge boxes from node boxes (v2s: vertex -> surface node)
+    if (A.St)
+        k_prim_box_from_nodes<3><<<grid_for(A.St), kBlock, 0, s>>>(A.St, A.stri, A.v2s, nbox, tbox);
+    if (A.Se)
+        k_prim_box_from_nodes<2><<<grid_for(A.Se), kBlock, 0, s>>>(A.Se, reinterpret_cast<const int*>(A.sedge), A.v2s,
+                                                                   nbox, ebox);
+    BoxGrid gt, ge;
+    int rc = build_box_grid(W, 0, tbox, A.st_inst, A.active, A.St, gp, nI, gt, s);
+    if (rc) return rc;
+    rc = build_box_grid(W, 1, ebox, A.se_inst, A.active, A.Se, gp, nI, ge, s);
+    if (rc) return rc;
+    // candidates
+    if (W[W_CAND_CNT].ensure(64)) return IDP_ERR_CUDA;
+    unsigned int* ccount = W[W_CAND_CNT].as<unsigned int>();
+    long cap = (long)(W[W_CAND].bytes / sizeof(CCand));
+    if (cap < 4 * (A.Sn + A.Se) + 1024) {
+        cap = 4 * (A.Sn + A.Se) + 1024;
+        if (W[W_CAND].ensure(sizeof(CCand) * cap)) return IDP_ERR_CUDA;
+    }
+    for (int attempt = 0; attempt < 6; ++attempt) {
+        CCand* cand = W[W_CAND].as<CCand>();
+        unsigned int hc[2] = {0, 0};
+        IDP_CUDA_TRY(cudaMemsetAsync(ccount, 0, 2 * sizeof(unsigned int), s));
+        if (A.Sn)
+            k_ccd_query_pt<<<grid_for(A.Sn), kBlock, 0, s>>>(A.Sn, A.snode, A.sn_inst, A.active, X, dir, A.dbc, A.stri,
+                                                             nbox, tbox, gp, A.thickness, gt.cell_keys, gt.cell_start,
+                                                             gt.ncell, gt.entries, cand, ccount, cap);
+        IDP_CUDA_TRY(cudaMemcpyAsync(hc, ccount, sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
+        IDP_CUDA_TRY(cudaStreamSynchronize(s));
+        long npt = hc[0];
+        long cap_ee = cap - npt;
+        if (A.Se && cap_ee > 0)
+            k_ccd_query_ee<<<grid_for(A.Se), kBlock, 0, s>>>(A.Se, A.sedge, A.se_inst, A.active, X, dir, A.dbc, ebox, gp,
+                                                             A.thickness, ge.cell_keys, ge.cell_start, ge.ncell,
+                                                             ge.entries, cand + npt, ccount + 1, cap_ee);
+        IDP_CUDA_TRY(cudaMemcpyAsync(hc + 1, ccount + 1, sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
+        IDP_CUDA_TRY(cudaStreamSynchronize(s));
+        long nee = hc[1];
+        if (npt + nee <= cap && (A.Se == 0 || cap_ee > 0)) {
+            k_fill<<<grid_for(nI), kBlock, 0, s>>>(nI, 1e300, amin);
+            IDP_CUDA_TRY(cudaMemsetAsync(flags, 0, sizeof(int) * nI, s));
+            if (npt + nee)
+                k_accd<<<grid_for(npt + nee, 128), 128, 0, s>>>(npt, nee, cand, A.snode, A.sn_inst, A.stri, A.sedge,
+                                                                A.se_inst, X, dir, A.thickness, alpha, amin, flags);
+            k_alpha_final<<<grid_for(nI), kBlock, 0, s>>>(nI, A.active, amin, alpha);
+            return cudaGetLastError() == cudaSuccess ? IDP_OK : IDP_ERR_CUDA;
+        }
+        cap = 2 * (npt + nee) + 1024;
+        if (W[W_CAND].ensure(sizeof(CCand) * cap)) return IDP_ERR_CUDA;
+    }
+    return IDP_ERR_CAPACITY;
+}
+
+}  // namespace idp

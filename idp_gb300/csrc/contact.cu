@@ -1,0 +1,641 @@
+// Constraint-set builder (compiled with --fmad=false): GPU restatement of
+// Compute_Constraint_Set, 3D branch (FEM/IPC.h:143-661).
+//
+//   1. per-instance grid over the surface (cell = rest mean edge length,
+//      origin = min surface-node position), triangles and edges binned into
+//      the cells their integer boxes cover, (instance, cell) radix-sorted;
+//   2. point-triangle and edge-edge queries walk their +-dHat box, report each
+//      candidate once (lowest shared cell) after the reference's exclusions and
+//      AABB test (CCD.h:149-185), compacted warp-cooperatively;
+//   3. narrow phase: FP64 distance type + squared distance, d < dHat^2, and the
+//      sign-tagged int4 encoding of IPC.h:202-250 / 434-554;
+//   4. records sorted by (instance, c0, c1, c2, c3); duplicate regular PP/PE
+//      records merged with multiplicity -count in slot 3 (IPC.h:599-654).
+// The grid is only a conservative filter; membership is decided by the same
+// FP64 tests the reference applies, so the set does not depend on the cell
+// size. The output order is the sort order, independent of thread timing.
+#include "engine.hpp"
+#include "grid.cuh"
+#include "geom.cuh"
+#include "prims.cuh"
+
+namespace idp {
+
+using namespace geo;
+
+namespace {
+
+__global__ void k_bbox(long n, const int* __restrict__ nodes, const int* __restrict__ ninst,
+                       const unsigned char* __restrict__ active, const double* __restrict__ X,
+                       unsigned long long* __restrict__ bb) {
+    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int inst = ninst[i];
+    if (!active[inst]) return;
+    D3 p = ld3(X, nodes[i]);
+    unsigned long long* b = bb + 6 * inst;
+    atomicMin(b + 0, ord_enc(p.x));
+    atomicMin(b + 1, ord_enc(p.y));
+    atomicMin(b + 2, ord_enc(p.z));
+    atomicMax(b + 3, ord_enc(p.x));
+    atomicMax(b + 4, ord_enc(p.y));
+    atomicMax(b + 5, ord_enc(p.z));
+}
+
+__global__ void k_bbox_init(int nI, unsigned long long* bb) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 6 * nI) return;
+    bb[i] = (i % 6) < 3 ? 0xffffffffffffffffull : 0ull;
+}
+
+// grid parameters of the constraint-set grid
+__global__ void k_grid_params(int nI, const unsigned long long* __restrict__ bb, const double* __restrict__ cell,
+                              const double* __restrict__ dHat2, const double* __restrict__ thick,
+                              const unsigned char* __restrict__ active, GridP* __restrict__ gp) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nI) return;
+    GridP g;
+    double r = sqrt(dHat2[i]) + thick[i];
+    double h = cell[i];
+    double ext[3];
+    for (int d = 0; d < 3; ++d) {
+        double lo = ord_dec(bb[6 * i + d]), hi = ord_dec(bb[6 * i + 3 + d]);
+        if (!active[i] || !(hi >= lo)) { lo = 0; hi = 0; }
+        g.lo[d] = lo - 2 * r;
+        ext[d] = (hi - lo) + 4 * r;
+    }
+    if (!(h > 0)) h = 1.0;
+    // keep the cell count per instance below 2^31
+    for (int it = 0; it < 64; ++it) {
+        double c = (floor(ext[0] / h) + 2) * (floor(ext[1] / h) + 2) * (floor(ext[2] / h) + 2);
+        if (c < 2.0e9) break;
+        h *= 1.5;
+    }
+    g.inv = 1.0 / h;
+    for (int d = 0; d < 3; ++d) g.n[d] = (int)floor(ext[d] * g.inv) + 1;
+    g.s1 = (long)g.n[0] + 1;
+    g.s2 = g.s1 * ((long)g.n[1] + 1);
+    gp[i] = g;
+}
+
+__device__ __forceinline__ void vox3(const GridP& g, D3 p, int o[3]) {
+    o[0] = clampi(vox(p.x, g.lo[0], g.inv), 0, g.n[0]);
+    o[1] = clampi(vox(p.y, g.lo[1], g.inv), 0, g.n[1]);
+    o[2] = clampi(vox(p.z, g.lo[2], g.inv), 0, g.n[2]);
+}
+
+template <int K>
+__global__ void k_prim_boxes(long n, const int* __restrict__ verts, const int* __restrict__ pinst,
+                             const unsigned char* __restrict__ active, const double* __restrict__ X,
+                             const GridP* __restrict__ gp, BoxI* __restrict__ boxes) {
+    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int inst = pinst[i];
+    BoxI b;
+    if (!active[inst]) {
+        for (int d = 0; d < 3; ++d) { b.lo[d] = 1; b.hi[d] = 0; }
+        boxes[i] = b;
+        return;
+    }
+    GridP g = gp[inst];
+    int o[3];
+    vox3(g, ld3(X, verts[K * i]), o);
+    for (int d = 0; d < 3; ++d) b.lo[d] = b.hi[d] = o[d];
+    for (int k = 1; k < K; ++k) {
+        vox3(g, ld3(X, verts[K * i + k]), o);
+        for (int d = 0; d < 3; ++d) {
+            b.lo[d] = min(b.lo[d], o[d]);
+            b.hi[d] = max(b.hi[d], o[d]);
+        }
+    }
+    boxes[i] = b;
+}
+
+// ---- generic grid build
+__global__ void k_box_count(long n, const BoxI* __restrict__ boxes, const int* __restrict__ pinst,
+                            const unsigned char* __restrict__ active, uint32_t* __restrict__ cnt) {
+    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    BoxI b = boxes[i];
+    uint32_t c = 0;
+    if (active[pinst[i]] && b.lo[0] <= b.hi[0] && b.lo[1] <= b.hi[1] && b.lo[2] <= b.hi[2])
+        c = (uint32_t)(b.hi[0] - b.lo[0] + 1) * (uint32_t)(b.hi[1] - b.lo[1] + 1) * (uint32_t)(b.hi[2] - b.lo[2] + 1);
+    cnt[i] = c;
+}
+
+__global__ void k_box_emit(long n, const BoxI* __restrict__ boxes, const int* __restrict__ pinst,
+                           const unsigned char* __restrict__ active, const GridP* __restrict__ gp,
+                           const uint32_t* __restrict__ off, uint64_t* __restrict__ keys,
+                           uint32_t* __restrict__ vals) {
+    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int inst = pinst[i];
+    if (!active[inst]) return;
+    BoxI b = boxes[i];
+    GridP g = gp[inst];
+    uint32_t o = off[i];
+    for (int z = b.lo[2]; z <= b.hi[2]; ++z)
+        for (int y = b.lo[1]; y <= b.hi[1]; ++y)
+            for (int x = b.lo[0]; x <= b.hi[0]; ++x) {
+                keys[o] = cell_key(inst, g, x, y, z);
+                vals[o] = (uint32_t)i;
+                ++o;
+            }
+}
+
+__global__ void k_mark_heads(long n, const uint64_t* __restrict__ keys, uint32_t* __restrict__ head) {
+    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    head[i] = (i == 0 || keys[i] != keys[i - 1]) ? 1u : 0u;
+}
+
+__global__ void k_cell_table(long n, const uint64_t* __restrict__ keys, const uint32_t* __restrict__ head,
+                             const uint32_t* __restrict__ idx, uint64_t* __restrict__ ckey,
+                             uint32_t* __restrict__ cstart, const uint32_t* __restrict__ ncell) {
+    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) cstart[*ncell] = (uint32_t)n;
+    if (i >= n) return;
+    if (head[i]) {
+        ckey[idx[i]] = keys[i];
+        cstart[idx[i]] = (uint32_t)i;
+    }
+}
+
+// ---- queries
+struct Cand {
+    int a, b;
+};
+
+__global__ void k_query_pt(long nN, const int* __restrict__ nodes, const int* __restrict__ ninst,
+                           const unsigned char* __restrict__ active, const double* __restrict__ X,
+                           const unsigned char* __restrict__ dbc, const int* __restrict__ tris,
+                           const BoxI* __restrict__ tbox, const GridP* __restrict__ gp,
+                           const double* __restrict__ dHat2, const double* __restrict__ thick,
+                           const uint64_t* __restrict__ ckey, const uint32_t* __restrict__ cstart, int ncell,
+                           const uint32_t* __restrict__ entries, Cand* __restrict__ out, unsigned int* counter,
+                           long cap) {
+    long s = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    bool more = s < nN;
+    int inst = 0, vI = 0;
+    D3 p = {0, 0, 0};
+    double r = 0;
+    Cursor q;
+    GridP g;
+    if (more) {
+        inst = ninst[s];
+        more = active[inst] != 0;
+    }
+    if (more) {
+        vI = nodes[s];
+        p = ld3(X, vI);
+        r = sqrt(dHat2[inst]) + thick[inst];
+        g = gp[inst];
+        double rq = r * (1.0 + 1e-12) + 1e-300;
+        int lo[3], hi[3];
+        vox3(g, mk3(p.x - rq, p.y - rq, p.z - rq), lo);
+        vox3(g, mk3(p.x + rq, p.y + rq, p.z + rq), hi);
+        BoxI qb;
+        for (int d = 0; d < 3; ++d) { qb.lo[d] = lo[d]; qb.hi[d] = hi[d]; }
+        cursor_init(q, qb);
+    }
+    while (__any_sync(0xffffffffu, more)) {
+        bool emit = false;
+        Cand c = {0, 0};
+        if (more) {
+            uint32_t e;
+            if (cursor_next(q, inst, g, ckey, cstart, ncell, e)) {
+                int f = (int)entries[e];
+                if (first_shared_cell(q, tbox[f])) {
+                    int t0 = tris[3 * f], t1 = tris[3 * f + 1], t2 = tris[3 * f + 2];
+                    if (!(vI == t0 || vI == t1 || vI == t2) && !(dbc[vI] && dbc[t0] && dbc[t1] && dbc[t2])) {
+                        D3 a = ld3(X, t0), b = ld3(X, t1), cc = ld3(X, t2);
+                        double mx[3] = {fmax(fmax(a.x, b.x), cc.x), fmax(fmax(a.y, b.y), cc.y), fmax(fmax(a.z, b.z), cc.z)};
+                        double mn[3] = {fmin(fmin(a.x, b.x), cc.x), fmin(fmin(a.y, b.y), cc.y), fmin(fmin(a.z, b.z), cc.z)};
+                        double pp[3] = {p.x, p.y, p.z};
+                        bool far = false;
+                        for (int d = 0; d < 3; ++d)
+                            if (pp[d] - mx[d] > r || mn[d] - pp[d] > r) far = true;
+                        if (!far) { emit = true; c = {(int)s, f}; }
+                    }
+                }
+            } else {
+                more = false;
+            }
+        }
+        warp_emit(emit, c, out, counter, cap);
+    }
+}
+
+__global__ void k_query_ee(long nE, const int2* __restrict__ edges, const int* __restrict__ einst,
+                           const unsigned char* __restrict__ active, const double* __restrict__ X,
+                           const unsigned char* __restrict__ dbc, const BoxI* __restrict__ ebox,
+                           const GridP* __restrict__ gp, const double* __restrict__ dHat2,
+                           const double* __restrict__ thick, const uint64_t* __restrict__ ckey,
+                           const uint32_t* __restrict__ cstart, int ncell, const uint32_t* __restrict__ entries,
+                           Cand* __restrict__ out, unsigned int* counter, long cap) {
+    long eI = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    bool more = eI < nE;
+    int inst = 0;
+    int2 mi = {0, 0};
+    D3 a0 = {0, 0, 0}, a1 = {0, 0, 0};
+    double r = 0;
+    Cursor q;
+    GridP g;
+    if (more) {
+        inst = einst[eI];
+        more = active[inst] != 0;
+    }
+    if (more) {
+        mi = edges[eI];
+        a0 = ld3(X, mi.x);
+        a1 = ld3(X, mi.y);
+        r = sqrt(dHat2[inst]) + thick[inst];
+        g = gp[inst];
+        double rq = r * (1.0 + 1e-12) + 1e-300;
+        int lo[3], hi[3];
+        vox3(g, mk3(fmin(a0.x, a1.x) - rq, fmin(a0.y, a1.y) - rq, fmin(a0.z, a1.z) - rq), lo);
+        vox3(g, mk3(fmax(a0.x, a1.x) + rq, fmax(a0.y, a1.y) + rq, fmax(a0.z, a1.z) + rq), hi);
+        BoxI qb;
+        for (int d = 0; d < 3; ++d) { qb.lo[d] = lo[d]; qb.hi[d] = hi[d]; }
+        cursor_init(q, qb);
+    }
+    while (__any_sync(0xffffffffu, more)) {
+        bool emit = false;
+        Cand c = {0, 0};
+        if (more) {
+            uint32_t e;
+            if (cursor_next(q, inst, g, ckey, cstart, ncell, e)) {
+                int eJ = (int)entries[e];
+                if (eJ > eI && first_shared_cell(q, ebox[eJ])) {
+                    int2 mj = edges[eJ];
+                    if (!(mi.x == mj.x || mi.x == mj.y || mi.y == mj.x || mi.y == mj.y) &&
+                        !(dbc[mi.x] && dbc[mi.y] && dbc[mj.x] && dbc[mj.y])) {
+                        D3 b0 = ld3(X, mj.x), b1 = ld3(X, mj.y);
+                        double amax[3] = {fmax(a0.x, a1.x), fmax(a0.y, a1.y), fmax(a0.z, a1.z)};
+                        double amin[3] = {fmin(a0.x, a1.x), fmin(a0.y, a1.y), fmin(a0.z, a1.z)};
+                        double bmax[3] = {fmax(b0.x, b1.x), fmax(b0.y, b1.y), fmax(b0.z, b1.z)};
+                        double bmin[3] = {fmin(b0.x, b1.x), fmin(b0.y, b1.y), fmin(b0.z, b1.z)};
+                        bool far = false;
+                        for (int d = 0; d < 3; ++d)
+                            if (amin[d] - bmax[d] > r || bmin[d] - amax[d] > r) far = true;
+                        if (!far) { emit = true; c = {(int)eI, eJ}; }
+                    }
+                }
+            } else {
+                more = false;
+            }
+        }
+        warp_emit(emit, c, out, counter, cap);
+    }
+}
+
+// ---- narrow phase
+struct Rec {
+    int4 c;
+    int inst;
+};
+
+__global__ void k_narrow_pt(long K, const Cand* __restrict__ cand, const int* __restrict__ nodes,
+                            const int* __restrict__ ninst, const int* __restrict__ tris,
+                            const double* __restrict__ X, const double* __restrict__ dHat2,
+                            const double* __restrict__ thick, Rec* __restrict__ out, unsigned int* counter,
+                            long cap) {
+    long k = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    bool emit = false;
+    Rec rec;
+    rec.c = make_int4(0, 0, 0, 0);
+    rec.inst = 0;
+    if (k < K) {
+        Cand cd = cand[k];
+        int vI = nodes[cd.a], inst = ninst[cd.a];
+        int t0 = tris[3 * cd.b], t1 = tris[3 * cd.b + 1], t2 = tris[3 * cd.b + 2];
+        D3 p = ld3(X, vI), a = ld3(X, t0), b = ld3(X, t1), c = ld3(X, t2);
+        double r = sqrt(dHat2[inst]) + thick[inst];
+        double r2 = r * r;
+        double d;
+        int4 cc;
+        switch (type_PT(p, a, b, c)) {
+            case 0: d = d_PP(p, a); cc = make_int4(-vI - 1, t0, -1, -1); break;
+            case 1: d = d_PP(p, b); cc = make_int4(-vI - 1, t1, -1, -1); break;
+            case 2: d = d_PP(p, c); cc = make_int4(-vI - 1, t2, -1, -1); break;
+            case 3: d = d_PE(p, a, b); cc = make_int4(-vI - 1, t0, t1, -1); break;
+            case 4: d = d_PE(p, b, c); cc = make_int4(-vI - 1, t1, t2, -1); break;
+            case 5: d = d_PE(p, c, a); cc = make_int4(-vI - 1, t2, t0, -1); break;
+            default: d = d_PT(p, a, b, c); cc = make_int4(-vI - 1, t0, t1, t2); break;
+        }
+        if (d < r2) {
+            emit = true;
+            rec.c = cc;
+            rec.inst = inst;
+        }
+    }
+    warp_emit(emit, rec, out, counter, cap);
+}
+
+__global__ void k_narrow_ee(long K, const Cand* __restrict__ cand, const int2* __restrict__ edges,
+                            const int* __restrict__ einst, const double* __restrict__ X,
+                            const double* __restrict__ X0, const double* __restrict__ dHat2,
+                            const double* __restrict__ thick, Rec* __restrict__ out, unsigned int* counter,
+                            long cap) {
+    long k = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    bool emit = false;
+    Rec rec;
+    rec.c = make_int4(0, 0, 0, 0);
+    rec.inst = 0;
+    if (k < K) {
+        Cand cd = cand[k];
+        int2 mi = edges[cd.a], mj = edges[cd.b];
+        int inst = einst[cd.a];
+        int a0 = mi.x, a1 = mi.y, b0 = mj.x, b1 = mj.y;
+        D3 ea0 = ld3(X, a0), ea1 = ld3(X, a1), eb0 = ld3(X, b0), eb1 = ld3(X, b1);
+        double r = sqrt(dHat2[inst]) + thick[inst];
+        double r2 = r * r;
+        double cn = ee_cross_norm2(ea0, ea1, eb0, eb1);
+        double eps_x = mollifier_threshold(ld3(X0, a0), ld3(X0, a1), ld3(X0, b0), ld3(X0, b1));
+        bool mol = cn < eps_x;
+        double d;
+        int4 c;
+        switch (type_EE(ea0, ea1, eb0, eb1)) {
+            case 0: d = d_PP(ea0, eb0); c = mol ? make_int4(a0, b0, -a1 - 1, -b1 - 1) : make_int4(-a0 - 1, b0, -1, -1); break;
+            case 1: d = d_PP(ea0, eb1); c = mol ? make_int4(a0, b1, -a1 - 1, -b0 - 1) : make_int4(-a0 - 1, b1, -1, -1); break;
+            case 2: d = d_PE(ea0, eb0, eb1); c = mol ? make_int4(a0, b0, b1, -a1 - 1) : make_int4(-a0 - 1, b0, b1, -1); break;
+            case 3: d = d_PP(ea1, eb0); c = mol ? make_int4(a1, b0, -a0 - 1, -b1 - 1) : make_int4(-a1 - 1, b0, -1, -1); break;
+            case 4: d = d_PP(ea1, eb1); c = mol ? make_int4(a1, b1, -a0 - 1, -b0 - 1) : make_int4(-a1 - 1, b1, -1, -1); break;
+            case 5: d = d_PE(ea1, eb0, eb1); c = mol ? make_int4(a1, b0, b1, -a0 - 1) : make_int4(-a1 - 1, b0, b1, -1); break;
+            case 6: d = d_PE(eb0, ea0, ea1); c = mol ? make_int4(b0, a0, a1, -b1 - 1) : make_int4(-b0 - 1, a0, a1, -1); break;
+            case 7: d = d_PE(eb1, ea0, ea1); c = mol ? make_int4(b1, a0, a1, -b0 - 1) : make_int4(-b1 - 1, a0, a1, -1); break;
+            default: d = d_EE(ea0, ea1, eb0, eb1); c = mol ? make_int4(a0, a1, -b0 - 1, b1) : make_int4(a0, a1, b0, b1); break;
+        }
+        if (d < r2) {
+            emit = true;
+            rec.c = c;
+            rec.inst = inst;
+        }
+    }
+    warp_emit(emit, rec, out, counter, cap);
+}
+
+// ---- sort + merge
+__global__ void k_rec_keys(long n, const Rec* __restrict__ recs, int b, int off, uint64_t* __restrict__ klo,
+                           uint32_t* __restrict__ perm) {
+    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int4 c = recs[i].c;
+    klo[i] = ((uint64_t)(uint32_t)(c.z + off) << b) | (uint64_t)(uint32_t)(c.w + off);
+    perm[i] = (uint32_t)i;
+}
+__global__ void k_rec_keys_hi(long n, const Rec* __restrict__ recs, const uint32_t* __restrict__ perm_in, int b,
+                              int off, uint64_t* __restrict__ khi, uint32_t* __restrict__ perm_out) {
+    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t j = perm_in[i];
+    Rec r = recs[j];
+    khi[i] = ((uint64_t)(uint32_t)r.inst << (2 * b)) | ((uint64_t)(uint32_t)(r.c.x + off) << b) |
+             (uint64_t)(uint32_t)(r.c.y + off);
+    perm_out[i] = j;
+}
+
+__device__ __forceinline__ bool same_rec(const Rec& a, const Rec& b) {
+    return a.inst == b.inst && a.c.x == b.c.x && a.c.y == b.c.y && a.c.z == b.c.z && a.c.w == b.c.w;
+}
+
+// head of a run: first record, or differs from predecessor, or not mergeable
+__global__ void k_merge_heads(long n, const Rec* __restrict__ recs, const uint32_t* __restrict__ perm,
+                              uint32_t* __restrict__ head) {
+    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    Rec r = recs[perm[i]];
+    bool mergeable = r.c.x < 0 && r.c.w < 0;
+    bool h = true;
+    if (i > 0 && mergeable) h = !same_rec(r, recs[perm[i - 1]]);
+    head[i] = h ? 1u : 0u;
+}
+
+__global__ void k_merge_write(long n, const Rec* __restrict__ recs, const uint32_t* __restrict__ perm,
+                              const uint32_t* __restrict__ head, const uint32_t* __restrict__ pos,
+                              int4* __restrict__ cons, int* __restrict__ cinst) {
+    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || !head[i]) return;
+    Rec r = recs[perm[i]];
+    int4 c = r.c;
+    if (c.x < 0 && c.w < 0) {
+        long j = i + 1;
+        int cnt = 1;
+        while (j < n && !head[j]) { ++cnt; ++j; }
+        c.w = -cnt;
+    }
+    cons[pos[i]] = c;
+    cinst[pos[i]] = r.inst;
+}
+
+__global__ void k_inst_offsets(int nI, long C, const int* __restrict__ cinst, int* __restrict__ off) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i > nI) return;
+    long lo = 0, hi = C;
+    while (lo < hi) {
+        long mid = (lo + hi) >> 1;
+        if (cinst[mid] < i) lo = mid + 1;
+        else hi = mid;
+    }
+    off[i] = (int)lo;
+}
+
+__global__ void k_min_dist2(long C, const int4* __restrict__ cons, const int* __restrict__ cinst,
+                            const unsigned char* __restrict__ active, const double* __restrict__ X,
+                            double* __restrict__ dist2, double* __restrict__ inst_min) {
+    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= C) return;
+    int inst = cinst[i];
+    Stencil st = decode(cons[i]);
+    double d = stencil_dist2(st, X);
+    if (dist2) dist2[i] = d;
+    if (inst_min && active[inst]) atomic_min_nonneg(inst_min + inst, d);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- host side
+int build_box_grid(Work& W, int slot, const BoxI* boxes, const int* inst, const unsigned char* active, long nprim,
+                   const GridP* gp, int nI, BoxGrid& out, cudaStream_t s) {
+    (void)nI;
+    int base = slot == 0 ? W_GRID0 : W_GRID1;
+    DBuf& bcnt = W[base + 0];
+    DBuf& bkeys = W[base + 1];
+    DBuf& bvals = W[base + 2];
+    DBuf& bkeys2 = W[base + 3];
+    DBuf& bvals2 = W[base + 4];
+    DBuf& bcell = W[base + 5];
+    long np = nprim > 0 ? nprim : 1;
+    if (bcnt.ensure(sizeof(uint32_t) * (np + 1))) return IDP_ERR_CUDA;
+    if (W[W_SCRATCH].ensure(scan_scratch_bytes(np) + 64)) return IDP_ERR_CUDA;
+    uint32_t* cnt = bcnt.as<uint32_t>();
+    k_box_count<<<grid_for(np), kBlock, 0, s>>>(nprim, boxes, inst, active, cnt);
+    if (scan_exclusive(cnt, cnt, nprim, cnt + nprim, W[W_SCRATCH].p, s) != cudaSuccess) return IDP_ERR_CUDA;
+    uint32_t total = 0;
+    IDP_CUDA_TRY(cudaMemcpyAsync(&total, cnt + nprim, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    IDP_CUDA_TRY(cudaStreamSynchronize(s));
+    long ne = total;
+    long nalloc = ne > 0 ? ne : 1;
+    if (bkeys.ensure(8 * nalloc) || bvals.ensure(4 * nalloc) || bkeys2.ensure(8 * nalloc) || bvals2.ensure(4 * nalloc))
+        return IDP_ERR_CUDA;
+    if (bcell.ensure((8 + 4) * (nalloc + 1) + 4 * (nalloc + 1) * 2 + 64)) return IDP_ERR_CUDA;
+    k_box_emit<<<grid_for(np), kBlock, 0, s>>>(nprim, boxes, inst, active, gp, cnt, bkeys.as<uint64_t>(),
+                                               bvals.as<uint32_t>());
+    int bits = 32 + bits_for((uint64_t)(nI > 0 ? nI : 1));
+    if (W[W_SCRATCH].ensure(radix_sort_scratch_bytes(nalloc) + scan_scratch_bytes(nalloc) + 64)) return IDP_ERR_CUDA;
+    if (radix_sort_pairs(bkeys.as<uint64_t>(), bvals.as<uint32_t>(), bkeys2.as<uint64_t>(), bvals2.as<uint32_t>(), ne,
+                         bits, W[W_SCRATCH].p, s) != cudaSuccess)
+        return IDP_ERR_CUDA;
+    // cell table: ckey (8B x (ne+1)) | cstart (4B x (ne+1)) | head | idx
+    uint64_t* ckey = bcell.as<uint64_t>();
+    uint32_t* cstart = reinterpret_cast<uint32_t*>(ckey + nalloc + 1);
+    uint32_t* head = cstart + nalloc + 1;
+    uint32_t* idx = head + nalloc + 1;
+    uint32_t ncell = 0;
+    if (ne > 0) {
+        k_mark_heads<<<grid_for(ne), kBlock, 0, s>>>(ne, bkeys.as<uint64_t>(), head);
+        if (scan_exclusive(head, idx, ne, idx + ne, W[W_SCRATCH].p, s) != cudaSuccess) return IDP_ERR_CUDA;
+        k_cell_table<<<grid_for(ne), kBlock, 0, s>>>(ne, bkeys.as<uint64_t>(), head, idx, ckey, cstart, idx + ne);
+        IDP_CUDA_TRY(cudaMemcpyAsync(&ncell, idx + ne, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+        IDP_CUDA_TRY(cudaStreamSynchronize(s));
+    } else {
+        IDP_CUDA_TRY(cudaMemsetAsync(cstart, 0, sizeof(uint32_t), s));
+    }
+    out.cell_keys = ckey;
+    out.cell_start = cstart;
+    out.entries = bvals.as<uint32_t>();
+    out.ncell = (int)ncell;
+    out.nent = ne;
+    return IDP_OK;
+}
+
+int build_constraint_set(Arena& A, Work& W, const double* X, ContactSet& cs, cudaStream_t s) {
+    const int nI = A.nI;
+    // 1. per-instance grid parameters
+    if (W[W_BBOX].ensure(sizeof(unsigned long long) * 6 * nI) || W[W_GRIDP].ensure(sizeof(GridP) * nI))
+        return IDP_ERR_CUDA;
+    unsigned long long* bb = W[W_BBOX].as<unsigned long long>();
+    GridP* gp = W[W_GRIDP].as<GridP>();
+    k_bbox_init<<<grid_for(6 * nI), kBlock, 0, s>>>(nI, bb);
+    if (A.Sn) k_bbox<<<grid_for(A.Sn), kBlock, 0, s>>>(A.Sn, A.snode, A.sn_inst, A.active, X, bb);
+    k_grid_params<<<grid_for(nI), kBlock, 0, s>>>(nI, bb, A.cell, A.dHat2, A.thickness, A.active, gp);
+    // 2. triangle and edge boxes + grids
+    long St = A.St > 0 ? A.St : 1, Se = A.Se > 0 ? A.Se : 1;
+    if (W[W_BOX_A].ensure(sizeof(BoxI) * St) || W[W_BOX_B].ensure(sizeof(BoxI) * Se)) return IDP_ERR_CUDA;
+    BoxI* tbox = W[W_BOX_A].as<BoxI>();
+    BoxI* ebox = W[W_BOX_B].as<BoxI>();
+    if (A.St) k_prim_boxes<3><<<grid_for(A.St), kBlock, 0, s>>>(A.St, A.stri, A.st_inst, A.active, X, gp, tbox);
+    if (A.Se)
+        k_prim_boxes<2><<<grid_for(A.Se), kBlock, 0, s>>>(A.Se, reinterpret_cast<const int*>(A.sedge), A.se_inst,
+                                                           A.active, X, gp, ebox);
+    BoxGrid gt, ge;
+    int rc = build_box_grid(W, 0, tbox, A.st_inst, A.active, A.St, gp, nI, gt, s);
+    if (rc) return rc;
+    rc = build_box_grid(W, 1, ebox, A.se_inst, A.active, A.Se, gp, nI, ge, s);
+    if (rc) return rc;
+
+    // 3. candidates (PT then EE share one list, PT first)
+    if (W[W_CAND_CNT].ensure(64)) return IDP_ERR_CUDA;
+    unsigned int* ccount = W[W_CAND_CNT].as<unsigned int>();
+    long cap = (long)(W[W_CAND].bytes / sizeof(Cand));
+    if (cap < 4 * (A.Sn + A.Se) + 1024) {
+        cap = 4 * (A.Sn + A.Se) + 1024;
+        if (W[W_CAND].ensure(sizeof(Cand) * cap)) return IDP_ERR_CUDA;
+    }
+    unsigned int hc[2];
+    for (int attempt = 0; attempt < 4; ++attempt) {
+        Cand* cand = W[W_CAND].as<Cand>();
+        IDP_CUDA_TRY(cudaMemsetAsync(ccount, 0, 2 * sizeof(unsigned int), s));
+        if (A.Sn)
+            k_query_pt<<<grid_for(A.Sn), kBlock, 0, s>>>(A.Sn, A.snode, A.sn_inst, A.active, X, A.dbc, A.stri, tbox, gp,
+                                                         A.dHat2, A.thickness, gt.cell_keys, gt.cell_start, gt.ncell,
+                                                         gt.entries, cand, ccount, cap);
+        IDP_CUDA_TRY(cudaMemcpyAsync(hc, ccount, sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
+        IDP_CUDA_TRY(cudaStreamSynchronize(s));
+        long npt = hc[0];
+        long cap_ee = cap - npt;
+        if (A.Se && cap_ee > 0)
+            k_query_ee<<<grid_for(A.Se), kBlock, 0, s>>>(A.Se, A.sedge, A.se_inst, A.active, X, A.dbc, ebox, gp, A.dHat2,
+                                                         A.thickness, ge.cell_keys, ge.cell_start, ge.ncell, ge.entries,
+                                                         cand + npt, ccount + 1, cap_ee);
+        IDP_CUDA_TRY(cudaMemcpyAsync(hc + 1, ccount + 1, sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
+        IDP_CUDA_TRY(cudaStreamSynchronize(s));
+        long nee = hc[1];
+        if (npt + nee <= cap && (A.Se == 0 || cap_ee > 0)) {
+            // 4. narrow phase
+            long rcap = (long)(W[W_CONS_TMP].bytes / sizeof(Rec));
+            if (rcap < npt + nee + 1) {
+                rcap = npt + nee + 1;
+                if (W[W_CONS_TMP].ensure(sizeof(Rec) * rcap)) return IDP_ERR_CUDA;
+            }
+            Rec* recs = W[W_CONS_TMP].as<Rec>();
+            IDP_CUDA_TRY(cudaMemsetAsync(ccount, 0, sizeof(unsigned int), s));
+            if (npt)
+                k_narrow_pt<<<grid_for(npt), kBlock, 0, s>>>(npt, cand, A.snode, A.sn_inst, A.stri, X, A.dHat2, A.thickness,
+                                                             recs, ccount, rcap);
+            if (nee)
+                k_narrow_ee<<<grid_for(nee), kBlock, 0, s>>>(nee, cand + npt, A.sedge, A.se_inst, X, A.X0, A.dHat2,
+                                                             A.thickness, recs, ccount, rcap);
+            unsigned int nrec = 0;
+            IDP_CUDA_TRY(cudaMemcpyAsync(&nrec, ccount, sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
+            IDP_CUDA_TRY(cudaStreamSynchronize(s));
+            long n = nrec;
+            // 5. sort by (inst, c0, c1, c2, c3) and merge PP/PE duplicates
+            long na = n > 0 ? n : 1;
+            if (W[W_CONS_KEY_LO].ensure(8 * na) || W[W_CONS_KEY_HI].ensure(8 * na) || W[W_CONS_PERM].ensure(4 * na) ||
+                W[W_CONS_PERM2].ensure(4 * na) || W[W_CONS_HEAD].ensure(8 * (na + 1)) ||
+                W[W_CONS].ensure(sizeof(int4) * na) || W[W_CONS_INST].ensure(sizeof(int) * na) ||
+                W[W_CONS_OFF].ensure(sizeof(int) * (nI + 1)) || W[W_SCRATCH2].ensure(8 * na + 64) ||
+                W[W_MISC2].ensure(4 * na + 64))
+                return IDP_ERR_CUDA;
+            if (W[W_SCRATCH].ensure(radix_sort_scratch_bytes(na) + scan_scratch_bytes(na) + 64)) return IDP_ERR_CUDA;
+            int b = bits_for((uint64_t)(2 * A.V + 4));
+            int offv = (int)(A.V + 2);
+            uint64_t* klo = W[W_CONS_KEY_LO].as<uint64_t>();
+            uint64_t* khi = W[W_CONS_KEY_HI].as<uint64_t>();
+            uint32_t* p1 = W[W_CONS_PERM].as<uint32_t>();
+            uint32_t* p2 = W[W_CONS_PERM2].as<uint32_t>();
+            uint64_t* kalt = W[W_SCRATCH2].as<uint64_t>();
+            uint32_t* valt = W[W_MISC2].as<uint32_t>();
+            int4* cons = W[W_CONS].as<int4>();
+            int* cinst = W[W_CONS_INST].as<int>();
+            uint32_t total = 0;
+            if (n > 0) {
+                k_rec_keys<<<grid_for(n), kBlock, 0, s>>>(n, recs, b, offv, klo, p1);
+                if (radix_sort_pairs(klo, p1, kalt, valt, n, 2 * b, W[W_SCRATCH].p, s) != cudaSuccess) return IDP_ERR_CUDA;
+                k_rec_keys_hi<<<grid_for(n), kBlock, 0, s>>>(n, recs, p1, b, offv, khi, p2);
+                if (radix_sort_pairs(khi, p2, kalt, valt, n, 2 * b + bits_for((uint64_t)nI), W[W_SCRATCH].p, s) !=
+                    cudaSuccess)
+                    return IDP_ERR_CUDA;
+                uint32_t* head = W[W_CONS_HEAD].as<uint32_t>();
+                uint32_t* pos = head + na + 1;
+                k_merge_heads<<<grid_for(n), kBlock, 0, s>>>(n, recs, p2, head);
+                if (scan_exclusive(head, pos, n, pos + n, W[W_SCRATCH].p, s) != cudaSuccess) return IDP_ERR_CUDA;
+                k_merge_write<<<grid_for(n), kBlock, 0, s>>>(n, recs, p2, head, pos, cons, cinst);
+                IDP_CUDA_TRY(cudaMemcpyAsync(&total, pos + n, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+                IDP_CUDA_TRY(cudaStreamSynchronize(s));
+            }
+            cs.C = total;
+            k_inst_offsets<<<grid_for(nI + 1), kBlock, 0, s>>>(nI, cs.C, cinst, W[W_CONS_OFF].as<int>());
+            cs.off.resize(nI + 1);
+            IDP_CUDA_TRY(cudaMemcpyAsync(cs.off.data(), W[W_CONS_OFF].as<int>(), sizeof(int) * (nI + 1),
+                                         cudaMemcpyDeviceToHost, s));
+            IDP_CUDA_TRY(cudaStreamSynchronize(s));
+            cs.d_off = W[W_CONS_OFF].as<int>();
+            return IDP_OK;
+        }
+        cap = 2 * (npt + nee) + 1024;
+        if (W[W_CAND].ensure(sizeof(Cand) * cap)) return IDP_ERR_CUDA;
+    }
+    return IDP_ERR_CAPACITY;
+}
+
+int constraint_min_dist2(Arena& A, Work& W, const double* X, const int4* cons, const int* cinst, long C,
+                         double* dist2, double* inst_min, cudaStream_t s) {
+    (void)W;
+    if (C <= 0) return IDP_OK;
+    k_min_dist2<<<grid_for(C), kBlock, 0, s>>>(C, cons, cinst, A.active, X, dist2, inst_min);
+    return cudaGetLastError() == cudaSuccess ? IDP_OK : IDP_ERR_CUDA;
+}
+
+}  // namespace idp

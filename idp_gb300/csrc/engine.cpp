@@ -1,0 +1,996 @@
+// Host side of the engine: context, instance upload, static structures
+// (surface primitives in the reference's order, BSR pattern, chunk tables)
+// and the batched Newton driver that restates
+// Advance_One_Step_IE_Discrete_Shell (FEM/Shell/IMPLICIT_EULER.h:151-891) and
+// Line_Search (IMPLICIT_EULER.h:9-149) for tet meshes with offset IPC.
+//
+// Every instance of a context runs its own Newton iteration; the kernels of
+// one Newton iteration serve all instances that are still iterating, and an
+// instance that converges drops out of the launches. Per-instance sums are
+// taken in a fixed order, so an instance's trajectory does not depend on the
+// other instances of the batch.
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <numeric>
+#include <vector>
+#include "engine.hpp"
+
+using namespace idp;
+
+int DBuf::ensure(size_t n) {
+    if (n <= bytes && p) return 0;
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+    size_t want = n < 256 ? 256 : n + n / 4;
+    if (cudaMalloc(&p, want) != cudaSuccess) {
+        p = nullptr;
+        return 1;
+    }
+    bytes = want;
+    return 0;
+}
+void DBuf::release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+}
+
+struct idp_ctx {
+    idp_params P;
+    cudaStream_t s = nullptr;
+    std::vector<HostInstance> inst;
+    std::vector<InstState> st;
+    Arena A;
+    Work W;
+    std::vector<DBuf> owned;  // arena storage
+    bool committed = false;
+    ContactSet cs;
+    long prevC = 0;
+    DBuf inst_buf;            // per-instance device scalars
+    DBuf vel;                 // velocities (3V)
+};
+
+namespace {
+
+template <class T>
+int upload(idp_ctx* c, T*& dst, const std::vector<T>& src) {
+    c->owned.emplace_back();
+    DBuf& b = c->owned.back();
+    if (b.ensure(sizeof(T) * (src.size() + 1))) return IDP_ERR_CUDA;
+    dst = b.as<T>();
+    if (!src.empty() && cudaMemcpy(dst, src.data(), sizeof(T) * src.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+        return IDP_ERR_CUDA;
+    return IDP_OK;
+}
+
+// Surface of a tet mesh in the reference's order: Find_Surface_TriMesh
+// (Utils/MESHIO.h:485-544) keeps faces whose opposite-orientation twin is
+// absent, ordered lexicographically by their oriented vertex triple;
+// Find_Surface_Primitives_And_Compute_Area (MESHIO.h:768-834) takes every edge
+// in the orientation of the first triangle that contains it, ordered
+// lexicographically, and the surface nodes ascending.
+void extract_surface(int V, const std::vector<int>& tets, std::vector<int>& tris, std::vector<int>& edges,
+                     std::vector<int>& nodes) {
+    long T = (long)tets.size() / 4;
+    struct Face {
+        int k[3];
+        int s[3];
+    };
+    std::vector<Face> faces;
+    faces.reserve(4 * T);
+    for (long t = 0; t < T; ++t) {
+        const int* e = &tets[4 * t];
+        int f[4][3] = {{e[0], e[2], e[1]}, {e[0], e[3], e[2]}, {e[0], e[1], e[3]}, {e[1], e[2], e[3]}};
+        for (auto& q : f) {
+            Face F;
+            for (int d = 0; d < 3; ++d) F.k[d] = F.s[d] = q[d];
+            std::sort(F.s, F.s + 3);
+            faces.push_back(F);
+        }
+    }
+    // parity of an oriented triple relative to its sorted order
+    auto parity = [](const int* k) {
+        int inv = (k[0] > k[1]) + (k[0] > k[2]) + (k[1] > k[2]);
+        return inv & 1;
+    };
+    std::vector<long> order(faces.size());
+    std::iota(order.begin(), order.end(), 0);
+    std::sort(order.begin(), order.end(), [&](long a, long b) {
+        const Face &A = faces[a], &B = faces[b];
+        for (int d = 0; d < 3; ++d)
+            if (A.s[d] != B.s[d]) return A.s[d] < B.s[d];
+        return a < b;
+    });
+    std::vector<std::array<int, 3>> bnd;
+    for (size_t i = 0; i < order.size();) {
+        size_t j = i;
+        while (j < order.size() && std::equal(faces[order[j]].s, faces[order[j]].s + 3, faces[order[i]].s)) ++j;
+        // a face is interior iff some face of the group has the opposite parity
+        for (size_t a = i; a < j; ++a) {
+            int pa = parity(faces[order[a]].k);
+            bool twin = false;
+            for (size_t b = i; b < j; ++b)
+                if (b != a && parity(faces[order[b]].k) != pa) twin = true;
+            if (!twin) {
+                const int* k = faces[order[a]].k;
+                bnd.push_back({k[0], k[1], k[2]});
+            }
+        }
+        i = j;
+    }
+    std::sort(bnd.begin(), bnd.end());
+    bnd.erase(std::unique(bnd.begin(), bnd.end()), bnd.end());
+    tris.clear();
+    for (auto& t : bnd) tris.insert(tris.end(), t.begin(), t.end());
+    // edges: orientation of the first triangle (in order) containing them
+    std::map<std::pair<int, int>, std::pair<int, int>> first;  // unordered key -> oriented
+    for (auto& t : bnd) {
+        int pr[3][2] = {{t[0], t[1]}, {t[1], t[2]}, {t[2], t[0]}};
+        for (auto& p : pr) {
+            auto key = std::make_pair(std::min(p[0], p[1]), std::max(p[0], p[1]));
+            if (!first.count(key)) first[key] = {p[0], p[1]};
+        }
+    }
+    std::vector<std::pair<int, int>> ev;
+    for (auto& kv : first) ev.push_back(kv.second);
+    std::sort(ev.begin(), ev.end());
+    edges.clear();
+    for (auto& e : ev) { edges.push_back(e.first); edges.push_back(e.second); }
+    std::vector<char> is(V, 0);
+    for (int v : tris) is[v] = 1;
+    nodes.clear();
+    for (int v = 0; v < V; ++v)
+        if (is[v]) nodes.push_back(v);
+}
+
+void build_chunks(const std::vector<int>& off, std::vector<Chunk>& ch, std::vector<int>& coff) {
+    ch.clear();
+    coff.assign(off.size(), 0);
+    for (size_t i = 0; i + 1 < off.size(); ++i) {
+        coff[i] = (int)ch.size();
+        for (int b = off[i]; b < off[i + 1]; b += kChunk) ch.push_back({(int)i, b, std::min(b + kChunk, off[i + 1])});
+    }
+    coff.back() = (int)ch.size();
+    if (ch.empty()) ch.push_back({0, 0, 0});
+}
+
+// per-instance device scalar layout inside ctx->inst_buf
+enum { S_ETET, S_EINERT, S_EBAR, S_MIND, S_NORM2, S_NUMD };
+enum { SI_BAD, SI_BADB, SI_KFLAG, SI_CCDF, S_NUMI };
+
+double* dsc(idp_ctx* c, int k) { return c->inst_buf.as<double>() + (long)k * c->A.nI; }
+int* isc(idp_ctx* c, int k) { return reinterpret_cast<int*>(c->inst_buf.as<double>() + (long)S_NUMD * c->A.nI) + (long)k * c->A.nI; }
+
+int set_mask(idp_ctx* c, const std::vector<unsigned char>& m) {
+    IDP_CUDA_TRY(cudaMemcpyAsync(c->A.active, m.data(), m.size(), cudaMemcpyHostToDevice, c->s));
+    return IDP_OK;
+}
+
+template <class T>
+int fetch(idp_ctx* c, const T* d, std::vector<T>& h) {
+    h.resize(c->A.nI);
+    IDP_CUDA_TRY(cudaMemcpyAsync(h.data(), d, sizeof(T) * c->A.nI, cudaMemcpyDeviceToHost, c->s));
+    IDP_CUDA_TRY(cudaStreamSynchronize(c->s));
+    return IDP_OK;
+}
+
+// incremental potential of the masked instances at X (INC_POTENTIAL.h:15-152):
+// E = h^2 sum vol*Psi + inertia [+ barrier over a freshly built constraint
+// set]. bad[i] = 1 when a tet is inverted, 2 when a constraint distance is
+// not positive (the reference exits there).
+int eval_energy(idp_ctx* c, const double* X, bool with_barrier, std::vector<double>& E, std::vector<int>& bad) {
+    Arena& A = c->A;
+    const int nI = A.nI;
+    double h2 = c->P.h * c->P.h;
+    IDP_CUDA_TRY(cudaMemsetAsync(isc(c, SI_BAD), 0, sizeof(int) * nI * 2, c->s));
+    IDP_CUDA_TRY(cudaMemsetAsync(dsc(c, S_EBAR), 0, sizeof(double) * nI, c->s));
+    int rc = tet_energy(A, c->W, X, h2, dsc(c, S_ETET), isc(c, SI_BAD), c->s);
+    if (rc) return rc;
+    rc = vec_inertia(A, c->W, X, dsc(c, S_EINERT), nullptr, c->s);
+    if (rc) return rc;
+    if (with_barrier) {
+        rc = barrier_energy(A, c->W, X, c->cs, dsc(c, S_EBAR), isc(c, SI_BADB), c->s);
+        if (rc) return rc;
+    }
+    std::vector<double> et, ei, eb;
+    std::vector<int> b1, b2;
+    if ((rc = fetch(c, dsc(c, S_ETET), et)) || (rc = fetch(c, dsc(c, S_EINERT), ei)) || (rc = fetch(c, dsc(c, S_EBAR), eb)) ||
+        (rc = fetch(c, isc(c, SI_BAD), b1)) || (rc = fetch(c, isc(c, SI_BADB), b2)))
+        return rc;
+    E.resize(nI);
+    bad.resize(nI);
+    for (int i = 0; i < nI; ++i) {
+        E[i] = et[i] + ei[i] + eb[i];
+        bad[i] = b1[i] ? 1 : (b2[i] ? 2 : 0);
+    }
+    return IDP_OK;
+}
+
+// gradient of the masked instances at X into A.g (INC_POTENTIAL.h:154-275),
+// DBC rows zeroed (IMPLICIT_EULER.h:476-480)
+int eval_gradient(idp_ctx* c, const double* X) {
+    Arena& A = c->A;
+    double h2 = c->P.h * c->P.h;
+    int rc = tet_gradient(A, c->W, X, h2, nullptr, c->s);
+    if (rc) return rc;
+    rc = grad_gather_tet(A, c->W, X, A.g, c->s);
+    if (rc) return rc;
+    rc = barrier_gradient(A, c->W, X, c->cs, A.g, c->s);
+    if (rc) return rc;
+    return vec_zero_dbc(A, A.g, c->s);
+}
+
+int eval_hessian(idp_ctx* c, const double* X) {
+    Arena& A = c->A;
+    bool fp64 = c->P.mode == IDP_MODE_FP64;
+    int rc = tet_hessian(A, c->W, X, c->P.h * c->P.h, fp64, c->s);
+    if (rc) return rc;
+    rc = barrier_hessian(A, c->W, X, c->cs, fp64, c->s);
+    if (rc) return rc;
+    return assemble(A, c->W, c->cs, fp64, c->s);
+}
+
+// copy the current constraint set to the "previous" slot with its distances
+int save_prev_set(idp_ctx* c, const double* X) {
+    Arena& A = c->A;
+    Work& W = c->W;
+    long C = c->cs.C;
+    long Ca = C > 0 ? C : 1;
+    if (W[W_PREV_CONS].ensure(sizeof(int4) * Ca) || W[W_PREV_INST].ensure(sizeof(int) * Ca) ||
+        W[W_PREV_DIST2].ensure(sizeof(double) * Ca))
+        return IDP_ERR_CUDA;
+    if (C > 0) {
+        IDP_CUDA_TRY(cudaMemcpyAsync(W[W_PREV_CONS].p, W[W_CONS].p, sizeof(int4) * C, cudaMemcpyDeviceToDevice, c->s));
+        IDP_CUDA_TRY(cudaMemcpyAsync(W[W_PREV_INST].p, W[W_CONS_INST].p, sizeof(int) * C, cudaMemcpyDeviceToDevice, c->s));
+        int rc = constraint_min_dist2(A, W, X, W[W_PREV_CONS].as<int4>(), W[W_PREV_INST].as<int>(), C,
+                                      W[W_PREV_DIST2].as<double>(), nullptr, c->s);
+        if (rc) return rc;
+    }
+    c->prevC = C;
+    return IDP_OK;
+}
+
+}  // namespace
+
+// ============================================================== C ABI
+extern "C" {
+
+void idp_default_params(idp_params* p) {
+    p->h = 0.1;
+    p->newton_tol = 1e-3;
+    p->max_newton = 2000;
+    p->mode = IDP_MODE_MIXED;
+    p->pcg_rel_tol = 1e-6;
+    p->pcg_max_iters = 2000;
+    p->thickness = 0.0;
+    p->device = 0;
+}
+
+const char* idp_status_str(int s) {
+    switch (s) {
+        case IDP_OK: return "ok";
+        case IDP_ERR_INVALID_ARG: return "invalid argument";
+        case IDP_ERR_CUDA: return "CUDA error";
+        case IDP_ERR_CAPACITY: return "capacity exceeded";
+        case IDP_ERR_INVERTED: return "inverted tet (det F <= 0)";
+        case IDP_ERR_NOT_CONVERGED: return "Newton did not converge within max_newton";
+        case IDP_ERR_ZERO_STEP: return "CCD returned a zero step";
+        case IDP_ERR_NONPOSITIVE_DIST: return "non-positive constraint distance";
+        case IDP_ERR_STATE: return "call out of order";
+        case IDP_WARN_ITER_CAP: return "ACCD iteration cap reached (step still conservative)";
+        default: return "unknown status";
+    }
+}
+
+idp_ctx* idp_create(const idp_params* p, int* status) {
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        if (status) *status = IDP_ERR_CUDA;
+        return nullptr;
+    }
+    idp_ctx* c = new idp_ctx();
+    if (p) c->P = *p;
+    else idp_default_params(&c->P);
+    if (cudaSetDevice(c->P.device) != cudaSuccess || cudaStreamCreateWithFlags(&c->s, cudaStreamNonBlocking) != cudaSuccess) {
+        delete c;
+        if (status) *status = IDP_ERR_CUDA;
+        return nullptr;
+    }
+    if (status) *status = IDP_OK;
+    return c;
+}
+
+void idp_destroy(idp_ctx* c) {
+    if (!c) return;
+    cudaSetDevice(c->P.device);
+    cudaStreamSynchronize(c->s);
+    for (auto& b : c->owned) b.release();
+    c->W.release();
+    c->inst_buf.release();
+    c->vel.release();
+    cudaStreamDestroy(c->s);
+    delete c;
+}
+
+int idp_add_instance(idp_ctx* c, int V, const double* X, const double* X0, int T, const int32_t* tets,
+                     const double* mass, const double* lam, const double* mu, int nDBC, const int32_t* dbc_idx,
+                     double dHat2, double kappa, double kappa_max) {
+    if (!c) return -IDP_ERR_INVALID_ARG;
+    if (c->committed) return -IDP_ERR_STATE;
+    if (V <= 0 || T <= 0 || !X || !tets || !mass || !lam || !mu || !(dHat2 > 0)) return -IDP_ERR_INVALID_ARG;
+    HostInstance h;
+    h.V = V;
+    h.T = T;
+    h.X.assign(X, X + 3 * (long)V);
+    h.X0.assign(X0 ? X0 : X, (X0 ? X0 : X) + 3 * (long)V);
+    h.tets.assign(tets, tets + 4 * (long)T);
+    for (int v : h.tets)
+        if (v < 0 || v >= V) return -IDP_ERR_INVALID_ARG;
+    h.mass.assign(mass, mass + V);
+    h.lam.assign(lam, lam + T);
+    h.mu.assign(mu, mu + T);
+    h.dbc.assign(V, 0);
+    for (int k = 0; k < nDBC; ++k) {
+        if (dbc_idx[k] < 0 || dbc_idx[k] >= V) return -IDP_ERR_INVALID_ARG;
+        h.dbc[dbc_idx[k]] = 1;
+    }
+    h.v.assign(3 * (long)V, 0.0);
+    h.dHat2 = dHat2;
+    h.kappa = kappa;
+    h.kappa_max = kappa_max;
+    extract_surface(V, h.tets, h.tris, h.edges, h.nodes);
+    double s = 0;
+    for (size_t e = 0; e + 1 < h.edges.size(); e += 2) {
+        const double* a = &h.X0[3 * h.edges[e]];
+        const double* b = &h.X0[3 * h.edges[e + 1]];
+        s += std::sqrt((a[0] - b[0]) * (a[0] - b[0]) + (a[1] - b[1]) * (a[1] - b[1]) + (a[2] - b[2]) * (a[2] - b[2]));
+    }
+    h.rest_mean_edge = h.edges.empty() ? 1.0 : s / (h.edges.size() / 2);
+    c->inst.push_back(std::move(h));
+    return (int)c->inst.size() - 1;
+}
+
+int idp_set_velocity(idp_ctx* c, int i, const double* v) {
+    if (!c || i < 0 || i >= (int)c->inst.size() || !v) return IDP_ERR_INVALID_ARG;
+    HostInstance& h = c->inst[i];
+    h.v.assign(v, v + 3 * (long)h.V);
+    if (c->committed) {
+        long o = 3L * c->A.v_off[i];
+        IDP_CUDA_TRY(cudaMemcpyAsync(c->vel.as<double>() + o, v, sizeof(double) * 3 * h.V, cudaMemcpyHostToDevice, c->s));
+        IDP_CUDA_TRY(cudaStreamSynchronize(c->s));
+    }
+    return IDP_OK;
+}
+
+int idp_set_positions(idp_ctx* c, int i, const double* X) {
+    if (!c || i < 0 || i >= (int)c->inst.size() || !X) return IDP_ERR_INVALID_ARG;
+    HostInstance& h = c->inst[i];
+    h.X.assign(X, X + 3 * (long)h.V);
+    if (c->committed) {
+        long o = 3L * c->A.v_off[i];
+        IDP_CUDA_TRY(cudaMemcpyAsync(c->A.X + o, X, sizeof(double) * 3 * h.V, cudaMemcpyHostToDevice, c->s));
+        IDP_CUDA_TRY(cudaStreamSynchronize(c->s));
+    }
+    return IDP_OK;
+}
+
+int idp_commit(idp_ctx* c) {
+    if (!c) return IDP_ERR_INVALID_ARG;
+    if (c->committed) return IDP_ERR_STATE;
+    if (c->inst.empty()) return IDP_ERR_INVALID_ARG;
+    cudaSetDevice(c->P.device);
+    Arena& A = c->A;
+    const int nI = (int)c->inst.size();
+    A.nI = nI;
+    A.v_off.assign(nI + 1, 0);
+    A.t_off.assign(nI + 1, 0);
+    A.sn_off.assign(nI + 1, 0);
+    A.se_off.assign(nI + 1, 0);
+    A.st_off.assign(nI + 1, 0);
+    for (int i = 0; i < nI; ++i) {
+        const HostInstance& h = c->inst[i];
+        A.v_off[i + 1] = A.v_off[i] + h.V;
+        A.t_off[i + 1] = A.t_off[i] + h.T;
+        A.sn_off[i + 1] = A.sn_off[i] + (int)h.nodes.size();
+        A.se_off[i + 1] = A.se_off[i] + (int)h.edges.size() / 2;
+        A.st_off[i + 1] = A.st_off[i] + (int)h.tris.size() / 3;
+    }
+    A.V = A.v_off[nI];
+    A.T = A.t_off[nI];
+    A.Sn = A.sn_off[nI];
+    A.Se = A.se_off[nI];
+    A.St = A.st_off[nI];
+    std::vector<double> X, X0, mass, vol, lam, mu, IB, vel, dHat2, kappa, thick, cell;
+    std::vector<unsigned char> dbc;
+    std::vector<int> vinst, snode, sedge, stri, sn_inst, se_inst, st_inst, v2s(A.V, -1);
+    std::vector<int4> tet;
+    for (int i = 0; i < nI; ++i) {
+        const HostInstance& h = c->inst[i];
+        int vo = A.v_off[i];
+        X.insert(X.end(), h.X.begin(), h.X.end());
+        X0.insert(X0.end(), h.X0.begin(), h.X0.end());
+        mass.insert(mass.end(), h.mass.begin(), h.mass.end());
+        lam.insert(lam.end(), h.lam.begin(), h.lam.end());
+        mu.insert(mu.end(), h.mu.begin(), h.mu.end());
+        vel.insert(vel.end(), h.v.begin(), h.v.end());
+        dbc.insert(dbc.end(), h.dbc.begin(), h.dbc.end());
+        vinst.insert(vinst.end(), h.V, i);
+        for (int t = 0; t < h.T; ++t) {
+            const int* e = &h.tets[4 * t];
+            tet.push_back(make_int4(e[0] + vo, e[1] + vo, e[2] + vo, e[3] + vo));
+            // rest basis and volume (FEM/DEFORMATION_GRADIENT.h:38-76)
+            double B[9];
+            for (int m = 0; m < 3; ++m)
+                for (int d = 0; d < 3; ++d) B[d * 3 + m] = h.X0[3 * e[m + 1] + d] - h.X0[3 * e[0] + d];
+            double C0 = B[4] * B[8] - B[5] * B[7], C1 = B[5] * B[6] - B[3] * B[8], C2 = B[3] * B[7] - B[4] * B[6];
+            double J = B[0] * C0 + B[1] * C1 + B[2] * C2;
+            if (!(J > 0)) return IDP_ERR_INVERTED;
+            double Cf[9] = {C0, C1, C2, B[2] * B[7] - B[1] * B[8], B[0] * B[8] - B[2] * B[6], B[1] * B[6] - B[0] * B[7],
+                            B[1] * B[5] - B[2] * B[4], B[2] * B[3] - B[0] * B[5], B[0] * B[4] - B[1] * B[3]};
+            vol.push_back(J / 6.0);
+            for (int r = 0; r < 3; ++r)
+                for (int q = 0; q < 3; ++q) IB.push_back(Cf[q * 3 + r] / J);
+        }
+        for (size_t k = 0; k < h.nodes.size(); ++k) {
+            v2s[h.nodes[k] + vo] = (int)snode.size();
+            snode.push_back(h.nodes[k] + vo);
+            sn_inst.push_back(i);
+        }
+        for (size_t k = 0; k < h.edges.size(); ++k) sedge.push_back(h.edges[k] + vo);
+        se_inst.insert(se_inst.end(), h.edges.size() / 2, i);
+        for (size_t k = 0; k < h.tris.size(); ++k) stri.push_back(h.tris[k] + vo);
+        st_inst.insert(st_inst.end(), h.tris.size() / 3, i);
+        dHat2.push_back(h.dHat2);
+        kappa.push_back(h.kappa);
+        thick.push_back(c->P.thickness);
+        cell.push_back(h.rest_mean_edge);
+        c->st.emplace_back();
+        c->st.back().kappa = h.kappa;
+        c->st.back().kappa_max = h.kappa_max;
+    }
+    int rc = IDP_OK;
+    std::vector<double> zeros(3 * A.V, 0.0);
+    std::vector<int4> tetv(tet);
+    rc |= upload(c, A.X, X);
+    rc |= upload(c, A.X0, X0);
+    rc |= upload(c, A.Xn, X);
+    rc |= upload(c, A.Xtilde, X);
+    rc |= upload(c, A.Xprev, X);
+    rc |= upload(c, A.g, zeros);
+    rc |= upload(c, A.dir, zeros);
+    rc |= upload(c, A.mass, mass);
+    rc |= upload(c, A.dbc, dbc);
+    rc |= upload(c, A.vinst, vinst);
+    rc |= upload(c, A.tet, tetv);
+    rc |= upload(c, A.IB, IB);
+    rc |= upload(c, A.vol, vol);
+    rc |= upload(c, A.lam, lam);
+    rc |= upload(c, A.mu, mu);
+    rc |= upload(c, A.snode, snode);
+    {
+        std::vector<int2> se2(A.Se);
+        for (long e = 0; e < A.Se; ++e) se2[e] = make_int2(sedge[2 * e], sedge[2 * e + 1]);
+        rc |= upload(c, A.sedge, se2);
+    }
+    rc |= upload(c, A.stri, stri);
+    rc |= upload(c, A.sn_inst, sn_inst);
+    rc |= upload(c, A.se_inst, se_inst);
+    rc |= upload(c, A.st_inst, st_inst);
+    rc |= upload(c, A.v2s, v2s);
+    rc |= upload(c, A.dHat2, dHat2);
+    rc |= upload(c, A.kappa, kappa);
+    rc |= upload(c, A.thickness, thick);
+    rc |= upload(c, A.cell, cell);
+    std::vector<unsigned char> act(nI, 1);
+    rc |= upload(c, A.active, act);
+    std::vector<double> alpha(nI, 1.0);
+    rc |= upload(c, A.alpha, alpha);
+    rc |= upload(c, A.d_v_off, A.v_off);
+    // chunk tables
+    std::vector<Chunk> tch, vch;
+    std::vector<int> tco, vco;
+    build_chunks(A.t_off, tch, tco);
+    build_chunks(A.v_off, vch, vco);
+    A.n_tet_chunks = (int)tch.size();
+    A.n_vert_chunks = (int)vch.size();
+    rc |= upload(c, A.tet_chunks, tch);
+    rc |= upload(c, A.vert_chunks, vch);
+    rc |= upload(c, A.tet_chunk_off, tco);
+    rc |= upload(c, A.vert_chunk_off, vco);
+    // BSR pattern of the tet stencil + contributor lists (fixed order)
+    {
+        std::vector<std::pair<long, int>> keys;  // (row*V + col, code)
+        keys.reserve(16 * A.T);
+        for (long t = 0; t < A.T; ++t) {
+            int v[4] = {tet[t].x, tet[t].y, tet[t].z, tet[t].w};
+            for (int a = 0; a < 4; ++a)
+                for (int b = 0; b < 4; ++b) {
+                    int lo = std::min(a, b), hi = std::max(a, b);
+                    int k = lo * 4 - lo * (lo - 1) / 2 + (hi - lo);
+                    int code = (int)((t * 10 + k) * 2 + (a > b ? 1 : 0));
+                    keys.push_back({(long)v[a] * A.V + v[b], code});
+                }
+        }
+        std::stable_sort(keys.begin(), keys.end(),
+                         [](const std::pair<long, int>& x, const std::pair<long, int>& y) { return x.first < y.first; });
+        std::vector<int> rowptr(A.V + 1, 0), colidx, brow, src_ptr, src, diag(A.V, -1);
+        for (size_t i = 0; i < keys.size();) {
+            size_t j = i;
+            while (j < keys.size() && keys[j].first == keys[i].first) ++j;
+            int r = (int)(keys[i].first / A.V), col = (int)(keys[i].first % A.V);
+            if (r == col) diag[r] = (int)colidx.size();
+            colidx.push_back(col);
+            brow.push_back(r);
+            src_ptr.push_back((int)src.size());
+            for (size_t k = i; k < j; ++k) src.push_back(keys[k].second);
+            rowptr[r + 1]++;
+            i = j;
+        }
+        src_ptr.push_back((int)src.size());
+        for (long v = 0; v < A.V; ++v) rowptr[v + 1] += rowptr[v];
+        A.B = (long)colidx.size();
+        // vertices without tets still need a diagonal block
+        for (long v = 0; v < A.V; ++v)
+            if (diag[v] < 0) return IDP_ERR_INVALID_ARG;
+        rc |= upload(c, A.rowptr, rowptr);
+        rc |= upload(c, A.colidx, colidx);
+        rc |= upload(c, A.brow, brow);
+        rc |= upload(c, A.src_ptr, src_ptr);
+        rc |= upload(c, A.src, src);
+        rc |= upload(c, A.diagblk, diag);
+        // vertex -> (tet, corner) lists in tet order
+        std::vector<int> vcp(A.V + 1, 0), vc(4 * A.T);
+        for (long t = 0; t < A.T; ++t) {
+            vcp[tet[t].x + 1]++; vcp[tet[t].y + 1]++; vcp[tet[t].z + 1]++; vcp[tet[t].w + 1]++;
+        }
+        for (long v = 0; v < A.V; ++v) vcp[v + 1] += vcp[v];
+        std::vector<int> fill(vcp.begin(), vcp.end() - 1);
+        for (long t = 0; t < A.T; ++t) {
+            int v[4] = {tet[t].x, tet[t].y, tet[t].z, tet[t].w};
+            for (int a = 0; a < 4; ++a) vc[fill[v[a]]++] = (int)(4 * t + a);
+        }
+        rc |= upload(c, A.vert_corner_ptr, vcp);
+        rc |= upload(c, A.vert_corner, vc);
+    }
+    if (c->inst_buf.ensure(sizeof(double) * (S_NUMD + S_NUMI) * (nI + 1))) rc = IDP_ERR_CUDA;
+    if (c->vel.ensure(sizeof(double) * 3 * (A.V + 1))) rc = IDP_ERR_CUDA;
+    else if (cudaMemcpy(c->vel.p, vel.data(), sizeof(double) * 3 * A.V, cudaMemcpyHostToDevice) != cudaSuccess)
+        rc = IDP_ERR_CUDA;
+    if (rc) return IDP_ERR_CUDA;
+    c->committed = true;
+    return IDP_OK;
+}
+
+int idp_advance(idp_ctx* c, idp_result* results) {
+    if (!c) return IDP_ERR_INVALID_ARG;
+    if (!c->committed) return IDP_ERR_STATE;
+    cudaSetDevice(c->P.device);
+    Arena& A = c->A;
+    Work& W = c->W;
+    const int nI = A.nI;
+    const double h = c->P.h;
+    const bool fp64 = c->P.mode == IDP_MODE_FP64;
+    cudaStream_t s = c->s;
+    int rc;
+    std::vector<unsigned char> all(nI, 1), mask(nI, 0);
+    if ((rc = set_mask(c, all))) return rc;
+    // x^n and x_tilde = x^n + h v (IMPLICIT_EULER.h:195-216)
+    IDP_CUDA_TRY(cudaMemcpyAsync(A.Xn, A.X, sizeof(double) * 3 * A.V, cudaMemcpyDeviceToDevice, s));
+    if ((rc = vec_xtilde(A, A.X, c->vel.as<double>(), h, A.Xtilde, s))) return rc;
+    std::vector<InstState>& st = c->st;
+    for (int i = 0; i < nI; ++i) {
+        InstState& S = st[i];
+        double k = S.kappa, km = S.kappa_max;
+        S = InstState();
+        S.kappa = k;
+        S.kappa_max = km;
+        S.active = true;
+        S.min_alpha = 1.0;
+    }
+    std::vector<double> kap(nI);
+    for (int i = 0; i < nI; ++i) kap[i] = st[i].kappa;
+    IDP_CUDA_TRY(cudaMemcpyAsync(A.kappa, kap.data(), sizeof(double) * nI, cudaMemcpyHostToDevice, s));
+    std::vector<int> nDBC(nI, 0), nvert(nI);
+    for (int i = 0; i < nI; ++i) {
+        for (unsigned char d : c->inst[i].dbc) nDBC[i] += d;
+        nvert[i] = c->inst[i].V;
+    }
+    // initial constraint set and energy (IMPLICIT_EULER.h:418-434)
+    if ((rc = build_constraint_set(A, W, A.X, c->cs, s))) return rc;
+    std::vector<double> E;
+    std::vector<int> bad;
+    if ((rc = eval_energy(c, A.X, true, E, bad))) return rc;
+    for (int i = 0; i < nI; ++i) {
+        st[i].Eprev = E[i];
+        if (bad[i] == 1) { st[i].status = IDP_ERR_INVERTED; st[i].active = false; }
+        if (bad[i] == 2) { st[i].status = IDP_ERR_NONPOSITIVE_DIST; st[i].active = false; }
+    }
+    c->prevC = 0;
+    bool have_prev = false;
+    std::vector<double> hv;
+    std::vector<int> hi;
+    while (true) {
+        bool any = false;
+        for (int i = 0; i < nI; ++i) {
+            mask[i] = st[i].active ? 1 : 0;
+            any |= st[i].active;
+        }
+        if (!any) break;
+        if ((rc = set_mask(c, mask))) return rc;
+        // ---- gradient, Hessian, direction
+        if ((rc = eval_gradient(c, A.X))) return rc;
+        if ((rc = vec_neg(3 * A.V, A.g, A.g, s))) return rc;  // rhs = -g
+        std::vector<unsigned char> newton(nI, 0), gd(nI, 0);
+        bool any_newton = false, any_gd = false;
+        for (int i = 0; i < nI; ++i) {
+            if (!mask[i]) continue;
+            if (st[i].use_gd) { gd[i] = 1; any_gd = true; }
+            else { newton[i] = 1; any_newton = true; }
+        }
+        if (any_newton) {
+            if ((rc = set_mask(c, newton))) return rc;
+            if ((rc = eval_hessian(c, A.X))) return rc;
+            std::vector<int> its;
+            std::vector<double> rel;
+            if ((rc = pcg_solve(A, W, c->cs, fp64, A.g, A.dir, c->P.pcg_rel_tol, c->P.pcg_max_iters, its, rel, s)))
+                return rc;
+            for (int i = 0; i < nI; ++i)
+                if (newton[i]) st[i].pcg_iters += its[i];
+        }
+        if (any_gd) {  // gradient descent direction (IMPLICIT_EULER.h:507-510)
+            if ((rc = set_mask(c, gd))) return rc;
+            if ((rc = vec_copy_masked(A, A.active, A.g, A.dir, s))) return rc;
+        }
+        if ((rc = set_mask(c, mask))) return rc;
+        // ---- Line_Search (IMPLICIT_EULER.h:9-149)
+        IDP_CUDA_TRY(cudaMemcpyAsync(A.Xprev, A.X, sizeof(double) * 3 * A.V, cudaMemcpyDeviceToDevice, s));
+        std::vector<double> alpha(nI, 1.0);
+        // inversion-feasible alpha (halve while any det F <= 0)
+        std::vector<unsigned char> srch = mask;
+        for (int trial = 0; trial < 80; ++trial) {
+            bool anys = false;
+            for (int i = 0; i < nI; ++i) anys |= srch[i] != 0;
+            if (!anys) break;
+            if ((rc = set_mask(c, srch))) return rc;
+            IDP_CUDA_TRY(cudaMemcpyAsync(A.alpha, alpha.data(), sizeof(double) * nI, cudaMemcpyHostToDevice, s));
+            if ((rc = vec_axpy_trial(A, A.Xprev, A.dir, A.X, s))) return rc;
+            IDP_CUDA_TRY(cudaMemsetAsync(isc(c, SI_BAD), 0, sizeof(int) * nI, s));
+            if ((rc = tet_energy(A, W, A.X, h * h, dsc(c, S_ETET), isc(c, SI_BAD), s))) return rc;
+            if ((rc = fetch(c, isc(c, SI_BAD), hi))) return rc;
+            for (int i = 0; i < nI; ++i) {
+                if (!srch[i]) continue;
+                if (hi[i]) alpha[i] /= 2.0;
+                else srch[i] = 0;
+            }
+        }
+        // CCD filter (IMPLICIT_EULER.h:96-100)
+        if ((rc = set_mask(c, mask))) return rc;
+        IDP_CUDA_TRY(cudaMemcpyAsync(A.alpha, alpha.data(), sizeof(double) * nI, cudaMemcpyHostToDevice, s));
+        if ((rc = ccd_stepsize(A, W, A.Xprev, A.dir, A.alpha, isc(c, SI_CCDF), s))) return rc;
+        if ((rc = fetch(c, A.alpha, alpha))) return rc;
+        if ((rc = fetch(c, isc(c, SI_CCDF), hi))) return rc;
+        std::vector<double> feasible = alpha;
+        for (int i = 0; i < nI; ++i) {
+            if (!mask[i]) continue;
+            if (hi[i] & 2) st[i].status = IDP_ERR_ZERO_STEP;
+            if ((hi[i] & 1) && st[i].status == IDP_OK) st[i].status = IDP_WARN_ITER_CAP;
+        }
+        // backtracking until E <= Eprev
+        srch = mask;
+        std::vector<double> Eacc(nI, 0.0);
+        for (int trial = 0; trial < 200; ++trial) {
+            bool anys = false;
+            for (int i = 0; i < nI; ++i) anys |= srch[i] != 0;
+            if (!anys) break;
+            if ((rc = set_mask(c, srch))) return rc;
+            IDP_CUDA_TRY(cudaMemcpyAsync(A.alpha, alpha.data(), sizeof(double) * nI, cudaMemcpyHostToDevice, s));
+            if ((rc = vec_axpy_trial(A, A.Xprev, A.dir, A.X, s))) return rc;
+            // validity (det F > 0) on the searching instances
+            IDP_CUDA_TRY(cudaMemsetAsync(isc(c, SI_BAD), 0, sizeof(int) * nI, s));
+            if ((rc = tet_energy(A, W, A.X, h * h, dsc(c, S_ETET), isc(c, SI_BAD), s))) return rc;
+            if ((rc = fetch(c, isc(c, SI_BAD), hi))) return rc;
+            std::vector<unsigned char> valid(nI, 0);
+            for (int i = 0; i < nI; ++i) valid[i] = srch[i] && !hi[i];
+            for (int i = 0; i < nI; ++i) st[i].ls_trials += srch[i];
+            // constraint set + min-distance safeguard on the valid ones
+            if ((rc = set_mask(c, valid))) return rc;
+            if ((rc = build_constraint_set(A, W, A.X, c->cs, s))) return rc;
+            std::vector<double> md(nI, 1e300);
+            IDP_CUDA_TRY(cudaMemcpyAsync(dsc(c, S_MIND), md.data(), sizeof(double) * nI, cudaMemcpyHostToDevice, s));
+            if ((rc = constraint_min_dist2(A, W, A.X, W[W_CONS].as<int4>(), W[W_CONS_INST].as<int>(), c->cs.C, nullptr,
+                                           dsc(c, S_MIND), s)))
+                return rc;
+            if ((rc = fetch(c, dsc(c, S_MIND), md))) return rc;
+            std::vector<unsigned char> evalm(nI, 0);
+            for (int i = 0; i < nI; ++i) {
+                if (!valid[i]) continue;
+                double t2 = c->P.thickness * c->P.thickness;
+                if (c->cs.off[i + 1] > c->cs.off[i] && md[i] - t2 <= 0) {
+                    alpha[i] /= 2;  // safe guard backtrack (IMPLICIT_EULER.h:120-129)
+                    continue;
+                }
+                evalm[i] = 1;
+            }
+            if ((rc = set_mask(c, evalm))) return rc;
+            if ((rc = eval_energy(c, A.X, true, E, bad))) return rc;
+            for (int i = 0; i < nI; ++i) {
+                if (!srch[i]) continue;
+                if (!valid[i]) { alpha[i] /= 2.0; continue; }
+                if (!evalm[i]) continue;
+                bool ok = bad[i] == 0 && !(E[i] > st[i].Eprev);
+                alpha[i] /= 2.0;
+                if (ok) {
+                    srch[i] = 0;
+                    Eacc[i] = E[i];
+                }
+            }
+        }
+        for (int i = 0; i < nI; ++i)
+            if (srch[i]) st[i].status = IDP_ERR_ZERO_STEP;  // line search exhausted
+        // X holds every instance's accepted trial; rebuild their constraint set
+        if ((rc = set_mask(c, mask))) return rc;
+        if ((rc = build_constraint_set(A, W, A.X, c->cs, s))) return rc;
+        for (int i = 0; i < nI; ++i)
+            if (mask[i]) {
+                st[i].Eprev = Eacc[i];
+                st[i].alpha = alpha[i] * 2;
+                st[i].min_alpha = std::min(st[i].min_alpha, alpha[i] * 2);
+                st[i].feasible_alpha = feasible[i];
+            }
+        // ---- kappa adaptation (IMPLICIT_EULER.h:566-595)
+        if (have_prev && c->prevC > 0) {
+            IDP_CUDA_TRY(cudaMemsetAsync(isc(c, SI_KFLAG), 0, sizeof(int) * nI, s));
+            if ((rc = kappa_check(A, W, A.X, W[W_PREV_CONS].as<int4>(), W[W_PREV_INST].as<int>(),
+                                  W[W_PREV_DIST2].as<double>(), c->prevC, isc(c, SI_KFLAG), s)))
+                return rc;
+            if ((rc = fetch(c, isc(c, SI_KFLAG), hi))) return rc;
+            std::vector<unsigned char> km(nI, 0);
+            bool anyk = false;
+            for (int i = 0; i < nI; ++i)
+                if (mask[i] && hi[i] && st[i].kappa < st[i].kappa_max) {
+                    st[i].kappa *= 2;
+                    km[i] = 1;
+                    anyk = true;
+                }
+            if (anyk) {
+                for (int i = 0; i < nI; ++i) kap[i] = st[i].kappa;
+                IDP_CUDA_TRY(cudaMemcpyAsync(A.kappa, kap.data(), sizeof(double) * nI, cudaMemcpyHostToDevice, s));
+                if ((rc = set_mask(c, km))) return rc;
+                if ((rc = eval_energy(c, A.X, true, E, bad))) return rc;
+                for (int i = 0; i < nI; ++i)
+                    if (km[i]) st[i].Eprev = E[i];
+                if ((rc = set_mask(c, mask))) return rc;
+            }
+        }
+        if ((rc = save_prev_set(c, A.X))) return rc;
+        have_prev = true;
+        // ---- stopping criterion (IMPLICIT_EULER.h:647-676, 759, 855)
+        if ((rc = vec_dir_norm2(A, W, A.dir, dsc(c, S_NORM2), s))) return rc;
+        if ((rc = fetch(c, dsc(c, S_NORM2), hv))) return rc;
+        for (int i = 0; i < nI; ++i) {
+            if (!mask[i]) continue;
+            InstState& S = st[i];
+            double L2 = std::sqrt(hv[i] / (nvert[i] - nDBC[i])) / h;
+            S.iters += 1;
+            S.last_res = L2;
+            if (S.nres < 3) S.res[S.nres++] = L2;
+            else { S.res[0] = S.res[1]; S.res[1] = S.res[2]; S.res[2] = L2; }
+            double L2m = *std::max_element(S.res, S.res + S.nres);
+            if (S.use_gd) L2m = c->P.newton_tol * 10;
+            // switch to gradient descent after a vanishing step (IMPLICIT_EULER.h:682-699)
+            S.use_gd = (S.alpha < 1e-8 && S.feasible_alpha > 1e-8);
+            if (S.status == IDP_ERR_ZERO_STEP || S.status == IDP_ERR_NONPOSITIVE_DIST) S.active = false;
+            else if (S.nres == 3 && L2m <= c->P.newton_tol) S.active = false;
+            else if (S.iters >= c->P.max_newton) {
+                S.active = false;
+                S.status = IDP_ERR_NOT_CONVERGED;
+            }
+        }
+    }
+    // v = (x - x^n) / h (IMPLICIT_EULER.h:882-888)
+    if ((rc = set_mask(c, all))) return rc;
+    if ((rc = vec_velocity(A, A.X, A.Xn, h, c->vel.as<double>(), s))) return rc;
+    IDP_CUDA_TRY(cudaStreamSynchronize(s));
+    int worst = IDP_OK;
+    for (int i = 0; i < nI; ++i) {
+        if (results) {
+            idp_result& r = results[i];
+            r.status = st[i].status;
+            r.newton_iters = st[i].iters;
+            r.pcg_iters = st[i].pcg_iters;
+            r.ls_trials = st[i].ls_trials;
+            r.num_constraints = c->cs.off.size() > (size_t)i + 1 ? c->cs.off[i + 1] - c->cs.off[i] : 0;
+            r.energy = st[i].Eprev;
+            r.kappa = st[i].kappa;
+            r.residual = st[i].last_res;
+            r.min_alpha = st[i].min_alpha;
+        }
+        if (st[i].status != IDP_OK && st[i].status != IDP_WARN_ITER_CAP && worst == IDP_OK) worst = st[i].status;
+    }
+    return worst;
+}
+
+int idp_get_state(idp_ctx* c, int i, double* X, double* v, double* kappa3) {
+    if (!c || i < 0 || i >= (int)c->inst.size()) return IDP_ERR_INVALID_ARG;
+    if (!c->committed) {
+        const HostInstance& h = c->inst[i];
+        if (X) std::memcpy(X, h.X.data(), sizeof(double) * 3 * h.V);
+        if (v) std::memcpy(v, h.v.data(), sizeof(double) * 3 * h.V);
+        if (kappa3) { kappa3[0] = h.kappa; kappa3[1] = h.kappa_max; kappa3[2] = 0; }
+        return IDP_OK;
+    }
+    long o = 3L * c->A.v_off[i], n = 3L * c->inst[i].V;
+    if (X) IDP_CUDA_TRY(cudaMemcpyAsync(X, c->A.X + o, sizeof(double) * n, cudaMemcpyDeviceToHost, c->s));
+    if (v) IDP_CUDA_TRY(cudaMemcpyAsync(v, c->vel.as<double>() + o, sizeof(double) * n, cudaMemcpyDeviceToHost, c->s));
+    IDP_CUDA_TRY(cudaStreamSynchronize(c->s));
+    if (kappa3) {
+        kappa3[0] = c->st[i].kappa;
+        kappa3[1] = c->st[i].kappa_max;
+        kappa3[2] = 0;
+    }
+    return IDP_OK;
+}
+
+int idp_instance_info(idp_ctx* c, int i, int* V, int* T, int* nn, int* ne, int* nt) {
+    if (!c) return IDP_ERR_INVALID_ARG;
+    if (i < 0) {
+        if (V) *V = (int)c->inst.size();
+        return IDP_OK;
+    }
+    if (i >= (int)c->inst.size()) return IDP_ERR_INVALID_ARG;
+    const HostInstance& h = c->inst[i];
+    if (V) *V = h.V;
+    if (T) *T = h.T;
+    if (nn) *nn = (int)h.nodes.size();
+    if (ne) *ne = (int)h.edges.size() / 2;
+    if (nt) *nt = (int)h.tris.size() / 3;
+    return IDP_OK;
+}
+
+int idp_get_surface(idp_ctx* c, int i, int32_t* nodes, int32_t* edges, int32_t* tris) {
+    if (!c || i < 0 || i >= (int)c->inst.size()) return IDP_ERR_INVALID_ARG;
+    const HostInstance& h = c->inst[i];
+    if (nodes) std::copy(h.nodes.begin(), h.nodes.end(), nodes);
+    if (edges) std::copy(h.edges.begin(), h.edges.end(), edges);
+    if (tris) std::copy(h.tris.begin(), h.tris.end(), tris);
+    return IDP_OK;
+}
+
+// ---- sub-steps on one instance at caller positions (scratch: A.Xprev)
+static int prep_one(idp_ctx* c, int i, const double* X) {
+    if (!c || !c->committed) return IDP_ERR_STATE;
+    if (i < 0 || i >= c->A.nI || !X) return IDP_ERR_INVALID_ARG;
+    cudaSetDevice(c->P.device);
+    std::vector<unsigned char> m(c->A.nI, 0);
+    m[i] = 1;
+    int rc = set_mask(c, m);
+    if (rc) return rc;
+    long o = 3L * c->A.v_off[i];
+    IDP_CUDA_TRY(cudaMemcpyAsync(c->A.Xprev + o, X, sizeof(double) * 3 * c->inst[i].V, cudaMemcpyHostToDevice, c->s));
+    // x_tilde from the instance's current positions and velocity
+    rc = vec_xtilde(c->A, c->A.X, c->vel.as<double>(), c->P.h, c->A.Xtilde, c->s);
+    if (rc) return rc;
+    std::vector<double> kap(c->A.nI);
+    for (int k = 0; k < c->A.nI; ++k) kap[k] = c->st[k].kappa;
+    IDP_CUDA_TRY(cudaMemcpyAsync(c->A.kappa, kap.data(), sizeof(double) * c->A.nI, cudaMemcpyHostToDevice, c->s));
+    return IDP_OK;
+}
+
+int idp_eval_energy(idp_ctx* c, int i, const double* X, double* Ee, double* Ei, double* Eb) {
+    int rc = prep_one(c, i, X);
+    if (rc) return rc;
+    if ((rc = build_constraint_set(c->A, c->W, c->A.Xprev, c->cs, c->s))) return rc;
+    std::vector<double> E;
+    std::vector<int> bad;
+    if ((rc = eval_energy(c, c->A.Xprev, true, E, bad))) return rc;
+    std::vector<double> et, ei, eb;
+    fetch(c, dsc(c, S_ETET), et);
+    fetch(c, dsc(c, S_EINERT), ei);
+    fetch(c, dsc(c, S_EBAR), eb);
+    if (Ee) *Ee = et[i];
+    if (Ei) *Ei = ei[i];
+    if (Eb) *Eb = eb[i];
+    if (bad[i] == 1) return IDP_ERR_INVERTED;
+    if (bad[i] == 2) return IDP_ERR_NONPOSITIVE_DIST;
+    return IDP_OK;
+}
+
+int idp_eval_gradient(idp_ctx* c, int i, const double* X, double* g) {
+    int rc = prep_one(c, i, X);
+    if (rc) return rc;
+    if ((rc = build_constraint_set(c->A, c->W, c->A.Xprev, c->cs, c->s))) return rc;
+    if ((rc = eval_gradient(c, c->A.Xprev))) return rc;
+    long o = 3L * c->A.v_off[i];
+    IDP_CUDA_TRY(cudaMemcpyAsync(g, c->A.g + o, sizeof(double) * 3 * c->inst[i].V, cudaMemcpyDeviceToHost, c->s));
+    IDP_CUDA_TRY(cudaStreamSynchronize(c->s));
+    return IDP_OK;
+}
+
+int idp_constraint_set(idp_ctx* c, int i, const double* X, int cap, int32_t* cons, int* count) {
+    int rc = prep_one(c, i, X);
+    if (rc) return rc;
+    if ((rc = build_constraint_set(c->A, c->W, c->A.Xprev, c->cs, c->s))) return rc;
+    int n = c->cs.off[i + 1] - c->cs.off[i];
+    if (count) *count = n;
+    if (n > cap) return IDP_ERR_CAPACITY;
+    if (n > 0 && cons) {
+        IDP_CUDA_TRY(cudaMemcpyAsync(cons, c->W[W_CONS].as<int4>() + c->cs.off[i], sizeof(int4) * n,
+                                     cudaMemcpyDeviceToHost, c->s));
+        IDP_CUDA_TRY(cudaStreamSynchronize(c->s));
+        // device ids are arena-global; return instance-local ids, keeping the
+        // sign tags (-v-1), the -1 markers and the -count multiplicity slot
+        int vo = c->A.v_off[i];
+        auto pos = [vo](int v) { return v - vo; };
+        auto tag = [vo](int v) { return -((-v - 1) - vo) - 1; };
+        for (int k = 0; k < n; ++k) {
+            int* q = cons + 4 * k;
+            if (q[0] >= 0) {  // edge-edge family: every negative entry is a tagged vertex
+                for (int j = 0; j < 4; ++j) q[j] = q[j] >= 0 ? pos(q[j]) : tag(q[j]);
+            } else {
+                q[0] = tag(q[0]);
+                q[1] = pos(q[1]);
+                if (q[3] >= 0) { q[2] = pos(q[2]); q[3] = pos(q[3]); }
+                else if (q[2] >= 0) q[2] = pos(q[2]);
+            }
+        }
+    }
+    return IDP_OK;
+}
+
+int idp_ccd_stepsize(idp_ctx* c, int i, const double* X, const double* dir, double* alpha) {
+    int rc = prep_one(c, i, X);
+    if (rc) return rc;
+    if (!dir || !alpha) return IDP_ERR_INVALID_ARG;
+    long o = 3L * c->A.v_off[i];
+    IDP_CUDA_TRY(cudaMemcpyAsync(c->A.dir + o, dir, sizeof(double) * 3 * c->inst[i].V, cudaMemcpyHostToDevice, c->s));
+    std::vector<double> a(c->A.nI, *alpha);
+    IDP_CUDA_TRY(cudaMemcpyAsync(c->A.alpha, a.data(), sizeof(double) * c->A.nI, cudaMemcpyHostToDevice, c->s));
+    if ((rc = ccd_stepsize(c->A, c->W, c->A.Xprev, c->A.dir, c->A.alpha, isc(c, SI_CCDF), c->s))) return rc;
+    std::vector<int> fl;
+    fetch(c, c->A.alpha, a);
+    fetch(c, isc(c, SI_CCDF), fl);
+    *alpha = a[i];
+    if (fl[i] & 2) return IDP_ERR_ZERO_STEP;
+    if (fl[i] & 1) return IDP_WARN_ITER_CAP;
+    return IDP_OK;
+}
+
+int idp_hessian_apply(idp_ctx* c, int i, const double* X, const double* x, double* y) {
+    int rc = prep_one(c, i, X);
+    if (rc) return rc;
+    if ((rc = build_constraint_set(c->A, c->W, c->A.Xprev, c->cs, c->s))) return rc;
+    if ((rc = eval_hessian(c, c->A.Xprev))) return rc;
+    long o = 3L * c->A.v_off[i], n = 3L * c->inst[i].V;
+    IDP_CUDA_TRY(cudaMemsetAsync(c->A.dir, 0, sizeof(double) * 3 * c->A.V, c->s));
+    IDP_CUDA_TRY(cudaMemcpyAsync(c->A.dir + o, x, sizeof(double) * n, cudaMemcpyHostToDevice, c->s));
+    if ((rc = hessian_apply(c->A, c->W, c->P.mode == IDP_MODE_FP64, c->A.dir, c->A.g, c->s))) return rc;
+    IDP_CUDA_TRY(cudaMemcpyAsync(y, c->A.g + o, sizeof(double) * n, cudaMemcpyDeviceToHost, c->s));
+    IDP_CUDA_TRY(cudaStreamSynchronize(c->s));
+    return IDP_OK;
+}
+
+int idp_newton_direction(idp_ctx* c, int i, const double* X, double* p, int* iters, double* relres) {
+    int rc = prep_one(c, i, X);
+    if (rc) return rc;
+    if ((rc = build_constraint_set(c->A, c->W, c->A.Xprev, c->cs, c->s))) return rc;
+    if ((rc = eval_gradient(c, c->A.Xprev))) return rc;
+    if ((rc = vec_neg(3 * c->A.V, c->A.g, c->A.g, c->s))) return rc;
+    if ((rc = eval_hessian(c, c->A.Xprev))) return rc;
+    std::vector<int> its;
+    std::vector<double> rel;
+    if ((rc = pcg_solve(c->A, c->W, c->cs, c->P.mode == IDP_MODE_FP64, c->A.g, c->A.dir, c->P.pcg_rel_tol,
+                        c->P.pcg_max_iters, its, rel, c->s)))
+        return rc;
+    long o = 3L * c->A.v_off[i];
+    IDP_CUDA_TRY(cudaMemcpyAsync(p, c->A.dir + o, sizeof(double) * 3 * c->inst[i].V, cudaMemcpyDeviceToHost, c->s));
+    IDP_CUDA_TRY(cudaStreamSynchronize(c->s));
+    if (iters) *iters = its[i];
+    if (relres) *relres = rel[i];
+    return IDP_OK;
+}
+
+}  // extern "C"

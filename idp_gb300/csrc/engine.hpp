@@ -1,0 +1,170 @@
+// Device arena and per-module launchers of the GB300 injective-deformation
+// engine. One arena holds every instance (mesh) of a context: vertices, tets
+// and surface primitives of all instances are concatenated with per-instance
+// offsets, so one launch serves the whole batch.
+#pragma once
+#include <vector>
+#include <string>
+#include "common.cuh"
+#include "../../include/idp_gb300.h"
+
+namespace idp {
+
+// growable device buffer (grown only between solves, never under capture)
+struct DBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    int ensure(size_t n);
+    void release();
+    template <class T>
+    T* as() const { return reinterpret_cast<T*>(p); }
+};
+
+// per-instance host description, filled by idp_add_instance
+struct HostInstance {
+    int V = 0, T = 0;
+    std::vector<double> X, X0, mass, lam, mu, v, xtilde;
+    std::vector<int> tets;      // 4T, local ids
+    std::vector<unsigned char> dbc;
+    std::vector<double> dbc_pos;  // 3V (only entries with dbc set are read)
+    bool has_xtilde = false;
+    double dHat2 = 0, kappa = 0, kappa_max = 0;
+    // surface in reference order (local ids)
+    std::vector<int> tris, edges, nodes;
+    double rest_mean_edge = 0;
+};
+
+// per-instance Newton state kept on the host
+struct InstState {
+    bool active = false;       // still iterating
+    bool searching = false;    // inside line search, trial not accepted yet
+    bool use_gd = false;
+    double Eprev = 0, alpha = 1, feasible_alpha = 1;
+    double res[3] = {0, 0, 0};
+    int nres = 0;
+    int iters = 0, pcg_iters = 0, ls_trials = 0, status = 0;
+    double last_res = 0;
+    double kappa = 0, kappa_max = 0;
+    double min_alpha = 1;
+};
+
+struct Arena {
+    int nI = 0;
+    long V = 0, T = 0, Sn = 0, Se = 0, St = 0;
+    std::vector<int> v_off, t_off, sn_off, se_off, st_off;  // host, size nI+1
+
+    // ---- device, per vertex (3V doubles unless noted)
+    double *X = nullptr, *X0 = nullptr, *Xn = nullptr, *Xtilde = nullptr, *Xprev = nullptr, *mass = nullptr;
+    double *g = nullptr, *dir = nullptr;          // gradient, Newton direction (3V)
+    unsigned char* dbc = nullptr;                 // V
+    int* vinst = nullptr;                         // V
+    // ---- per tet
+    int4* tet = nullptr;
+    double *IB = nullptr, *vol = nullptr, *lam = nullptr, *mu = nullptr;
+    // ---- surface primitives (global vertex ids)
+    int* snode = nullptr;
+    int2* sedge = nullptr;
+    int* stri = nullptr;                          // 3 St
+    int *sn_inst = nullptr, *se_inst = nullptr, *st_inst = nullptr;
+    // ---- per instance
+    double *dHat2 = nullptr, *kappa = nullptr, *thickness = nullptr, *cell = nullptr;
+    unsigned char* active = nullptr;              // nI: instance participates in this launch
+    double* alpha = nullptr;                      // nI: current step per instance
+    int* d_v_off = nullptr;
+    // ---- chunk tables
+    Chunk* tet_chunks = nullptr;
+    int n_tet_chunks = 0;
+    Chunk* vert_chunks = nullptr;
+    int n_vert_chunks = 0;
+    Chunk* node_chunks = nullptr;
+    int n_node_chunks = 0;
+    Chunk* edge_chunks = nullptr;
+    int n_edge_chunks = 0;
+    // ---- BSR pattern of the tet stencil (3x3 blocks)
+    long B = 0;
+    int *rowptr = nullptr, *colidx = nullptr, *diagblk = nullptr;
+    int *src_ptr = nullptr, *src = nullptr;       // per BSR block: contributing (tet*10+k)*2+transposed
+    int* vert_corner_ptr = nullptr;               // per vertex: list of tet*4+corner
+    int* vert_corner = nullptr;
+    int* brow = nullptr;                          // row (vertex) of every BSR block
+    int *tet_chunk_off = nullptr, *vert_chunk_off = nullptr;  // nI+1 chunk ranges
+    int* v2s = nullptr;                           // vertex -> surface node (or -1)
+};
+
+// all scratch/work buffers reused across calls, indexed by slot
+enum WorkSlot {
+    W_SCRATCH, W_SCRATCH2, W_TET_GRAD, W_TET_HESS, W_CHUNK_SUM, W_INST_SUM, W_FLAGS,
+    // grids (two slots: 0 and 1), 6 buffers each
+    W_GRID0, W_GRID0_END = W_GRID0 + 6, W_GRID1 = W_GRID0_END, W_GRID1_END = W_GRID1 + 6,
+    W_BOX_A, W_BOX_B, W_GRIDP, W_BBOX,
+    W_CAND, W_CAND_CNT,
+    W_CONS, W_CONS_INST, W_CONS_KEY_HI, W_CONS_KEY_LO, W_CONS_PERM, W_CONS_PERM2, W_CONS_TMP, W_CONS_TMP_INST,
+    W_CONS_HEAD, W_CONS_OFF, W_CONS_CNT, W_DIST2,
+    W_PREV_CONS, W_PREV_INST, W_PREV_DIST2,
+    W_BH, W_BG, W_GENT_KEY, W_GENT_VAL, W_GENT_KEY2, W_GENT_VAL2, W_GENT_HEAD,
+    W_TAIL_ROWPTR, W_TAIL_COL, W_TAIL_VAL, W_TAIL_KEYS,
+    W_BSR_VAL, W_DIAG_INV, W_PCG_VEC, W_PCG_SCAL, W_PCG_VEC64, W_CCD_TMP, W_CCD_ALPHA, W_MISC, W_MISC2,
+    W_NUM
+};
+struct Work {
+    DBuf b[W_NUM];
+    DBuf& operator[](int i) { return b[i]; }
+    void release() { for (auto& x : b) x.release(); }
+};
+
+struct Params {
+    idp_params p;
+};
+
+// ---------------------------------------------------------------- launchers
+// tet.cu
+int tet_energy(Arena& A, Work& W, const double* X, double w_h2, double* inst_E, int* inst_bad, cudaStream_t s);
+int tet_detcheck(Arena& A, Work& W, const double* X, int* inst_bad, cudaStream_t s);
+int tet_gradient(Arena& A, Work& W, const double* X, double w_h2, double* g, cudaStream_t s);
+int tet_hessian(Arena& A, Work& W, const double* X, double w_h2, bool fp64, cudaStream_t s);
+
+// contact.cu
+struct ContactSet {
+    long C = 0;                        // total constraints
+    std::vector<int> off;              // host per-instance offsets (nI+1)
+    int* d_off = nullptr;              // device offsets
+};
+int build_constraint_set(Arena& A, Work& W, const double* X, ContactSet& cs, cudaStream_t s);
+int constraint_min_dist2(Arena& A, Work& W, const double* X, const int4* cons, const int* cinst, long C,
+                         double* dist2, double* inst_min, cudaStream_t s);
+
+// barrier.cu
+int barrier_energy(Arena& A, Work& W, const double* X, const ContactSet& cs, double* inst_E, int* inst_bad,
+                   cudaStream_t s);
+int barrier_gradient(Arena& A, Work& W, const double* X, const ContactSet& cs, double* g, cudaStream_t s);
+int barrier_hessian(Arena& A, Work& W, const double* X, const ContactSet& cs, bool fp64, cudaStream_t s);
+
+// ccd.cu
+int ccd_stepsize(Arena& A, Work& W, const double* X, const double* dir, double* alpha /*device nI*/, int* flags,
+                 cudaStream_t s);
+
+// solver.cu
+int assemble(Arena& A, Work& W, const ContactSet& cs, bool fp64, cudaStream_t s);
+int pcg_solve(Arena& A, Work& W, const ContactSet& cs, bool fp64, const double* rhs, double* sol,
+              double rel_tol, int max_iters, std::vector<int>& iters_out, std::vector<double>& relres_out,
+              cudaStream_t s);
+
+// vector helpers (solver.cu)
+int vec_inertia(Arena& A, Work& W, const double* X, double* inst_E, double* g /*nullable*/, cudaStream_t s);
+int vec_axpy_trial(Arena& A, const double* Xprev, const double* dir, double* Xout, cudaStream_t s);
+int vec_zero_dbc(Arena& A, double* g, cudaStream_t s);
+int chunk_reduce(Arena& A, Work& W, const Chunk* chunks, int nchunks, const double* chunk_vals, double* inst_out,
+                 cudaStream_t s);
+int chunk_reduce_off(Arena& A, const int* coff, const double* part, double* out, bool accumulate, cudaStream_t s);
+int grad_gather_tet(Arena& A, Work& W, const double* X, double* g, cudaStream_t s);
+int hessian_apply(Arena& A, Work& W, bool fp64, const double* x, double* y, cudaStream_t s);
+// vecops.cu
+int vec_neg(long n, const double* a, double* out, cudaStream_t s);
+int vec_copy_masked(Arena& A, const unsigned char* mask, const double* src, double* dst, cudaStream_t s);
+int vec_dir_norm2(Arena& A, Work& W, const double* dir, double* inst_out, cudaStream_t s);
+int vec_velocity(Arena& A, const double* X, const double* Xn, double h, double* v, cudaStream_t s);
+int vec_xtilde(Arena& A, const double* X, const double* v, double h, double* Xt, cudaStream_t s);
+int kappa_check(Arena& A, Work& W, const double* X, const int4* cons, const int* cinst, const double* d2prev, long C,
+                int* inst_flag, cudaStream_t s);
+
+}  // namespace idp

@@ -1,0 +1,133 @@
+// Uniform-grid broad phase shared by the constraint-set builder and the CCD:
+// every primitive is binned into the cells its integer box covers, the
+// (instance, cell) keys are radix-sorted, and queries walk the cells of their
+// own box with a cursor, binary-searching each cell in the sorted table.
+// Candidate pairs are compacted warp-cooperatively (ballot + popc) into a
+// global list.
+#pragma once
+#include "common.cuh"
+
+namespace idp {
+
+struct GridP {
+    double lo[3];
+    double inv;
+    int n[3];      // cells per axis (indices clamped to [0, n])
+    long s1, s2;   // linear strides: cell = x + y*s1 + z*s2
+};
+
+struct BoxI {
+    int lo[3], hi[3];
+};
+
+// order-preserving map of doubles to u64 (for exact atomic min/max)
+__device__ __forceinline__ unsigned long long ord_enc(double x) {
+    unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double ord_dec(unsigned long long u) {
+    unsigned long long b = (u >> 63) ? (u & 0x7fffffffffffffffull) : ~u;
+    return __longlong_as_double((long long)b);
+}
+
+__device__ __forceinline__ int clampi(int v, int a, int b) { return v < a ? a : (v > b ? b : v); }
+
+__device__ __forceinline__ int vox(double x, double lo, double inv) { return (int)floor((x - lo) * inv); }
+
+__device__ __forceinline__ uint64_t cell_key(int inst, const GridP& g, int x, int y, int z) {
+    return ((uint64_t)inst << 32) | (uint64_t)((long)x + (long)y * g.s1 + (long)z * g.s2);
+}
+
+__device__ __forceinline__ int lower_bound_u64(const uint64_t* __restrict__ a, int n, uint64_t key) {
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (a[mid] < key) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// cursor over the cells of one query box
+struct Cursor {
+    int lo[3], hi[3], c[3], fc[3];
+    uint32_t e, eend;
+    bool done;
+};
+
+__device__ __forceinline__ void cursor_init(Cursor& q, const BoxI& b) {
+    for (int d = 0; d < 3; ++d) { q.lo[d] = b.lo[d]; q.hi[d] = b.hi[d]; q.c[d] = b.lo[d]; q.fc[d] = 0; }
+    q.e = q.eend = 0;
+    q.done = (b.lo[0] > b.hi[0]) || (b.lo[1] > b.hi[1]) || (b.lo[2] > b.hi[2]);
+}
+
+// next entry index of the sorted entry list, or false when exhausted
+__device__ __forceinline__ bool cursor_next(Cursor& q, int inst, const GridP& g, const uint64_t* __restrict__ ckey,
+                                            const uint32_t* __restrict__ cstart, int ncell, uint32_t& entry) {
+    while (q.e >= q.eend) {
+        if (q.done) return false;
+        uint64_t key = cell_key(inst, g, q.c[0], q.c[1], q.c[2]);
+        int k = lower_bound_u64(ckey, ncell, key);
+        if (k < ncell && ckey[k] == key) {
+            q.e = cstart[k];
+            q.eend = cstart[k + 1];
+            q.fc[0] = q.c[0]; q.fc[1] = q.c[1]; q.fc[2] = q.c[2];
+        }
+        if (++q.c[0] > q.hi[0]) {
+            q.c[0] = q.lo[0];
+            if (++q.c[1] > q.hi[1]) {
+                q.c[1] = q.lo[1];
+                if (++q.c[2] > q.hi[2]) q.done = true;
+            }
+        }
+    }
+    entry = q.e++;
+    return true;
+}
+
+// the pair (query box, primitive box) is reported once: in the lowest corner
+// cell of the two boxes' intersection
+__device__ __forceinline__ bool first_shared_cell(const Cursor& q, const BoxI& b) {
+    for (int d = 0; d < 3; ++d) {
+        if (b.lo[d] > q.hi[d] || b.hi[d] < q.lo[d]) return false;
+        int c = q.lo[d] > b.lo[d] ? q.lo[d] : b.lo[d];
+        if (c != q.fc[d]) return false;
+    }
+    return true;
+}
+
+// warp-cooperative append: lanes with emit=true write v to out[] in a block
+// reserved by one atomicAdd per warp. Writes beyond cap are dropped (the
+// counter still counts them so the caller can grow and retry).
+template <class V>
+__device__ __forceinline__ void warp_emit(bool emit, const V& v, V* __restrict__ out, unsigned int* counter, long cap) {
+    unsigned int m = __ballot_sync(0xffffffffu, emit);
+    if (!m) return;
+    int lane = threadIdx.x & 31;
+    int leader = __ffs(m) - 1;
+    unsigned int base = 0;
+    if (lane == leader) base = atomicAdd(counter, (unsigned int)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (emit) {
+        unsigned int pos = base + __popc(m & ((1u << lane) - 1u));
+        if (pos < cap) out[pos] = v;
+    }
+}
+
+// ---- host-side builder (contact.cu): sorted (instance, cell) entry table
+struct BoxGrid {
+    uint64_t* cell_keys = nullptr;   // ncell sorted unique keys
+    uint32_t* cell_start = nullptr;  // ncell + 1
+    uint32_t* entries = nullptr;     // primitive ids, grouped by cell
+    int ncell = 0;
+    long nent = 0;
+};
+
+struct Work;
+// Bins nprim boxes (box[i], instance inst[i]; skipped when active[inst]==0)
+// into their cells. Buffers come from W; which selects one of two slots so a
+// point grid and an edge grid can coexist.
+int build_box_grid(Work& W, int slot, const BoxI* boxes, const int* inst, const unsigned char* active, long nprim,
+                   const GridP* gp, int nI, BoxGrid& out, cudaStream_t s);
+
+}  // namespace idp

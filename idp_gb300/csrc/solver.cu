@@ -1,0 +1,613 @@
+// Sparse system assembly and the linear solve that replaces the direct
+// factorisation of Math/DIRECT_SOLVER.h:13-65, plus the per-vertex vector
+// kernels of the Newton loop.
+//
+// Matrix: 3x3 BSR over the fixed tet stencil (pattern built once per
+// context) + a per-iteration contact tail (CSR of 3x3 blocks from the barrier
+// Hessians) + the lumped mass on the diagonal, with the DBC rows and columns
+// replaced by identity (Math/CSR_MATRIX.h:130-141). Each BSR block is the sum,
+// in a fixed order, of the element blocks listed for it, so assembly is
+// deterministic.
+//
+// Solve: block-Jacobi PCG per instance (every instance of the batch carries
+// its own scalars and stops on its own). Mixed mode runs PCG in FP32 and
+// recovers the direction by iterative refinement against an FP64 residual
+// r = b - A x (FP32 matrix, FP64 accumulation); FP64 mode runs PCG in FP64.
+#include "engine.hpp"
+#include "prims.cuh"
+
+namespace idp {
+
+namespace {
+
+template <class T>
+__device__ __forceinline__ T blk_get(const T* tet_hess, int code, int q) {
+    // code = (tet*10 + k)*2 + transposed
+    long base = (long)(code >> 1) * 9;
+    if (code & 1) return tet_hess[base + (q % 3) * 3 + q / 3];
+    return tet_hess[base + q];
+}
+
+template <class T>
+__global__ void k_assemble_tet(long B, const int* __restrict__ src_ptr, const int* __restrict__ src,
+                               const T* __restrict__ tet_hess, const int* __restrict__ brow,
+                               const int* __restrict__ colidx, const double* __restrict__ mass,
+                               const unsigned char* __restrict__ dbc, const int* __restrict__ vinst,
+                               const unsigned char* __restrict__ active, T* __restrict__ val) {
+    long b = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= B) return;
+    int row = brow[b], col = colidx[b];
+    if (!active[vinst[row]]) return;
+    T acc[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) acc[q] = T(0);
+    for (int k = src_ptr[b]; k < src_ptr[b + 1]; ++k) {
+        int code = src[k];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) acc[q] += blk_get(tet_hess, code, q);
+    }
+    if (row == col) {
+        T m = (T)mass[row];
+        acc[0] += m; acc[4] += m; acc[8] += m;
+    }
+    if (dbc[row] || dbc[col]) {
+#pragma unroll
+        for (int q = 0; q < 9; ++q) acc[q] = T(0);
+        if (row == col) { acc[0] = acc[4] = acc[8] = T(1); }
+    }
+    T* o = val + 9 * b;
+#pragma unroll
+    for (int q = 0; q < 9; ++q) o[q] = acc[q];
+}
+
+template <class T>
+__device__ __forceinline__ void inv3(const T a[9], T o[9]) {
+    T c00 = a[4] * a[8] - a[5] * a[7], c01 = a[5] * a[6] - a[3] * a[8], c02 = a[3] * a[7] - a[4] * a[6];
+    T det = a[0] * c00 + a[1] * c01 + a[2] * c02;
+    T id = T(1) / det;
+    o[0] = c00 * id;
+    o[1] = (a[2] * a[7] - a[1] * a[8]) * id;
+    o[2] = (a[1] * a[5] - a[2] * a[4]) * id;
+    o[3] = c01 * id;
+    o[4] = (a[0] * a[8] - a[2] * a[6]) * id;
+    o[5] = (a[2] * a[3] - a[0] * a[5]) * id;
+    o[6] = c02 * id;
+    o[7] = (a[1] * a[6] - a[0] * a[7]) * id;
+    o[8] = (a[0] * a[4] - a[1] * a[3]) * id;
+}
+
+// block-Jacobi: inverse of (tet diagonal block + tail diagonal block)
+template <class T>
+__global__ void k_diag_inv(long V, const int* __restrict__ diagblk, const T* __restrict__ val,
+                           const int* __restrict__ trp, const int* __restrict__ tcol, const T* __restrict__ tval,
+                           const unsigned char* __restrict__ dbc, const int* __restrict__ vinst,
+                           const unsigned char* __restrict__ active, T* __restrict__ dinv) {
+    long v = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= V || !active[vinst[v]]) return;
+    T a[9];
+    const T* d = val + 9 * (long)diagblk[v];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) a[q] = d[q];
+    if (!dbc[v])
+        for (int k = trp[v]; k < trp[v + 1]; ++k)
+            if (tcol[k] == v)
+#pragma unroll
+                for (int q = 0; q < 9; ++q) a[q] += tval[9 * (long)k + q];
+    T o[9];
+    inv3(a, o);
+#pragma unroll
+    for (int q = 0; q < 9; ++q) dinv[9 * v + q] = o[q];
+}
+
+// y = A x for the rows of instances with run[inst] != 0; optional partial
+// dot products p.y per vertex chunk
+template <class T, class TX, class TY>
+__device__ __forceinline__ void spmv_row(long v, const int* __restrict__ rowptr, const int* __restrict__ colidx,
+                                         const T* __restrict__ val, const int* __restrict__ trp,
+                                         const int* __restrict__ tcol, const T* __restrict__ tval,
+                                         const unsigned char* __restrict__ dbc, const TX* __restrict__ x, TY y[3]) {
+    if (dbc[v]) {
+        y[0] = (TY)x[3 * v]; y[1] = (TY)x[3 * v + 1]; y[2] = (TY)x[3 * v + 2];
+        return;
+    }
+    TY a0 = 0, a1 = 0, a2 = 0;
+    for (int k = rowptr[v]; k < rowptr[v + 1]; ++k) {
+        int c = colidx[k];
+        const T* m = val + 9 * (long)k;
+        TY x0 = (TY)x[3 * c], x1 = (TY)x[3 * c + 1], x2 = (TY)x[3 * c + 2];
+        a0 += (TY)m[0] * x0 + (TY)m[1] * x1 + (TY)m[2] * x2;
+        a1 += (TY)m[3] * x0 + (TY)m[4] * x1 + (TY)m[5] * x2;
+        a2 += (TY)m[6] * x0 + (TY)m[7] * x1 + (TY)m[8] * x2;
+    }
+    for (int k = trp[v]; k < trp[v + 1]; ++k) {
+        int c = tcol[k];
+        if (dbc[c]) continue;
+        const T* m = tval + 9 * (long)k;
+        TY x0 = (TY)x[3 * c], x1 = (TY)x[3 * c + 1], x2 = (TY)x[3 * c + 2];
+        a0 += (TY)m[0] * x0 + (TY)m[1] * x1 + (TY)m[2] * x2;
+        a1 += (TY)m[3] * x0 + (TY)m[4] * x1 + (TY)m[5] * x2;
+        a2 += (TY)m[6] * x0 + (TY)m[7] * x1 + (TY)m[8] * x2;
+    }
+    y[0] = a0; y[1] = a1; y[2] = a2;
+}
+
+__device__ double cta_sum(double v) {
+    __shared__ double sh[kBlock];
+    sh[threadIdx.x] = v;
+    __syncthreads();
+    for (int st = kBlock / 2; st > 0; st >>= 1) {
+        if (threadIdx.x < st) sh[threadIdx.x] += sh[threadIdx.x + st];
+        __syncthreads();
+    }
+    double r = sh[0];
+    __syncthreads();
+    return r;
+}
+
+// per-instance PCG scalars
+struct PcgS {
+    double rz, rz_new, pAp, rr, bnorm2, tol2;
+    double alpha, beta;
+    int run;    // still iterating
+    int iters;
+};
+
+// Ap = A p and chunk partials of p.Ap (one CTA per vertex chunk)
+template <class T>
+__global__ void k_pcg_spmv(const Chunk* __restrict__ chunks, const PcgS* __restrict__ S, const int* __restrict__ rowptr,
+                           const int* __restrict__ colidx, const T* __restrict__ val, const int* __restrict__ trp,
+                           const int* __restrict__ tcol, const T* __restrict__ tval,
+                           const unsigned char* __restrict__ dbc, const T* __restrict__ p, T* __restrict__ Ap,
+                           double* __restrict__ part) {
+    Chunk c = chunks[blockIdx.x];
+    if (!S[c.inst].run) return;
+    double acc = 0;
+    for (int v = c.begin + threadIdx.x; v < c.end; v += blockDim.x) {
+        T y[3];
+        spmv_row<T, T, T>(v, rowptr, colidx, val, trp, tcol, tval, dbc, p, y);
+        Ap[3 * v] = y[0]; Ap[3 * v + 1] = y[1]; Ap[3 * v + 2] = y[2];
+        acc += (double)p[3 * v] * (double)y[0] + (double)p[3 * v + 1] * (double)y[1] + (double)p[3 * v + 2] * (double)y[2];
+    }
+    double s = cta_sum(acc);
+    if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+// x += alpha p, r -= alpha Ap, z = Dinv r, partials r.z and r.r
+template <class T>
+__global__ void k_pcg_update(const Chunk* __restrict__ chunks, const PcgS* __restrict__ S, const T* __restrict__ dinv,
+                             const unsigned char* __restrict__ dbc, T* __restrict__ x, T* __restrict__ r,
+                             T* __restrict__ z, const T* __restrict__ p, const T* __restrict__ Ap,
+                             double* __restrict__ part) {
+    Chunk c = chunks[blockIdx.x];
+    if (!S[c.inst].run) return;
+    T a = (T)S[c.inst].alpha;
+    double rz = 0, rr = 0;
+    for (int v = c.begin + threadIdx.x; v < c.end; v += blockDim.x) {
+        T rv[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            x[3 * v + d] += a * p[3 * v + d];
+            rv[d] = r[3 * v + d] - a * Ap[3 * v + d];
+            r[3 * v + d] = rv[d];
+        }
+        const T* D = dinv + 9 * (long)v;
+        T zv[3];
+        if (dbc[v]) { zv[0] = rv[0]; zv[1] = rv[1]; zv[2] = rv[2]; }
+        else {
+            zv[0] = D[0] * rv[0] + D[1] * rv[1] + D[2] * rv[2];
+            zv[1] = D[3] * rv[0] + D[4] * rv[1] + D[5] * rv[2];
+            zv[2] = D[6] * rv[0] + D[7] * rv[1] + D[8] * rv[2];
+        }
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            z[3 * v + d] = zv[d];
+            rz += (double)rv[d] * (double)zv[d];
+            rr += (double)rv[d] * (double)rv[d];
+        }
+    }
+    double s1 = cta_sum(rz);
+    double s2 = cta_sum(rr);
+    if (threadIdx.x == 0) { part[2 * blockIdx.x] = s1; part[2 * blockIdx.x + 1] = s2; }
+}
+
+// init: x = 0, r = b, z = Dinv r, p = z ; partials r.z, r.r
+template <class T>
+__global__ void k_pcg_init(const Chunk* __restrict__ chunks, const unsigned char* __restrict__ active,
+                           const T* __restrict__ dinv, const unsigned char* __restrict__ dbc, const double* __restrict__ b,
+                           T* __restrict__ x, T* __restrict__ r, T* __restrict__ z, T* __restrict__ p,
+                           double* __restrict__ part) {
+    Chunk c = chunks[blockIdx.x];
+    if (!active[c.inst]) return;
+    double rz = 0, rr = 0;
+    for (int v = c.begin + threadIdx.x; v < c.end; v += blockDim.x) {
+        T rv[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            rv[d] = dbc[v] ? T(0) : (T)b[3 * v + d];
+            x[3 * v + d] = T(0);
+            r[3 * v + d] = rv[d];
+        }
+        const T* D = dinv + 9 * (long)v;
+        T zv[3];
+        if (dbc[v]) { zv[0] = zv[1] = zv[2] = T(0); }
+        else {
+            zv[0] = D[0] * rv[0] + D[1] * rv[1] + D[2] * rv[2];
+            zv[1] = D[3] * rv[0] + D[4] * rv[1] + D[5] * rv[2];
+            zv[2] = D[6] * rv[0] + D[7] * rv[1] + D[8] * rv[2];
+        }
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            z[3 * v + d] = zv[d];
+            p[3 * v + d] = zv[d];
+            rz += (double)rv[d] * (double)zv[d];
+            rr += (double)rv[d] * (double)rv[d];
+        }
+    }
+    double s1 = cta_sum(rz);
+    double s2 = cta_sum(rr);
+    if (threadIdx.x == 0) { part[2 * blockIdx.x] = s1; part[2 * blockIdx.x + 1] = s2; }
+}
+
+template <class T>
+__global__ void k_pcg_pupdate(const Chunk* __restrict__ chunks, const PcgS* __restrict__ S, const T* __restrict__ z,
+                              T* __restrict__ p) {
+    Chunk c = chunks[blockIdx.x];
+    if (!S[c.inst].run) return;
+    T bt = (T)S[c.inst].beta;
+    for (int v = c.begin + threadIdx.x; v < c.end; v += blockDim.x)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) p[3 * v + d] = z[3 * v + d] + bt * p[3 * v + d];
+}
+
+// per-instance scalar steps; partial sums reduced in chunk order
+__global__ void k_pcg_scal_init(int nI, const int* __restrict__ coff, const unsigned char* __restrict__ active,
+                                const double* __restrict__ part, double rel_tol, PcgS* __restrict__ S) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nI) return;
+    PcgS s;
+    double rz = 0, rr = 0;
+    for (int c = coff[i]; c < coff[i + 1]; ++c) { rz += part[2 * c]; rr += part[2 * c + 1]; }
+    s.rz = rz; s.rz_new = rz; s.rr = rr; s.bnorm2 = rr; s.tol2 = rel_tol * rel_tol * rr;
+    s.alpha = 0; s.beta = 0; s.pAp = 0; s.iters = 0;
+    s.run = active[i] && rr > 0 && rr > s.tol2;
+    S[i] = s;
+}
+
+__global__ void k_pcg_scal_alpha(int nI, const int* __restrict__ coff, const double* __restrict__ part,
+                                 PcgS* __restrict__ S) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nI || !S[i].run) return;
+    double pAp = 0;
+    for (int c = coff[i]; c < coff[i + 1]; ++c) pAp += part[c];
+    S[i].pAp = pAp;
+    if (!(pAp > 0)) {  // direction of non-positive curvature: stop here
+        S[i].run = 0;
+        S[i].alpha = 0;
+        return;
+    }
+    S[i].alpha = S[i].rz / pAp;
+}
+
+__global__ void k_pcg_scal_beta(int nI, const int* __restrict__ coff, const double* __restrict__ part, int max_iters,
+                                PcgS* __restrict__ S, int* __restrict__ any_running) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nI || !S[i].run) return;
+    double rz = 0, rr = 0;
+    for (int c = coff[i]; c < coff[i + 1]; ++c) { rz += part[2 * c]; rr += part[2 * c + 1]; }
+    PcgS s = S[i];
+    s.iters += 1;
+    s.rr = rr;
+    s.beta = rz / s.rz;
+    s.rz = rz;
+    if (rr <= s.tol2 || s.iters >= max_iters) s.run = 0;
+    if (s.run) atomicOr(any_running, 1);
+    S[i] = s;
+}
+
+// FP64 residual: res = b - A x64 (FP32/FP64 matrix, FP64 accumulation);
+// chunk partials of res.res
+template <class T>
+__global__ void k_residual64(const Chunk* __restrict__ chunks, const unsigned char* __restrict__ active,
+                             const int* __restrict__ rowptr, const int* __restrict__ colidx, const T* __restrict__ val,
+                             const int* __restrict__ trp, const int* __restrict__ tcol, const T* __restrict__ tval,
+                             const unsigned char* __restrict__ dbc, const double* __restrict__ b,
+                             const double* __restrict__ x, double* __restrict__ res, double* __restrict__ part) {
+    Chunk c = chunks[blockIdx.x];
+    if (!active[c.inst]) return;
+    double acc = 0;
+    for (int v = c.begin + threadIdx.x; v < c.end; v += blockDim.x) {
+        double y[3];
+        spmv_row<T, double, double>(v, rowptr, colidx, val, trp, tcol, tval, dbc, x, y);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            double r = dbc[v] ? 0.0 : b[3 * v + d] - y[d];
+            res[3 * v + d] = r;
+            acc += r * r;
+        }
+    }
+    double s = cta_sum(acc);
+    if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+template <class T>
+__global__ void k_add_correction(long V, const int* __restrict__ vinst, const unsigned char* __restrict__ active,
+                                 const T* __restrict__ e, double* __restrict__ x) {
+    long v = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= V || !active[vinst[v]]) return;
+    for (int d = 0; d < 3; ++d) x[3 * v + d] += (double)e[3 * v + d];
+}
+
+template <class T>
+__global__ void k_spmv_plain(long V, const int* __restrict__ vinst, const unsigned char* __restrict__ active,
+                             const int* __restrict__ rowptr, const int* __restrict__ colidx, const T* __restrict__ val,
+                             const int* __restrict__ trp, const int* __restrict__ tcol, const T* __restrict__ tval,
+                             const unsigned char* __restrict__ dbc, const double* __restrict__ x,
+                             double* __restrict__ y) {
+    long v = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= V || !active[vinst[v]]) return;
+    double o[3];
+    spmv_row<T, double, double>(v, rowptr, colidx, val, trp, tcol, tval, dbc, x, o);
+    y[3 * v] = o[0]; y[3 * v + 1] = o[1]; y[3 * v + 2] = o[2];
+}
+
+// ---- per-vertex Newton kernels
+__global__ void k_grad_gather_tet(long V, const int* __restrict__ vinst, const unsigned char* __restrict__ active,
+                                  const int* __restrict__ vcp, const int* __restrict__ vc,
+                                  const double* __restrict__ tg, const double* __restrict__ mass,
+                                  const double* __restrict__ X, const double* __restrict__ Xt, double* __restrict__ g) {
+    long v = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= V || !active[vinst[v]]) return;
+    double s0 = 0, s1 = 0, s2 = 0;
+    for (int k = vcp[v]; k < vcp[v + 1]; ++k) {
+        int code = vc[k];  // tet*4 + corner
+        const double* p = tg + 12 * (long)(code >> 2) + 3 * (code & 3);
+        s0 += p[0]; s1 += p[1]; s2 += p[2];
+    }
+    double m = mass[v];
+    g[3 * v] = s0 + m * (X[3 * v] - Xt[3 * v]);
+    g[3 * v + 1] = s1 + m * (X[3 * v + 1] - Xt[3 * v + 1]);
+    g[3 * v + 2] = s2 + m * (X[3 * v + 2] - Xt[3 * v + 2]);
+}
+
+__global__ void k_inertia_energy(const Chunk* __restrict__ chunks, const unsigned char* __restrict__ active,
+                                 const double* __restrict__ mass, const double* __restrict__ X,
+                                 const double* __restrict__ Xt, double* __restrict__ part) {
+    Chunk c = chunks[blockIdx.x];
+    double acc = 0;
+    if (active[c.inst])
+        for (int v = c.begin + threadIdx.x; v < c.end; v += blockDim.x) {
+            double d0 = X[3 * v] - Xt[3 * v], d1 = X[3 * v + 1] - Xt[3 * v + 1], d2 = X[3 * v + 2] - Xt[3 * v + 2];
+            acc += 0.5 * mass[v] * (d0 * d0 + d1 * d1 + d2 * d2);
+        }
+    double s = cta_sum(acc);
+    if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+__global__ void k_chunk_reduce(int nI, const int* __restrict__ coff, const double* __restrict__ part,
+                               double* __restrict__ out, int accumulate) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nI) return;
+    double s = 0;
+    for (int c = coff[i]; c < coff[i + 1]; ++c) s += part[c];
+    out[i] = accumulate ? out[i] + s : s;
+}
+
+__global__ void k_axpy_trial(long V, const int* __restrict__ vinst, const unsigned char* __restrict__ active,
+                             const double* __restrict__ alpha, const double* __restrict__ Xp,
+                             const double* __restrict__ dir, double* __restrict__ Xo) {
+    long v = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= V) return;
+    int i = vinst[v];
+    if (!active[i]) return;
+    double a = alpha[i];
+    for (int d = 0; d < 3; ++d) Xo[3 * v + d] = Xp[3 * v + d] + a * dir[3 * v + d];
+}
+
+__global__ void k_zero_dbc(long V, const unsigned char* __restrict__ dbc, double* __restrict__ g) {
+    long v = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= V || !dbc[v]) return;
+    g[3 * v] = g[3 * v + 1] = g[3 * v + 2] = 0;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- host side
+int chunk_reduce_off(Arena& A, const int* coff, const double* part, double* out, bool accumulate, cudaStream_t s) {
+    k_chunk_reduce<<<grid_for(A.nI), kBlock, 0, s>>>(A.nI, coff, part, out, accumulate ? 1 : 0);
+    return cudaGetLastError() == cudaSuccess ? IDP_OK : IDP_ERR_CUDA;
+}
+
+int chunk_reduce(Arena& A, Work& W, const Chunk* chunks, int nchunks, const double* part, double* out, cudaStream_t s) {
+    (void)W;
+    (void)nchunks;
+    const int* coff = (chunks == A.tet_chunks) ? A.tet_chunk_off : A.vert_chunk_off;
+    return chunk_reduce_off(A, coff, part, out, false, s);
+}
+
+int vec_inertia(Arena& A, Work& W, const double* X, double* inst_E, double* g, cudaStream_t s) {
+    (void)g;
+    if (W[W_CHUNK_SUM].ensure(sizeof(double) * (A.n_vert_chunks + A.n_tet_chunks + 2))) return IDP_ERR_CUDA;
+    double* part = W[W_CHUNK_SUM].as<double>();
+    k_inertia_energy<<<A.n_vert_chunks, kBlock, 0, s>>>(A.vert_chunks, A.active, A.mass, X, A.Xtilde, part);
+    return chunk_reduce_off(A, A.vert_chunk_off, part, inst_E, false, s);
+}
+
+int grad_gather_tet(Arena& A, Work& W, const double* X, double* g, cudaStream_t s) {
+    k_grad_gather_tet<<<grid_for(A.V), kBlock, 0, s>>>(A.V, A.vinst, A.active, A.vert_corner_ptr, A.vert_corner,
+                                                       W[W_TET_GRAD].as<double>(), A.mass, X, A.Xtilde, g);
+    return cudaGetLastError() == cudaSuccess ? IDP_OK : IDP_ERR_CUDA;
+}
+
+int vec_axpy_trial(Arena& A, const double* Xprev, const double* dir, double* Xout, cudaStream_t s) {
+    k_axpy_trial<<<grid_for(A.V), kBlock, 0, s>>>(A.V, A.vinst, A.active, A.alpha, Xprev, dir, Xout);
+    return cudaGetLastError() == cudaSuccess ? IDP_OK : IDP_ERR_CUDA;
+}
+
+int vec_zero_dbc(Arena& A, double* g, cudaStream_t s) {
+    k_zero_dbc<<<grid_for(A.V), kBlock, 0, s>>>(A.V, A.dbc, g);
+    return cudaGetLastError() == cudaSuccess ? IDP_OK : IDP_ERR_CUDA;
+}
+
+int assemble(Arena& A, Work& W, const ContactSet& cs, bool fp64, cudaStream_t s) {
+    (void)cs;
+    size_t el = fp64 ? sizeof(double) : sizeof(float);
+    if (W[W_BSR_VAL].ensure(el * 9 * (A.B + 1)) || W[W_DIAG_INV].ensure(el * 9 * (A.V + 1))) return IDP_ERR_CUDA;
+    const int* trp = W[W_TAIL_ROWPTR].as<int>();
+    const int* tcol = W[W_TAIL_COL].as<int>();
+    if (fp64) {
+        k_assemble_tet<double><<<grid_for(A.B), kBlock, 0, s>>>(A.B, A.src_ptr, A.src, W[W_TET_HESS].as<double>(), A.brow,
+                                                                A.colidx, A.mass, A.dbc, A.vinst, A.active,
+                                                                W[W_BSR_VAL].as<double>());
+        k_diag_inv<double><<<grid_for(A.V), kBlock, 0, s>>>(A.V, A.diagblk, W[W_BSR_VAL].as<double>(), trp, tcol,
+                                                            W[W_TAIL_VAL].as<double>(), A.dbc, A.vinst, A.active,
+                                                            W[W_DIAG_INV].as<double>());
+    } else {
+        k_assemble_tet<float><<<grid_for(A.B), kBlock, 0, s>>>(A.B, A.src_ptr, A.src, W[W_TET_HESS].as<float>(), A.brow,
+                                                               A.colidx, A.mass, A.dbc, A.vinst, A.active,
+                                                               W[W_BSR_VAL].as<float>());
+        k_diag_inv<float><<<grid_for(A.V), kBlock, 0, s>>>(A.V, A.diagblk, W[W_BSR_VAL].as<float>(), trp, tcol,
+                                                           W[W_TAIL_VAL].as<float>(), A.dbc, A.vinst, A.active,
+                                                           W[W_DIAG_INV].as<float>());
+    }
+    return cudaGetLastError() == cudaSuccess ? IDP_OK : IDP_ERR_CUDA;
+}
+
+int hessian_apply(Arena& A, Work& W, bool fp64, const double* x, double* y, cudaStream_t s) {
+    const int* trp = W[W_TAIL_ROWPTR].as<int>();
+    const int* tcol = W[W_TAIL_COL].as<int>();
+    if (fp64)
+        k_spmv_plain<double><<<grid_for(A.V), kBlock, 0, s>>>(A.V, A.vinst, A.active, A.rowptr, A.colidx,
+                                                              W[W_BSR_VAL].as<double>(), trp, tcol,
+                                                              W[W_TAIL_VAL].as<double>(), A.dbc, x, y);
+    else
+        k_spmv_plain<float><<<grid_for(A.V), kBlock, 0, s>>>(A.V, A.vinst, A.active, A.rowptr, A.colidx,
+                                                             W[W_BSR_VAL].as<float>(), trp, tcol,
+                                                             W[W_TAIL_VAL].as<float>(), A.dbc, x, y);
+    return cudaGetLastError() == cudaSuccess ? IDP_OK : IDP_ERR_CUDA;
+}
+
+// PCG on b (FP64 rhs), result added to nothing: x (type T) holds the solution
+template <class T>
+static int pcg_inner(Arena& A, Work& W, const double* b, double rel_tol, int max_iters, std::vector<int>& iters,
+                     T** xout, cudaStream_t s) {
+    const int nI = A.nI;
+    long n3 = 3 * A.V;
+    if (W[W_PCG_VEC].ensure(sizeof(T) * 5 * (n3 + 4)) || W[W_PCG_SCAL].ensure(sizeof(PcgS) * nI + 64) ||
+        W[W_CHUNK_SUM].ensure(sizeof(double) * 2 * (A.n_vert_chunks + 2)))
+        return IDP_ERR_CUDA;
+    T* base = W[W_PCG_VEC].as<T>();
+    T *x = base, *r = base + n3 + 4, *z = r + n3 + 4, *p = z + n3 + 4, *Ap = p + n3 + 4;
+    PcgS* S = W[W_PCG_SCAL].as<PcgS>();
+    int* any = reinterpret_cast<int*>(S + nI);
+    double* part = W[W_CHUNK_SUM].as<double>();
+    const T* val = W[W_BSR_VAL].as<T>();
+    const T* dinv = W[W_DIAG_INV].as<T>();
+    const int* trp = W[W_TAIL_ROWPTR].as<int>();
+    const int* tcol = W[W_TAIL_COL].as<int>();
+    const T* tval = W[W_TAIL_VAL].as<T>();
+    const int nc = A.n_vert_chunks;
+    k_pcg_init<T><<<nc, kBlock, 0, s>>>(A.vert_chunks, A.active, dinv, A.dbc, b, x, r, z, p, part);
+    k_pcg_scal_init<<<grid_for(nI), kBlock, 0, s>>>(nI, A.vert_chunk_off, A.active, part, rel_tol, S);
+    const int check_every = 8;
+    for (int it = 0; it < max_iters; it += check_every) {
+        IDP_CUDA_TRY(cudaMemsetAsync(any, 0, sizeof(int), s));
+        for (int k = 0; k < check_every; ++k) {
+            k_pcg_spmv<T><<<nc, kBlock, 0, s>>>(A.vert_chunks, S, A.rowptr, A.colidx, val, trp, tcol, tval, A.dbc, p, Ap,
+                                                part);
+            k_pcg_scal_alpha<<<grid_for(nI), kBlock, 0, s>>>(nI, A.vert_chunk_off, part, S);
+            k_pcg_update<T><<<nc, kBlock, 0, s>>>(A.vert_chunks, S, dinv, A.dbc, x, r, z, p, Ap, part);
+            k_pcg_scal_beta<<<grid_for(nI), kBlock, 0, s>>>(nI, A.vert_chunk_off, part, max_iters, S, any);
+            k_pcg_pupdate<T><<<nc, kBlock, 0, s>>>(A.vert_chunks, S, z, p);
+        }
+        int hany = 0;
+        IDP_CUDA_TRY(cudaMemcpyAsync(&hany, any, sizeof(int), cudaMemcpyDeviceToHost, s));
+        IDP_CUDA_TRY(cudaStreamSynchronize(s));
+        if (!hany) break;
+    }
+    std::vector<PcgS> hs(nI);
+    IDP_CUDA_TRY(cudaMemcpyAsync(hs.data(), S, sizeof(PcgS) * nI, cudaMemcpyDeviceToHost, s));
+    IDP_CUDA_TRY(cudaStreamSynchronize(s));
+    iters.resize(nI);
+    for (int i = 0; i < nI; ++i) iters[i] = hs[i].iters;
+    *xout = x;
+    return IDP_OK;
+}
+
+int pcg_solve(Arena& A, Work& W, const ContactSet& cs, bool fp64, const double* rhs, double* sol, double rel_tol,
+              int max_iters, std::vector<int>& iters_out, std::vector<double>& relres_out, cudaStream_t s) {
+    (void)cs;
+    const int nI = A.nI;
+    long n3 = 3 * A.V;
+    iters_out.assign(nI, 0);
+    relres_out.assign(nI, 0.0);
+    if (W[W_PCG_VEC64].ensure(sizeof(double) * (n3 + 4)) ||
+        W[W_INST_SUM].ensure(sizeof(double) * 8 * (nI + 1)) || W[W_MISC].ensure(sizeof(double) * (A.n_vert_chunks + 2)))
+        return IDP_ERR_CUDA;
+    double* res = W[W_PCG_VEC64].as<double>();
+    double* inst_rr = W[W_INST_SUM].as<double>();
+    double* part = W[W_MISC].as<double>();
+    const int* trp = W[W_TAIL_ROWPTR].as<int>();
+    const int* tcol = W[W_TAIL_COL].as<int>();
+    IDP_CUDA_TRY(cudaMemsetAsync(sol, 0, sizeof(double) * n3, s));
+    std::vector<double> b2(nI, 0.0), hrr(nI);
+    std::vector<unsigned char> act(nI), act0(nI);
+    IDP_CUDA_TRY(cudaMemcpyAsync(act0.data(), A.active, nI, cudaMemcpyDeviceToHost, s));
+    // |b|^2 per instance (x = 0 gives res = b)
+    auto residual = [&](std::vector<double>& out) -> int {
+        if (fp64)
+            k_residual64<double><<<A.n_vert_chunks, kBlock, 0, s>>>(A.vert_chunks, A.active, A.rowptr, A.colidx,
+                                                                    W[W_BSR_VAL].as<double>(), trp, tcol,
+                                                                    W[W_TAIL_VAL].as<double>(), A.dbc, rhs, sol, res, part);
+        else
+            k_residual64<float><<<A.n_vert_chunks, kBlock, 0, s>>>(A.vert_chunks, A.active, A.rowptr, A.colidx,
+                                                                   W[W_BSR_VAL].as<float>(), trp, tcol,
+                                                                   W[W_TAIL_VAL].as<float>(), A.dbc, rhs, sol, res, part);
+        if (chunk_reduce_off(A, A.vert_chunk_off, part, inst_rr, false, s)) return IDP_ERR_CUDA;
+        IDP_CUDA_TRY(cudaMemcpyAsync(out.data(), inst_rr, sizeof(double) * nI, cudaMemcpyDeviceToHost, s));
+        IDP_CUDA_TRY(cudaStreamSynchronize(s));
+        return IDP_OK;
+    };
+    int rc = residual(b2);
+    if (rc) return rc;
+    const int max_refine = fp64 ? 1 : 8;
+    const double inner_tol = fp64 ? rel_tol : std::max(rel_tol, 1e-3);
+    for (int ref = 0; ref < max_refine; ++ref) {
+        // instances whose FP64 residual is already small stop refining
+        bool any = false;
+        if (ref > 0) {
+            rc = residual(hrr);
+            if (rc) return rc;
+        } else {
+            hrr = b2;
+        }
+        for (int i = 0; i < nI; ++i) {
+            act[i] = act0[i] && b2[i] > 0 && hrr[i] > rel_tol * rel_tol * b2[i];
+            relres_out[i] = b2[i] > 0 ? std::sqrt(hrr[i] / b2[i]) : 0.0;
+            any |= act[i] != 0;
+        }
+        if (!any) break;
+        IDP_CUDA_TRY(cudaMemcpyAsync(A.active, act.data(), nI, cudaMemcpyHostToDevice, s));
+        std::vector<int> its;
+        if (fp64) {
+            double* e = nullptr;
+            rc = pcg_inner<double>(A, W, res, inner_tol, max_iters, its, &e, s);
+            if (rc) break;
+            k_add_correction<double><<<grid_for(A.V), kBlock, 0, s>>>(A.V, A.vinst, A.active, e, sol);
+        } else {
+            float* e = nullptr;
+            rc = pcg_inner<float>(A, W, res, inner_tol, max_iters, its, &e, s);
+            if (rc) break;
+            k_add_correction<float><<<grid_for(A.V), kBlock, 0, s>>>(A.V, A.vinst, A.active, e, sol);
+        }
+        for (int i = 0; i < nI; ++i)
+            if (act[i]) iters_out[i] += its[i];
+    }
+    IDP_CUDA_TRY(cudaMemcpyAsync(A.active, act0.data(), nI, cudaMemcpyHostToDevice, s));
+    if (rc) return rc;
+    rc = residual(hrr);
+    if (rc) return rc;
+    for (int i = 0; i < nI; ++i) relres_out[i] = b2[i] > 0 ? std::sqrt(hrr[i] / b2[i]) : 0.0;
+    return IDP_OK;
+}
+
+}  // namespace idp

@@ -1,0 +1,189 @@
+"""Seeded synthetic tet meshes and deformation targets for the Newton-step
+workloads (host-side input generation; numpy only).
+
+* ``bar``: a box on an nx x ny x nz cube grid, every cube split into 5 tets
+  (alternating split so faces conform), interior vertices jittered.
+* ``bend_target``: maps the bar's centreline onto a circle (optionally with a
+  twist), keeping cross-sections orthogonal, which makes the target surface
+  self-intersect once the arc spans more than 2*pi.
+* ``blob``: a star-shaped body r(u) = 1 + a * sum of real spherical harmonics,
+  tetrahedralised on a background cube grid (cubes whose centre is inside).
+* ``bar_batch``: many bars with log-uniform tet counts, for batched solves.
+
+The reference reads these shapes from .vtk/.obj files
+(``Python/Drivers/FEMDiscreteShellBase.py:184-188``); here they are generated
+so every workload is reproducible from a seed.
+"""
+from __future__ import annotations
+
+import math
+import numpy as np
+
+# corner index (a, b, c) -> local id a + 2b + 4c
+_C = {(a, b, c): a + 2 * b + 4 * c for a in (0, 1) for b in (0, 1) for c in (0, 1)}
+_SPLIT_EVEN = [
+    [_C[0, 0, 0], _C[1, 1, 0], _C[1, 0, 1], _C[0, 1, 1]],
+    [_C[1, 0, 0], _C[0, 0, 0], _C[1, 1, 0], _C[1, 0, 1]],
+    [_C[0, 1, 0], _C[0, 0, 0], _C[1, 1, 0], _C[0, 1, 1]],
+    [_C[0, 0, 1], _C[0, 0, 0], _C[1, 0, 1], _C[0, 1, 1]],
+    [_C[1, 1, 1], _C[1, 1, 0], _C[1, 0, 1], _C[0, 1, 1]],
+]
+_SPLIT_ODD = [
+    [_C[1, 0, 0], _C[0, 1, 0], _C[0, 0, 1], _C[1, 1, 1]],
+    [_C[0, 0, 0], _C[1, 0, 0], _C[0, 1, 0], _C[0, 0, 1]],
+    [_C[1, 1, 0], _C[1, 0, 0], _C[0, 1, 0], _C[1, 1, 1]],
+    [_C[1, 0, 1], _C[1, 0, 0], _C[0, 0, 1], _C[1, 1, 1]],
+    [_C[0, 1, 1], _C[0, 1, 0], _C[0, 0, 1], _C[1, 1, 1]],
+]
+
+
+def _orient(X: np.ndarray, tets: np.ndarray) -> np.ndarray:
+    """Swap two vertices of every negatively oriented tet."""
+    d = X[tets[:, 1:]] - X[tets[:, :1]]
+    det = np.einsum("ti,ti->t", d[:, 0], np.cross(d[:, 1], d[:, 2]))
+    tets = tets.copy()
+    neg = det < 0
+    tets[neg, 1], tets[neg, 2] = tets[neg, 2].copy(), tets[neg, 1].copy()
+    return tets
+
+
+def cube_grid_tets(mask: np.ndarray):
+    """Tets of the cubes where ``mask[i, j, k]`` is True on a vertex lattice
+    of shape (nx+1, ny+1, nz+1). Returns (vertex_ids_used, tets over lattice ids)."""
+    nx, ny, nz = mask.shape
+    vid = lambda i, j, k: (i * (ny + 1) + j) * (nz + 1) + k  # noqa: E731
+    cubes = np.argwhere(mask)
+    tets = []
+    for i, j, k in cubes:
+        corners = np.array([vid(i + a, j + b, k + c) for c in (0, 1) for b in (0, 1) for a in (0, 1)])
+        split = _SPLIT_EVEN if (i + j + k) % 2 == 0 else _SPLIT_ODD
+        for t in split:
+            tets.append(corners[t])
+    return np.asarray(tets, dtype=np.int64).reshape(-1, 4)
+
+
+def _compact(Xlat: np.ndarray, tets: np.ndarray):
+    used = np.unique(tets)
+    remap = -np.ones(Xlat.shape[0], dtype=np.int64)
+    remap[used] = np.arange(used.size)
+    return Xlat[used].copy(), remap[tets]
+
+
+def bar(nx=6, ny=6, nz=24, size=(1.0, 1.0, 4.0), jitter=0.05, seed=0):
+    """Box [0,sx]x[0,sy]x[0,sz] on an nx x ny x nz cube grid, 5 tets per cube.
+    Interior vertices are jittered uniformly by +-jitter*h (h = cube edge)."""
+    sx, sy, sz = size
+    xs = np.linspace(0, sx, nx + 1)
+    ys = np.linspace(0, sy, ny + 1)
+    zs = np.linspace(0, sz, nz + 1)
+    X = np.stack(np.meshgrid(xs, ys, zs, indexing="ij"), -1).reshape(-1, 3)
+    tets = cube_grid_tets(np.ones((nx, ny, nz), dtype=bool))
+    h = min(sx / nx, sy / ny, sz / nz)
+    rng = np.random.default_rng(seed)
+    ii, jj, kk = np.meshgrid(np.arange(nx + 1), np.arange(ny + 1), np.arange(nz + 1), indexing="ij")
+    interior = ((ii > 0) & (ii < nx) & (jj > 0) & (jj < ny) & (kk > 0) & (kk < nz)).reshape(-1)
+    J = rng.uniform(-jitter * h, jitter * h, size=X.shape)
+    X = X + J * interior[:, None]
+    tets = _orient(X, tets)
+    return X, tets.astype(np.int32)
+
+
+def bend_target(X, angle=2.2 * math.pi, radius=0.5, size=(1.0, 1.0, 4.0), twist=0.0):
+    """Centreline (x=sx/2, y=sy/2, z in [0,sz]) mapped onto a circle of the
+    given radius spanning ``angle`` radians; cross-sections stay orthogonal to
+    the centreline (x offset -> radial, y offset -> binormal). ``twist``
+    rotates cross-sections by twist*s about the centreline."""
+    sx, sy, sz = size
+    s = X[:, 2] / sz
+    th = angle * s
+    ox, oy = X[:, 0] - sx / 2, X[:, 1] - sy / 2
+    if twist:
+        ph = twist * s
+        ox, oy = ox * np.cos(ph) - oy * np.sin(ph), ox * np.sin(ph) + oy * np.cos(ph)
+    n = np.stack([np.cos(th), np.sin(th), np.zeros_like(th)], -1)
+    r = (radius + ox)[:, None]
+    return r * n + oy[:, None] * np.array([0.0, 0.0, 1.0])
+
+
+def _real_sh(lmax, theta, phi):
+    """Real spherical harmonics up to degree lmax (unnormalised associated
+    Legendre via scipy), columns ordered (l, m)."""
+    from scipy.special import sph_harm_y  # scipy >= 1.15
+
+    cols, lm = [], []
+    for l in range(1, lmax + 1):
+        for m in range(-l, l + 1):
+            Y = sph_harm_y(l, abs(m), theta, phi)
+            if m < 0:
+                cols.append(math.sqrt(2) * (-1) ** m * Y.imag)
+            elif m == 0:
+                cols.append(Y.real)
+            else:
+                cols.append(math.sqrt(2) * (-1) ** m * Y.real)
+            lm.append(l)
+    return np.stack(cols, -1), np.asarray(lm)
+
+
+def blob(n=64, lmax=8, amp=0.3, seed=0):
+    """Closed bumpy blob r(u) = 1 + amp * sum_{l<=lmax} c_lm Y_lm(u),
+    c_lm ~ N(0, 1/l^2), tetrahedralised on an n^3 background grid: every cube
+    whose centre lies inside is split into 5 tets."""
+    rng = np.random.default_rng(seed)
+    nlm = sum(2 * l + 1 for l in range(1, lmax + 1))
+    ls = np.concatenate([[l] * (2 * l + 1) for l in range(1, lmax + 1)])
+    coef = rng.normal(0.0, 1.0, nlm) / ls
+    # bound the radius range so the grid covers it
+    ext = 1.0 + amp * np.abs(coef).sum() * 0.5
+    ext = min(ext, 2.5)
+    g = np.linspace(-ext, ext, n + 1)
+    h = g[1] - g[0]
+    cc = (g[:-1] + g[1:]) / 2
+    C = np.stack(np.meshgrid(cc, cc, cc, indexing="ij"), -1).reshape(-1, 3)
+    rr = np.linalg.norm(C, axis=1)
+    theta = np.arccos(np.clip(C[:, 2] / np.maximum(rr, 1e-30), -1, 1))
+    phi = np.arctan2(C[:, 1], C[:, 0])
+    Y, _ = _real_sh(lmax, theta, phi)
+    R = 1.0 + amp * (Y @ coef)
+    inside = (rr < R).reshape(n, n, n)
+    Xlat = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3)
+    tets = cube_grid_tets(inside)
+    X, tets = _compact(Xlat, tets)
+    tets = _orient(X, tets)
+    return X, tets.astype(np.int32), h
+
+
+def bar_dims_for_tets(target_tets: float):
+    """Grid (n, n, 4n) whose 5*4n^3 tets is closest to target_tets."""
+    n = max(1, int(round((target_tets / 20.0) ** (1.0 / 3.0))))
+    return n, n, 4 * n
+
+
+def bar_batch(count=256, tmin=1_000, tmax=50_000, seed=0):
+    """Bars with tet counts log-uniform in [tmin, tmax] and bend angles uniform
+    in [1.5pi, 2.5pi]. Returns a list of dicts (X, tets, target, angle)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(count):
+        t = math.exp(rng.uniform(math.log(tmin), math.log(tmax)))
+        nx, ny, nz = bar_dims_for_tets(t)
+        ang = rng.uniform(1.5 * math.pi, 2.5 * math.pi)
+        X, tets = bar(nx, ny, nz, jitter=0.05, seed=int(rng.integers(1 << 31)))
+        out.append(dict(X=X, tets=tets, target=bend_target(X, angle=ang), angle=ang))
+    return out
+
+
+def lumped_mass(X, tets, density):
+    """Per-vertex lumped mass, vol * density / 4 per tet corner
+    (FEM/ELEM_TO_NODE.h:11-46)."""
+    d = X[tets[:, 1:]] - X[tets[:, :1]]
+    vol = np.einsum("ti,ti->t", d[:, 0], np.cross(d[:, 1], d[:, 2])) / 6.0
+    m = np.zeros(X.shape[0])
+    np.add.at(m, tets.reshape(-1), np.repeat(vol * density / 4.0, 4))
+    return m
+
+
+def lame(E, nu):
+    """Lame parameters as NEOHOOKEAN_FUNCTOR::Append (Physics/NEOHOOKEAN.h:45-50)."""
+    lam = E * nu / ((1 + nu) * (1 - 2 * nu))
+    mu = E / (2 * (1 + nu))
+    return lam, mu

@@ -1,0 +1,151 @@
+/*
+ * idp_gb300 — C ABI of the GB300 injective-deformation Newton step.
+ *
+ * Replaces the pybind11 entry point FEM.DiscreteShell.Advance_One_Step_IE_Hinge
+ * (Library/FEM/Shell/DISCRETE_SHELL.h:1110, body
+ * Library/FEM/Shell/IMPLICIT_EULER.h:151-891) for tet meshes with offset IPC
+ * self-contact, and exposes the sub-steps the reference computes inside it so
+ * a caller (or a test) can check each one.
+ *
+ * Conventions: positions are double[3*V] (x0,y0,z0,x1,...), tets int32[4*T]
+ * with instance-local vertex ids. The caller owns every host buffer; the
+ * library owns device state between calls and copies explicitly. No call
+ * exits the process: every failure is an IDP_* status.
+ */
+#ifndef IDP_GB300_H
+#define IDP_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes (the reference prints and calls exit(-1) where these return) */
+#define IDP_OK 0
+#define IDP_ERR_INVALID_ARG 1
+#define IDP_ERR_CUDA 2
+#define IDP_ERR_CAPACITY 3
+#define IDP_ERR_INVERTED 4          /* input has a tet with det F <= 0            */
+#define IDP_ERR_NOT_CONVERGED 5     /* Newton stopped at max_newton               */
+#define IDP_ERR_ZERO_STEP 6         /* CCD step 0 (IPC.h:2014-2031 exits)         */
+#define IDP_ERR_NONPOSITIVE_DIST 7  /* barrier at d <= 0 (IPC.h:925-928 exits)    */
+#define IDP_ERR_STATE 8             /* call out of order (e.g. advance before commit) */
+#define IDP_WARN_ITER_CAP 9         /* an ACCD loop hit its cap; step still safe  */
+
+#define IDP_MODE_FP64 0   /* plain FP64 path: FP64 Hessians, BSR and PCG          */
+#define IDP_MODE_MIXED 1  /* FP32 Hessians/BSR/PCG + FP64 residual refinement   */
+
+typedef struct idp_ctx idp_ctx;
+
+typedef struct idp_params {
+    double h;             /* time step (IMPLICIT_EULER.h:164 `h`)                   */
+    double newton_tol;    /* PNTol, stop when max of last 3 ||p||/sqrt(N-nDBC)/h <= tol
+                             (IMPLICIT_EULER.h:647-676,759,855)                       */
+    int max_newton;       /* Newton iteration cap                                   */
+    int mode;             /* IDP_MODE_FP64 or IDP_MODE_MIXED                        */
+    double pcg_rel_tol;   /* relative residual of each Newton direction            */
+    int pcg_max_iters;    /* PCG iteration cap per refinement sweep                 */
+    double thickness;     /* IPC offset (`thickness` argument, IPC.h:53,757)        */
+    int device;           /* CUDA device ordinal                                    */
+} idp_params;
+
+typedef struct idp_result {
+    int status;           /* IDP_* of this instance                                 */
+    int newton_iters;     /* return value of Advance_One_Step_IE_Discrete_Shell     */
+    int pcg_iters;        /* total PCG iterations over the step                     */
+    int ls_trials;        /* line-search energy evaluations                         */
+    int num_constraints;  /* |constraint set| at the end (IMPLICIT_EULER.h:860)     */
+    double energy;        /* final incremental potential                            */
+    double kappa;         /* barrier stiffness after adaptation (kappaVec[0])       */
+    double residual;      /* last Newton residual                                   */
+    double min_alpha;     /* smallest accepted line-search step                     */
+} idp_result;
+
+/* Defaults: h=0.1, newton_tol=1e-3, max_newton=2000, mode=MIXED,
+   pcg_rel_tol=1e-6, pcg_max_iters=2000, thickness=0, device=0. */
+void idp_default_params(idp_params* p);
+
+/* Context: one CUDA stream and one device arena. */
+idp_ctx* idp_create(const idp_params* p, int* status);
+void idp_destroy(idp_ctx* ctx);
+const char* idp_status_str(int status);
+
+/* Add one mesh instance. Stands for the state the Python driver hands the
+ * reference (FEMDiscreteShellBase.add_object_3D / initialize_added_objects /
+ * initialize_OIPC, Python/Drivers/FEMDiscreteShellBase.py:184-242):
+ *   X     current positions (X argument, mutated by the step)
+ *   X0    rest positions (nodeAttr x0; used for Dm^-1, volumes, mollifier)
+ *   mass  lumped mass per vertex (diagonal of M)
+ *   lam, mu per-tet Lame parameters (tetElasticityAttr)
+ *   dbc_idx fixed Dirichlet vertices (DBC storage with zero displacement)
+ *   dHat2, kappa, kappa_max as returned by Initialize_OIPC
+ *     (FEM/Shell/DISCRETE_SHELL.h:555-577).
+ * Returns the instance id (>= 0) or -IDP_* on error. Before idp_commit only. */
+int idp_add_instance(idp_ctx* ctx, int V, const double* X, const double* X0, int T, const int32_t* tets,
+                     const double* mass, const double* lam, const double* mu, int nDBC, const int32_t* dbc_idx,
+                     double dHat2, double kappa, double kappa_max);
+
+/* Velocity v (3V); x_tilde = x + h v (IMPLICIT_EULER.h:195-216, no body force).
+ * MeshIO.Load_Velocity_X0 (Utils/MESHIO.h:986-1004) sets v = (target - x)/h. */
+int idp_set_velocity(idp_ctx* ctx, int inst, const double* v);
+/* Current positions (3V), e.g. a warm start between frames. */
+int idp_set_positions(idp_ctx* ctx, int inst, const double* X);
+
+/* Upload every instance to the device and build the static structures
+ * (surface primitives, BSR pattern). */
+int idp_commit(idp_ctx* ctx);
+
+/* One implicit-Euler step of every instance: Newton to convergence with
+ * PSD-projected Hessians, CCD-filtered backtracking line search and
+ * adaptive kappa. Replaces Advance_One_Step_IE_Hinge
+ * (FEM/Shell/DISCRETE_SHELL.h:1110 -> IMPLICIT_EULER.h:151-891).
+ * results: array of idp_result, one per instance (may be NULL). */
+int idp_advance(idp_ctx* ctx, idp_result* results);
+
+/* Read back positions X (3V), velocity v (3V) and kappa[3] of one instance. */
+int idp_get_state(idp_ctx* ctx, int inst, double* X, double* v, double* kappa3);
+
+/* Number of instances, and vertex/tet/surface counts of one instance. */
+int idp_instance_info(idp_ctx* ctx, int inst, int* V, int* T, int* n_nodes, int* n_edges, int* n_tris);
+
+/* Surface primitives of an instance, in the reference's order
+ * (Find_Surface_TriMesh, Utils/MESHIO.h:485-544, and
+ * Find_Surface_Primitives_And_Compute_Area, MESHIO.h:768-834). */
+int idp_get_surface(idp_ctx* ctx, int inst, int32_t* nodes, int32_t* edges, int32_t* tris);
+
+/* ---- sub-steps at caller-given positions (all for one instance) ---- */
+
+/* Incremental potential parts at X: h^2 * sum vol*Psi (NEOHOOKEAN.h:78-93),
+ * 0.5 (x-xt)^T M (x-xt) (INC_POTENTIAL.h:132-144) and the barrier sum over the
+ * constraint set built at X (IPC.h:742-941). Returns IDP_ERR_INVERTED if a
+ * tet has det F <= 0 (INC_POTENTIAL.h:98-108). */
+int idp_eval_energy(idp_ctx* ctx, int inst, const double* X, double* E_elastic, double* E_inertia,
+                    double* E_barrier);
+
+/* Gradient (3V) of the incremental potential at X (INC_POTENTIAL.h:154-275),
+ * with DBC rows zeroed (IMPLICIT_EULER.h:476-480). */
+int idp_eval_gradient(idp_ctx* ctx, int inst, const double* X, double* g);
+
+/* Constraint set at X (Compute_Constraint_Set, FEM/IPC.h:143-661): sign-tagged
+ * int4 records sorted lexicographically. *count receives the size; at most cap
+ * records are written (IDP_ERR_CAPACITY if cap is too small). */
+int idp_constraint_set(idp_ctx* ctx, int inst, const double* X, int cap, int32_t* cons, int* count);
+
+/* Largest intersection-free step alpha <= *alpha along dir from X
+ * (Compute_Intersection_Free_StepSize, FEM/IPC.h:1879-2244). */
+int idp_ccd_stepsize(idp_ctx* ctx, int inst, const double* X, const double* dir, double* alpha);
+
+/* Assembled system matrix at X (tets + barrier + mass, PSD-projected;
+ * Compute_IncPotential_Hessian, INC_POTENTIAL.h:277-395) times a vector:
+ * y = H x (3V). Uses the precision of the context's mode. */
+int idp_hessian_apply(idp_ctx* ctx, int inst, const double* X, const double* x, double* y);
+
+/* Solve H p = -g at X with the context's PCG (mixed or FP64); returns PCG
+ * iterations in *iters and the final relative residual in *relres. */
+int idp_newton_direction(idp_ctx* ctx, int inst, const double* X, double* p, int* iters, double* relres);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* IDP_GB300_H */

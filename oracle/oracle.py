@@ -1,0 +1,423 @@
+"""ORACLE — test infrastructure only. ctypes bindings to the CPU restatement
+(``oracle/libidp_oracle.so``) and the Newton driver restating
+``FEM/Shell/IMPLICIT_EULER.h:9-891`` for tet meshes with offset IPC contact.
+
+Only tests/, ``__graft_entry__.smoke()`` and the cpu_baseline leg of
+bench.py import this module; the product never does.
+
+Parity status: UNPINNED (the reference ships no tests or golden vectors and
+cannot be built here). The linear solve uses scipy's sparse LU in place of
+CHOLMOD (``Math/DIRECT_SOLVER.h:13-65``).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import os
+import subprocess
+import time
+from collections import deque
+from dataclasses import dataclass, field
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = os.path.join(_HERE, "libidp_oracle.so")
+_lib = None
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+_up = C.POINTER(C.c_ubyte)
+
+
+def build(force=False):
+    """Compile the oracle with its Makefile (g++ -ffp-contract=off)."""
+    if force or not os.path.exists(_LIB) or os.path.getmtime(_LIB) < max(
+        os.path.getmtime(os.path.join(_HERE, f)) for f in ("idp_oracle.cpp", "geom.hpp", "deriv.hpp")
+    ):
+        subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return _LIB
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(_LIB)
+        L.ora_surface.restype = C.c_int
+        L.ora_tet_energy.restype = C.c_int
+        L.ora_constraint_set.restype = C.c_int
+        L.ora_barrier_energy.restype = C.c_double
+        L.ora_min_dist2.restype = C.c_double
+        L.ora_ccd_stepsize.restype = C.c_int
+        L.ora_kappa_init.restype = C.c_double
+        L.ora_type_pt.restype = C.c_int
+        L.ora_type_ee.restype = C.c_int
+        L.ora_dist_pt_unclassified.restype = C.c_double
+        L.ora_dist_ee_unclassified.restype = C.c_double
+        _lib = L
+    return _lib
+
+
+def _d(a):
+    return a.ctypes.data_as(_dp)
+
+
+def _i(a):
+    return a.ctypes.data_as(_ip)
+
+
+def _u(a):
+    return a.ctypes.data_as(_up)
+
+
+def f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+# ---------------------------------------------------------------- wrappers
+def surface(X, tets):
+    X, tets = f64(X), i32(tets)
+    V, T = X.shape[0], tets.shape[0]
+    capT, capE = 4 * T, 6 * T
+    tris = np.zeros((capT, 3), np.int32)
+    edges = np.zeros((capE, 2), np.int32)
+    nodes = np.zeros(V, np.int32)
+    A_t, A_e, A_n = np.zeros(capT), np.zeros(capE), np.zeros(V)
+    nT, nE, nN = C.c_int(), C.c_int(), C.c_int()
+    rc = lib().ora_surface(V, T, _i(tets), _d(X), capT, capE, C.byref(nT), _i(tris), C.byref(nE), _i(edges),
+                           C.byref(nN), _i(nodes), _d(A_t), _d(A_e), _d(A_n))
+    assert rc == 0
+    return dict(tris=tris[: nT.value].copy(), edges=edges[: nE.value].copy(), nodes=nodes[: nN.value].copy(),
+                tri_area=A_t[: nT.value].copy(), edge_area=A_e[: nE.value].copy(), node_area=A_n[: nN.value].copy())
+
+
+def tet_rest(X, tets):
+    X, tets = f64(X), i32(tets)
+    T = tets.shape[0]
+    IB, vol = np.zeros((T, 3, 3)), np.zeros(T)
+    lib().ora_tet_rest(T, _i(tets), _d(X), _d(IB), _d(vol))
+    return IB, vol
+
+
+def tet_energy(X, tets, IB, vol, lam, mu, w):
+    E = C.c_double()
+    ok = lib().ora_tet_energy(tets.shape[0], _i(tets), _d(f64(X)), _d(IB), _d(vol), _d(lam), _d(mu), C.c_double(w), C.byref(E))
+    return (E.value if ok else None)
+
+
+def tet_gradient(X, tets, IB, vol, lam, mu, w):
+    g = np.zeros(X.size)
+    lib().ora_tet_gradient(X.shape[0], tets.shape[0], _i(tets), _d(f64(X)), _d(IB), _d(vol), _d(lam), _d(mu), C.c_double(w), _d(g))
+    return g
+
+
+def tet_hessian(X, tets, IB, vol, lam, mu, w, project=True):
+    H = np.zeros((tets.shape[0], 12, 12))
+    lib().ora_tet_hessian(tets.shape[0], _i(tets), _d(f64(X)), _d(IB), _d(vol), _d(lam), _d(mu), C.c_double(w), int(project), _d(H))
+    return H
+
+
+def constraint_set(X, X0, surf, dbc, dHat2, thickness=0.0):
+    X, X0 = f64(X), f64(X0)
+    cap = max(1024, 8 * (surf["nodes"].size + surf["edges"].shape[0]))
+    while True:
+        cons = np.zeros((cap, 4), np.int32)
+        info = np.zeros((cap, 2))
+        n = lib().ora_constraint_set(X.shape[0], _d(X), _d(X0), surf["nodes"].size, _i(surf["nodes"]),
+                                     surf["edges"].shape[0], _i(surf["edges"]), surf["tris"].shape[0], _i(surf["tris"]),
+                                     _u(dbc), C.c_double(dHat2), C.c_double(thickness), cap, _i(cons), _d(info))
+        if n >= 0:
+            return cons[:n].copy(), info[:n].copy()
+        cap = -n
+
+
+def barrier_energy(cons, info, X, X0, dHat2, kappa, thickness=0.0):
+    if cons.shape[0] == 0:
+        return 0.0
+    return lib().ora_barrier_energy(cons.shape[0], _i(cons), _d(info), _d(f64(X)), _d(f64(X0)), C.c_double(dHat2),
+                                    C.c_double(kappa), C.c_double(thickness))
+
+
+def barrier_gradient(cons, info, X, X0, dHat2, kappa, thickness=0.0):
+    g = np.zeros(X.size)
+    if cons.shape[0]:
+        lib().ora_barrier_gradient(cons.shape[0], _i(cons), _d(info), _d(f64(X)), _d(f64(X0)), C.c_double(dHat2),
+                                   C.c_double(kappa), C.c_double(thickness), _d(g))
+    return g
+
+
+def barrier_hessian(cons, info, X, X0, dHat2, kappa, thickness=0.0, project=True):
+    n = cons.shape[0]
+    verts = np.zeros((n, 4), np.int32)
+    H = np.zeros((n, 144))
+    if n:
+        lib().ora_barrier_hessian(n, _i(cons), _d(info), _d(f64(X)), _d(f64(X0)), C.c_double(dHat2), C.c_double(kappa),
+                                  C.c_double(thickness), int(project), _i(verts), _d(H))
+    return verts, H
+
+
+def min_dist2(cons, X, thickness=0.0):
+    d2 = np.zeros(cons.shape[0])
+    if cons.shape[0] == 0:
+        return math.inf, d2
+    m = lib().ora_min_dist2(cons.shape[0], _i(cons), _d(f64(X)), C.c_double(thickness), _d(d2))
+    return m, d2
+
+
+def ccd_stepsize(X, dirn, surf, dbc, alpha=1.0, thickness=0.0):
+    a = C.c_double(alpha)
+    rc = lib().ora_ccd_stepsize(surf["nodes"].size, _i(surf["nodes"]), surf["edges"].shape[0], _i(surf["edges"]),
+                                surf["tris"].shape[0], _i(surf["tris"]), _u(dbc), _d(f64(X)), _d(f64(dirn)),
+                                C.c_double(thickness), C.byref(a))
+    return a.value, rc
+
+
+def kappa_init(mean_mass_diag, dHat2, stiff_mult=1.0):
+    km = C.c_double()
+    k = lib().ora_kappa_init(C.c_double(mean_mass_diag), C.c_double(dHat2), C.c_double(stiff_mult), C.byref(km))
+    return k, km.value
+
+
+def dist_derivs(kind, x):
+    x = f64(x).reshape(-1)
+    xx = np.zeros(12)
+    xx[: x.size] = x
+    d = C.c_double()
+    g, H = np.zeros(12), np.zeros(144)
+    lib().ora_dist_derivs(kind, _d(xx), C.byref(d), _d(g), _d(H))
+    n = {0: 6, 1: 9}.get(kind, 12)
+    return d.value, g[:n].copy(), H[: n * n].reshape(n, n).copy()
+
+
+def make_pd(A):
+    A = f64(A).copy()
+    lib().ora_make_pd(A.shape[0], _d(A))
+    return A
+
+
+# ---------------------------------------------------------------- Newton step
+@dataclass
+class Problem:
+    """One tet mesh with everything Advance_One_Step_IE_Discrete_Shell reads
+    for the tet + offset-IPC configuration."""
+    X: np.ndarray            # (V,3) current positions (mutated)
+    X0: np.ndarray           # (V,3) rest positions (mollifier threshold, IB)
+    tets: np.ndarray         # (T,4) int32
+    mass: np.ndarray         # (V,) lumped mass
+    lam: np.ndarray          # (T,)
+    mu: np.ndarray           # (T,)
+    h: float
+    dHat2: float
+    kappa: list              # [kappa, kappa_max, 0]
+    v: np.ndarray            # (V,3) velocity (mutated)
+    dbc: np.ndarray = None   # (V,) uint8 fixed-DBC mask
+    thickness: float = 0.0
+    tol: float = 1e-3
+    max_iters: int = 1000
+    IB: np.ndarray = None
+    vol: np.ndarray = None
+    surf: dict = None
+    log: list = field(default_factory=list)
+
+    def __post_init__(self):
+        self.X = f64(self.X).copy()
+        self.X0 = f64(self.X0)
+        self.tets = i32(self.tets)
+        if self.dbc is None:
+            self.dbc = np.zeros(self.X.shape[0], np.uint8)
+        if self.IB is None:
+            self.IB, self.vol = tet_rest(self.X0, self.tets)
+
+
+def _energy(pb, X, Xtilde, with_barrier, cons, info):
+    """Compute_IncPotential (INC_POTENTIAL.h:15-152); None when a tet inverts."""
+    h2 = pb.h * pb.h
+    E = tet_energy(X, pb.tets, pb.IB, pb.vol, pb.lam, pb.mu, h2)
+    if E is None:
+        return None
+    dx = (X - Xtilde)
+    E += 0.5 * float(np.dot((pb.mass[:, None] * dx).reshape(-1), dx.reshape(-1)))
+    if with_barrier:
+        E += barrier_energy(cons, info, X, pb.X0, pb.dHat2, pb.kappa[0], pb.thickness)
+    return E
+
+
+def _gradient(pb, X, Xtilde, cons, info):
+    """Compute_IncPotential_Gradient (INC_POTENTIAL.h:154-275)."""
+    h2 = pb.h * pb.h
+    g = tet_gradient(X, pb.tets, pb.IB, pb.vol, pb.lam, pb.mu, h2)
+    g += (pb.mass[:, None] * (X - Xtilde)).reshape(-1)
+    g += barrier_gradient(cons, info, X, pb.X0, pb.dHat2, pb.kappa[0], pb.thickness)
+    return g
+
+
+def _hessian(pb, X, cons, info):
+    """Compute_IncPotential_Hessian (INC_POTENTIAL.h:277-395) as scipy CSR."""
+    import scipy.sparse as sp
+
+    n = X.size
+    h2 = pb.h * pb.h
+    He = tet_hessian(X, pb.tets, pb.IB, pb.vol, pb.lam, pb.mu, h2, True)
+    dofs = (3 * pb.tets[:, :, None] + np.arange(3)).reshape(-1, 12)
+    rows = np.repeat(dofs[:, :, None], 12, axis=2).reshape(-1)
+    cols = np.repeat(dofs[:, None, :], 12, axis=1).reshape(-1)
+    vals = He.reshape(-1)
+    R, Cc, Vv = [rows], [cols], [vals]
+    if cons.shape[0]:
+        verts, Hb = barrier_hessian(cons, info, X, pb.X0, pb.dHat2, pb.kappa[0], pb.thickness, True)
+        for nv in (2, 3, 4):
+            sel = (verts >= 0).sum(1) == nv
+            if not sel.any():
+                continue
+            vd = (3 * verts[sel, :nv, None] + np.arange(3)).reshape(-1, 3 * nv)
+            k = 3 * nv
+            R.append(np.repeat(vd[:, :, None], k, axis=2).reshape(-1))
+            Cc.append(np.repeat(vd[:, None, :], k, axis=1).reshape(-1))
+            Vv.append(Hb[sel, : k * k].reshape(-1))
+    R.append(np.arange(n))
+    Cc.append(np.arange(n))
+    Vv.append(np.repeat(pb.mass, 3))
+    H = sp.coo_matrix((np.concatenate(Vv), (np.concatenate(R), np.concatenate(Cc))), shape=(n, n)).tocsr()
+    # Project_DBC (Math/CSR_MATRIX.h:130-141): DBC rows/cols -> identity
+    if pb.dbc.any():
+        m = np.repeat(pb.dbc.astype(bool), 3)
+        keep = sp.diags((~m).astype(float))
+        H = keep @ H @ keep + sp.diags(m.astype(float))
+    return H.tocsr()
+
+
+def advance_one_step(pb: Problem, Xtilde=None, verbose=False):
+    """Advance_One_Step_IE_Discrete_Shell<double,3,false,false,false>
+    (FEM/Shell/IMPLICIT_EULER.h:151-891) for tets with fixed DBC, no friction.
+    Returns the Newton iteration count; pb.X and pb.v are updated."""
+    import scipy.sparse.linalg as spla
+
+    h = pb.h
+    Xn = pb.X.copy()
+    if Xtilde is None:
+        Xtilde = Xn + h * pb.v            # IMPLICIT_EULER.h:195-216 (no body force)
+    if pb.surf is None:
+        pb.surf = surface(pb.X0, pb.tets)  # IMPLICIT_EULER.h:235-241
+    surf, dbc = pb.surf, pb.dbc
+    nDBC = int(dbc.sum())
+    X = pb.X
+    cons, info = constraint_set(X, pb.X0, surf, dbc, pb.dHat2, pb.thickness)
+    Eprev = _energy(pb, X, Xtilde, True, cons, info)
+    res_record = deque()
+    it = 0
+    use_gd = False
+    cons_prev, dist2_prev = np.zeros((0, 4), np.int32), np.zeros(0)
+    stats = dict(ls_trials=0, ccd_calls=0, alphas=[], t_solve=0.0)
+    while True:
+        g = _gradient(pb, X, Xtilde, cons, info)
+        if nDBC:
+            g.reshape(-1, 3)[dbc.astype(bool)] = 0
+        rhs = -g
+        if not use_gd:
+            Hm = _hessian(pb, X, cons, info)
+            t0 = time.perf_counter()
+            try:
+                sol = spla.spsolve(Hm.tocsc(), rhs, permc_spec="MMD_AT_PLUS_A")
+                ok = np.all(np.isfinite(sol))
+            except Exception:
+                ok = False
+            stats["t_solve"] += time.perf_counter() - t0
+            if not ok:
+                use_gd = True
+                sol = rhs.copy()
+        else:
+            sol = rhs.copy()
+        # ---- Line_Search (IMPLICIT_EULER.h:9-149)
+        Xprev = X.copy()
+        p = sol.reshape(-1, 3)
+        alpha = 1.0
+        while True:
+            Xt = Xprev + alpha * p
+            if _energy(pb, Xt, Xtilde, False, cons, info) is not None:
+                break
+            alpha /= 2.0
+        stats["ccd_calls"] += 1
+        alpha, rc = ccd_stepsize(Xprev, sol, surf, dbc, alpha, pb.thickness)
+        if rc < 0:
+            raise RuntimeError("zero CCD step")
+        feasible_alpha = alpha
+        E = None
+        while True:
+            stats["ls_trials"] += 1
+            Xt = Xprev + alpha * p
+            E = _energy(pb, Xt, Xtilde, False, cons, info)
+            valid = E is not None
+            if valid:
+                cons, info = constraint_set(Xt, pb.X0, surf, dbc, pb.dHat2, pb.thickness)
+                if cons.shape[0]:
+                    md, _ = min_dist2(cons, Xt, pb.thickness)
+                    if md <= 0:
+                        alpha /= 2
+                        E = Eprev + 1
+                        continue
+                E = _energy(pb, Xt, Xtilde, True, cons, info)
+            alpha /= 2.0
+            if valid and not (E > Eprev):
+                break
+        X[:] = Xt
+        Eprev = E
+        stats["alphas"].append(alpha * 2)
+        # ---- kappa adaptation (IMPLICIT_EULER.h:566-595)
+        if cons_prev.shape[0]:
+            _, cur = min_dist2(cons_prev, X, pb.thickness)
+            upd = bool(np.any((dist2_prev < 1e-18) & (cur < dist2_prev)))
+            if upd and pb.kappa[0] < pb.kappa[1]:
+                pb.kappa[0] *= 2
+                Eprev = _energy(pb, X, Xtilde, True, cons, info)
+        dist2 = min_dist2(cons, X, pb.thickness)[1] if cons.shape[0] else np.zeros(0)
+        cons_prev, dist2_prev = cons.copy(), dist2
+        # ---- stopping criterion (IMPLICIT_EULER.h:647-676, 759, 855)
+        n = sol.size // 3
+        L2 = math.sqrt(float(np.dot(sol, sol)) / (n - nDBC)) / h
+        it += 1
+        res_record.append(L2)
+        if len(res_record) > 3:
+            res_record.popleft()
+        L2m = max(res_record)
+        if use_gd:
+            L2m = pb.tol * 10
+        if alpha * 2 < 1e-8 and feasible_alpha > 1e-8:
+            use_gd = True
+        else:
+            use_gd = False
+        pb.log.append(dict(it=it, E=Eprev, res=L2, alpha=alpha * 2, ncons=int(cons.shape[0]), kappa=pb.kappa[0]))
+        if verbose:
+            print(f"it {it} E {Eprev:.12e} res {L2:.3e} alpha {alpha*2:.3e} C {cons.shape[0]} kappa {pb.kappa[0]:.3e}")
+        if (len(res_record) == 3 and L2m <= pb.tol) or it >= pb.max_iters:
+            break
+    pb.v = (X - Xn) / h                     # IMPLICIT_EULER.h:882-888
+    pb.last_stats = stats
+    pb.last_energy = Eprev
+    return it
+
+
+def make_bar_problem(nx=6, ny=6, nz=24, size=(1.0, 1.0, 4.0), angle=2.2 * math.pi, seed=0, E=1e4, nu=0.3,
+                     density=1000.0, h=0.1, tol=1e-3, dhat_rel=1e-3):
+    """Config-0 style problem: jittered bar, bent self-intersecting target,
+    x_tilde = target (v = (target - x)/h as MeshIO.Load_Velocity_X0)."""
+    import sys
+    sys.path.insert(0, os.path.dirname(_HERE))
+    from idp_gb300 import meshgen
+
+    X, tets = meshgen.bar(nx, ny, nz, size=size, seed=seed)
+    target = meshgen.bend_target(X, angle=angle, size=size)
+    mass = meshgen.lumped_mass(X, tets, density)
+    lam, mu = meshgen.lame(E, nu)
+    T = tets.shape[0]
+    diag = float(np.linalg.norm(X.max(0) - X.min(0)))
+    dHat2 = (dhat_rel * diag) ** 2
+    k, kmax = kappa_init(float(mass.mean()), dHat2)
+    pb = Problem(X=X, X0=X.copy(), tets=tets, mass=mass, lam=np.full(T, lam), mu=np.full(T, mu), h=h, dHat2=dHat2,
+                 kappa=[k, kmax, 0.0], v=(target - X) / h, tol=tol)
+    pb.target = target
+    return pb
