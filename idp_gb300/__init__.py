@@ -34,7 +34,7 @@ EXPORTS = [
     "idp_default_params", "idp_create", "idp_destroy", "idp_status_str", "idp_add_instance", "idp_set_velocity",
     "idp_set_positions", "idp_commit", "idp_advance", "idp_get_state", "idp_instance_info", "idp_get_surface",
     "idp_eval_energy", "idp_eval_gradient", "idp_constraint_set", "idp_ccd_stepsize", "idp_hessian_apply",
-    "idp_newton_direction",
+    "idp_newton_direction", "idp_get_stats", "idp_save_state", "idp_restore_state",
 ]
 
 
@@ -47,7 +47,16 @@ class Params(C.Structure):
 class Result(C.Structure):
     _fields_ = [("status", C.c_int), ("newton_iters", C.c_int), ("pcg_iters", C.c_int), ("ls_trials", C.c_int),
                 ("num_constraints", C.c_int), ("energy", C.c_double), ("kappa", C.c_double),
-                ("residual", C.c_double), ("min_alpha", C.c_double)]
+                ("residual", C.c_double), ("min_alpha", C.c_double), ("latency_ms", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class Stats(C.Structure):
+    _fields_ = [("pcg_ms", C.c_double), ("pcg_bytes", C.c_double), ("pcg_iters", C.c_longlong),
+                ("pcg_launches", C.c_int), ("tet_ms", C.c_double), ("contact_ms", C.c_double), ("ccd_ms", C.c_double),
+                ("total_ms", C.c_double), ("kernel_launches", C.c_longlong)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -94,6 +103,9 @@ def load(path: str | None = None):
     L.idp_ccd_stepsize.argtypes = [C.c_void_p, C.c_int, _dp, _dp, _dp]
     L.idp_hessian_apply.argtypes = [C.c_void_p, C.c_int, _dp, _dp, _dp]
     L.idp_newton_direction.argtypes = [C.c_void_p, C.c_int, _dp, _dp, C.POINTER(C.c_int), _dp]
+    L.idp_get_stats.argtypes = [C.c_void_p, C.POINTER(Stats)]
+    L.idp_save_state.argtypes = [C.c_void_p]
+    L.idp_restore_state.argtypes = [C.c_void_p]
     _lib = L
     return L
 
@@ -191,6 +203,28 @@ class Context:
         if check:
             self._check(rc, "idp_advance", ok=(IDP_OK, IDP_WARN_ITER_CAP))
         return rc, out
+
+    def save_state(self):
+        self._check(load().idp_save_state(self._h), "idp_save_state")
+
+    def restore_state(self):
+        self._check(load().idp_restore_state(self._h), "idp_restore_state")
+
+    def set_positions_ptr(self, i, ptr):
+        """Upload positions from a raw host pointer (e.g. pinned memory)."""
+        self._check(load().idp_set_positions(self._h, i, C.cast(ptr, _dp)), "idp_set_positions")
+
+    def set_velocity_ptr(self, i, ptr):
+        self._check(load().idp_set_velocity(self._h, i, C.cast(ptr, _dp)), "idp_set_velocity")
+
+    def state_ptr(self, i, x_ptr):
+        """Read positions of instance i into a raw host pointer."""
+        self._check(load().idp_get_state(self._h, i, C.cast(x_ptr, _dp), None, None), "idp_get_state")
+
+    def stats(self):
+        st = Stats()
+        self._check(load().idp_get_stats(self._h, C.byref(st)), "idp_get_stats")
+        return st.as_dict()
 
     def state(self, i):
         V = self._V[i]

@@ -498,9 +498,9 @@ int barrier_energy(Arena& A, Work& W, const double* X, const ContactSet& cs, dou
     if (cs.C <= 0) return IDP_OK;
     if (W[W_MISC].ensure(sizeof(double) * (cs.C + 1))) return IDP_ERR_CUDA;
     double* val = W[W_MISC].as<double>();
-    k_barrier_energy<<<grid_for(cs.C), kBlock, 0, s>>>(cs.C, W[W_CONS].as<int4>(), W[W_CONS_INST].as<int>(), A.active, X,
-                                                       A.X0, A.dHat2, A.kappa, A.thickness, val, inst_bad);
-    k_segment_sum<<<A.nI, kBlock, 0, s>>>(A.nI, cs.d_off, val, inst_E, 1);
+    (::idp::count_launch(), k_barrier_energy<<<grid_for(cs.C), kBlock, 0, s>>>(cs.C, W[W_CONS].as<int4>(), W[W_CONS_INST].as<int>(), A.active, X,
+                                                       A.X0, A.dHat2, A.kappa, A.thickness, val, inst_bad));
+    (::idp::count_launch(), k_segment_sum<<<A.nI, kBlock, 0, s>>>(A.nI, cs.d_off, val, inst_E, 1));
     return cudaGetLastError() == cudaSuccess ? IDP_OK : IDP_ERR_CUDA;
 }
 
@@ -517,14 +517,14 @@ static int barrier_gh(Arena& A, Work& W, const double* X, const ContactSet& cs, 
     if (hess_mode >= 0 && W[W_BH].ensure(el * 90 * Ca)) return IDP_ERR_CUDA;
     if (C > 0) {
         if (hess_mode == 1)
-            k_barrier_gh<double><<<grid_for(C, 64), 64, 0, s>>>(C, cons, cinst, A.active, X, A.X0, A.dHat2, A.kappa,
-                                                                 A.thickness, W[W_BG].as<double>(), W[W_BH].as<double>());
+            (::idp::count_launch(), k_barrier_gh<double><<<grid_for(C, 64), 64, 0, s>>>(C, cons, cinst, A.active, X, A.X0, A.dHat2, A.kappa,
+                                                                 A.thickness, W[W_BG].as<double>(), W[W_BH].as<double>()));
         else if (hess_mode == 0)
-            k_barrier_gh<float><<<grid_for(C, 64), 64, 0, s>>>(C, cons, cinst, A.active, X, A.X0, A.dHat2, A.kappa,
-                                                                A.thickness, W[W_BG].as<double>(), W[W_BH].as<float>());
+            (::idp::count_launch(), k_barrier_gh<float><<<grid_for(C, 64), 64, 0, s>>>(C, cons, cinst, A.active, X, A.X0, A.dHat2, A.kappa,
+                                                                A.thickness, W[W_BG].as<double>(), W[W_BH].as<float>()));
         else
-            k_barrier_gh<float><<<grid_for(C, 64), 64, 0, s>>>(C, cons, cinst, A.active, X, A.X0, A.dHat2, A.kappa,
-                                                                A.thickness, W[W_BG].as<double>(), nullptr);
+            (::idp::count_launch(), k_barrier_gh<float><<<grid_for(C, 64), 64, 0, s>>>(C, cons, cinst, A.active, X, A.X0, A.dHat2, A.kappa,
+                                                                A.thickness, W[W_BG].as<double>(), nullptr));
     }
     // gradient scatter: sort (vertex, constraint*4+slot) pairs, sum runs in order
     if (g && C > 0) {
@@ -532,13 +532,13 @@ static int barrier_gh(Arena& A, Work& W, const double* X, const ContactSet& cs, 
         if (W[W_GENT_KEY].ensure(8 * n) || W[W_GENT_VAL].ensure(4 * n) || W[W_GENT_KEY2].ensure(8 * n) ||
             W[W_GENT_VAL2].ensure(4 * n) || W[W_SCRATCH].ensure(radix_sort_scratch_bytes(n) + 64))
             return IDP_ERR_CUDA;
-        k_grad_entries<<<grid_for(C), kBlock, 0, s>>>(C, cons, cinst, A.active, A.V, W[W_GENT_KEY].as<uint64_t>(),
-                                                      W[W_GENT_VAL].as<uint32_t>());
+        (::idp::count_launch(), k_grad_entries<<<grid_for(C), kBlock, 0, s>>>(C, cons, cinst, A.active, A.V, W[W_GENT_KEY].as<uint64_t>(),
+                                                      W[W_GENT_VAL].as<uint32_t>()));
         if (radix_sort_pairs(W[W_GENT_KEY].as<uint64_t>(), W[W_GENT_VAL].as<uint32_t>(), W[W_GENT_KEY2].as<uint64_t>(),
                              W[W_GENT_VAL2].as<uint32_t>(), n, bits_for((uint64_t)A.V), W[W_SCRATCH].p, s) != cudaSuccess)
             return IDP_ERR_CUDA;
-        k_grad_gather<<<grid_for(n), kBlock, 0, s>>>(n, A.V, W[W_GENT_KEY].as<uint64_t>(), W[W_GENT_VAL].as<uint32_t>(),
-                                                     W[W_BG].as<double>(), g);
+        (::idp::count_launch(), k_grad_gather<<<grid_for(n), kBlock, 0, s>>>(n, A.V, W[W_GENT_KEY].as<uint64_t>(), W[W_GENT_VAL].as<uint32_t>(),
+                                                     W[W_BG].as<double>(), g));
     }
     if (hess_mode < 0) return cudaGetLastError() == cudaSuccess ? IDP_OK : IDP_ERR_CUDA;
     // Hessian tail: sort (row*V+col) keys, sum equal keys in order
@@ -554,7 +554,7 @@ static int barrier_gh(Arena& A, Work& W, const double* X, const ContactSet& cs, 
     if (n > 0) {
         uint64_t* keys = W[W_GENT_KEY].as<uint64_t>();
         uint32_t* vals = W[W_GENT_VAL].as<uint32_t>();
-        k_hess_entries<<<grid_for(C), kBlock, 0, s>>>(C, cons, cinst, A.active, A.V, keys, vals);
+        (::idp::count_launch(), k_hess_entries<<<grid_for(C), kBlock, 0, s>>>(C, cons, cinst, A.active, A.V, keys, vals));
         uint64_t marker = (uint64_t)A.V * (uint64_t)A.V;
         int bits = bits_for(marker);
         if (radix_sort_pairs(keys, vals, W[W_GENT_KEY2].as<uint64_t>(), W[W_GENT_VAL2].as<uint32_t>(), n, bits,
@@ -562,7 +562,7 @@ static int barrier_gh(Arena& A, Work& W, const double* X, const ContactSet& cs, 
             return IDP_ERR_CUDA;
         uint32_t* head = W[W_GENT_HEAD].as<uint32_t>();
         uint32_t* pos = head + na + 1;
-        k_heads<<<grid_for(n), kBlock, 0, s>>>(n, marker, keys, head);
+        (::idp::count_launch(), k_heads<<<grid_for(n), kBlock, 0, s>>>(n, marker, keys, head));
         if (scan_exclusive(head, pos, n, pos + n, W[W_SCRATCH].p, s) != cudaSuccess) return IDP_ERR_CUDA;
         uint32_t hnb = 0;
         IDP_CUDA_TRY(cudaMemcpyAsync(&hnb, pos + n, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
@@ -571,12 +571,12 @@ static int barrier_gh(Arena& A, Work& W, const double* X, const ContactSet& cs, 
         int* tcol = W[W_TAIL_COL].as<int>();
         int* trow = tcol + na;
         if (hess_mode == 1)
-            k_tail_blocks<double><<<grid_for(n), kBlock, 0, s>>>(n, A.V, keys, vals, head, pos, W[W_BH].as<double>(), tcol,
-                                                                 trow, W[W_TAIL_VAL].as<double>());
+            (::idp::count_launch(), k_tail_blocks<double><<<grid_for(n), kBlock, 0, s>>>(n, A.V, keys, vals, head, pos, W[W_BH].as<double>(), tcol,
+                                                                 trow, W[W_TAIL_VAL].as<double>()));
         else
-            k_tail_blocks<float><<<grid_for(n), kBlock, 0, s>>>(n, A.V, keys, vals, head, pos, W[W_BH].as<float>(), tcol,
-                                                                trow, W[W_TAIL_VAL].as<float>());
-        k_tail_rowptr<<<grid_for(A.V + 1), kBlock, 0, s>>>(A.V, nb, trow, W[W_TAIL_ROWPTR].as<int>());
+            (::idp::count_launch(), k_tail_blocks<float><<<grid_for(n), kBlock, 0, s>>>(n, A.V, keys, vals, head, pos, W[W_BH].as<float>(), tcol,
+                                                                trow, W[W_TAIL_VAL].as<float>()));
+        (::idp::count_launch(), k_tail_rowptr<<<grid_for(A.V + 1), kBlock, 0, s>>>(A.V, nb, trow, W[W_TAIL_ROWPTR].as<int>()));
     } else {
         IDP_CUDA_TRY(cudaMemsetAsync(W[W_TAIL_ROWPTR].p, 0, sizeof(int) * (A.V + 1), s));
     }

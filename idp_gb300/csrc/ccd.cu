@@ -226,6 +226,37 @@ struct CCand {
     int a, b;
 };
 
+// candidate search runs on a grid K reference voxels wide; the reference's
+// test (integer voxel boxes overlap) is applied to every pair it returns
+constexpr int CCD_COARSE = 4;
+
+__global__ void k_coarse_boxes(long n, const BoxI* __restrict__ in, BoxI* __restrict__ out) {
+    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    BoxI b = in[i], c;
+    for (int d = 0; d < 3; ++d) {
+        c.lo[d] = b.lo[d] >= 0 ? b.lo[d] / CCD_COARSE : -1;
+        c.hi[d] = b.hi[d] >= 0 ? b.hi[d] / CCD_COARSE : -1;
+    }
+    out[i] = c;
+}
+
+__global__ void k_coarse_grid(int nI, const GridP* __restrict__ gp, GridP* __restrict__ gc) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nI) return;
+    GridP g = gp[i];
+    for (int d = 0; d < 3; ++d) g.n[d] = g.n[d] / CCD_COARSE + 1;
+    g.s1 = (long)g.n[0] + 1;
+    g.s2 = g.s1 * ((long)g.n[1] + 1);
+    gc[i] = g;
+}
+
+__device__ __forceinline__ bool boxes_overlap(const BoxI& a, const BoxI& b) {
+    for (int d = 0; d < 3; ++d)
+        if (a.lo[d] > b.hi[d] || b.lo[d] > a.hi[d]) return false;
+    return true;
+}
+
 __device__ __forceinline__ bool swept_far(const double* lo_a, const double* hi_a, const double* lo_b,
                                           const double* hi_b, double dist) {
     for (int d = 0; d < 3; ++d)
@@ -233,135 +264,113 @@ __device__ __forceinline__ bool swept_far(const double* lo_a, const double* hi_a
     return false;
 }
 
+// warp per surface node: triangles whose voxel boxes overlap the node's
+// swept voxel box (Query_Point_For_Primitives, SPATIAL_HASH.h:624-647), then
+// the exclusions and swept-AABB test of IPC.h:1980-2006
 __global__ void k_ccd_query_pt(long nN, const int* __restrict__ nodes, const int* __restrict__ ninst,
                                const unsigned char* __restrict__ active, const double* __restrict__ X,
                                const double* __restrict__ dir, const unsigned char* __restrict__ dbc,
                                const int* __restrict__ tris, const BoxI* __restrict__ nbox,
-                               const BoxI* __restrict__ tbox, const GridP* __restrict__ gp,
+                               const BoxI* __restrict__ tbox, const BoxI* __restrict__ nboxc,
+                               const BoxI* __restrict__ tboxc, const GridP* __restrict__ gp,
                                const double* __restrict__ thick, const uint64_t* __restrict__ ckey,
                                const uint32_t* __restrict__ cstart, int ncell, const uint32_t* __restrict__ entries,
                                CCand* __restrict__ out, unsigned int* counter, long cap) {
-    long s = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    bool more = s < nN;
-    int inst = 0, vI = 0;
-    Cursor q;
-    GridP g;
-    double plo[3], phi[3], th = 0;
-    if (more) {
-        inst = ninst[s];
-        more = active[inst] != 0;
+    long s = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (s >= nN) return;
+    int inst = ninst[s];
+    if (!active[inst]) return;
+    int vI = nodes[s];
+    GridP g = gp[inst];
+    double th = thick[inst];
+    double plo[3], phi[3];
+    for (int d = 0; d < 3; ++d) {
+        double p = X[3 * vI + d], pe = p + dir[3 * vI + d];
+        plo[d] = fmin(p, pe);
+        phi[d] = fmax(p, pe);
     }
-    if (more) {
-        vI = nodes[s];
-        g = gp[inst];
-        th = thick[inst];
-        cursor_init(q, nbox[s]);
-        for (int d = 0; d < 3; ++d) {
-            double p = X[3 * vI + d], pe = p + dir[3 * vI + d];
-            plo[d] = fmin(p, pe);
-            phi[d] = fmax(p, pe);
-        }
-    }
-    while (__any_sync(0xffffffffu, more)) {
-        bool emit = false;
-        CCand c = {0, 0};
-        if (more) {
-            uint32_t e;
-            if (cursor_next(q, inst, g, ckey, cstart, ncell, e)) {
-                int f = (int)entries[e];
-                if (first_shared_cell(q, tbox[f])) {
-                    int t0 = tris[3 * f], t1 = tris[3 * f + 1], t2 = tris[3 * f + 2];
-                    if (!(vI == t0 || vI == t1 || vI == t2) && !(dbc[vI] && dbc[t0] && dbc[t1] && dbc[t2])) {
-                        double tlo[3], thi[3];
-                        int tv[3] = {t0, t1, t2};
-                        for (int d = 0; d < 3; ++d) {
-                            double mn = X[3 * t0 + d], mx = mn;
-                            for (int k = 0; k < 3; ++k) {
-                                double a = X[3 * tv[k] + d], b = a + dir[3 * tv[k] + d];
-                                mn = fmin(mn, fmin(a, b));
-                                mx = fmax(mx, fmax(a, b));
-                            }
-                            tlo[d] = mn;
-                            thi[d] = mx;
-                        }
-                        if (!swept_far(plo, phi, tlo, thi, th)) { emit = true; c = {(int)s, f}; }
-                    }
-                }
-            } else {
-                more = false;
-            }
-        }
-        warp_emit(emit, c, out, counter, cap);
-    }
+    const BoxI qc = nboxc[s], qx = nbox[s];
+    const bool pdbc = dbc[vI] != 0;
+    warp_walk_emit(qc, inst, g, ckey, cstart, ncell, entries, out, counter, cap,
+                   [&](uint32_t ent, int cx, int cy, int cz, CCand& c) -> bool {
+                       int f = (int)ent;
+                       if (!is_first_shared(qc, tboxc[f], cx, cy, cz) || !boxes_overlap(qx, tbox[f])) return false;
+                       int t0 = tris[3 * f], t1 = tris[3 * f + 1], t2 = tris[3 * f + 2];
+                       if (vI == t0 || vI == t1 || vI == t2) return false;
+                       if (pdbc && dbc[t0] && dbc[t1] && dbc[t2]) return false;
+                       double tlo[3], thi[3];
+                       const int tv[3] = {t0, t1, t2};
+                       for (int d = 0; d < 3; ++d) {
+                           double mn = X[3 * t0 + d], mx = mn;
+                           for (int k = 0; k < 3; ++k) {
+                               double a = X[3 * tv[k] + d], b = a + dir[3 * tv[k] + d];
+                               mn = fmin(mn, fmin(a, b));
+                               mx = fmax(mx, fmax(a, b));
+                           }
+                           tlo[d] = mn;
+                           thi[d] = mx;
+                       }
+                       if (swept_far(plo, phi, tlo, thi, th)) return false;
+                       c = {(int)s, f};
+                       return true;
+                   });
 }
 
+// warp per surface edge: edges eJ > eI with overlapping voxel boxes
+// (SPATIAL_HASH.h:650-662), exclusions and swept-AABB test of IPC.h:2193-2230
 __global__ void k_ccd_query_ee(long nE, const int2* __restrict__ edges, const int* __restrict__ einst,
                                const unsigned char* __restrict__ active, const double* __restrict__ X,
                                const double* __restrict__ dir, const unsigned char* __restrict__ dbc,
-                               const BoxI* __restrict__ ebox, const GridP* __restrict__ gp,
-                               const double* __restrict__ thick, const uint64_t* __restrict__ ckey,
-                               const uint32_t* __restrict__ cstart, int ncell, const uint32_t* __restrict__ entries,
-                               CCand* __restrict__ out, unsigned int* counter, long cap) {
-    long eI = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    bool more = eI < nE;
-    int inst = 0;
-    int2 mi = {0, 0};
-    Cursor q;
-    GridP g;
-    double alo[3], ahi[3], th = 0;
-    if (more) {
-        inst = einst[eI];
-        more = active[inst] != 0;
-    }
-    if (more) {
-        mi = edges[eI];
-        g = gp[inst];
-        th = thick[inst];
-        cursor_init(q, ebox[eI]);
-        int av[2] = {mi.x, mi.y};
-        for (int d = 0; d < 3; ++d) {
-            double mn = X[3 * mi.x + d], mx = mn;
-            for (int k = 0; k < 2; ++k) {
-                double a = X[3 * av[k] + d], b = a + dir[3 * av[k] + d];
-                mn = fmin(mn, fmin(a, b));
-                mx = fmax(mx, fmax(a, b));
-            }
-            alo[d] = mn;
-            ahi[d] = mx;
+                               const BoxI* __restrict__ ebox, const BoxI* __restrict__ eboxc,
+                               const GridP* __restrict__ gp, const double* __restrict__ thick,
+                               const uint64_t* __restrict__ ckey, const uint32_t* __restrict__ cstart, int ncell,
+                               const uint32_t* __restrict__ entries, CCand* __restrict__ out, unsigned int* counter,
+                               long cap) {
+    long eI = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (eI >= nE) return;
+    int inst = einst[eI];
+    if (!active[inst]) return;
+    int2 mi = edges[eI];
+    GridP g = gp[inst];
+    double th = thick[inst];
+    double alo[3], ahi[3];
+    const int av[2] = {mi.x, mi.y};
+    for (int d = 0; d < 3; ++d) {
+        double mn = X[3 * mi.x + d], mx = mn;
+        for (int k = 0; k < 2; ++k) {
+            double a = X[3 * av[k] + d], b = a + dir[3 * av[k] + d];
+            mn = fmin(mn, fmin(a, b));
+            mx = fmax(mx, fmax(a, b));
         }
+        alo[d] = mn;
+        ahi[d] = mx;
     }
-    while (__any_sync(0xffffffffu, more)) {
-        bool emit = false;
-        CCand c = {0, 0};
-        if (more) {
-            uint32_t e;
-            if (cursor_next(q, inst, g, ckey, cstart, ncell, e)) {
-                int eJ = (int)entries[e];
-                if (eJ > eI && first_shared_cell(q, ebox[eJ])) {
-                    int2 mj = edges[eJ];
-                    if (!(mi.x == mj.x || mi.x == mj.y || mi.y == mj.x || mi.y == mj.y) &&
-                        !(dbc[mi.x] && dbc[mi.y] && dbc[mj.x] && dbc[mj.y])) {
-                        double blo[3], bhi[3];
-                        int bv[2] = {mj.x, mj.y};
-                        for (int d = 0; d < 3; ++d) {
-                            double mn = X[3 * mj.x + d], mx = mn;
-                            for (int k = 0; k < 2; ++k) {
-                                double a = X[3 * bv[k] + d], b = a + dir[3 * bv[k] + d];
-                                mn = fmin(mn, fmin(a, b));
-                                mx = fmax(mx, fmax(a, b));
-                            }
-                            blo[d] = mn;
-                            bhi[d] = mx;
-                        }
-                        if (!swept_far(alo, ahi, blo, bhi, th)) { emit = true; c = {(int)eI, eJ}; }
-                    }
-                }
-            } else {
-                more = false;
-            }
-        }
-        warp_emit(emit, c, out, counter, cap);
-    }
+    const BoxI qc = eboxc[eI], qx = ebox[eI];
+    const bool adbc = dbc[mi.x] && dbc[mi.y];
+    warp_walk_emit(qc, inst, g, ckey, cstart, ncell, entries, out, counter, cap,
+                   [&](uint32_t ent, int cx, int cy, int cz, CCand& c) -> bool {
+                       int eJ = (int)ent;
+                       if (eJ <= eI || !is_first_shared(qc, eboxc[eJ], cx, cy, cz) || !boxes_overlap(qx, ebox[eJ]))
+                           return false;
+                       int2 mj = edges[eJ];
+                       if (mi.x == mj.x || mi.x == mj.y || mi.y == mj.x || mi.y == mj.y) return false;
+                       if (adbc && dbc[mj.x] && dbc[mj.y]) return false;
+                       double blo[3], bhi[3];
+                       const int bv[2] = {mj.x, mj.y};
+                       for (int d = 0; d < 3; ++d) {
+                           double mn = X[3 * mj.x + d], mx = mn;
+                           for (int k = 0; k < 2; ++k) {
+                               double a = X[3 * bv[k] + d], b = a + dir[3 * bv[k] + d];
+                               mn = fmin(mn, fmin(a, b));
+                               mx = fmax(mx, fmax(a, b));
+                           }
+                           blo[d] = mn;
+                           bhi[d] = mx;
+                       }
+                       if (swept_far(alo, ahi, blo, bhi, th)) return false;
+                       c = {(int)eI, eJ};
+                       return true;
+                   });
 }
 
 // ---- ACCD (CCD.h:279-328, 330-395)
@@ -485,37 +494,42 @@ int ccd_stepsize(Arena& A, Work& W, const double* X, const double* dir, double* 
     int* d_sn_off = d_se_off + nI + 1;
     IDP_CUDA_TRY(cudaMemcpyAsync(d_se_off, A.se_off.data(), sizeof(int) * (nI + 1), cudaMemcpyHostToDevice, s));
     IDP_CUDA_TRY(cudaMemcpyAsync(d_sn_off, A.sn_off.data(), sizeof(int) * (nI + 1), cudaMemcpyHostToDevice, s));
-    if (A.Se) k_edge_len<<<grid_for(A.Se), kBlock, 0, s>>>(A.Se, A.sedge, X, len);
-    if (A.Sn) k_abs_dir<<<grid_for(A.Sn), kBlock, 0, s>>>(A.Sn, A.snode, dir, absdir);
-    k_span_cap<<<nI, 256, 0, s>>>(nI, A.active, d_se_off, d_sn_off, len, absdir, sumsc, alpha, vsz);
+    if (A.Se) (::idp::count_launch(), k_edge_len<<<grid_for(A.Se), kBlock, 0, s>>>(A.Se, A.sedge, X, len));
+    if (A.Sn) (::idp::count_launch(), k_abs_dir<<<grid_for(A.Sn), kBlock, 0, s>>>(A.Sn, A.snode, dir, absdir));
+    (::idp::count_launch(), k_span_cap<<<nI, 256, 0, s>>>(nI, A.active, d_se_off, d_sn_off, len, absdir, sumsc, alpha, vsz));
     // grid
     if (W[W_BBOX].ensure(sizeof(unsigned long long) * 6 * nI) || W[W_GRIDP].ensure(sizeof(GridP) * nI))
         return IDP_ERR_CUDA;
     unsigned long long* bb = W[W_BBOX].as<unsigned long long>();
     GridP* gp = W[W_GRIDP].as<GridP>();
-    k_bb_init<<<grid_for(6 * nI), kBlock, 0, s>>>(nI, bb);
-    if (A.Sn) k_ccd_bbox<<<grid_for(A.Sn), kBlock, 0, s>>>(A.Sn, A.snode, A.sn_inst, A.active, X, dir, alpha, bb);
-    k_ccd_grid<<<grid_for(nI), kBlock, 0, s>>>(nI, A.active, bb, A.thickness, vsz, gp);
+    (::idp::count_launch(), k_bb_init<<<grid_for(6 * nI), kBlock, 0, s>>>(nI, bb));
+    if (A.Sn) (::idp::count_launch(), k_ccd_bbox<<<grid_for(A.Sn), kBlock, 0, s>>>(A.Sn, A.snode, A.sn_inst, A.active, X, dir, alpha, bb));
+    (::idp::count_launch(), k_ccd_grid<<<grid_for(nI), kBlock, 0, s>>>(nI, A.active, bb, A.thickness, vsz, gp));
     long St = A.St > 0 ? A.St : 1;
-    if (W[W_BOX_A].ensure(sizeof(BoxI) * (St + Se + Sn))) return IDP_ERR_CUDA;
+    if (W[W_BOX_A].ensure(sizeof(BoxI) * 2 * (St + Se + Sn)) || W[W_BOX_B].ensure(sizeof(GridP) * (nI + 1)))
+        return IDP_ERR_CUDA;
     BoxI* tbox = W[W_BOX_A].as<BoxI>();
     BoxI* ebox = tbox + St;
     BoxI* nbox = ebox + Se;
+    BoxI* tboxc = nbox + Sn;
+    BoxI* eboxc = tboxc + St;
+    BoxI* nboxc = eboxc + Se;
+    GridP* gc = W[W_BOX_B].as<GridP>();
     if (A.Sn)
-        k_node_box<<<grid_for(A.Sn), kBlock, 0, s>>>(A.Sn, A.snode, A.sn_inst, A.active, X, dir, alpha, A.thickness, gp,
-                                                     nbox);
-    extern int* g_v2s_hack;
-    (void)0;
+        (::idp::count_launch(), k_node_box<<<grid_for(A.Sn), kBlock, 0, s>>>(A.Sn, A.snode, A.sn_inst, A.active, X, dir, alpha, A.thickness, gp,
+                                                     nbox));
     // triangle / edge boxes from node boxes (v2s: vertex -> surface node)
     if (A.St)
-        k_prim_box_from_nodes<3><<<grid_for(A.St), kBlock, 0, s>>>(A.St, A.stri, A.v2s, nbox, tbox);
+        (::idp::count_launch(), k_prim_box_from_nodes<3><<<grid_for(A.St), kBlock, 0, s>>>(A.St, A.stri, A.v2s, nbox, tbox));
     if (A.Se)
-        k_prim_box_from_nodes<2><<<grid_for(A.Se), kBlock, 0, s>>>(A.Se, reinterpret_cast<const int*>(A.sedge), A.v2s,
-                                                                   nbox, ebox);
+        (::idp::count_launch(), k_prim_box_from_nodes<2><<<grid_for(A.Se), kBlock, 0, s>>>(A.Se, reinterpret_cast<const int*>(A.sedge), A.v2s,
+                                                                   nbox, ebox));
+    (::idp::count_launch(), k_coarse_boxes<<<grid_for(St + Se + Sn), kBlock, 0, s>>>(St + Se + Sn, tbox, tboxc));
+    (::idp::count_launch(), k_coarse_grid<<<grid_for(nI), kBlock, 0, s>>>(nI, gp, gc));
     BoxGrid gt, ge;
-    int rc = build_box_grid(W, 0, tbox, A.st_inst, A.active, A.St, gp, nI, gt, s);
+    int rc = build_box_grid(W, 0, tboxc, A.st_inst, A.active, A.St, gc, nI, gt, s);
     if (rc) return rc;
-    rc = build_box_grid(W, 1, ebox, A.se_inst, A.active, A.Se, gp, nI, ge, s);
+    rc = build_box_grid(W, 1, eboxc, A.se_inst, A.active, A.Se, gc, nI, ge, s);
     if (rc) return rc;
     // candidates
     if (W[W_CAND_CNT].ensure(64)) return IDP_ERR_CUDA;
@@ -530,27 +544,27 @@ int ccd_stepsize(Arena& A, Work& W, const double* X, const double* dir, double* 
         unsigned int hc[2] = {0, 0};
         IDP_CUDA_TRY(cudaMemsetAsync(ccount, 0, 2 * sizeof(unsigned int), s));
         if (A.Sn)
-            k_ccd_query_pt<<<grid_for(A.Sn), kBlock, 0, s>>>(A.Sn, A.snode, A.sn_inst, A.active, X, dir, A.dbc, A.stri,
-                                                             nbox, tbox, gp, A.thickness, gt.cell_keys, gt.cell_start,
-                                                             gt.ncell, gt.entries, cand, ccount, cap);
+            (::idp::count_launch(), k_ccd_query_pt<<<grid_for(32 * A.Sn), kBlock, 0, s>>>(A.Sn, A.snode, A.sn_inst, A.active, X, dir, A.dbc, A.stri,
+                                                             nbox, tbox, nboxc, tboxc, gc, A.thickness, gt.cell_keys, gt.cell_start,
+                                                             gt.ncell, gt.entries, cand, ccount, cap));
         IDP_CUDA_TRY(cudaMemcpyAsync(hc, ccount, sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
         IDP_CUDA_TRY(cudaStreamSynchronize(s));
         long npt = hc[0];
         long cap_ee = cap - npt;
         if (A.Se && cap_ee > 0)
-            k_ccd_query_ee<<<grid_for(A.Se), kBlock, 0, s>>>(A.Se, A.sedge, A.se_inst, A.active, X, dir, A.dbc, ebox, gp,
+            (::idp::count_launch(), k_ccd_query_ee<<<grid_for(32 * A.Se), kBlock, 0, s>>>(A.Se, A.sedge, A.se_inst, A.active, X, dir, A.dbc, ebox, eboxc, gc,
                                                              A.thickness, ge.cell_keys, ge.cell_start, ge.ncell,
-                                                             ge.entries, cand + npt, ccount + 1, cap_ee);
+                                                             ge.entries, cand + npt, ccount + 1, cap_ee));
         IDP_CUDA_TRY(cudaMemcpyAsync(hc + 1, ccount + 1, sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
         IDP_CUDA_TRY(cudaStreamSynchronize(s));
         long nee = hc[1];
         if (npt + nee <= cap && (A.Se == 0 || cap_ee > 0)) {
-            k_fill<<<grid_for(nI), kBlock, 0, s>>>(nI, 1e300, amin);
+            (::idp::count_launch(), k_fill<<<grid_for(nI), kBlock, 0, s>>>(nI, 1e300, amin));
             IDP_CUDA_TRY(cudaMemsetAsync(flags, 0, sizeof(int) * nI, s));
             if (npt + nee)
-                k_accd<<<grid_for(npt + nee, 128), 128, 0, s>>>(npt, nee, cand, A.snode, A.sn_inst, A.stri, A.sedge,
-                                                                A.se_inst, X, dir, A.thickness, alpha, amin, flags);
-            k_alpha_final<<<grid_for(nI), kBlock, 0, s>>>(nI, A.active, amin, alpha);
+                (::idp::count_launch(), k_accd<<<grid_for(npt + nee, 128), 128, 0, s>>>(npt, nee, cand, A.snode, A.sn_inst, A.stri, A.sedge,
+                                                                A.se_inst, X, dir, A.thickness, alpha, amin, flags));
+            (::idp::count_launch(), k_alpha_final<<<grid_for(nI), kBlock, 0, s>>>(nI, A.active, amin, alpha));
             return cudaGetLastError() == cudaSuccess ? IDP_OK : IDP_ERR_CUDA;
         }
         cap = 2 * (npt + nee) + 1024;

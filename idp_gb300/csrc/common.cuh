@@ -18,6 +18,11 @@ namespace idp {
 
 constexpr int kBlock = 256;
 
+// host-side count of kernel launches made by this library (every launch
+// site is written as (count_launch(), kernel<<<...>>>(...)))
+extern long long g_launch_count;
+inline void count_launch() { ++g_launch_count; }
+
 inline int grid_for(long n, int block = kBlock) {
     long g = (n + block - 1) / block;
     if (g < 1) g = 1;
@@ -35,6 +40,9 @@ struct Chunk {
     int end;
 };
 constexpr int kChunk = 1024;
+// instances up to this many vertices run PCG in one persistent thread-block
+// cluster; larger ones use the multi-launch path
+constexpr long kClusterPcgMaxV = 262144;
 
 // ---- small vector math (templated so FP32 and FP64 paths share code)
 template <class T>

@@ -166,6 +166,7 @@ struct Cand {
     int a, b;
 };
 
+// warp per surface node: triangles within the +-dHat box (IPC.h:158-196)
 __global__ void k_query_pt(long nN, const int* __restrict__ nodes, const int* __restrict__ ninst,
                            const unsigned char* __restrict__ active, const double* __restrict__ X,
                            const unsigned char* __restrict__ dbc, const int* __restrict__ tris,
@@ -174,58 +175,40 @@ __global__ void k_query_pt(long nN, const int* __restrict__ nodes, const int* __
                            const uint64_t* __restrict__ ckey, const uint32_t* __restrict__ cstart, int ncell,
                            const uint32_t* __restrict__ entries, Cand* __restrict__ out, unsigned int* counter,
                            long cap) {
-    long s = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    bool more = s < nN;
-    int inst = 0, vI = 0;
-    D3 p = {0, 0, 0};
-    double r = 0;
-    Cursor q;
-    GridP g;
-    if (more) {
-        inst = ninst[s];
-        more = active[inst] != 0;
-    }
-    if (more) {
-        vI = nodes[s];
-        p = ld3(X, vI);
-        r = sqrt(dHat2[inst]) + thick[inst];
-        g = gp[inst];
-        double rq = r * (1.0 + 1e-12) + 1e-300;
-        int lo[3], hi[3];
-        vox3(g, mk3(p.x - rq, p.y - rq, p.z - rq), lo);
-        vox3(g, mk3(p.x + rq, p.y + rq, p.z + rq), hi);
-        BoxI qb;
-        for (int d = 0; d < 3; ++d) { qb.lo[d] = lo[d]; qb.hi[d] = hi[d]; }
-        cursor_init(q, qb);
-    }
-    while (__any_sync(0xffffffffu, more)) {
-        bool emit = false;
-        Cand c = {0, 0};
-        if (more) {
-            uint32_t e;
-            if (cursor_next(q, inst, g, ckey, cstart, ncell, e)) {
-                int f = (int)entries[e];
-                if (first_shared_cell(q, tbox[f])) {
-                    int t0 = tris[3 * f], t1 = tris[3 * f + 1], t2 = tris[3 * f + 2];
-                    if (!(vI == t0 || vI == t1 || vI == t2) && !(dbc[vI] && dbc[t0] && dbc[t1] && dbc[t2])) {
-                        D3 a = ld3(X, t0), b = ld3(X, t1), cc = ld3(X, t2);
-                        double mx[3] = {fmax(fmax(a.x, b.x), cc.x), fmax(fmax(a.y, b.y), cc.y), fmax(fmax(a.z, b.z), cc.z)};
-                        double mn[3] = {fmin(fmin(a.x, b.x), cc.x), fmin(fmin(a.y, b.y), cc.y), fmin(fmin(a.z, b.z), cc.z)};
-                        double pp[3] = {p.x, p.y, p.z};
-                        bool far = false;
-                        for (int d = 0; d < 3; ++d)
-                            if (pp[d] - mx[d] > r || mn[d] - pp[d] > r) far = true;
-                        if (!far) { emit = true; c = {(int)s, f}; }
-                    }
-                }
-            } else {
-                more = false;
-            }
-        }
-        warp_emit(emit, c, out, counter, cap);
-    }
+    long s = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (s >= nN) return;  // whole warp leaves together
+    int inst = ninst[s];
+    if (!active[inst]) return;
+    int vI = nodes[s];
+    D3 p = ld3(X, vI);
+    double r = sqrt(dHat2[inst]) + thick[inst];
+    GridP g = gp[inst];
+    double rq = r * (1.0 + 1e-12) + 1e-300;
+    int lo[3], hi[3];
+    vox3(g, mk3(p.x - rq, p.y - rq, p.z - rq), lo);
+    vox3(g, mk3(p.x + rq, p.y + rq, p.z + rq), hi);
+    BoxI qb;
+    for (int d = 0; d < 3; ++d) { qb.lo[d] = lo[d]; qb.hi[d] = hi[d]; }
+    const double pp[3] = {p.x, p.y, p.z};
+    const bool pdbc = dbc[vI] != 0;
+    warp_walk_emit(qb, inst, g, ckey, cstart, ncell, entries, out, counter, cap,
+                   [&](uint32_t ent, int cx, int cy, int cz, Cand& c) -> bool {
+                       int f = (int)ent;
+                       if (!is_first_shared(qb, tbox[f], cx, cy, cz)) return false;
+                       int t0 = tris[3 * f], t1 = tris[3 * f + 1], t2 = tris[3 * f + 2];
+                       if (vI == t0 || vI == t1 || vI == t2) return false;
+                       if (pdbc && dbc[t0] && dbc[t1] && dbc[t2]) return false;
+                       D3 a = ld3(X, t0), b = ld3(X, t1), cc = ld3(X, t2);
+                       double mx[3] = {fmax(fmax(a.x, b.x), cc.x), fmax(fmax(a.y, b.y), cc.y), fmax(fmax(a.z, b.z), cc.z)};
+                       double mn[3] = {fmin(fmin(a.x, b.x), cc.x), fmin(fmin(a.y, b.y), cc.y), fmin(fmin(a.z, b.z), cc.z)};
+                       for (int d = 0; d < 3; ++d)
+                           if (pp[d] - mx[d] > r || mn[d] - pp[d] > r) return false;
+                       c = {(int)s, f};
+                       return true;
+                   });
 }
 
+// warp per surface edge: edges eJ > eI within the +-dHat box (IPC.h:371-420)
 __global__ void k_query_ee(long nE, const int2* __restrict__ edges, const int* __restrict__ einst,
                            const unsigned char* __restrict__ active, const double* __restrict__ X,
                            const unsigned char* __restrict__ dbc, const BoxI* __restrict__ ebox,
@@ -233,60 +216,38 @@ __global__ void k_query_ee(long nE, const int2* __restrict__ edges, const int* _
                            const double* __restrict__ thick, const uint64_t* __restrict__ ckey,
                            const uint32_t* __restrict__ cstart, int ncell, const uint32_t* __restrict__ entries,
                            Cand* __restrict__ out, unsigned int* counter, long cap) {
-    long eI = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    bool more = eI < nE;
-    int inst = 0;
-    int2 mi = {0, 0};
-    D3 a0 = {0, 0, 0}, a1 = {0, 0, 0};
-    double r = 0;
-    Cursor q;
-    GridP g;
-    if (more) {
-        inst = einst[eI];
-        more = active[inst] != 0;
-    }
-    if (more) {
-        mi = edges[eI];
-        a0 = ld3(X, mi.x);
-        a1 = ld3(X, mi.y);
-        r = sqrt(dHat2[inst]) + thick[inst];
-        g = gp[inst];
-        double rq = r * (1.0 + 1e-12) + 1e-300;
-        int lo[3], hi[3];
-        vox3(g, mk3(fmin(a0.x, a1.x) - rq, fmin(a0.y, a1.y) - rq, fmin(a0.z, a1.z) - rq), lo);
-        vox3(g, mk3(fmax(a0.x, a1.x) + rq, fmax(a0.y, a1.y) + rq, fmax(a0.z, a1.z) + rq), hi);
-        BoxI qb;
-        for (int d = 0; d < 3; ++d) { qb.lo[d] = lo[d]; qb.hi[d] = hi[d]; }
-        cursor_init(q, qb);
-    }
-    while (__any_sync(0xffffffffu, more)) {
-        bool emit = false;
-        Cand c = {0, 0};
-        if (more) {
-            uint32_t e;
-            if (cursor_next(q, inst, g, ckey, cstart, ncell, e)) {
-                int eJ = (int)entries[e];
-                if (eJ > eI && first_shared_cell(q, ebox[eJ])) {
-                    int2 mj = edges[eJ];
-                    if (!(mi.x == mj.x || mi.x == mj.y || mi.y == mj.x || mi.y == mj.y) &&
-                        !(dbc[mi.x] && dbc[mi.y] && dbc[mj.x] && dbc[mj.y])) {
-                        D3 b0 = ld3(X, mj.x), b1 = ld3(X, mj.y);
-                        double amax[3] = {fmax(a0.x, a1.x), fmax(a0.y, a1.y), fmax(a0.z, a1.z)};
-                        double amin[3] = {fmin(a0.x, a1.x), fmin(a0.y, a1.y), fmin(a0.z, a1.z)};
-                        double bmax[3] = {fmax(b0.x, b1.x), fmax(b0.y, b1.y), fmax(b0.z, b1.z)};
-                        double bmin[3] = {fmin(b0.x, b1.x), fmin(b0.y, b1.y), fmin(b0.z, b1.z)};
-                        bool far = false;
-                        for (int d = 0; d < 3; ++d)
-                            if (amin[d] - bmax[d] > r || bmin[d] - amax[d] > r) far = true;
-                        if (!far) { emit = true; c = {(int)eI, eJ}; }
-                    }
-                }
-            } else {
-                more = false;
-            }
-        }
-        warp_emit(emit, c, out, counter, cap);
-    }
+    long eI = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (eI >= nE) return;
+    int inst = einst[eI];
+    if (!active[inst]) return;
+    int2 mi = edges[eI];
+    D3 a0 = ld3(X, mi.x), a1 = ld3(X, mi.y);
+    double r = sqrt(dHat2[inst]) + thick[inst];
+    GridP g = gp[inst];
+    double rq = r * (1.0 + 1e-12) + 1e-300;
+    int lo[3], hi[3];
+    vox3(g, mk3(fmin(a0.x, a1.x) - rq, fmin(a0.y, a1.y) - rq, fmin(a0.z, a1.z) - rq), lo);
+    vox3(g, mk3(fmax(a0.x, a1.x) + rq, fmax(a0.y, a1.y) + rq, fmax(a0.z, a1.z) + rq), hi);
+    BoxI qb;
+    for (int d = 0; d < 3; ++d) { qb.lo[d] = lo[d]; qb.hi[d] = hi[d]; }
+    const double amax[3] = {fmax(a0.x, a1.x), fmax(a0.y, a1.y), fmax(a0.z, a1.z)};
+    const double amin[3] = {fmin(a0.x, a1.x), fmin(a0.y, a1.y), fmin(a0.z, a1.z)};
+    const bool adbc = dbc[mi.x] && dbc[mi.y];
+    warp_walk_emit(qb, inst, g, ckey, cstart, ncell, entries, out, counter, cap,
+                   [&](uint32_t ent, int cx, int cy, int cz, Cand& c) -> bool {
+                       int eJ = (int)ent;
+                       if (eJ <= eI || !is_first_shared(qb, ebox[eJ], cx, cy, cz)) return false;
+                       int2 mj = edges[eJ];
+                       if (mi.x == mj.x || mi.x == mj.y || mi.y == mj.x || mi.y == mj.y) return false;
+                       if (adbc && dbc[mj.x] && dbc[mj.y]) return false;
+                       D3 b0 = ld3(X, mj.x), b1 = ld3(X, mj.y);
+                       double bmax[3] = {fmax(b0.x, b1.x), fmax(b0.y, b1.y), fmax(b0.z, b1.z)};
+                       double bmin[3] = {fmin(b0.x, b1.x), fmin(b0.y, b1.y), fmin(b0.z, b1.z)};
+                       for (int d = 0; d < 3; ++d)
+                           if (amin[d] - bmax[d] > r || bmin[d] - amax[d] > r) return false;
+                       c = {(int)eI, eJ};
+                       return true;
+                   });
 }
 
 // ---- narrow phase
@@ -469,7 +430,7 @@ int build_box_grid(Work& W, int slot, const BoxI* boxes, const int* inst, const 
     if (bcnt.ensure(sizeof(uint32_t) * (np + 1))) return IDP_ERR_CUDA;
     if (W[W_SCRATCH].ensure(scan_scratch_bytes(np) + 64)) return IDP_ERR_CUDA;
     uint32_t* cnt = bcnt.as<uint32_t>();
-    k_box_count<<<grid_for(np), kBlock, 0, s>>>(nprim, boxes, inst, active, cnt);
+    (::idp::count_launch(), k_box_count<<<grid_for(np), kBlock, 0, s>>>(nprim, boxes, inst, active, cnt));
     if (scan_exclusive(cnt, cnt, nprim, cnt + nprim, W[W_SCRATCH].p, s) != cudaSuccess) return IDP_ERR_CUDA;
     uint32_t total = 0;
     IDP_CUDA_TRY(cudaMemcpyAsync(&total, cnt + nprim, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
@@ -479,8 +440,8 @@ int build_box_grid(Work& W, int slot, const BoxI* boxes, const int* inst, const 
     if (bkeys.ensure(8 * nalloc) || bvals.ensure(4 * nalloc) || bkeys2.ensure(8 * nalloc) || bvals2.ensure(4 * nalloc))
         return IDP_ERR_CUDA;
     if (bcell.ensure((8 + 4) * (nalloc + 1) + 4 * (nalloc + 1) * 2 + 64)) return IDP_ERR_CUDA;
-    k_box_emit<<<grid_for(np), kBlock, 0, s>>>(nprim, boxes, inst, active, gp, cnt, bkeys.as<uint64_t>(),
-                                               bvals.as<uint32_t>());
+    (::idp::count_launch(), k_box_emit<<<grid_for(np), kBlock, 0, s>>>(nprim, boxes, inst, active, gp, cnt, bkeys.as<uint64_t>(),
+                                               bvals.as<uint32_t>()));
     int bits = 32 + bits_for((uint64_t)(nI > 0 ? nI : 1));
     if (W[W_SCRATCH].ensure(radix_sort_scratch_bytes(nalloc) + scan_scratch_bytes(nalloc) + 64)) return IDP_ERR_CUDA;
     if (radix_sort_pairs(bkeys.as<uint64_t>(), bvals.as<uint32_t>(), bkeys2.as<uint64_t>(), bvals2.as<uint32_t>(), ne,
@@ -493,9 +454,9 @@ int build_box_grid(Work& W, int slot, const BoxI* boxes, const int* inst, const 
     uint32_t* idx = head + nalloc + 1;
     uint32_t ncell = 0;
     if (ne > 0) {
-        k_mark_heads<<<grid_for(ne), kBlock, 0, s>>>(ne, bkeys.as<uint64_t>(), head);
+        (::idp::count_launch(), k_mark_heads<<<grid_for(ne), kBlock, 0, s>>>(ne, bkeys.as<uint64_t>(), head));
         if (scan_exclusive(head, idx, ne, idx + ne, W[W_SCRATCH].p, s) != cudaSuccess) return IDP_ERR_CUDA;
-        k_cell_table<<<grid_for(ne), kBlock, 0, s>>>(ne, bkeys.as<uint64_t>(), head, idx, ckey, cstart, idx + ne);
+        (::idp::count_launch(), k_cell_table<<<grid_for(ne), kBlock, 0, s>>>(ne, bkeys.as<uint64_t>(), head, idx, ckey, cstart, idx + ne));
         IDP_CUDA_TRY(cudaMemcpyAsync(&ncell, idx + ne, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
         IDP_CUDA_TRY(cudaStreamSynchronize(s));
     } else {
@@ -516,18 +477,18 @@ int build_constraint_set(Arena& A, Work& W, const double* X, ContactSet& cs, cud
         return IDP_ERR_CUDA;
     unsigned long long* bb = W[W_BBOX].as<unsigned long long>();
     GridP* gp = W[W_GRIDP].as<GridP>();
-    k_bbox_init<<<grid_for(6 * nI), kBlock, 0, s>>>(nI, bb);
-    if (A.Sn) k_bbox<<<grid_for(A.Sn), kBlock, 0, s>>>(A.Sn, A.snode, A.sn_inst, A.active, X, bb);
-    k_grid_params<<<grid_for(nI), kBlock, 0, s>>>(nI, bb, A.cell, A.dHat2, A.thickness, A.active, gp);
+    (::idp::count_launch(), k_bbox_init<<<grid_for(6 * nI), kBlock, 0, s>>>(nI, bb));
+    if (A.Sn) (::idp::count_launch(), k_bbox<<<grid_for(A.Sn), kBlock, 0, s>>>(A.Sn, A.snode, A.sn_inst, A.active, X, bb));
+    (::idp::count_launch(), k_grid_params<<<grid_for(nI), kBlock, 0, s>>>(nI, bb, A.cell, A.dHat2, A.thickness, A.active, gp));
     // 2. triangle and edge boxes + grids
     long St = A.St > 0 ? A.St : 1, Se = A.Se > 0 ? A.Se : 1;
     if (W[W_BOX_A].ensure(sizeof(BoxI) * St) || W[W_BOX_B].ensure(sizeof(BoxI) * Se)) return IDP_ERR_CUDA;
     BoxI* tbox = W[W_BOX_A].as<BoxI>();
     BoxI* ebox = W[W_BOX_B].as<BoxI>();
-    if (A.St) k_prim_boxes<3><<<grid_for(A.St), kBlock, 0, s>>>(A.St, A.stri, A.st_inst, A.active, X, gp, tbox);
+    if (A.St) (::idp::count_launch(), k_prim_boxes<3><<<grid_for(A.St), kBlock, 0, s>>>(A.St, A.stri, A.st_inst, A.active, X, gp, tbox));
     if (A.Se)
-        k_prim_boxes<2><<<grid_for(A.Se), kBlock, 0, s>>>(A.Se, reinterpret_cast<const int*>(A.sedge), A.se_inst,
-                                                           A.active, X, gp, ebox);
+        (::idp::count_launch(), k_prim_boxes<2><<<grid_for(A.Se), kBlock, 0, s>>>(A.Se, reinterpret_cast<const int*>(A.sedge), A.se_inst,
+                                                           A.active, X, gp, ebox));
     BoxGrid gt, ge;
     int rc = build_box_grid(W, 0, tbox, A.st_inst, A.active, A.St, gp, nI, gt, s);
     if (rc) return rc;
@@ -547,17 +508,17 @@ int build_constraint_set(Arena& A, Work& W, const double* X, ContactSet& cs, cud
         Cand* cand = W[W_CAND].as<Cand>();
         IDP_CUDA_TRY(cudaMemsetAsync(ccount, 0, 2 * sizeof(unsigned int), s));
         if (A.Sn)
-            k_query_pt<<<grid_for(A.Sn), kBlock, 0, s>>>(A.Sn, A.snode, A.sn_inst, A.active, X, A.dbc, A.stri, tbox, gp,
+            (::idp::count_launch(), k_query_pt<<<grid_for(32 * A.Sn), kBlock, 0, s>>>(A.Sn, A.snode, A.sn_inst, A.active, X, A.dbc, A.stri, tbox, gp,
                                                          A.dHat2, A.thickness, gt.cell_keys, gt.cell_start, gt.ncell,
-                                                         gt.entries, cand, ccount, cap);
+                                                         gt.entries, cand, ccount, cap));
         IDP_CUDA_TRY(cudaMemcpyAsync(hc, ccount, sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
         IDP_CUDA_TRY(cudaStreamSynchronize(s));
         long npt = hc[0];
         long cap_ee = cap - npt;
         if (A.Se && cap_ee > 0)
-            k_query_ee<<<grid_for(A.Se), kBlock, 0, s>>>(A.Se, A.sedge, A.se_inst, A.active, X, A.dbc, ebox, gp, A.dHat2,
+            (::idp::count_launch(), k_query_ee<<<grid_for(32 * A.Se), kBlock, 0, s>>>(A.Se, A.sedge, A.se_inst, A.active, X, A.dbc, ebox, gp, A.dHat2,
                                                          A.thickness, ge.cell_keys, ge.cell_start, ge.ncell, ge.entries,
-                                                         cand + npt, ccount + 1, cap_ee);
+                                                         cand + npt, ccount + 1, cap_ee));
         IDP_CUDA_TRY(cudaMemcpyAsync(hc + 1, ccount + 1, sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
         IDP_CUDA_TRY(cudaStreamSynchronize(s));
         long nee = hc[1];
@@ -571,11 +532,11 @@ int build_constraint_set(Arena& A, Work& W, const double* X, ContactSet& cs, cud
             Rec* recs = W[W_CONS_TMP].as<Rec>();
             IDP_CUDA_TRY(cudaMemsetAsync(ccount, 0, sizeof(unsigned int), s));
             if (npt)
-                k_narrow_pt<<<grid_for(npt), kBlock, 0, s>>>(npt, cand, A.snode, A.sn_inst, A.stri, X, A.dHat2, A.thickness,
-                                                             recs, ccount, rcap);
+                (::idp::count_launch(), k_narrow_pt<<<grid_for(npt), kBlock, 0, s>>>(npt, cand, A.snode, A.sn_inst, A.stri, X, A.dHat2, A.thickness,
+                                                             recs, ccount, rcap));
             if (nee)
-                k_narrow_ee<<<grid_for(nee), kBlock, 0, s>>>(nee, cand + npt, A.sedge, A.se_inst, X, A.X0, A.dHat2,
-                                                             A.thickness, recs, ccount, rcap);
+                (::idp::count_launch(), k_narrow_ee<<<grid_for(nee), kBlock, 0, s>>>(nee, cand + npt, A.sedge, A.se_inst, X, A.X0, A.dHat2,
+                                                             A.thickness, recs, ccount, rcap));
             unsigned int nrec = 0;
             IDP_CUDA_TRY(cudaMemcpyAsync(&nrec, ccount, sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
             IDP_CUDA_TRY(cudaStreamSynchronize(s));
@@ -601,22 +562,22 @@ int build_constraint_set(Arena& A, Work& W, const double* X, ContactSet& cs, cud
             int* cinst = W[W_CONS_INST].as<int>();
             uint32_t total = 0;
             if (n > 0) {
-                k_rec_keys<<<grid_for(n), kBlock, 0, s>>>(n, recs, b, offv, klo, p1);
+                (::idp::count_launch(), k_rec_keys<<<grid_for(n), kBlock, 0, s>>>(n, recs, b, offv, klo, p1));
                 if (radix_sort_pairs(klo, p1, kalt, valt, n, 2 * b, W[W_SCRATCH].p, s) != cudaSuccess) return IDP_ERR_CUDA;
-                k_rec_keys_hi<<<grid_for(n), kBlock, 0, s>>>(n, recs, p1, b, offv, khi, p2);
+                (::idp::count_launch(), k_rec_keys_hi<<<grid_for(n), kBlock, 0, s>>>(n, recs, p1, b, offv, khi, p2));
                 if (radix_sort_pairs(khi, p2, kalt, valt, n, 2 * b + bits_for((uint64_t)nI), W[W_SCRATCH].p, s) !=
                     cudaSuccess)
                     return IDP_ERR_CUDA;
                 uint32_t* head = W[W_CONS_HEAD].as<uint32_t>();
                 uint32_t* pos = head + na + 1;
-                k_merge_heads<<<grid_for(n), kBlock, 0, s>>>(n, recs, p2, head);
+                (::idp::count_launch(), k_merge_heads<<<grid_for(n), kBlock, 0, s>>>(n, recs, p2, head));
                 if (scan_exclusive(head, pos, n, pos + n, W[W_SCRATCH].p, s) != cudaSuccess) return IDP_ERR_CUDA;
-                k_merge_write<<<grid_for(n), kBlock, 0, s>>>(n, recs, p2, head, pos, cons, cinst);
+                (::idp::count_launch(), k_merge_write<<<grid_for(n), kBlock, 0, s>>>(n, recs, p2, head, pos, cons, cinst));
                 IDP_CUDA_TRY(cudaMemcpyAsync(&total, pos + n, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
                 IDP_CUDA_TRY(cudaStreamSynchronize(s));
             }
             cs.C = total;
-            k_inst_offsets<<<grid_for(nI + 1), kBlock, 0, s>>>(nI, cs.C, cinst, W[W_CONS_OFF].as<int>());
+            (::idp::count_launch(), k_inst_offsets<<<grid_for(nI + 1), kBlock, 0, s>>>(nI, cs.C, cinst, W[W_CONS_OFF].as<int>()));
             cs.off.resize(nI + 1);
             IDP_CUDA_TRY(cudaMemcpyAsync(cs.off.data(), W[W_CONS_OFF].as<int>(), sizeof(int) * (nI + 1),
                                          cudaMemcpyDeviceToHost, s));
@@ -634,7 +595,7 @@ int constraint_min_dist2(Arena& A, Work& W, const double* X, const int4* cons, c
                          double* dist2, double* inst_min, cudaStream_t s) {
     (void)W;
     if (C <= 0) return IDP_OK;
-    k_min_dist2<<<grid_for(C), kBlock, 0, s>>>(C, cons, cinst, A.active, X, dist2, inst_min);
+    (::idp::count_launch(), k_min_dist2<<<grid_for(C), kBlock, 0, s>>>(C, cons, cinst, A.active, X, dist2, inst_min));
     return cudaGetLastError() == cudaSuccess ? IDP_OK : IDP_ERR_CUDA;
 }
 

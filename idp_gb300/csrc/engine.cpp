@@ -11,7 +11,9 @@
 // other instances of the batch.
 #include <algorithm>
 #include <array>
+#include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <numeric>
@@ -19,6 +21,8 @@
 #include "engine.hpp"
 
 using namespace idp;
+
+long long idp::g_launch_count = 0;
 
 int DBuf::ensure(size_t n) {
     if (n <= bytes && p) return 0;
@@ -52,6 +56,9 @@ struct idp_ctx {
     long prevC = 0;
     DBuf inst_buf;            // per-instance device scalars
     DBuf vel;                 // velocities (3V)
+    DBuf snap;                // saved X and v (6V)
+    std::vector<double> snap_kappa;
+    bool has_snap = false;
 };
 
 namespace {
@@ -188,7 +195,9 @@ int eval_energy(idp_ctx* c, const double* X, bool with_barrier, std::vector<doub
     double h2 = c->P.h * c->P.h;
     IDP_CUDA_TRY(cudaMemsetAsync(isc(c, SI_BAD), 0, sizeof(int) * nI * 2, c->s));
     IDP_CUDA_TRY(cudaMemsetAsync(dsc(c, S_EBAR), 0, sizeof(double) * nI, c->s));
+    c->W.timer.start(PhaseTimer::TET, c->s);
     int rc = tet_energy(A, c->W, X, h2, dsc(c, S_ETET), isc(c, SI_BAD), c->s);
+    c->W.timer.stop(c->s);
     if (rc) return rc;
     rc = vec_inertia(A, c->W, X, dsc(c, S_EINERT), nullptr, c->s);
     if (rc) return rc;
@@ -215,11 +224,15 @@ int eval_energy(idp_ctx* c, const double* X, bool with_barrier, std::vector<doub
 int eval_gradient(idp_ctx* c, const double* X) {
     Arena& A = c->A;
     double h2 = c->P.h * c->P.h;
+    c->W.timer.start(PhaseTimer::TET, c->s);
     int rc = tet_gradient(A, c->W, X, h2, nullptr, c->s);
+    c->W.timer.stop(c->s);
     if (rc) return rc;
     rc = grad_gather_tet(A, c->W, X, A.g, c->s);
     if (rc) return rc;
+    c->W.timer.start(PhaseTimer::BARRIER, c->s);
     rc = barrier_gradient(A, c->W, X, c->cs, A.g, c->s);
+    c->W.timer.stop(c->s);
     if (rc) return rc;
     return vec_zero_dbc(A, A.g, c->s);
 }
@@ -227,11 +240,18 @@ int eval_gradient(idp_ctx* c, const double* X) {
 int eval_hessian(idp_ctx* c, const double* X) {
     Arena& A = c->A;
     bool fp64 = c->P.mode == IDP_MODE_FP64;
+    c->W.timer.start(PhaseTimer::TET, c->s);
     int rc = tet_hessian(A, c->W, X, c->P.h * c->P.h, fp64, c->s);
+    c->W.timer.stop(c->s);
     if (rc) return rc;
+    c->W.timer.start(PhaseTimer::BARRIER, c->s);
     rc = barrier_hessian(A, c->W, X, c->cs, fp64, c->s);
+    c->W.timer.stop(c->s);
     if (rc) return rc;
-    return assemble(A, c->W, c->cs, fp64, c->s);
+    c->W.timer.start(PhaseTimer::ASSEMBLY, c->s);
+    rc = assemble(A, c->W, c->cs, fp64, c->s);
+    c->W.timer.stop(c->s);
+    return rc;
 }
 
 // copy the current constraint set to the "previous" slot with its distances
@@ -312,6 +332,7 @@ void idp_destroy(idp_ctx* c) {
     c->W.release();
     c->inst_buf.release();
     c->vel.release();
+    c->snap.release();
     cudaStreamDestroy(c->s);
     delete c;
 }
@@ -556,6 +577,19 @@ int idp_commit(idp_ctx* c) {
         rc |= upload(c, A.vert_corner_ptr, vcp);
         rc |= upload(c, A.vert_corner, vc);
     }
+    // algorithmic bytes of one FP32 PCG iteration per instance: BSR values
+    // and column ids once, and ~7 vector reads/writes plus the 3x3
+    // preconditioner block per vertex (FP64 mode doubles the value bytes)
+    {
+        std::vector<int> rp(A.V + 1);
+        cudaMemcpy(rp.data(), A.rowptr, sizeof(int) * (A.V + 1), cudaMemcpyDeviceToHost);
+        c->W.pcg_bytes_per_iter.assign(nI, 0.0);
+        for (int i = 0; i < nI; ++i) {
+            double Bi = rp[A.v_off[i + 1]] - rp[A.v_off[i]];
+            double Vi = A.v_off[i + 1] - A.v_off[i];
+            c->W.pcg_bytes_per_iter[i] = Bi * (36 + 4) + Vi * (12 * 7 + 36 + 4);
+        }
+    }
     if (c->inst_buf.ensure(sizeof(double) * (S_NUMD + S_NUMI) * (nI + 1))) rc = IDP_ERR_CUDA;
     if (c->vel.ensure(sizeof(double) * 3 * (A.V + 1))) rc = IDP_ERR_CUDA;
     else if (cudaMemcpy(c->vel.p, vel.data(), sizeof(double) * 3 * A.V, cudaMemcpyHostToDevice) != cudaSuccess)
@@ -576,6 +610,21 @@ int idp_advance(idp_ctx* c, idp_result* results) {
     const bool fp64 = c->P.mode == IDP_MODE_FP64;
     cudaStream_t s = c->s;
     int rc;
+    W.timer.reset();
+    W.stats = idp_stats{};
+    const long long launches0 = g_launch_count;
+    W.timer.start(PhaseTimer::TOTAL, s);
+    const auto t_start = std::chrono::steady_clock::now();
+    std::vector<double> latency(nI, 0.0);
+    auto now_ms = [&]() {
+        return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
+    };
+    auto build_cs = [&](const double* Xp) {
+        W.timer.start(PhaseTimer::CONTACT, s);
+        int r = build_constraint_set(A, W, Xp, c->cs, s);
+        W.timer.stop(s);
+        return r;
+    };
     std::vector<unsigned char> all(nI, 1), mask(nI, 0);
     if ((rc = set_mask(c, all))) return rc;
     // x^n and x_tilde = x^n + h v (IMPLICIT_EULER.h:195-216)
@@ -600,7 +649,7 @@ int idp_advance(idp_ctx* c, idp_result* results) {
         nvert[i] = c->inst[i].V;
     }
     // initial constraint set and energy (IMPLICIT_EULER.h:418-434)
-    if ((rc = build_constraint_set(A, W, A.X, c->cs, s))) return rc;
+    if ((rc = build_cs(A.X))) return rc;
     std::vector<double> E;
     std::vector<int> bad;
     if ((rc = eval_energy(c, A.X, true, E, bad))) return rc;
@@ -647,6 +696,7 @@ int idp_advance(idp_ctx* c, idp_result* results) {
         }
         if ((rc = set_mask(c, mask))) return rc;
         // ---- Line_Search (IMPLICIT_EULER.h:9-149)
+        W.timer.start(PhaseTimer::LINESEARCH, s);
         IDP_CUDA_TRY(cudaMemcpyAsync(A.Xprev, A.X, sizeof(double) * 3 * A.V, cudaMemcpyDeviceToDevice, s));
         std::vector<double> alpha(nI, 1.0);
         // inversion-feasible alpha (halve while any det F <= 0)
@@ -670,7 +720,10 @@ int idp_advance(idp_ctx* c, idp_result* results) {
         // CCD filter (IMPLICIT_EULER.h:96-100)
         if ((rc = set_mask(c, mask))) return rc;
         IDP_CUDA_TRY(cudaMemcpyAsync(A.alpha, alpha.data(), sizeof(double) * nI, cudaMemcpyHostToDevice, s));
-        if ((rc = ccd_stepsize(A, W, A.Xprev, A.dir, A.alpha, isc(c, SI_CCDF), s))) return rc;
+        W.timer.start(PhaseTimer::CCD, s);
+        rc = ccd_stepsize(A, W, A.Xprev, A.dir, A.alpha, isc(c, SI_CCDF), s);
+        W.timer.stop(s);
+        if (rc) return rc;
         if ((rc = fetch(c, A.alpha, alpha))) return rc;
         if ((rc = fetch(c, isc(c, SI_CCDF), hi))) return rc;
         std::vector<double> feasible = alpha;
@@ -698,7 +751,7 @@ int idp_advance(idp_ctx* c, idp_result* results) {
             for (int i = 0; i < nI; ++i) st[i].ls_trials += srch[i];
             // constraint set + min-distance safeguard on the valid ones
             if ((rc = set_mask(c, valid))) return rc;
-            if ((rc = build_constraint_set(A, W, A.X, c->cs, s))) return rc;
+            if ((rc = build_cs(A.X))) return rc;
             std::vector<double> md(nI, 1e300);
             IDP_CUDA_TRY(cudaMemcpyAsync(dsc(c, S_MIND), md.data(), sizeof(double) * nI, cudaMemcpyHostToDevice, s));
             if ((rc = constraint_min_dist2(A, W, A.X, W[W_CONS].as<int4>(), W[W_CONS_INST].as<int>(), c->cs.C, nullptr,
@@ -731,9 +784,10 @@ int idp_advance(idp_ctx* c, idp_result* results) {
         }
         for (int i = 0; i < nI; ++i)
             if (srch[i]) st[i].status = IDP_ERR_ZERO_STEP;  // line search exhausted
+        W.timer.stop(s);
         // X holds every instance's accepted trial; rebuild their constraint set
         if ((rc = set_mask(c, mask))) return rc;
-        if ((rc = build_constraint_set(A, W, A.X, c->cs, s))) return rc;
+        if ((rc = build_cs(A.X))) return rc;
         for (int i = 0; i < nI; ++i)
             if (mask[i]) {
                 st[i].Eprev = Eacc[i];
@@ -789,12 +843,29 @@ int idp_advance(idp_ctx* c, idp_result* results) {
                 S.active = false;
                 S.status = IDP_ERR_NOT_CONVERGED;
             }
+            if (!S.active) latency[i] = now_ms();
         }
     }
     // v = (x - x^n) / h (IMPLICIT_EULER.h:882-888)
     if ((rc = set_mask(c, all))) return rc;
     if ((rc = vec_velocity(A, A.X, A.Xn, h, c->vel.as<double>(), s))) return rc;
+    W.timer.stop(s);
     IDP_CUDA_TRY(cudaStreamSynchronize(s));
+    {
+        double ms[PhaseTimer::NPHASE], hms[PhaseTimer::NPHASE];
+        W.timer.collect(ms, hms);
+        if (std::getenv("IDP_PROFILE")) {
+            const char* nm[] = {"pcg", "tet", "contact", "ccd", "total", "barrier", "assembly", "linesearch"};
+            for (int k = 0; k < PhaseTimer::NPHASE; ++k)
+                std::fprintf(stderr, "idp phase %-10s device %10.3f ms  host %10.3f ms\n", nm[k], ms[k], hms[k]);
+        }
+        W.stats.pcg_ms = ms[PhaseTimer::PCG];
+        W.stats.tet_ms = ms[PhaseTimer::TET];
+        W.stats.contact_ms = ms[PhaseTimer::CONTACT];
+        W.stats.ccd_ms = ms[PhaseTimer::CCD];
+        W.stats.total_ms = ms[PhaseTimer::TOTAL];
+        W.stats.kernel_launches = g_launch_count - launches0;
+    }
     int worst = IDP_OK;
     for (int i = 0; i < nI; ++i) {
         if (results) {
@@ -808,10 +879,42 @@ int idp_advance(idp_ctx* c, idp_result* results) {
             r.kappa = st[i].kappa;
             r.residual = st[i].last_res;
             r.min_alpha = st[i].min_alpha;
+            r.latency_ms = latency[i] > 0 ? latency[i] : now_ms();
         }
         if (st[i].status != IDP_OK && st[i].status != IDP_WARN_ITER_CAP && worst == IDP_OK) worst = st[i].status;
     }
     return worst;
+}
+
+int idp_save_state(idp_ctx* c) {
+    if (!c || !c->committed) return IDP_ERR_STATE;
+    long n = 3L * c->A.V;
+    if (c->snap.ensure(sizeof(double) * 2 * (n + 1))) return IDP_ERR_CUDA;
+    IDP_CUDA_TRY(cudaMemcpyAsync(c->snap.as<double>(), c->A.X, sizeof(double) * n, cudaMemcpyDeviceToDevice, c->s));
+    IDP_CUDA_TRY(cudaMemcpyAsync(c->snap.as<double>() + n, c->vel.as<double>(), sizeof(double) * n,
+                                 cudaMemcpyDeviceToDevice, c->s));
+    IDP_CUDA_TRY(cudaStreamSynchronize(c->s));
+    c->snap_kappa.clear();
+    for (auto& S : c->st) c->snap_kappa.push_back(S.kappa);
+    c->has_snap = true;
+    return IDP_OK;
+}
+
+int idp_restore_state(idp_ctx* c) {
+    if (!c || !c->committed || !c->has_snap) return IDP_ERR_STATE;
+    long n = 3L * c->A.V;
+    IDP_CUDA_TRY(cudaMemcpyAsync(c->A.X, c->snap.as<double>(), sizeof(double) * n, cudaMemcpyDeviceToDevice, c->s));
+    IDP_CUDA_TRY(cudaMemcpyAsync(c->vel.as<double>(), c->snap.as<double>() + n, sizeof(double) * n,
+                                 cudaMemcpyDeviceToDevice, c->s));
+    IDP_CUDA_TRY(cudaStreamSynchronize(c->s));
+    for (size_t i = 0; i < c->st.size(); ++i) c->st[i].kappa = c->snap_kappa[i];
+    return IDP_OK;
+}
+
+int idp_get_stats(idp_ctx* c, idp_stats* out) {
+    if (!c || !out) return IDP_ERR_INVALID_ARG;
+    *out = c->W.stats;
+    return IDP_OK;
 }
 
 int idp_get_state(idp_ctx* c, int i, double* X, double* v, double* kappa3) {

@@ -5,6 +5,7 @@
 #pragma once
 #include <vector>
 #include <string>
+#include <chrono>
 #include "common.cuh"
 #include "../../include/idp_gb300.h"
 
@@ -91,6 +92,73 @@ struct Arena {
     int* v2s = nullptr;                           // vertex -> surface node (or -1)
 };
 
+// CUDA-event timing of the engine's phases on the context stream; elapsed
+// times are collected once, when the caller asks for them
+struct PhaseTimer {
+    enum { PCG, TET, CONTACT, CCD, TOTAL, BARRIER, ASSEMBLY, LINESEARCH, NPHASE };
+    struct Rec {
+        int phase;
+        cudaEvent_t a, b;
+        double host_ms;
+        std::chrono::steady_clock::time_point t0;
+    };
+    std::vector<cudaEvent_t> pool;
+    std::vector<Rec> recs;
+    std::vector<int> open;      // stack of open records
+    size_t used = 0;
+    bool enabled = true;
+    cudaEvent_t take() {
+        if (used == pool.size()) {
+            cudaEvent_t e;
+            cudaEventCreate(&e);
+            pool.push_back(e);
+        }
+        return pool[used++];
+    }
+    void start(int ph, cudaStream_t s) {
+        if (!enabled) return;
+        Rec r;
+        r.phase = ph;
+        r.a = take();
+        r.b = nullptr;
+        r.host_ms = 0;
+        cudaEventRecord(r.a, s);
+        r.t0 = std::chrono::steady_clock::now();
+        open.push_back((int)recs.size());
+        recs.push_back(r);
+    }
+    void stop(cudaStream_t s) {
+        if (!enabled || open.empty()) return;
+        Rec& r = recs[open.back()];
+        open.pop_back();
+        r.b = take();
+        cudaEventRecord(r.b, s);
+        r.host_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - r.t0).count();
+    }
+    void reset() {
+        recs.clear();
+        open.clear();
+        used = 0;
+    }
+    // device (event) and host (enqueue-to-return) milliseconds per phase
+    void collect(double* ms, double* host) {
+        for (int k = 0; k < NPHASE; ++k) ms[k] = host[k] = 0;
+        for (auto& r : recs) {
+            if (!r.b) continue;
+            float t = 0;
+            cudaEventSynchronize(r.b);
+            cudaEventElapsedTime(&t, r.a, r.b);
+            ms[r.phase] += t;
+            host[r.phase] += r.host_ms;
+        }
+    }
+    void release() {
+        for (auto e : pool) cudaEventDestroy(e);
+        pool.clear();
+        reset();
+    }
+};
+
 // all scratch/work buffers reused across calls, indexed by slot
 enum WorkSlot {
     W_SCRATCH, W_SCRATCH2, W_TET_GRAD, W_TET_HESS, W_CHUNK_SUM, W_INST_SUM, W_FLAGS,
@@ -108,8 +176,14 @@ enum WorkSlot {
 };
 struct Work {
     DBuf b[W_NUM];
+    idp_stats stats{};
+    PhaseTimer timer;
+    std::vector<double> pcg_bytes_per_iter;  // per instance
     DBuf& operator[](int i) { return b[i]; }
-    void release() { for (auto& x : b) x.release(); }
+    void release() {
+        for (auto& x : b) x.release();
+        timer.release();
+    }
 };
 
 struct Params {

@@ -96,6 +96,27 @@ __device__ __forceinline__ bool first_shared_cell(const Cursor& q, const BoxI& b
     return true;
 }
 
+// warp-per-query walk: the whole warp visits the cells of box qb in order;
+// for every occupied cell, lanes take the cell's entries 32 at a time and
+// call test(entry, cell) -> emit?; emitted values are compacted with one
+// ballot per 32 entries. All lanes of the warp must call this together.
+template <class V, class Test>
+__device__ __forceinline__ void warp_walk_emit(const BoxI& qb, int inst, const GridP& g, const uint64_t* __restrict__ ckey,
+                                               const uint32_t* __restrict__ cstart, int ncell,
+                                               const uint32_t* __restrict__ entries, V* __restrict__ out,
+                                               unsigned int* counter, long cap, Test&& test);
+
+// lowest corner cell of the intersection of the query box and box b
+__device__ __forceinline__ bool is_first_shared(const BoxI& q, const BoxI& b, int cx, int cy, int cz) {
+    int c[3] = {cx, cy, cz};
+    for (int d = 0; d < 3; ++d) {
+        if (b.lo[d] > q.hi[d] || b.hi[d] < q.lo[d]) return false;
+        int m = q.lo[d] > b.lo[d] ? q.lo[d] : b.lo[d];
+        if (m != c[d]) return false;
+    }
+    return true;
+}
+
 // warp-cooperative append: lanes with emit=true write v to out[] in a block
 // reserved by one atomicAdd per warp. Writes beyond cap are dropped (the
 // counter still counts them so the caller can grow and retry).
@@ -112,6 +133,29 @@ __device__ __forceinline__ void warp_emit(bool emit, const V& v, V* __restrict__
         unsigned int pos = base + __popc(m & ((1u << lane) - 1u));
         if (pos < cap) out[pos] = v;
     }
+}
+
+template <class V, class Test>
+__device__ __forceinline__ void warp_walk_emit(const BoxI& qb, int inst, const GridP& g, const uint64_t* __restrict__ ckey,
+                                               const uint32_t* __restrict__ cstart, int ncell,
+                                               const uint32_t* __restrict__ entries, V* __restrict__ out,
+                                               unsigned int* counter, long cap, Test&& test) {
+    const int lane = threadIdx.x & 31;
+    for (int z = qb.lo[2]; z <= qb.hi[2]; ++z)
+        for (int y = qb.lo[1]; y <= qb.hi[1]; ++y)
+            for (int x = qb.lo[0]; x <= qb.hi[0]; ++x) {
+                uint64_t key = cell_key(inst, g, x, y, z);
+                int k = lower_bound_u64(ckey, ncell, key);
+                if (k >= ncell || ckey[k] != key) continue;
+                uint32_t e0 = cstart[k], e1 = cstart[k + 1];
+                for (uint32_t base = e0; base < e1; base += 32) {
+                    uint32_t e = base + lane;
+                    V v;
+                    bool emit = false;
+                    if (e < e1) emit = test(entries[e], x, y, z, v);
+                    warp_emit(emit, v, out, counter, cap);
+                }
+            }
 }
 
 // ---- host-side builder (contact.cu): sorted (instance, cell) entry table

@@ -184,17 +184,17 @@ cudaError_t scan_exclusive(const uint32_t* in, uint32_t* out, long n, uint32_t* 
     }
     long tiles = (n + SC_TILE - 1) / SC_TILE;
     if (tiles == 1) {
-        scan_tiles<<<1, SC_THREADS, 0, s>>>(in, out, n, nullptr, total);
+        (::idp::count_launch(), scan_tiles<<<1, SC_THREADS, 0, s>>>(in, out, n, nullptr, total));
         return cudaGetLastError();
     }
     uint32_t* sums = reinterpret_cast<uint32_t*>(scratch);
     long padded = (tiles + 63) / 64 * 64;
     uint32_t* offs = sums + padded;
     void* rest = offs + padded;
-    scan_tile_sums<<<(int)tiles, SC_THREADS, 0, s>>>(in, n, sums);
+    (::idp::count_launch(), scan_tile_sums<<<(int)tiles, SC_THREADS, 0, s>>>(in, n, sums));
     cudaError_t e = scan_exclusive(sums, offs, tiles, nullptr, rest, s);
     if (e != cudaSuccess) return e;
-    scan_tiles<<<(int)tiles, SC_THREADS, 0, s>>>(in, out, n, offs, total);
+    (::idp::count_launch(), scan_tiles<<<(int)tiles, SC_THREADS, 0, s>>>(in, out, n, offs, total));
     return cudaGetLastError();
 }
 
@@ -211,10 +211,10 @@ cudaError_t radix_sort_pairs(uint64_t* keys, uint32_t* vals, uint64_t* keys_alt,
     int passes = (bits + 7) / 8;
     for (int p = 0; p < passes; ++p) {
         int shift = 8 * p;
-        rs_histogram<<<(int)tiles, RS_THREADS, 0, s>>>(kin, n, shift, counts, (int)tiles);
+        (::idp::count_launch(), rs_histogram<<<(int)tiles, RS_THREADS, 0, s>>>(kin, n, shift, counts, (int)tiles));
         cudaError_t e = scan_exclusive(counts, counts, 256 * tiles, nullptr, scan_scratch, s);
         if (e != cudaSuccess) return e;
-        rs_scatter<<<(int)tiles, RS_THREADS, 0, s>>>(kin, vin, n, shift, counts, (int)tiles, kout, vout);
+        (::idp::count_launch(), rs_scatter<<<(int)tiles, RS_THREADS, 0, s>>>(kin, vin, n, shift, counts, (int)tiles, kout, vout));
         std::swap(kin, kout);
         std::swap(vin, vout);
     }
@@ -234,7 +234,7 @@ cudaError_t det_sum(const double* x, long n, double* result, double* scratch, cu
     while (true) {
         long tiles = (m + DS_TILE - 1) / DS_TILE;
         double* out = (tiles == 1) ? result : buf[which];
-        det_sum_tiles<<<(int)tiles, DS_THREADS, 0, s>>>(in, m, out);
+        (::idp::count_launch(), det_sum_tiles<<<(int)tiles, DS_THREADS, 0, s>>>(in, m, out));
         if (tiles == 1) break;
         in = out;
         m = tiles;

@@ -13,8 +13,11 @@
 // its own scalars and stops on its own). Mixed mode runs PCG in FP32 and
 // recovers the direction by iterative refinement against an FP64 residual
 // r = b - A x (FP32 matrix, FP64 accumulation); FP64 mode runs PCG in FP64.
+#include <cooperative_groups.h>
 #include "engine.hpp"
 #include "prims.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace idp {
 
@@ -304,27 +307,29 @@ __global__ void k_pcg_scal_beta(int nI, const int* __restrict__ coff, const doub
     S[i] = s;
 }
 
-// FP64 residual: res = b - A x64 (FP32/FP64 matrix, FP64 accumulation);
-// chunk partials of res.res
+// FP64 residual: res = b - A x64 (FP32/FP64 matrix, FP64 accumulation).
+// FP64 throughput is low on this part, so rows are spread over many small
+// CTAs; the squared norm is reduced afterwards per vertex chunk.
 template <class T>
-__global__ void k_residual64(const Chunk* __restrict__ chunks, const unsigned char* __restrict__ active,
+__global__ void k_residual64(long V, const int* __restrict__ vinst, const unsigned char* __restrict__ active,
                              const int* __restrict__ rowptr, const int* __restrict__ colidx, const T* __restrict__ val,
                              const int* __restrict__ trp, const int* __restrict__ tcol, const T* __restrict__ tval,
                              const unsigned char* __restrict__ dbc, const double* __restrict__ b,
-                             const double* __restrict__ x, double* __restrict__ res, double* __restrict__ part) {
-    Chunk c = chunks[blockIdx.x];
-    if (!active[c.inst]) return;
-    double acc = 0;
-    for (int v = c.begin + threadIdx.x; v < c.end; v += blockDim.x) {
-        double y[3];
-        spmv_row<T, double, double>(v, rowptr, colidx, val, trp, tcol, tval, dbc, x, y);
+                             const double* __restrict__ x, double* __restrict__ res) {
+    long v = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= V || !active[vinst[v]]) return;
+    double y[3];
+    spmv_row<T, double, double>(v, rowptr, colidx, val, trp, tcol, tval, dbc, x, y);
 #pragma unroll
-        for (int d = 0; d < 3; ++d) {
-            double r = dbc[v] ? 0.0 : b[3 * v + d] - y[d];
-            res[3 * v + d] = r;
-            acc += r * r;
-        }
-    }
+    for (int d = 0; d < 3; ++d) res[3 * v + d] = dbc[v] ? 0.0 : b[3 * v + d] - y[d];
+}
+
+__global__ void k_norm2_chunks(const Chunk* __restrict__ chunks, const unsigned char* __restrict__ active,
+                               const double* __restrict__ a, double* __restrict__ part) {
+    Chunk c = chunks[blockIdx.x];
+    double acc = 0;
+    if (active[c.inst])
+        for (int k = 3 * c.begin + threadIdx.x; k < 3 * c.end; k += blockDim.x) acc += a[k] * a[k];
     double s = cta_sum(acc);
     if (threadIdx.x == 0) part[blockIdx.x] = s;
 }
@@ -409,11 +414,147 @@ __global__ void k_zero_dbc(long V, const unsigned char* __restrict__ dbc, double
     g[3 * v] = g[3 * v + 1] = g[3 * v + 2] = 0;
 }
 
+template <class T>
+__device__ __forceinline__ void precond(long v, const T* __restrict__ dinv, const unsigned char* __restrict__ dbc,
+                                        const T rv[3], T zv[3]) {
+    if (dbc[v]) { zv[0] = zv[1] = zv[2] = T(0); return; }
+    const T* D = dinv + 9 * v;
+    zv[0] = D[0] * rv[0] + D[1] * rv[1] + D[2] * rv[2];
+    zv[1] = D[3] * rv[0] + D[4] * rv[1] + D[5] * rv[2];
+    zv[2] = D[6] * rv[0] + D[7] * rv[1] + D[8] * rv[2];
+}
+
+// ---- persistent PCG: one thread-block cluster runs the whole solve of one
+// instance. CTA r of the cluster owns a contiguous slice of the instance's
+// vertices; dot products are reduced inside each CTA (warp shuffles, then
+// warp partials in order) and across the cluster through distributed shared
+// memory (every CTA adds the cluster's partials in rank order, so all CTAs
+// hold the same bit-identical scalar). Cluster barriers order the phases.
+// Accumulation precision follows the vectors (FP32 in mixed mode).
+constexpr int CL_THREADS = 512;
+
+template <class T>
+__device__ __forceinline__ T cta_reduce2(T a, T b, T* wsh, T& out_b) {
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_down_sync(0xffffffffu, a, o);
+        b += __shfl_down_sync(0xffffffffu, b, o);
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    __syncthreads();
+    if (lane == 0) { wsh[2 * warp] = a; wsh[2 * warp + 1] = b; }
+    __syncthreads();
+    T ra = 0, rb = 0;
+    for (int w = 0; w < nw; ++w) { ra += wsh[2 * w]; rb += wsh[2 * w + 1]; }
+    out_b = rb;
+    return ra;
+}
+
+template <class T>
+__device__ __forceinline__ void cluster_sum2(cg::cluster_group& cl, T a, T b, T (*slot)[2], int which, T& sa, T& sb) {
+    if (threadIdx.x == 0) { slot[which][0] = a; slot[which][1] = b; }
+    cl.sync();
+    T ra = 0, rb = 0;
+    const int n = (int)cl.num_blocks();
+    for (int r = 0; r < n; ++r) {
+        T* rp = cl.map_shared_rank(&slot[which][0], r);
+        ra += rp[0];
+        rb += rp[1];
+    }
+    sa = ra;
+    sb = rb;
+}
+
+template <class T>
+__global__ void __launch_bounds__(CL_THREADS) k_pcg_cluster(
+    const int* __restrict__ inst_list, const int* __restrict__ v_off, const int* __restrict__ rowptr,
+    const int* __restrict__ colidx, const T* __restrict__ val, const int* __restrict__ trp, const int* __restrict__ tcol,
+    const T* __restrict__ tval, const unsigned char* __restrict__ dbc, const T* __restrict__ dinv,
+    const double* __restrict__ b, T* __restrict__ x, T* __restrict__ r, T* __restrict__ z, T* __restrict__ p,
+    T* __restrict__ Ap, double rel_tol, int max_iters, int* __restrict__ iters_out) {
+    __shared__ T wsh[2 * (CL_THREADS / 32)];
+    __shared__ T slot[4][2];
+    cg::cluster_group cl = cg::this_cluster();
+    const int csize = (int)cl.num_blocks(), crank = (int)cl.block_rank();
+    const int inst = inst_list[blockIdx.x / csize];
+    const int iv0 = v_off[inst], iv1 = v_off[inst + 1];
+    const int per = (iv1 - iv0 + csize - 1) / csize;
+    const int v0 = iv0 + crank * per, v1 = min(iv1, v0 + per);
+    int which = 0;
+    T rz_l = 0, rr_l = 0;
+    for (int v = v0 + threadIdx.x; v < v1; v += blockDim.x) {
+        T rv[3], zv[3];
+        for (int d = 0; d < 3; ++d) {
+            rv[d] = dbc[v] ? T(0) : (T)b[3 * v + d];
+            x[3 * v + d] = T(0);
+            r[3 * v + d] = rv[d];
+        }
+        precond(v, dinv, dbc, rv, zv);
+        for (int d = 0; d < 3; ++d) {
+            z[3 * v + d] = zv[d];
+            p[3 * v + d] = zv[d];
+            rz_l += rv[d] * zv[d];
+            rr_l += rv[d] * rv[d];
+        }
+    }
+    T rr_c, rz = cta_reduce2(rz_l, rr_l, wsh, rr_c);
+    T rr;
+    cluster_sum2(cl, rz, rr_c, slot, which, rz, rr);
+    which ^= 1;
+    const T tol2 = (T)(rel_tol * rel_tol) * rr;
+    int it = 0;
+    if (rr > T(0) && rr > tol2) {
+        for (it = 0; it < max_iters;) {
+            cl.sync();  // every CTA's p is written before any CTA reads neighbours
+            T pAp_l = 0;
+            for (int v = v0 + threadIdx.x; v < v1; v += blockDim.x) {
+                T y[3];
+                spmv_row<T, T, T>(v, rowptr, colidx, val, trp, tcol, tval, dbc, p, y);
+                for (int d = 0; d < 3; ++d) {
+                    Ap[3 * v + d] = y[d];
+                    pAp_l += p[3 * v + d] * y[d];
+                }
+            }
+            T dummy, pAp = cta_reduce2(pAp_l, T(0), wsh, dummy);
+            cluster_sum2(cl, pAp, T(0), slot, which, pAp, dummy);
+            which ^= 1;
+            if (!(pAp > T(0))) break;
+            const T alpha = rz / pAp;
+            T rzn_l = 0, rrn_l = 0;
+            for (int v = v0 + threadIdx.x; v < v1; v += blockDim.x) {
+                T rv[3], zv[3];
+                for (int d = 0; d < 3; ++d) {
+                    x[3 * v + d] += alpha * p[3 * v + d];
+                    rv[d] = r[3 * v + d] - alpha * Ap[3 * v + d];
+                    r[3 * v + d] = rv[d];
+                }
+                precond(v, dinv, dbc, rv, zv);
+                for (int d = 0; d < 3; ++d) {
+                    z[3 * v + d] = zv[d];
+                    rzn_l += rv[d] * zv[d];
+                    rrn_l += rv[d] * rv[d];
+                }
+            }
+            T rrn_c, rzn = cta_reduce2(rzn_l, rrn_l, wsh, rrn_c);
+            T rrn;
+            cluster_sum2(cl, rzn, rrn_c, slot, which, rzn, rrn);
+            which ^= 1;
+            ++it;
+            if (rrn <= tol2) break;
+            const T beta = rzn / rz;
+            rz = rzn;
+            for (int v = v0 + threadIdx.x; v < v1; v += blockDim.x)
+                for (int d = 0; d < 3; ++d) p[3 * v + d] = z[3 * v + d] + beta * p[3 * v + d];
+        }
+    }
+    cl.sync();  // no CTA leaves while others may still read its shared memory
+    if (crank == 0 && threadIdx.x == 0) iters_out[inst] = it;
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------- host side
 int chunk_reduce_off(Arena& A, const int* coff, const double* part, double* out, bool accumulate, cudaStream_t s) {
-    k_chunk_reduce<<<grid_for(A.nI), kBlock, 0, s>>>(A.nI, coff, part, out, accumulate ? 1 : 0);
+    (::idp::count_launch(), k_chunk_reduce<<<grid_for(A.nI), kBlock, 0, s>>>(A.nI, coff, part, out, accumulate ? 1 : 0));
     return cudaGetLastError() == cudaSuccess ? IDP_OK : IDP_ERR_CUDA;
 }
 
@@ -428,23 +569,23 @@ int vec_inertia(Arena& A, Work& W, const double* X, double* inst_E, double* g, c
     (void)g;
     if (W[W_CHUNK_SUM].ensure(sizeof(double) * (A.n_vert_chunks + A.n_tet_chunks + 2))) return IDP_ERR_CUDA;
     double* part = W[W_CHUNK_SUM].as<double>();
-    k_inertia_energy<<<A.n_vert_chunks, kBlock, 0, s>>>(A.vert_chunks, A.active, A.mass, X, A.Xtilde, part);
+    (::idp::count_launch(), k_inertia_energy<<<A.n_vert_chunks, kBlock, 0, s>>>(A.vert_chunks, A.active, A.mass, X, A.Xtilde, part));
     return chunk_reduce_off(A, A.vert_chunk_off, part, inst_E, false, s);
 }
 
 int grad_gather_tet(Arena& A, Work& W, const double* X, double* g, cudaStream_t s) {
-    k_grad_gather_tet<<<grid_for(A.V), kBlock, 0, s>>>(A.V, A.vinst, A.active, A.vert_corner_ptr, A.vert_corner,
-                                                       W[W_TET_GRAD].as<double>(), A.mass, X, A.Xtilde, g);
+    (::idp::count_launch(), k_grad_gather_tet<<<grid_for(A.V), kBlock, 0, s>>>(A.V, A.vinst, A.active, A.vert_corner_ptr, A.vert_corner,
+                                                       W[W_TET_GRAD].as<double>(), A.mass, X, A.Xtilde, g));
     return cudaGetLastError() == cudaSuccess ? IDP_OK : IDP_ERR_CUDA;
 }
 
 int vec_axpy_trial(Arena& A, const double* Xprev, const double* dir, double* Xout, cudaStream_t s) {
-    k_axpy_trial<<<grid_for(A.V), kBlock, 0, s>>>(A.V, A.vinst, A.active, A.alpha, Xprev, dir, Xout);
+    (::idp::count_launch(), k_axpy_trial<<<grid_for(A.V), kBlock, 0, s>>>(A.V, A.vinst, A.active, A.alpha, Xprev, dir, Xout));
     return cudaGetLastError() == cudaSuccess ? IDP_OK : IDP_ERR_CUDA;
 }
 
 int vec_zero_dbc(Arena& A, double* g, cudaStream_t s) {
-    k_zero_dbc<<<grid_for(A.V), kBlock, 0, s>>>(A.V, A.dbc, g);
+    (::idp::count_launch(), k_zero_dbc<<<grid_for(A.V), kBlock, 0, s>>>(A.V, A.dbc, g));
     return cudaGetLastError() == cudaSuccess ? IDP_OK : IDP_ERR_CUDA;
 }
 
@@ -455,19 +596,19 @@ int assemble(Arena& A, Work& W, const ContactSet& cs, bool fp64, cudaStream_t s)
     const int* trp = W[W_TAIL_ROWPTR].as<int>();
     const int* tcol = W[W_TAIL_COL].as<int>();
     if (fp64) {
-        k_assemble_tet<double><<<grid_for(A.B), kBlock, 0, s>>>(A.B, A.src_ptr, A.src, W[W_TET_HESS].as<double>(), A.brow,
+        (::idp::count_launch(), k_assemble_tet<double><<<grid_for(A.B), kBlock, 0, s>>>(A.B, A.src_ptr, A.src, W[W_TET_HESS].as<double>(), A.brow,
                                                                 A.colidx, A.mass, A.dbc, A.vinst, A.active,
-                                                                W[W_BSR_VAL].as<double>());
-        k_diag_inv<double><<<grid_for(A.V), kBlock, 0, s>>>(A.V, A.diagblk, W[W_BSR_VAL].as<double>(), trp, tcol,
+                                                                W[W_BSR_VAL].as<double>()));
+        (::idp::count_launch(), k_diag_inv<double><<<grid_for(A.V), kBlock, 0, s>>>(A.V, A.diagblk, W[W_BSR_VAL].as<double>(), trp, tcol,
                                                             W[W_TAIL_VAL].as<double>(), A.dbc, A.vinst, A.active,
-                                                            W[W_DIAG_INV].as<double>());
+                                                            W[W_DIAG_INV].as<double>()));
     } else {
-        k_assemble_tet<float><<<grid_for(A.B), kBlock, 0, s>>>(A.B, A.src_ptr, A.src, W[W_TET_HESS].as<float>(), A.brow,
+        (::idp::count_launch(), k_assemble_tet<float><<<grid_for(A.B), kBlock, 0, s>>>(A.B, A.src_ptr, A.src, W[W_TET_HESS].as<float>(), A.brow,
                                                                A.colidx, A.mass, A.dbc, A.vinst, A.active,
-                                                               W[W_BSR_VAL].as<float>());
-        k_diag_inv<float><<<grid_for(A.V), kBlock, 0, s>>>(A.V, A.diagblk, W[W_BSR_VAL].as<float>(), trp, tcol,
+                                                               W[W_BSR_VAL].as<float>()));
+        (::idp::count_launch(), k_diag_inv<float><<<grid_for(A.V), kBlock, 0, s>>>(A.V, A.diagblk, W[W_BSR_VAL].as<float>(), trp, tcol,
                                                            W[W_TAIL_VAL].as<float>(), A.dbc, A.vinst, A.active,
-                                                           W[W_DIAG_INV].as<float>());
+                                                           W[W_DIAG_INV].as<float>()));
     }
     return cudaGetLastError() == cudaSuccess ? IDP_OK : IDP_ERR_CUDA;
 }
@@ -476,13 +617,13 @@ int hessian_apply(Arena& A, Work& W, bool fp64, const double* x, double* y, cuda
     const int* trp = W[W_TAIL_ROWPTR].as<int>();
     const int* tcol = W[W_TAIL_COL].as<int>();
     if (fp64)
-        k_spmv_plain<double><<<grid_for(A.V), kBlock, 0, s>>>(A.V, A.vinst, A.active, A.rowptr, A.colidx,
+        (::idp::count_launch(), k_spmv_plain<double><<<grid_for(A.V), kBlock, 0, s>>>(A.V, A.vinst, A.active, A.rowptr, A.colidx,
                                                               W[W_BSR_VAL].as<double>(), trp, tcol,
-                                                              W[W_TAIL_VAL].as<double>(), A.dbc, x, y);
+                                                              W[W_TAIL_VAL].as<double>(), A.dbc, x, y));
     else
-        k_spmv_plain<float><<<grid_for(A.V), kBlock, 0, s>>>(A.V, A.vinst, A.active, A.rowptr, A.colidx,
+        (::idp::count_launch(), k_spmv_plain<float><<<grid_for(A.V), kBlock, 0, s>>>(A.V, A.vinst, A.active, A.rowptr, A.colidx,
                                                              W[W_BSR_VAL].as<float>(), trp, tcol,
-                                                             W[W_TAIL_VAL].as<float>(), A.dbc, x, y);
+                                                             W[W_TAIL_VAL].as<float>(), A.dbc, x, y));
     return cudaGetLastError() == cudaSuccess ? IDP_OK : IDP_ERR_CUDA;
 }
 
@@ -506,18 +647,100 @@ static int pcg_inner(Arena& A, Work& W, const double* b, double rel_tol, int max
     const int* tcol = W[W_TAIL_COL].as<int>();
     const T* tval = W[W_TAIL_VAL].as<T>();
     const int nc = A.n_vert_chunks;
-    k_pcg_init<T><<<nc, kBlock, 0, s>>>(A.vert_chunks, A.active, dinv, A.dbc, b, x, r, z, p, part);
-    k_pcg_scal_init<<<grid_for(nI), kBlock, 0, s>>>(nI, A.vert_chunk_off, A.active, part, rel_tol, S);
+    // instances up to kClusterPcgMaxV vertices: one thread-block cluster each,
+    // grouped by cluster size (one launch per size)
+    std::vector<unsigned char> act(nI), small(nI, 0), large(nI, 0);
+    IDP_CUDA_TRY(cudaMemcpyAsync(act.data(), A.active, nI, cudaMemcpyDeviceToHost, s));
+    IDP_CUDA_TRY(cudaStreamSynchronize(s));
+    bool any_small = false, any_large = false;
+    long vtot = 0;
+    for (int i = 0; i < nI; ++i)
+        if (act[i]) vtot += A.v_off[i + 1] - A.v_off[i];
+    std::vector<int> by_size[5];  // cluster sizes 1, 2, 4, 8, 16
+    for (int i = 0; i < nI; ++i) {
+        if (!act[i]) continue;
+        long vi = A.v_off[i + 1] - A.v_off[i];
+        if (vi > kClusterPcgMaxV) { large[i] = 1; any_large = true; continue; }
+        small[i] = 1;
+        any_small = true;
+        // aim for about two CTAs per SM over the whole launch, at most 16 per instance
+        double want = (double)vi * 2.0 * 152.0 / (double)(vtot > 0 ? vtot : 1);
+        int k = 0;
+        while (k < 4 && (1 << (k + 1)) <= want && (long)(CL_THREADS) * (1 << k) < vi) ++k;
+        by_size[k].push_back(i);
+    }
+    if (W[W_MISC2].ensure(sizeof(int) * (2 * nI + 64))) return IDP_ERR_CUDA;
+    int* d_list = W[W_MISC2].as<int>();
+    int* d_iters = d_list + nI + 32;
+    iters.assign(nI, 0);
+    if (any_small) {
+        std::vector<int> flat;
+        for (int k = 0; k < 5; ++k) flat.insert(flat.end(), by_size[k].begin(), by_size[k].end());
+        IDP_CUDA_TRY(cudaMemcpyAsync(d_list, flat.data(), sizeof(int) * flat.size(), cudaMemcpyHostToDevice, s));
+        static bool attr_set[2] = {false, false};
+        if (!attr_set[sizeof(T) == 8]) {
+            cudaFuncSetAttribute(k_pcg_cluster<T>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+            attr_set[sizeof(T) == 8] = true;
+        }
+        W.timer.start(PhaseTimer::PCG, s);
+        int base = 0;
+        for (int k = 0; k < 5; ++k) {
+            int n = (int)by_size[k].size();
+            if (!n) continue;
+            int cs = 1 << k;
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3(n * cs);
+            cfg.blockDim = dim3(CL_THREADS);
+            cfg.stream = s;
+            cudaLaunchAttribute at[1];
+            at[0].id = cudaLaunchAttributeClusterDimension;
+            at[0].val.clusterDim.x = cs;
+            at[0].val.clusterDim.y = 1;
+            at[0].val.clusterDim.z = 1;
+            cfg.attrs = at;
+            cfg.numAttrs = 1;
+            const int* lst = d_list + base;
+            ::idp::count_launch();
+            IDP_CUDA_TRY(cudaLaunchKernelEx(&cfg, k_pcg_cluster<T>, lst, (const int*)A.d_v_off, (const int*)A.rowptr,
+                                            (const int*)A.colidx, val, trp, tcol, tval, (const unsigned char*)A.dbc,
+                                            dinv, b, x, r, z, p, Ap, rel_tol, max_iters, d_iters));
+            W.stats.pcg_launches += 1;
+            base += n;
+        }
+        W.timer.stop(s);
+        std::vector<int> hit(nI);
+        IDP_CUDA_TRY(cudaMemcpyAsync(hit.data(), d_iters, sizeof(int) * nI, cudaMemcpyDeviceToHost, s));
+        IDP_CUDA_TRY(cudaStreamSynchronize(s));
+        for (int i = 0; i < nI; ++i)
+            if (small[i]) iters[i] = hit[i];
+    }
+    auto account = [&](const std::vector<unsigned char>& which) {
+        for (int i = 0; i < nI; ++i)
+            if (which[i]) {
+                W.stats.pcg_iters += iters[i];
+                if ((int)W.pcg_bytes_per_iter.size() == nI)
+                    W.stats.pcg_bytes += (double)iters[i] * W.pcg_bytes_per_iter[i] * (sizeof(T) / 4.0);
+            }
+    };
+    account(small);
+    if (!any_large) {
+        *xout = x;
+        return IDP_OK;
+    }
+    IDP_CUDA_TRY(cudaMemcpyAsync(A.active, large.data(), nI, cudaMemcpyHostToDevice, s));
+    (::idp::count_launch(), k_pcg_init<T><<<nc, kBlock, 0, s>>>(A.vert_chunks, A.active, dinv, A.dbc, b, x, r, z, p, part));
+    (::idp::count_launch(), k_pcg_scal_init<<<grid_for(nI), kBlock, 0, s>>>(nI, A.vert_chunk_off, A.active, part, rel_tol, S));
+    W.timer.start(PhaseTimer::PCG, s);
     const int check_every = 8;
     for (int it = 0; it < max_iters; it += check_every) {
         IDP_CUDA_TRY(cudaMemsetAsync(any, 0, sizeof(int), s));
         for (int k = 0; k < check_every; ++k) {
-            k_pcg_spmv<T><<<nc, kBlock, 0, s>>>(A.vert_chunks, S, A.rowptr, A.colidx, val, trp, tcol, tval, A.dbc, p, Ap,
-                                                part);
-            k_pcg_scal_alpha<<<grid_for(nI), kBlock, 0, s>>>(nI, A.vert_chunk_off, part, S);
-            k_pcg_update<T><<<nc, kBlock, 0, s>>>(A.vert_chunks, S, dinv, A.dbc, x, r, z, p, Ap, part);
-            k_pcg_scal_beta<<<grid_for(nI), kBlock, 0, s>>>(nI, A.vert_chunk_off, part, max_iters, S, any);
-            k_pcg_pupdate<T><<<nc, kBlock, 0, s>>>(A.vert_chunks, S, z, p);
+            (::idp::count_launch(), k_pcg_spmv<T><<<nc, kBlock, 0, s>>>(A.vert_chunks, S, A.rowptr, A.colidx, val, trp, tcol, tval, A.dbc, p, Ap,
+                                                part));
+            (::idp::count_launch(), k_pcg_scal_alpha<<<grid_for(nI), kBlock, 0, s>>>(nI, A.vert_chunk_off, part, S));
+            (::idp::count_launch(), k_pcg_update<T><<<nc, kBlock, 0, s>>>(A.vert_chunks, S, dinv, A.dbc, x, r, z, p, Ap, part));
+            (::idp::count_launch(), k_pcg_scal_beta<<<grid_for(nI), kBlock, 0, s>>>(nI, A.vert_chunk_off, part, max_iters, S, any));
+            (::idp::count_launch(), k_pcg_pupdate<T><<<nc, kBlock, 0, s>>>(A.vert_chunks, S, z, p));
         }
         int hany = 0;
         IDP_CUDA_TRY(cudaMemcpyAsync(&hany, any, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -526,9 +749,12 @@ static int pcg_inner(Arena& A, Work& W, const double* b, double rel_tol, int max
     }
     std::vector<PcgS> hs(nI);
     IDP_CUDA_TRY(cudaMemcpyAsync(hs.data(), S, sizeof(PcgS) * nI, cudaMemcpyDeviceToHost, s));
+    IDP_CUDA_TRY(cudaMemcpyAsync(A.active, act.data(), nI, cudaMemcpyHostToDevice, s));
     IDP_CUDA_TRY(cudaStreamSynchronize(s));
-    iters.resize(nI);
-    for (int i = 0; i < nI; ++i) iters[i] = hs[i].iters;
+    W.timer.stop(s);
+    for (int i = 0; i < nI; ++i)
+        if (large[i]) iters[i] = hs[i].iters;
+    account(large);
     *xout = x;
     return IDP_OK;
 }
@@ -555,13 +781,14 @@ int pcg_solve(Arena& A, Work& W, const ContactSet& cs, bool fp64, const double* 
     // |b|^2 per instance (x = 0 gives res = b)
     auto residual = [&](std::vector<double>& out) -> int {
         if (fp64)
-            k_residual64<double><<<A.n_vert_chunks, kBlock, 0, s>>>(A.vert_chunks, A.active, A.rowptr, A.colidx,
+            (::idp::count_launch(), k_residual64<double><<<grid_for(A.V, 64), 64, 0, s>>>(A.V, A.vinst, A.active, A.rowptr, A.colidx,
                                                                     W[W_BSR_VAL].as<double>(), trp, tcol,
-                                                                    W[W_TAIL_VAL].as<double>(), A.dbc, rhs, sol, res, part);
+                                                                    W[W_TAIL_VAL].as<double>(), A.dbc, rhs, sol, res));
         else
-            k_residual64<float><<<A.n_vert_chunks, kBlock, 0, s>>>(A.vert_chunks, A.active, A.rowptr, A.colidx,
+            (::idp::count_launch(), k_residual64<float><<<grid_for(A.V, 64), 64, 0, s>>>(A.V, A.vinst, A.active, A.rowptr, A.colidx,
                                                                    W[W_BSR_VAL].as<float>(), trp, tcol,
-                                                                   W[W_TAIL_VAL].as<float>(), A.dbc, rhs, sol, res, part);
+                                                                   W[W_TAIL_VAL].as<float>(), A.dbc, rhs, sol, res));
+        (::idp::count_launch(), k_norm2_chunks<<<A.n_vert_chunks, kBlock, 0, s>>>(A.vert_chunks, A.active, res, part));
         if (chunk_reduce_off(A, A.vert_chunk_off, part, inst_rr, false, s)) return IDP_ERR_CUDA;
         IDP_CUDA_TRY(cudaMemcpyAsync(out.data(), inst_rr, sizeof(double) * nI, cudaMemcpyDeviceToHost, s));
         IDP_CUDA_TRY(cudaStreamSynchronize(s));
@@ -570,7 +797,7 @@ int pcg_solve(Arena& A, Work& W, const ContactSet& cs, bool fp64, const double* 
     int rc = residual(b2);
     if (rc) return rc;
     const int max_refine = fp64 ? 1 : 8;
-    const double inner_tol = fp64 ? rel_tol : std::max(rel_tol, 1e-3);
+    const double inner_tol = fp64 ? rel_tol : std::max(rel_tol, 2e-3);
     for (int ref = 0; ref < max_refine; ++ref) {
         // instances whose FP64 residual is already small stop refining
         bool any = false;
@@ -592,12 +819,12 @@ int pcg_solve(Arena& A, Work& W, const ContactSet& cs, bool fp64, const double* 
             double* e = nullptr;
             rc = pcg_inner<double>(A, W, res, inner_tol, max_iters, its, &e, s);
             if (rc) break;
-            k_add_correction<double><<<grid_for(A.V), kBlock, 0, s>>>(A.V, A.vinst, A.active, e, sol);
+            (::idp::count_launch(), k_add_correction<double><<<grid_for(A.V), kBlock, 0, s>>>(A.V, A.vinst, A.active, e, sol));
         } else {
             float* e = nullptr;
             rc = pcg_inner<float>(A, W, res, inner_tol, max_iters, its, &e, s);
             if (rc) break;
-            k_add_correction<float><<<grid_for(A.V), kBlock, 0, s>>>(A.V, A.vinst, A.active, e, sol);
+            (::idp::count_launch(), k_add_correction<float><<<grid_for(A.V), kBlock, 0, s>>>(A.V, A.vinst, A.active, e, sol));
         }
         for (int i = 0; i < nI; ++i)
             if (act[i]) iters_out[i] += its[i];

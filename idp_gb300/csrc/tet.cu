@@ -319,16 +319,16 @@ __global__ void k_tet_hessian(long T_, const int* __restrict__ tinst, const unsi
 
 int tet_energy(Arena& A, Work& W, const double* X, double w_h2, double* inst_E, int* inst_bad, cudaStream_t s) {
     if (W[W_CHUNK_SUM].ensure(sizeof(double) * (A.n_tet_chunks + 1))) return IDP_ERR_CUDA;
-    k_tet_energy<<<A.n_tet_chunks, kBlock, 0, s>>>(A.tet_chunks, A.active, X, A.tet, A.IB, A.vol, A.lam, A.mu, w_h2,
-                                                     W[W_CHUNK_SUM].as<double>(), inst_bad);
+    (::idp::count_launch(), k_tet_energy<<<A.n_tet_chunks, kBlock, 0, s>>>(A.tet_chunks, A.active, X, A.tet, A.IB, A.vol, A.lam, A.mu, w_h2,
+                                                     W[W_CHUNK_SUM].as<double>(), inst_bad));
     return chunk_reduce(A, W, A.tet_chunks, A.n_tet_chunks, W[W_CHUNK_SUM].as<double>(), inst_E, s);
 }
 
 int tet_gradient(Arena& A, Work& W, const double* X, double w_h2, double* g_corners_unused, cudaStream_t s) {
     (void)g_corners_unused;
     if (W[W_TET_GRAD].ensure(sizeof(double) * 12 * (A.T + 1))) return IDP_ERR_CUDA;
-    k_tet_gradient<<<grid_for(A.T), kBlock, 0, s>>>(A.T, nullptr, A.active, X, A.tet, A.IB, A.vol, A.lam, A.mu, w_h2,
-                                                     W[W_TET_GRAD].as<double>());
+    (::idp::count_launch(), k_tet_gradient<<<grid_for(A.T), kBlock, 0, s>>>(A.T, nullptr, A.active, X, A.tet, A.IB, A.vol, A.lam, A.mu, w_h2,
+                                                     W[W_TET_GRAD].as<double>()));
     return cudaGetLastError() == cudaSuccess ? IDP_OK : IDP_ERR_CUDA;
 }
 
@@ -336,11 +336,11 @@ int tet_hessian(Arena& A, Work& W, const double* X, double w_h2, bool fp64, cuda
     size_t el = fp64 ? sizeof(double) : sizeof(float);
     if (W[W_TET_HESS].ensure(el * 90 * (A.T + 1))) return IDP_ERR_CUDA;
     if (fp64)
-        k_tet_hessian<double><<<grid_for(A.T, 128), 128, 0, s>>>(A.T, nullptr, A.active, X, A.tet, A.IB, A.vol, A.lam,
-                                                                  A.mu, w_h2, W[W_TET_HESS].as<double>());
+        (::idp::count_launch(), k_tet_hessian<double><<<grid_for(A.T, 128), 128, 0, s>>>(A.T, nullptr, A.active, X, A.tet, A.IB, A.vol, A.lam,
+                                                                  A.mu, w_h2, W[W_TET_HESS].as<double>()));
     else
-        k_tet_hessian<float><<<grid_for(A.T, 128), 128, 0, s>>>(A.T, nullptr, A.active, X, A.tet, A.IB, A.vol, A.lam,
-                                                                 A.mu, w_h2, W[W_TET_HESS].as<float>());
+        (::idp::count_launch(), k_tet_hessian<float><<<grid_for(A.T, 128), 128, 0, s>>>(A.T, nullptr, A.active, X, A.tet, A.IB, A.vol, A.lam,
+                                                                 A.mu, w_h2, W[W_TET_HESS].as<float>()));
     return cudaGetLastError() == cudaSuccess ? IDP_OK : IDP_ERR_CUDA;
 }
 

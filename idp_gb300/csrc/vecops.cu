@@ -69,29 +69,29 @@ __global__ void k_kappa_check(long C, const int4* __restrict__ cons, const int* 
 }  // namespace
 
 int vec_neg(long n, const double* a, double* out, cudaStream_t s) {
-    k_neg<<<grid_for(n), kBlock, 0, s>>>(n, a, out);
+    (::idp::count_launch(), k_neg<<<grid_for(n), kBlock, 0, s>>>(n, a, out));
     return cudaGetLastError() == cudaSuccess ? IDP_OK : IDP_ERR_CUDA;
 }
 
 int vec_copy_masked(Arena& A, const unsigned char* mask, const double* src, double* dst, cudaStream_t s) {
-    k_copy_masked<<<grid_for(A.V), kBlock, 0, s>>>(A.V, A.vinst, mask, src, dst);
+    (::idp::count_launch(), k_copy_masked<<<grid_for(A.V), kBlock, 0, s>>>(A.V, A.vinst, mask, src, dst));
     return cudaGetLastError() == cudaSuccess ? IDP_OK : IDP_ERR_CUDA;
 }
 
 int vec_dir_norm2(Arena& A, Work& W, const double* dir, double* inst_out, cudaStream_t s) {
     if (W[W_CHUNK_SUM].ensure(sizeof(double) * (A.n_vert_chunks + A.n_tet_chunks + 2))) return IDP_ERR_CUDA;
     double* part = W[W_CHUNK_SUM].as<double>();
-    k_dir_norm2<<<A.n_vert_chunks, kBlock, 0, s>>>(A.vert_chunks, A.active, dir, part);
+    (::idp::count_launch(), k_dir_norm2<<<A.n_vert_chunks, kBlock, 0, s>>>(A.vert_chunks, A.active, dir, part));
     return chunk_reduce_off(A, A.vert_chunk_off, part, inst_out, false, s);
 }
 
 int vec_velocity(Arena& A, const double* X, const double* Xn, double h, double* v, cudaStream_t s) {
-    k_velocity<<<grid_for(A.V), kBlock, 0, s>>>(A.V, A.vinst, A.active, X, Xn, h, v);
+    (::idp::count_launch(), k_velocity<<<grid_for(A.V), kBlock, 0, s>>>(A.V, A.vinst, A.active, X, Xn, h, v));
     return cudaGetLastError() == cudaSuccess ? IDP_OK : IDP_ERR_CUDA;
 }
 
 int vec_xtilde(Arena& A, const double* X, const double* v, double h, double* Xt, cudaStream_t s) {
-    k_xtilde<<<grid_for(A.V), kBlock, 0, s>>>(A.V, A.vinst, A.active, X, v, h, Xt);
+    (::idp::count_launch(), k_xtilde<<<grid_for(A.V), kBlock, 0, s>>>(A.V, A.vinst, A.active, X, v, h, Xt));
     return cudaGetLastError() == cudaSuccess ? IDP_OK : IDP_ERR_CUDA;
 }
 
@@ -99,7 +99,7 @@ int kappa_check(Arena& A, Work& W, const double* X, const int4* cons, const int*
                 int* inst_flag, cudaStream_t s) {
     (void)W;
     if (C <= 0) return IDP_OK;
-    k_kappa_check<<<grid_for(C), kBlock, 0, s>>>(C, cons, cinst, A.active, X, d2prev, inst_flag);
+    (::idp::count_launch(), k_kappa_check<<<grid_for(C), kBlock, 0, s>>>(C, cons, cinst, A.active, X, d2prev, inst_flag));
     return cudaGetLastError() == cudaSuccess ? IDP_OK : IDP_ERR_CUDA;
 }
 

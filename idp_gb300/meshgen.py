@@ -91,7 +91,8 @@ def bar(nx=6, ny=6, nz=24, size=(1.0, 1.0, 4.0), jitter=0.05, seed=0):
 def bend_target(X, angle=2.2 * math.pi, radius=0.5, size=(1.0, 1.0, 4.0), twist=0.0):
     """Centreline (x=sx/2, y=sy/2, z in [0,sz]) mapped onto a circle of the
     given radius spanning ``angle`` radians; cross-sections stay orthogonal to
-    the centreline (x offset -> radial, y offset -> binormal). ``twist``
+    the centreline (x offset -> radial, y offset -> -z, orientation
+    preserving). ``twist``
     rotates cross-sections by twist*s about the centreline."""
     sx, sy, sz = size
     s = X[:, 2] / sz
@@ -102,7 +103,8 @@ def bend_target(X, angle=2.2 * math.pi, radius=0.5, size=(1.0, 1.0, 4.0), twist=
         ox, oy = ox * np.cos(ph) - oy * np.sin(ph), ox * np.sin(ph) + oy * np.cos(ph)
     n = np.stack([np.cos(th), np.sin(th), np.zeros_like(th)], -1)
     r = (radius + ox)[:, None]
-    return r * n + oy[:, None] * np.array([0.0, 0.0, 1.0])
+    # (radial, -z, tangent) is right-handed, so the map keeps tet orientation
+    return r * n - oy[:, None] * np.array([0.0, 0.0, 1.0])
 
 
 def _real_sh(lmax, theta, phi):

@@ -60,7 +60,24 @@ typedef struct idp_result {
     double kappa;         /* barrier stiffness after adaptation (kappaVec[0])       */
     double residual;      /* last Newton residual                                   */
     double min_alpha;     /* smallest accepted line-search step                     */
+    double latency_ms;    /* host time from the start of idp_advance until this
+                             instance stopped iterating                             */
 } idp_result;
+
+/* Device-time accounting of the last idp_advance (CUDA events on the
+ * context's stream; no counterpart in the reference, whose TIMER_FLAG scopes,
+ * Utils/PROFILER.h:66-105,175-201, time the same phases on the host). */
+typedef struct idp_stats {
+    double pcg_ms;          /* PCG kernels                                        */
+    double pcg_bytes;       /* algorithmic bytes of those PCG iterations          */
+    long long pcg_iters;    /* PCG iterations, summed over instances              */
+    int pcg_launches;       /* PCG kernel launches                                */
+    double tet_ms;          /* elastic energy / gradient / Hessian kernels        */
+    double contact_ms;      /* constraint-set builds                              */
+    double ccd_ms;          /* CCD step-size evaluations                          */
+    double total_ms;        /* the whole idp_advance                              */
+    long long kernel_launches; /* kernels this library launched in idp_advance    */
+} idp_stats;
 
 /* Defaults: h=0.1, newton_tol=1e-3, max_newton=2000, mode=MIXED,
    pcg_rel_tol=1e-6, pcg_max_iters=2000, thickness=0, device=0. */
@@ -102,6 +119,16 @@ int idp_commit(idp_ctx* ctx);
  * (FEM/Shell/DISCRETE_SHELL.h:1110 -> IMPLICIT_EULER.h:151-891).
  * results: array of idp_result, one per instance (may be NULL). */
 int idp_advance(idp_ctx* ctx, idp_result* results);
+
+/* Device-side checkpoint of every instance's positions, velocity and kappa
+ * (the reference restarts from OBJ files instead,
+ * Python/Drivers/FEMDiscreteShellBase.py:244-253). Restore copies it back
+ * device to device. */
+int idp_save_state(idp_ctx* ctx);
+int idp_restore_state(idp_ctx* ctx);
+
+/* Stats of the last idp_advance (zeros before the first). */
+int idp_get_stats(idp_ctx* ctx, idp_stats* out);
 
 /* Read back positions X (3V), velocity v (3V) and kappa[3] of one instance. */
 int idp_get_state(idp_ctx* ctx, int inst, double* X, double* v, double* kappa3);

@@ -156,6 +156,38 @@ void deformation_gradient(const double* X, const int* t, const double* IB, doubl
         for (int j = 0; j < 3; ++j) F[i * 3 + j] = Ds[i * 3 + 0] * IB[0 * 3 + j] + Ds[i * 3 + 1] * IB[1 * 3 + j] + Ds[i * 3 + 2] * IB[2 * 3 + j];
 }
 
+// Fixed-order sum used for the two means of the CCD hash (mean edge length,
+// mean |dir|). The reference takes them with Eigen's mean() and a serial loop
+// (SPATIAL_HASH.h:455-475); this restatement fixes one order that a GPU can
+// reproduce: tiles of 2048 items, item t of a 256-lane tile sums items
+// t, t+256, ..., t+1792 in turn, then lanes are added pairwise with strides
+// 128, 64, ..., 1; tile sums are reduced the same way until one is left.
+double det_sum(const double* x, long n) {
+    if (n <= 0) return 0.0;
+    std::vector<double> cur(x, x + n);
+    while (true) {
+        long m = (long)cur.size();
+        long tiles = (m + 2047) / 2048;
+        std::vector<double> nxt(tiles);
+        for (long k = 0; k < tiles; ++k) {
+            double a[256];
+            for (int t = 0; t < 256; ++t) {
+                double s = 0.0;
+                for (int r = 0; r < 8; ++r) {
+                    long i = k * 2048 + r * 256 + t;
+                    if (i < m) s += cur[i];
+                }
+                a[t] = s;
+            }
+            for (int st = 128; st > 0; st >>= 1)
+                for (int t = 0; t < st; ++t) a[t] += a[t + st];
+            nxt[k] = a[0];
+        }
+        if (tiles == 1) return nxt[0];
+        cur.swap(nxt);
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Spatial hash, restating Grid/SPATIAL_HASH.h
 // ---------------------------------------------------------------------------
@@ -284,18 +316,14 @@ struct SpatialHash {
                    const double* dir, double& curMaxStepSize, double thickness) {
         double voxelSize = 1.0;
         if (nE) {
-            double s = 0;
-            for (int e = 0; e < nE; ++e) s += std::sqrt(sq(v3(X + 3 * edges[2 * e]) - v3(X + 3 * edges[2 * e + 1])));
-            voxelSize *= s / nE;
+            std::vector<double> len(nE);
+            for (int e = 0; e < nE; ++e) len[e] = std::sqrt(sq(v3(X + 3 * edges[2 * e]) - v3(X + 3 * edges[2 * e + 1])));
+            voxelSize *= det_sum(len.data(), nE) / (double)nE;
         }
-        double pSize = 0;
-        for (int s = 0; s < nN; ++s) {
-            int v = nodes[s];
-            pSize += std::fabs(dir[3 * v]);
-            pSize += std::fabs(dir[3 * v + 1]);
-            pSize += std::fabs(dir[3 * v + 2]);
-        }
-        pSize /= (double)nN * 3;
+        std::vector<double> ad(3 * (size_t)nN);
+        for (int s = 0; s < nN; ++s)
+            for (int d = 0; d < 3; ++d) ad[3 * s + d] = std::fabs(dir[3 * nodes[s] + d]);
+        double pSize = det_sum(ad.data(), 3L * nN) / (double)(nN * 3);
         double spanSize = curMaxStepSize * pSize / voxelSize;
         if (spanSize > 1) curMaxStepSize /= spanSize;
 

@@ -40,7 +40,7 @@ def contact_configs():
         out.append((f"two_bars_{seed}", X, tets, X, 5e-3))
     X0, tets, Xd = cases.folded_bar(seed=0, frac=1.0)
     out.append(("folded_overlap_far", X0, tets, Xd, 0.08))
-    X0, tets, Xd = cases.folded_bar(seed=1, n=(2, 2, 8), frac=0.97)
+    X0, tets, Xd = cases.folded_bar(seed=1, n=(2, 2, 8), frac=0.97, radius=1.0)
     out.append(("folded_near", X0, tets, Xd, 0.05))
     return out
 
