@@ -1,25 +1,35 @@
 """Benchmark of the injective-deformation Newton step on GB300.
 
-Default workload (the one the benchmark spec's target is quoted on): 256
-independent bars, tet counts log-uniform in [1k, 50k], bend angles uniform in
-[1.5pi, 2.5pi], jitter 0.05h, all in one device arena (BASELINE config 3).
-A step is one implicit-Euler solve of every bar (Newton to convergence with
-CCD-filtered line search): ``idp_advance``.
+Default workload ``blob`` (single large normal-flow solve): a closed bumpy
+blob r(u) = 1 + 0.3 * sum_{l<=8} c_lm Y_lm (c ~ N(0, 1/l^2), seed 0),
+tetrahedralised on a 64^3 background grid (220,515 tets, 49,863 vertices).
+A step is one normal-flow solve: every surface vertex's predictor moves by
+0.05 along its area-weighted outward normal, interior vertices are held
+(x_tilde = x), and idp_advance runs Newton to convergence with the IPC
+barrier, CCD-filtered line search and the mixed-precision PCG. W warm-up
+steps and K timed steps continue one flow sequence (20 steps for K=17, W=3).
 
-* value: solves/s with inputs resident in HBM (device snapshot restored
-  device-to-device before each step); time = the library's CUDA-event time of
-  idp_advance on its own stream.
-* e2e: the same through the public API with host buffers: pinned positions
-  and velocities uploaded, the step solved, positions read back, all inside
+* value: solves/s with the state resident in HBM; time = the library's
+  CUDA-event time of each step on its own stream, summed over the K steps.
+* fp64: the same K steps re-solved in FP64 mode from the identical start
+  states (positions, velocity, kappa); its solves/s and the relative energy
+  difference mixed vs FP64 are reported per run.
+* e2e: the same K steps through the public API with host buffers: pinned
+  positions uploaded, normal flow set, solved, positions read back, all in
   the timed region (host wall clock around synchronous calls).
-* roofline: the persistent PCG kernel (dominant), algorithmic bytes per
-  launch / event time, against MEASURED_PEAKS.json hbm_gbs.
-* cpu_baseline: the CPU oracle (FP64, scipy sparse LU) on a bounded sample,
-  extrapolated to the batch by tet count.
+* roofline: the cluster PCG kernel (dominant), algorithmic bytes per launch /
+  event time, against MEASURED_PEAKS.json hbm_gbs.
+* cpu_baseline: the CPU oracle (FP64, sparse LU) running the first flow step
+  of the same blob at 24^3 resolution (bounded sample), solves/s scaled to
+  the full blob by tet count.
 
-``--impl reference`` times the reference's CPU path (here the oracle port,
-because the reference does not build in this environment) on the same
-metric, one bounded sample per step.
+``--workload batch256`` (256 bars, tet counts log-uniform in [1k, 50k]) and
+``--workload bar`` (6x6x24 bar, bend 2.2pi) time one batched solve per step
+from a restored device snapshot instead.
+
+``--impl reference`` times the reference's CPU path (the oracle port: the
+reference does not build in this environment) on the same metric, one
+bounded sample per step.
 """
 from __future__ import annotations
 
@@ -43,10 +53,13 @@ UNIT = "solves/s"
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=17)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="batch256", choices=["batch256", "bar"])
+    ap.add_argument("--workload", default="blob", choices=["blob", "batch256", "bar"])
+    ap.add_argument("--blob-n", type=int, default=64)
+    ap.add_argument("--flow-step", type=float, default=0.05)
+    ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--instances", type=int, default=256)
     ap.add_argument("--mode", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--max-newton", type=int, default=2000)
@@ -191,16 +204,218 @@ def cpu_baseline(probs, budget_s):
                       f"iterations, {t_used:.1f} s); solves/s scaled to the mean instance ({mean_tets:.0f} tets)"}
 
 
+H = 0.1
+
+
+def blob_problem(n, seed=0):
+    import numpy as np
+    from idp_gb300 import meshgen
+    from idp_gb300.api import initialize_oipc
+
+    X, tets, _ = meshgen.blob(n=n, lmax=8, amp=0.3, seed=seed)
+    mass = meshgen.lumped_mass(X, tets, 1000.0)
+    lam, mu = meshgen.lame(1e4, 0.3)
+    dHat2 = (1e-3 * float(np.linalg.norm(X.max(0) - X.min(0)))) ** 2
+    k, km = initialize_oipc(float(mass.mean()), dHat2)
+    return dict(X=X, tets=tets, mass=mass, lam=lam, mu=mu, dHat2=dHat2, kappa=k, kappa_max=km)
+
+
+def blob_desc(p, n, step):
+    return (f"blob_normal_flow: SH blob lmax 8 amp 0.3 seed 0 on {n}^3 grid ({p['tets'].shape[0]} tets, "
+            f"{p['X'].shape[0]} verts), surface x_tilde = x + {step} n, interior x_tilde = x, h=0.1, "
+            f"E=1e4 nu=0.3 rho=1e3, dhat=1e-3 bbox diag")
+
+
+def cpu_baseline_flow(full_tets, step, budget_s, n_small=24):
+    """Oracle (FP64, direct solve) running the first normal-flow step of the
+    same blob at n_small^3 resolution, repeated while the budget lasts;
+    solves/s scaled to the full blob by tet count (linear, which favours the
+    CPU: its sparse LU grows faster than linearly)."""
+    import numpy as np
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    O.build()
+    p = blob_problem(n_small)
+    T = p["tets"].shape[0]
+    surf = O.surface(p["X"], p["tets"])
+    v = O.normal_flow_velocity(p["X"], surf["tris"], step, H)
+    t_used, solves, iters = 0.0, 0, 0
+    while True:
+        pb = O.Problem(X=p["X"].copy(), X0=p["X"], tets=p["tets"], mass=p["mass"], lam=np.full(T, p["lam"]),
+                       mu=np.full(T, p["mu"]), h=H, dHat2=p["dHat2"], kappa=[p["kappa"], p["kappa_max"], 0.0],
+                       v=v.copy(), tol=1e-3, max_iters=500)
+        t0 = time.perf_counter()
+        iters += O.advance_one_step(pb)
+        t_used += time.perf_counter() - t0
+        solves += 1
+        if t_used >= budget_s:
+            break
+    rate = solves * T / t_used / full_tets
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    return {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"oracle first flow step of the blob at {n_small}^3 ({T} tets), {solves} solve(s), {iters} "
+                      f"Newton iterations, {t_used:.1f} s; solves/s scaled to {full_tets} tets by tet count"}
+
+
+def run_flow(args):
+    import numpy as np
+    import torch
+    import idp_gb300 as idp
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    mode = idp.MODE_MIXED if args.mode == "mixed" else idp.MODE_FP64
+    # replicas: every rank runs its own blob (seeded by rank)
+    p = blob_problem(args.blob_n, seed=rank)
+    desc = blob_desc(p, args.blob_n, args.flow_step)
+    V = p["X"].shape[0]
+
+    def make_ctx(m):
+        c = idp.Context(h=H, newton_tol=1e-3, max_newton=args.max_newton, mode=m, device=local)
+        c.add_instance(p["X"], p["tets"], p["mass"], p["lam"], p["mu"], p["dHat2"], p["kappa"], p["kappa_max"])
+        c.commit()
+        return c
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    ctx = make_ctx(mode)
+    for _ in range(args.warmup):
+        ctx.set_normal_flow(0, args.flow_step)
+        ctx.advance(check=False)
+    # start states of the timed steps (host copies taken outside the device
+    # time of each step; they let the FP64 and e2e passes redo the same work)
+    starts = []
+    dev_ms, wall, results = [], [], []
+    launches = 0
+    pcg_ms = pcg_bytes = 0.0
+    phase = {k: 0.0 for k in ("pcg_ms", "tet_ms", "contact_ms", "ccd_ms")}
+    barrier()
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            starts.append(ctx.state(0))
+            t0 = time.perf_counter()
+            ctx.set_normal_flow(0, args.flow_step)
+            rc, res = ctx.advance(check=False)
+            wall.append(time.perf_counter() - t0)
+            st = ctx.stats()
+            dev_ms.append(st["total_ms"])
+            pcg_ms += st["pcg_ms"]
+            pcg_bytes += st["pcg_bytes"]
+            launches += st["kernel_launches"] + 1
+            for k in phase:
+                phase[k] += st[k]
+            results.append(res[0])
+    barrier()
+    total_ms = sum(dev_ms)
+    if world > 1:
+        t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * args.steps / (total_ms / 1000.0)
+
+    # ---- FP64 arm from the same start states
+    fp64 = None
+    if not args.no_fp64 and mode == idp.MODE_MIXED:
+        cd = make_ctx(idp.MODE_FP64)
+        d_ms, rel = [], []
+        for k, (Xs, vs, ks) in enumerate(starts):
+            cd.set_positions(0, Xs)
+            cd.set_kappa(0, ks)
+            cd.set_normal_flow(0, args.flow_step)
+            _, rd = cd.advance(check=False)
+            d_ms.append(cd.stats()["total_ms"])
+            Em, Ed = results[k]["energy"], rd[0]["energy"]
+            rel.append(abs(Em - Ed) / max(abs(Ed), 1e-300))
+        fp64 = {"solves_per_s": len(d_ms) / (sum(d_ms) / 1000.0), "ms_per_step": statistics.mean(d_ms),
+                "rel_energy_err_max": max(rel), "rel_energy_err_mean": statistics.mean(rel),
+                "mixed_speedup": (sum(d_ms) / total_ms) if total_ms > 0 else None}
+        cd.close()
+
+    # ---- end to end through the public API with pinned host buffers
+    Xh = [torch.from_numpy(np.ascontiguousarray(Xs)).pin_memory() for Xs, _, _ in starts]
+    Xo = torch.empty_like(Xh[0]).pin_memory()
+    e2e_wall = []
+    for k, (Xs, vs, ks) in enumerate(starts):
+        ctx.set_kappa(0, ks)
+        barrier()
+        t0 = time.perf_counter()
+        ctx.set_positions_ptr(0, Xh[k].data_ptr())
+        ctx.set_normal_flow(0, args.flow_step)
+        ctx.advance(check=False)
+        ctx.state_ptr(0, Xo.data_ptr())
+        e2e_wall.append(time.perf_counter() - t0)
+    e2e_s = sum(e2e_wall)
+    if world > 1:
+        t = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_val = world * len(e2e_wall) / e2e_s
+    if rank != 0:
+        return
+    peak, peak_kind = measured_peak()
+    achieved = (pcg_bytes / (pcg_ms / 1000.0) / 1e9) if pcg_ms > 0 else None
+    traffic = ncu_traffic()
+    lat = [r["latency_ms"] for r in results]
+    newton = [r["newton_iters"] for r in results]
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+f64" if mode == idp.MODE_MIXED else "f64", "data": "synthetic",
+        "config": {"workload": desc, "tets": int(p["tets"].shape[0]), "verts": V, "mode": args.mode,
+                   "parallelism": f"replicas{world}",
+                   "l2": "working set larger than L2 (BSR + tet data + vectors > 129 MB); no flush"},
+        "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
+        "newton_iters": {"mean": float(np.mean(newton)), "max": int(np.max(newton)), "total": int(np.sum(newton))},
+        "status": sorted({int(r["status"]) for r in results}),
+        "phase_ms_per_step": {k: v / args.steps for k, v in phase.items()},
+        "fp64": fp64,
+        "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": 3 * V * 8, "d2h_bytes_per_step": 3 * V * 8},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": (achieved / peak) if achieved else None,
+                     "traffic": traffic.get("bytes_per_launch") if traffic else None,
+                     "kernel": "k_pcg_cluster (thread-block-cluster PCG, FP32 BSR SpMV + block-Jacobi)",
+                     "peak_source": peak_kind},
+        "gpu_launches": launches,
+        "clocks": clocks.summary(),
+        "wall_ms_per_step": 1000 * statistics.mean(wall),
+    }
+    if not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline_flow(int(p["tets"].shape[0]), args.flow_step, args.cpu_sample_s)
+    print(json.dumps(out), flush=True)
+
+
 def run_reference(args):
     rank, world, local = dist_env()
     if rank != 0:
         return
-    probs, desc = make_workload(args, seed=0)
     vals = []
     bl = None
-    for _ in range(args.warmup + args.steps):
-        bl = cpu_baseline(probs, args.cpu_sample_s)
-        vals.append(bl["value"])
+    if args.workload == "blob":
+        import numpy as np
+        from idp_gb300 import meshgen
+
+        X, tets, _ = meshgen.blob(n=args.blob_n, lmax=8, amp=0.3, seed=0)
+        probs = [dict(X=X, tets=tets)]
+        desc = blob_desc(probs[0], args.blob_n, args.flow_step)
+        # every step is one bounded sample; the whole run stays near 2.5 min
+        per_step = min(args.cpu_sample_s, 150.0 / max(1, args.warmup + args.steps))
+        for _ in range(args.warmup + args.steps):
+            bl = cpu_baseline_flow(int(tets.shape[0]), args.flow_step, per_step)
+            vals.append(bl["value"])
+    else:
+        probs, desc = make_workload(args, seed=0)
+        for _ in range(args.warmup + args.steps):
+            bl = cpu_baseline(probs, args.cpu_sample_s)
+            vals.append(bl["value"])
     v = statistics.mean(vals[args.warmup:]) if args.steps else vals[-1]
     out = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / v if v else None,
@@ -332,6 +547,8 @@ def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "blob":
+        run_flow(args)
     else:
         run_gpu(args)
 

@@ -35,13 +35,14 @@ EXPORTS = [
     "idp_set_positions", "idp_commit", "idp_advance", "idp_get_state", "idp_instance_info", "idp_get_surface",
     "idp_eval_energy", "idp_eval_gradient", "idp_constraint_set", "idp_ccd_stepsize", "idp_hessian_apply",
     "idp_newton_direction", "idp_get_stats", "idp_save_state", "idp_restore_state",
+    "idp_set_normal_flow", "idp_set_kappa",
 ]
 
 
 class Params(C.Structure):
     _fields_ = [("h", C.c_double), ("newton_tol", C.c_double), ("max_newton", C.c_int), ("mode", C.c_int),
                 ("pcg_rel_tol", C.c_double), ("pcg_max_iters", C.c_int), ("thickness", C.c_double),
-                ("device", C.c_int)]
+                ("device", C.c_int), ("pcg_grid_min_vertices", C.c_int), ("pcg_grid_cta_vertices", C.c_int)]
 
 
 class Result(C.Structure):
@@ -92,6 +93,8 @@ def load(path: str | None = None):
                                    C.c_double, C.c_double, C.c_double]
     L.idp_set_velocity.argtypes = [C.c_void_p, C.c_int, _dp]
     L.idp_set_positions.argtypes = [C.c_void_p, C.c_int, _dp]
+    L.idp_set_normal_flow.argtypes = [C.c_void_p, C.c_int, C.c_double]
+    L.idp_set_kappa.argtypes = [C.c_void_p, C.c_int, _dp]
     L.idp_commit.argtypes = [C.c_void_p]
     L.idp_advance.argtypes = [C.c_void_p, C.POINTER(Result)]
     L.idp_get_state.argtypes = [C.c_void_p, C.c_int, _dp, _dp, _dp]
@@ -187,6 +190,17 @@ class Context:
     def set_velocity(self, i, v):
         v = _f64(v)
         self._check(load().idp_set_velocity(self._h, i, _pd(v)), "idp_set_velocity")
+
+    def set_normal_flow(self, i, step):
+        """x_tilde = x + step * n on surface vertices, x_tilde = x inside
+        (instance i, or every instance for i = -1)."""
+        self._check(load().idp_set_normal_flow(self._h, int(i), C.c_double(step)), "idp_set_normal_flow")
+
+    def set_kappa(self, i, kappa3):
+        k = np.ascontiguousarray(np.asarray(kappa3, dtype=np.float64).reshape(-1)[:3])
+        if k.size < 3:
+            k = np.concatenate([k, np.zeros(3 - k.size)])
+        self._check(load().idp_set_kappa(self._h, int(i), _pd(k)), "idp_set_kappa")
 
     def set_positions(self, i, X):
         X = _f64(X)

@@ -15,6 +15,8 @@
 // pair either finishes below the bound with its own toc, or is discarded), so
 // alpha = min(capped alpha, min over pairs) is exact. ACCD loops carry an
 // iteration cap; a capped pair reports its accumulated (still safe) toc.
+#include <cstdlib>
+#include <algorithm>
 #include "engine.hpp"
 #include "grid.cuh"
 #include "geom.cuh"
@@ -27,6 +29,9 @@ using namespace geo;
 namespace {
 
 constexpr int ACCD_MAX_ITERS = 200000;
+// diagnostics (read back when IDP_PROFILE is set): longest ACCD loop,
+// pairs above 1000 iterations, total iterations, pairs
+__device__ unsigned long long g_accd_stats[4];
 
 // fixed-order sum by one CTA of 256 threads (same tiling as det_sum)
 __device__ double cta_det_sum(const double* x, long n, double* scratch) {
@@ -375,7 +380,7 @@ __global__ void k_ccd_query_ee(long nE, const int2* __restrict__ edges, const in
 
 // ---- ACCD (CCD.h:279-328, 330-395)
 __device__ int accd_pt(D3 p, D3 t0, D3 t1, D3 t2, D3 dp, D3 dt0, D3 dt1, D3 dt2, double eta, double thickness,
-                       double& toc) {
+                       double& toc, int& its) {
     D3 mov = 0.25 * (((dt0 + dt1) + dt2) + dp);
     dt0 = dt0 - mov; dt1 = dt1 - mov; dt2 = dt2 - mov; dp = dp - mov;
     double m2 = fmax(sqn(dt0), fmax(sqn(dt1), sqn(dt2)));
@@ -387,7 +392,7 @@ __device__ int accd_pt(D3 p, D3 t0, D3 t1, D3 t2, D3 dp, D3 dt0, D3 dt1, D3 dt2,
     double gap = eta * (dist2_cur - th2) / (dist_cur + thickness);
     double toc_prev = toc;
     toc = 0;
-    for (int it = 0; it < ACCD_MAX_ITERS; ++it) {
+    for (its = 0; its < ACCD_MAX_ITERS; ++its) {
         double tocLB = (1 - eta) * (dist2_cur - th2) / ((dist_cur + thickness) * maxDispMag);
         p = p + tocLB * dp; t0 = t0 + tocLB * dt0; t1 = t1 + tocLB * dt1; t2 = t2 + tocLB * dt2;
         dist2_cur = d_PT_unclassified(p, t0, t1, t2);
@@ -409,7 +414,7 @@ __device__ __forceinline__ void ee_eval(D3 ea0, D3 ea1, D3 eb0, D3 eb1, double t
 }
 
 __device__ int accd_ee(D3 ea0, D3 ea1, D3 eb0, D3 eb1, D3 dea0, D3 dea1, D3 deb0, D3 deb1, double eta,
-                       double thickness, double& toc) {
+                       double thickness, double& toc, int& its) {
     D3 mov = 0.25 * (((dea0 + dea1) + deb0) + deb1);
     dea0 = dea0 - mov; dea1 = dea1 - mov; deb0 = deb0 - mov; deb1 = deb1 - mov;
     double maxDispMag = sqrt(fmax(sqn(dea0), sqn(dea1))) + sqrt(fmax(sqn(deb0), sqn(deb1)));
@@ -421,7 +426,7 @@ __device__ int accd_ee(D3 ea0, D3 ea1, D3 eb0, D3 eb1, D3 dea0, D3 dea1, D3 deb0
     double gap = eta * dFunc / (dist_cur + thickness);
     double toc_prev = toc;
     toc = 0;
-    for (int it = 0; it < ACCD_MAX_ITERS; ++it) {
+    for (its = 0; its < ACCD_MAX_ITERS; ++its) {
         double tocLB = (1 - eta) * dFunc / ((dist_cur + thickness) * maxDispMag);
         ea0 = ea0 + tocLB * dea0; ea1 = ea1 + tocLB * dea1; eb0 = eb0 + tocLB * deb0; eb1 = eb1 + tocLB * deb1;
         ee_eval(ea0, ea1, eb0, eb1, th2, dist2_cur, dFunc);
@@ -444,24 +449,34 @@ __global__ void k_accd(long npt, long nee, const CCand* __restrict__ cand, const
     CCand c = cand[k];
     int inst;
     double toc;
-    int r;
+    int r, its = 0;
     if (k < npt) {
         int v = nodes[c.a];
         inst = ninst[c.a];
         int t0 = tris[3 * c.b], t1 = tris[3 * c.b + 1], t2 = tris[3 * c.b + 2];
         toc = alpha_cap[inst];
         r = accd_pt(ld3(X, v), ld3(X, t0), ld3(X, t1), ld3(X, t2), ld3(dir, v), ld3(dir, t0), ld3(dir, t1),
-                    ld3(dir, t2), 0.1, thick[inst], toc);
+                    ld3(dir, t2), 0.1, thick[inst], toc, its);
         if (toc == 0) atomicOr(flags + inst, 2);
     } else {
         int2 mi = edges[c.a], mj = edges[c.b];
         inst = einst[c.a];
         toc = alpha_cap[inst];
         r = accd_ee(ld3(X, mi.x), ld3(X, mi.y), ld3(X, mj.x), ld3(X, mj.y), ld3(dir, mi.x), ld3(dir, mi.y),
-                    ld3(dir, mj.x), ld3(dir, mj.y), 0.1, thick[inst], toc);
+                    ld3(dir, mj.x), ld3(dir, mj.y), 0.1, thick[inst], toc, its);
     }
     if (r == 2) atomicOr(flags + inst, 1);
     if (r != 0) atomic_min_nonneg(alpha_min + inst, toc);
+    const unsigned int am = __activemask();
+    const unsigned int mx = __reduce_max_sync(am, (unsigned int)its);
+    const unsigned int nl = __reduce_add_sync(am, its > 1000 ? 1u : 0u);
+    const unsigned int tot = __reduce_add_sync(am, (unsigned int)its);
+    if ((threadIdx.x & 31) == __ffs(am) - 1) {
+        atomicMax(&g_accd_stats[0], (unsigned long long)mx);
+        atomicAdd(&g_accd_stats[1], (unsigned long long)nl);
+        atomicAdd(&g_accd_stats[2], (unsigned long long)tot);
+        atomicAdd(&g_accd_stats[3], (unsigned long long)__popc(am));
+    }
 }
 
 __global__ void k_alpha_final(int nI, const unsigned char* __restrict__ active, const double* __restrict__ amin,
@@ -565,6 +580,18 @@ int ccd_stepsize(Arena& A, Work& W, const double* X, const double* dir, double* 
                 (::idp::count_launch(), k_accd<<<grid_for(npt + nee, 128), 128, 0, s>>>(npt, nee, cand, A.snode, A.sn_inst, A.stri, A.sedge,
                                                                 A.se_inst, X, dir, A.thickness, alpha, amin, flags));
             (::idp::count_launch(), k_alpha_final<<<grid_for(nI), kBlock, 0, s>>>(nI, A.active, amin, alpha));
+            if (std::getenv("IDP_PROFILE")) {
+                unsigned long long st[4] = {0, 0, 0, 0};
+                void* sym = nullptr;
+                IDP_CUDA_TRY(cudaGetSymbolAddress(&sym, g_accd_stats));
+                IDP_CUDA_TRY(cudaMemcpyAsync(st, sym, sizeof(st), cudaMemcpyDeviceToHost, s));
+                IDP_CUDA_TRY(cudaMemsetAsync(sym, 0, sizeof(st), s));
+                IDP_CUDA_TRY(cudaStreamSynchronize(s));
+                W.accd_maxit = std::max<long long>(W.accd_maxit, (long long)st[0]);
+                W.accd_long += (long long)st[1];
+                W.accd_total += (long long)st[2];
+                W.accd_pairs += (long long)st[3];
+            }
             return cudaGetLastError() == cudaSuccess ? IDP_OK : IDP_ERR_CUDA;
         }
         cap = 2 * (npt + nee) + 1024;

@@ -43,6 +43,8 @@ constexpr int kChunk = 1024;
 // instances up to this many vertices run PCG in one persistent thread-block
 // cluster; larger ones use the multi-launch path
 constexpr long kClusterPcgMaxV = 262144;
+// vertices per dense contact-cluster block of the preconditioner (576 x 576)
+constexpr int kClusterCap = 192;
 
 // ---- small vector math (templated so FP32 and FP64 paths share code)
 template <class T>

@@ -166,7 +166,7 @@ void build_chunks(const std::vector<int>& off, std::vector<Chunk>& ch, std::vect
 }
 
 // per-instance device scalar layout inside ctx->inst_buf
-enum { S_ETET, S_EINERT, S_EBAR, S_MIND, S_NORM2, S_NUMD };
+enum { S_ETET, S_EINERT, S_EBAR, S_MIND, S_NORM2, S_TOL, S_NUMD };
 enum { SI_BAD, SI_BADB, SI_KFLAG, SI_CCDF, S_NUMI };
 
 double* dsc(idp_ctx* c, int k) { return c->inst_buf.as<double>() + (long)k * c->A.nI; }
@@ -250,6 +250,7 @@ int eval_hessian(idp_ctx* c, const double* X) {
     if (rc) return rc;
     c->W.timer.start(PhaseTimer::ASSEMBLY, c->s);
     rc = assemble(A, c->W, c->cs, fp64, c->s);
+    if (!rc) rc = build_contact_clusters(A, c->W, c->cs, fp64, c->s);
     c->W.timer.stop(c->s);
     return rc;
 }
@@ -288,6 +289,8 @@ void idp_default_params(idp_params* p) {
     p->pcg_max_iters = 2000;
     p->thickness = 0.0;
     p->device = 0;
+    p->pcg_grid_min_vertices = 0;
+    p->pcg_grid_cta_vertices = 0;
 }
 
 const char* idp_status_str(int s) {
@@ -315,6 +318,8 @@ idp_ctx* idp_create(const idp_params* p, int* status) {
     idp_ctx* c = new idp_ctx();
     if (p) c->P = *p;
     else idp_default_params(&c->P);
+    c->W.grid_min_v = c->P.pcg_grid_min_vertices > 0 ? c->P.pcg_grid_min_vertices : 16384;
+    c->W.grid_vper = c->P.pcg_grid_cta_vertices > 0 ? c->P.pcg_grid_cta_vertices : 128;
     if (cudaSetDevice(c->P.device) != cudaSuccess || cudaStreamCreateWithFlags(&c->s, cudaStreamNonBlocking) != cudaSuccess) {
         delete c;
         if (status) *status = IDP_ERR_CUDA;
@@ -384,6 +389,17 @@ int idp_set_velocity(idp_ctx* c, int i, const double* v) {
         IDP_CUDA_TRY(cudaMemcpyAsync(c->vel.as<double>() + o, v, sizeof(double) * 3 * h.V, cudaMemcpyHostToDevice, c->s));
         IDP_CUDA_TRY(cudaStreamSynchronize(c->s));
     }
+    return IDP_OK;
+}
+
+int idp_set_normal_flow(idp_ctx* c, int i, double step) {
+    if (!c || i < -1 || i >= (int)c->inst.size() || !std::isfinite(step)) return IDP_ERR_INVALID_ARG;
+    if (!c->committed) return IDP_ERR_STATE;
+    cudaSetDevice(c->P.device);
+    if (c->A.nI == 0) return IDP_OK;
+    int rc = normal_flow_velocity(c->A, i, step, c->P.h, c->vel.as<double>(), c->s);
+    if (rc) return rc;
+    IDP_CUDA_TRY(cudaStreamSynchronize(c->s));
     return IDP_OK;
 }
 
@@ -576,6 +592,15 @@ int idp_commit(idp_ctx* c) {
         }
         rc |= upload(c, A.vert_corner_ptr, vcp);
         rc |= upload(c, A.vert_corner, vc);
+        // vertex -> incident surface triangles, ascending (normal-flow sums)
+        std::vector<int> vtp(A.V + 1, 0), vt(stri.size());
+        for (size_t k = 0; k < stri.size(); ++k) vtp[stri[k] + 1]++;
+        for (long v = 0; v < A.V; ++v) vtp[v + 1] += vtp[v];
+        std::vector<int> vfill(vtp.begin(), vtp.end() - 1);
+        for (size_t f = 0; f < stri.size() / 3; ++f)
+            for (int a = 0; a < 3; ++a) vt[vfill[stri[3 * f + a]]++] = (int)f;
+        rc |= upload(c, A.vtri_ptr, vtp);
+        rc |= upload(c, A.vtri, vt);
     }
     // algorithmic bytes of one FP32 PCG iteration per instance: BSR values
     // and column ids once, and ~7 vector reads/writes plus the 3x3
@@ -591,6 +616,11 @@ int idp_commit(idp_ctx* c) {
         }
     }
     if (c->inst_buf.ensure(sizeof(double) * (S_NUMD + S_NUMI) * (nI + 1))) rc = IDP_ERR_CUDA;
+    else {
+        c->W.tol_inst = dsc(c, S_TOL);
+        std::vector<double> tl(nI, c->P.pcg_rel_tol);
+        rc |= cudaMemcpy(c->W.tol_inst, tl.data(), sizeof(double) * nI, cudaMemcpyHostToDevice) != cudaSuccess;
+    }
     if (c->vel.ensure(sizeof(double) * 3 * (A.V + 1))) rc = IDP_ERR_CUDA;
     else if (cudaMemcpy(c->vel.p, vel.data(), sizeof(double) * 3 * A.V, cudaMemcpyHostToDevice) != cudaSuccess)
         rc = IDP_ERR_CUDA;
@@ -672,6 +702,21 @@ int idp_advance(idp_ctx* c, idp_result* results) {
         if ((rc = set_mask(c, mask))) return rc;
         // ---- gradient, Hessian, direction
         if ((rc = eval_gradient(c, A.X))) return rc;
+        // inexact Newton: PCG tolerance per instance follows |g| / |g_0|
+        // (tight near convergence, where the step-length test is decided)
+        if ((rc = vec_dir_norm2(A, W, A.g, dsc(c, S_NORM2), s))) return rc;
+        if ((rc = fetch(c, dsc(c, S_NORM2), hv))) return rc;
+        std::vector<double> tol(nI, c->P.pcg_rel_tol);
+        {
+            for (int i = 0; i < nI; ++i) {
+                if (!mask[i]) continue;
+                double gn = std::sqrt(hv[i]);
+                if (st[i].iters == 0 || !(st[i].g0 > 0)) st[i].g0 = gn;
+                double eta = st[i].g0 > 0 ? gn / st[i].g0 : 1.0;
+                tol[i] = std::max(c->P.pcg_rel_tol, std::min(1e-2, eta));
+            }
+            IDP_CUDA_TRY(cudaMemcpyAsync(W.tol_inst, tol.data(), sizeof(double) * nI, cudaMemcpyHostToDevice, s));
+        }
         if ((rc = vec_neg(3 * A.V, A.g, A.g, s))) return rc;  // rhs = -g
         std::vector<unsigned char> newton(nI, 0), gd(nI, 0);
         bool any_newton = false, any_gd = false;
@@ -685,7 +730,8 @@ int idp_advance(idp_ctx* c, idp_result* results) {
             if ((rc = eval_hessian(c, A.X))) return rc;
             std::vector<int> its;
             std::vector<double> rel;
-            if ((rc = pcg_solve(A, W, c->cs, fp64, A.g, A.dir, c->P.pcg_rel_tol, c->P.pcg_max_iters, its, rel, s)))
+            if ((rc = pcg_solve(A, W, c->cs, fp64, A.g, A.dir, c->P.pcg_rel_tol, c->P.pcg_max_iters, its, rel, s,
+                                 tol.data())))
                 return rc;
             for (int i = 0; i < nI; ++i)
                 if (newton[i]) st[i].pcg_iters += its[i];
@@ -858,6 +904,12 @@ int idp_advance(idp_ctx* c, idp_result* results) {
             const char* nm[] = {"pcg", "tet", "contact", "ccd", "total", "barrier", "assembly", "linesearch"};
             for (int k = 0; k < PhaseTimer::NPHASE; ++k)
                 std::fprintf(stderr, "idp phase %-10s device %10.3f ms  host %10.3f ms\n", nm[k], ms[k], hms[k]);
+            std::fprintf(stderr,
+                         "idp accd pairs %lld, iterations %lld, longest %lld, pairs over 1000 iterations %lld; "
+                         "contact blocks %d (max %d vertices); pcg iterations %lld\n",
+                         W.accd_pairs, W.accd_total, W.accd_maxit, W.accd_long, W.cl.n, W.cl.max_n,
+                         (long long)W.stats.pcg_iters);
+            W.accd_maxit = W.accd_long = W.accd_total = W.accd_pairs = 0;
         }
         W.stats.pcg_ms = ms[PhaseTimer::PCG];
         W.stats.tet_ms = ms[PhaseTimer::TET];
@@ -934,6 +986,18 @@ int idp_get_state(idp_ctx* c, int i, double* X, double* v, double* kappa3) {
         kappa3[0] = c->st[i].kappa;
         kappa3[1] = c->st[i].kappa_max;
         kappa3[2] = 0;
+    }
+    return IDP_OK;
+}
+
+int idp_set_kappa(idp_ctx* c, int i, const double* kappa3) {
+    if (!c || i < 0 || i >= (int)c->inst.size() || !kappa3) return IDP_ERR_INVALID_ARG;
+    if (!(kappa3[0] > 0) || !(kappa3[1] >= kappa3[0])) return IDP_ERR_INVALID_ARG;
+    c->inst[i].kappa = kappa3[0];
+    c->inst[i].kappa_max = kappa3[1];
+    if (c->committed) {
+        c->st[i].kappa = kappa3[0];
+        c->st[i].kappa_max = kappa3[1];
     }
     return IDP_OK;
 }

@@ -47,6 +47,7 @@ struct InstState {
     double last_res = 0;
     double kappa = 0, kappa_max = 0;
     double min_alpha = 1;
+    double g0 = 0;             // gradient norm at the first Newton iteration
 };
 
 struct Arena {
@@ -85,6 +86,8 @@ struct Arena {
     long B = 0;
     int *rowptr = nullptr, *colidx = nullptr, *diagblk = nullptr;
     int *src_ptr = nullptr, *src = nullptr;       // per BSR block: contributing (tet*10+k)*2+transposed
+    int* vtri_ptr = nullptr;                      // per vertex: incident surface triangles, ascending
+    int* vtri = nullptr;
     int* vert_corner_ptr = nullptr;               // per vertex: list of tet*4+corner
     int* vert_corner = nullptr;
     int* brow = nullptr;                          // row (vertex) of every BSR block
@@ -171,7 +174,8 @@ enum WorkSlot {
     W_PREV_CONS, W_PREV_INST, W_PREV_DIST2,
     W_BH, W_BG, W_GENT_KEY, W_GENT_VAL, W_GENT_KEY2, W_GENT_VAL2, W_GENT_HEAD,
     W_TAIL_ROWPTR, W_TAIL_COL, W_TAIL_VAL, W_TAIL_KEYS,
-    W_BSR_VAL, W_DIAG_INV, W_PCG_VEC, W_PCG_SCAL, W_PCG_VEC64, W_CCD_TMP, W_CCD_ALPHA, W_MISC, W_MISC2,
+    W_BSR_VAL, W_DIAG_INV, W_PCG_VEC, W_PCG_SCAL, W_PCG_GRID, W_PCG_VEC64, W_CCD_TMP, W_CCD_ALPHA, W_MISC, W_MISC2,
+    W_CL_INT, W_CL_DENSE, W_CL_HOSTCONS,
     W_NUM
 };
 struct Work {
@@ -179,6 +183,25 @@ struct Work {
     idp_stats stats{};
     PhaseTimer timer;
     std::vector<double> pcg_bytes_per_iter;  // per instance
+    double* tol_inst = nullptr;              // per-instance PCG tolerance (device)
+    long grid_min_v = 16384;                 // grid-wide PCG above this many vertices
+    long grid_vper = 128;                    // vertices per CTA in the grid-wide PCG
+    long long accd_maxit = 0;                // diagnostics (IDP_PROFILE)
+    long long accd_long = 0, accd_total = 0, accd_pairs = 0;
+    // contact-cluster preconditioner (rebuilt with every Hessian)
+    struct Clusters {
+        int n = 0;                 // clusters of >= 2 vertices
+        long nvert = 0;            // vertices in clusters
+        long dense = 0;            // total dense entries
+        int* vcl = nullptr;        // V: cluster id or -1
+        int* vloc = nullptr;       // V: index inside its cluster
+        int* off = nullptr;        // n+1: vertex offsets
+        int* vert = nullptr;       // nvert: vertex ids
+        long long* doff = nullptr; // n+1: dense offsets
+        int* ioff = nullptr;       // nI+1: clusters of each instance (clusters sorted by instance)
+        int* ok = nullptr;         // n: factorisation succeeded
+        int max_n = 0;
+    } cl;
     DBuf& operator[](int i) { return b[i]; }
     void release() {
         for (auto& x : b) x.release();
@@ -219,9 +242,10 @@ int ccd_stepsize(Arena& A, Work& W, const double* X, const double* dir, double* 
 
 // solver.cu
 int assemble(Arena& A, Work& W, const ContactSet& cs, bool fp64, cudaStream_t s);
+int normal_flow_velocity(Arena& A, int sel, double step, double h, double* vel, cudaStream_t s);
 int pcg_solve(Arena& A, Work& W, const ContactSet& cs, bool fp64, const double* rhs, double* sol,
               double rel_tol, int max_iters, std::vector<int>& iters_out, std::vector<double>& relres_out,
-              cudaStream_t s);
+              cudaStream_t s, const double* tol_host = nullptr);
 
 // vector helpers (solver.cu)
 int vec_inertia(Arena& A, Work& W, const double* X, double* inst_E, double* g /*nullable*/, cudaStream_t s);
@@ -232,6 +256,8 @@ int chunk_reduce(Arena& A, Work& W, const Chunk* chunks, int nchunks, const doub
 int chunk_reduce_off(Arena& A, const int* coff, const double* part, double* out, bool accumulate, cudaStream_t s);
 int grad_gather_tet(Arena& A, Work& W, const double* X, double* g, cudaStream_t s);
 int hessian_apply(Arena& A, Work& W, bool fp64, const double* x, double* y, cudaStream_t s);
+// contact-cluster blocks of the preconditioner from the current constraint set
+int build_contact_clusters(Arena& A, Work& W, const ContactSet& cs, bool fp64, cudaStream_t s);
 // vecops.cu
 int vec_neg(long n, const double* a, double* out, cudaStream_t s);
 int vec_copy_masked(Arena& A, const unsigned char* mask, const double* src, double* dst, cudaStream_t s);

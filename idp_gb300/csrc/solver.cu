@@ -464,43 +464,110 @@ __device__ __forceinline__ void cluster_sum2(cg::cluster_group& cl, T a, T b, T 
     sb = rb;
 }
 
+// contact-cluster blocks of the preconditioner, as seen by the PCG kernel
+template <class T>
+struct ClusterPC {
+    const int* vcl;        // V: block id or -1
+    const int* ioff;       // nI+1: blocks of each instance
+    const int* off;        // blocks: vertex offsets
+    const int* vert;       // block vertices
+    const long long* doff; // dense offsets
+    const int* ok;         // factorisation succeeded
+    const T* Kinv;         // dense inverses
+};
+
+// z = M^{-1} r on the rows of the blocks owned by this CTA (blocks c of the
+// instance with c % csize == crank): dense inverse, or 3x3 inverses when
+// the block's factorisation failed
+template <class T>
+__device__ void apply_blocks(const ClusterPC<T>& pc, int inst, int crank, int csize, const T* __restrict__ dinv,
+                             const unsigned char* __restrict__ dbc, const T* __restrict__ r, T* __restrict__ z,
+                             T* __restrict__ p_init, T* rc) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int c = pc.ioff[inst] + crank; c < pc.ioff[inst + 1]; c += csize) {
+        const int o = pc.off[c], n = pc.off[c + 1] - o, N = 3 * n;
+        if (!pc.ok[c]) {
+            for (int li = threadIdx.x; li < n; li += blockDim.x) {
+                int v = pc.vert[o + li];
+                T rv[3] = {__ldcg(r + 3 * v), __ldcg(r + 3 * v + 1), __ldcg(r + 3 * v + 2)}, zv[3];
+                precond(v, dinv, dbc, rv, zv);
+                for (int d = 0; d < 3; ++d) {
+                    z[3 * v + d] = zv[d];
+                    if (p_init) p_init[3 * v + d] = zv[d];
+                }
+            }
+            continue;
+        }
+        for (int a = threadIdx.x; a < N; a += blockDim.x) rc[a] = __ldcg(r + 3 * pc.vert[o + a / 3] + a % 3);
+        __syncthreads();
+        const T* Ki = pc.Kinv + pc.doff[c];
+        for (int a = warp; a < N; a += nw) {
+            const T* row = Ki + (long)a * N;
+            T acc = 0;
+            for (int bb = lane; bb < N; bb += 32) acc += row[bb] * rc[bb];
+            for (int ofs = 16; ofs > 0; ofs >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, ofs);
+            if (lane == 0) {
+                int v = pc.vert[o + a / 3];
+                T zz = dbc[v] ? T(0) : acc;
+                z[3 * v + a % 3] = zz;
+                if (p_init) p_init[3 * v + a % 3] = zz;
+            }
+        }
+        __syncthreads();
+    }
+}
+
 template <class T>
 __global__ void __launch_bounds__(CL_THREADS) k_pcg_cluster(
     const int* __restrict__ inst_list, const int* __restrict__ v_off, const int* __restrict__ rowptr,
     const int* __restrict__ colidx, const T* __restrict__ val, const int* __restrict__ trp, const int* __restrict__ tcol,
-    const T* __restrict__ tval, const unsigned char* __restrict__ dbc, const T* __restrict__ dinv,
+    const T* __restrict__ tval, const unsigned char* __restrict__ dbc, const T* __restrict__ dinv, ClusterPC<T> pc,
     const double* __restrict__ b, T* __restrict__ x, T* __restrict__ r, T* __restrict__ z, T* __restrict__ p,
-    T* __restrict__ Ap, double rel_tol, int max_iters, int* __restrict__ iters_out) {
+    T* __restrict__ Ap, const double* __restrict__ tol_inst, double rel_tol, int max_iters,
+    int* __restrict__ iters_out) {
     __shared__ T wsh[2 * (CL_THREADS / 32)];
     __shared__ T slot[4][2];
+    __shared__ T rc[3 * kClusterCap];
     cg::cluster_group cl = cg::this_cluster();
     const int csize = (int)cl.num_blocks(), crank = (int)cl.block_rank();
     const int inst = inst_list[blockIdx.x / csize];
     const int iv0 = v_off[inst], iv1 = v_off[inst + 1];
     const int per = (iv1 - iv0 + csize - 1) / csize;
     const int v0 = iv0 + crank * per, v1 = min(iv1, v0 + per);
+    const bool has_blocks = pc.ioff[inst + 1] > pc.ioff[inst];
     int which = 0;
-    T rz_l = 0, rr_l = 0;
+    // r = b, z = M^{-1} r, p = z
+    T rr_l = 0;
     for (int v = v0 + threadIdx.x; v < v1; v += blockDim.x) {
         T rv[3], zv[3];
         for (int d = 0; d < 3; ++d) {
             rv[d] = dbc[v] ? T(0) : (T)b[3 * v + d];
             x[3 * v + d] = T(0);
             r[3 * v + d] = rv[d];
-        }
-        precond(v, dinv, dbc, rv, zv);
-        for (int d = 0; d < 3; ++d) {
-            z[3 * v + d] = zv[d];
-            p[3 * v + d] = zv[d];
-            rz_l += rv[d] * zv[d];
             rr_l += rv[d] * rv[d];
         }
+        if (pc.vcl[v] < 0) {
+            precond(v, dinv, dbc, rv, zv);
+            for (int d = 0; d < 3; ++d) {
+                z[3 * v + d] = zv[d];
+                p[3 * v + d] = zv[d];
+            }
+        }
     }
+    if (has_blocks) {
+        cl.sync();
+        apply_blocks(pc, inst, crank, csize, dinv, dbc, r, z, p, rc);
+        cl.sync();
+    }
+    T rz_l = 0;
+    for (int v = v0 + threadIdx.x; v < v1; v += blockDim.x)
+        for (int d = 0; d < 3; ++d) rz_l += r[3 * v + d] * z[3 * v + d];
     T rr_c, rz = cta_reduce2(rz_l, rr_l, wsh, rr_c);
     T rr;
     cluster_sum2(cl, rz, rr_c, slot, which, rz, rr);
     which ^= 1;
-    const T tol2 = (T)(rel_tol * rel_tol) * rr;
+    const double tl = tol_inst ? fmax(tol_inst[inst], rel_tol) : rel_tol;
+    const T tol2 = (T)(tl * tl) * rr;
     int it = 0;
     if (rr > T(0) && rr > tol2) {
         for (it = 0; it < max_iters;) {
@@ -519,21 +586,28 @@ __global__ void __launch_bounds__(CL_THREADS) k_pcg_cluster(
             which ^= 1;
             if (!(pAp > T(0))) break;
             const T alpha = rz / pAp;
-            T rzn_l = 0, rrn_l = 0;
+            T rrn_l = 0;
             for (int v = v0 + threadIdx.x; v < v1; v += blockDim.x) {
                 T rv[3], zv[3];
                 for (int d = 0; d < 3; ++d) {
                     x[3 * v + d] += alpha * p[3 * v + d];
                     rv[d] = r[3 * v + d] - alpha * Ap[3 * v + d];
                     r[3 * v + d] = rv[d];
-                }
-                precond(v, dinv, dbc, rv, zv);
-                for (int d = 0; d < 3; ++d) {
-                    z[3 * v + d] = zv[d];
-                    rzn_l += rv[d] * zv[d];
                     rrn_l += rv[d] * rv[d];
                 }
+                if (pc.vcl[v] < 0) {
+                    precond(v, dinv, dbc, rv, zv);
+                    for (int d = 0; d < 3; ++d) z[3 * v + d] = zv[d];
+                }
             }
+            if (has_blocks) {
+                cl.sync();
+                apply_blocks(pc, inst, crank, csize, dinv, dbc, r, z, (T*)nullptr, rc);
+                cl.sync();
+            }
+            T rzn_l = 0;
+            for (int v = v0 + threadIdx.x; v < v1; v += blockDim.x)
+                for (int d = 0; d < 3; ++d) rzn_l += r[3 * v + d] * z[3 * v + d];
             T rrn_c, rzn = cta_reduce2(rzn_l, rrn_l, wsh, rrn_c);
             T rrn;
             cluster_sum2(cl, rzn, rrn_c, slot, which, rzn, rrn);
@@ -548,6 +622,227 @@ __global__ void __launch_bounds__(CL_THREADS) k_pcg_cluster(
     }
     cl.sync();  // no CTA leaves while others may still read its shared memory
     if (crank == 0 && threadIdx.x == 0) iters_out[inst] = it;
+}
+
+// ---- grid-wide PCG for large instances: one cooperative launch holds every
+// CTA of the wave resident; instance i owns CTAs [c0, c0+nc) (nc depends only
+// on the instance's size, so results do not depend on what else is solved)
+// and synchronises them with its own counter barrier. Dot products: fixed
+// in-CTA tree, then the instance's CTA partials summed in CTA order by every
+// CTA (bit-identical scalars everywhere). Two barriers per iteration: the
+// direction update is folded into the SpMV pass (w = A z, p = z + beta p,
+// q = w + beta q with q = A p kept by recurrence). Vectors written inside
+// the kernel are read through L2 (ld.cg) so no CTA sees a stale L1 line.
+constexpr int GP_THREADS = 256;
+constexpr unsigned int kSpinLimit = 1u << 22;  // ~1 s of polling, then error
+
+struct GridCta {
+    int inst, v0, v1, c0, nc, slot;
+};
+
+// y = A x for block row v, one warp: lanes stride over the row's 9*nb
+// contiguous BSR values (coalesced), then a butterfly per component (every
+// lane ends with the same sums)
+template <class T>
+__device__ __forceinline__ void spmv_row_warp(int v, const int* __restrict__ rowptr, const int* __restrict__ colidx,
+                                              const T* __restrict__ val, const int* __restrict__ trp,
+                                              const int* __restrict__ tcol, const T* __restrict__ tval,
+                                              const unsigned char* __restrict__ dbc, const T* x, T y[3]) {
+    const int lane = threadIdx.x & 31;
+    if (dbc[v]) {
+        y[0] = __ldcg(x + 3 * v); y[1] = __ldcg(x + 3 * v + 1); y[2] = __ldcg(x + 3 * v + 2);
+        return;
+    }
+    T a0 = 0, a1 = 0, a2 = 0;
+    const int k0 = rowptr[v], n9 = 9 * (rowptr[v + 1] - k0);
+    for (int e = lane; e < n9; e += 32) {
+        const int kk = e / 9, q = e - 9 * kk;
+        const int c = colidx[k0 + kk];
+        const T pr = val[9L * k0 + e] * __ldcg(x + 3 * c + (q % 3));
+        const int rr = q / 3;
+        a0 += rr == 0 ? pr : T(0);
+        a1 += rr == 1 ? pr : T(0);
+        a2 += rr == 2 ? pr : T(0);
+    }
+    const int t0 = trp[v], t9 = 9 * (trp[v + 1] - t0);
+    for (int e = lane; e < t9; e += 32) {
+        const int kk = e / 9, q = e - 9 * kk;
+        const int c = tcol[t0 + kk];
+        if (dbc[c]) continue;
+        const T pr = tval[9L * t0 + e] * __ldcg(x + 3 * c + (q % 3));
+        const int rr = q / 3;
+        a0 += rr == 0 ? pr : T(0);
+        a1 += rr == 1 ? pr : T(0);
+        a2 += rr == 2 ? pr : T(0);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+        a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+        a2 += __shfl_xor_sync(0xffffffffu, a2, o);
+    }
+    y[0] = a0; y[1] = a1; y[2] = a2;
+}
+
+// counter barrier over the nc CTAs of one instance; the k-th barrier of the
+// launch completes when the counter reaches k*nc. Bounded: after
+// kSpinLimit polls the CTA records an error and reports failure.
+__device__ __forceinline__ bool inst_barrier(unsigned int* ctr, unsigned int target, int* err, int* ok_sh) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        __threadfence();
+        atomicAdd(ctr, 1u);
+        unsigned int n = 0;
+        while (*(volatile unsigned int*)ctr < target) {
+            if (++n > kSpinLimit) {
+                atomicExch(err, 1);
+                ok = 0;
+                break;
+            }
+            __nanosleep(64);
+        }
+        __threadfence();
+        *ok_sh = ok;
+    }
+    __syncthreads();
+    return *ok_sh != 0;
+}
+
+// sum of the instance's CTA partials (two values each) in CTA order
+template <class T>
+__device__ __forceinline__ void inst_sum2(const T* part, int c0, int nc, T* sh, T& s0, T& s1) {
+    if (threadIdx.x < 32) {
+        T a = 0, b = 0;
+        for (int j = threadIdx.x; j < nc; j += 32) {
+            a += __ldcg(part + 2 * (c0 + j));
+            b += __ldcg(part + 2 * (c0 + j) + 1);
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            a += __shfl_xor_sync(0xffffffffu, a, o);
+            b += __shfl_xor_sync(0xffffffffu, b, o);
+        }
+        if (threadIdx.x == 0) { sh[0] = a; sh[1] = b; }
+    }
+    __syncthreads();
+    s0 = sh[0];
+    s1 = sh[1];
+}
+
+template <class T>
+__global__ void __launch_bounds__(GP_THREADS) k_pcg_grid(
+    const GridCta* __restrict__ plan, int G, const int* __restrict__ rowptr, const int* __restrict__ colidx,
+    const T* __restrict__ val, const int* __restrict__ trp, const int* __restrict__ tcol, const T* __restrict__ tval,
+    const unsigned char* __restrict__ dbc, const T* __restrict__ dinv, ClusterPC<T> pc, const double* __restrict__ b,
+    T* x, T* r, T* z, T* p, T* q, T* part, unsigned int* bar, int* err, const double* __restrict__ tol_inst,
+    double rel_tol, int max_iters, int* __restrict__ iters_out) {
+    __shared__ T wsh[2 * (GP_THREADS / 32)];
+    __shared__ T ssum[2];
+    __shared__ int ok_sh;
+    __shared__ T rc[3 * kClusterCap];
+    const GridCta me = plan[blockIdx.x];
+    const int inst = me.inst, v0 = me.v0, v1 = me.v1, c0 = me.c0, nc = me.nc, rank = blockIdx.x - me.c0;
+    unsigned int* ctr = bar + me.slot;
+    unsigned int nbar = 0;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = GP_THREADS / 32;
+    const bool has_blocks = pc.ioff[inst + 1] > pc.ioff[inst];
+    auto sync_all = [&]() { return inst_barrier(ctr, (++nbar) * (unsigned int)nc, err, &ok_sh); };
+    auto slot = [&]() { return part + 2L * G * (nbar & 1u); };  // partials of the next barrier
+    // r = b, x = 0, z = M^{-1} r, p = q = 0
+    T rr_l = 0;
+    for (int v = v0 + threadIdx.x; v < v1; v += GP_THREADS) {
+        T rv[3], zv[3];
+        for (int d = 0; d < 3; ++d) {
+            rv[d] = dbc[v] ? T(0) : (T)b[3 * v + d];
+            x[3 * v + d] = T(0);
+            r[3 * v + d] = rv[d];
+            p[3 * v + d] = T(0);
+            q[3 * v + d] = T(0);
+            rr_l += rv[d] * rv[d];
+        }
+        if (pc.vcl[v] < 0) {
+            precond(v, dinv, dbc, rv, zv);
+            for (int d = 0; d < 3; ++d) z[3 * v + d] = zv[d];
+        }
+    }
+    if (has_blocks) {
+        if (!sync_all()) return;
+        apply_blocks(pc, inst, rank, nc, dinv, dbc, r, z, (T*)nullptr, rc);
+        if (!sync_all()) return;
+    }
+    T rz_l = 0;
+    for (int v = v0 + threadIdx.x; v < v1; v += GP_THREADS)
+        for (int d = 0; d < 3; ++d) rz_l += r[3 * v + d] * __ldcg(z + 3 * v + d);
+    T rr_c, rz_c = cta_reduce2(rz_l, rr_l, wsh, rr_c);
+    T* ps = slot();
+    if (threadIdx.x == 0) { ps[2 * blockIdx.x] = rz_c; ps[2 * blockIdx.x + 1] = rr_c; }
+    if (!sync_all()) return;
+    T rz, rr0;
+    inst_sum2(ps, c0, nc, ssum, rz, rr0);
+    const double tl = tol_inst ? fmax(tol_inst[inst], rel_tol) : rel_tol;
+    const T tol2 = (T)(tl * tl) * rr0;
+    T beta = 0;
+    int it = 0;
+    if (rr0 > T(0) && rr0 > tol2) {
+        for (it = 0; it < max_iters;) {
+            // w = A z (rows of this CTA, warp per row); p = z + beta p; q = w + beta q
+            T pq_l = 0;
+            for (int v = v0 + warp; v < v1; v += nw) {
+                T w[3];
+                spmv_row_warp<T>(v, rowptr, colidx, val, trp, tcol, tval, dbc, z, w);
+                if (lane < 3) {
+                    const int i3 = 3 * v + lane;
+                    const T wl = lane == 0 ? w[0] : (lane == 1 ? w[1] : w[2]);
+                    const T pn = __ldcg(z + i3) + beta * p[i3];
+                    const T qn = wl + beta * q[i3];
+                    p[i3] = pn;
+                    q[i3] = qn;
+                    pq_l += pn * qn;
+                }
+            }
+            T dummy, pq_c = cta_reduce2(pq_l, T(0), wsh, dummy);
+            ps = slot();
+            if (threadIdx.x == 0) { ps[2 * blockIdx.x] = pq_c; ps[2 * blockIdx.x + 1] = T(0); }
+            if (!sync_all()) return;
+            T pq;
+            inst_sum2(ps, c0, nc, ssum, pq, dummy);
+            if (!(pq > T(0))) break;
+            const T alpha = rz / pq;
+            // x += alpha p; r -= alpha q; z = M^{-1} r
+            T rrn_l = 0;
+            for (int v = v0 + threadIdx.x; v < v1; v += GP_THREADS) {
+                T rv[3], zv[3];
+                for (int d = 0; d < 3; ++d) {
+                    x[3 * v + d] += alpha * p[3 * v + d];
+                    rv[d] = r[3 * v + d] - alpha * q[3 * v + d];
+                    r[3 * v + d] = rv[d];
+                    rrn_l += rv[d] * rv[d];
+                }
+                if (pc.vcl[v] < 0) {
+                    precond(v, dinv, dbc, rv, zv);
+                    for (int d = 0; d < 3; ++d) z[3 * v + d] = zv[d];
+                }
+            }
+            if (has_blocks) {
+                if (!sync_all()) return;
+                apply_blocks(pc, inst, rank, nc, dinv, dbc, r, z, (T*)nullptr, rc);
+                if (!sync_all()) return;
+            }
+            T rzn_l = 0;
+            for (int v = v0 + threadIdx.x; v < v1; v += GP_THREADS)
+                for (int d = 0; d < 3; ++d) rzn_l += r[3 * v + d] * __ldcg(z + 3 * v + d);
+            T rrn_c, rzn_c = cta_reduce2(rzn_l, rrn_l, wsh, rrn_c);
+            ps = slot();
+            if (threadIdx.x == 0) { ps[2 * blockIdx.x] = rzn_c; ps[2 * blockIdx.x + 1] = rrn_c; }
+            if (!sync_all()) return;
+            T rzn, rrn;
+            inst_sum2(ps, c0, nc, ssum, rzn, rrn);
+            ++it;
+            if (rrn <= tol2) break;
+            beta = rzn / rz;
+            rz = rzn;
+        }
+    }
+    if (rank == 0 && threadIdx.x == 0) iters_out[inst] = it;
 }
 
 }  // namespace
@@ -660,13 +955,14 @@ static int pcg_inner(Arena& A, Work& W, const double* b, double rel_tol, int max
     for (int i = 0; i < nI; ++i) {
         if (!act[i]) continue;
         long vi = A.v_off[i + 1] - A.v_off[i];
-        if (vi > kClusterPcgMaxV) { large[i] = 1; any_large = true; continue; }
+        if (vi > W.grid_min_v) { large[i] = 1; any_large = true; continue; }
         small[i] = 1;
         any_small = true;
-        // aim for about two CTAs per SM over the whole launch, at most 16 per instance
-        double want = (double)vi * 2.0 * 152.0 / (double)(vtot > 0 ? vtot : 1);
+        // one CTA per ~1.5k vertices (at most 16), but no more than the
+        // launch can keep resident (about two CTAs per SM in total)
+        double fair = (double)vi * 2.0 * 152.0 / (double)(vtot > 0 ? vtot : 1);
         int k = 0;
-        while (k < 4 && (1 << (k + 1)) <= want && (long)(CL_THREADS) * (1 << k) < vi) ++k;
+        while (k < 4 && (1L << k) * 1536L < vi && ((1 << (k + 1)) <= fair || (1 << (k + 1)) <= 4)) ++k;
         by_size[k].push_back(i);
     }
     if (W[W_MISC2].ensure(sizeof(int) * (2 * nI + 64))) return IDP_ERR_CUDA;
@@ -682,6 +978,14 @@ static int pcg_inner(Arena& A, Work& W, const double* b, double rel_tol, int max
             cudaFuncSetAttribute(k_pcg_cluster<T>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
             attr_set[sizeof(T) == 8] = true;
         }
+        ClusterPC<T> pcb;
+        pcb.vcl = W.cl.vcl;
+        pcb.ioff = W.cl.ioff;
+        pcb.off = W.cl.off;
+        pcb.vert = W.cl.vert;
+        pcb.doff = W.cl.doff;
+        pcb.ok = W.cl.ok;
+        pcb.Kinv = W.cl.n > 0 ? W[W_CL_DENSE].as<T>() : nullptr;
         W.timer.start(PhaseTimer::PCG, s);
         int base = 0;
         for (int k = 0; k < 5; ++k) {
@@ -703,7 +1007,8 @@ static int pcg_inner(Arena& A, Work& W, const double* b, double rel_tol, int max
             ::idp::count_launch();
             IDP_CUDA_TRY(cudaLaunchKernelEx(&cfg, k_pcg_cluster<T>, lst, (const int*)A.d_v_off, (const int*)A.rowptr,
                                             (const int*)A.colidx, val, trp, tcol, tval, (const unsigned char*)A.dbc,
-                                            dinv, b, x, r, z, p, Ap, rel_tol, max_iters, d_iters));
+                                            dinv, pcb, b, x, r, z, p, Ap, (const double*)W.tol_inst, rel_tol,
+                                            max_iters, d_iters));
             W.stats.pcg_launches += 1;
             base += n;
         }
@@ -727,40 +1032,100 @@ static int pcg_inner(Arena& A, Work& W, const double* b, double rel_tol, int max
         *xout = x;
         return IDP_OK;
     }
-    IDP_CUDA_TRY(cudaMemcpyAsync(A.active, large.data(), nI, cudaMemcpyHostToDevice, s));
-    (::idp::count_launch(), k_pcg_init<T><<<nc, kBlock, 0, s>>>(A.vert_chunks, A.active, dinv, A.dbc, b, x, r, z, p, part));
-    (::idp::count_launch(), k_pcg_scal_init<<<grid_for(nI), kBlock, 0, s>>>(nI, A.vert_chunk_off, A.active, part, rel_tol, S));
-    W.timer.start(PhaseTimer::PCG, s);
-    const int check_every = 8;
-    for (int it = 0; it < max_iters; it += check_every) {
-        IDP_CUDA_TRY(cudaMemsetAsync(any, 0, sizeof(int), s));
-        for (int k = 0; k < check_every; ++k) {
-            (::idp::count_launch(), k_pcg_spmv<T><<<nc, kBlock, 0, s>>>(A.vert_chunks, S, A.rowptr, A.colidx, val, trp, tcol, tval, A.dbc, p, Ap,
-                                                part));
-            (::idp::count_launch(), k_pcg_scal_alpha<<<grid_for(nI), kBlock, 0, s>>>(nI, A.vert_chunk_off, part, S));
-            (::idp::count_launch(), k_pcg_update<T><<<nc, kBlock, 0, s>>>(A.vert_chunks, S, dinv, A.dbc, x, r, z, p, Ap, part));
-            (::idp::count_launch(), k_pcg_scal_beta<<<grid_for(nI), kBlock, 0, s>>>(nI, A.vert_chunk_off, part, max_iters, S, any));
-            (::idp::count_launch(), k_pcg_pupdate<T><<<nc, kBlock, 0, s>>>(A.vert_chunks, S, z, p));
-        }
-        int hany = 0;
-        IDP_CUDA_TRY(cudaMemcpyAsync(&hany, any, sizeof(int), cudaMemcpyDeviceToHost, s));
-        IDP_CUDA_TRY(cudaStreamSynchronize(s));
-        if (!hany) break;
+    // large instances: grid-wide PCG, in waves of at most gmax CTAs
+    static int gmax_cache[2] = {0, 0};
+    int& gmax = gmax_cache[sizeof(T) == 8];
+    if (!gmax) {
+        int dev = 0, nsm = 0, per = 0;
+        IDP_CUDA_TRY(cudaGetDevice(&dev));
+        IDP_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+        IDP_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pcg_grid<T>, GP_THREADS, 0));
+        gmax = nsm * per;
+        if (gmax <= 0) return IDP_ERR_CUDA;
     }
-    std::vector<PcgS> hs(nI);
-    IDP_CUDA_TRY(cudaMemcpyAsync(hs.data(), S, sizeof(PcgS) * nI, cudaMemcpyDeviceToHost, s));
-    IDP_CUDA_TRY(cudaMemcpyAsync(A.active, act.data(), nI, cudaMemcpyHostToDevice, s));
-    IDP_CUDA_TRY(cudaStreamSynchronize(s));
+    const long vper = W.grid_vper;
+    std::vector<GridCta> plan;
+    std::vector<std::vector<GridCta>> waves;
+    int slot = 0;
+    for (int i = 0; i < nI; ++i) {
+        if (!large[i]) continue;
+        const int iv0 = A.v_off[i], iv1 = A.v_off[i + 1];
+        const long vi = iv1 - iv0;
+        int ncta = (int)std::min<long>((vi + vper - 1) / vper, (long)gmax);
+        if ((int)plan.size() + ncta > gmax) {
+            waves.push_back(plan);
+            plan.clear();
+            slot = 0;
+        }
+        const int c0 = (int)plan.size();
+        const long per = (vi + ncta - 1) / ncta;
+        for (int k = 0; k < ncta; ++k) {
+            GridCta g;
+            g.inst = i;
+            g.v0 = (int)std::min<long>(iv1, iv0 + k * per);
+            g.v1 = (int)std::min<long>(iv1, iv0 + (k + 1) * per);
+            g.c0 = c0;
+            g.nc = ncta;
+            g.slot = slot;
+            plan.push_back(g);
+        }
+        ++slot;
+    }
+    if (!plan.empty()) waves.push_back(plan);
+    size_t need = sizeof(GridCta) * gmax + sizeof(T) * 4 * (size_t)gmax + sizeof(unsigned int) * (nI + 1) + 256;
+    if (W[W_PCG_GRID].ensure(need)) return IDP_ERR_CUDA;
+    char* gb = W[W_PCG_GRID].as<char>();
+    GridCta* d_plan = reinterpret_cast<GridCta*>(gb);
+    T* d_part = reinterpret_cast<T*>(gb + sizeof(GridCta) * gmax);
+    unsigned int* d_bar = reinterpret_cast<unsigned int*>(gb + sizeof(GridCta) * gmax + sizeof(T) * 4 * (size_t)gmax);
+    int* d_err = reinterpret_cast<int*>(d_bar + nI + 1);
+    ClusterPC<T> pcb;
+    pcb.vcl = W.cl.vcl;
+    pcb.ioff = W.cl.ioff;
+    pcb.off = W.cl.off;
+    pcb.vert = W.cl.vert;
+    pcb.doff = W.cl.doff;
+    pcb.ok = W.cl.ok;
+    pcb.Kinv = W.cl.n > 0 ? W[W_CL_DENSE].as<T>() : nullptr;
+    W.timer.start(PhaseTimer::PCG, s);
+    IDP_CUDA_TRY(cudaMemsetAsync(d_err, 0, sizeof(int), s));
+    for (auto& wv : waves) {
+        const int G = (int)wv.size();
+        IDP_CUDA_TRY(cudaMemcpyAsync(d_plan, wv.data(), sizeof(GridCta) * G, cudaMemcpyHostToDevice, s));
+        IDP_CUDA_TRY(cudaMemsetAsync(d_bar, 0, sizeof(unsigned int) * (nI + 1), s));
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(G);
+        cfg.blockDim = dim3(GP_THREADS);
+        cfg.stream = s;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeCooperative;
+        at[0].val.cooperative = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        ::idp::count_launch();
+        IDP_CUDA_TRY(cudaLaunchKernelEx(&cfg, k_pcg_grid<T>, (const GridCta*)d_plan, G, (const int*)A.rowptr,
+                                        (const int*)A.colidx, val, trp, tcol, tval, (const unsigned char*)A.dbc, dinv,
+                                        pcb, b, x, r, z, p, Ap, d_part, d_bar, d_err, (const double*)W.tol_inst,
+                                        rel_tol, max_iters, d_iters));
+        W.stats.pcg_launches += 1;
+    }
     W.timer.stop(s);
+    int herr = 0;
+    std::vector<int> hit(nI);
+    IDP_CUDA_TRY(cudaMemcpyAsync(&herr, d_err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    IDP_CUDA_TRY(cudaMemcpyAsync(hit.data(), d_iters, sizeof(int) * nI, cudaMemcpyDeviceToHost, s));
+    IDP_CUDA_TRY(cudaStreamSynchronize(s));
+    if (herr) return IDP_ERR_CUDA;  // a barrier wait ran out (never expected)
     for (int i = 0; i < nI; ++i)
-        if (large[i]) iters[i] = hs[i].iters;
+        if (large[i]) iters[i] = hit[i];
     account(large);
     *xout = x;
     return IDP_OK;
 }
 
 int pcg_solve(Arena& A, Work& W, const ContactSet& cs, bool fp64, const double* rhs, double* sol, double rel_tol,
-              int max_iters, std::vector<int>& iters_out, std::vector<double>& relres_out, cudaStream_t s) {
+              int max_iters, std::vector<int>& iters_out, std::vector<double>& relres_out, cudaStream_t s,
+              const double* tol_host) {
     (void)cs;
     const int nI = A.nI;
     long n3 = 3 * A.V;
@@ -808,7 +1173,8 @@ int pcg_solve(Arena& A, Work& W, const ContactSet& cs, bool fp64, const double* 
             hrr = b2;
         }
         for (int i = 0; i < nI; ++i) {
-            act[i] = act0[i] && b2[i] > 0 && hrr[i] > rel_tol * rel_tol * b2[i];
+            const double ti = tol_host ? std::max(rel_tol, tol_host[i]) : rel_tol;
+            act[i] = act0[i] && b2[i] > 0 && hrr[i] > ti * ti * b2[i];
             relres_out[i] = b2[i] > 0 ? std::sqrt(hrr[i] / b2[i]) : 0.0;
             any |= act[i] != 0;
         }

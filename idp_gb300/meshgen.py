@@ -129,14 +129,17 @@ def _real_sh(lmax, theta, phi):
 def blob(n=64, lmax=8, amp=0.3, seed=0):
     """Closed bumpy blob r(u) = 1 + amp * sum_{l<=lmax} c_lm Y_lm(u),
     c_lm ~ N(0, 1/l^2), tetrahedralised on an n^3 background grid: every cube
-    whose centre lies inside is split into 5 tets."""
+    whose centre lies inside is split into 5 tets. The grid spans the blob's
+    largest radius (sampled on 20k Fibonacci directions) plus 2%; at n=64 and
+    seed 0 this gives 220,515 tets."""
     rng = np.random.default_rng(seed)
     nlm = sum(2 * l + 1 for l in range(1, lmax + 1))
     ls = np.concatenate([[l] * (2 * l + 1) for l in range(1, lmax + 1)])
     coef = rng.normal(0.0, 1.0, nlm) / ls
-    # bound the radius range so the grid covers it
-    ext = 1.0 + amp * np.abs(coef).sum() * 0.5
-    ext = min(ext, 2.5)
+    m = 20000
+    k = np.arange(m) + 0.5
+    Yd, _ = _real_sh(lmax, np.arccos(1.0 - 2.0 * k / m), np.pi * (1.0 + 5.0 ** 0.5) * k)
+    ext = 1.02 * float((1.0 + amp * (Yd @ coef)).max())
     g = np.linspace(-ext, ext, n + 1)
     h = g[1] - g[0]
     cc = (g[:-1] + g[1:]) / 2

@@ -48,6 +48,10 @@ typedef struct idp_params {
     int pcg_max_iters;    /* PCG iteration cap per refinement sweep                 */
     double thickness;     /* IPC offset (`thickness` argument, IPC.h:53,757)        */
     int device;           /* CUDA device ordinal                                    */
+    int pcg_grid_min_vertices; /* instances above this many vertices solve with the
+                             grid-wide PCG (all SMs), the others with one thread-block
+                             cluster each; 0 = default (16384)                        */
+    int pcg_grid_cta_vertices; /* vertices per CTA in the grid-wide PCG; 0 = default (128) */
 } idp_params;
 
 typedef struct idp_result {
@@ -109,6 +113,16 @@ int idp_set_velocity(idp_ctx* ctx, int inst, const double* v);
 /* Current positions (3V), e.g. a warm start between frames. */
 int idp_set_positions(idp_ctx* ctx, int inst, const double* X);
 
+/* Normal-flow predictor for one instance (inst >= 0) or all (inst = -1),
+ * computed on the device from the current positions: every surface vertex
+ * gets x_tilde = x + step * n, n its normalised sum of incident surface
+ * triangle normals cross(X2-X1, X3-X1); interior vertices get x_tilde = x.
+ * Stored as the velocity v = (step / |n_sum|) * n_sum / h (zero inside).
+ * Replaces Update_Normal_Flow_Neumann (FEM/Shell/DISCRETE_SHELL.h:359-395),
+ * whose body force b = magnitude * m * n shifts x_tilde by h^2 * magnitude * n,
+ * i.e. step = h^2 * magnitude. After idp_commit only. */
+int idp_set_normal_flow(idp_ctx* ctx, int inst, double step);
+
 /* Upload every instance to the device and build the static structures
  * (surface primitives, BSR pattern). */
 int idp_commit(idp_ctx* ctx);
@@ -132,6 +146,11 @@ int idp_get_stats(idp_ctx* ctx, idp_stats* out);
 
 /* Read back positions X (3V), velocity v (3V) and kappa[3] of one instance. */
 int idp_get_state(idp_ctx* ctx, int inst, double* X, double* v, double* kappa3);
+
+/* Set kappa[0..1] = (kappa, kappa_max) of one instance, the in/out kappaVec
+ * argument of Advance_One_Step_IE_Hinge (FEM/Shell/IMPLICIT_EULER.h:151-187,
+ * doubled in place at :566-595); kappa[2] is ignored. */
+int idp_set_kappa(idp_ctx* ctx, int inst, const double* kappa3);
 
 /* Number of instances, and vertex/tet/surface counts of one instance. */
 int idp_instance_info(idp_ctx* ctx, int inst, int* V, int* T, int* n_nodes, int* n_edges, int* n_tris);

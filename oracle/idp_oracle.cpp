@@ -1079,4 +1079,29 @@ void ora_dist_derivs(int kind, const double* x, double* d, double* g, double* H)
 }
 void ora_make_pd(int n, double* A) { make_pd(n, A); }
 
+// Normal-flow predictor shift (Update_Normal_Flow_Neumann,
+// FEM/Shell/DISCRETE_SHELL.h:359-395): b_v += cross(X2-X1, X3-X1) over the
+// surface triangles in order, then normalised; the shift `step` along b_v is
+// returned as a velocity over h. Vertices on no triangle get zero.
+void ora_normal_flow(int V, int nT, const int* tris, const double* X, double step, double h, double* vel) {
+    std::vector<double> b(3 * (size_t)V, 0.0);
+    std::vector<int> deg(V, 0);
+    for (int f = 0; f < nT; ++f) {
+        const int a = tris[3 * f], c1 = tris[3 * f + 1], c2 = tris[3 * f + 2];
+        const double e1[3] = {X[3 * c1] - X[3 * a], X[3 * c1 + 1] - X[3 * a + 1], X[3 * c1 + 2] - X[3 * a + 2]};
+        const double e2[3] = {X[3 * c2] - X[3 * a], X[3 * c2 + 1] - X[3 * a + 1], X[3 * c2 + 2] - X[3 * a + 2]};
+        const double n[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
+        for (int k = 0; k < 3; ++k) {
+            const int v = tris[3 * f + k];
+            deg[v]++;
+            for (int d = 0; d < 3; ++d) b[3 * v + d] += n[d];
+        }
+    }
+    for (int v = 0; v < V; ++v) {
+        const double sq = b[3 * v] * b[3 * v] + b[3 * v + 1] * b[3 * v + 1] + b[3 * v + 2] * b[3 * v + 2];
+        const double w = (deg[v] > 0 && sq > 0) ? step / std::sqrt(sq) : 0.0;
+        for (int d = 0; d < 3; ++d) vel[3 * v + d] = w * b[3 * v + d] / h;
+    }
+}
+
 }  // extern "C"

@@ -200,6 +200,16 @@ def make_pd(A):
     return A
 
 
+def normal_flow_velocity(X, tris, step, h):
+    """Velocity whose predictor moves surface vertices by ``step`` along the
+    normalised sum of incident triangle normals (DISCRETE_SHELL.h:359-395)."""
+    X = f64(X)
+    tris = i32(tris)
+    vel = np.zeros_like(X)
+    lib().ora_normal_flow(X.shape[0], tris.shape[0], _i(tris), _d(X), C.c_double(step), C.c_double(h), _d(vel))
+    return vel
+
+
 # ---------------------------------------------------------------- Newton step
 @dataclass
 class Problem:

@@ -164,8 +164,14 @@ def test_hessian_apply_parity(oracle, gpu_lib, mode, tol):
     ctx.close()
 
 
+# PCG paths: one thread-block cluster per instance (default at these sizes),
+# or the grid-wide cooperative PCG forced down to small instances
+PCG_PATHS = {"cluster": {}, "grid": {"pcg_grid_min_vertices": 1, "pcg_grid_cta_vertices": 16}}
+
+
+@pytest.mark.parametrize("path", sorted(PCG_PATHS))
 @pytest.mark.parametrize("mode", [0, 1])
-def test_newton_direction_solves_system(oracle, gpu_lib, mode):
+def test_newton_direction_solves_system(oracle, gpu_lib, mode, path):
     import idp_gb300 as idp
     import scipy.sparse.linalg as spla
 
@@ -173,7 +179,7 @@ def test_newton_direction_solves_system(oracle, gpu_lib, mode):
     pr = cases.problem(X0, tets, dHat=dhat)
     rng = np.random.default_rng(1)
     v = rng.normal(size=X.shape)
-    ctx = ctx_for(idp, X0, tets, pr, mode, v=v, pcg_rel_tol=1e-8)
+    ctx = ctx_for(idp, X0, tets, pr, mode, v=v, pcg_rel_tol=1e-8, **PCG_PATHS[path])
     p, its, rel = ctx.newton_direction(0, X)
     assert rel <= 1e-7 and its > 0
     pb = oracle_problem(oracle, X, tets, pr, X0=X0)
@@ -195,14 +201,15 @@ def small_bar_problem():
     return X, tets, target, pr
 
 
+@pytest.mark.parametrize("path", sorted(PCG_PATHS))
 @pytest.mark.parametrize("mode", [0, 1])
-def test_full_step_injective_and_close_to_oracle(oracle, gpu_lib, mode):
+def test_full_step_injective_and_close_to_oracle(oracle, gpu_lib, mode, path):
     import idp_gb300 as idp
 
     X, tets, target, pr = small_bar_problem()
     h = 0.1
     v = (target - X) / h
-    ctx = ctx_for(idp, X, tets, pr, mode, h=h, v=v, newton_tol=1e-3, max_newton=600)
+    ctx = ctx_for(idp, X, tets, pr, mode, h=h, v=v, newton_tol=1e-3, max_newton=600, **PCG_PATHS[path])
     rc, res = ctx.advance(check=False)
     assert rc in (idp.IDP_OK, idp.IDP_WARN_ITER_CAP), res
     Xg, vg, kap = ctx.state(0)
@@ -224,7 +231,8 @@ def test_full_step_injective_and_close_to_oracle(oracle, gpu_lib, mode):
     ctx.close()
 
 
-def test_batch_is_bitwise_identical_to_alone(oracle, gpu_lib):
+@pytest.mark.parametrize("path", sorted(PCG_PATHS))
+def test_batch_is_bitwise_identical_to_alone(oracle, gpu_lib, path):
     import idp_gb300 as idp
     from idp_gb300 import meshgen
 
@@ -234,14 +242,14 @@ def test_batch_is_bitwise_identical_to_alone(oracle, gpu_lib):
         X, tets = meshgen.bar(nx, nx, nz, size=(1.0, 1.0, 2.0), seed=seed)
         tgt = meshgen.bend_target(X, angle=ang, radius=0.4, size=(1.0, 1.0, 2.0))
         probs.append((X, tets, tgt, cases.problem(X, tets)))
-    batch = idp.Context(h=h, mode=idp.MODE_MIXED, max_newton=40)
+    batch = idp.Context(h=h, mode=idp.MODE_MIXED, max_newton=40, **PCG_PATHS[path])
     for i, (X, tets, tgt, pr) in enumerate(probs):
         batch.add_instance(X, tets, pr["mass"], pr["lam"], pr["mu"], pr["dHat2"], pr["kappa"], pr["kappa_max"])
         batch.set_velocity(i, (tgt - X) / h)
     batch.commit()
     _, rb = batch.advance(check=False)
     for i, (X, tets, tgt, pr) in enumerate(probs):
-        alone = ctx_for(idp, X, tets, pr, idp.MODE_MIXED, h=h, v=(tgt - X) / h, max_newton=40)
+        alone = ctx_for(idp, X, tets, pr, idp.MODE_MIXED, h=h, v=(tgt - X) / h, max_newton=40, **PCG_PATHS[path])
         _, ra = alone.advance(check=False)
         Xa, _, _ = alone.state(0)
         Xb, _, _ = batch.state(i)
@@ -265,4 +273,65 @@ def test_inverted_input_is_rejected(gpu_lib):
     with pytest.raises(idp.IDPError) as e:
         ctx.commit()
     assert e.value.code == idp.IDP_ERR_INVERTED
+    ctx.close()
+
+
+def test_normal_flow_velocity_bitexact(oracle, gpu_lib):
+    """Device normal-flow predictor equals the oracle's bit for bit, per
+    instance and for all instances at once."""
+    import idp_gb300 as idp
+    from idp_gb300 import meshgen
+
+    h = 0.1
+    meshes = [meshgen.bar(3, 2, 5, seed=0)[:2], meshgen.blob(n=12, lmax=4, seed=1)[:2]]
+    ctx = idp.Context(h=h, mode=idp.MODE_MIXED)
+    rng = np.random.default_rng(3)
+    moved = []
+    for X, tets in meshes:
+        pr = cases.problem(X, tets)
+        ctx.add_instance(X, tets, pr["mass"], pr["lam"], pr["mu"], pr["dHat2"], pr["kappa"], pr["kappa_max"])
+    ctx.commit()
+    for i, (X, tets) in enumerate(meshes):
+        Xm = X + rng.uniform(-0.01, 0.01, X.shape)
+        ctx.set_positions(i, Xm)
+        moved.append(Xm)
+    ctx.set_normal_flow(-1, 0.05)
+    for i, (X, tets) in enumerate(meshes):
+        _, v, _ = ctx.state(i)
+        o = oracle.normal_flow_velocity(moved[i], oracle.surface(X, tets)["tris"], 0.05, h)
+        assert np.array_equal(v, o), i
+    ctx.set_normal_flow(1, -0.02)
+    _, v0, _ = ctx.state(0)
+    _, v1, _ = ctx.state(1)
+    assert np.array_equal(v0, oracle.normal_flow_velocity(moved[0], oracle.surface(*meshes[0])["tris"], 0.05, h))
+    assert np.array_equal(v1, oracle.normal_flow_velocity(moved[1], oracle.surface(*meshes[1])["tris"], -0.02, h))
+    ctx.close()
+
+
+@pytest.mark.parametrize("mode", [0, 1], ids=["fp64", "mixed"])
+def test_normal_flow_step_close_to_oracle(oracle, gpu_lib, mode):
+    """One normal-flow solve on a small blob: injective, and the final
+    incremental potential within 1e-3 relative of the oracle's direct-solve
+    Newton step on the same predictor."""
+    import idp_gb300 as idp
+    from idp_gb300 import meshgen
+
+    X, tets, _ = meshgen.blob(n=10, lmax=6, seed=2)
+    pr = cases.problem(X, tets)
+    h = 0.1
+    ctx = ctx_for(idp, X, tets, pr, mode, h=h, newton_tol=1e-3, max_newton=200)
+    ctx.set_normal_flow(0, 0.05)
+    _, v0, _ = ctx.state(0)
+    rc, res = ctx.advance(check=False)
+    assert rc == idp.IDP_OK, res
+    Xg, _, _ = ctx.state(0)
+    pb = oracle_problem(oracle, X, tets, pr)
+    assert oracle.tet_energy(Xg, tets, pb.IB, pb.vol, pb.lam, pb.mu, 1.0) is not None
+    po = oracle_problem(oracle, X, tets, pr)
+    po.v = oracle.normal_flow_velocity(X, oracle.surface(X, tets)["tris"], 0.05, h)
+    assert np.array_equal(po.v, v0)
+    po.max_iters = 200
+    oracle.advance_one_step(po)
+    rel = abs(res[0]["energy"] - po.last_energy) / abs(po.last_energy)
+    assert rel <= 1e-3, (res[0]["energy"], po.last_energy)
     ctx.close()

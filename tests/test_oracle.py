@@ -236,3 +236,19 @@ def test_ccd_step_is_conservative(oracle):
     d2[V // 2:, 0] = 0.2
     a2, _ = oracle.ccd_stepsize(X, d2.reshape(-1), s, dbc, 1.0)
     assert a2 == pytest.approx(1.0) or a2 > 0.5
+
+
+def test_normal_flow_outward_unit(oracle):
+    """Oracle normal-flow shift has length |step| on surface vertices, points
+    out of a star-shaped blob, and is zero inside."""
+    from idp_gb300 import meshgen
+
+    X, tets, _ = meshgen.blob(n=10, lmax=6, seed=2)
+    surf = oracle.surface(X, tets)
+    h = 0.1
+    v = oracle.normal_flow_velocity(X, surf["tris"], 0.05, h)
+    on = np.zeros(X.shape[0], bool)
+    on[surf["nodes"]] = True
+    assert np.allclose(np.linalg.norm(v[on], axis=1) * h, 0.05)
+    assert np.all(v[~on] == 0)
+    assert np.all(np.einsum("ij,ij->i", v[on], X[on] - X.mean(0)) > 0)
