@@ -35,7 +35,7 @@ EXPORTS = [
     "idp_set_positions", "idp_commit", "idp_advance", "idp_get_state", "idp_instance_info", "idp_get_surface",
     "idp_eval_energy", "idp_eval_gradient", "idp_constraint_set", "idp_ccd_stepsize", "idp_hessian_apply",
     "idp_newton_direction", "idp_get_stats", "idp_save_state", "idp_restore_state",
-    "idp_set_normal_flow", "idp_set_kappa",
+    "idp_set_normal_flow", "idp_set_kappa", "idp_tet_energy_noalloc",
 ]
 
 
@@ -95,6 +95,8 @@ def load(path: str | None = None):
     L.idp_set_positions.argtypes = [C.c_void_p, C.c_int, _dp]
     L.idp_set_normal_flow.argtypes = [C.c_void_p, C.c_int, C.c_double]
     L.idp_set_kappa.argtypes = [C.c_void_p, C.c_int, _dp]
+    L.idp_tet_energy_noalloc.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                         C.c_void_p, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p]
     L.idp_commit.argtypes = [C.c_void_p]
     L.idp_advance.argtypes = [C.c_void_p, C.POINTER(Result)]
     L.idp_get_state.argtypes = [C.c_void_p, C.c_int, _dp, _dp, _dp]

@@ -14,6 +14,7 @@
 // eigenvalue 2*right — the eigen-decomposition of the reference's 2x2 B
 // blocks [[l+r, l-r], [l-r, l+r]]. Each mode Q contributes
 // lambda * g g^T with g = dF/dx^T vec(Q), computed as Q * IB^T.
+#include <mutex>
 #include "engine.hpp"
 #include "prims.cuh"
 
@@ -350,4 +351,101 @@ int tet_detcheck(Arena& A, Work& W, const double* X, int* inst_bad, cudaStream_t
     return tet_energy(A, W, X, 0.0, W[W_INST_SUM].as<double>() + 4 * A.nI, inst_bad, s);
 }
 
+namespace {
+
+// ---- allocation-free elastic energy (exported as idp_tet_energy_noalloc)
+//
+// Some callers cannot allocate device memory while they run: a host
+// application that reserves the whole GPU budget up front and hands the
+// library only its own buffers (a DCC plug-in or engine fixing one animation
+// frame after another), or a latency-bound loop that cannot afford the
+// device-wide synchronisation cudaMalloc/cudaFree imply. For them this entry
+// point evaluates w * sum_t vol_t * Psi(F_t) over caller-owned device arrays
+// with the same per-tet arithmetic and the same reduction order as the
+// arena path (CTA tree per 1024-tet chunk, then the chunk sums in order),
+// using only the fixed scratch below for the chunk sums and the inversion
+// flag.
+constexpr int kNoAllocMaxChunks = 16384;  // => at most 16,777,216 tets per call
+constexpr size_t kNoAllocScratchBytes = sizeof(double) * kNoAllocMaxChunks + 256;
+// Held by every GPU that loads the library, until exit (128 KB + 256 B).
+// Every call shares it and the last call's contents stay: the flag word is
+// cleared at the start of each call, the chunk sums are overwritten.
+static __device__ __align__(256) unsigned char g_tet_energy_scratch[kNoAllocScratchBytes];
+
+__global__ void k_tet_energy_noalloc(int T, const int4* __restrict__ tet, const double* __restrict__ X,
+                                     const double* __restrict__ IB, const double* __restrict__ vol,
+                                     const double* __restrict__ lam, const double* __restrict__ mu, double w,
+                                     unsigned char* __restrict__ scratch) {
+    double* chunk_E = reinterpret_cast<double*>(scratch);
+    int* bad_flag = reinterpret_cast<int*>(scratch + sizeof(double) * kNoAllocMaxChunks);
+    const int begin = blockIdx.x * kChunk, end = min(T, begin + kChunk);
+    double acc = 0.0;
+    int bad = 0;
+    for (int t = begin + threadIdx.x; t < end; t += blockDim.x) {
+        double F[9];
+        load_F(X, tet[t], IB + 9 * (long)t, F);
+        double J = det3(F);
+        if (J <= 0) { bad = 1; continue; }
+        double f2 = 0;
+#pragma unroll
+        for (int k = 0; k < 9; ++k) f2 += F[k] * F[k];
+        double lJ = log(J);
+        double m = mu[t], l = lam[t];
+        acc += w * vol[t] * (m / 2.0 * (f2 - 3.0) - (m - l / 2.0 * lJ) * lJ);
+    }
+    double s = block_sum(acc);
+    if (bad) *bad_flag = 1;
+    if (threadIdx.x == 0) chunk_E[blockIdx.x] = s;
+}
+
+__global__ void k_tet_energy_noalloc_sum(int nchunks, const unsigned char* __restrict__ scratch,
+                                         double* __restrict__ energy, int* __restrict__ inverted) {
+    const double* chunk_E = reinterpret_cast<const double*>(scratch);
+    const int* bad_flag = reinterpret_cast<const int*>(scratch + sizeof(double) * kNoAllocMaxChunks);
+    double s = 0;
+    for (int c = 0; c < nchunks; ++c) s += chunk_E[c];
+    *energy = s;
+    *inverted = *bad_flag;
+}
+
+// device address of the scratch array, looked up once per device
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+unsigned char* g_noalloc_addr[kNoAllocMaxDevices] = {};
+
+}  // namespace
+
 }  // namespace idp
+
+extern "C" int idp_tet_energy_noalloc(int T, const int32_t* tets, const double* X, const double* IB,
+                                      const double* vol, const double* lam, const double* mu, double weight,
+                                      double* energy, int32_t* inverted, void* stream) {
+    using namespace idp;
+    if (T < 0 || !energy || !inverted) return IDP_ERR_INVALID_ARG;
+    if (T > 0 && (!tets || !X || !IB || !vol || !lam || !mu)) return IDP_ERR_INVALID_ARG;
+    if ((long)T > (long)kNoAllocMaxChunks * kChunk) return IDP_ERR_CAPACITY;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices) return IDP_ERR_CUDA;
+    unsigned char* scratch = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_noalloc_mu);
+        if (!g_noalloc_addr[dev]) {
+            // first call on this device: the symbol's device address (the
+            // name itself is only a host-side stand-in)
+            void* p = nullptr;
+            if (cudaGetSymbolAddress(&p, g_tet_energy_scratch) != cudaSuccess || !p) return IDP_ERR_CUDA;
+            g_noalloc_addr[dev] = static_cast<unsigned char*>(p);
+        }
+        scratch = g_noalloc_addr[dev];
+    }
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const int nchunks = (T + kChunk - 1) / kChunk;
+    if (cudaMemsetAsync(scratch + sizeof(double) * kNoAllocMaxChunks, 0, sizeof(int), s) != cudaSuccess)
+        return IDP_ERR_CUDA;
+    if (nchunks > 0)
+        (::idp::count_launch(),
+         k_tet_energy_noalloc<<<nchunks, kBlock, 0, s>>>(T, reinterpret_cast<const int4*>(tets), X, IB, vol, lam, mu,
+                                                         weight, scratch));
+    (::idp::count_launch(), k_tet_energy_noalloc_sum<<<1, 1, 0, s>>>(nchunks, scratch, energy, inverted));
+    return cudaGetLastError() == cudaSuccess ? IDP_OK : IDP_ERR_CUDA;
+}

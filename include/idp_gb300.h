@@ -191,6 +191,28 @@ int idp_hessian_apply(idp_ctx* ctx, int inst, const double* X, const double* x, 
  * iterations in *iters and the final relative residual in *relres. */
 int idp_newton_direction(idp_ctx* ctx, int inst, const double* X, double* p, int* iters, double* relres);
 
+/* Elastic energy weight * sum_t vol_t * Psi(F_t) of one tet mesh held in the
+ * caller's DEVICE memory, without allocating anything: for callers that may
+ * not call cudaMalloc while they run (a host application that reserved the
+ * whole GPU budget up front and lends the library only its own buffers, or a
+ * frame loop that cannot take the device-wide synchronisation of
+ * cudaMalloc/cudaFree). No counterpart in the reference; it gives the same
+ * number as idp_eval_energy's elastic term (same per-tet arithmetic and
+ * reduction order) for a context-free caller.
+ *   tets (4T int32), X (3V), IB (9T, row-major inverse rest basis), vol (T),
+ *   lam (T), mu (T): device pointers. energy (1 double) and inverted (1 int32,
+ *   set to 1 when some det F <= 0) are device pointers written by the call.
+ *   stream: a cudaStream_t (NULL = legacy default stream); the call is
+ *   asynchronous on it.
+ * At most 16,777,216 tets per call (IDP_ERR_CAPACITY beyond). Scratch is a
+ * fixed 128 KB device array inside the library shared by every call on a GPU:
+ * calls that overlap on the GPU (other streams, other threads) race on it, so
+ * order them. The first call on each device looks up that array's device
+ * address; make it before any stream capture. */
+int idp_tet_energy_noalloc(int T, const int32_t* tets, const double* X, const double* IB, const double* vol,
+                           const double* lam, const double* mu, double weight, double* energy, int32_t* inverted,
+                           void* stream);
+
 #ifdef __cplusplus
 }
 #endif
