@@ -60,6 +60,8 @@ def parse():
     ap.add_argument("--blob-n", type=int, default=64)
     ap.add_argument("--flow-step", type=float, default=0.05)
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--pcg-grid-cta-vertices", type=int, default=0,
+                    help="vertices per CTA of the grid-wide PCG (0 = library default)")
     ap.add_argument("--instances", type=int, default=256)
     ap.add_argument("--mode", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--max-newton", type=int, default=2000)
@@ -277,7 +279,8 @@ def run_flow(args):
     V = p["X"].shape[0]
 
     def make_ctx(m):
-        c = idp.Context(h=H, newton_tol=1e-3, max_newton=args.max_newton, mode=m, device=local)
+        c = idp.Context(h=H, newton_tol=1e-3, max_newton=args.max_newton, mode=m, device=local,
+                        pcg_grid_cta_vertices=args.pcg_grid_cta_vertices)
         c.add_instance(p["X"], p["tets"], p["mass"], p["lam"], p["mu"], p["dHat2"], p["kappa"], p["kappa_max"])
         c.commit()
         return c

@@ -279,8 +279,9 @@ __global__ void k_ccd_query_pt(long nN, const int* __restrict__ nodes, const int
                                const BoxI* __restrict__ tbox, const BoxI* __restrict__ nboxc,
                                const BoxI* __restrict__ tboxc, const GridP* __restrict__ gp,
                                const double* __restrict__ thick, const uint64_t* __restrict__ ckey,
-                               const uint32_t* __restrict__ cstart, int ncell, const uint32_t* __restrict__ entries,
+                               const uint32_t* __restrict__ cstart, const uint32_t* __restrict__ ncell_p, const uint32_t* __restrict__ entries,
                                CCand* __restrict__ out, unsigned int* counter, long cap) {
+    const int ncell = (int)*ncell_p;
     long s = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (s >= nN) return;
     int inst = ninst[s];
@@ -328,9 +329,10 @@ __global__ void k_ccd_query_ee(long nE, const int2* __restrict__ edges, const in
                                const double* __restrict__ dir, const unsigned char* __restrict__ dbc,
                                const BoxI* __restrict__ ebox, const BoxI* __restrict__ eboxc,
                                const GridP* __restrict__ gp, const double* __restrict__ thick,
-                               const uint64_t* __restrict__ ckey, const uint32_t* __restrict__ cstart, int ncell,
+                               const uint64_t* __restrict__ ckey, const uint32_t* __restrict__ cstart, const uint32_t* __restrict__ ncell_p,
                                const uint32_t* __restrict__ entries, CCand* __restrict__ out, unsigned int* counter,
                                long cap) {
+    const int ncell = (int)*ncell_p;
     long eI = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (eI >= nE) return;
     int inst = einst[eI];
@@ -439,14 +441,15 @@ __device__ int accd_ee(D3 ea0, D3 ea1, D3 eb0, D3 eb1, D3 dea0, D3 dea1, D3 deb0
 }
 
 // flags per instance: bit 0 = an ACCD hit its cap, bit 1 = zero step
-__global__ void k_accd(long npt, long nee, const CCand* __restrict__ cand, const int* __restrict__ nodes,
+__global__ void k_accd(long npt, long nee, const CCand* __restrict__ cand_pt, const CCand* __restrict__ cand_ee,
+                       const int* __restrict__ nodes,
                        const int* __restrict__ ninst, const int* __restrict__ tris, const int2* __restrict__ edges,
                        const int* __restrict__ einst, const double* __restrict__ X, const double* __restrict__ dir,
                        const double* __restrict__ thick, const double* __restrict__ alpha_cap,
                        double* __restrict__ alpha_min, int* __restrict__ flags) {
     long k = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= npt + nee) return;
-    CCand c = cand[k];
+    CCand c = k < npt ? cand_pt[k] : cand_ee[k - npt];
     int inst;
     double toc;
     int r, its = 0;
@@ -542,42 +545,41 @@ int ccd_stepsize(Arena& A, Work& W, const double* X, const double* dir, double* 
     (::idp::count_launch(), k_coarse_boxes<<<grid_for(St + Se + Sn), kBlock, 0, s>>>(St + Se + Sn, tbox, tboxc));
     (::idp::count_launch(), k_coarse_grid<<<grid_for(nI), kBlock, 0, s>>>(nI, gp, gc));
     BoxGrid gt, ge;
-    int rc = build_box_grid(W, 0, tboxc, A.st_inst, A.active, A.St, gc, nI, gt, s);
+    uint32_t* hp = W.pinned();
+    if (!hp) return IDP_ERR_CUDA;
+    int rc = box_grid_count(W, 0, tboxc, A.st_inst, A.active, A.St, hp, s);
+    if (!rc) rc = box_grid_count(W, 1, eboxc, A.se_inst, A.active, A.Se, hp + 1, s);
     if (rc) return rc;
-    rc = build_box_grid(W, 1, eboxc, A.se_inst, A.active, A.Se, gc, nI, ge, s);
-    if (rc) return rc;
-    // candidates
+    IDP_CUDA_TRY(cudaStreamSynchronize(s));
+    const long nt_ent = hp[0], ne_ent = hp[1];
+    if ((rc = box_grid_finish(W, 0, tboxc, A.st_inst, A.active, A.St, gc, nI, nt_ent, gt, s))) return rc;
+    if ((rc = box_grid_finish(W, 1, eboxc, A.se_inst, A.active, A.Se, gc, nI, ne_ent, ge, s))) return rc;
+    // candidates: PT in [0, cap_pt), EE in [cap_pt, cap_pt + cap_ee), one
+    // host round trip for both counts
     if (W[W_CAND_CNT].ensure(64)) return IDP_ERR_CUDA;
     unsigned int* ccount = W[W_CAND_CNT].as<unsigned int>();
-    long cap = (long)(W[W_CAND].bytes / sizeof(CCand));
-    if (cap < 4 * (A.Sn + A.Se) + 1024) {
-        cap = 4 * (A.Sn + A.Se) + 1024;
-        if (W[W_CAND].ensure(sizeof(CCand) * cap)) return IDP_ERR_CUDA;
-    }
+    long cap_pt = std::max<long>(W.ccd_cap_pt, 4 * A.Sn + 1024);
+    long cap_ee = std::max<long>(W.ccd_cap_ee, 4 * A.Se + 1024);
     for (int attempt = 0; attempt < 6; ++attempt) {
+        if (W[W_CAND].ensure(sizeof(CCand) * (cap_pt + cap_ee))) return IDP_ERR_CUDA;
         CCand* cand = W[W_CAND].as<CCand>();
-        unsigned int hc[2] = {0, 0};
         IDP_CUDA_TRY(cudaMemsetAsync(ccount, 0, 2 * sizeof(unsigned int), s));
         if (A.Sn)
             (::idp::count_launch(), k_ccd_query_pt<<<grid_for(32 * A.Sn), kBlock, 0, s>>>(A.Sn, A.snode, A.sn_inst, A.active, X, dir, A.dbc, A.stri,
                                                              nbox, tbox, nboxc, tboxc, gc, A.thickness, gt.cell_keys, gt.cell_start,
-                                                             gt.ncell, gt.entries, cand, ccount, cap));
-        IDP_CUDA_TRY(cudaMemcpyAsync(hc, ccount, sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
-        IDP_CUDA_TRY(cudaStreamSynchronize(s));
-        long npt = hc[0];
-        long cap_ee = cap - npt;
-        if (A.Se && cap_ee > 0)
+                                                             gt.d_ncell, gt.entries, cand, ccount, cap_pt));
+        if (A.Se)
             (::idp::count_launch(), k_ccd_query_ee<<<grid_for(32 * A.Se), kBlock, 0, s>>>(A.Se, A.sedge, A.se_inst, A.active, X, dir, A.dbc, ebox, eboxc, gc,
-                                                             A.thickness, ge.cell_keys, ge.cell_start, ge.ncell,
-                                                             ge.entries, cand + npt, ccount + 1, cap_ee));
-        IDP_CUDA_TRY(cudaMemcpyAsync(hc + 1, ccount + 1, sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
+                                                             A.thickness, ge.cell_keys, ge.cell_start, ge.d_ncell,
+                                                             ge.entries, cand + cap_pt, ccount + 1, cap_ee));
+        IDP_CUDA_TRY(cudaMemcpyAsync(hp + 2, ccount, 2 * sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
         IDP_CUDA_TRY(cudaStreamSynchronize(s));
-        long nee = hc[1];
-        if (npt + nee <= cap && (A.Se == 0 || cap_ee > 0)) {
+        const long npt = hp[2], nee = hp[3];
+        if (npt <= cap_pt && nee <= cap_ee) {
             (::idp::count_launch(), k_fill<<<grid_for(nI), kBlock, 0, s>>>(nI, 1e300, amin));
             IDP_CUDA_TRY(cudaMemsetAsync(flags, 0, sizeof(int) * nI, s));
             if (npt + nee)
-                (::idp::count_launch(), k_accd<<<grid_for(npt + nee, 128), 128, 0, s>>>(npt, nee, cand, A.snode, A.sn_inst, A.stri, A.sedge,
+                (::idp::count_launch(), k_accd<<<grid_for(npt + nee, 128), 128, 0, s>>>(npt, nee, cand, cand + cap_pt, A.snode, A.sn_inst, A.stri, A.sedge,
                                                                 A.se_inst, X, dir, A.thickness, alpha, amin, flags));
             (::idp::count_launch(), k_alpha_final<<<grid_for(nI), kBlock, 0, s>>>(nI, A.active, amin, alpha));
             if (std::getenv("IDP_PROFILE")) {
@@ -594,8 +596,10 @@ int ccd_stepsize(Arena& A, Work& W, const double* X, const double* dir, double* 
             }
             return cudaGetLastError() == cudaSuccess ? IDP_OK : IDP_ERR_CUDA;
         }
-        cap = 2 * (npt + nee) + 1024;
-        if (W[W_CAND].ensure(sizeof(CCand) * cap)) return IDP_ERR_CUDA;
+        if (npt > cap_pt) cap_pt = npt + npt / 2 + 1024;
+        if (nee > cap_ee) cap_ee = nee + nee / 2 + 1024;
+        W.ccd_cap_pt = cap_pt;
+        W.ccd_cap_ee = cap_ee;
     }
     return IDP_ERR_CAPACITY;
 }

@@ -172,9 +172,10 @@ __global__ void k_query_pt(long nN, const int* __restrict__ nodes, const int* __
                            const unsigned char* __restrict__ dbc, const int* __restrict__ tris,
                            const BoxI* __restrict__ tbox, const GridP* __restrict__ gp,
                            const double* __restrict__ dHat2, const double* __restrict__ thick,
-                           const uint64_t* __restrict__ ckey, const uint32_t* __restrict__ cstart, int ncell,
+                           const uint64_t* __restrict__ ckey, const uint32_t* __restrict__ cstart, const uint32_t* __restrict__ ncell_p,
                            const uint32_t* __restrict__ entries, Cand* __restrict__ out, unsigned int* counter,
                            long cap) {
+    const int ncell = (int)*ncell_p;
     long s = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (s >= nN) return;  // whole warp leaves together
     int inst = ninst[s];
@@ -214,8 +215,9 @@ __global__ void k_query_ee(long nE, const int2* __restrict__ edges, const int* _
                            const unsigned char* __restrict__ dbc, const BoxI* __restrict__ ebox,
                            const GridP* __restrict__ gp, const double* __restrict__ dHat2,
                            const double* __restrict__ thick, const uint64_t* __restrict__ ckey,
-                           const uint32_t* __restrict__ cstart, int ncell, const uint32_t* __restrict__ entries,
+                           const uint32_t* __restrict__ cstart, const uint32_t* __restrict__ ncell_p, const uint32_t* __restrict__ entries,
                            Cand* __restrict__ out, unsigned int* counter, long cap) {
+    const int ncell = (int)*ncell_p;
     long eI = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (eI >= nE) return;
     int inst = einst[eI];
@@ -389,10 +391,11 @@ __global__ void k_merge_write(long n, const Rec* __restrict__ recs, const uint32
     cinst[pos[i]] = r.inst;
 }
 
-__global__ void k_inst_offsets(int nI, long C, const int* __restrict__ cinst, int* __restrict__ off) {
+__global__ void k_inst_offsets(int nI, const uint32_t* __restrict__ count, const int* __restrict__ cinst,
+                               int* __restrict__ off) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i > nI) return;
-    long lo = 0, hi = C;
+    long lo = 0, hi = *count;
     while (lo < hi) {
         long mid = (lo + hi) >> 1;
         if (cinst[mid] < i) lo = mid + 1;
@@ -416,9 +419,21 @@ __global__ void k_min_dist2(long C, const int4* __restrict__ cons, const int* __
 }  // namespace
 
 // ---------------------------------------------------------------- host side
-int build_box_grid(Work& W, int slot, const BoxI* boxes, const int* inst, const unsigned char* active, long nprim,
-                   const GridP* gp, int nI, BoxGrid& out, cudaStream_t s) {
-    (void)nI;
+int box_grid_count(Work& W, int slot, const BoxI* boxes, const int* inst, const unsigned char* active, long nprim,
+                   uint32_t* h_total, cudaStream_t s) {
+    DBuf& bcnt = W[(slot == 0 ? W_GRID0 : W_GRID1) + 0];
+    long np = nprim > 0 ? nprim : 1;
+    if (bcnt.ensure(sizeof(uint32_t) * (np + 1))) return IDP_ERR_CUDA;
+    if (W[W_SCRATCH].ensure(scan_scratch_bytes(np) + 64)) return IDP_ERR_CUDA;
+    uint32_t* cnt = bcnt.as<uint32_t>();
+    (::idp::count_launch(), k_box_count<<<grid_for(np), kBlock, 0, s>>>(nprim, boxes, inst, active, cnt));
+    if (scan_exclusive(cnt, cnt, nprim, cnt + nprim, W[W_SCRATCH].p, s) != cudaSuccess) return IDP_ERR_CUDA;
+    IDP_CUDA_TRY(cudaMemcpyAsync(h_total, cnt + nprim, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    return IDP_OK;
+}
+
+int box_grid_finish(Work& W, int slot, const BoxI* boxes, const int* inst, const unsigned char* active, long nprim,
+                    const GridP* gp, int nI, long ne, BoxGrid& out, cudaStream_t s) {
     int base = slot == 0 ? W_GRID0 : W_GRID1;
     DBuf& bcnt = W[base + 0];
     DBuf& bkeys = W[base + 1];
@@ -427,45 +442,36 @@ int build_box_grid(Work& W, int slot, const BoxI* boxes, const int* inst, const 
     DBuf& bvals2 = W[base + 4];
     DBuf& bcell = W[base + 5];
     long np = nprim > 0 ? nprim : 1;
-    if (bcnt.ensure(sizeof(uint32_t) * (np + 1))) return IDP_ERR_CUDA;
-    if (W[W_SCRATCH].ensure(scan_scratch_bytes(np) + 64)) return IDP_ERR_CUDA;
-    uint32_t* cnt = bcnt.as<uint32_t>();
-    (::idp::count_launch(), k_box_count<<<grid_for(np), kBlock, 0, s>>>(nprim, boxes, inst, active, cnt));
-    if (scan_exclusive(cnt, cnt, nprim, cnt + nprim, W[W_SCRATCH].p, s) != cudaSuccess) return IDP_ERR_CUDA;
-    uint32_t total = 0;
-    IDP_CUDA_TRY(cudaMemcpyAsync(&total, cnt + nprim, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-    IDP_CUDA_TRY(cudaStreamSynchronize(s));
-    long ne = total;
     long nalloc = ne > 0 ? ne : 1;
     if (bkeys.ensure(8 * nalloc) || bvals.ensure(4 * nalloc) || bkeys2.ensure(8 * nalloc) || bvals2.ensure(4 * nalloc))
         return IDP_ERR_CUDA;
     if (bcell.ensure((8 + 4) * (nalloc + 1) + 4 * (nalloc + 1) * 2 + 64)) return IDP_ERR_CUDA;
-    (::idp::count_launch(), k_box_emit<<<grid_for(np), kBlock, 0, s>>>(nprim, boxes, inst, active, gp, cnt, bkeys.as<uint64_t>(),
-                                               bvals.as<uint32_t>()));
+    uint32_t* cnt = bcnt.as<uint32_t>();
+    (::idp::count_launch(), k_box_emit<<<grid_for(np), kBlock, 0, s>>>(nprim, boxes, inst, active, gp, cnt,
+                                                                       bkeys.as<uint64_t>(), bvals.as<uint32_t>()));
     int bits = 32 + bits_for((uint64_t)(nI > 0 ? nI : 1));
     if (W[W_SCRATCH].ensure(radix_sort_scratch_bytes(nalloc) + scan_scratch_bytes(nalloc) + 64)) return IDP_ERR_CUDA;
     if (radix_sort_pairs(bkeys.as<uint64_t>(), bvals.as<uint32_t>(), bkeys2.as<uint64_t>(), bvals2.as<uint32_t>(), ne,
                          bits, W[W_SCRATCH].p, s) != cudaSuccess)
         return IDP_ERR_CUDA;
-    // cell table: ckey (8B x (ne+1)) | cstart (4B x (ne+1)) | head | idx
+    // cell table: ckey (8B x (ne+1)) | cstart (4B x (ne+1)) | head | idx (+ cell count at idx[ne])
     uint64_t* ckey = bcell.as<uint64_t>();
     uint32_t* cstart = reinterpret_cast<uint32_t*>(ckey + nalloc + 1);
     uint32_t* head = cstart + nalloc + 1;
     uint32_t* idx = head + nalloc + 1;
-    uint32_t ncell = 0;
     if (ne > 0) {
         (::idp::count_launch(), k_mark_heads<<<grid_for(ne), kBlock, 0, s>>>(ne, bkeys.as<uint64_t>(), head));
         if (scan_exclusive(head, idx, ne, idx + ne, W[W_SCRATCH].p, s) != cudaSuccess) return IDP_ERR_CUDA;
-        (::idp::count_launch(), k_cell_table<<<grid_for(ne), kBlock, 0, s>>>(ne, bkeys.as<uint64_t>(), head, idx, ckey, cstart, idx + ne));
-        IDP_CUDA_TRY(cudaMemcpyAsync(&ncell, idx + ne, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-        IDP_CUDA_TRY(cudaStreamSynchronize(s));
+        (::idp::count_launch(), k_cell_table<<<grid_for(ne), kBlock, 0, s>>>(ne, bkeys.as<uint64_t>(), head, idx, ckey,
+                                                                              cstart, idx + ne));
     } else {
         IDP_CUDA_TRY(cudaMemsetAsync(cstart, 0, sizeof(uint32_t), s));
+        IDP_CUDA_TRY(cudaMemsetAsync(idx + ne, 0, sizeof(uint32_t), s));
     }
     out.cell_keys = ckey;
     out.cell_start = cstart;
     out.entries = bvals.as<uint32_t>();
-    out.ncell = (int)ncell;
+    out.d_ncell = idx + ne;
     out.nent = ne;
     return IDP_OK;
 }
@@ -490,39 +496,55 @@ int build_constraint_set(Arena& A, Work& W, const double* X, ContactSet& cs, cud
         (::idp::count_launch(), k_prim_boxes<2><<<grid_for(A.Se), kBlock, 0, s>>>(A.Se, reinterpret_cast<const int*>(A.sedge), A.se_inst,
                                                            A.active, X, gp, ebox));
     BoxGrid gt, ge;
-    int rc = build_box_grid(W, 0, tbox, A.st_inst, A.active, A.St, gp, nI, gt, s);
+    uint32_t* hp = W.pinned();
+    if (!hp) return IDP_ERR_CUDA;
+    int rc = box_grid_count(W, 0, tbox, A.st_inst, A.active, A.St, hp, s);
+    if (!rc) rc = box_grid_count(W, 1, ebox, A.se_inst, A.active, A.Se, hp + 1, s);
     if (rc) return rc;
-    rc = build_box_grid(W, 1, ebox, A.se_inst, A.active, A.Se, gp, nI, ge, s);
-    if (rc) return rc;
+    IDP_CUDA_TRY(cudaStreamSynchronize(s));
+    const long nt_ent = hp[0], ne_ent = hp[1];
+    if ((rc = box_grid_finish(W, 0, tbox, A.st_inst, A.active, A.St, gp, nI, nt_ent, gt, s))) return rc;
+    if ((rc = box_grid_finish(W, 1, ebox, A.se_inst, A.active, A.Se, gp, nI, ne_ent, ge, s))) return rc;
 
-    // 3. candidates (PT then EE share one list, PT first)
+    // 3. candidates: PT in [0, cap_pt), EE in [cap_pt, cap_pt + cap_ee);
+    // both queries run before one host round trip reads both counts
     if (W[W_CAND_CNT].ensure(64)) return IDP_ERR_CUDA;
     unsigned int* ccount = W[W_CAND_CNT].as<unsigned int>();
-    long cap = (long)(W[W_CAND].bytes / sizeof(Cand));
-    if (cap < 4 * (A.Sn + A.Se) + 1024) {
-        cap = 4 * (A.Sn + A.Se) + 1024;
-        if (W[W_CAND].ensure(sizeof(Cand) * cap)) return IDP_ERR_CUDA;
-    }
-    unsigned int hc[2];
+    long cap_pt = std::max<long>(W.cand_cap_pt, 2 * A.Sn + 512);
+    long cap_ee = std::max<long>(W.cand_cap_ee, 2 * A.Se + 512);
     for (int attempt = 0; attempt < 4; ++attempt) {
+        if (W[W_CAND].ensure(sizeof(Cand) * (cap_pt + cap_ee))) return IDP_ERR_CUDA;
         Cand* cand = W[W_CAND].as<Cand>();
         IDP_CUDA_TRY(cudaMemsetAsync(ccount, 0, 2 * sizeof(unsigned int), s));
         if (A.Sn)
             (::idp::count_launch(), k_query_pt<<<grid_for(32 * A.Sn), kBlock, 0, s>>>(A.Sn, A.snode, A.sn_inst, A.active, X, A.dbc, A.stri, tbox, gp,
-                                                         A.dHat2, A.thickness, gt.cell_keys, gt.cell_start, gt.ncell,
-                                                         gt.entries, cand, ccount, cap));
-        IDP_CUDA_TRY(cudaMemcpyAsync(hc, ccount, sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
-        IDP_CUDA_TRY(cudaStreamSynchronize(s));
-        long npt = hc[0];
-        long cap_ee = cap - npt;
-        if (A.Se && cap_ee > 0)
+                                                         A.dHat2, A.thickness, gt.cell_keys, gt.cell_start, gt.d_ncell,
+                                                         gt.entries, cand, ccount, cap_pt));
+        if (A.Se)
             (::idp::count_launch(), k_query_ee<<<grid_for(32 * A.Se), kBlock, 0, s>>>(A.Se, A.sedge, A.se_inst, A.active, X, A.dbc, ebox, gp, A.dHat2,
-                                                         A.thickness, ge.cell_keys, ge.cell_start, ge.ncell, ge.entries,
-                                                         cand + npt, ccount + 1, cap_ee));
-        IDP_CUDA_TRY(cudaMemcpyAsync(hc + 1, ccount + 1, sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
+                                                         A.thickness, ge.cell_keys, ge.cell_start, ge.d_ncell, ge.entries,
+                                                         cand + cap_pt, ccount + 1, cap_ee));
+        IDP_CUDA_TRY(cudaMemcpyAsync(hp + 2, ccount, 2 * sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
         IDP_CUDA_TRY(cudaStreamSynchronize(s));
-        long nee = hc[1];
-        if (npt + nee <= cap && (A.Se == 0 || cap_ee > 0)) {
+        const long npt = hp[2], nee = hp[3];
+        if (npt > cap_pt || nee > cap_ee) {
+            if (npt > cap_pt) cap_pt = npt + npt / 2 + 1024;
+            if (nee > cap_ee) cap_ee = nee + nee / 2 + 1024;
+            W.cand_cap_pt = cap_pt;
+            W.cand_cap_ee = cap_ee;
+            continue;
+        }
+        if (npt + nee == 0) {
+            cs.C = 0;
+            cs.off.assign(nI + 1, 0);
+            if (W[W_CONS_OFF].ensure(sizeof(int) * (nI + 1)) || W[W_CONS].ensure(sizeof(int4)) ||
+                W[W_CONS_INST].ensure(sizeof(int)))
+                return IDP_ERR_CUDA;
+            IDP_CUDA_TRY(cudaMemsetAsync(W[W_CONS_OFF].p, 0, sizeof(int) * (nI + 1), s));
+            cs.d_off = W[W_CONS_OFF].as<int>();
+            return IDP_OK;
+        }
+        {
             // 4. narrow phase
             long rcap = (long)(W[W_CONS_TMP].bytes / sizeof(Rec));
             if (rcap < npt + nee + 1) {
@@ -535,7 +557,7 @@ int build_constraint_set(Arena& A, Work& W, const double* X, ContactSet& cs, cud
                 (::idp::count_launch(), k_narrow_pt<<<grid_for(npt), kBlock, 0, s>>>(npt, cand, A.snode, A.sn_inst, A.stri, X, A.dHat2, A.thickness,
                                                              recs, ccount, rcap));
             if (nee)
-                (::idp::count_launch(), k_narrow_ee<<<grid_for(nee), kBlock, 0, s>>>(nee, cand + npt, A.sedge, A.se_inst, X, A.X0, A.dHat2,
+                (::idp::count_launch(), k_narrow_ee<<<grid_for(nee), kBlock, 0, s>>>(nee, cand + cap_pt, A.sedge, A.se_inst, X, A.X0, A.dHat2,
                                                              A.thickness, recs, ccount, rcap));
             unsigned int nrec = 0;
             IDP_CUDA_TRY(cudaMemcpyAsync(&nrec, ccount, sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
@@ -573,20 +595,23 @@ int build_constraint_set(Arena& A, Work& W, const double* X, ContactSet& cs, cud
                 (::idp::count_launch(), k_merge_heads<<<grid_for(n), kBlock, 0, s>>>(n, recs, p2, head));
                 if (scan_exclusive(head, pos, n, pos + n, W[W_SCRATCH].p, s) != cudaSuccess) return IDP_ERR_CUDA;
                 (::idp::count_launch(), k_merge_write<<<grid_for(n), kBlock, 0, s>>>(n, recs, p2, head, pos, cons, cinst));
+                // per-instance offsets from the device-side count, then one
+                // round trip for the count and the offsets
+                (::idp::count_launch(), k_inst_offsets<<<grid_for(nI + 1), kBlock, 0, s>>>(nI, pos + n, cinst,
+                                                                                            W[W_CONS_OFF].as<int>()));
+                cs.off.resize(nI + 1);
                 IDP_CUDA_TRY(cudaMemcpyAsync(&total, pos + n, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+                IDP_CUDA_TRY(cudaMemcpyAsync(cs.off.data(), W[W_CONS_OFF].as<int>(), sizeof(int) * (nI + 1),
+                                             cudaMemcpyDeviceToHost, s));
                 IDP_CUDA_TRY(cudaStreamSynchronize(s));
+            } else {
+                cs.off.assign(nI + 1, 0);
+                IDP_CUDA_TRY(cudaMemsetAsync(W[W_CONS_OFF].p, 0, sizeof(int) * (nI + 1), s));
             }
             cs.C = total;
-            (::idp::count_launch(), k_inst_offsets<<<grid_for(nI + 1), kBlock, 0, s>>>(nI, cs.C, cinst, W[W_CONS_OFF].as<int>()));
-            cs.off.resize(nI + 1);
-            IDP_CUDA_TRY(cudaMemcpyAsync(cs.off.data(), W[W_CONS_OFF].as<int>(), sizeof(int) * (nI + 1),
-                                         cudaMemcpyDeviceToHost, s));
-            IDP_CUDA_TRY(cudaStreamSynchronize(s));
             cs.d_off = W[W_CONS_OFF].as<int>();
             return IDP_OK;
         }
-        cap = 2 * (npt + nee) + 1024;
-        if (W[W_CAND].ensure(sizeof(Cand) * cap)) return IDP_ERR_CUDA;
     }
     return IDP_ERR_CAPACITY;
 }

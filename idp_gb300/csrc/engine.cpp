@@ -205,11 +205,17 @@ int eval_energy(idp_ctx* c, const double* X, bool with_barrier, std::vector<doub
         rc = barrier_energy(A, c->W, X, c->cs, dsc(c, S_EBAR), isc(c, SI_BADB), c->s);
         if (rc) return rc;
     }
-    std::vector<double> et, ei, eb;
-    std::vector<int> b1, b2;
-    if ((rc = fetch(c, dsc(c, S_ETET), et)) || (rc = fetch(c, dsc(c, S_EINERT), ei)) || (rc = fetch(c, dsc(c, S_EBAR), eb)) ||
-        (rc = fetch(c, isc(c, SI_BAD), b1)) || (rc = fetch(c, isc(c, SI_BADB), b2)))
-        return rc;
+    // one copy of the whole per-instance scalar block, one synchronisation
+    std::vector<double> hb((size_t)(S_NUMD + S_NUMI) * nI);
+    IDP_CUDA_TRY(cudaMemcpyAsync(hb.data(), c->inst_buf.p, sizeof(double) * S_NUMD * nI + sizeof(int) * S_NUMI * nI,
+                                 cudaMemcpyDeviceToHost, c->s));
+    IDP_CUDA_TRY(cudaStreamSynchronize(c->s));
+    const double* et = hb.data() + (size_t)S_ETET * nI;
+    const double* ei = hb.data() + (size_t)S_EINERT * nI;
+    const double* eb = hb.data() + (size_t)S_EBAR * nI;
+    const int* hi = reinterpret_cast<const int*>(hb.data() + (size_t)S_NUMD * nI);
+    const int* b1 = hi + (size_t)SI_BAD * nI;
+    const int* b2 = hi + (size_t)SI_BADB * nI;
     E.resize(nI);
     bad.resize(nI);
     for (int i = 0; i < nI; ++i) {
@@ -319,7 +325,7 @@ idp_ctx* idp_create(const idp_params* p, int* status) {
     if (p) c->P = *p;
     else idp_default_params(&c->P);
     c->W.grid_min_v = c->P.pcg_grid_min_vertices > 0 ? c->P.pcg_grid_min_vertices : 16384;
-    c->W.grid_vper = c->P.pcg_grid_cta_vertices > 0 ? c->P.pcg_grid_cta_vertices : 128;
+    c->W.grid_vper = c->P.pcg_grid_cta_vertices > 0 ? c->P.pcg_grid_cta_vertices : 112;
     if (cudaSetDevice(c->P.device) != cudaSuccess || cudaStreamCreateWithFlags(&c->s, cudaStreamNonBlocking) != cudaSuccess) {
         delete c;
         if (status) *status = IDP_ERR_CUDA;
@@ -781,6 +787,8 @@ int idp_advance(idp_ctx* c, idp_result* results) {
         // backtracking until E <= Eprev
         srch = mask;
         std::vector<double> Eacc(nI, 0.0);
+        std::vector<int> acc_trial(nI, -1);
+        int last_trial = -1;
         for (int trial = 0; trial < 200; ++trial) {
             bool anys = false;
             for (int i = 0; i < nI; ++i) anys |= srch[i] != 0;
@@ -798,6 +806,7 @@ int idp_advance(idp_ctx* c, idp_result* results) {
             // constraint set + min-distance safeguard on the valid ones
             if ((rc = set_mask(c, valid))) return rc;
             if ((rc = build_cs(A.X))) return rc;
+            last_trial = trial;
             std::vector<double> md(nI, 1e300);
             IDP_CUDA_TRY(cudaMemcpyAsync(dsc(c, S_MIND), md.data(), sizeof(double) * nI, cudaMemcpyHostToDevice, s));
             if ((rc = constraint_min_dist2(A, W, A.X, W[W_CONS].as<int4>(), W[W_CONS_INST].as<int>(), c->cs.C, nullptr,
@@ -825,15 +834,20 @@ int idp_advance(idp_ctx* c, idp_result* results) {
                 if (ok) {
                     srch[i] = 0;
                     Eacc[i] = E[i];
+                    acc_trial[i] = trial;
                 }
             }
         }
         for (int i = 0; i < nI; ++i)
             if (srch[i]) st[i].status = IDP_ERR_ZERO_STEP;  // line search exhausted
         W.timer.stop(s);
-        // X holds every instance's accepted trial; rebuild their constraint set
+        // X holds every instance's accepted trial; rebuild their constraint
+        // set unless the last trial's build already covered all of them
         if ((rc = set_mask(c, mask))) return rc;
-        if ((rc = build_cs(A.X))) return rc;
+        bool fresh = last_trial >= 0;
+        for (int i = 0; i < nI; ++i)
+            if (mask[i] && acc_trial[i] != last_trial) fresh = false;
+        if (!fresh && (rc = build_cs(A.X))) return rc;
         for (int i = 0; i < nI; ++i)
             if (mask[i]) {
                 st[i].Eprev = Eacc[i];
@@ -910,6 +924,13 @@ int idp_advance(idp_ctx* c, idp_result* results) {
                          W.accd_pairs, W.accd_total, W.accd_maxit, W.accd_long, W.cl.n, W.cl.max_n,
                          (long long)W.stats.pcg_iters);
             W.accd_maxit = W.accd_long = W.accd_total = W.accd_pairs = 0;
+            if (W.grid_prof[4]) {
+                const double n = (double)W.grid_prof[4];
+                std::fprintf(stderr, "idp grid pcg per iteration (CTA 0): spmv %.2f us, round1 %.2f us, update %.2f us, round2 %.2f us (%llu iterations)\n",
+                             W.grid_prof[0] / n / 1e3, W.grid_prof[1] / n / 1e3, W.grid_prof[2] / n / 1e3, W.grid_prof[3] / n / 1e3,
+                             W.grid_prof[4]);
+                for (auto& v : W.grid_prof) v = 0;
+            }
         }
         W.stats.pcg_ms = ms[PhaseTimer::PCG];
         W.stats.tet_ms = ms[PhaseTimer::TET];

@@ -185,7 +185,7 @@ struct Work {
     std::vector<double> pcg_bytes_per_iter;  // per instance
     double* tol_inst = nullptr;              // per-instance PCG tolerance (device)
     long grid_min_v = 16384;                 // grid-wide PCG above this many vertices
-    long grid_vper = 128;                    // vertices per CTA in the grid-wide PCG
+    long grid_vper = 112;                    // vertices per CTA in the grid-wide PCG
     long long accd_maxit = 0;                // diagnostics (IDP_PROFILE)
     long long accd_long = 0, accd_total = 0, accd_pairs = 0;
     // contact-cluster preconditioner (rebuilt with every Hessian)
@@ -202,10 +202,22 @@ struct Work {
         int* ok = nullptr;         // n: factorisation succeeded
         int max_n = 0;
     } cl;
+    long cand_cap_pt = 0, cand_cap_ee = 0;   // candidate list capacities (grown on overflow)
+    long ccd_cap_pt = 0, ccd_cap_ee = 0;
+    unsigned long long grid_prof[5] = {0, 0, 0, 0, 0};  // grid PCG phase ns (IDP_PROFILE)
+    bool grid_prof_init = false;
+    uint32_t* hpin = nullptr;                // 64 words of pinned host memory for batched readbacks
+    uint32_t* pinned() {
+        if (!hpin && cudaMallocHost(reinterpret_cast<void**>(&hpin), 64 * sizeof(uint32_t)) != cudaSuccess)
+            hpin = nullptr;
+        return hpin;
+    }
     DBuf& operator[](int i) { return b[i]; }
     void release() {
         for (auto& x : b) x.release();
         timer.release();
+        if (hpin) cudaFreeHost(hpin);
+        hpin = nullptr;
     }
 };
 

@@ -1,7 +1,7 @@
 // Uniform-grid broad phase shared by the constraint-set builder and the CCD:
 // every primitive is binned into the cells its integer box covers, the
-// (instance, cell) keys are radix-sorted, and queries walk the cells of their
-// own box with a cursor, binary-searching each cell in the sorted table.
+// (instance, cell) keys are radix-sorted, and each query (one warp) walks the
+// cells of its own box, binary-searching each cell in the sorted table.
 // Candidate pairs are compacted warp-cooperatively (ballot + popc) into a
 // global list.
 #pragma once
@@ -46,54 +46,6 @@ __device__ __forceinline__ int lower_bound_u64(const uint64_t* __restrict__ a, i
         else hi = mid;
     }
     return lo;
-}
-
-// cursor over the cells of one query box
-struct Cursor {
-    int lo[3], hi[3], c[3], fc[3];
-    uint32_t e, eend;
-    bool done;
-};
-
-__device__ __forceinline__ void cursor_init(Cursor& q, const BoxI& b) {
-    for (int d = 0; d < 3; ++d) { q.lo[d] = b.lo[d]; q.hi[d] = b.hi[d]; q.c[d] = b.lo[d]; q.fc[d] = 0; }
-    q.e = q.eend = 0;
-    q.done = (b.lo[0] > b.hi[0]) || (b.lo[1] > b.hi[1]) || (b.lo[2] > b.hi[2]);
-}
-
-// next entry index of the sorted entry list, or false when exhausted
-__device__ __forceinline__ bool cursor_next(Cursor& q, int inst, const GridP& g, const uint64_t* __restrict__ ckey,
-                                            const uint32_t* __restrict__ cstart, int ncell, uint32_t& entry) {
-    while (q.e >= q.eend) {
-        if (q.done) return false;
-        uint64_t key = cell_key(inst, g, q.c[0], q.c[1], q.c[2]);
-        int k = lower_bound_u64(ckey, ncell, key);
-        if (k < ncell && ckey[k] == key) {
-            q.e = cstart[k];
-            q.eend = cstart[k + 1];
-            q.fc[0] = q.c[0]; q.fc[1] = q.c[1]; q.fc[2] = q.c[2];
-        }
-        if (++q.c[0] > q.hi[0]) {
-            q.c[0] = q.lo[0];
-            if (++q.c[1] > q.hi[1]) {
-                q.c[1] = q.lo[1];
-                if (++q.c[2] > q.hi[2]) q.done = true;
-            }
-        }
-    }
-    entry = q.e++;
-    return true;
-}
-
-// the pair (query box, primitive box) is reported once: in the lowest corner
-// cell of the two boxes' intersection
-__device__ __forceinline__ bool first_shared_cell(const Cursor& q, const BoxI& b) {
-    for (int d = 0; d < 3; ++d) {
-        if (b.lo[d] > q.hi[d] || b.hi[d] < q.lo[d]) return false;
-        int c = q.lo[d] > b.lo[d] ? q.lo[d] : b.lo[d];
-        if (c != q.fc[d]) return false;
-    }
-    return true;
 }
 
 // warp-per-query walk: the whole warp visits the cells of box qb in order;
@@ -160,18 +112,23 @@ __device__ __forceinline__ void warp_walk_emit(const BoxI& qb, int inst, const G
 
 // ---- host-side builder (contact.cu): sorted (instance, cell) entry table
 struct BoxGrid {
-    uint64_t* cell_keys = nullptr;   // ncell sorted unique keys
-    uint32_t* cell_start = nullptr;  // ncell + 1
-    uint32_t* entries = nullptr;     // primitive ids, grouped by cell
-    int ncell = 0;
+    uint64_t* cell_keys = nullptr;       // sorted unique keys
+    uint32_t* cell_start = nullptr;      // cells + 1
+    uint32_t* entries = nullptr;         // primitive ids, grouped by cell
+    const uint32_t* d_ncell = nullptr;   // device: number of cells
     long nent = 0;
 };
 
 struct Work;
 // Bins nprim boxes (box[i], instance inst[i]; skipped when active[inst]==0)
-// into their cells. Buffers come from W; which selects one of two slots so a
-// point grid and an edge grid can coexist.
-int build_box_grid(Work& W, int slot, const BoxI* boxes, const int* inst, const unsigned char* active, long nprim,
-                   const GridP* gp, int nI, BoxGrid& out, cudaStream_t s);
+// into their cells, in two steps so several grids share one host round trip:
+// box_grid_count writes the number of (box, cell) entries to *h_total (pinned
+// host memory, valid after the stream is synchronised); box_grid_finish then
+// emits, sorts and tabulates them. slot selects one of two buffer sets so a
+// triangle grid and an edge grid can coexist.
+int box_grid_count(Work& W, int slot, const BoxI* boxes, const int* inst, const unsigned char* active, long nprim,
+                   uint32_t* h_total, cudaStream_t s);
+int box_grid_finish(Work& W, int slot, const BoxI* boxes, const int* inst, const unsigned char* active, long nprim,
+                    const GridP* gp, int nI, long ne, BoxGrid& out, cudaStream_t s);
 
 }  // namespace idp

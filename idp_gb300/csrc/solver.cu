@@ -433,6 +433,58 @@ __device__ __forceinline__ void precond(long v, const T* __restrict__ dinv, cons
 // Accumulation precision follows the vectors (FP32 in mixed mode).
 constexpr int CL_THREADS = 512;
 
+// y = A x over block rows [v0, v1) of one CTA: 8 lanes per row, 4 rows per
+// warp in flight (lane j of a row takes blocks k0+j, k0+j+8, ...), a 3-step
+// butterfly per component, then emit(v, y) on the row's first lane. The
+// vector x may have been written by other CTAs of the same launch, so it is
+// read through L2 (ld.cg). All lanes of every warp must call this together.
+template <class T, class Emit>
+__device__ __forceinline__ void spmv_rows8(int v0, int v1, const int* __restrict__ rowptr,
+                                           const int* __restrict__ colidx, const T* __restrict__ val,
+                                           const int* __restrict__ trp, const int* __restrict__ tcol,
+                                           const T* __restrict__ tval, const unsigned char* __restrict__ dbc,
+                                           const T* x, Emit&& emit) {
+    const int lane = threadIdx.x & 31, l8 = lane & 7;
+    const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int base = v0 + 4 * warp; base < v1; base += 4 * nw) {
+        const int v = base + (lane >> 3);
+        const bool act = v < v1;
+        const bool fixed = act && dbc[v];
+        T a0 = 0, a1 = 0, a2 = 0;
+        if (act && !fixed) {
+            const int k1 = rowptr[v + 1];
+            for (int k = rowptr[v] + l8; k < k1; k += 8) {
+                const int c = colidx[k];
+                const T* m = val + 9L * k;
+                const T x0 = __ldcg(x + 3 * c), x1 = __ldcg(x + 3 * c + 1), x2 = __ldcg(x + 3 * c + 2);
+                a0 += m[0] * x0 + m[1] * x1 + m[2] * x2;
+                a1 += m[3] * x0 + m[4] * x1 + m[5] * x2;
+                a2 += m[6] * x0 + m[7] * x1 + m[8] * x2;
+            }
+            const int t1 = trp[v + 1];
+            for (int k = trp[v] + l8; k < t1; k += 8) {
+                const int c = tcol[k];
+                if (dbc[c]) continue;
+                const T* m = tval + 9L * k;
+                const T x0 = __ldcg(x + 3 * c), x1 = __ldcg(x + 3 * c + 1), x2 = __ldcg(x + 3 * c + 2);
+                a0 += m[0] * x0 + m[1] * x1 + m[2] * x2;
+                a1 += m[3] * x0 + m[4] * x1 + m[5] * x2;
+                a2 += m[6] * x0 + m[7] * x1 + m[8] * x2;
+            }
+        }
+        for (int o = 4; o > 0; o >>= 1) {
+            a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+            a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+            a2 += __shfl_xor_sync(0xffffffffu, a2, o);
+        }
+        if (act && l8 == 0) {
+            T y[3] = {a0, a1, a2};
+            if (fixed) { y[0] = __ldcg(x + 3 * v); y[1] = __ldcg(x + 3 * v + 1); y[2] = __ldcg(x + 3 * v + 2); }
+            emit(v, y);
+        }
+    }
+}
+
 template <class T>
 __device__ __forceinline__ T cta_reduce2(T a, T b, T* wsh, T& out_b) {
     for (int o = 16; o > 0; o >>= 1) {
@@ -501,16 +553,34 @@ __device__ void apply_blocks(const ClusterPC<T>& pc, int inst, int crank, int cs
         for (int a = threadIdx.x; a < N; a += blockDim.x) rc[a] = __ldcg(r + 3 * pc.vert[o + a / 3] + a % 3);
         __syncthreads();
         const T* Ki = pc.Kinv + pc.doff[c];
-        for (int a = warp; a < N; a += nw) {
-            const T* row = Ki + (long)a * N;
-            T acc = 0;
-            for (int bb = lane; bb < N; bb += 32) acc += row[bb] * rc[bb];
-            for (int ofs = 16; ofs > 0; ofs >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, ofs);
+        // two rows per warp, every load of both rows issued before the sums
+        constexpr int kPer = (3 * kClusterCap + 31) / 32;
+        for (int a = 2 * warp; a < N; a += 2 * nw) {
+            const T* r0 = Ki + (long)a * N;
+            const T* r1 = r0 + N;
+            const bool two = a + 1 < N;
+            T acc0 = 0, acc1 = 0;
+#pragma unroll
+            for (int j = 0; j < kPer; ++j) {
+                const int bb = lane + 32 * j;
+                if (bb < N) {
+                    const T rv = rc[bb];
+                    acc0 += __ldg(r0 + bb) * rv;
+                    if (two) acc1 += __ldg(r1 + bb) * rv;
+                }
+            }
+            for (int ofs = 16; ofs > 0; ofs >>= 1) {
+                acc0 += __shfl_down_sync(0xffffffffu, acc0, ofs);
+                acc1 += __shfl_down_sync(0xffffffffu, acc1, ofs);
+            }
             if (lane == 0) {
-                int v = pc.vert[o + a / 3];
-                T zz = dbc[v] ? T(0) : acc;
-                z[3 * v + a % 3] = zz;
-                if (p_init) p_init[3 * v + a % 3] = zz;
+                for (int e = 0; e < (two ? 2 : 1); ++e) {
+                    const int ae = a + e;
+                    const int v = pc.vert[o + ae / 3];
+                    const T zz = dbc[v] ? T(0) : (e ? acc1 : acc0);
+                    z[3 * v + ae % 3] = zz;
+                    if (p_init) p_init[3 * v + ae % 3] = zz;
+                }
             }
         }
         __syncthreads();
@@ -573,20 +643,18 @@ __global__ void __launch_bounds__(CL_THREADS) k_pcg_cluster(
         for (it = 0; it < max_iters;) {
             cl.sync();  // every CTA's p is written before any CTA reads neighbours
             T pAp_l = 0;
-            for (int v = v0 + threadIdx.x; v < v1; v += blockDim.x) {
-                T y[3];
-                spmv_row<T, T, T>(v, rowptr, colidx, val, trp, tcol, tval, dbc, p, y);
+            spmv_rows8<T>(v0, v1, rowptr, colidx, val, trp, tcol, tval, dbc, p, [&](int v, const T* y) {
                 for (int d = 0; d < 3; ++d) {
                     Ap[3 * v + d] = y[d];
-                    pAp_l += p[3 * v + d] * y[d];
+                    pAp_l += __ldcg(p + 3 * v + d) * y[d];
                 }
-            }
+            });
             T dummy, pAp = cta_reduce2(pAp_l, T(0), wsh, dummy);
             cluster_sum2(cl, pAp, T(0), slot, which, pAp, dummy);
             which ^= 1;
             if (!(pAp > T(0))) break;
             const T alpha = rz / pAp;
-            T rrn_l = 0;
+            T rrn_l = 0, rzn_l = 0;
             for (int v = v0 + threadIdx.x; v < v1; v += blockDim.x) {
                 T rv[3], zv[3];
                 for (int d = 0; d < 3; ++d) {
@@ -597,17 +665,19 @@ __global__ void __launch_bounds__(CL_THREADS) k_pcg_cluster(
                 }
                 if (pc.vcl[v] < 0) {
                     precond(v, dinv, dbc, rv, zv);
-                    for (int d = 0; d < 3; ++d) z[3 * v + d] = zv[d];
+                    for (int d = 0; d < 3; ++d) {
+                        z[3 * v + d] = zv[d];
+                        if (!has_blocks) rzn_l += rv[d] * zv[d];
+                    }
                 }
             }
             if (has_blocks) {
                 cl.sync();
                 apply_blocks(pc, inst, crank, csize, dinv, dbc, r, z, (T*)nullptr, rc);
                 cl.sync();
+                for (int v = v0 + threadIdx.x; v < v1; v += blockDim.x)
+                    for (int d = 0; d < 3; ++d) rzn_l += r[3 * v + d] * __ldcg(z + 3 * v + d);
             }
-            T rzn_l = 0;
-            for (int v = v0 + threadIdx.x; v < v1; v += blockDim.x)
-                for (int d = 0; d < 3; ++d) rzn_l += r[3 * v + d] * z[3 * v + d];
             T rrn_c, rzn = cta_reduce2(rzn_l, rrn_l, wsh, rrn_c);
             T rrn;
             cluster_sum2(cl, rzn, rrn_c, slot, which, rzn, rrn);
@@ -627,132 +697,177 @@ __global__ void __launch_bounds__(CL_THREADS) k_pcg_cluster(
 // ---- grid-wide PCG for large instances: one cooperative launch holds every
 // CTA of the wave resident; instance i owns CTAs [c0, c0+nc) (nc depends only
 // on the instance's size, so results do not depend on what else is solved)
-// and synchronises them with its own counter barrier. Dot products: fixed
-// in-CTA tree, then the instance's CTA partials summed in CTA order by every
-// CTA (bit-identical scalars everywhere). Two barriers per iteration: the
-// direction update is folded into the SpMV pass (w = A z, p = z + beta p,
+// and synchronises them through its own control block. Dot products: fixed
+// in-CTA tree, then the last CTA to arrive sums the instance's CTA partials
+// in CTA order and publishes the result (bit-identical scalars everywhere,
+// whichever CTA arrives last). Two such rounds per iteration: the direction
+// update is folded into the SpMV pass (w = A z, p = z + beta p,
 // q = w + beta q with q = A p kept by recurrence). Vectors written inside
 // the kernel are read through L2 (ld.cg) so no CTA sees a stale L1 line.
 constexpr int GP_THREADS = 256;
 constexpr unsigned int kSpinLimit = 1u << 22;  // ~1 s of polling, then error
+constexpr int kCtlWords = 64;                   // per instance: counter at [0], release word at [32]
+constexpr int kGridSmem = 72 * 1024;            // dynamic shared memory per CTA (three CTAs per SM)
 
 struct GridCta {
     int inst, v0, v1, c0, nc, slot;
 };
 
-// y = A x for block row v, one warp: lanes stride over the row's 9*nb
-// contiguous BSR values (coalesced), then a butterfly per component (every
-// lane ends with the same sums)
-template <class T>
-__device__ __forceinline__ void spmv_row_warp(int v, const int* __restrict__ rowptr, const int* __restrict__ colidx,
-                                              const T* __restrict__ val, const int* __restrict__ trp,
-                                              const int* __restrict__ tcol, const T* __restrict__ tval,
-                                              const unsigned char* __restrict__ dbc, const T* x, T y[3]) {
-    const int lane = threadIdx.x & 31;
-    if (dbc[v]) {
-        y[0] = __ldcg(x + 3 * v); y[1] = __ldcg(x + 3 * v + 1); y[2] = __ldcg(x + 3 * v + 2);
-        return;
-    }
-    T a0 = 0, a1 = 0, a2 = 0;
-    const int k0 = rowptr[v], n9 = 9 * (rowptr[v + 1] - k0);
-    for (int e = lane; e < n9; e += 32) {
-        const int kk = e / 9, q = e - 9 * kk;
-        const int c = colidx[k0 + kk];
-        const T pr = val[9L * k0 + e] * __ldcg(x + 3 * c + (q % 3));
-        const int rr = q / 3;
-        a0 += rr == 0 ? pr : T(0);
-        a1 += rr == 1 ? pr : T(0);
-        a2 += rr == 2 ? pr : T(0);
-    }
-    const int t0 = trp[v], t9 = 9 * (trp[v + 1] - t0);
-    for (int e = lane; e < t9; e += 32) {
-        const int kk = e / 9, q = e - 9 * kk;
-        const int c = tcol[t0 + kk];
-        if (dbc[c]) continue;
-        const T pr = tval[9L * t0 + e] * __ldcg(x + 3 * c + (q % 3));
-        const int rr = q / 3;
-        a0 += rr == 0 ? pr : T(0);
-        a1 += rr == 1 ? pr : T(0);
-        a2 += rr == 2 ? pr : T(0);
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-        a0 += __shfl_xor_sync(0xffffffffu, a0, o);
-        a1 += __shfl_xor_sync(0xffffffffu, a1, o);
-        a2 += __shfl_xor_sync(0xffffffffu, a2, o);
-    }
-    y[0] = a0; y[1] = a1; y[2] = a2;
+__device__ __forceinline__ unsigned long long gtimer() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
 }
 
-// counter barrier over the nc CTAs of one instance; the k-th barrier of the
-// launch completes when the counter reaches k*nc. Bounded: after
-// kSpinLimit polls the CTA records an error and reports failure.
-__device__ __forceinline__ bool inst_barrier(unsigned int* ctr, unsigned int target, int* err, int* ok_sh) {
-    __syncthreads();
+// Round k (1, 2, ...) over the nc CTAs of one instance. Every CTA adds its
+// partials (a, b; thread 0's values) and arrives on the counter; the CTA
+// whose arrival completes the round (counter = k*nc) sums the partials when
+// `reduce` is set, stores the sums in red and releases the others, who spin
+// (bounded: after kSpinLimit polls the error flag is set and false returned)
+// on the release word. The counter and the release word sit on separate
+// 128-byte lines so the arrivals do not queue behind the polling.
+template <class T>
+__device__ __forceinline__ bool inst_round(unsigned int* ctl, T* red, T* part, int c0, int nc, unsigned int k,
+                                           bool reduce, T a, T b, T& ra, T& rb, int* err, int* sh_i, T* sh_t) {
     if (threadIdx.x == 0) {
-        int ok = 1;
+        if (reduce) {
+            part[2 * blockIdx.x] = a;
+            part[2 * blockIdx.x + 1] = b;
+        }
         __threadfence();
-        atomicAdd(ctr, 1u);
+        const unsigned int old = atomicAdd(ctl, 1u);
+        sh_i[0] = old == k * (unsigned int)nc - 1u;
+        sh_i[1] = 1;
+    }
+    __syncthreads();
+    if (sh_i[0]) {
+        if (reduce && threadIdx.x < 32) {
+            __threadfence();
+            T sa = 0, sb = 0;
+            for (int j = threadIdx.x; j < nc; j += 32) {
+                sa += __ldcg(part + 2 * (c0 + j));
+                sb += __ldcg(part + 2 * (c0 + j) + 1);
+            }
+            for (int o = 16; o > 0; o >>= 1) {
+                sa += __shfl_xor_sync(0xffffffffu, sa, o);
+                sb += __shfl_xor_sync(0xffffffffu, sb, o);
+            }
+            if (threadIdx.x == 0) {
+                red[0] = sa;
+                red[1] = sb;
+            }
+        }
+        if (threadIdx.x == 0) {
+            __threadfence();
+            atomicExch(ctl + 32, k);
+        }
+    } else if (threadIdx.x == 0) {
         unsigned int n = 0;
-        while (*(volatile unsigned int*)ctr < target) {
+        while (*(volatile unsigned int*)(ctl + 32) < k) {
             if (++n > kSpinLimit) {
                 atomicExch(err, 1);
-                ok = 0;
+                sh_i[1] = 0;
                 break;
             }
-            __nanosleep(64);
+            if (n > 256) __nanosleep(32);  // tight polling first, then back off
         }
         __threadfence();
-        *ok_sh = ok;
     }
     __syncthreads();
-    return *ok_sh != 0;
+    const bool ok = sh_i[1] != 0;
+    if (reduce) {
+        if (threadIdx.x == 0) {
+            sh_t[0] = __ldcg(red);
+            sh_t[1] = __ldcg(red + 1);
+        }
+        __syncthreads();
+        ra = sh_t[0];
+        rb = sh_t[1];
+    }
+    __syncthreads();  // sh_i / sh_t are reused by the next round
+    return ok;
 }
 
-// sum of the instance's CTA partials (two values each) in CTA order
+// Rows of a grid-PCG CTA held in dynamic shared memory for the whole solve:
+//   int srow[nv + 1]        row offsets relative to the CTA's first block
+//   T   sdinv[9 nv]         3x3 block-Jacobi inverses
+//   T   sval[9 ncache]      BSR values of a prefix of the CTA's blocks
+//   int scol[ncache]        their block columns
+// (ncache = every block when they fit, else the prefix that does; rows past
+// it read the matrix from global memory). Only the vector gathers of the
+// SpMV then leave the SM.
 template <class T>
-__device__ __forceinline__ void inst_sum2(const T* part, int c0, int nc, T* sh, T& s0, T& s1) {
-    if (threadIdx.x < 32) {
-        T a = 0, b = 0;
-        for (int j = threadIdx.x; j < nc; j += 32) {
-            a += __ldcg(part + 2 * (c0 + j));
-            b += __ldcg(part + 2 * (c0 + j) + 1);
-        }
-        for (int o = 16; o > 0; o >>= 1) {
-            a += __shfl_xor_sync(0xffffffffu, a, o);
-            b += __shfl_xor_sync(0xffffffffu, b, o);
-        }
-        if (threadIdx.x == 0) { sh[0] = a; sh[1] = b; }
-    }
-    __syncthreads();
-    s0 = sh[0];
-    s1 = sh[1];
+struct GridRows {
+    int* row;
+    T* dinv;
+    T* val;
+    int* col;
+    int ncache;
+};
+
+__host__ __device__ inline size_t grid_smem_fixed(int nvmax, size_t tsize) {
+    size_t a = ((size_t)(nvmax + 1) * 4 + 15) & ~size_t(15);
+    return a + tsize * 9 * (size_t)nvmax;
+}
+
+template <class T>
+__device__ __forceinline__ void grid_precond(const T* D, bool fixed, const T rv[3], T zv[3]) {
+    if (fixed) { zv[0] = zv[1] = zv[2] = T(0); return; }
+    zv[0] = D[0] * rv[0] + D[1] * rv[1] + D[2] * rv[2];
+    zv[1] = D[3] * rv[0] + D[4] * rv[1] + D[5] * rv[2];
+    zv[2] = D[6] * rv[0] + D[7] * rv[1] + D[8] * rv[2];
 }
 
 template <class T>
 __global__ void __launch_bounds__(GP_THREADS) k_pcg_grid(
-    const GridCta* __restrict__ plan, int G, const int* __restrict__ rowptr, const int* __restrict__ colidx,
-    const T* __restrict__ val, const int* __restrict__ trp, const int* __restrict__ tcol, const T* __restrict__ tval,
-    const unsigned char* __restrict__ dbc, const T* __restrict__ dinv, ClusterPC<T> pc, const double* __restrict__ b,
-    T* x, T* r, T* z, T* p, T* q, T* part, unsigned int* bar, int* err, const double* __restrict__ tol_inst,
-    double rel_tol, int max_iters, int* __restrict__ iters_out) {
+    const GridCta* __restrict__ plan, int cap_blocks, int nvmax, const int* __restrict__ rowptr,
+    const int* __restrict__ colidx, const T* __restrict__ val, const int* __restrict__ trp,
+    const int* __restrict__ tcol, const T* __restrict__ tval, const unsigned char* __restrict__ dbc,
+    const T* __restrict__ dinv, ClusterPC<T> pc, const double* __restrict__ b, T* x, T* r, T* z, T* p, T* q,
+    T* part, T* redbuf, unsigned int* ctlbuf, int* err, const double* __restrict__ tol_inst, double rel_tol,
+    int max_iters, int* __restrict__ iters_out, unsigned long long* prof) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ T wsh[2 * (GP_THREADS / 32)];
-    __shared__ T ssum[2];
-    __shared__ int ok_sh;
+    __shared__ T sh_t[2];
+    __shared__ int sh_i[2];
     __shared__ T rc[3 * kClusterCap];
     const GridCta me = plan[blockIdx.x];
     const int inst = me.inst, v0 = me.v0, v1 = me.v1, c0 = me.c0, nc = me.nc, rank = blockIdx.x - me.c0;
-    unsigned int* ctr = bar + me.slot;
-    unsigned int nbar = 0;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = GP_THREADS / 32;
+    const int nv = v1 - v0;
+    unsigned int* ctl = ctlbuf + (long)kCtlWords * me.slot;
+    T* red = redbuf + 2L * me.slot;
+    unsigned int round = 0;
     const bool has_blocks = pc.ioff[inst + 1] > pc.ioff[inst];
-    auto sync_all = [&]() { return inst_barrier(ctr, (++nbar) * (unsigned int)nc, err, &ok_sh); };
-    auto slot = [&]() { return part + 2L * G * (nbar & 1u); };  // partials of the next barrier
+    const int lane = threadIdx.x & 31, l8 = lane & 7, warp = threadIdx.x >> 5, nw = GP_THREADS / 32;
+    // ---- stage the CTA's rows in shared memory
+    GridRows<T> S;
+    S.row = reinterpret_cast<int*>(smem_raw);
+    S.dinv = reinterpret_cast<T*>(smem_raw + (((size_t)(nvmax + 1) * 4 + 15) & ~size_t(15)));
+    S.val = reinterpret_cast<T*>(smem_raw + grid_smem_fixed(nvmax, sizeof(T)));
+    S.col = reinterpret_cast<int*>(S.val + 9L * cap_blocks);
+    const int kb0 = rowptr[v0];
+    const int nbk = rowptr[v1] - kb0;
+    S.ncache = min(nbk, cap_blocks);
+    for (int i = threadIdx.x; i <= nv; i += GP_THREADS) S.row[i] = rowptr[v0 + i] - kb0;
+    for (int i = threadIdx.x; i < 9 * nv; i += GP_THREADS) S.dinv[i] = dinv[9L * v0 + i];
+    for (int i = threadIdx.x; i < S.ncache; i += GP_THREADS) S.col[i] = colidx[kb0 + i];
+    for (int i = threadIdx.x; i < 9 * S.ncache; i += GP_THREADS) S.val[i] = val[9L * kb0 + i];
+    __syncthreads();
+    T dummy0, dummy1;
+    auto barrier = [&]() {
+        return inst_round<T>(ctl, red, part, c0, nc, ++round, false, T(0), T(0), dummy0, dummy1, err, sh_i, sh_t);
+    };
+    auto allreduce = [&](T a, T bb, T& ra, T& rb) {
+        return inst_round<T>(ctl, red, part, c0, nc, ++round, true, a, bb, ra, rb, err, sh_i, sh_t);
+    };
     // r = b, x = 0, z = M^{-1} r, p = q = 0
-    T rr_l = 0;
-    for (int v = v0 + threadIdx.x; v < v1; v += GP_THREADS) {
+    T rr_l = 0, rz_l = 0;
+    for (int lv = threadIdx.x; lv < nv; lv += GP_THREADS) {
+        const int v = v0 + lv;
+        const bool fixed = dbc[v];
         T rv[3], zv[3];
         for (int d = 0; d < 3; ++d) {
-            rv[d] = dbc[v] ? T(0) : (T)b[3 * v + d];
+            rv[d] = fixed ? T(0) : (T)b[3 * v + d];
             x[3 * v + d] = T(0);
             r[3 * v + d] = rv[d];
             p[3 * v + d] = T(0);
@@ -760,56 +875,106 @@ __global__ void __launch_bounds__(GP_THREADS) k_pcg_grid(
             rr_l += rv[d] * rv[d];
         }
         if (pc.vcl[v] < 0) {
-            precond(v, dinv, dbc, rv, zv);
-            for (int d = 0; d < 3; ++d) z[3 * v + d] = zv[d];
+            grid_precond(S.dinv + 9 * lv, fixed, rv, zv);
+            for (int d = 0; d < 3; ++d) {
+                z[3 * v + d] = zv[d];
+                if (!has_blocks) rz_l += rv[d] * zv[d];
+            }
         }
     }
     if (has_blocks) {
-        if (!sync_all()) return;
+        if (!barrier()) return;
         apply_blocks(pc, inst, rank, nc, dinv, dbc, r, z, (T*)nullptr, rc);
-        if (!sync_all()) return;
+        if (!barrier()) return;
+        for (int lv = threadIdx.x; lv < nv; lv += GP_THREADS)
+            for (int d = 0; d < 3; ++d) rz_l += r[3 * (v0 + lv) + d] * __ldcg(z + 3 * (v0 + lv) + d);
     }
-    T rz_l = 0;
-    for (int v = v0 + threadIdx.x; v < v1; v += GP_THREADS)
-        for (int d = 0; d < 3; ++d) rz_l += r[3 * v + d] * __ldcg(z + 3 * v + d);
     T rr_c, rz_c = cta_reduce2(rz_l, rr_l, wsh, rr_c);
-    T* ps = slot();
-    if (threadIdx.x == 0) { ps[2 * blockIdx.x] = rz_c; ps[2 * blockIdx.x + 1] = rr_c; }
-    if (!sync_all()) return;
     T rz, rr0;
-    inst_sum2(ps, c0, nc, ssum, rz, rr0);
+    if (!allreduce(rz_c, rr_c, rz, rr0)) return;
     const double tl = tol_inst ? fmax(tol_inst[inst], rel_tol) : rel_tol;
     const T tol2 = (T)(tl * tl) * rr0;
     T beta = 0;
     int it = 0;
     if (rr0 > T(0) && rr0 > tol2) {
+        const bool timed = prof && blockIdx.x == 0 && threadIdx.x == 0;
+        unsigned long long t0 = timed ? gtimer() : 0, t1;
         for (it = 0; it < max_iters;) {
-            // w = A z (rows of this CTA, warp per row); p = z + beta p; q = w + beta q
+            // w = A z on this CTA's rows (8 lanes per row, 4 rows per warp);
+            // lane d < 3 of each row then forms p = z + beta p, q = w + beta q
+            // for component d
             T pq_l = 0;
-            for (int v = v0 + warp; v < v1; v += nw) {
-                T w[3];
-                spmv_row_warp<T>(v, rowptr, colidx, val, trp, tcol, tval, dbc, z, w);
-                if (lane < 3) {
-                    const int i3 = 3 * v + lane;
-                    const T wl = lane == 0 ? w[0] : (lane == 1 ? w[1] : w[2]);
-                    const T pn = __ldcg(z + i3) + beta * p[i3];
-                    const T qn = wl + beta * q[i3];
-                    p[i3] = pn;
-                    q[i3] = qn;
+            for (int base = 4 * warp; base < nv; base += 4 * nw) {
+                const int lv = base + (lane >> 3);
+                const bool act = lv < nv;
+                const int v = v0 + (act ? lv : 0);
+                const bool fixed = act && dbc[v];
+                T zo = 0, po = 0, qo = 0;
+                if (act && l8 < 3) {
+                    zo = __ldcg(z + 3 * v + l8);
+                    po = p[3 * v + l8];
+                    qo = q[3 * v + l8];
+                }
+                T a0 = 0, a1 = 0, a2 = 0;
+                if (act && !fixed) {
+                    const int ka = S.row[lv], kz = S.row[lv + 1];
+                    if (kz <= S.ncache) {
+                        for (int k = ka + l8; k < kz; k += 8) {
+                            const int c = S.col[k];
+                            const T* m = S.val + 9 * k;
+                            const T x0 = __ldcg(z + 3 * c), x1 = __ldcg(z + 3 * c + 1), x2 = __ldcg(z + 3 * c + 2);
+                            a0 += m[0] * x0 + m[1] * x1 + m[2] * x2;
+                            a1 += m[3] * x0 + m[4] * x1 + m[5] * x2;
+                            a2 += m[6] * x0 + m[7] * x1 + m[8] * x2;
+                        }
+                    } else {
+                        for (int k = ka + l8; k < kz; k += 8) {
+                            const int c = colidx[kb0 + k];
+                            const T* m = val + 9L * (kb0 + k);
+                            const T x0 = __ldcg(z + 3 * c), x1 = __ldcg(z + 3 * c + 1), x2 = __ldcg(z + 3 * c + 2);
+                            a0 += m[0] * x0 + m[1] * x1 + m[2] * x2;
+                            a1 += m[3] * x0 + m[4] * x1 + m[5] * x2;
+                            a2 += m[6] * x0 + m[7] * x1 + m[8] * x2;
+                        }
+                    }
+                    const int t1e = trp[v + 1];
+                    for (int k = trp[v] + l8; k < t1e; k += 8) {
+                        const int c = tcol[k];
+                        if (dbc[c]) continue;
+                        const T* m = tval + 9L * k;
+                        const T x0 = __ldcg(z + 3 * c), x1 = __ldcg(z + 3 * c + 1), x2 = __ldcg(z + 3 * c + 2);
+                        a0 += m[0] * x0 + m[1] * x1 + m[2] * x2;
+                        a1 += m[3] * x0 + m[4] * x1 + m[5] * x2;
+                        a2 += m[6] * x0 + m[7] * x1 + m[8] * x2;
+                    }
+                }
+                for (int o = 4; o > 0; o >>= 1) {
+                    a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+                    a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+                    a2 += __shfl_xor_sync(0xffffffffu, a2, o);
+                }
+                if (act && l8 < 3) {
+                    // DBC rows: A is the identity there, so w = z
+                    const T w = fixed ? zo : (l8 == 0 ? a0 : (l8 == 1 ? a1 : a2));
+                    const T pn = zo + beta * po;
+                    const T qn = w + beta * qo;
+                    p[3 * v + l8] = pn;
+                    q[3 * v + l8] = qn;
                     pq_l += pn * qn;
                 }
             }
-            T dummy, pq_c = cta_reduce2(pq_l, T(0), wsh, dummy);
-            ps = slot();
-            if (threadIdx.x == 0) { ps[2 * blockIdx.x] = pq_c; ps[2 * blockIdx.x + 1] = T(0); }
-            if (!sync_all()) return;
+            T d0, pq_c = cta_reduce2(pq_l, T(0), wsh, d0);
+            if (timed) { t1 = gtimer(); prof[0] += t1 - t0; t0 = t1; }
             T pq;
-            inst_sum2(ps, c0, nc, ssum, pq, dummy);
+            if (!allreduce(pq_c, T(0), pq, d0)) return;
+            if (timed) { t1 = gtimer(); prof[1] += t1 - t0; t0 = t1; }
             if (!(pq > T(0))) break;
             const T alpha = rz / pq;
-            // x += alpha p; r -= alpha q; z = M^{-1} r
-            T rrn_l = 0;
-            for (int v = v0 + threadIdx.x; v < v1; v += GP_THREADS) {
+            // x += alpha p; r -= alpha q; z = M^{-1} r (r.z in the same pass
+            // unless contact blocks write z of other CTAs' rows)
+            T rrn_l = 0, rzn_l = 0;
+            for (int lv = threadIdx.x; lv < nv; lv += GP_THREADS) {
+                const int v = v0 + lv;
                 T rv[3], zv[3];
                 for (int d = 0; d < 3; ++d) {
                     x[3 * v + d] += alpha * p[3 * v + d];
@@ -818,24 +983,25 @@ __global__ void __launch_bounds__(GP_THREADS) k_pcg_grid(
                     rrn_l += rv[d] * rv[d];
                 }
                 if (pc.vcl[v] < 0) {
-                    precond(v, dinv, dbc, rv, zv);
-                    for (int d = 0; d < 3; ++d) z[3 * v + d] = zv[d];
+                    grid_precond(S.dinv + 9 * lv, dbc[v] != 0, rv, zv);
+                    for (int d = 0; d < 3; ++d) {
+                        z[3 * v + d] = zv[d];
+                        if (!has_blocks) rzn_l += rv[d] * zv[d];
+                    }
                 }
             }
             if (has_blocks) {
-                if (!sync_all()) return;
+                if (!barrier()) return;
                 apply_blocks(pc, inst, rank, nc, dinv, dbc, r, z, (T*)nullptr, rc);
-                if (!sync_all()) return;
+                if (!barrier()) return;
+                for (int lv = threadIdx.x; lv < nv; lv += GP_THREADS)
+                    for (int d = 0; d < 3; ++d) rzn_l += r[3 * (v0 + lv) + d] * __ldcg(z + 3 * (v0 + lv) + d);
             }
-            T rzn_l = 0;
-            for (int v = v0 + threadIdx.x; v < v1; v += GP_THREADS)
-                for (int d = 0; d < 3; ++d) rzn_l += r[3 * v + d] * __ldcg(z + 3 * v + d);
             T rrn_c, rzn_c = cta_reduce2(rzn_l, rrn_l, wsh, rrn_c);
-            ps = slot();
-            if (threadIdx.x == 0) { ps[2 * blockIdx.x] = rzn_c; ps[2 * blockIdx.x + 1] = rrn_c; }
-            if (!sync_all()) return;
+            if (timed) { t1 = gtimer(); prof[2] += t1 - t0; t0 = t1; }
             T rzn, rrn;
-            inst_sum2(ps, c0, nc, ssum, rzn, rrn);
+            if (!allreduce(rzn_c, rrn_c, rzn, rrn)) return;
+            if (timed) { t1 = gtimer(); prof[3] += t1 - t0; t0 = t1; prof[4] += 1; }
             ++it;
             if (rrn <= tol2) break;
             beta = rzn / rz;
@@ -1039,7 +1205,8 @@ static int pcg_inner(Arena& A, Work& W, const double* b, double rel_tol, int max
         int dev = 0, nsm = 0, per = 0;
         IDP_CUDA_TRY(cudaGetDevice(&dev));
         IDP_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-        IDP_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pcg_grid<T>, GP_THREADS, 0));
+        IDP_CUDA_TRY(cudaFuncSetAttribute(k_pcg_grid<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, kGridSmem));
+        IDP_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pcg_grid<T>, GP_THREADS, kGridSmem));
         gmax = nsm * per;
         if (gmax <= 0) return IDP_ERR_CUDA;
     }
@@ -1072,13 +1239,22 @@ static int pcg_inner(Arena& A, Work& W, const double* b, double rel_tol, int max
         ++slot;
     }
     if (!plan.empty()) waves.push_back(plan);
-    size_t need = sizeof(GridCta) * gmax + sizeof(T) * 4 * (size_t)gmax + sizeof(unsigned int) * (nI + 1) + 256;
-    if (W[W_PCG_GRID].ensure(need)) return IDP_ERR_CUDA;
+    // W_PCG_GRID: plan | partials (2 per CTA) | sums (2 per instance) | control words | error flag
+    const size_t o_part = sizeof(GridCta) * gmax;
+    const size_t o_red = o_part + sizeof(T) * 2 * (size_t)gmax;
+    const size_t o_ctl = (o_red + sizeof(T) * 2 * (size_t)(nI + 1) + 255) & ~size_t(255);
+    const size_t o_err = o_ctl + sizeof(unsigned int) * kCtlWords * (size_t)(nI + 1);
+    if (W[W_PCG_GRID].ensure(o_err + 256)) return IDP_ERR_CUDA;
+    // phase timers of CTA 0 (spmv, round 1, update, round 2, iterations) when profiling
+    static const bool profiling = std::getenv("IDP_PROFILE") != nullptr;
+    unsigned long long* d_prof = profiling ? reinterpret_cast<unsigned long long*>(W[W_PCG_GRID].as<char>() + o_err + 64)
+                                           : nullptr;
     char* gb = W[W_PCG_GRID].as<char>();
     GridCta* d_plan = reinterpret_cast<GridCta*>(gb);
-    T* d_part = reinterpret_cast<T*>(gb + sizeof(GridCta) * gmax);
-    unsigned int* d_bar = reinterpret_cast<unsigned int*>(gb + sizeof(GridCta) * gmax + sizeof(T) * 4 * (size_t)gmax);
-    int* d_err = reinterpret_cast<int*>(d_bar + nI + 1);
+    T* d_part = reinterpret_cast<T*>(gb + o_part);
+    T* d_red = reinterpret_cast<T*>(gb + o_red);
+    unsigned int* d_ctl = reinterpret_cast<unsigned int*>(gb + o_ctl);
+    int* d_err = reinterpret_cast<int*>(gb + o_err);
     ClusterPC<T> pcb;
     pcb.vcl = W.cl.vcl;
     pcb.ioff = W.cl.ioff;
@@ -1089,13 +1265,23 @@ static int pcg_inner(Arena& A, Work& W, const double* b, double rel_tol, int max
     pcb.Kinv = W.cl.n > 0 ? W[W_CL_DENSE].as<T>() : nullptr;
     W.timer.start(PhaseTimer::PCG, s);
     IDP_CUDA_TRY(cudaMemsetAsync(d_err, 0, sizeof(int), s));
+    if (d_prof && !W.grid_prof_init) {
+        IDP_CUDA_TRY(cudaMemsetAsync(d_prof, 0, 5 * sizeof(unsigned long long), s));
+        W.grid_prof_init = true;
+    }
     for (auto& wv : waves) {
         const int G = (int)wv.size();
+        int nvmax = 1;
+        for (const GridCta& g : wv) nvmax = std::max(nvmax, g.v1 - g.v0);
+        const long fixed = (long)grid_smem_fixed(nvmax, sizeof(T));
+        const int cap_blocks = (int)((kGridSmem - fixed) / (long)(9 * sizeof(T) + 4));
+        if (cap_blocks < 0) return IDP_ERR_CAPACITY;  // rows per CTA beyond the shared-memory image
         IDP_CUDA_TRY(cudaMemcpyAsync(d_plan, wv.data(), sizeof(GridCta) * G, cudaMemcpyHostToDevice, s));
-        IDP_CUDA_TRY(cudaMemsetAsync(d_bar, 0, sizeof(unsigned int) * (nI + 1), s));
+        IDP_CUDA_TRY(cudaMemsetAsync(d_ctl, 0, sizeof(unsigned int) * kCtlWords * (nI + 1), s));
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(G);
         cfg.blockDim = dim3(GP_THREADS);
+        cfg.dynamicSmemBytes = kGridSmem;
         cfg.stream = s;
         cudaLaunchAttribute at[1];
         at[0].id = cudaLaunchAttributeCooperative;
@@ -1103,10 +1289,11 @@ static int pcg_inner(Arena& A, Work& W, const double* b, double rel_tol, int max
         cfg.attrs = at;
         cfg.numAttrs = 1;
         ::idp::count_launch();
-        IDP_CUDA_TRY(cudaLaunchKernelEx(&cfg, k_pcg_grid<T>, (const GridCta*)d_plan, G, (const int*)A.rowptr,
+        IDP_CUDA_TRY(cudaLaunchKernelEx(&cfg, k_pcg_grid<T>, (const GridCta*)d_plan, cap_blocks, nvmax,
+                                        (const int*)A.rowptr,
                                         (const int*)A.colidx, val, trp, tcol, tval, (const unsigned char*)A.dbc, dinv,
-                                        pcb, b, x, r, z, p, Ap, d_part, d_bar, d_err, (const double*)W.tol_inst,
-                                        rel_tol, max_iters, d_iters));
+                                        pcb, b, x, r, z, p, Ap, d_part, d_red, d_ctl, d_err,
+                                        (const double*)W.tol_inst, rel_tol, max_iters, d_iters, d_prof));
         W.stats.pcg_launches += 1;
     }
     W.timer.stop(s);
@@ -1116,6 +1303,12 @@ static int pcg_inner(Arena& A, Work& W, const double* b, double rel_tol, int max
     IDP_CUDA_TRY(cudaMemcpyAsync(hit.data(), d_iters, sizeof(int) * nI, cudaMemcpyDeviceToHost, s));
     IDP_CUDA_TRY(cudaStreamSynchronize(s));
     if (herr) return IDP_ERR_CUDA;  // a barrier wait ran out (never expected)
+    if (d_prof) {
+        unsigned long long hp[5];
+        IDP_CUDA_TRY(cudaMemcpy(hp, d_prof, sizeof(hp), cudaMemcpyDeviceToHost));
+        IDP_CUDA_TRY(cudaMemset(d_prof, 0, sizeof(hp)));
+        for (int k = 0; k < 5; ++k) W.grid_prof[k] += hp[k];
+    }
     for (int i = 0; i < nI; ++i)
         if (large[i]) iters[i] = hit[i];
     account(large);

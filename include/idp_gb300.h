@@ -51,7 +51,7 @@ typedef struct idp_params {
     int pcg_grid_min_vertices; /* instances above this many vertices solve with the
                              grid-wide PCG (all SMs), the others with one thread-block
                              cluster each; 0 = default (16384)                        */
-    int pcg_grid_cta_vertices; /* vertices per CTA in the grid-wide PCG; 0 = default (128) */
+    int pcg_grid_cta_vertices; /* vertices per CTA in the grid-wide PCG; 0 = default (112) */
 } idp_params;
 
 typedef struct idp_result {
