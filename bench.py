@@ -60,6 +60,8 @@ def parse():
     ap.add_argument("--blob-n", type=int, default=64)
     ap.add_argument("--flow-step", type=float, default=0.05)
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--pcg-rel-tol", type=float, default=0.0,
+                    help="PCG relative tolerance of the timed arm (0 = library default); the FP64 arm keeps the default")
     ap.add_argument("--pcg-grid-cta-vertices", type=int, default=0,
                     help="vertices per CTA of the grid-wide PCG (0 = library default)")
     ap.add_argument("--instances", type=int, default=256)
@@ -278,9 +280,12 @@ def run_flow(args):
     desc = blob_desc(p, args.blob_n, args.flow_step)
     V = p["X"].shape[0]
 
-    def make_ctx(m):
+    def make_ctx(m, timed_arm=True):
+        kw = {}
+        if timed_arm and args.pcg_rel_tol > 0:
+            kw["pcg_rel_tol"] = args.pcg_rel_tol
         c = idp.Context(h=H, newton_tol=1e-3, max_newton=args.max_newton, mode=m, device=local,
-                        pcg_grid_cta_vertices=args.pcg_grid_cta_vertices)
+                        pcg_grid_cta_vertices=args.pcg_grid_cta_vertices, **kw)
         c.add_instance(p["X"], p["tets"], p["mass"], p["lam"], p["mu"], p["dHat2"], p["kappa"], p["kappa_max"])
         c.commit()
         return c
@@ -328,7 +333,7 @@ def run_flow(args):
     # ---- FP64 arm from the same start states
     fp64 = None
     if not args.no_fp64 and mode == idp.MODE_MIXED:
-        cd = make_ctx(idp.MODE_FP64)
+        cd = make_ctx(idp.MODE_FP64, timed_arm=False)
         d_ms, rel = [], []
         for k, (Xs, vs, ks) in enumerate(starts):
             cd.set_positions(0, Xs)

@@ -85,20 +85,48 @@ __global__ void k_abs_dir(long nN, const int* __restrict__ nodes, const double* 
 }
 
 // per instance: voxel size, span cap (SPATIAL_HASH.h:455-482)
+// first level of the fixed-order sums, one CTA per 2048-item tile of every
+// instance's edge-length and |dir| segments (tile t of a segment of length m
+// covers items 2048 t ...; same arithmetic as one tile of cta_det_sum)
+__global__ void k_span_tiles(const SpanTile* __restrict__ tiles, const unsigned char* __restrict__ active,
+                             const double* __restrict__ len, const double* __restrict__ absdir,
+                             double* __restrict__ out) {
+    __shared__ double a[256];
+    const SpanTile t = tiles[blockIdx.x];
+    if (!active[t.inst]) return;
+    const double* in = (t.kind ? absdir : len) + t.start;
+    double s = 0.0;
+    for (int r = 0; r < 8; ++r) {
+        long i = (long)t.k * 2048 + r * 256 + threadIdx.x;
+        if (i < t.m) s += in[i];
+    }
+    a[threadIdx.x] = s;
+    __syncthreads();
+    for (int st = 128; st > 0; st >>= 1) {
+        if (threadIdx.x < st) a[threadIdx.x] += a[threadIdx.x + st];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[blockIdx.x] = a[0];
+}
+
+// the rest of the recursion per instance: a segment of one tile is its tile
+// sum; otherwise the tile sums are summed by the same fixed-order scheme
 __global__ void k_span_cap(int nI, const unsigned char* __restrict__ active, const int* __restrict__ se_off,
-                           const int* __restrict__ sn_off, const double* __restrict__ len,
-                           const double* __restrict__ absdir, double* __restrict__ scratch, double* __restrict__ alpha,
+                           const int* __restrict__ sn_off, const int* __restrict__ tile_off,
+                           const double* __restrict__ tsum, double* __restrict__ scratch, double* __restrict__ alpha,
                            double* __restrict__ voxel_size) {
     int i = blockIdx.x;
     if (!active[i]) return;
     long ne = se_off[i + 1] - se_off[i], nn = sn_off[i + 1] - sn_off[i];
-    double* sc = scratch + 2 * ((long)se_off[i] + 3 * (long)sn_off[i]) / 1024 + 8 * (long)i;
+    const int te0 = tile_off[2 * i], tn0 = tile_off[2 * i + 1], tn1 = tile_off[2 * i + 2];
+    const int nte = tn0 - te0, ntn = tn1 - tn0;
+    double* sc = scratch + 2 * (long)tile_off[2 * i] + 8 * (long)i;
     double vsz = 1.0;
     if (ne) {
-        double s = cta_det_sum(len + se_off[i], ne, sc);
+        double s = nte == 1 ? tsum[te0] : cta_det_sum(tsum + te0, nte, sc);
         vsz *= s / (double)ne;
     }
-    double ps = cta_det_sum(absdir + 3 * (long)sn_off[i], 3 * nn, sc);
+    double ps = ntn == 0 ? 0.0 : (ntn == 1 ? tsum[tn0] : cta_det_sum(tsum + tn0, ntn, sc));
     if (threadIdx.x == 0) {
         double pSize = ps / (double)(nn * 3);
         double a = alpha[i];
@@ -114,18 +142,21 @@ __global__ void k_ccd_bbox(long nN, const int* __restrict__ nodes, const int* __
                            const double* __restrict__ dir, const double* __restrict__ alpha,
                            unsigned long long* __restrict__ bb) {
     long s = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= nN) return;
-    int inst = ninst[s];
-    if (!active[inst]) return;
-    int v = nodes[s];
-    double a = alpha[inst];
-    double p[3] = {X[3 * v], X[3 * v + 1], X[3 * v + 2]};
-    double q[3] = {X[3 * v] + a * dir[3 * v], X[3 * v + 1] + a * dir[3 * v + 1], X[3 * v + 2] + a * dir[3 * v + 2]};
-    unsigned long long* b = bb + 6 * inst;
-    for (int d = 0; d < 3; ++d) {
-        atomicMin(b + d, ord_enc(fmin(p[d], q[d])));
-        atomicMax(b + 3 + d, ord_enc(fmax(p[d], q[d])));
+    const int inst = s < nN ? ninst[s] : 0;
+    const int inst_first = ninst[(long)blockIdx.x * blockDim.x];
+    const bool valid = s < nN && active[inst];
+    unsigned long long lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+    if (valid) {
+        int v = nodes[s];
+        double a = alpha[inst];
+        double p[3] = {X[3 * v], X[3 * v + 1], X[3 * v + 2]};
+        double q[3] = {X[3 * v] + a * dir[3 * v], X[3 * v + 1] + a * dir[3 * v + 1], X[3 * v + 2] + a * dir[3 * v + 2]};
+        for (int d = 0; d < 3; ++d) {
+            lo[d] = ord_enc(fmin(p[d], q[d]));
+            hi[d] = ord_enc(fmax(p[d], q[d]));
+        }
     }
+    bbox_block_update(valid, inst, inst_first, lo, hi, bb);
 }
 
 __global__ void k_bb_init(int nI, unsigned long long* bb) {
@@ -235,13 +266,37 @@ struct CCand {
 // test (integer voxel boxes overlap) is applied to every pair it returns
 constexpr int CCD_COARSE = 4;
 
-__global__ void k_coarse_boxes(long n, const BoxI* __restrict__ in, BoxI* __restrict__ out) {
+// coarse boxes of the triangles, edges and nodes (stored in that order),
+// clamped to the coarse grid [0, n]: the clamp is monotone, so every pair of
+// overlapping boxes still overlaps, and all query and table cells exist
+__global__ void k_coarse_boxes(long pt, long pe, long pn, long nt, long ne, long nn, const int* __restrict__ tinst,
+                               const int* __restrict__ einst, const int* __restrict__ ninst,
+                               const GridP* __restrict__ gc, const BoxI* __restrict__ in, BoxI* __restrict__ out) {
+    // segments are padded to pt, pe, pn boxes (at least one each); padding
+    // boxes are left empty
     long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    if (i >= pt + pe + pn) return;
+    int inst = -1;
+    if (i < pt) { if (i < nt) inst = tinst[i]; }
+    else if (i < pt + pe) { if (i - pt < ne) inst = einst[i - pt]; }
+    else if (i - pt - pe < nn) inst = ninst[i - pt - pe];
     BoxI b = in[i], c;
+    if (inst < 0) {
+        for (int d = 0; d < 3; ++d) { c.lo[d] = 1; c.hi[d] = 0; }
+        out[i] = c;
+        return;
+    }
+    const GridP g = gc[inst];
     for (int d = 0; d < 3; ++d) {
-        c.lo[d] = b.lo[d] >= 0 ? b.lo[d] / CCD_COARSE : -1;
-        c.hi[d] = b.hi[d] >= 0 ? b.hi[d] / CCD_COARSE : -1;
+        if (b.lo[d] > b.hi[d]) {  // empty box (inactive instance) stays empty
+            c.lo[d] = 1;
+            c.hi[d] = 0;
+            continue;
+        }
+        const int lo = b.lo[d] >= 0 ? b.lo[d] / CCD_COARSE : -1;
+        const int hi = b.hi[d] >= 0 ? b.hi[d] / CCD_COARSE : -1;
+        c.lo[d] = clampi(lo, 0, g.n[d]);
+        c.hi[d] = clampi(hi, 0, g.n[d]);
     }
     out[i] = c;
 }
@@ -269,7 +324,7 @@ __device__ __forceinline__ bool swept_far(const double* lo_a, const double* hi_a
     return false;
 }
 
-// warp per surface node: triangles whose voxel boxes overlap the node's
+// one lane group per surface node: triangles whose voxel boxes overlap the node's
 // swept voxel box (Query_Point_For_Primitives, SPATIAL_HASH.h:624-647), then
 // the exclusions and swept-AABB test of IPC.h:1980-2006
 __global__ void k_ccd_query_pt(long nN, const int* __restrict__ nodes, const int* __restrict__ ninst,
@@ -278,11 +333,10 @@ __global__ void k_ccd_query_pt(long nN, const int* __restrict__ nodes, const int
                                const int* __restrict__ tris, const BoxI* __restrict__ nbox,
                                const BoxI* __restrict__ tbox, const BoxI* __restrict__ nboxc,
                                const BoxI* __restrict__ tboxc, const GridP* __restrict__ gp,
-                               const double* __restrict__ thick, const uint64_t* __restrict__ ckey,
-                               const uint32_t* __restrict__ cstart, const uint32_t* __restrict__ ncell_p, const uint32_t* __restrict__ entries,
+                               const double* __restrict__ thick, CellHash cells,
+                               const uint32_t* __restrict__ cstart, const uint32_t* __restrict__ entries,
                                CCand* __restrict__ out, unsigned int* counter, long cap) {
-    const int ncell = (int)*ncell_p;
-    long s = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    long s = ((long)blockIdx.x * blockDim.x + threadIdx.x) / kCcdQueryLanes;
     if (s >= nN) return;
     int inst = ninst[s];
     if (!active[inst]) return;
@@ -297,7 +351,7 @@ __global__ void k_ccd_query_pt(long nN, const int* __restrict__ nodes, const int
     }
     const BoxI qc = nboxc[s], qx = nbox[s];
     const bool pdbc = dbc[vI] != 0;
-    warp_walk_emit(qc, inst, g, ckey, cstart, ncell, entries, out, counter, cap,
+    group_walk_emit<kCcdQueryLanes>(qc, inst, g, cells, cstart, entries, out, counter, cap,
                    [&](uint32_t ent, int cx, int cy, int cz, CCand& c) -> bool {
                        int f = (int)ent;
                        if (!is_first_shared(qc, tboxc[f], cx, cy, cz) || !boxes_overlap(qx, tbox[f])) return false;
@@ -322,18 +376,17 @@ __global__ void k_ccd_query_pt(long nN, const int* __restrict__ nodes, const int
                    });
 }
 
-// warp per surface edge: edges eJ > eI with overlapping voxel boxes
+// one lane group per surface edge: edges eJ > eI with overlapping voxel boxes
 // (SPATIAL_HASH.h:650-662), exclusions and swept-AABB test of IPC.h:2193-2230
 __global__ void k_ccd_query_ee(long nE, const int2* __restrict__ edges, const int* __restrict__ einst,
                                const unsigned char* __restrict__ active, const double* __restrict__ X,
                                const double* __restrict__ dir, const unsigned char* __restrict__ dbc,
                                const BoxI* __restrict__ ebox, const BoxI* __restrict__ eboxc,
                                const GridP* __restrict__ gp, const double* __restrict__ thick,
-                               const uint64_t* __restrict__ ckey, const uint32_t* __restrict__ cstart, const uint32_t* __restrict__ ncell_p,
+                               CellHash cells, const uint32_t* __restrict__ cstart,
                                const uint32_t* __restrict__ entries, CCand* __restrict__ out, unsigned int* counter,
                                long cap) {
-    const int ncell = (int)*ncell_p;
-    long eI = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    long eI = ((long)blockIdx.x * blockDim.x + threadIdx.x) / kCcdQueryLanes;
     if (eI >= nE) return;
     int inst = einst[eI];
     if (!active[inst]) return;
@@ -354,7 +407,7 @@ __global__ void k_ccd_query_ee(long nE, const int2* __restrict__ edges, const in
     }
     const BoxI qc = eboxc[eI], qx = ebox[eI];
     const bool adbc = dbc[mi.x] && dbc[mi.y];
-    warp_walk_emit(qc, inst, g, ckey, cstart, ncell, entries, out, counter, cap,
+    group_walk_emit<kCcdQueryLanes>(qc, inst, g, cells, cstart, entries, out, counter, cap,
                    [&](uint32_t ent, int cx, int cy, int cz, CCand& c) -> bool {
                        int eJ = (int)ent;
                        if (eJ <= eI || !is_first_shared(qc, eboxc[eJ], cx, cy, cz) || !boxes_overlap(qx, ebox[eJ]))
@@ -514,7 +567,12 @@ int ccd_stepsize(Arena& A, Work& W, const double* X, const double* dir, double* 
     IDP_CUDA_TRY(cudaMemcpyAsync(d_sn_off, A.sn_off.data(), sizeof(int) * (nI + 1), cudaMemcpyHostToDevice, s));
     if (A.Se) (::idp::count_launch(), k_edge_len<<<grid_for(A.Se), kBlock, 0, s>>>(A.Se, A.sedge, X, len));
     if (A.Sn) (::idp::count_launch(), k_abs_dir<<<grid_for(A.Sn), kBlock, 0, s>>>(A.Sn, A.snode, dir, absdir));
-    (::idp::count_launch(), k_span_cap<<<nI, 256, 0, s>>>(nI, A.active, d_se_off, d_sn_off, len, absdir, sumsc, alpha, vsz));
+    if (W[W_SPAN].ensure(sizeof(double) * (A.n_span_tiles + 1))) return IDP_ERR_CUDA;
+    double* tsum = W[W_SPAN].as<double>();
+    if (A.n_span_tiles > 0)
+        (::idp::count_launch(), k_span_tiles<<<A.n_span_tiles, 256, 0, s>>>(A.span_tiles, A.active, len, absdir, tsum));
+    (::idp::count_launch(), k_span_cap<<<nI, 256, 0, s>>>(nI, A.active, d_se_off, d_sn_off, A.span_tile_off, tsum,
+                                                          sumsc, alpha, vsz));
     // grid
     if (W[W_BBOX].ensure(sizeof(unsigned long long) * 6 * nI) || W[W_GRIDP].ensure(sizeof(GridP) * nI))
         return IDP_ERR_CUDA;
@@ -542,18 +600,22 @@ int ccd_stepsize(Arena& A, Work& W, const double* X, const double* dir, double* 
     if (A.Se)
         (::idp::count_launch(), k_prim_box_from_nodes<2><<<grid_for(A.Se), kBlock, 0, s>>>(A.Se, reinterpret_cast<const int*>(A.sedge), A.v2s,
                                                                    nbox, ebox));
-    (::idp::count_launch(), k_coarse_boxes<<<grid_for(St + Se + Sn), kBlock, 0, s>>>(St + Se + Sn, tbox, tboxc));
     (::idp::count_launch(), k_coarse_grid<<<grid_for(nI), kBlock, 0, s>>>(nI, gp, gc));
+    (::idp::count_launch(), k_coarse_boxes<<<grid_for(St + Se + Sn), kBlock, 0, s>>>(
+                                St, Se, Sn, A.St, A.Se, A.Sn, A.st_inst, A.se_inst, A.sn_inst, gc, tbox, tboxc));
     BoxGrid gt, ge;
     uint32_t* hp = W.pinned();
     if (!hp) return IDP_ERR_CUDA;
+    unsigned long long* hcells = reinterpret_cast<unsigned long long*>(hp + 8);
     int rc = box_grid_count(W, 0, tboxc, A.st_inst, A.active, A.St, hp, s);
     if (!rc) rc = box_grid_count(W, 1, eboxc, A.se_inst, A.active, A.Se, hp + 1, s);
+    if (!rc) rc = grid_cell_bases(W, gc, nI, hcells, s);
     if (rc) return rc;
     IDP_CUDA_TRY(cudaStreamSynchronize(s));
     const long nt_ent = hp[0], ne_ent = hp[1];
-    if ((rc = box_grid_finish(W, 0, tboxc, A.st_inst, A.active, A.St, gc, nI, nt_ent, gt, s))) return rc;
-    if ((rc = box_grid_finish(W, 1, eboxc, A.se_inst, A.active, A.Se, gc, nI, ne_ent, ge, s))) return rc;
+    const unsigned long long ncells = *hcells;
+    if ((rc = box_grid_finish(W, 0, tboxc, A.st_inst, A.active, A.St, gc, nI, nt_ent, ncells, gt, s))) return rc;
+    if ((rc = box_grid_finish(W, 1, eboxc, A.se_inst, A.active, A.Se, gc, nI, ne_ent, ncells, ge, s))) return rc;
     // candidates: PT in [0, cap_pt), EE in [cap_pt, cap_pt + cap_ee), one
     // host round trip for both counts
     if (W[W_CAND_CNT].ensure(64)) return IDP_ERR_CUDA;
@@ -565,12 +627,12 @@ int ccd_stepsize(Arena& A, Work& W, const double* X, const double* dir, double* 
         CCand* cand = W[W_CAND].as<CCand>();
         IDP_CUDA_TRY(cudaMemsetAsync(ccount, 0, 2 * sizeof(unsigned int), s));
         if (A.Sn)
-            (::idp::count_launch(), k_ccd_query_pt<<<grid_for(32 * A.Sn), kBlock, 0, s>>>(A.Sn, A.snode, A.sn_inst, A.active, X, dir, A.dbc, A.stri,
-                                                             nbox, tbox, nboxc, tboxc, gc, A.thickness, gt.cell_keys, gt.cell_start,
-                                                             gt.d_ncell, gt.entries, cand, ccount, cap_pt));
+            (::idp::count_launch(), k_ccd_query_pt<<<grid_for(kCcdQueryLanes * A.Sn), kBlock, 0, s>>>(A.Sn, A.snode, A.sn_inst, A.active, X, dir, A.dbc, A.stri,
+                                                             nbox, tbox, nboxc, tboxc, gc, A.thickness, gt.cells, gt.cell_start,
+                                                             gt.entries, cand, ccount, cap_pt));
         if (A.Se)
-            (::idp::count_launch(), k_ccd_query_ee<<<grid_for(32 * A.Se), kBlock, 0, s>>>(A.Se, A.sedge, A.se_inst, A.active, X, dir, A.dbc, ebox, eboxc, gc,
-                                                             A.thickness, ge.cell_keys, ge.cell_start, ge.d_ncell,
+            (::idp::count_launch(), k_ccd_query_ee<<<grid_for(kCcdQueryLanes * A.Se), kBlock, 0, s>>>(A.Se, A.sedge, A.se_inst, A.active, X, dir, A.dbc, ebox, eboxc, gc,
+                                                             A.thickness, ge.cells, ge.cell_start,
                                                              ge.entries, cand + cap_pt, ccount + 1, cap_ee));
         IDP_CUDA_TRY(cudaMemcpyAsync(hp + 2, ccount, 2 * sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
         IDP_CUDA_TRY(cudaStreamSynchronize(s));

@@ -29,17 +29,17 @@ __global__ void k_bbox(long n, const int* __restrict__ nodes, const int* __restr
                        const unsigned char* __restrict__ active, const double* __restrict__ X,
                        unsigned long long* __restrict__ bb) {
     long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    int inst = ninst[i];
-    if (!active[inst]) return;
-    D3 p = ld3(X, nodes[i]);
-    unsigned long long* b = bb + 6 * inst;
-    atomicMin(b + 0, ord_enc(p.x));
-    atomicMin(b + 1, ord_enc(p.y));
-    atomicMin(b + 2, ord_enc(p.z));
-    atomicMax(b + 3, ord_enc(p.x));
-    atomicMax(b + 4, ord_enc(p.y));
-    atomicMax(b + 5, ord_enc(p.z));
+    const int inst = i < n ? ninst[i] : 0;
+    const int inst_first = ninst[(long)blockIdx.x * blockDim.x];
+    const bool valid = i < n && active[inst];
+    unsigned long long lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+    if (valid) {
+        D3 p = ld3(X, nodes[i]);
+        lo[0] = hi[0] = ord_enc(p.x);
+        lo[1] = hi[1] = ord_enc(p.y);
+        lo[2] = hi[2] = ord_enc(p.z);
+    }
+    bbox_block_update(valid, inst, inst_first, lo, hi, bb);
 }
 
 __global__ void k_bbox_init(int nI, unsigned long long* bb) {
@@ -143,21 +143,88 @@ __global__ void k_box_emit(long n, const BoxI* __restrict__ boxes, const int* __
             }
 }
 
+// first cell of every instance (prefix of the per-instance cell counts) and
+// the total; one thread, instances are few
+__global__ void k_cell_bases(int nI, const GridP* __restrict__ gp, uint32_t* __restrict__ cbase,
+                             unsigned long long* __restrict__ total) {
+    unsigned long long acc = 0;
+    for (int i = 0; i < nI; ++i) {
+        cbase[i] = (uint32_t)(acc < 0xffffffffull ? acc : 0xffffffffull);
+        const GridP g = gp[i];
+        acc += (unsigned long long)g.s2 * (unsigned long long)(g.n[2] + 1);
+    }
+    cbase[nI] = (uint32_t)(acc < 0xffffffffull ? acc : 0xffffffffull);
+    *total = acc;
+}
+
+// dense table: occupancy count per cell, then each box's cells take a slot
+// (the order of the entries inside a cell is immaterial to every consumer:
+// constraint records are sorted afterwards and CCD keeps a minimum)
+__global__ void k_dense_count(long n, const BoxI* __restrict__ boxes, const int* __restrict__ pinst,
+                              const unsigned char* __restrict__ active, const GridP* __restrict__ gp,
+                              const uint32_t* __restrict__ cbase, uint32_t* __restrict__ ccount) {
+    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int inst = pinst[i];
+    if (!active[inst]) return;
+    const BoxI b = boxes[i];
+    const GridP g = gp[inst];
+    const uint32_t c0 = cbase[inst];
+    // boxes are built inside [0, n]; the clamp only guards the table bounds
+    const int zl = max(b.lo[2], 0), zh = min(b.hi[2], g.n[2]), yl = max(b.lo[1], 0), yh = min(b.hi[1], g.n[1]);
+    const int xl = max(b.lo[0], 0), xh = min(b.hi[0], g.n[0]);
+    for (int z = zl; z <= zh; ++z)
+        for (int y = yl; y <= yh; ++y)
+            for (int x = xl; x <= xh; ++x)
+                atomicAdd(ccount + c0 + (uint32_t)((long)x + (long)y * g.s1 + (long)z * g.s2), 1u);
+}
+
+__global__ void k_dense_fill(long n, const BoxI* __restrict__ boxes, const int* __restrict__ pinst,
+                             const unsigned char* __restrict__ active, const GridP* __restrict__ gp,
+                             const uint32_t* __restrict__ cbase, const uint32_t* __restrict__ cstart,
+                             uint32_t* __restrict__ ccount, uint32_t* __restrict__ entries) {
+    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int inst = pinst[i];
+    if (!active[inst]) return;
+    const BoxI b = boxes[i];
+    const GridP g = gp[inst];
+    const uint32_t c0 = cbase[inst];
+    // boxes are built inside [0, n]; the clamp only guards the table bounds
+    const int zl = max(b.lo[2], 0), zh = min(b.hi[2], g.n[2]), yl = max(b.lo[1], 0), yh = min(b.hi[1], g.n[1]);
+    const int xl = max(b.lo[0], 0), xh = min(b.hi[0], g.n[0]);
+    for (int z = zl; z <= zh; ++z)
+        for (int y = yl; y <= yh; ++y)
+            for (int x = xl; x <= xh; ++x) {
+                const uint32_t c = c0 + (uint32_t)((long)x + (long)y * g.s1 + (long)z * g.s2);
+                entries[cstart[c] + atomicSub(ccount + c, 1u) - 1u] = (uint32_t)i;
+            }
+}
+
 __global__ void k_mark_heads(long n, const uint64_t* __restrict__ keys, uint32_t* __restrict__ head) {
     long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     head[i] = (i == 0 || keys[i] != keys[i - 1]) ? 1u : 0u;
 }
 
+// cell starts of the sorted entries and the key -> cell hash
 __global__ void k_cell_table(long n, const uint64_t* __restrict__ keys, const uint32_t* __restrict__ head,
-                             const uint32_t* __restrict__ idx, uint64_t* __restrict__ ckey,
-                             uint32_t* __restrict__ cstart, const uint32_t* __restrict__ ncell) {
+                             const uint32_t* __restrict__ idx, uint32_t* __restrict__ cstart,
+                             const uint32_t* __restrict__ ncell, unsigned long long* __restrict__ hkey,
+                             uint32_t* __restrict__ hval, uint32_t mask) {
     long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i == 0) cstart[*ncell] = (uint32_t)n;
-    if (i >= n) return;
-    if (head[i]) {
-        ckey[idx[i]] = keys[i];
-        cstart[idx[i]] = (uint32_t)i;
+    if (i >= n || !head[i]) return;
+    const uint32_t c = idx[i];
+    cstart[c] = (uint32_t)i;
+    const unsigned long long key = keys[i];
+    uint32_t h = cell_hash(key, mask);
+    for (uint32_t probe = 0; probe <= mask; ++probe) {
+        if (atomicCAS(hkey + h, kHashEmpty, key) == kHashEmpty) {
+            hval[h] = c;
+            return;
+        }
+        h = (h + 1) & mask;
     }
 }
 
@@ -166,18 +233,17 @@ struct Cand {
     int a, b;
 };
 
-// warp per surface node: triangles within the +-dHat box (IPC.h:158-196)
+// one lane group per surface node: triangles within the +-dHat box (IPC.h:158-196)
 __global__ void k_query_pt(long nN, const int* __restrict__ nodes, const int* __restrict__ ninst,
                            const unsigned char* __restrict__ active, const double* __restrict__ X,
                            const unsigned char* __restrict__ dbc, const int* __restrict__ tris,
                            const BoxI* __restrict__ tbox, const GridP* __restrict__ gp,
                            const double* __restrict__ dHat2, const double* __restrict__ thick,
-                           const uint64_t* __restrict__ ckey, const uint32_t* __restrict__ cstart, const uint32_t* __restrict__ ncell_p,
+                           CellHash cells, const uint32_t* __restrict__ cstart,
                            const uint32_t* __restrict__ entries, Cand* __restrict__ out, unsigned int* counter,
                            long cap) {
-    const int ncell = (int)*ncell_p;
-    long s = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (s >= nN) return;  // whole warp leaves together
+    long s = ((long)blockIdx.x * blockDim.x + threadIdx.x) / kQueryLanes;
+    if (s >= nN) return;  // the whole group leaves together
     int inst = ninst[s];
     if (!active[inst]) return;
     int vI = nodes[s];
@@ -192,7 +258,7 @@ __global__ void k_query_pt(long nN, const int* __restrict__ nodes, const int* __
     for (int d = 0; d < 3; ++d) { qb.lo[d] = lo[d]; qb.hi[d] = hi[d]; }
     const double pp[3] = {p.x, p.y, p.z};
     const bool pdbc = dbc[vI] != 0;
-    warp_walk_emit(qb, inst, g, ckey, cstart, ncell, entries, out, counter, cap,
+    group_walk_emit<kQueryLanes>(qb, inst, g, cells, cstart, entries, out, counter, cap,
                    [&](uint32_t ent, int cx, int cy, int cz, Cand& c) -> bool {
                        int f = (int)ent;
                        if (!is_first_shared(qb, tbox[f], cx, cy, cz)) return false;
@@ -209,16 +275,15 @@ __global__ void k_query_pt(long nN, const int* __restrict__ nodes, const int* __
                    });
 }
 
-// warp per surface edge: edges eJ > eI within the +-dHat box (IPC.h:371-420)
+// one lane group per surface edge: edges eJ > eI within the +-dHat box (IPC.h:371-420)
 __global__ void k_query_ee(long nE, const int2* __restrict__ edges, const int* __restrict__ einst,
                            const unsigned char* __restrict__ active, const double* __restrict__ X,
                            const unsigned char* __restrict__ dbc, const BoxI* __restrict__ ebox,
                            const GridP* __restrict__ gp, const double* __restrict__ dHat2,
-                           const double* __restrict__ thick, const uint64_t* __restrict__ ckey,
-                           const uint32_t* __restrict__ cstart, const uint32_t* __restrict__ ncell_p, const uint32_t* __restrict__ entries,
+                           const double* __restrict__ thick, CellHash cells,
+                           const uint32_t* __restrict__ cstart, const uint32_t* __restrict__ entries,
                            Cand* __restrict__ out, unsigned int* counter, long cap) {
-    const int ncell = (int)*ncell_p;
-    long eI = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    long eI = ((long)blockIdx.x * blockDim.x + threadIdx.x) / kQueryLanes;
     if (eI >= nE) return;
     int inst = einst[eI];
     if (!active[inst]) return;
@@ -235,7 +300,7 @@ __global__ void k_query_ee(long nE, const int2* __restrict__ edges, const int* _
     const double amax[3] = {fmax(a0.x, a1.x), fmax(a0.y, a1.y), fmax(a0.z, a1.z)};
     const double amin[3] = {fmin(a0.x, a1.x), fmin(a0.y, a1.y), fmin(a0.z, a1.z)};
     const bool adbc = dbc[mi.x] && dbc[mi.y];
-    warp_walk_emit(qb, inst, g, ckey, cstart, ncell, entries, out, counter, cap,
+    group_walk_emit<kQueryLanes>(qb, inst, g, cells, cstart, entries, out, counter, cap,
                    [&](uint32_t ent, int cx, int cy, int cz, Cand& c) -> bool {
                        int eJ = (int)ent;
                        if (eJ <= eI || !is_first_shared(qb, ebox[eJ], cx, cy, cz)) return false;
@@ -292,7 +357,7 @@ __global__ void k_narrow_pt(long K, const Cand* __restrict__ cand, const int* __
             rec.inst = inst;
         }
     }
-    warp_emit(emit, rec, out, counter, cap);
+    group_emit<32>(emit, rec, out, counter, cap);
 }
 
 __global__ void k_narrow_ee(long K, const Cand* __restrict__ cand, const int2* __restrict__ edges,
@@ -335,7 +400,7 @@ __global__ void k_narrow_ee(long K, const Cand* __restrict__ cand, const int2* _
             rec.inst = inst;
         }
     }
-    warp_emit(emit, rec, out, counter, cap);
+    group_emit<32>(emit, rec, out, counter, cap);
 }
 
 // ---- sort + merge
@@ -432,8 +497,18 @@ int box_grid_count(Work& W, int slot, const BoxI* boxes, const int* inst, const 
     return IDP_OK;
 }
 
+int grid_cell_bases(Work& W, const GridP* gp, int nI, unsigned long long* h_cells, cudaStream_t s) {
+    if (W[W_CBASE].ensure(sizeof(uint32_t) * (nI + 1) + 64)) return IDP_ERR_CUDA;
+    uint32_t* cbase = W[W_CBASE].as<uint32_t>();
+    unsigned long long* total = reinterpret_cast<unsigned long long*>(W[W_CBASE].as<char>() +
+                                                                      ((sizeof(uint32_t) * (nI + 1) + 15) & ~size_t(15)));
+    (::idp::count_launch(), k_cell_bases<<<1, 1, 0, s>>>(nI, gp, cbase, total));
+    IDP_CUDA_TRY(cudaMemcpyAsync(h_cells, total, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    return IDP_OK;
+}
+
 int box_grid_finish(Work& W, int slot, const BoxI* boxes, const int* inst, const unsigned char* active, long nprim,
-                    const GridP* gp, int nI, long ne, BoxGrid& out, cudaStream_t s) {
+                    const GridP* gp, int nI, long ne, unsigned long long ncells, BoxGrid& out, cudaStream_t s) {
     int base = slot == 0 ? W_GRID0 : W_GRID1;
     DBuf& bcnt = W[base + 0];
     DBuf& bkeys = W[base + 1];
@@ -443,7 +518,36 @@ int box_grid_finish(Work& W, int slot, const BoxI* boxes, const int* inst, const
     DBuf& bcell = W[base + 5];
     long np = nprim > 0 ? nprim : 1;
     long nalloc = ne > 0 ? ne : 1;
-    if (bkeys.ensure(8 * nalloc) || bvals.ensure(4 * nalloc) || bkeys2.ensure(8 * nalloc) || bvals2.ensure(4 * nalloc))
+    if (ncells > 0 && ncells <= kDenseMaxCells) {
+        // dense table: cstart (ncells + 1) | per-cell counts (ncells + 1)
+        const long nc = (long)ncells;
+        if (bvals.ensure(4 * nalloc) || bcell.ensure(sizeof(uint32_t) * 2 * (nc + 1) + 64) ||
+            W[W_SCRATCH].ensure(scan_scratch_bytes(nc) + 64))
+            return IDP_ERR_CUDA;
+        uint32_t* cstart = bcell.as<uint32_t>();
+        uint32_t* ccount = cstart + nc + 1;
+        const uint32_t* cbase = W[W_CBASE].as<uint32_t>();
+        IDP_CUDA_TRY(cudaMemsetAsync(ccount, 0, sizeof(uint32_t) * (nc + 1), s));
+        if (nprim > 0)
+            (::idp::count_launch(), k_dense_count<<<grid_for(np), kBlock, 0, s>>>(nprim, boxes, inst, active, gp, cbase,
+                                                                                  ccount));
+        if (scan_exclusive(ccount, cstart, nc, cstart + nc, W[W_SCRATCH].p, s) != cudaSuccess) return IDP_ERR_CUDA;
+        if (nprim > 0)
+            (::idp::count_launch(), k_dense_fill<<<grid_for(np), kBlock, 0, s>>>(nprim, boxes, inst, active, gp, cbase,
+                                                                                 cstart, ccount, bvals.as<uint32_t>()));
+        out.cell_start = cstart;
+        out.entries = bvals.as<uint32_t>();
+        out.cells = CellHash();
+        out.cells.dense = 1;
+        out.cells.cbase = cbase;
+        out.nent = ne;
+        return IDP_OK;
+    }
+    // the sort's spare buffers later hold the cell hash (2x entries, power of two)
+    uint32_t hcap = 16;
+    while ((long)hcap < 2 * nalloc) hcap <<= 1;
+    if (bkeys.ensure(8 * nalloc) || bvals.ensure(4 * nalloc) || bkeys2.ensure(8 * (long)hcap) ||
+        bvals2.ensure(4 * (long)hcap))
         return IDP_ERR_CUDA;
     if (bcell.ensure((8 + 4) * (nalloc + 1) + 4 * (nalloc + 1) * 2 + 64)) return IDP_ERR_CUDA;
     uint32_t* cnt = bcnt.as<uint32_t>();
@@ -454,24 +558,29 @@ int box_grid_finish(Work& W, int slot, const BoxI* boxes, const int* inst, const
     if (radix_sort_pairs(bkeys.as<uint64_t>(), bvals.as<uint32_t>(), bkeys2.as<uint64_t>(), bvals2.as<uint32_t>(), ne,
                          bits, W[W_SCRATCH].p, s) != cudaSuccess)
         return IDP_ERR_CUDA;
-    // cell table: ckey (8B x (ne+1)) | cstart (4B x (ne+1)) | head | idx (+ cell count at idx[ne])
-    uint64_t* ckey = bcell.as<uint64_t>();
-    uint32_t* cstart = reinterpret_cast<uint32_t*>(ckey + nalloc + 1);
+    // cell table: cstart (4B x (ne+1)) | head | idx (+ cell count at idx[ne]);
+    // the hash (twice the entries, rounded up to a power of two) reuses the
+    // sort's spare buffers
+    uint32_t* cstart = bcell.as<uint32_t>();
     uint32_t* head = cstart + nalloc + 1;
     uint32_t* idx = head + nalloc + 1;
+    unsigned long long* hkey = bkeys2.as<unsigned long long>();
+    uint32_t* hval = bvals2.as<uint32_t>();
+    IDP_CUDA_TRY(cudaMemsetAsync(hkey, 0xff, sizeof(unsigned long long) * hcap, s));
     if (ne > 0) {
         (::idp::count_launch(), k_mark_heads<<<grid_for(ne), kBlock, 0, s>>>(ne, bkeys.as<uint64_t>(), head));
         if (scan_exclusive(head, idx, ne, idx + ne, W[W_SCRATCH].p, s) != cudaSuccess) return IDP_ERR_CUDA;
-        (::idp::count_launch(), k_cell_table<<<grid_for(ne), kBlock, 0, s>>>(ne, bkeys.as<uint64_t>(), head, idx, ckey,
-                                                                              cstart, idx + ne));
+        (::idp::count_launch(), k_cell_table<<<grid_for(ne), kBlock, 0, s>>>(ne, bkeys.as<uint64_t>(), head, idx, cstart,
+                                                                              idx + ne, hkey, hval, hcap - 1));
     } else {
         IDP_CUDA_TRY(cudaMemsetAsync(cstart, 0, sizeof(uint32_t), s));
-        IDP_CUDA_TRY(cudaMemsetAsync(idx + ne, 0, sizeof(uint32_t), s));
     }
-    out.cell_keys = ckey;
     out.cell_start = cstart;
     out.entries = bvals.as<uint32_t>();
-    out.d_ncell = idx + ne;
+    out.cells = CellHash();
+    out.cells.key = hkey;
+    out.cells.val = hval;
+    out.cells.mask = hcap - 1;
     out.nent = ne;
     return IDP_OK;
 }
@@ -498,13 +607,16 @@ int build_constraint_set(Arena& A, Work& W, const double* X, ContactSet& cs, cud
     BoxGrid gt, ge;
     uint32_t* hp = W.pinned();
     if (!hp) return IDP_ERR_CUDA;
+    unsigned long long* hcells = reinterpret_cast<unsigned long long*>(hp + 8);
     int rc = box_grid_count(W, 0, tbox, A.st_inst, A.active, A.St, hp, s);
     if (!rc) rc = box_grid_count(W, 1, ebox, A.se_inst, A.active, A.Se, hp + 1, s);
+    if (!rc) rc = grid_cell_bases(W, gp, nI, hcells, s);
     if (rc) return rc;
     IDP_CUDA_TRY(cudaStreamSynchronize(s));
     const long nt_ent = hp[0], ne_ent = hp[1];
-    if ((rc = box_grid_finish(W, 0, tbox, A.st_inst, A.active, A.St, gp, nI, nt_ent, gt, s))) return rc;
-    if ((rc = box_grid_finish(W, 1, ebox, A.se_inst, A.active, A.Se, gp, nI, ne_ent, ge, s))) return rc;
+    const unsigned long long ncells = *hcells;
+    if ((rc = box_grid_finish(W, 0, tbox, A.st_inst, A.active, A.St, gp, nI, nt_ent, ncells, gt, s))) return rc;
+    if ((rc = box_grid_finish(W, 1, ebox, A.se_inst, A.active, A.Se, gp, nI, ne_ent, ncells, ge, s))) return rc;
 
     // 3. candidates: PT in [0, cap_pt), EE in [cap_pt, cap_pt + cap_ee);
     // both queries run before one host round trip reads both counts
@@ -517,12 +629,12 @@ int build_constraint_set(Arena& A, Work& W, const double* X, ContactSet& cs, cud
         Cand* cand = W[W_CAND].as<Cand>();
         IDP_CUDA_TRY(cudaMemsetAsync(ccount, 0, 2 * sizeof(unsigned int), s));
         if (A.Sn)
-            (::idp::count_launch(), k_query_pt<<<grid_for(32 * A.Sn), kBlock, 0, s>>>(A.Sn, A.snode, A.sn_inst, A.active, X, A.dbc, A.stri, tbox, gp,
-                                                         A.dHat2, A.thickness, gt.cell_keys, gt.cell_start, gt.d_ncell,
+            (::idp::count_launch(), k_query_pt<<<grid_for(kQueryLanes * A.Sn), kBlock, 0, s>>>(A.Sn, A.snode, A.sn_inst, A.active, X, A.dbc, A.stri, tbox, gp,
+                                                         A.dHat2, A.thickness, gt.cells, gt.cell_start,
                                                          gt.entries, cand, ccount, cap_pt));
         if (A.Se)
-            (::idp::count_launch(), k_query_ee<<<grid_for(32 * A.Se), kBlock, 0, s>>>(A.Se, A.sedge, A.se_inst, A.active, X, A.dbc, ebox, gp, A.dHat2,
-                                                         A.thickness, ge.cell_keys, ge.cell_start, ge.d_ncell, ge.entries,
+            (::idp::count_launch(), k_query_ee<<<grid_for(kQueryLanes * A.Se), kBlock, 0, s>>>(A.Se, A.sedge, A.se_inst, A.active, X, A.dbc, ebox, gp, A.dHat2,
+                                                         A.thickness, ge.cells, ge.cell_start, ge.entries,
                                                          cand + cap_pt, ccount + 1, cap_ee));
         IDP_CUDA_TRY(cudaMemcpyAsync(hp + 2, ccount, 2 * sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
         IDP_CUDA_TRY(cudaStreamSynchronize(s));

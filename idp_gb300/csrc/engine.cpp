@@ -607,6 +607,21 @@ int idp_commit(idp_ctx* c) {
             for (int a = 0; a < 3; ++a) vt[vfill[stri[3 * f + a]]++] = (int)f;
         rc |= upload(c, A.vtri_ptr, vtp);
         rc |= upload(c, A.vtri, vt);
+        // tiles of the CCD span sums (2048 items each) per instance
+        std::vector<SpanTile> tiles;
+        std::vector<int> toff(2 * nI + 1, 0);
+        for (int i = 0; i < nI; ++i) {
+            const int seg[2][2] = {{A.se_off[i], A.se_off[i + 1] - A.se_off[i]},
+                                   {3 * A.sn_off[i], 3 * (A.sn_off[i + 1] - A.sn_off[i])}};
+            for (int kind = 0; kind < 2; ++kind) {
+                toff[2 * i + kind] = (int)tiles.size();
+                for (int k = 0; k * 2048 < seg[kind][1]; ++k) tiles.push_back({i, kind, seg[kind][0], seg[kind][1], k});
+            }
+        }
+        toff[2 * nI] = (int)tiles.size();
+        A.n_span_tiles = (int)tiles.size();
+        rc |= upload(c, A.span_tiles, tiles);
+        rc |= upload(c, A.span_tile_off, toff);
     }
     // algorithmic bytes of one FP32 PCG iteration per instance: BSR values
     // and column ids once, and ~7 vector reads/writes plus the 3x3

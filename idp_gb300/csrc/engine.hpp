@@ -50,6 +50,15 @@ struct InstState {
     double g0 = 0;             // gradient norm at the first Newton iteration
 };
 
+// one 2048-item tile of an instance's CCD span sums (edge lengths or |dir|)
+struct SpanTile {
+    int inst;
+    int kind;   // 0: edge lengths, 1: |dir| components
+    int start;  // segment start in its array
+    int m;      // segment length
+    int k;      // tile index inside the segment
+};
+
 struct Arena {
     int nI = 0;
     long V = 0, T = 0, Sn = 0, Se = 0, St = 0;
@@ -86,6 +95,9 @@ struct Arena {
     long B = 0;
     int *rowptr = nullptr, *colidx = nullptr, *diagblk = nullptr;
     int *src_ptr = nullptr, *src = nullptr;       // per BSR block: contributing (tet*10+k)*2+transposed
+    SpanTile* span_tiles = nullptr;               // CCD span-sum tiles, instance by instance
+    int* span_tile_off = nullptr;                 // 2 nI + 1: first edge tile, first |dir| tile per instance
+    int n_span_tiles = 0;
     int* vtri_ptr = nullptr;                      // per vertex: incident surface triangles, ascending
     int* vtri = nullptr;
     int* vert_corner_ptr = nullptr;               // per vertex: list of tet*4+corner
@@ -174,7 +186,7 @@ enum WorkSlot {
     W_PREV_CONS, W_PREV_INST, W_PREV_DIST2,
     W_BH, W_BG, W_GENT_KEY, W_GENT_VAL, W_GENT_KEY2, W_GENT_VAL2, W_GENT_HEAD,
     W_TAIL_ROWPTR, W_TAIL_COL, W_TAIL_VAL, W_TAIL_KEYS,
-    W_BSR_VAL, W_DIAG_INV, W_PCG_VEC, W_PCG_SCAL, W_PCG_GRID, W_PCG_VEC64, W_CCD_TMP, W_CCD_ALPHA, W_MISC, W_MISC2,
+    W_BSR_VAL, W_DIAG_INV, W_PCG_VEC, W_PCG_SCAL, W_PCG_GRID, W_SPAN, W_CBASE, W_PCG_VEC64, W_CCD_TMP, W_CCD_ALPHA, W_MISC, W_MISC2,
     W_CL_INT, W_CL_DENSE, W_CL_HOSTCONS,
     W_NUM
 };

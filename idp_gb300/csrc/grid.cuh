@@ -9,6 +9,11 @@
 
 namespace idp {
 
+// lanes per broad-phase query: constraint-set cells (edge-length sized) hold
+// a handful of primitives; the CCD's coarse cells hold many more
+constexpr int kQueryLanes = 8;
+constexpr int kCcdQueryLanes = 32;
+
 struct GridP {
     double lo[3];
     double inv;
@@ -30,6 +35,50 @@ __device__ __forceinline__ double ord_dec(unsigned long long u) {
     return __longlong_as_double((long long)b);
 }
 
+// Block-wide min (lo) / max (hi) of order-encoded coordinates into bb[6*inst]:
+// when every valid thread of the block belongs to the same instance (the
+// usual case: primitives are stored instance by instance) one atomic per
+// value per block, else one per thread. Every thread of the block must call
+// this (valid = false for threads without an element).
+__device__ __forceinline__ void bbox_block_update(bool valid, int inst, int inst_first, const unsigned long long lo[3],
+                                                  const unsigned long long hi[3], unsigned long long* bb) {
+    __shared__ unsigned long long s_v[6][32];
+    const bool uni = __syncthreads_and(!valid || inst == inst_first);
+    const bool any = __syncthreads_or(valid);
+    if (!any) return;
+    if (!uni) {
+        if (valid)
+            for (int d = 0; d < 3; ++d) {
+                atomicMin(bb + 6 * inst + d, lo[d]);
+                atomicMax(bb + 6 * inst + 3 + d, hi[d]);
+            }
+        return;
+    }
+    unsigned long long v[6];
+    for (int d = 0; d < 3; ++d) {
+        v[d] = valid ? lo[d] : ~0ull;
+        v[3 + d] = valid ? hi[d] : 0ull;
+    }
+    for (int o = 16; o > 0; o >>= 1)
+        for (int d = 0; d < 3; ++d) {
+            unsigned long long a = __shfl_xor_sync(0xffffffffu, v[d], o);
+            unsigned long long b = __shfl_xor_sync(0xffffffffu, v[3 + d], o);
+            v[d] = a < v[d] ? a : v[d];
+            v[3 + d] = b > v[3 + d] ? b : v[3 + d];
+        }
+    const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if ((threadIdx.x & 31) == 0)
+        for (int d = 0; d < 6; ++d) s_v[d][warp] = v[d];
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        const int d = threadIdx.x;
+        unsigned long long r = s_v[d][0];
+        for (int w = 1; w < nw; ++w) r = d < 3 ? (s_v[d][w] < r ? s_v[d][w] : r) : (s_v[d][w] > r ? s_v[d][w] : r);
+        if (d < 3) atomicMin(bb + 6 * inst_first + d, r);
+        else atomicMax(bb + 6 * inst_first + d, r);
+    }
+}
+
 __device__ __forceinline__ int clampi(int v, int a, int b) { return v < a ? a : (v > b ? b : v); }
 
 __device__ __forceinline__ int vox(double x, double lo, double inv) { return (int)floor((x - lo) * inv); }
@@ -38,25 +87,62 @@ __device__ __forceinline__ uint64_t cell_key(int inst, const GridP& g, int x, in
     return ((uint64_t)inst << 32) | (uint64_t)((long)x + (long)y * g.s1 + (long)z * g.s2);
 }
 
-__device__ __forceinline__ int lower_bound_u64(const uint64_t* __restrict__ a, int n, uint64_t key) {
-    int lo = 0, hi = n;
-    while (lo < hi) {
-        int mid = (lo + hi) >> 1;
-        if (a[mid] < key) lo = mid + 1;
-        else hi = mid;
-    }
-    return lo;
+
+// open-addressing hash from (instance, cell) key to the cell's index in the
+// sorted cell table (linear probing, table at most half full)
+constexpr unsigned long long kHashEmpty = ~0ull;
+
+// cell lookup of a box grid: either a dense table (cell id = first cell of
+// the instance + linear cell index) or, when the grids would hold too many
+// cells, an open-addressing hash of the occupied cells
+struct CellHash {
+    int dense = 0;
+    const uint32_t* cbase = nullptr;  // dense: first cell of every instance
+    const unsigned long long* key = nullptr;
+    const uint32_t* val = nullptr;
+    uint32_t mask = 0;
+};
+
+// dense tables up to this many cells (all instances of a grid together)
+constexpr unsigned long long kDenseMaxCells = 1ull << 25;
+
+__device__ __forceinline__ uint32_t cell_hash(uint64_t key, uint32_t mask) {
+    uint64_t h = key * 0x9E3779B97F4A7C15ull;
+    h ^= h >> 29;
+    return (uint32_t)h & mask;
 }
 
-// warp-per-query walk: the whole warp visits the cells of box qb in order;
-// for every occupied cell, lanes take the cell's entries 32 at a time and
-// call test(entry, cell) -> emit?; emitted values are compacted with one
-// ballot per 32 entries. All lanes of the warp must call this together.
-template <class V, class Test>
-__device__ __forceinline__ void warp_walk_emit(const BoxI& qb, int inst, const GridP& g, const uint64_t* __restrict__ ckey,
-                                               const uint32_t* __restrict__ cstart, int ncell,
-                                               const uint32_t* __restrict__ entries, V* __restrict__ out,
-                                               unsigned int* counter, long cap, Test&& test);
+__device__ __forceinline__ int cell_find(const CellHash& t, int inst, const GridP& g, int x, int y, int z);
+
+__device__ __forceinline__ int cell_find_key(const CellHash& t, uint64_t key) {
+    uint32_t h = cell_hash(key, t.mask);
+    for (uint32_t probe = 0; probe <= t.mask; ++probe) {
+        const unsigned long long k = t.key[h];
+        if (k == key) return (int)t.val[h];
+        if (k == kHashEmpty) return -1;
+        h = (h + 1) & t.mask;
+    }
+    return -1;
+}
+
+__device__ __forceinline__ int cell_find(const CellHash& t, int inst, const GridP& g, int x, int y, int z) {
+    if (t.dense) {
+        if (x < 0 || y < 0 || z < 0 || x > g.n[0] || y > g.n[1] || z > g.n[2]) return -1;
+        return (int)(t.cbase[inst] + (uint32_t)((long)x + (long)y * g.s1 + (long)z * g.s2));
+    }
+    return cell_find_key(t, cell_key(inst, g, x, y, z));
+}
+
+// group-per-query walk: the G lanes of a group (G divides 32, groups aligned
+// in the warp) visit the cells of box qb in order; for every occupied cell
+// they take the cell's entries G at a time and call
+// test(entry, cx, cy, cz, value) -> emit?; emitted values are compacted with
+// one ballot per G entries. All lanes of the group must call this together.
+template <int G, class V, class Test>
+__device__ __forceinline__ void group_walk_emit(const BoxI& qb, int inst, const GridP& g, const CellHash& cells,
+                                                const uint32_t* __restrict__ cstart,
+                                                const uint32_t* __restrict__ entries, V* __restrict__ out,
+                                                unsigned int* counter, long cap, Test&& test);
 
 // lowest corner cell of the intersection of the query box and box b
 __device__ __forceinline__ bool is_first_shared(const BoxI& q, const BoxI& b, int cx, int cy, int cz) {
@@ -69,53 +155,52 @@ __device__ __forceinline__ bool is_first_shared(const BoxI& q, const BoxI& b, in
     return true;
 }
 
-// warp-cooperative append: lanes with emit=true write v to out[] in a block
-// reserved by one atomicAdd per warp. Writes beyond cap are dropped (the
+// group-cooperative append: lanes with emit=true write v to out[] in a block
+// reserved by one atomicAdd per group. Writes beyond cap are dropped (the
 // counter still counts them so the caller can grow and retry).
-template <class V>
-__device__ __forceinline__ void warp_emit(bool emit, const V& v, V* __restrict__ out, unsigned int* counter, long cap) {
-    unsigned int m = __ballot_sync(0xffffffffu, emit);
+template <int G, class V>
+__device__ __forceinline__ void group_emit(bool emit, const V& v, V* __restrict__ out, unsigned int* counter, long cap) {
+    const int lane = threadIdx.x & 31;
+    const unsigned int gmask = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << (lane & ~(G - 1)));
+    const unsigned int m = __ballot_sync(gmask, emit) & gmask;
     if (!m) return;
-    int lane = threadIdx.x & 31;
-    int leader = __ffs(m) - 1;
+    const int leader = __ffs(m) - 1;
     unsigned int base = 0;
     if (lane == leader) base = atomicAdd(counter, (unsigned int)__popc(m));
-    base = __shfl_sync(0xffffffffu, base, leader);
+    base = __shfl_sync(gmask, base, leader);
     if (emit) {
         unsigned int pos = base + __popc(m & ((1u << lane) - 1u));
         if (pos < cap) out[pos] = v;
     }
 }
 
-template <class V, class Test>
-__device__ __forceinline__ void warp_walk_emit(const BoxI& qb, int inst, const GridP& g, const uint64_t* __restrict__ ckey,
-                                               const uint32_t* __restrict__ cstart, int ncell,
-                                               const uint32_t* __restrict__ entries, V* __restrict__ out,
-                                               unsigned int* counter, long cap, Test&& test) {
-    const int lane = threadIdx.x & 31;
+template <int G, class V, class Test>
+__device__ __forceinline__ void group_walk_emit(const BoxI& qb, int inst, const GridP& g, const CellHash& cells,
+                                                const uint32_t* __restrict__ cstart,
+                                                const uint32_t* __restrict__ entries, V* __restrict__ out,
+                                                unsigned int* counter, long cap, Test&& test) {
+    const int gl = threadIdx.x & (G - 1);
     for (int z = qb.lo[2]; z <= qb.hi[2]; ++z)
         for (int y = qb.lo[1]; y <= qb.hi[1]; ++y)
             for (int x = qb.lo[0]; x <= qb.hi[0]; ++x) {
-                uint64_t key = cell_key(inst, g, x, y, z);
-                int k = lower_bound_u64(ckey, ncell, key);
-                if (k >= ncell || ckey[k] != key) continue;
-                uint32_t e0 = cstart[k], e1 = cstart[k + 1];
-                for (uint32_t base = e0; base < e1; base += 32) {
-                    uint32_t e = base + lane;
+                const int k = cell_find(cells, inst, g, x, y, z);
+                if (k < 0) continue;
+                const uint32_t e0 = cstart[k], e1 = cstart[k + 1];
+                for (uint32_t base = e0; base < e1; base += G) {
+                    const uint32_t e = base + gl;
                     V v;
                     bool emit = false;
                     if (e < e1) emit = test(entries[e], x, y, z, v);
-                    warp_emit(emit, v, out, counter, cap);
+                    group_emit<G>(emit, v, out, counter, cap);
                 }
             }
 }
 
 // ---- host-side builder (contact.cu): sorted (instance, cell) entry table
 struct BoxGrid {
-    uint64_t* cell_keys = nullptr;       // sorted unique keys
     uint32_t* cell_start = nullptr;      // cells + 1
     uint32_t* entries = nullptr;         // primitive ids, grouped by cell
-    const uint32_t* d_ncell = nullptr;   // device: number of cells
+    CellHash cells;                      // (instance, cell) key -> cell index
     long nent = 0;
 };
 
@@ -129,6 +214,9 @@ struct Work;
 int box_grid_count(Work& W, int slot, const BoxI* boxes, const int* inst, const unsigned char* active, long nprim,
                    uint32_t* h_total, cudaStream_t s);
 int box_grid_finish(Work& W, int slot, const BoxI* boxes, const int* inst, const unsigned char* active, long nprim,
-                    const GridP* gp, int nI, long ne, BoxGrid& out, cudaStream_t s);
+                    const GridP* gp, int nI, long ne, unsigned long long ncells, BoxGrid& out, cudaStream_t s);
+// first cell of every instance of a grid and the total cell count (written
+// to *h_cells, pinned host memory, valid after the stream is synchronised)
+int grid_cell_bases(Work& W, const GridP* gp, int nI, unsigned long long* h_cells, cudaStream_t s);
 
 }  // namespace idp

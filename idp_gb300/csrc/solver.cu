@@ -501,6 +501,13 @@ __device__ __forceinline__ T cta_reduce2(T a, T b, T* wsh, T& out_b) {
     return ra;
 }
 
+// sum of one value over the CTA in a fixed order (result on every thread)
+template <class T>
+__device__ __forceinline__ T cta_sum1(T a, T* wsh) {
+    T dummy;
+    return cta_reduce2(a, T(0), wsh, dummy);
+}
+
 template <class T>
 __device__ __forceinline__ void cluster_sum2(cg::cluster_group& cl, T a, T b, T (*slot)[2], int which, T& sa, T& sb) {
     if (threadIdx.x == 0) { slot[which][0] = a; slot[which][1] = b; }
@@ -720,20 +727,20 @@ __device__ __forceinline__ unsigned long long gtimer() {
 }
 
 // Round k (1, 2, ...) over the nc CTAs of one instance. Every CTA adds its
-// partials (a, b; thread 0's values) and arrives on the counter; the CTA
-// whose arrival completes the round (counter = k*nc) sums the partials when
-// `reduce` is set, stores the sums in red and releases the others, who spin
-// (bounded: after kSpinLimit polls the error flag is set and false returned)
-// on the release word. The counter and the release word sit on separate
-// 128-byte lines so the arrivals do not queue behind the polling.
+// partials (kRed values; thread 0's) and arrives on the counter; the CTA
+// whose arrival completes the round (counter = k*nc) sums the partials in
+// CTA order when `reduce` is set, stores the sums in red and releases the
+// others, who spin (bounded: after kSpinLimit polls the error flag is set and
+// false returned) on the release word. The counter and the release word sit
+// on separate 128-byte lines so the arrivals do not queue behind the polling.
+constexpr int kRed = 4;
+
 template <class T>
 __device__ __forceinline__ bool inst_round(unsigned int* ctl, T* red, T* part, int c0, int nc, unsigned int k,
-                                           bool reduce, T a, T b, T& ra, T& rb, int* err, int* sh_i, T* sh_t) {
+                                           bool reduce, const T* a, T* ra, int* err, int* sh_i, T* sh_t) {
     if (threadIdx.x == 0) {
-        if (reduce) {
-            part[2 * blockIdx.x] = a;
-            part[2 * blockIdx.x + 1] = b;
-        }
+        if (reduce)
+            for (int j = 0; j < kRed; ++j) part[kRed * blockIdx.x + j] = a[j];
         __threadfence();
         const unsigned int old = atomicAdd(ctl, 1u);
         sh_i[0] = old == k * (unsigned int)nc - 1u;
@@ -743,19 +750,13 @@ __device__ __forceinline__ bool inst_round(unsigned int* ctl, T* red, T* part, i
     if (sh_i[0]) {
         if (reduce && threadIdx.x < 32) {
             __threadfence();
-            T sa = 0, sb = 0;
-            for (int j = threadIdx.x; j < nc; j += 32) {
-                sa += __ldcg(part + 2 * (c0 + j));
-                sb += __ldcg(part + 2 * (c0 + j) + 1);
-            }
-            for (int o = 16; o > 0; o >>= 1) {
-                sa += __shfl_xor_sync(0xffffffffu, sa, o);
-                sb += __shfl_xor_sync(0xffffffffu, sb, o);
-            }
-            if (threadIdx.x == 0) {
-                red[0] = sa;
-                red[1] = sb;
-            }
+            T acc[kRed] = {};
+            for (int c = threadIdx.x; c < nc; c += 32)
+                for (int j = 0; j < kRed; ++j) acc[j] += __ldcg(part + kRed * (c0 + c) + j);
+            for (int o = 16; o > 0; o >>= 1)
+                for (int j = 0; j < kRed; ++j) acc[j] += __shfl_xor_sync(0xffffffffu, acc[j], o);
+            if (threadIdx.x == 0)
+                for (int j = 0; j < kRed; ++j) red[j] = acc[j];
         }
         if (threadIdx.x == 0) {
             __threadfence();
@@ -776,13 +777,9 @@ __device__ __forceinline__ bool inst_round(unsigned int* ctl, T* red, T* part, i
     __syncthreads();
     const bool ok = sh_i[1] != 0;
     if (reduce) {
-        if (threadIdx.x == 0) {
-            sh_t[0] = __ldcg(red);
-            sh_t[1] = __ldcg(red + 1);
-        }
+        if (threadIdx.x < kRed) sh_t[threadIdx.x] = __ldcg(red + threadIdx.x);
         __syncthreads();
-        ra = sh_t[0];
-        rb = sh_t[1];
+        for (int j = 0; j < kRed; ++j) ra[j] = sh_t[j];
     }
     __syncthreads();  // sh_i / sh_t are reused by the next round
     return ok;
@@ -824,18 +821,19 @@ __global__ void __launch_bounds__(GP_THREADS) k_pcg_grid(
     const int* __restrict__ colidx, const T* __restrict__ val, const int* __restrict__ trp,
     const int* __restrict__ tcol, const T* __restrict__ tval, const unsigned char* __restrict__ dbc,
     const T* __restrict__ dinv, ClusterPC<T> pc, const double* __restrict__ b, T* x, T* r, T* z, T* p, T* q,
-    T* part, T* redbuf, unsigned int* ctlbuf, int* err, const double* __restrict__ tol_inst, double rel_tol,
-    int max_iters, int* __restrict__ iters_out, unsigned long long* prof) {
+    T* u, T* w, T* sv, T* m0, T* m1, T* part, T* redbuf, unsigned int* ctlbuf, int* err,
+    const double* __restrict__ tol_inst, double rel_tol, int max_iters, int* __restrict__ iters_out,
+    unsigned long long* prof) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ T wsh[2 * (GP_THREADS / 32)];
-    __shared__ T sh_t[2];
+    __shared__ T sh_t[kRed];
     __shared__ int sh_i[2];
     __shared__ T rc[3 * kClusterCap];
     const GridCta me = plan[blockIdx.x];
     const int inst = me.inst, v0 = me.v0, v1 = me.v1, c0 = me.c0, nc = me.nc, rank = blockIdx.x - me.c0;
     const int nv = v1 - v0;
     unsigned int* ctl = ctlbuf + (long)kCtlWords * me.slot;
-    T* red = redbuf + 2L * me.slot;
+    T* red = redbuf + (long)kRed * me.slot;
     unsigned int round = 0;
     const bool has_blocks = pc.ioff[inst + 1] > pc.ioff[inst];
     const int lane = threadIdx.x & 31, l8 = lane & 7, warp = threadIdx.x >> 5, nw = GP_THREADS / 32;
@@ -853,13 +851,190 @@ __global__ void __launch_bounds__(GP_THREADS) k_pcg_grid(
     for (int i = threadIdx.x; i < S.ncache; i += GP_THREADS) S.col[i] = colidx[kb0 + i];
     for (int i = threadIdx.x; i < 9 * S.ncache; i += GP_THREADS) S.val[i] = val[9L * kb0 + i];
     __syncthreads();
-    T dummy0, dummy1;
     auto barrier = [&]() {
-        return inst_round<T>(ctl, red, part, c0, nc, ++round, false, T(0), T(0), dummy0, dummy1, err, sh_i, sh_t);
+        T none[kRed] = {};
+        return inst_round<T>(ctl, red, part, c0, nc, ++round, false, none, none, err, sh_i, sh_t);
     };
     auto allreduce = [&](T a, T bb, T& ra, T& rb) {
-        return inst_round<T>(ctl, red, part, c0, nc, ++round, true, a, bb, ra, rb, err, sh_i, sh_t);
+        T in[kRed] = {a, bb}, out[kRed];
+        const bool ok = inst_round<T>(ctl, red, part, c0, nc, ++round, true, in, out, err, sh_i, sh_t);
+        ra = out[0];
+        rb = out[1];
+        return ok;
     };
+    // (a0, a1, a2) = row lv of A times vin; the 8 lanes of a row group each
+    // take every 8th block, the caller reduces across the group
+    auto row_spmv = [&](int lv, const T* vin, T& a0, T& a1, T& a2) {
+        const int v = v0 + lv;
+        const int ka = S.row[lv], kz = S.row[lv + 1];
+        if (kz <= S.ncache) {
+            for (int k = ka + l8; k < kz; k += 8) {
+                const int c = S.col[k];
+                const T* mm = S.val + 9 * k;
+                const T x0 = __ldcg(vin + 3 * c), x1 = __ldcg(vin + 3 * c + 1), x2 = __ldcg(vin + 3 * c + 2);
+                a0 += mm[0] * x0 + mm[1] * x1 + mm[2] * x2;
+                a1 += mm[3] * x0 + mm[4] * x1 + mm[5] * x2;
+                a2 += mm[6] * x0 + mm[7] * x1 + mm[8] * x2;
+            }
+        } else {
+            for (int k = ka + l8; k < kz; k += 8) {
+                const int c = colidx[kb0 + k];
+                const T* mm = val + 9L * (kb0 + k);
+                const T x0 = __ldcg(vin + 3 * c), x1 = __ldcg(vin + 3 * c + 1), x2 = __ldcg(vin + 3 * c + 2);
+                a0 += mm[0] * x0 + mm[1] * x1 + mm[2] * x2;
+                a1 += mm[3] * x0 + mm[4] * x1 + mm[5] * x2;
+                a2 += mm[6] * x0 + mm[7] * x1 + mm[8] * x2;
+            }
+        }
+        const int t1e = trp[v + 1];
+        for (int k = trp[v] + l8; k < t1e; k += 8) {
+            const int c = tcol[k];
+            if (dbc[c]) continue;
+            const T* mm = tval + 9L * k;
+            const T x0 = __ldcg(vin + 3 * c), x1 = __ldcg(vin + 3 * c + 1), x2 = __ldcg(vin + 3 * c + 2);
+            a0 += mm[0] * x0 + mm[1] * x1 + mm[2] * x2;
+            a1 += mm[3] * x0 + mm[4] * x1 + mm[5] * x2;
+            a2 += mm[6] * x0 + mm[7] * x1 + mm[8] * x2;
+        }
+    };
+    auto group_sum3 = [&](T& a0, T& a1, T& a2) {
+        for (int o = 4; o > 0; o >>= 1) {
+            a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+            a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+            a2 += __shfl_xor_sync(0xffffffffu, a2, o);
+        }
+    };
+    if (!has_blocks) {
+        // ---- pipelined PCG (Ghysels & Vanroose): one reduction round per
+        // iteration, which also publishes the vector the next SpMV gathers.
+        // Recurrences: w = A u, m = M w, z = A q, q = M s, s = A p; m is
+        // double-buffered because neighbours gather it while it is updated.
+        for (int lv = threadIdx.x; lv < nv; lv += GP_THREADS) {
+            const int v = v0 + lv;
+            const bool fixed = dbc[v];
+            T rv[3], uv[3];
+            for (int d = 0; d < 3; ++d) rv[d] = fixed ? T(0) : (T)b[3 * v + d];
+            grid_precond(S.dinv + 9 * lv, fixed, rv, uv);
+            for (int d = 0; d < 3; ++d) {
+                const int i3 = 3 * v + d;
+                x[i3] = T(0);
+                r[i3] = rv[d];
+                u[i3] = uv[d];
+                z[i3] = T(0);
+                q[i3] = T(0);
+                sv[i3] = T(0);
+                p[i3] = T(0);
+            }
+        }
+        if (!barrier()) return;
+        // w = A u, m = M w; partials gamma = r.u, delta = w.u, rho = r.r
+        T gam_l = 0, del_l = 0, rho_l = 0;
+        for (int base = 4 * warp; base < nv; base += 4 * nw) {
+            const int lv = base + (lane >> 3);
+            const bool act = lv < nv;
+            const int v = v0 + (act ? lv : 0);
+            const bool fixed = act && dbc[v];
+            T a0 = 0, a1 = 0, a2 = 0;
+            if (act && !fixed) row_spmv(lv, u, a0, a1, a2);
+            group_sum3(a0, a1, a2);
+            T wn = 0;
+            if (act && l8 < 3) {
+                const int i3 = 3 * v + l8;
+                const T uo = u[i3], ro = r[i3];
+                wn = fixed ? T(0) : (l8 == 0 ? a0 : (l8 == 1 ? a1 : a2));
+                w[i3] = wn;
+                gam_l += ro * uo;
+                del_l += wn * uo;
+                rho_l += ro * ro;
+            }
+            const int gb = lane & ~7;
+            const T w0 = __shfl_sync(0xffffffffu, wn, gb), w1 = __shfl_sync(0xffffffffu, wn, gb + 1),
+                    w2 = __shfl_sync(0xffffffffu, wn, gb + 2);
+            if (act && l8 < 3) {
+                const T* D = S.dinv + 9 * lv;
+                m0[3 * v + l8] = fixed ? T(0) : D[3 * l8] * w0 + D[3 * l8 + 1] * w1 + D[3 * l8 + 2] * w2;
+            }
+        }
+        T red3[kRed];
+        {
+            T in[kRed] = {cta_sum1(gam_l, wsh), cta_sum1(del_l, wsh), cta_sum1(rho_l, wsh), T(0)};
+            if (!inst_round<T>(ctl, red, part, c0, nc, ++round, true, in, red3, err, sh_i, sh_t)) return;
+        }
+        T gam = red3[0], del = red3[1];
+        const T rho0 = red3[2];
+        const double tl = tol_inst ? fmax(tol_inst[inst], rel_tol) : rel_tol;
+        const T tol2 = (T)(tl * tl) * rho0;
+        int it = 0;
+        T* mc = m0;
+        T* mn_ = m1;
+        T gam_prev = 0, alpha_prev = 0;
+        if (rho0 > T(0) && rho0 > tol2) {
+            const bool timed = prof && blockIdx.x == 0 && threadIdx.x == 0;
+            unsigned long long t0 = timed ? gtimer() : 0, t1;
+            for (it = 0; it < max_iters;) {
+                T beta = 0, alpha;
+                if (it == 0) {
+                    alpha = gam / del;
+                } else {
+                    beta = gam / gam_prev;
+                    alpha = gam / (del - beta * gam / alpha_prev);
+                }
+                if (!(alpha > T(0)) || !(alpha < T(INFINITY))) break;  // breakdown: keep the current x
+                gam_l = del_l = rho_l = 0;
+                for (int base = 4 * warp; base < nv; base += 4 * nw) {
+                    const int lv = base + (lane >> 3);
+                    const bool act = lv < nv;
+                    const int v = v0 + (act ? lv : 0);
+                    const bool fixed = act && dbc[v];
+                    T mo = 0, zo = 0, qo = 0, so = 0, po = 0, uo = 0, wo = 0, xo = 0, ro = 0;
+                    if (act && l8 < 3) {
+                        const int i3 = 3 * v + l8;
+                        mo = __ldcg(mc + i3);
+                        zo = z[i3]; qo = q[i3]; so = sv[i3]; po = p[i3];
+                        uo = u[i3]; wo = w[i3]; xo = x[i3]; ro = r[i3];
+                    }
+                    T a0 = 0, a1 = 0, a2 = 0;
+                    if (act && !fixed) row_spmv(lv, mc, a0, a1, a2);
+                    group_sum3(a0, a1, a2);
+                    T wn = 0;
+                    if (act && l8 < 3) {
+                        const int i3 = 3 * v + l8;
+                        const T n = fixed ? T(0) : (l8 == 0 ? a0 : (l8 == 1 ? a1 : a2));
+                        const T zn = n + beta * zo, qn = mo + beta * qo, sn = wo + beta * so, pn = uo + beta * po;
+                        const T xn = xo + alpha * pn, rn = ro - alpha * sn, un = uo - alpha * qn;
+                        wn = wo - alpha * zn;
+                        z[i3] = zn; q[i3] = qn; sv[i3] = sn; p[i3] = pn;
+                        x[i3] = xn; r[i3] = rn; u[i3] = un; w[i3] = wn;
+                        gam_l += rn * un;
+                        del_l += wn * un;
+                        rho_l += rn * rn;
+                    }
+                    const int gb = lane & ~7;
+                    const T w0 = __shfl_sync(0xffffffffu, wn, gb), w1 = __shfl_sync(0xffffffffu, wn, gb + 1),
+                            w2 = __shfl_sync(0xffffffffu, wn, gb + 2);
+                    if (act && l8 < 3) {
+                        const T* D = S.dinv + 9 * lv;
+                        mn_[3 * v + l8] = fixed ? T(0) : D[3 * l8] * w0 + D[3 * l8 + 1] * w1 + D[3 * l8 + 2] * w2;
+                    }
+                }
+                T in[kRed] = {cta_sum1(gam_l, wsh), cta_sum1(del_l, wsh), cta_sum1(rho_l, wsh), T(0)};
+                if (timed) { t1 = gtimer(); prof[0] += t1 - t0; t0 = t1; }
+                if (!inst_round<T>(ctl, red, part, c0, nc, ++round, true, in, red3, err, sh_i, sh_t)) return;
+                if (timed) { t1 = gtimer(); prof[1] += t1 - t0; t0 = t1; prof[4] += 1; }
+                ++it;
+                if (red3[2] <= tol2) break;
+                T* tmp = mc;
+                mc = mn_;
+                mn_ = tmp;
+                gam_prev = gam;
+                alpha_prev = alpha;
+                gam = red3[0];
+                del = red3[1];
+            }
+        }
+        if (rank == 0 && threadIdx.x == 0) iters_out[inst] = it;
+        return;
+    }
     // r = b, x = 0, z = M^{-1} r, p = q = 0
     T rr_l = 0, rz_l = 0;
     for (int lv = threadIdx.x; lv < nv; lv += GP_THREADS) {
@@ -1094,11 +1269,12 @@ static int pcg_inner(Arena& A, Work& W, const double* b, double rel_tol, int max
                      T** xout, cudaStream_t s) {
     const int nI = A.nI;
     long n3 = 3 * A.V;
-    if (W[W_PCG_VEC].ensure(sizeof(T) * 5 * (n3 + 4)) || W[W_PCG_SCAL].ensure(sizeof(PcgS) * nI + 64) ||
+    if (W[W_PCG_VEC].ensure(sizeof(T) * 10 * (n3 + 4)) || W[W_PCG_SCAL].ensure(sizeof(PcgS) * nI + 64) ||
         W[W_CHUNK_SUM].ensure(sizeof(double) * 2 * (A.n_vert_chunks + 2)))
         return IDP_ERR_CUDA;
     T* base = W[W_PCG_VEC].as<T>();
     T *x = base, *r = base + n3 + 4, *z = r + n3 + 4, *p = z + n3 + 4, *Ap = p + n3 + 4;
+    T *pu = Ap + n3 + 4, *pw = pu + n3 + 4, *psv = pw + n3 + 4, *pm0 = psv + n3 + 4, *pm1 = pm0 + n3 + 4;
     PcgS* S = W[W_PCG_SCAL].as<PcgS>();
     int* any = reinterpret_cast<int*>(S + nI);
     double* part = W[W_CHUNK_SUM].as<double>();
@@ -1239,10 +1415,10 @@ static int pcg_inner(Arena& A, Work& W, const double* b, double rel_tol, int max
         ++slot;
     }
     if (!plan.empty()) waves.push_back(plan);
-    // W_PCG_GRID: plan | partials (2 per CTA) | sums (2 per instance) | control words | error flag
+    // W_PCG_GRID: plan | partials (kRed per CTA) | sums (kRed per instance) | control words | error flag
     const size_t o_part = sizeof(GridCta) * gmax;
-    const size_t o_red = o_part + sizeof(T) * 2 * (size_t)gmax;
-    const size_t o_ctl = (o_red + sizeof(T) * 2 * (size_t)(nI + 1) + 255) & ~size_t(255);
+    const size_t o_red = o_part + sizeof(T) * kRed * (size_t)gmax;
+    const size_t o_ctl = (o_red + sizeof(T) * kRed * (size_t)(nI + 1) + 255) & ~size_t(255);
     const size_t o_err = o_ctl + sizeof(unsigned int) * kCtlWords * (size_t)(nI + 1);
     if (W[W_PCG_GRID].ensure(o_err + 256)) return IDP_ERR_CUDA;
     // phase timers of CTA 0 (spmv, round 1, update, round 2, iterations) when profiling
@@ -1292,7 +1468,7 @@ static int pcg_inner(Arena& A, Work& W, const double* b, double rel_tol, int max
         IDP_CUDA_TRY(cudaLaunchKernelEx(&cfg, k_pcg_grid<T>, (const GridCta*)d_plan, cap_blocks, nvmax,
                                         (const int*)A.rowptr,
                                         (const int*)A.colidx, val, trp, tcol, tval, (const unsigned char*)A.dbc, dinv,
-                                        pcb, b, x, r, z, p, Ap, d_part, d_red, d_ctl, d_err,
+                                        pcb, b, x, r, z, p, Ap, pu, pw, psv, pm0, pm1, d_part, d_red, d_ctl, d_err,
                                         (const double*)W.tol_inst, rel_tol, max_iters, d_iters, d_prof));
         W.stats.pcg_launches += 1;
     }

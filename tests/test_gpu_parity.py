@@ -192,6 +192,34 @@ def test_newton_direction_solves_system(oracle, gpu_lib, mode, path):
     ctx.close()
 
 
+@pytest.mark.parametrize("path", sorted(PCG_PATHS))
+@pytest.mark.parametrize("mode", [0, 1])
+def test_newton_direction_contact_free(oracle, gpu_lib, mode, path):
+    """A direction without contact constraints (the grid PCG takes its
+    pipelined branch there) against a direct solve."""
+    import idp_gb300 as idp
+    import scipy.sparse.linalg as spla
+    from idp_gb300 import meshgen
+
+    X0, tets, _ = meshgen.blob(n=12, lmax=6, seed=4)
+    pr = cases.problem(X0, tets)
+    rng = np.random.default_rng(5)
+    X = X0 + rng.uniform(-0.01, 0.01, X0.shape)
+    v = rng.normal(size=X0.shape)
+    ctx = ctx_for(idp, X0, tets, pr, mode, v=v, pcg_rel_tol=1e-8, **PCG_PATHS[path])
+    p, its, rel = ctx.newton_direction(0, X)
+    assert rel <= 1e-7 and its > 0
+    pb = oracle_problem(oracle, X, tets, pr, X0=X0)
+    cons, info = oracle.constraint_set(X, X0, oracle.surface(X0, tets), np.zeros(X0.shape[0], np.uint8), pr["dHat2"])
+    assert len(cons) == 0
+    H = oracle._hessian(pb, X, cons, info)
+    g = oracle._gradient(pb, X, X0 + 0.1 * v, cons, info)
+    po = spla.spsolve(H.tocsc(), -g)
+    tol = 1e-6 if mode == 0 else 2e-3
+    assert np.linalg.norm(p - po) <= tol * np.linalg.norm(po)
+    ctx.close()
+
+
 def small_bar_problem():
     from idp_gb300 import meshgen
 
