@@ -390,7 +390,10 @@ def run_flow(args):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None,
                      "traffic": traffic.get("bytes_per_launch") if traffic else None,
-                     "kernel": "k_pcg_cluster (thread-block-cluster PCG, FP32 BSR SpMV + block-Jacobi)",
+                     "kernel": "k_pcg_grid (grid-wide cooperative PCG: BSR rows resident in shared memory, "
+                               "FP32 SpMV + block-Jacobi, one reduction round per iteration)",
+                     "achieved_basis": "algorithmic bytes of the PCG iterations / PCG event time",
+                     "traffic_basis": "ncu DRAM read+write bytes of one launch (profiles/pcg_traffic.json)",
                      "peak_source": peak_kind},
         "gpu_launches": launches,
         "clocks": clocks.summary(),
