@@ -79,6 +79,20 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(value, world):
+    """Max of a per-rank float over all ranks (every rank gets it); the
+    ranks' timed regions are reported by their slowest rank."""
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([value], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def make_workload(args, seed):
     import numpy as np
     from idp_gb300 import meshgen
@@ -323,11 +337,7 @@ def run_flow(args):
                 phase[k] += st[k]
             results.append(res[0])
     barrier()
-    total_ms = sum(dev_ms)
-    if world > 1:
-        t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(sum(dev_ms), world)
     value = world * args.steps / (total_ms / 1000.0)
 
     # ---- FP64 arm from the same start states
@@ -361,11 +371,7 @@ def run_flow(args):
         ctx.advance(check=False)
         ctx.state_ptr(0, Xo.data_ptr())
         e2e_wall.append(time.perf_counter() - t0)
-    e2e_s = sum(e2e_wall)
-    if world > 1:
-        t = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(sum(e2e_wall), world)
     e2e_val = world * len(e2e_wall) / e2e_s
     if rank != 0:
         return
@@ -488,11 +494,7 @@ def run_gpu(args):
             launches += st["kernel_launches"]
             lat += [r["latency_ms"] for r in results]
     barrier()
-    step_ms = statistics.mean(dev_ms)
-    if world > 1:
-        t = torch.tensor([step_ms], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        step_ms = float(t.item())
+    step_ms = max_over_ranks(statistics.mean(dev_ms), world)
     value = world * nI / (step_ms / 1000.0)
 
     # ---- end to end with host buffers (pinned), copies inside the timed region
@@ -511,11 +513,7 @@ def run_gpu(args):
         for i in range(nI):
             ctx.state_ptr(i, Xo[i].data_ptr())
         e2e_wall.append(time.perf_counter() - t0)
-    e2e_s = statistics.mean(e2e_wall)
-    if world > 1:
-        t = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(statistics.mean(e2e_wall), world)
     e2e_val = world * nI / e2e_s
     h2d = 2 * 3 * total_verts * 8
     d2h = 3 * total_verts * 8

@@ -434,8 +434,19 @@ __global__ void k_ccd_query_ee(long nE, const int2* __restrict__ edges, const in
 }
 
 // ---- ACCD (CCD.h:279-328, 330-395)
+// Every 64 iterations a running pair compares its accumulated time of impact
+// with the instance's best result so far (atomic minimum of the finished
+// pairs): once above it, the pair can no longer lower the minimum (its own
+// result only grows), so it stops and contributes nothing. The per-instance
+// minimum, the step size, is unchanged by this.
+constexpr int ACCD_POLL = 64;
+
+__device__ __forceinline__ bool accd_beaten(double toc, const double* best) {
+    return toc > *(volatile const double*)best;
+}
+
 __device__ int accd_pt(D3 p, D3 t0, D3 t1, D3 t2, D3 dp, D3 dt0, D3 dt1, D3 dt2, double eta, double thickness,
-                       double& toc, int& its) {
+                       double& toc, int& its, const double* best) {
     D3 mov = 0.25 * (((dt0 + dt1) + dt2) + dp);
     dt0 = dt0 - mov; dt1 = dt1 - mov; dt2 = dt2 - mov; dp = dp - mov;
     double m2 = fmax(sqn(dt0), fmax(sqn(dt1), sqn(dt2)));
@@ -455,6 +466,7 @@ __device__ int accd_pt(D3 p, D3 t0, D3 t1, D3 t2, D3 dp, D3 dt0, D3 dt1, D3 dt2,
         if (toc != 0 && ((dist2_cur - th2) / (dist_cur + thickness) < gap)) return 1;
         toc += tocLB;
         if (toc > toc_prev) return 0;
+        if ((its & (ACCD_POLL - 1)) == ACCD_POLL - 1 && accd_beaten(toc, best)) return 0;
     }
     return 2;
 }
@@ -469,7 +481,7 @@ __device__ __forceinline__ void ee_eval(D3 ea0, D3 ea1, D3 eb0, D3 eb1, double t
 }
 
 __device__ int accd_ee(D3 ea0, D3 ea1, D3 eb0, D3 eb1, D3 dea0, D3 dea1, D3 deb0, D3 deb1, double eta,
-                       double thickness, double& toc, int& its) {
+                       double thickness, double& toc, int& its, const double* best) {
     D3 mov = 0.25 * (((dea0 + dea1) + deb0) + deb1);
     dea0 = dea0 - mov; dea1 = dea1 - mov; deb0 = deb0 - mov; deb1 = deb1 - mov;
     double maxDispMag = sqrt(fmax(sqn(dea0), sqn(dea1))) + sqrt(fmax(sqn(deb0), sqn(deb1)));
@@ -489,6 +501,7 @@ __device__ int accd_ee(D3 ea0, D3 ea1, D3 eb0, D3 eb1, D3 dea0, D3 dea1, D3 deb0
         if (toc != 0 && (dFunc / (dist_cur + thickness) < gap)) return 1;
         toc += tocLB;
         if (toc > toc_prev) return 0;
+        if ((its & (ACCD_POLL - 1)) == ACCD_POLL - 1 && accd_beaten(toc, best)) return 0;
     }
     return 2;
 }
@@ -512,14 +525,14 @@ __global__ void k_accd(long npt, long nee, const CCand* __restrict__ cand_pt, co
         int t0 = tris[3 * c.b], t1 = tris[3 * c.b + 1], t2 = tris[3 * c.b + 2];
         toc = alpha_cap[inst];
         r = accd_pt(ld3(X, v), ld3(X, t0), ld3(X, t1), ld3(X, t2), ld3(dir, v), ld3(dir, t0), ld3(dir, t1),
-                    ld3(dir, t2), 0.1, thick[inst], toc, its);
+                    ld3(dir, t2), 0.1, thick[inst], toc, its, alpha_min + inst);
         if (toc == 0) atomicOr(flags + inst, 2);
     } else {
         int2 mi = edges[c.a], mj = edges[c.b];
         inst = einst[c.a];
         toc = alpha_cap[inst];
         r = accd_ee(ld3(X, mi.x), ld3(X, mi.y), ld3(X, mj.x), ld3(X, mj.y), ld3(dir, mi.x), ld3(dir, mi.y),
-                    ld3(dir, mj.x), ld3(dir, mj.y), 0.1, thick[inst], toc, its);
+                    ld3(dir, mj.x), ld3(dir, mj.y), 0.1, thick[inst], toc, its, alpha_min + inst);
     }
     if (r == 2) atomicOr(flags + inst, 1);
     if (r != 0) atomic_min_nonneg(alpha_min + inst, toc);

@@ -297,6 +297,7 @@ void idp_default_params(idp_params* p) {
     p->device = 0;
     p->pcg_grid_min_vertices = 0;
     p->pcg_grid_cta_vertices = 0;
+    p->contact_block_vertices = 0;
 }
 
 const char* idp_status_str(int s) {
@@ -326,6 +327,8 @@ idp_ctx* idp_create(const idp_params* p, int* status) {
     else idp_default_params(&c->P);
     c->W.grid_min_v = c->P.pcg_grid_min_vertices > 0 ? c->P.pcg_grid_min_vertices : 16384;
     c->W.grid_vper = c->P.pcg_grid_cta_vertices > 0 ? c->P.pcg_grid_cta_vertices : 112;
+    c->W.cl_cap = c->P.contact_block_vertices > 0 ? std::max(2, std::min(c->P.contact_block_vertices, kClusterCap))
+                                                  : kClusterCap;
     if (cudaSetDevice(c->P.device) != cudaSuccess || cudaStreamCreateWithFlags(&c->s, cudaStreamNonBlocking) != cudaSuccess) {
         delete c;
         if (status) *status = IDP_ERR_CUDA;

@@ -5,9 +5,9 @@
 // cannot see those couplings. Vertices linked through constraints are grouped
 // (union-find over the constraint stencils, groups larger than kClusterCap
 // split in breadth-first order so coupled vertices stay together); every
-// group's dense block of the system matrix is gathered, factored
-// (Cholesky) and inverted on the device, one CTA per group, and the PCG
-// applies the inverse to the group's rows. All other vertices keep their 3x3
+// group's dense block of the system matrix is gathered and factored
+// (Cholesky, then the inverse factor) on the device, one CTA per group, and
+// the PCG applies the block inverse to the group's rows. All other vertices keep their 3x3
 // block-Jacobi inverse. A block whose factorisation fails falls back to the
 // 3x3 inverses of its vertices.
 #include <algorithm>
@@ -55,62 +55,55 @@ __global__ void k_cl_gather(int ncl, const int* __restrict__ off, const int* __r
     }
 }
 
-// in place: K_c <- K_c^{-1} via Cholesky L, W = L^{-1}, K^{-1} = W^T W.
-// ok[c] = 0 when a pivot is not positive.
+// Factor every block: K_c = L L^T (right-looking Cholesky in place, the
+// pivot column staged in shared memory, each warp updating whole rows of the
+// trailing triangle with coalesced accesses), then Y = L^{-1} into Ybuf by
+// forward substitution on the identity, all columns in lock-step (thread c
+// owns column c; row k of Y is read coalesced, L[i][k] is a broadcast).
+// The PCG applies K_c^{-1} = Y^T Y as z = Y^T (Y r). ok[c] = 0 when a pivot
+// is not positive (the block then falls back to 3x3 inverses).
+constexpr int kInvThreads = 1024;
+
 template <class T>
-__global__ void k_cl_invert(int ncl, const int* __restrict__ off, const long long* __restrict__ doff, T* __restrict__ K,
-                            T* __restrict__ Wbuf, int* __restrict__ ok) {
-    __shared__ int fail;
-    int c = blockIdx.x;
-    int N = 3 * (off[c + 1] - off[c]);
+__global__ void __launch_bounds__(kInvThreads) k_cl_invert(int ncl, const int* __restrict__ off,
+                                                           const long long* __restrict__ doff, T* __restrict__ K,
+                                                           T* __restrict__ Ybuf, int* __restrict__ ok) {
+    __shared__ T colj[3 * kClusterCap];
+    const int c = blockIdx.x;
+    const int N = 3 * (off[c + 1] - off[c]);
     T* L = K + doff[c];
-    T* Wm = Wbuf + doff[c];
-    if (threadIdx.x == 0) fail = 0;
-    __syncthreads();
-    // right-looking Cholesky, lower triangle
+    T* Y = Ybuf + doff[c];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     for (int j = 0; j < N; ++j) {
-        if (threadIdx.x == 0) {
-            T d = L[(long)j * N + j];
-            if (!(d > T(0))) fail = 1;
-            L[(long)j * N + j] = sqrt(d > T(0) ? d : T(1));
+        const T d = L[(long)j * N + j];
+        if (!(d > T(0))) {  // every thread sees the same pivot
+            if (threadIdx.x == 0) ok[c] = 0;
+            return;
+        }
+        const T ljj = sqrt(d);
+        for (int i = j + threadIdx.x; i < N; i += blockDim.x) {
+            const T v = i == j ? ljj : L[(long)i * N + j] / ljj;
+            L[(long)i * N + j] = v;
+            colj[i] = v;
         }
         __syncthreads();
-        if (fail) break;
-        T ljj = L[(long)j * N + j];
-        for (int i = j + 1 + threadIdx.x; i < N; i += blockDim.x) L[(long)i * N + j] /= ljj;
-        __syncthreads();
-        int m = N - j - 1;
-        for (long idx = threadIdx.x; idx < (long)m * m; idx += blockDim.x) {
-            int i = j + 1 + (int)(idx / m), k = j + 1 + (int)(idx % m);
-            if (k <= i) L[(long)i * N + k] -= L[(long)i * N + j] * L[(long)k * N + j];
+        for (int i = j + 1 + warp; i < N; i += nw) {
+            const T lij = colj[i];
+            T* Li = L + (long)i * N;
+            for (int k = j + 1 + lane; k <= i; k += 32) Li[k] -= lij * colj[k];
         }
         __syncthreads();
     }
-    if (fail) {
-        if (threadIdx.x == 0) ok[c] = 0;
-        return;
-    }
-    // W = L^{-1}, row by row
+    // Y = L^{-1}: row i of Y from rows k < i (columns c <= k are nonzero)
     for (int i = 0; i < N; ++i) {
-        T lii = L[(long)i * N + i];
-        for (int j = threadIdx.x; j <= i; j += blockDim.x) {
-            if (j == i) {
-                Wm[(long)i * N + i] = T(1) / lii;
-            } else {
-                T sacc = 0;
-                for (int k = j; k < i; ++k) sacc += L[(long)i * N + k] * Wm[(long)k * N + j];
-                Wm[(long)i * N + j] = -sacc / lii;
-            }
+        const T* Li = L + (long)i * N;
+        const T inv = T(1) / Li[i];
+        for (int col = threadIdx.x; col < N; col += blockDim.x) {
+            T acc = col == i ? T(1) : T(0);
+            for (int k = col; k < i; ++k) acc -= Li[k] * Y[(long)k * N + col];
+            Y[(long)i * N + col] = col <= i ? acc * inv : T(0);
         }
         __syncthreads();
-    }
-    // K^{-1}[a][b] = sum_{k >= max(a,b)} W[k][a] W[k][b]
-    for (long idx = threadIdx.x; idx < (long)N * N; idx += blockDim.x) {
-        int a = (int)(idx / N), b = (int)(idx % N);
-        int k0 = a > b ? a : b;
-        T sacc = 0;
-        for (int k = k0; k < N; ++k) sacc += Wm[(long)k * N + a] * Wm[(long)k * N + b];
-        L[idx] = sacc;
     }
     if (threadIdx.x == 0) ok[c] = 1;
 }
@@ -212,7 +205,7 @@ int build_contact_clusters(Arena& A, Work& W, const ContactSet& cs, bool fp64, c
     std::vector<char> taken(m, 0);
     for (auto& comp : comps) {
         if ((int)comp.size() < 2) continue;
-        if ((int)comp.size() <= kClusterCap) {
+        if ((int)comp.size() <= W.cl_cap) {
             blocks.push_back(comp);
             continue;
         }
@@ -221,12 +214,12 @@ int build_contact_clusters(Arena& A, Work& W, const ContactSet& cs, bool fp64, c
             std::vector<int> blk;
             std::deque<int> q{st};
             taken[st] = 1;
-            while (!q.empty() && (int)blk.size() < kClusterCap) {
+            while (!q.empty() && (int)blk.size() < W.cl_cap) {
                 int u = q.front();
                 q.pop_front();
                 blk.push_back(u);
                 for (int w : adj[u])
-                    if (!taken[w] && (int)(blk.size() + q.size()) < kClusterCap) {
+                    if (!taken[w] && (int)(blk.size() + q.size()) < W.cl_cap) {
                         taken[w] = 1;
                         q.push_back(w);
                     }
@@ -307,13 +300,13 @@ int build_contact_clusters(Arena& A, Work& W, const ContactSet& cs, bool fp64, c
         (::idp::count_launch(), k_cl_gather<double><<<ncl, 256, 0, s>>>(ncl, cl.off, cl.vert, cl.vcl, cl.vloc, cl.doff, A.rowptr, A.colidx,
                                                   W[W_BSR_VAL].as<double>(), trp, tcol, W[W_TAIL_VAL].as<double>(),
                                                   A.dbc, K));
-        (::idp::count_launch(), k_cl_invert<double><<<ncl, 1024, 0, s>>>(ncl, cl.off, cl.doff, K, K + cl.dense, okp));
+        (::idp::count_launch(), k_cl_invert<double><<<ncl, kInvThreads, 0, s>>>(ncl, cl.off, cl.doff, K, K + cl.dense, okp));
     } else {
         float* K = W[W_CL_DENSE].as<float>();
         (::idp::count_launch(), k_cl_gather<float><<<ncl, 256, 0, s>>>(ncl, cl.off, cl.vert, cl.vcl, cl.vloc, cl.doff, A.rowptr, A.colidx,
                                                  W[W_BSR_VAL].as<float>(), trp, tcol, W[W_TAIL_VAL].as<float>(), A.dbc,
                                                  K));
-        (::idp::count_launch(), k_cl_invert<float><<<ncl, 1024, 0, s>>>(ncl, cl.off, cl.doff, K, K + cl.dense, okp));
+        (::idp::count_launch(), k_cl_invert<float><<<ncl, kInvThreads, 0, s>>>(ncl, cl.off, cl.doff, K, K + cl.dense, okp));
     }
     return cudaGetLastError() == cudaSuccess ? IDP_OK : IDP_ERR_CUDA;
 }

@@ -432,6 +432,7 @@ __device__ __forceinline__ void precond(long v, const T* __restrict__ dinv, cons
 // hold the same bit-identical scalar). Cluster barriers order the phases.
 // Accumulation precision follows the vectors (FP32 in mixed mode).
 constexpr int CL_THREADS = 512;
+constexpr long kClusterCtaVertices = 160;
 
 // y = A x over block rows [v0, v1) of one CTA: 8 lanes per row, 4 rows per
 // warp in flight (lane j of a row takes blocks k0+j, k0+j+8, ...), a 3-step
@@ -536,12 +537,14 @@ struct ClusterPC {
 };
 
 // z = M^{-1} r on the rows of the blocks owned by this CTA (blocks c of the
-// instance with c % csize == crank): dense inverse, or 3x3 inverses when
-// the block's factorisation failed
+// instance with c % csize == crank): z = Y^T (Y r) with Y = L^{-1} the inverse
+// Cholesky factor of the block, or 3x3 inverses when the factorisation failed.
+// rc must hold 6 * kClusterCap values (r of the block, then Y r).
 template <class T>
 __device__ void apply_blocks(const ClusterPC<T>& pc, int inst, int crank, int csize, const T* __restrict__ dinv,
                              const unsigned char* __restrict__ dbc, const T* __restrict__ r, T* __restrict__ z,
                              T* __restrict__ p_init, T* rc) {
+    T* tc = rc + 3 * kClusterCap;  // second half of the caller's shared buffer
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     for (int c = pc.ioff[inst] + crank; c < pc.ioff[inst + 1]; c += csize) {
         const int o = pc.off[c], n = pc.off[c + 1] - o, N = 3 * n;
@@ -559,20 +562,21 @@ __device__ void apply_blocks(const ClusterPC<T>& pc, int inst, int crank, int cs
         }
         for (int a = threadIdx.x; a < N; a += blockDim.x) rc[a] = __ldcg(r + 3 * pc.vert[o + a / 3] + a % 3);
         __syncthreads();
-        const T* Ki = pc.Kinv + pc.doff[c];
-        // two rows per warp, every load of both rows issued before the sums
+        const T* Yc = pc.Kinv + pc.doff[c];
+        // t = Y r (Y lower triangular; rows by warps, two rows per warp, every
+        // load of both rows issued before the sums); t overwrites tc
         constexpr int kPer = (3 * kClusterCap + 31) / 32;
         for (int a = 2 * warp; a < N; a += 2 * nw) {
-            const T* r0 = Ki + (long)a * N;
+            const T* r0 = Yc + (long)a * N;
             const T* r1 = r0 + N;
             const bool two = a + 1 < N;
             T acc0 = 0, acc1 = 0;
 #pragma unroll
             for (int j = 0; j < kPer; ++j) {
                 const int bb = lane + 32 * j;
-                if (bb < N) {
+                if (bb <= a + 1 && bb < N) {
                     const T rv = rc[bb];
-                    acc0 += __ldg(r0 + bb) * rv;
+                    if (bb <= a) acc0 += __ldg(r0 + bb) * rv;
                     if (two) acc1 += __ldg(r1 + bb) * rv;
                 }
             }
@@ -581,14 +585,21 @@ __device__ void apply_blocks(const ClusterPC<T>& pc, int inst, int crank, int cs
                 acc1 += __shfl_down_sync(0xffffffffu, acc1, ofs);
             }
             if (lane == 0) {
-                for (int e = 0; e < (two ? 2 : 1); ++e) {
-                    const int ae = a + e;
-                    const int v = pc.vert[o + ae / 3];
-                    const T zz = dbc[v] ? T(0) : (e ? acc1 : acc0);
-                    z[3 * v + ae % 3] = zz;
-                    if (p_init) p_init[3 * v + ae % 3] = zz;
-                }
+                tc[a] = acc0;
+                if (two) tc[a + 1] = acc1;
             }
+        }
+        __syncthreads();
+        // z = Y^T t: column b of Y against t, threads over b (row k of Y is
+        // read coalesced)
+        for (int b = threadIdx.x; b < N; b += blockDim.x) {
+            T acc = 0;
+#pragma unroll 4
+            for (int k = b; k < N; ++k) acc += __ldg(Yc + (long)k * N + b) * tc[k];
+            const int v = pc.vert[o + b / 3];
+            const T zz = dbc[v] ? T(0) : acc;
+            z[3 * v + b % 3] = zz;
+            if (p_init) p_init[3 * v + b % 3] = zz;
         }
         __syncthreads();
     }
@@ -604,7 +615,7 @@ __global__ void __launch_bounds__(CL_THREADS) k_pcg_cluster(
     int* __restrict__ iters_out) {
     __shared__ T wsh[2 * (CL_THREADS / 32)];
     __shared__ T slot[4][2];
-    __shared__ T rc[3 * kClusterCap];
+    __shared__ T rc[6 * kClusterCap];
     cg::cluster_group cl = cg::this_cluster();
     const int csize = (int)cl.num_blocks(), crank = (int)cl.block_rank();
     const int inst = inst_list[blockIdx.x / csize];
@@ -714,7 +725,7 @@ __global__ void __launch_bounds__(CL_THREADS) k_pcg_cluster(
 constexpr int GP_THREADS = 256;
 constexpr unsigned int kSpinLimit = 1u << 22;  // ~1 s of polling, then error
 constexpr int kCtlWords = 64;                   // per instance: counter at [0], release word at [32]
-constexpr int kGridSmem = 72 * 1024;            // dynamic shared memory per CTA (three CTAs per SM)
+constexpr int kGridSmem = 69 * 1024;            // dynamic shared memory per CTA (three CTAs per SM)
 
 struct GridCta {
     int inst, v0, v1, c0, nc, slot;
@@ -828,7 +839,7 @@ __global__ void __launch_bounds__(GP_THREADS) k_pcg_grid(
     __shared__ T wsh[2 * (GP_THREADS / 32)];
     __shared__ T sh_t[kRed];
     __shared__ int sh_i[2];
-    __shared__ T rc[3 * kClusterCap];
+    __shared__ T rc[6 * kClusterCap];
     const GridCta me = plan[blockIdx.x];
     const int inst = me.inst, v0 = me.v0, v1 = me.v1, c0 = me.c0, nc = me.nc, rank = blockIdx.x - me.c0;
     const int nv = v1 - v0;
@@ -1290,9 +1301,6 @@ static int pcg_inner(Arena& A, Work& W, const double* b, double rel_tol, int max
     IDP_CUDA_TRY(cudaMemcpyAsync(act.data(), A.active, nI, cudaMemcpyDeviceToHost, s));
     IDP_CUDA_TRY(cudaStreamSynchronize(s));
     bool any_small = false, any_large = false;
-    long vtot = 0;
-    for (int i = 0; i < nI; ++i)
-        if (act[i]) vtot += A.v_off[i + 1] - A.v_off[i];
     std::vector<int> by_size[5];  // cluster sizes 1, 2, 4, 8, 16
     for (int i = 0; i < nI; ++i) {
         if (!act[i]) continue;
@@ -1300,11 +1308,11 @@ static int pcg_inner(Arena& A, Work& W, const double* b, double rel_tol, int max
         if (vi > W.grid_min_v) { large[i] = 1; any_large = true; continue; }
         small[i] = 1;
         any_small = true;
-        // one CTA per ~1.5k vertices (at most 16), but no more than the
-        // launch can keep resident (about two CTAs per SM in total)
-        double fair = (double)vi * 2.0 * 152.0 / (double)(vtot > 0 ? vtot : 1);
+        // cluster size from the instance's own size only (one CTA per ~160
+        // vertices, at most 16), so its reduction order, hence its result,
+        // does not depend on what else is solved in the launch
         int k = 0;
-        while (k < 4 && (1L << k) * 1536L < vi && ((1 << (k + 1)) <= fair || (1 << (k + 1)) <= 4)) ++k;
+        while (k < 4 && (1L << k) * kClusterCtaVertices < vi) ++k;
         by_size[k].push_back(i);
     }
     if (W[W_MISC2].ensure(sizeof(int) * (2 * nI + 64))) return IDP_ERR_CUDA;
@@ -1327,7 +1335,7 @@ static int pcg_inner(Arena& A, Work& W, const double* b, double rel_tol, int max
         pcb.vert = W.cl.vert;
         pcb.doff = W.cl.doff;
         pcb.ok = W.cl.ok;
-        pcb.Kinv = W.cl.n > 0 ? W[W_CL_DENSE].as<T>() : nullptr;
+        pcb.Kinv = W.cl.n > 0 ? W[W_CL_DENSE].as<T>() + W.cl.dense : nullptr;
         W.timer.start(PhaseTimer::PCG, s);
         int base = 0;
         for (int k = 0; k < 5; ++k) {
@@ -1438,7 +1446,7 @@ static int pcg_inner(Arena& A, Work& W, const double* b, double rel_tol, int max
     pcb.vert = W.cl.vert;
     pcb.doff = W.cl.doff;
     pcb.ok = W.cl.ok;
-    pcb.Kinv = W.cl.n > 0 ? W[W_CL_DENSE].as<T>() : nullptr;
+    pcb.Kinv = W.cl.n > 0 ? W[W_CL_DENSE].as<T>() + W.cl.dense : nullptr;
     W.timer.start(PhaseTimer::PCG, s);
     IDP_CUDA_TRY(cudaMemsetAsync(d_err, 0, sizeof(int), s));
     if (d_prof && !W.grid_prof_init) {

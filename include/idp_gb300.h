@@ -52,6 +52,9 @@ typedef struct idp_params {
                              grid-wide PCG (all SMs), the others with one thread-block
                              cluster each; 0 = default (16384)                        */
     int pcg_grid_cta_vertices; /* vertices per CTA in the grid-wide PCG; 0 = default (112) */
+    int contact_block_vertices; /* largest group of contact-coupled vertices the
+                             preconditioner inverts as one dense block (2..192);
+                             0 = default (192)                                        */
 } idp_params;
 
 typedef struct idp_result {
