@@ -262,9 +262,11 @@ struct CCand {
     int a, b;
 };
 
-// candidate search runs on a grid K reference voxels wide; the reference's
-// test (integer voxel boxes overlap) is applied to every pair it returns
-constexpr int CCD_COARSE = 4;
+// candidate search runs on a grid of cells `coarse` reference voxels wide
+// (per instance: the smallest power of two that keeps the instance's grid
+// within kCcdCellBudget cells); the reference's test (integer voxel boxes
+// overlap) is applied to every pair it returns
+constexpr double kCcdCellBudget = 4194304.0;
 
 // coarse boxes of the triangles, edges and nodes (stored in that order),
 // clamped to the coarse grid [0, n]: the clamp is monotone, so every pair of
@@ -293,8 +295,8 @@ __global__ void k_coarse_boxes(long pt, long pe, long pn, long nt, long ne, long
             c.hi[d] = 0;
             continue;
         }
-        const int lo = b.lo[d] >= 0 ? b.lo[d] / CCD_COARSE : -1;
-        const int hi = b.hi[d] >= 0 ? b.hi[d] / CCD_COARSE : -1;
+        const int lo = b.lo[d] >= 0 ? b.lo[d] / g.coarse : -1;
+        const int hi = b.hi[d] >= 0 ? b.hi[d] / g.coarse : -1;
         c.lo[d] = clampi(lo, 0, g.n[d]);
         c.hi[d] = clampi(hi, 0, g.n[d]);
     }
@@ -305,7 +307,12 @@ __global__ void k_coarse_grid(int nI, const GridP* __restrict__ gp, GridP* __res
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nI) return;
     GridP g = gp[i];
-    for (int d = 0; d < 3; ++d) g.n[d] = g.n[d] / CCD_COARSE + 1;
+    int c = 1;
+    while (c < (1 << 20) && ((double)(g.n[0] / c + 2) * (double)(g.n[1] / c + 2) * (double)(g.n[2] / c + 2)) >
+                                kCcdCellBudget)
+        c *= 2;
+    g.coarse = c;
+    for (int d = 0; d < 3; ++d) g.n[d] = g.n[d] / c + 1;
     g.s1 = (long)g.n[0] + 1;
     g.s2 = g.s1 * ((long)g.n[1] + 1);
     gc[i] = g;
@@ -507,14 +514,13 @@ __device__ int accd_ee(D3 ea0, D3 ea1, D3 eb0, D3 eb1, D3 dea0, D3 dea1, D3 deb0
 }
 
 // flags per instance: bit 0 = an ACCD hit its cap, bit 1 = zero step
-__global__ void k_accd(long npt, long nee, const CCand* __restrict__ cand_pt, const CCand* __restrict__ cand_ee,
-                       const int* __restrict__ nodes,
-                       const int* __restrict__ ninst, const int* __restrict__ tris, const int2* __restrict__ edges,
-                       const int* __restrict__ einst, const double* __restrict__ X, const double* __restrict__ dir,
-                       const double* __restrict__ thick, const double* __restrict__ alpha_cap,
-                       double* __restrict__ alpha_min, int* __restrict__ flags) {
-    long k = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= npt + nee) return;
+__device__ __forceinline__ void accd_one(long k, long npt, const CCand* __restrict__ cand_pt,
+                                         const CCand* __restrict__ cand_ee, const int* __restrict__ nodes,
+                                         const int* __restrict__ ninst, const int* __restrict__ tris,
+                                         const int2* __restrict__ edges, const int* __restrict__ einst,
+                                         const double* __restrict__ X, const double* __restrict__ dir,
+                                         const double* __restrict__ thick, const double* __restrict__ alpha_cap,
+                                         double* __restrict__ alpha_min, int* __restrict__ flags) {
     CCand c = k < npt ? cand_pt[k] : cand_ee[k - npt];
     int inst;
     double toc;
@@ -548,6 +554,22 @@ __global__ void k_accd(long npt, long nee, const CCand* __restrict__ cand_pt, co
     }
 }
 
+constexpr int kAccdBlocks = 4 * 152;
+
+// grid-stride over the candidates; the counts come from the device (clamped
+// to the list capacities: an overflowing build is redone by the caller)
+__global__ void k_accd(const unsigned int* __restrict__ counts, long cap_pt, long cap_ee,
+                       const CCand* __restrict__ cand_pt, const CCand* __restrict__ cand_ee,
+                       const int* __restrict__ nodes,
+                       const int* __restrict__ ninst, const int* __restrict__ tris, const int2* __restrict__ edges,
+                       const int* __restrict__ einst, const double* __restrict__ X, const double* __restrict__ dir,
+                       const double* __restrict__ thick, const double* __restrict__ alpha_cap,
+                       double* __restrict__ alpha_min, int* __restrict__ flags) {
+    const long npt = min((long)counts[0], cap_pt), nee = min((long)counts[1], cap_ee);
+    for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < npt + nee; k += (long)gridDim.x * blockDim.x)
+        accd_one(k, npt, cand_pt, cand_ee, nodes, ninst, tris, edges, einst, X, dir, thick, alpha_cap, alpha_min, flags);
+}
+
 __global__ void k_alpha_final(int nI, const unsigned char* __restrict__ active, const double* __restrict__ amin,
                               double* __restrict__ alpha) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -573,11 +595,8 @@ int ccd_stepsize(Arena& A, Work& W, const double* X, const double* dir, double* 
     double* sumsc = absdir + 3 * Sn;
     double* vsz = sumsc + nsum;
     double* amin = vsz + nI;
-    if (W[W_MISC2].ensure(sizeof(int) * (nI + 1) * 2)) return IDP_ERR_CUDA;
-    int* d_se_off = W[W_MISC2].as<int>();
-    int* d_sn_off = d_se_off + nI + 1;
-    IDP_CUDA_TRY(cudaMemcpyAsync(d_se_off, A.se_off.data(), sizeof(int) * (nI + 1), cudaMemcpyHostToDevice, s));
-    IDP_CUDA_TRY(cudaMemcpyAsync(d_sn_off, A.sn_off.data(), sizeof(int) * (nI + 1), cudaMemcpyHostToDevice, s));
+    const int* d_se_off = A.d_se_off;
+    const int* d_sn_off = A.d_sn_off;
     if (A.Se) (::idp::count_launch(), k_edge_len<<<grid_for(A.Se), kBlock, 0, s>>>(A.Se, A.sedge, X, len));
     if (A.Sn) (::idp::count_launch(), k_abs_dir<<<grid_for(A.Sn), kBlock, 0, s>>>(A.Sn, A.snode, dir, absdir));
     if (W[W_SPAN].ensure(sizeof(double) * (A.n_span_tiles + 1))) return IDP_ERR_CUDA;
@@ -616,29 +635,24 @@ int ccd_stepsize(Arena& A, Work& W, const double* X, const double* dir, double* 
     (::idp::count_launch(), k_coarse_grid<<<grid_for(nI), kBlock, 0, s>>>(nI, gp, gc));
     (::idp::count_launch(), k_coarse_boxes<<<grid_for(St + Se + Sn), kBlock, 0, s>>>(
                                 St, Se, Sn, A.St, A.Se, A.Sn, A.st_inst, A.se_inst, A.sn_inst, gc, tbox, tboxc));
-    BoxGrid gt, ge;
+    // grids, candidates (PT in [0, cap_pt), EE in [cap_pt, cap_pt + cap_ee))
+    // and ACCD without a host round trip; one synchronisation at the end reads
+    // the candidate counts and the grids' overflow flag (ccount[2]), and only
+    // a build that fitted publishes its step sizes
     uint32_t* hp = W.pinned();
     if (!hp) return IDP_ERR_CUDA;
-    unsigned long long* hcells = reinterpret_cast<unsigned long long*>(hp + 8);
-    int rc = box_grid_count(W, 0, tboxc, A.st_inst, A.active, A.St, hp, s);
-    if (!rc) rc = box_grid_count(W, 1, eboxc, A.se_inst, A.active, A.Se, hp + 1, s);
-    if (!rc) rc = grid_cell_bases(W, gc, nI, hcells, s);
-    if (rc) return rc;
-    IDP_CUDA_TRY(cudaStreamSynchronize(s));
-    const long nt_ent = hp[0], ne_ent = hp[1];
-    const unsigned long long ncells = *hcells;
-    if ((rc = box_grid_finish(W, 0, tboxc, A.st_inst, A.active, A.St, gc, nI, nt_ent, ncells, gt, s))) return rc;
-    if ((rc = box_grid_finish(W, 1, eboxc, A.se_inst, A.active, A.Se, gc, nI, ne_ent, ncells, ge, s))) return rc;
-    // candidates: PT in [0, cap_pt), EE in [cap_pt, cap_pt + cap_ee), one
-    // host round trip for both counts
     if (W[W_CAND_CNT].ensure(64)) return IDP_ERR_CUDA;
     unsigned int* ccount = W[W_CAND_CNT].as<unsigned int>();
     long cap_pt = std::max<long>(W.ccd_cap_pt, 4 * A.Sn + 1024);
     long cap_ee = std::max<long>(W.ccd_cap_ee, 4 * A.Se + 1024);
-    for (int attempt = 0; attempt < 6; ++attempt) {
+    for (int attempt = 0; attempt < 8; ++attempt) {
+        BoxGrid gt, ge;
+        IDP_CUDA_TRY(cudaMemsetAsync(ccount, 0, 3 * sizeof(unsigned int), s));
+        int rc = grids_build(W, 1, tboxc, A.St, A.st_inst, eboxc, A.Se, A.se_inst, A.active, gc, nI, ccount + 2, gt, ge,
+                             s);
+        if (rc) return rc;
         if (W[W_CAND].ensure(sizeof(CCand) * (cap_pt + cap_ee))) return IDP_ERR_CUDA;
         CCand* cand = W[W_CAND].as<CCand>();
-        IDP_CUDA_TRY(cudaMemsetAsync(ccount, 0, 2 * sizeof(unsigned int), s));
         if (A.Sn)
             (::idp::count_launch(), k_ccd_query_pt<<<grid_for(kCcdQueryLanes * A.Sn), kBlock, 0, s>>>(A.Sn, A.snode, A.sn_inst, A.active, X, dir, A.dbc, A.stri,
                                                              nbox, tbox, nboxc, tboxc, gc, A.thickness, gt.cells, gt.cell_start,
@@ -647,36 +661,38 @@ int ccd_stepsize(Arena& A, Work& W, const double* X, const double* dir, double* 
             (::idp::count_launch(), k_ccd_query_ee<<<grid_for(kCcdQueryLanes * A.Se), kBlock, 0, s>>>(A.Se, A.sedge, A.se_inst, A.active, X, dir, A.dbc, ebox, eboxc, gc,
                                                              A.thickness, ge.cells, ge.cell_start,
                                                              ge.entries, cand + cap_pt, ccount + 1, cap_ee));
-        IDP_CUDA_TRY(cudaMemcpyAsync(hp + 2, ccount, 2 * sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
+        (::idp::count_launch(), k_fill<<<grid_for(nI), kBlock, 0, s>>>(nI, 1e300, amin));
+        IDP_CUDA_TRY(cudaMemsetAsync(flags, 0, sizeof(int) * nI, s));
+        (::idp::count_launch(), k_accd<<<kAccdBlocks, 128, 0, s>>>(ccount, cap_pt, cap_ee, cand, cand + cap_pt, A.snode,
+                                                                    A.sn_inst, A.stri, A.sedge, A.se_inst, X, dir,
+                                                                    A.thickness, alpha, amin, flags));
+        IDP_CUDA_TRY(cudaMemcpyAsync(hp + 2, ccount, 3 * sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
         IDP_CUDA_TRY(cudaStreamSynchronize(s));
         const long npt = hp[2], nee = hp[3];
-        if (npt <= cap_pt && nee <= cap_ee) {
-            (::idp::count_launch(), k_fill<<<grid_for(nI), kBlock, 0, s>>>(nI, 1e300, amin));
-            IDP_CUDA_TRY(cudaMemsetAsync(flags, 0, sizeof(int) * nI, s));
-            if (npt + nee)
-                (::idp::count_launch(), k_accd<<<grid_for(npt + nee, 128), 128, 0, s>>>(npt, nee, cand, cand + cap_pt, A.snode, A.sn_inst, A.stri, A.sedge,
-                                                                A.se_inst, X, dir, A.thickness, alpha, amin, flags));
-            (::idp::count_launch(), k_alpha_final<<<grid_for(nI), kBlock, 0, s>>>(nI, A.active, amin, alpha));
-            if (std::getenv("IDP_PROFILE")) {
-                unsigned long long st[4] = {0, 0, 0, 0};
-                void* sym = nullptr;
-                IDP_CUDA_TRY(cudaGetSymbolAddress(&sym, g_accd_stats));
-                IDP_CUDA_TRY(cudaMemcpyAsync(st, sym, sizeof(st), cudaMemcpyDeviceToHost, s));
-                IDP_CUDA_TRY(cudaMemsetAsync(sym, 0, sizeof(st), s));
-                IDP_CUDA_TRY(cudaStreamSynchronize(s));
-                W.accd_maxit = std::max<long long>(W.accd_maxit, (long long)st[0]);
-                W.accd_long += (long long)st[1];
-                W.accd_total += (long long)st[2];
-                W.accd_pairs += (long long)st[3];
-            }
-            return cudaGetLastError() == cudaSuccess ? IDP_OK : IDP_ERR_CUDA;
+        if (grids_overflowed(W, 1, hp[4])) continue;
+        if (npt > cap_pt || nee > cap_ee) {
+            if (npt > cap_pt) cap_pt = npt + npt / 2 + 1024;
+            if (nee > cap_ee) cap_ee = nee + nee / 2 + 1024;
+            W.ccd_cap_pt = cap_pt;
+            W.ccd_cap_ee = cap_ee;
+            continue;
         }
-        if (npt > cap_pt) cap_pt = npt + npt / 2 + 1024;
-        if (nee > cap_ee) cap_ee = nee + nee / 2 + 1024;
-        W.ccd_cap_pt = cap_pt;
-        W.ccd_cap_ee = cap_ee;
+        (::idp::count_launch(), k_alpha_final<<<grid_for(nI), kBlock, 0, s>>>(nI, A.active, amin, alpha));
+        if (std::getenv("IDP_PROFILE")) {
+            unsigned long long st[4] = {0, 0, 0, 0};
+            void* sym = nullptr;
+            IDP_CUDA_TRY(cudaGetSymbolAddress(&sym, g_accd_stats));
+            IDP_CUDA_TRY(cudaMemcpyAsync(st, sym, sizeof(st), cudaMemcpyDeviceToHost, s));
+            IDP_CUDA_TRY(cudaMemsetAsync(sym, 0, sizeof(st), s));
+            IDP_CUDA_TRY(cudaStreamSynchronize(s));
+            W.accd_maxit = std::max<long long>(W.accd_maxit, (long long)st[0]);
+            W.accd_long += (long long)st[1];
+            W.accd_total += (long long)st[2];
+            W.accd_pairs += (long long)st[3];
+        }
+        return cudaGetLastError() == cudaSuccess ? IDP_OK : IDP_ERR_CUDA;
     }
-    return IDP_ERR_CAPACITY;
+        return IDP_ERR_CAPACITY;
 }
 
 }  // namespace idp

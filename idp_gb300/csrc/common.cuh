@@ -40,9 +40,6 @@ struct Chunk {
     int end;
 };
 constexpr int kChunk = 1024;
-// instances up to this many vertices run PCG in one persistent thread-block
-// cluster; larger ones use the multi-launch path
-constexpr long kClusterPcgMaxV = 262144;
 // vertices per dense contact-cluster block of the preconditioner (576 x 576)
 constexpr int kClusterCap = 192;
 

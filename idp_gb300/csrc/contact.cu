@@ -146,7 +146,8 @@ __global__ void k_box_emit(long n, const BoxI* __restrict__ boxes, const int* __
 // first cell of every instance (prefix of the per-instance cell counts) and
 // the total; one thread, instances are few
 __global__ void k_cell_bases(int nI, const GridP* __restrict__ gp, uint32_t* __restrict__ cbase,
-                             unsigned long long* __restrict__ total) {
+                             unsigned long long* __restrict__ total, unsigned long long cap,
+                             unsigned int* __restrict__ flag) {
     unsigned long long acc = 0;
     for (int i = 0; i < nI; ++i) {
         cbase[i] = (uint32_t)(acc < 0xffffffffull ? acc : 0xffffffffull);
@@ -155,6 +156,70 @@ __global__ void k_cell_bases(int nI, const GridP* __restrict__ gp, uint32_t* __r
     }
     cbase[nI] = (uint32_t)(acc < 0xffffffffull ? acc : 0xffffffffull);
     *total = acc;
+    if (flag && acc > cap) atomicOr(flag, 1u);
+}
+
+// both grids of a broad phase in one pass (boxes [0, nt) are triangles,
+// [nt, nt + ne) edges); cell tables side by side: grid g's cell c is slot
+// g * (cap + 1) + c. Cells past the capacity are skipped (the build is redone).
+__device__ __forceinline__ bool dense2_box(long i, long nt, const BoxI* __restrict__ tbox, const int* __restrict__ tinst,
+                                           const BoxI* __restrict__ ebox, const int* __restrict__ einst,
+                                           const unsigned char* __restrict__ active, BoxI& b, int& inst, int& grid) {
+    grid = i < nt ? 0 : 1;
+    inst = grid ? einst[i - nt] : tinst[i];
+    if (!active[inst]) return false;
+    b = grid ? ebox[i - nt] : tbox[i];
+    return true;
+}
+
+__global__ void k_dense_count2(long nt, long ne, const BoxI* __restrict__ tbox, const int* __restrict__ tinst,
+                               const BoxI* __restrict__ ebox, const int* __restrict__ einst,
+                               const unsigned char* __restrict__ active, const GridP* __restrict__ gp,
+                               const uint32_t* __restrict__ cbase, uint32_t cap, uint32_t* __restrict__ ccount) {
+    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nt + ne) return;
+    BoxI b;
+    int inst, grid;
+    if (!dense2_box(i, nt, tbox, tinst, ebox, einst, active, b, inst, grid)) return;
+    const GridP g = gp[inst];
+    const uint32_t c0 = cbase[inst];
+    uint32_t* cnt = ccount + (size_t)grid * (cap + 1);
+    const int zl = max(b.lo[2], 0), zh = min(b.hi[2], g.n[2]), yl = max(b.lo[1], 0), yh = min(b.hi[1], g.n[1]);
+    const int xl = max(b.lo[0], 0), xh = min(b.hi[0], g.n[0]);
+    for (int z = zl; z <= zh; ++z)
+        for (int y = yl; y <= yh; ++y)
+            for (int x = xl; x <= xh; ++x) {
+                const uint32_t c = c0 + (uint32_t)((long)x + (long)y * g.s1 + (long)z * g.s2);
+                if (c < cap) atomicAdd(cnt + c, 1u);
+            }
+}
+
+__global__ void k_dense_fill2(long nt, long ne, const BoxI* __restrict__ tbox, const int* __restrict__ tinst,
+                              const BoxI* __restrict__ ebox, const int* __restrict__ einst,
+                              const unsigned char* __restrict__ active, const GridP* __restrict__ gp,
+                              const uint32_t* __restrict__ cbase, uint32_t cap, const uint32_t* __restrict__ cstart,
+                              uint32_t* __restrict__ ccount, uint32_t* __restrict__ entries, long ent_cap,
+                              unsigned int* __restrict__ flag) {
+    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nt + ne) return;
+    BoxI b;
+    int inst, grid;
+    if (!dense2_box(i, nt, tbox, tinst, ebox, einst, active, b, inst, grid)) return;
+    const GridP g = gp[inst];
+    const uint32_t c0 = cbase[inst];
+    const size_t base = (size_t)grid * (cap + 1);
+    const int zl = max(b.lo[2], 0), zh = min(b.hi[2], g.n[2]), yl = max(b.lo[1], 0), yh = min(b.hi[1], g.n[1]);
+    const int xl = max(b.lo[0], 0), xh = min(b.hi[0], g.n[0]);
+    const uint32_t prim = (uint32_t)(grid ? i - nt : i);
+    for (int z = zl; z <= zh; ++z)
+        for (int y = yl; y <= yh; ++y)
+            for (int x = xl; x <= xh; ++x) {
+                const uint32_t c = c0 + (uint32_t)((long)x + (long)y * g.s1 + (long)z * g.s2);
+                if (c >= cap) continue;
+                const uint32_t pos = cstart[base + c] + atomicSub(ccount + base + c, 1u) - 1u;
+                if (pos < ent_cap) entries[pos] = prim;
+                else atomicOr(flag, 2u);
+            }
 }
 
 // dense table: occupancy count per cell, then each box's cells take a slot
@@ -502,7 +567,7 @@ int grid_cell_bases(Work& W, const GridP* gp, int nI, unsigned long long* h_cell
     uint32_t* cbase = W[W_CBASE].as<uint32_t>();
     unsigned long long* total = reinterpret_cast<unsigned long long*>(W[W_CBASE].as<char>() +
                                                                       ((sizeof(uint32_t) * (nI + 1) + 15) & ~size_t(15)));
-    (::idp::count_launch(), k_cell_bases<<<1, 1, 0, s>>>(nI, gp, cbase, total));
+    (::idp::count_launch(), k_cell_bases<<<1, 1, 0, s>>>(nI, gp, cbase, total, ~0ull, nullptr));
     IDP_CUDA_TRY(cudaMemcpyAsync(h_cells, total, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
     return IDP_OK;
 }
@@ -540,6 +605,7 @@ int box_grid_finish(Work& W, int slot, const BoxI* boxes, const int* inst, const
         out.cells = CellHash();
         out.cells.dense = 1;
         out.cells.cbase = cbase;
+        out.cells.cap = (uint32_t)nc;
         out.nent = ne;
         return IDP_OK;
     }
@@ -585,6 +651,77 @@ int box_grid_finish(Work& W, int slot, const BoxI* boxes, const int* inst, const
     return IDP_OK;
 }
 
+bool grids_overflowed(Work& W, int set, unsigned int flag) {
+    if (!flag) return false;
+    W.dense_ready[set] = false;  // the next build counts with a round trip and resizes
+    return true;
+}
+
+int grids_build(Work& W, int set, const BoxI* tbox, long nt, const int* tinst, const BoxI* ebox, long ne,
+                const int* einst, const unsigned char* active, const GridP* gp, int nI, unsigned int* d_flag,
+                BoxGrid& gt, BoxGrid& ge, cudaStream_t s) {
+    if (W[W_CBASE].ensure(sizeof(uint32_t) * (nI + 1) + 64)) return IDP_ERR_CUDA;
+    uint32_t* cbase = W[W_CBASE].as<uint32_t>();
+    unsigned long long* d_total = reinterpret_cast<unsigned long long*>(W[W_CBASE].as<char>() +
+                                                                        ((sizeof(uint32_t) * (nI + 1) + 15) & ~size_t(15)));
+    if (W.dense_ready[set]) {
+        // dense tables at the capacities of earlier builds, no round trip
+        const unsigned long long cap = W.dense_cells_cap[set];
+        const long ent_cap = W.dense_ent_cap[set];
+        const size_t slots = 2 * (size_t)(cap + 1);
+        DBuf& tab = W[set ? W_DENSE1 : W_DENSE0];
+        DBuf& ent = W[W_GRID0 + 2];
+        if (tab.ensure(sizeof(uint32_t) * (2 * slots + 2)) || ent.ensure(sizeof(uint32_t) * (ent_cap + 1)) ||
+            W[W_SCRATCH].ensure(scan_scratch_bytes((long)slots) + 64))
+            return IDP_ERR_CUDA;
+        uint32_t* ccount = tab.as<uint32_t>();
+        uint32_t* cstart = ccount + slots + 1;
+        (::idp::count_launch(), k_cell_bases<<<1, 1, 0, s>>>(nI, gp, cbase, d_total, cap, d_flag));
+        IDP_CUDA_TRY(cudaMemsetAsync(ccount, 0, sizeof(uint32_t) * slots, s));
+        const long n = nt + ne;
+        if (n > 0)
+            (::idp::count_launch(), k_dense_count2<<<grid_for(n), kBlock, 0, s>>>(nt, ne, tbox, tinst, ebox, einst, active,
+                                                                                  gp, cbase, (uint32_t)cap, ccount));
+        if (scan_exclusive(ccount, cstart, (long)slots, cstart + slots, W[W_SCRATCH].p, s) != cudaSuccess)
+            return IDP_ERR_CUDA;
+        if (n > 0)
+            (::idp::count_launch(), k_dense_fill2<<<grid_for(n), kBlock, 0, s>>>(
+                                        nt, ne, tbox, tinst, ebox, einst, active, gp, cbase, (uint32_t)cap, cstart,
+                                        ccount, ent.as<uint32_t>(), ent_cap, d_flag));
+        for (int g = 0; g < 2; ++g) {
+            BoxGrid& o = g ? ge : gt;
+            o.cell_start = cstart + (size_t)g * (cap + 1);
+            o.entries = ent.as<uint32_t>();
+            o.cells = CellHash();
+            o.cells.dense = 1;
+            o.cells.cbase = cbase;
+            o.cells.cap = (uint32_t)cap;
+            o.cells.ent_cap = (uint32_t)ent_cap;
+            o.nent = -1;
+        }
+        return IDP_OK;
+    }
+    // counted build with one round trip; records capacities for the next ones
+    uint32_t* hp = W.pinned();
+    if (!hp) return IDP_ERR_CUDA;
+    unsigned long long* hcells = reinterpret_cast<unsigned long long*>(hp + 8);
+    int rc = box_grid_count(W, 0, tbox, tinst, active, nt, hp, s);
+    if (!rc) rc = box_grid_count(W, 1, ebox, einst, active, ne, hp + 1, s);
+    if (!rc) rc = grid_cell_bases(W, gp, nI, hcells, s);
+    if (rc) return rc;
+    IDP_CUDA_TRY(cudaStreamSynchronize(s));
+    const long nt_ent = hp[0], ne_ent = hp[1];
+    const unsigned long long ncells = *hcells;
+    if ((rc = box_grid_finish(W, 0, tbox, tinst, active, nt, gp, nI, nt_ent, ncells, gt, s))) return rc;
+    if ((rc = box_grid_finish(W, 1, ebox, einst, active, ne, gp, nI, ne_ent, ncells, ge, s))) return rc;
+    if (ncells > 0 && ncells * 5 / 4 + 1024 <= kDenseMaxCells) {
+        W.dense_ready[set] = true;
+        W.dense_cells_cap[set] = std::max(W.dense_cells_cap[set], ncells * 5 / 4 + 1024);
+        W.dense_ent_cap[set] = std::max(W.dense_ent_cap[set], (nt_ent + ne_ent) * 5 / 4 + 1024);
+    }
+    return IDP_OK;
+}
+
 int build_constraint_set(Arena& A, Work& W, const double* X, ContactSet& cs, cudaStream_t s) {
     const int nI = A.nI;
     // 1. per-instance grid parameters
@@ -604,30 +741,24 @@ int build_constraint_set(Arena& A, Work& W, const double* X, ContactSet& cs, cud
     if (A.Se)
         (::idp::count_launch(), k_prim_boxes<2><<<grid_for(A.Se), kBlock, 0, s>>>(A.Se, reinterpret_cast<const int*>(A.sedge), A.se_inst,
                                                            A.active, X, gp, ebox));
-    BoxGrid gt, ge;
+    // 3. grids and candidates: PT in [0, cap_pt), EE in [cap_pt, cap_pt +
+    // cap_ee); one host round trip reads both counts and the grids' overflow
+    // flag (ccount[2])
     uint32_t* hp = W.pinned();
     if (!hp) return IDP_ERR_CUDA;
-    unsigned long long* hcells = reinterpret_cast<unsigned long long*>(hp + 8);
-    int rc = box_grid_count(W, 0, tbox, A.st_inst, A.active, A.St, hp, s);
-    if (!rc) rc = box_grid_count(W, 1, ebox, A.se_inst, A.active, A.Se, hp + 1, s);
-    if (!rc) rc = grid_cell_bases(W, gp, nI, hcells, s);
-    if (rc) return rc;
-    IDP_CUDA_TRY(cudaStreamSynchronize(s));
-    const long nt_ent = hp[0], ne_ent = hp[1];
-    const unsigned long long ncells = *hcells;
-    if ((rc = box_grid_finish(W, 0, tbox, A.st_inst, A.active, A.St, gp, nI, nt_ent, ncells, gt, s))) return rc;
-    if ((rc = box_grid_finish(W, 1, ebox, A.se_inst, A.active, A.Se, gp, nI, ne_ent, ncells, ge, s))) return rc;
-
-    // 3. candidates: PT in [0, cap_pt), EE in [cap_pt, cap_pt + cap_ee);
-    // both queries run before one host round trip reads both counts
     if (W[W_CAND_CNT].ensure(64)) return IDP_ERR_CUDA;
     unsigned int* ccount = W[W_CAND_CNT].as<unsigned int>();
     long cap_pt = std::max<long>(W.cand_cap_pt, 2 * A.Sn + 512);
     long cap_ee = std::max<long>(W.cand_cap_ee, 2 * A.Se + 512);
-    for (int attempt = 0; attempt < 4; ++attempt) {
+    int rc = IDP_OK;
+    for (int attempt = 0; attempt < 6; ++attempt) {
+        BoxGrid gt, ge;
+        IDP_CUDA_TRY(cudaMemsetAsync(ccount, 0, 3 * sizeof(unsigned int), s));
+        if ((rc = grids_build(W, 0, tbox, A.St, A.st_inst, ebox, A.Se, A.se_inst, A.active, gp, nI, ccount + 2, gt, ge,
+                              s)))
+            return rc;
         if (W[W_CAND].ensure(sizeof(Cand) * (cap_pt + cap_ee))) return IDP_ERR_CUDA;
         Cand* cand = W[W_CAND].as<Cand>();
-        IDP_CUDA_TRY(cudaMemsetAsync(ccount, 0, 2 * sizeof(unsigned int), s));
         if (A.Sn)
             (::idp::count_launch(), k_query_pt<<<grid_for(kQueryLanes * A.Sn), kBlock, 0, s>>>(A.Sn, A.snode, A.sn_inst, A.active, X, A.dbc, A.stri, tbox, gp,
                                                          A.dHat2, A.thickness, gt.cells, gt.cell_start,
@@ -636,9 +767,10 @@ int build_constraint_set(Arena& A, Work& W, const double* X, ContactSet& cs, cud
             (::idp::count_launch(), k_query_ee<<<grid_for(kQueryLanes * A.Se), kBlock, 0, s>>>(A.Se, A.sedge, A.se_inst, A.active, X, A.dbc, ebox, gp, A.dHat2,
                                                          A.thickness, ge.cells, ge.cell_start, ge.entries,
                                                          cand + cap_pt, ccount + 1, cap_ee));
-        IDP_CUDA_TRY(cudaMemcpyAsync(hp + 2, ccount, 2 * sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
+        IDP_CUDA_TRY(cudaMemcpyAsync(hp + 2, ccount, 3 * sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
         IDP_CUDA_TRY(cudaStreamSynchronize(s));
         const long npt = hp[2], nee = hp[3];
+        if (grids_overflowed(W, 0, hp[4])) continue;
         if (npt > cap_pt || nee > cap_ee) {
             if (npt > cap_pt) cap_pt = npt + npt / 2 + 1024;
             if (nee > cap_ee) cap_ee = nee + nee / 2 + 1024;

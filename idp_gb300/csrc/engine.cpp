@@ -625,6 +625,8 @@ int idp_commit(idp_ctx* c) {
         A.n_span_tiles = (int)tiles.size();
         rc |= upload(c, A.span_tiles, tiles);
         rc |= upload(c, A.span_tile_off, toff);
+        rc |= upload(c, A.d_se_off, A.se_off);
+        rc |= upload(c, A.d_sn_off, A.sn_off);
     }
     // algorithmic bytes of one FP32 PCG iteration per instance: BSR values
     // and column ids once, and ~7 vector reads/writes plus the 3x3

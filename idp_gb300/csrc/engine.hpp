@@ -95,6 +95,8 @@ struct Arena {
     long B = 0;
     int *rowptr = nullptr, *colidx = nullptr, *diagblk = nullptr;
     int *src_ptr = nullptr, *src = nullptr;       // per BSR block: contributing (tet*10+k)*2+transposed
+    int* d_se_off = nullptr;                      // device copies of se_off / sn_off
+    int* d_sn_off = nullptr;
     SpanTile* span_tiles = nullptr;               // CCD span-sum tiles, instance by instance
     int* span_tile_off = nullptr;                 // 2 nI + 1: first edge tile, first |dir| tile per instance
     int n_span_tiles = 0;
@@ -186,7 +188,7 @@ enum WorkSlot {
     W_PREV_CONS, W_PREV_INST, W_PREV_DIST2,
     W_BH, W_BG, W_GENT_KEY, W_GENT_VAL, W_GENT_KEY2, W_GENT_VAL2, W_GENT_HEAD,
     W_TAIL_ROWPTR, W_TAIL_COL, W_TAIL_VAL, W_TAIL_KEYS,
-    W_BSR_VAL, W_DIAG_INV, W_PCG_VEC, W_PCG_SCAL, W_PCG_GRID, W_SPAN, W_CBASE, W_PCG_VEC64, W_CCD_TMP, W_CCD_ALPHA, W_MISC, W_MISC2,
+    W_BSR_VAL, W_DIAG_INV, W_PCG_VEC, W_PCG_GRID, W_SPAN, W_CBASE, W_DENSE0, W_DENSE1, W_PCG_VEC64, W_CCD_TMP, W_CCD_ALPHA, W_MISC, W_MISC2,
     W_CL_INT, W_CL_DENSE, W_CL_HOSTCONS,
     W_NUM
 };
@@ -217,6 +219,11 @@ struct Work {
     } cl;
     long cand_cap_pt = 0, cand_cap_ee = 0;   // candidate list capacities (grown on overflow)
     long ccd_cap_pt = 0, ccd_cap_ee = 0;
+    // dense cell tables of the two broad phases (0: constraint set, 1: CCD):
+    // capacities from the last synchronised build, reused without a round trip
+    bool dense_ready[2] = {false, false};
+    unsigned long long dense_cells_cap[2] = {0, 0};
+    long dense_ent_cap[2] = {0, 0};
     unsigned long long grid_prof[5] = {0, 0, 0, 0, 0};  // grid PCG phase ns (IDP_PROFILE)
     bool grid_prof_init = false;
     uint32_t* hpin = nullptr;                // 64 words of pinned host memory for batched readbacks

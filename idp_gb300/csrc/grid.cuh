@@ -10,14 +10,15 @@
 namespace idp {
 
 // lanes per broad-phase query: constraint-set cells (edge-length sized) hold
-// a handful of primitives; the CCD's coarse cells hold many more
+// a handful of primitives; CCD cells (one or more reference voxels) hold more
 constexpr int kQueryLanes = 8;
-constexpr int kCcdQueryLanes = 32;
+constexpr int kCcdQueryLanes = 16;
 
 struct GridP {
     double lo[3];
     double inv;
     int n[3];      // cells per axis (indices clamped to [0, n])
+    int coarse;    // CCD candidate grid: reference voxels per cell along each axis
     long s1, s2;   // linear strides: cell = x + y*s1 + z*s2
 };
 
@@ -98,6 +99,8 @@ constexpr unsigned long long kHashEmpty = ~0ull;
 struct CellHash {
     int dense = 0;
     const uint32_t* cbase = nullptr;  // dense: first cell of every instance
+    uint32_t cap = 0xffffffffu;        // dense: cells in the table (lookups past it miss)
+    uint32_t ent_cap = 0xffffffffu;    // entries in the table
     const unsigned long long* key = nullptr;
     const uint32_t* val = nullptr;
     uint32_t mask = 0;
@@ -128,7 +131,8 @@ __device__ __forceinline__ int cell_find_key(const CellHash& t, uint64_t key) {
 __device__ __forceinline__ int cell_find(const CellHash& t, int inst, const GridP& g, int x, int y, int z) {
     if (t.dense) {
         if (x < 0 || y < 0 || z < 0 || x > g.n[0] || y > g.n[1] || z > g.n[2]) return -1;
-        return (int)(t.cbase[inst] + (uint32_t)((long)x + (long)y * g.s1 + (long)z * g.s2));
+        const uint32_t c = t.cbase[inst] + (uint32_t)((long)x + (long)y * g.s1 + (long)z * g.s2);
+        return c < t.cap ? (int)c : -1;
     }
     return cell_find_key(t, cell_key(inst, g, x, y, z));
 }
@@ -185,7 +189,7 @@ __device__ __forceinline__ void group_walk_emit(const BoxI& qb, int inst, const 
             for (int x = qb.lo[0]; x <= qb.hi[0]; ++x) {
                 const int k = cell_find(cells, inst, g, x, y, z);
                 if (k < 0) continue;
-                const uint32_t e0 = cstart[k], e1 = cstart[k + 1];
+                const uint32_t e0 = cstart[k], e1 = min(cstart[k + 1], cells.ent_cap);
                 for (uint32_t base = e0; base < e1; base += G) {
                     const uint32_t e = base + gl;
                     V v;
@@ -215,6 +219,16 @@ int box_grid_count(Work& W, int slot, const BoxI* boxes, const int* inst, const 
                    uint32_t* h_total, cudaStream_t s);
 int box_grid_finish(Work& W, int slot, const BoxI* boxes, const int* inst, const unsigned char* active, long nprim,
                     const GridP* gp, int nI, long ne, unsigned long long ncells, BoxGrid& out, cudaStream_t s);
+// Triangle (gt) and edge (ge) grids of one broad phase (set 0: constraint
+// set, 1: CCD). Once a set has been built with a host round trip, later
+// builds reuse its table capacities without one: the kernels record in
+// *d_flag (bit 0: more cells, bit 1: more entries than the capacities) what
+// did not fit, and the caller, at its next synchronisation, calls
+// grids_overflowed and rebuilds when it returns true.
+int grids_build(Work& W, int set, const BoxI* tbox, long nt, const int* tinst, const BoxI* ebox, long ne,
+                const int* einst, const unsigned char* active, const GridP* gp, int nI, unsigned int* d_flag,
+                BoxGrid& gt, BoxGrid& ge, cudaStream_t s);
+bool grids_overflowed(Work& W, int set, unsigned int flag);
 // first cell of every instance of a grid and the total cell count (written
 // to *h_cells, pinned host memory, valid after the stream is synchronised)
 int grid_cell_bases(Work& W, const GridP* gp, int nI, unsigned long long* h_cells, cudaStream_t s);

@@ -147,181 +147,50 @@ __device__ double cta_sum(double v) {
     return r;
 }
 
-// per-instance PCG scalars
-struct PcgS {
-    double rz, rz_new, pAp, rr, bnorm2, tol2;
-    double alpha, beta;
-    int run;    // still iterating
-    int iters;
-};
-
-// Ap = A p and chunk partials of p.Ap (one CTA per vertex chunk)
-template <class T>
-__global__ void k_pcg_spmv(const Chunk* __restrict__ chunks, const PcgS* __restrict__ S, const int* __restrict__ rowptr,
-                           const int* __restrict__ colidx, const T* __restrict__ val, const int* __restrict__ trp,
-                           const int* __restrict__ tcol, const T* __restrict__ tval,
-                           const unsigned char* __restrict__ dbc, const T* __restrict__ p, T* __restrict__ Ap,
-                           double* __restrict__ part) {
-    Chunk c = chunks[blockIdx.x];
-    if (!S[c.inst].run) return;
-    double acc = 0;
-    for (int v = c.begin + threadIdx.x; v < c.end; v += blockDim.x) {
-        T y[3];
-        spmv_row<T, T, T>(v, rowptr, colidx, val, trp, tcol, tval, dbc, p, y);
-        Ap[3 * v] = y[0]; Ap[3 * v + 1] = y[1]; Ap[3 * v + 2] = y[2];
-        acc += (double)p[3 * v] * (double)y[0] + (double)p[3 * v + 1] * (double)y[1] + (double)p[3 * v + 2] * (double)y[2];
-    }
-    double s = cta_sum(acc);
-    if (threadIdx.x == 0) part[blockIdx.x] = s;
-}
-
-// x += alpha p, r -= alpha Ap, z = Dinv r, partials r.z and r.r
-template <class T>
-__global__ void k_pcg_update(const Chunk* __restrict__ chunks, const PcgS* __restrict__ S, const T* __restrict__ dinv,
-                             const unsigned char* __restrict__ dbc, T* __restrict__ x, T* __restrict__ r,
-                             T* __restrict__ z, const T* __restrict__ p, const T* __restrict__ Ap,
-                             double* __restrict__ part) {
-    Chunk c = chunks[blockIdx.x];
-    if (!S[c.inst].run) return;
-    T a = (T)S[c.inst].alpha;
-    double rz = 0, rr = 0;
-    for (int v = c.begin + threadIdx.x; v < c.end; v += blockDim.x) {
-        T rv[3];
-#pragma unroll
-        for (int d = 0; d < 3; ++d) {
-            x[3 * v + d] += a * p[3 * v + d];
-            rv[d] = r[3 * v + d] - a * Ap[3 * v + d];
-            r[3 * v + d] = rv[d];
-        }
-        const T* D = dinv + 9 * (long)v;
-        T zv[3];
-        if (dbc[v]) { zv[0] = rv[0]; zv[1] = rv[1]; zv[2] = rv[2]; }
-        else {
-            zv[0] = D[0] * rv[0] + D[1] * rv[1] + D[2] * rv[2];
-            zv[1] = D[3] * rv[0] + D[4] * rv[1] + D[5] * rv[2];
-            zv[2] = D[6] * rv[0] + D[7] * rv[1] + D[8] * rv[2];
-        }
-#pragma unroll
-        for (int d = 0; d < 3; ++d) {
-            z[3 * v + d] = zv[d];
-            rz += (double)rv[d] * (double)zv[d];
-            rr += (double)rv[d] * (double)rv[d];
-        }
-    }
-    double s1 = cta_sum(rz);
-    double s2 = cta_sum(rr);
-    if (threadIdx.x == 0) { part[2 * blockIdx.x] = s1; part[2 * blockIdx.x + 1] = s2; }
-}
-
-// init: x = 0, r = b, z = Dinv r, p = z ; partials r.z, r.r
-template <class T>
-__global__ void k_pcg_init(const Chunk* __restrict__ chunks, const unsigned char* __restrict__ active,
-                           const T* __restrict__ dinv, const unsigned char* __restrict__ dbc, const double* __restrict__ b,
-                           T* __restrict__ x, T* __restrict__ r, T* __restrict__ z, T* __restrict__ p,
-                           double* __restrict__ part) {
-    Chunk c = chunks[blockIdx.x];
-    if (!active[c.inst]) return;
-    double rz = 0, rr = 0;
-    for (int v = c.begin + threadIdx.x; v < c.end; v += blockDim.x) {
-        T rv[3];
-#pragma unroll
-        for (int d = 0; d < 3; ++d) {
-            rv[d] = dbc[v] ? T(0) : (T)b[3 * v + d];
-            x[3 * v + d] = T(0);
-            r[3 * v + d] = rv[d];
-        }
-        const T* D = dinv + 9 * (long)v;
-        T zv[3];
-        if (dbc[v]) { zv[0] = zv[1] = zv[2] = T(0); }
-        else {
-            zv[0] = D[0] * rv[0] + D[1] * rv[1] + D[2] * rv[2];
-            zv[1] = D[3] * rv[0] + D[4] * rv[1] + D[5] * rv[2];
-            zv[2] = D[6] * rv[0] + D[7] * rv[1] + D[8] * rv[2];
-        }
-#pragma unroll
-        for (int d = 0; d < 3; ++d) {
-            z[3 * v + d] = zv[d];
-            p[3 * v + d] = zv[d];
-            rz += (double)rv[d] * (double)zv[d];
-            rr += (double)rv[d] * (double)rv[d];
-        }
-    }
-    double s1 = cta_sum(rz);
-    double s2 = cta_sum(rr);
-    if (threadIdx.x == 0) { part[2 * blockIdx.x] = s1; part[2 * blockIdx.x + 1] = s2; }
-}
-
-template <class T>
-__global__ void k_pcg_pupdate(const Chunk* __restrict__ chunks, const PcgS* __restrict__ S, const T* __restrict__ z,
-                              T* __restrict__ p) {
-    Chunk c = chunks[blockIdx.x];
-    if (!S[c.inst].run) return;
-    T bt = (T)S[c.inst].beta;
-    for (int v = c.begin + threadIdx.x; v < c.end; v += blockDim.x)
-#pragma unroll
-        for (int d = 0; d < 3; ++d) p[3 * v + d] = z[3 * v + d] + bt * p[3 * v + d];
-}
-
-// per-instance scalar steps; partial sums reduced in chunk order
-__global__ void k_pcg_scal_init(int nI, const int* __restrict__ coff, const unsigned char* __restrict__ active,
-                                const double* __restrict__ part, double rel_tol, PcgS* __restrict__ S) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nI) return;
-    PcgS s;
-    double rz = 0, rr = 0;
-    for (int c = coff[i]; c < coff[i + 1]; ++c) { rz += part[2 * c]; rr += part[2 * c + 1]; }
-    s.rz = rz; s.rz_new = rz; s.rr = rr; s.bnorm2 = rr; s.tol2 = rel_tol * rel_tol * rr;
-    s.alpha = 0; s.beta = 0; s.pAp = 0; s.iters = 0;
-    s.run = active[i] && rr > 0 && rr > s.tol2;
-    S[i] = s;
-}
-
-__global__ void k_pcg_scal_alpha(int nI, const int* __restrict__ coff, const double* __restrict__ part,
-                                 PcgS* __restrict__ S) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nI || !S[i].run) return;
-    double pAp = 0;
-    for (int c = coff[i]; c < coff[i + 1]; ++c) pAp += part[c];
-    S[i].pAp = pAp;
-    if (!(pAp > 0)) {  // direction of non-positive curvature: stop here
-        S[i].run = 0;
-        S[i].alpha = 0;
-        return;
-    }
-    S[i].alpha = S[i].rz / pAp;
-}
-
-__global__ void k_pcg_scal_beta(int nI, const int* __restrict__ coff, const double* __restrict__ part, int max_iters,
-                                PcgS* __restrict__ S, int* __restrict__ any_running) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nI || !S[i].run) return;
-    double rz = 0, rr = 0;
-    for (int c = coff[i]; c < coff[i + 1]; ++c) { rz += part[2 * c]; rr += part[2 * c + 1]; }
-    PcgS s = S[i];
-    s.iters += 1;
-    s.rr = rr;
-    s.beta = rz / s.rz;
-    s.rz = rz;
-    if (rr <= s.tol2 || s.iters >= max_iters) s.run = 0;
-    if (s.run) atomicOr(any_running, 1);
-    S[i] = s;
-}
-
-// FP64 residual: res = b - A x64 (FP32/FP64 matrix, FP64 accumulation).
-// FP64 throughput is low on this part, so rows are spread over many small
-// CTAs; the squared norm is reduced afterwards per vertex chunk.
+// FP64 residual res = b - A x64: 8 lanes per block row (4 rows per warp),
+// FP64 accumulation of the stored (FP32 or FP64) operator against the FP64
+// solution; the squared norm is reduced afterwards per vertex chunk
 template <class T>
 __global__ void k_residual64(long V, const int* __restrict__ vinst, const unsigned char* __restrict__ active,
                              const int* __restrict__ rowptr, const int* __restrict__ colidx, const T* __restrict__ val,
                              const int* __restrict__ trp, const int* __restrict__ tcol, const T* __restrict__ tval,
                              const unsigned char* __restrict__ dbc, const double* __restrict__ b,
                              const double* __restrict__ x, double* __restrict__ res) {
-    long v = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= V || !active[vinst[v]]) return;
-    double y[3];
-    spmv_row<T, double, double>(v, rowptr, colidx, val, trp, tcol, tval, dbc, x, y);
-#pragma unroll
-    for (int d = 0; d < 3; ++d) res[3 * v + d] = dbc[v] ? 0.0 : b[3 * v + d] - y[d];
+    const int lane = threadIdx.x & 31, l8 = lane & 7;
+    const long v = (((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 4 + (lane >> 3);
+    const bool act = v < V && active[vinst[v]];
+    const bool fixed = act && dbc[v];
+    double a0 = 0, a1 = 0, a2 = 0;
+    if (act && !fixed) {
+        const int k1 = rowptr[v + 1];
+        for (int k = rowptr[v] + l8; k < k1; k += 8) {
+            const int c = colidx[k];
+            const T* m = val + 9L * k;
+            const double x0 = x[3 * c], x1 = x[3 * c + 1], x2 = x[3 * c + 2];
+            a0 += (double)m[0] * x0 + (double)m[1] * x1 + (double)m[2] * x2;
+            a1 += (double)m[3] * x0 + (double)m[4] * x1 + (double)m[5] * x2;
+            a2 += (double)m[6] * x0 + (double)m[7] * x1 + (double)m[8] * x2;
+        }
+        const int t1 = trp[v + 1];
+        for (int k = trp[v] + l8; k < t1; k += 8) {
+            const int c = tcol[k];
+            if (dbc[c]) continue;
+            const T* m = tval + 9L * k;
+            const double x0 = x[3 * c], x1 = x[3 * c + 1], x2 = x[3 * c + 2];
+            a0 += (double)m[0] * x0 + (double)m[1] * x1 + (double)m[2] * x2;
+            a1 += (double)m[3] * x0 + (double)m[4] * x1 + (double)m[5] * x2;
+            a2 += (double)m[6] * x0 + (double)m[7] * x1 + (double)m[8] * x2;
+        }
+    }
+    for (int o = 4; o > 0; o >>= 1) {
+        a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+        a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+        a2 += __shfl_xor_sync(0xffffffffu, a2, o);
+    }
+    if (act && l8 < 3) {
+        const double y = l8 == 0 ? a0 : (l8 == 1 ? a1 : a2);
+        res[3 * v + l8] = fixed ? 0.0 : b[3 * v + l8] - y;
+    }
 }
 
 __global__ void k_norm2_chunks(const Chunk* __restrict__ chunks, const unsigned char* __restrict__ active,
@@ -388,13 +257,16 @@ __global__ void k_inertia_energy(const Chunk* __restrict__ chunks, const unsigne
     if (threadIdx.x == 0) part[blockIdx.x] = s;
 }
 
+// per instance: its chunk partials summed by one warp (lane-strided, then a
+// butterfly; fixed order)
 __global__ void k_chunk_reduce(int nI, const int* __restrict__ coff, const double* __restrict__ part,
                                double* __restrict__ out, int accumulate) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nI) return;
+    const int i = (int)(((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    if (i >= nI) return;  // whole warp
     double s = 0;
-    for (int c = coff[i]; c < coff[i + 1]; ++c) s += part[c];
-    out[i] = accumulate ? out[i] + s : s;
+    for (int c = coff[i] + lane; c < coff[i + 1]; c += 32) s += part[c];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) out[i] = accumulate ? out[i] + s : s;
 }
 
 __global__ void k_axpy_trial(long V, const int* __restrict__ vinst, const unsigned char* __restrict__ active,
@@ -1201,7 +1073,7 @@ __global__ void __launch_bounds__(GP_THREADS) k_pcg_grid(
 
 // ---------------------------------------------------------------- host side
 int chunk_reduce_off(Arena& A, const int* coff, const double* part, double* out, bool accumulate, cudaStream_t s) {
-    (::idp::count_launch(), k_chunk_reduce<<<grid_for(A.nI), kBlock, 0, s>>>(A.nI, coff, part, out, accumulate ? 1 : 0));
+    (::idp::count_launch(), k_chunk_reduce<<<grid_for(32L * A.nI), kBlock, 0, s>>>(A.nI, coff, part, out, accumulate ? 1 : 0));
     return cudaGetLastError() == cudaSuccess ? IDP_OK : IDP_ERR_CUDA;
 }
 
@@ -1280,23 +1152,17 @@ static int pcg_inner(Arena& A, Work& W, const double* b, double rel_tol, int max
                      T** xout, cudaStream_t s) {
     const int nI = A.nI;
     long n3 = 3 * A.V;
-    if (W[W_PCG_VEC].ensure(sizeof(T) * 10 * (n3 + 4)) || W[W_PCG_SCAL].ensure(sizeof(PcgS) * nI + 64) ||
-        W[W_CHUNK_SUM].ensure(sizeof(double) * 2 * (A.n_vert_chunks + 2)))
-        return IDP_ERR_CUDA;
+    if (W[W_PCG_VEC].ensure(sizeof(T) * 10 * (n3 + 4))) return IDP_ERR_CUDA;
     T* base = W[W_PCG_VEC].as<T>();
     T *x = base, *r = base + n3 + 4, *z = r + n3 + 4, *p = z + n3 + 4, *Ap = p + n3 + 4;
     T *pu = Ap + n3 + 4, *pw = pu + n3 + 4, *psv = pw + n3 + 4, *pm0 = psv + n3 + 4, *pm1 = pm0 + n3 + 4;
-    PcgS* S = W[W_PCG_SCAL].as<PcgS>();
-    int* any = reinterpret_cast<int*>(S + nI);
-    double* part = W[W_CHUNK_SUM].as<double>();
     const T* val = W[W_BSR_VAL].as<T>();
     const T* dinv = W[W_DIAG_INV].as<T>();
     const int* trp = W[W_TAIL_ROWPTR].as<int>();
     const int* tcol = W[W_TAIL_COL].as<int>();
     const T* tval = W[W_TAIL_VAL].as<T>();
-    const int nc = A.n_vert_chunks;
-    // instances up to kClusterPcgMaxV vertices: one thread-block cluster each,
-    // grouped by cluster size (one launch per size)
+    // instances up to W.grid_min_v vertices: one thread-block cluster each,
+    // grouped by cluster size (one launch per size); larger ones: grid PCG
     std::vector<unsigned char> act(nI), small(nI, 0), large(nI, 0);
     IDP_CUDA_TRY(cudaMemcpyAsync(act.data(), A.active, nI, cudaMemcpyDeviceToHost, s));
     IDP_CUDA_TRY(cudaStreamSynchronize(s));
@@ -1523,11 +1389,11 @@ int pcg_solve(Arena& A, Work& W, const ContactSet& cs, bool fp64, const double* 
     // |b|^2 per instance (x = 0 gives res = b)
     auto residual = [&](std::vector<double>& out) -> int {
         if (fp64)
-            (::idp::count_launch(), k_residual64<double><<<grid_for(A.V, 64), 64, 0, s>>>(A.V, A.vinst, A.active, A.rowptr, A.colidx,
+            (::idp::count_launch(), k_residual64<double><<<grid_for(8 * A.V, kBlock), kBlock, 0, s>>>(A.V, A.vinst, A.active, A.rowptr, A.colidx,
                                                                     W[W_BSR_VAL].as<double>(), trp, tcol,
                                                                     W[W_TAIL_VAL].as<double>(), A.dbc, rhs, sol, res));
         else
-            (::idp::count_launch(), k_residual64<float><<<grid_for(A.V, 64), 64, 0, s>>>(A.V, A.vinst, A.active, A.rowptr, A.colidx,
+            (::idp::count_launch(), k_residual64<float><<<grid_for(8 * A.V, kBlock), kBlock, 0, s>>>(A.V, A.vinst, A.active, A.rowptr, A.colidx,
                                                                    W[W_BSR_VAL].as<float>(), trp, tcol,
                                                                    W[W_TAIL_VAL].as<float>(), A.dbc, rhs, sol, res));
         (::idp::count_launch(), k_norm2_chunks<<<A.n_vert_chunks, kBlock, 0, s>>>(A.vert_chunks, A.active, res, part));

@@ -98,6 +98,30 @@ def test_constraint_set_empty_and_dbc(oracle, gpu_lib):
     ctx.close()
 
 
+def test_repeated_builds_match_oracle(oracle, gpu_lib):
+    """Later constraint-set and CCD builds of a context reuse the table
+    capacities of the first one without a host round trip; they must give the
+    same results as a fresh build."""
+    import idp_gb300 as idp
+
+    X0, tets, Xd = cases.folded_bar(seed=1, n=(2, 2, 8), frac=0.97, radius=1.0)
+    pr = cases.problem(X0, tets, dHat=0.05)
+    ctx = ctx_for(idp, X0, tets, pr, idp.MODE_MIXED)
+    surf = oracle.surface(X0, tets)
+    z = np.zeros(X0.shape[0], np.uint8)
+    rng = np.random.default_rng(9)
+    for k, frac in enumerate((0.0, 0.5, 1.0, 0.8, 1.0)):
+        X = X0 + frac * (Xd - X0)
+        g = ctx.constraint_set(0, X)
+        o, _ = oracle.constraint_set(X, X0, surf, z, pr["dHat2"])
+        assert sort_rows(g) == sort_rows(o), k
+        d = 0.05 * rng.normal(size=X.shape)
+        ag, _ = ctx.ccd_stepsize(0, X, d.reshape(-1), 1.0)
+        ao, rc = oracle.ccd_stepsize(X, d.reshape(-1), surf, z, 1.0)
+        assert ag == ao, (k, ag, ao)
+    ctx.close()
+
+
 @pytest.mark.parametrize("seed", [0, 1, 2, 3])
 def test_ccd_stepsize_bitexact(oracle, gpu_lib, seed):
     import idp_gb300 as idp
