@@ -58,7 +58,8 @@ class Result(C.Structure):
 class Stats(C.Structure):
     _fields_ = [("pcg_ms", C.c_double), ("pcg_bytes", C.c_double), ("pcg_iters", C.c_longlong),
                 ("pcg_launches", C.c_int), ("tet_ms", C.c_double), ("contact_ms", C.c_double), ("ccd_ms", C.c_double),
-                ("total_ms", C.c_double), ("kernel_launches", C.c_longlong)]
+                ("total_ms", C.c_double), ("kernel_launches", C.c_longlong), ("barrier_ms", C.c_double),
+                ("assembly_ms", C.c_double), ("fp64_fallbacks", C.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -243,9 +243,9 @@ int eval_gradient(idp_ctx* c, const double* X) {
     return vec_zero_dbc(A, A.g, c->s);
 }
 
-int eval_hessian(idp_ctx* c, const double* X) {
+int eval_hessian(idp_ctx* c, const double* X, bool force_fp64 = false) {
     Arena& A = c->A;
-    bool fp64 = c->P.mode == IDP_MODE_FP64;
+    bool fp64 = force_fp64 || c->P.mode == IDP_MODE_FP64;
     c->W.timer.start(PhaseTimer::TET, c->s);
     int rc = tet_hessian(A, c->W, X, c->P.h * c->P.h, fp64, c->s);
     c->W.timer.stop(c->s);
@@ -761,6 +761,30 @@ int idp_advance(idp_ctx* c, idp_result* results) {
                 return rc;
             for (int i = 0; i < nI; ++i)
                 if (newton[i]) st[i].pcg_iters += its[i];
+            if (!fp64) {
+                // FP64 fallback: instances whose refined mixed direction still
+                // misses its tolerance by 10x (stiff contact the FP32 operator
+                // cannot resolve) are re-solved with an FP64 Hessian
+                std::vector<unsigned char> fb(nI, 0);
+                bool any_fb = false;
+                for (int i = 0; i < nI; ++i)
+                    if (newton[i] && rel[i] > std::max(1e-2, 10.0 * tol[i])) {
+                        fb[i] = 1;
+                        any_fb = true;
+                    }
+                if (any_fb) {
+                    if ((rc = set_mask(c, fb))) return rc;
+                    if ((rc = eval_hessian(c, A.X, true))) return rc;
+                    if ((rc = pcg_solve(A, W, c->cs, true, A.g, A.dir, c->P.pcg_rel_tol, c->P.pcg_max_iters, its, rel, s,
+                                         tol.data())))
+                        return rc;
+                    for (int i = 0; i < nI; ++i)
+                        if (fb[i]) {
+                            st[i].pcg_iters += its[i];
+                            W.stats.fp64_fallbacks += 1;
+                        }
+                }
+            }
         }
         if (any_gd) {  // gradient descent direction (IMPLICIT_EULER.h:507-510)
             if ((rc = set_mask(c, gd))) return rc;
@@ -940,9 +964,9 @@ int idp_advance(idp_ctx* c, idp_result* results) {
                 std::fprintf(stderr, "idp phase %-10s device %10.3f ms  host %10.3f ms\n", nm[k], ms[k], hms[k]);
             std::fprintf(stderr,
                          "idp accd pairs %lld, iterations %lld, longest %lld, pairs over 1000 iterations %lld; "
-                         "contact blocks %d (max %d vertices); pcg iterations %lld\n",
+                         "contact blocks %d (max %d vertices); pcg iterations %lld; fp64 fallbacks %d\n",
                          W.accd_pairs, W.accd_total, W.accd_maxit, W.accd_long, W.cl.n, W.cl.max_n,
-                         (long long)W.stats.pcg_iters);
+                         (long long)W.stats.pcg_iters, W.stats.fp64_fallbacks);
             W.accd_maxit = W.accd_long = W.accd_total = W.accd_pairs = 0;
             if (W.grid_prof[4]) {
                 const double n = (double)W.grid_prof[4];
@@ -952,6 +976,8 @@ int idp_advance(idp_ctx* c, idp_result* results) {
                 for (auto& v : W.grid_prof) v = 0;
             }
         }
+        W.stats.barrier_ms = ms[PhaseTimer::BARRIER];
+        W.stats.assembly_ms = ms[PhaseTimer::ASSEMBLY];
         W.stats.pcg_ms = ms[PhaseTimer::PCG];
         W.stats.tet_ms = ms[PhaseTimer::TET];
         W.stats.contact_ms = ms[PhaseTimer::CONTACT];

@@ -203,6 +203,15 @@ __global__ void k_norm2_chunks(const Chunk* __restrict__ chunks, const unsigned 
     if (threadIdx.x == 0) part[blockIdx.x] = s;
 }
 
+__global__ void k_zero_masked(long V, const int* __restrict__ vinst, const unsigned char* __restrict__ active,
+                              double* __restrict__ x) {
+    long v = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= V || !active[vinst[v]]) return;
+    x[3 * v] = 0.0;
+    x[3 * v + 1] = 0.0;
+    x[3 * v + 2] = 0.0;
+}
+
 template <class T>
 __global__ void k_add_correction(long V, const int* __restrict__ vinst, const unsigned char* __restrict__ active,
                                  const T* __restrict__ e, double* __restrict__ x) {
@@ -1382,7 +1391,9 @@ int pcg_solve(Arena& A, Work& W, const ContactSet& cs, bool fp64, const double* 
     double* part = W[W_MISC].as<double>();
     const int* trp = W[W_TAIL_ROWPTR].as<int>();
     const int* tcol = W[W_TAIL_COL].as<int>();
-    IDP_CUDA_TRY(cudaMemsetAsync(sol, 0, sizeof(double) * n3, s));
+    // only the active instances' solutions are reset: a later solve of some
+    // instances (FP64 fallback) must not disturb the others' directions
+    (::idp::count_launch(), k_zero_masked<<<grid_for(A.V), kBlock, 0, s>>>(A.V, A.vinst, A.active, sol));
     std::vector<double> b2(nI, 0.0), hrr(nI);
     std::vector<unsigned char> act(nI), act0(nI);
     IDP_CUDA_TRY(cudaMemcpyAsync(act0.data(), A.active, nI, cudaMemcpyDeviceToHost, s));
@@ -1406,8 +1417,10 @@ int pcg_solve(Arena& A, Work& W, const ContactSet& cs, bool fp64, const double* 
     if (rc) return rc;
     const int max_refine = fp64 ? 1 : 8;
     const double inner_tol = fp64 ? rel_tol : std::max(rel_tol, 2e-3);
+    std::vector<double> prev(nI, 0.0);
     for (int ref = 0; ref < max_refine; ++ref) {
-        // instances whose FP64 residual is already small stop refining
+        // instances whose FP64 residual is already small, or that stopped
+        // improving (the FP32 operator cannot resolve them), stop refining
         bool any = false;
         if (ref > 0) {
             rc = residual(hrr);
@@ -1417,8 +1430,10 @@ int pcg_solve(Arena& A, Work& W, const ContactSet& cs, bool fp64, const double* 
         }
         for (int i = 0; i < nI; ++i) {
             const double ti = tol_host ? std::max(rel_tol, tol_host[i]) : rel_tol;
-            act[i] = act0[i] && b2[i] > 0 && hrr[i] > ti * ti * b2[i];
+            const bool stalled = ref > 0 && act[i] && hrr[i] > 0.25 * prev[i];
+            act[i] = act0[i] && b2[i] > 0 && hrr[i] > ti * ti * b2[i] && (ref == 0 || act[i]) && !stalled;
             relres_out[i] = b2[i] > 0 ? std::sqrt(hrr[i] / b2[i]) : 0.0;
+            prev[i] = hrr[i];
             any |= act[i] != 0;
         }
         if (!any) break;

@@ -84,6 +84,9 @@ typedef struct idp_stats {
     double ccd_ms;          /* CCD step-size evaluations                          */
     double total_ms;        /* the whole idp_advance                              */
     long long kernel_launches; /* kernels this library launched in idp_advance    */
+    double barrier_ms;      /* barrier gradient / Hessian kernels                 */
+    double assembly_ms;     /* BSR assembly and contact-block factorisation       */
+    int fp64_fallbacks;     /* mixed-mode directions re-solved in FP64            */
 } idp_stats;
 
 /* Defaults: h=0.1, newton_tol=1e-3, max_newton=2000, mode=MIXED,
