@@ -604,6 +604,7 @@ __global__ void __launch_bounds__(CL_THREADS) k_pcg_cluster(
 // q = w + beta q with q = A p kept by recurrence). Vectors written inside
 // the kernel are read through L2 (ld.cg) so no CTA sees a stale L1 line.
 constexpr int GP_THREADS = 256;
+constexpr int kRL = 4;  // lanes per block row in the grid PCG's SpMV (8 rows per warp step)
 constexpr unsigned int kSpinLimit = 1u << 22;  // ~1 s of polling, then error
 constexpr int kCtlWords = 64;                   // per instance: counter at [0], release word at [32]
 constexpr int kGridSmem = 69 * 1024;            // dynamic shared memory per CTA (three CTAs per SM)
@@ -708,7 +709,7 @@ __device__ __forceinline__ void grid_precond(const T* D, bool fixed, const T rv[
 }
 
 template <class T>
-__global__ void __launch_bounds__(GP_THREADS) k_pcg_grid(
+__global__ void __launch_bounds__(GP_THREADS, 3) k_pcg_grid(
     const GridCta* __restrict__ plan, int cap_blocks, int nvmax, const int* __restrict__ rowptr,
     const int* __restrict__ colidx, const T* __restrict__ val, const int* __restrict__ trp,
     const int* __restrict__ tcol, const T* __restrict__ tval, const unsigned char* __restrict__ dbc,
@@ -728,7 +729,8 @@ __global__ void __launch_bounds__(GP_THREADS) k_pcg_grid(
     T* red = redbuf + (long)kRed * me.slot;
     unsigned int round = 0;
     const bool has_blocks = pc.ioff[inst + 1] > pc.ioff[inst];
-    const int lane = threadIdx.x & 31, l8 = lane & 7, warp = threadIdx.x >> 5, nw = GP_THREADS / 32;
+    const int lane = threadIdx.x & 31, l8 = lane & (kRL - 1), warp = threadIdx.x >> 5, nw = GP_THREADS / 32;
+    constexpr int kRows = 32 / kRL;  // rows per warp step
     // ---- stage the CTA's rows in shared memory
     GridRows<T> S;
     S.row = reinterpret_cast<int*>(smem_raw);
@@ -760,7 +762,8 @@ __global__ void __launch_bounds__(GP_THREADS) k_pcg_grid(
         const int v = v0 + lv;
         const int ka = S.row[lv], kz = S.row[lv + 1];
         if (kz <= S.ncache) {
-            for (int k = ka + l8; k < kz; k += 8) {
+#pragma unroll 4
+            for (int k = ka + l8; k < kz; k += kRL) {
                 const int c = S.col[k];
                 const T* mm = S.val + 9 * k;
                 const T x0 = __ldcg(vin + 3 * c), x1 = __ldcg(vin + 3 * c + 1), x2 = __ldcg(vin + 3 * c + 2);
@@ -769,7 +772,7 @@ __global__ void __launch_bounds__(GP_THREADS) k_pcg_grid(
                 a2 += mm[6] * x0 + mm[7] * x1 + mm[8] * x2;
             }
         } else {
-            for (int k = ka + l8; k < kz; k += 8) {
+            for (int k = ka + l8; k < kz; k += kRL) {
                 const int c = colidx[kb0 + k];
                 const T* mm = val + 9L * (kb0 + k);
                 const T x0 = __ldcg(vin + 3 * c), x1 = __ldcg(vin + 3 * c + 1), x2 = __ldcg(vin + 3 * c + 2);
@@ -779,7 +782,7 @@ __global__ void __launch_bounds__(GP_THREADS) k_pcg_grid(
             }
         }
         const int t1e = trp[v + 1];
-        for (int k = trp[v] + l8; k < t1e; k += 8) {
+        for (int k = trp[v] + l8; k < t1e; k += kRL) {
             const int c = tcol[k];
             if (dbc[c]) continue;
             const T* mm = tval + 9L * k;
@@ -790,7 +793,7 @@ __global__ void __launch_bounds__(GP_THREADS) k_pcg_grid(
         }
     };
     auto group_sum3 = [&](T& a0, T& a1, T& a2) {
-        for (int o = 4; o > 0; o >>= 1) {
+        for (int o = kRL / 2; o > 0; o >>= 1) {
             a0 += __shfl_xor_sync(0xffffffffu, a0, o);
             a1 += __shfl_xor_sync(0xffffffffu, a1, o);
             a2 += __shfl_xor_sync(0xffffffffu, a2, o);
@@ -821,8 +824,8 @@ __global__ void __launch_bounds__(GP_THREADS) k_pcg_grid(
         if (!barrier()) return;
         // w = A u, m = M w; partials gamma = r.u, delta = w.u, rho = r.r
         T gam_l = 0, del_l = 0, rho_l = 0;
-        for (int base = 4 * warp; base < nv; base += 4 * nw) {
-            const int lv = base + (lane >> 3);
+        for (int base = kRows * warp; base < nv; base += kRows * nw) {
+            const int lv = base + lane / kRL;
             const bool act = lv < nv;
             const int v = v0 + (act ? lv : 0);
             const bool fixed = act && dbc[v];
@@ -839,7 +842,7 @@ __global__ void __launch_bounds__(GP_THREADS) k_pcg_grid(
                 del_l += wn * uo;
                 rho_l += ro * ro;
             }
-            const int gb = lane & ~7;
+            const int gb = lane & ~(kRL - 1);
             const T w0 = __shfl_sync(0xffffffffu, wn, gb), w1 = __shfl_sync(0xffffffffu, wn, gb + 1),
                     w2 = __shfl_sync(0xffffffffu, wn, gb + 2);
             if (act && l8 < 3) {
@@ -873,8 +876,8 @@ __global__ void __launch_bounds__(GP_THREADS) k_pcg_grid(
                 }
                 if (!(alpha > T(0)) || !(alpha < T(INFINITY))) break;  // breakdown: keep the current x
                 gam_l = del_l = rho_l = 0;
-                for (int base = 4 * warp; base < nv; base += 4 * nw) {
-                    const int lv = base + (lane >> 3);
+                for (int base = kRows * warp; base < nv; base += kRows * nw) {
+                    const int lv = base + lane / kRL;
                     const bool act = lv < nv;
                     const int v = v0 + (act ? lv : 0);
                     const bool fixed = act && dbc[v];
@@ -901,7 +904,7 @@ __global__ void __launch_bounds__(GP_THREADS) k_pcg_grid(
                         del_l += wn * un;
                         rho_l += rn * rn;
                     }
-                    const int gb = lane & ~7;
+                    const int gb = lane & ~(kRL - 1);
                     const T w0 = __shfl_sync(0xffffffffu, wn, gb), w1 = __shfl_sync(0xffffffffu, wn, gb + 1),
                             w2 = __shfl_sync(0xffffffffu, wn, gb + 2);
                     if (act && l8 < 3) {
@@ -971,8 +974,8 @@ __global__ void __launch_bounds__(GP_THREADS) k_pcg_grid(
             // lane d < 3 of each row then forms p = z + beta p, q = w + beta q
             // for component d
             T pq_l = 0;
-            for (int base = 4 * warp; base < nv; base += 4 * nw) {
-                const int lv = base + (lane >> 3);
+            for (int base = kRows * warp; base < nv; base += kRows * nw) {
+                const int lv = base + lane / kRL;
                 const bool act = lv < nv;
                 const int v = v0 + (act ? lv : 0);
                 const bool fixed = act && dbc[v];
@@ -986,7 +989,7 @@ __global__ void __launch_bounds__(GP_THREADS) k_pcg_grid(
                 if (act && !fixed) {
                     const int ka = S.row[lv], kz = S.row[lv + 1];
                     if (kz <= S.ncache) {
-                        for (int k = ka + l8; k < kz; k += 8) {
+                        for (int k = ka + l8; k < kz; k += kRL) {
                             const int c = S.col[k];
                             const T* m = S.val + 9 * k;
                             const T x0 = __ldcg(z + 3 * c), x1 = __ldcg(z + 3 * c + 1), x2 = __ldcg(z + 3 * c + 2);
@@ -995,7 +998,7 @@ __global__ void __launch_bounds__(GP_THREADS) k_pcg_grid(
                             a2 += m[6] * x0 + m[7] * x1 + m[8] * x2;
                         }
                     } else {
-                        for (int k = ka + l8; k < kz; k += 8) {
+                        for (int k = ka + l8; k < kz; k += kRL) {
                             const int c = colidx[kb0 + k];
                             const T* m = val + 9L * (kb0 + k);
                             const T x0 = __ldcg(z + 3 * c), x1 = __ldcg(z + 3 * c + 1), x2 = __ldcg(z + 3 * c + 2);
@@ -1005,7 +1008,7 @@ __global__ void __launch_bounds__(GP_THREADS) k_pcg_grid(
                         }
                     }
                     const int t1e = trp[v + 1];
-                    for (int k = trp[v] + l8; k < t1e; k += 8) {
+                    for (int k = trp[v] + l8; k < t1e; k += kRL) {
                         const int c = tcol[k];
                         if (dbc[c]) continue;
                         const T* m = tval + 9L * k;
@@ -1015,7 +1018,7 @@ __global__ void __launch_bounds__(GP_THREADS) k_pcg_grid(
                         a2 += m[6] * x0 + m[7] * x1 + m[8] * x2;
                     }
                 }
-                for (int o = 4; o > 0; o >>= 1) {
+                for (int o = kRL / 2; o > 0; o >>= 1) {
                     a0 += __shfl_xor_sync(0xffffffffu, a0, o);
                     a1 += __shfl_xor_sync(0xffffffffu, a1, o);
                     a2 += __shfl_xor_sync(0xffffffffu, a2, o);
