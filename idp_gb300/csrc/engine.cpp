@@ -185,6 +185,27 @@ int fetch(idp_ctx* c, const T* d, std::vector<T>& h) {
     return IDP_OK;
 }
 
+// every per-instance scalar (energies, norms, flags) in one copy and one
+// synchronisation
+struct InstScalars {
+    std::vector<double> buf;
+    int nI = 0;
+    double d(int k, int i) const { return buf[(size_t)k * nI + i]; }
+    int flag(int k, int i) const {
+        return reinterpret_cast<const int*>(buf.data() + (size_t)S_NUMD * nI)[(size_t)k * nI + i];
+    }
+};
+
+int fetch_scalars(idp_ctx* c, InstScalars& out) {
+    const int nI = c->A.nI;
+    out.nI = nI;
+    out.buf.resize((size_t)(S_NUMD + S_NUMI) * nI);
+    IDP_CUDA_TRY(cudaMemcpyAsync(out.buf.data(), c->inst_buf.p, sizeof(double) * S_NUMD * nI + sizeof(int) * S_NUMI * nI,
+                                 cudaMemcpyDeviceToHost, c->s));
+    IDP_CUDA_TRY(cudaStreamSynchronize(c->s));
+    return IDP_OK;
+}
+
 // incremental potential of the masked instances at X (INC_POTENTIAL.h:15-152):
 // E = h^2 sum vol*Psi + inertia [+ barrier over a freshly built constraint
 // set]. bad[i] = 1 when a tet is inverted, 2 when a constraint distance is
@@ -820,8 +841,10 @@ int idp_advance(idp_ctx* c, idp_result* results) {
         rc = ccd_stepsize(A, W, A.Xprev, A.dir, A.alpha, isc(c, SI_CCDF), s);
         W.timer.stop(s);
         if (rc) return rc;
-        if ((rc = fetch(c, A.alpha, alpha))) return rc;
-        if ((rc = fetch(c, isc(c, SI_CCDF), hi))) return rc;
+        hi.resize(nI);
+        IDP_CUDA_TRY(cudaMemcpyAsync(alpha.data(), A.alpha, sizeof(double) * nI, cudaMemcpyDeviceToHost, s));
+        IDP_CUDA_TRY(cudaMemcpyAsync(hi.data(), isc(c, SI_CCDF), sizeof(int) * nI, cudaMemcpyDeviceToHost, s));
+        IDP_CUDA_TRY(cudaStreamSynchronize(s));
         std::vector<double> feasible = alpha;
         for (int i = 0; i < nI; ++i) {
             if (!mask[i]) continue;
@@ -840,44 +863,44 @@ int idp_advance(idp_ctx* c, idp_result* results) {
             if ((rc = set_mask(c, srch))) return rc;
             IDP_CUDA_TRY(cudaMemcpyAsync(A.alpha, alpha.data(), sizeof(double) * nI, cudaMemcpyHostToDevice, s));
             if ((rc = vec_axpy_trial(A, A.Xprev, A.dir, A.X, s))) return rc;
-            // validity (det F > 0) on the searching instances
-            IDP_CUDA_TRY(cudaMemsetAsync(isc(c, SI_BAD), 0, sizeof(int) * nI, s));
+            // one pass over every searching instance: validity (det F > 0)
+            // and elastic energy, inertia, constraint set, minimum distance
+            // and barrier energy; one readback decides. An instance that
+            // turns out inverted, or fails the distance safeguard, ignores
+            // the values computed past that point.
+            IDP_CUDA_TRY(cudaMemsetAsync(isc(c, SI_BAD), 0, sizeof(int) * nI * 2, s));
+            IDP_CUDA_TRY(cudaMemsetAsync(dsc(c, S_EBAR), 0, sizeof(double) * nI, s));
+            W.timer.start(PhaseTimer::TET, s);
             if ((rc = tet_energy(A, W, A.X, h * h, dsc(c, S_ETET), isc(c, SI_BAD), s))) return rc;
-            if ((rc = fetch(c, isc(c, SI_BAD), hi))) return rc;
-            std::vector<unsigned char> valid(nI, 0);
-            for (int i = 0; i < nI; ++i) valid[i] = srch[i] && !hi[i];
+            W.timer.stop(s);
+            if ((rc = vec_inertia(A, W, A.X, dsc(c, S_EINERT), nullptr, s))) return rc;
             for (int i = 0; i < nI; ++i) st[i].ls_trials += srch[i];
-            // constraint set + min-distance safeguard on the valid ones
-            if ((rc = set_mask(c, valid))) return rc;
             if ((rc = build_cs(A.X))) return rc;
             last_trial = trial;
-            std::vector<double> md(nI, 1e300);
-            IDP_CUDA_TRY(cudaMemcpyAsync(dsc(c, S_MIND), md.data(), sizeof(double) * nI, cudaMemcpyHostToDevice, s));
+            if ((rc = vec_fill(dsc(c, S_MIND), nI, 1e300, s))) return rc;
             if ((rc = constraint_min_dist2(A, W, A.X, W[W_CONS].as<int4>(), W[W_CONS_INST].as<int>(), c->cs.C, nullptr,
                                            dsc(c, S_MIND), s)))
                 return rc;
-            if ((rc = fetch(c, dsc(c, S_MIND), md))) return rc;
-            std::vector<unsigned char> evalm(nI, 0);
+            if ((rc = barrier_energy(A, W, A.X, c->cs, dsc(c, S_EBAR), isc(c, SI_BADB), s))) return rc;
+            InstScalars sc;
+            if ((rc = fetch_scalars(c, sc))) return rc;
+            const double t2 = c->P.thickness * c->P.thickness;
             for (int i = 0; i < nI; ++i) {
-                if (!valid[i]) continue;
-                double t2 = c->P.thickness * c->P.thickness;
-                if (c->cs.off[i + 1] > c->cs.off[i] && md[i] - t2 <= 0) {
+                if (!srch[i]) continue;
+                if (sc.flag(SI_BAD, i)) {  // inverted: halve (IMPLICIT_EULER.h:106-113)
+                    alpha[i] /= 2.0;
+                    continue;
+                }
+                if (c->cs.off[i + 1] > c->cs.off[i] && sc.d(S_MIND, i) - t2 <= 0) {
                     alpha[i] /= 2;  // safe guard backtrack (IMPLICIT_EULER.h:120-129)
                     continue;
                 }
-                evalm[i] = 1;
-            }
-            if ((rc = set_mask(c, evalm))) return rc;
-            if ((rc = eval_energy(c, A.X, true, E, bad))) return rc;
-            for (int i = 0; i < nI; ++i) {
-                if (!srch[i]) continue;
-                if (!valid[i]) { alpha[i] /= 2.0; continue; }
-                if (!evalm[i]) continue;
-                bool ok = bad[i] == 0 && !(E[i] > st[i].Eprev);
+                const double Ei = sc.d(S_ETET, i) + sc.d(S_EINERT, i) + sc.d(S_EBAR, i);
+                bool ok = sc.flag(SI_BADB, i) == 0 && !(Ei > st[i].Eprev);
                 alpha[i] /= 2.0;
                 if (ok) {
                     srch[i] = 0;
-                    Eacc[i] = E[i];
+                    Eacc[i] = Ei;
                     acc_trial[i] = trial;
                 }
             }
@@ -899,17 +922,21 @@ int idp_advance(idp_ctx* c, idp_result* results) {
                 st[i].min_alpha = std::min(st[i].min_alpha, alpha[i] * 2);
                 st[i].feasible_alpha = feasible[i];
             }
-        // ---- kappa adaptation (IMPLICIT_EULER.h:566-595)
-        if (have_prev && c->prevC > 0) {
-            IDP_CUDA_TRY(cudaMemsetAsync(isc(c, SI_KFLAG), 0, sizeof(int) * nI, s));
+        // ---- kappa adaptation (IMPLICIT_EULER.h:566-595) and the direction
+        // norm of the stopping test, read back together
+        IDP_CUDA_TRY(cudaMemsetAsync(isc(c, SI_KFLAG), 0, sizeof(int) * nI, s));
+        if (have_prev && c->prevC > 0)
             if ((rc = kappa_check(A, W, A.X, W[W_PREV_CONS].as<int4>(), W[W_PREV_INST].as<int>(),
                                   W[W_PREV_DIST2].as<double>(), c->prevC, isc(c, SI_KFLAG), s)))
                 return rc;
-            if ((rc = fetch(c, isc(c, SI_KFLAG), hi))) return rc;
+        if ((rc = vec_dir_norm2(A, W, A.dir, dsc(c, S_NORM2), s))) return rc;
+        InstScalars ksc;
+        if ((rc = fetch_scalars(c, ksc))) return rc;
+        if (have_prev && c->prevC > 0) {
             std::vector<unsigned char> km(nI, 0);
             bool anyk = false;
             for (int i = 0; i < nI; ++i)
-                if (mask[i] && hi[i] && st[i].kappa < st[i].kappa_max) {
+                if (mask[i] && ksc.flag(SI_KFLAG, i) && st[i].kappa < st[i].kappa_max) {
                     st[i].kappa *= 2;
                     km[i] = 1;
                     anyk = true;
@@ -927,12 +954,10 @@ int idp_advance(idp_ctx* c, idp_result* results) {
         if ((rc = save_prev_set(c, A.X))) return rc;
         have_prev = true;
         // ---- stopping criterion (IMPLICIT_EULER.h:647-676, 759, 855)
-        if ((rc = vec_dir_norm2(A, W, A.dir, dsc(c, S_NORM2), s))) return rc;
-        if ((rc = fetch(c, dsc(c, S_NORM2), hv))) return rc;
         for (int i = 0; i < nI; ++i) {
             if (!mask[i]) continue;
             InstState& S = st[i];
-            double L2 = std::sqrt(hv[i] / (nvert[i] - nDBC[i])) / h;
+            double L2 = std::sqrt(ksc.d(S_NORM2, i) / (nvert[i] - nDBC[i])) / h;
             S.iters += 1;
             S.last_res = L2;
             if (S.nres < 3) S.res[S.nres++] = L2;

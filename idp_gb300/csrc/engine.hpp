@@ -232,12 +232,27 @@ struct Work {
             hpin = nullptr;
         return hpin;
     }
+    double* hpin_d = nullptr;               // pinned host doubles (per-instance readbacks)
+    long hpin_d_n = 0;
+    double* pinned_doubles(long n) {
+        if (n > hpin_d_n) {
+            if (hpin_d) cudaFreeHost(hpin_d);
+            hpin_d = nullptr;
+            hpin_d_n = 0;
+            if (cudaMallocHost(reinterpret_cast<void**>(&hpin_d), sizeof(double) * (n + 8)) != cudaSuccess) return nullptr;
+            hpin_d_n = n;
+        }
+        return hpin_d;
+    }
     DBuf& operator[](int i) { return b[i]; }
     void release() {
         for (auto& x : b) x.release();
         timer.release();
         if (hpin) cudaFreeHost(hpin);
         hpin = nullptr;
+        if (hpin_d) cudaFreeHost(hpin_d);
+        hpin_d = nullptr;
+        hpin_d_n = 0;
     }
 };
 
@@ -292,6 +307,7 @@ int hessian_apply(Arena& A, Work& W, bool fp64, const double* x, double* y, cuda
 int build_contact_clusters(Arena& A, Work& W, const ContactSet& cs, bool fp64, cudaStream_t s);
 // vecops.cu
 int vec_neg(long n, const double* a, double* out, cudaStream_t s);
+int vec_fill(double* a, long n, double v, cudaStream_t s);
 int vec_copy_masked(Arena& A, const unsigned char* mask, const double* src, double* dst, cudaStream_t s);
 int vec_dir_norm2(Arena& A, Work& W, const double* dir, double* inst_out, cudaStream_t s);
 int vec_velocity(Arena& A, const double* X, const double* Xn, double h, double* v, cudaStream_t s);

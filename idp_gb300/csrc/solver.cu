@@ -1400,8 +1400,12 @@ int pcg_solve(Arena& A, Work& W, const ContactSet& cs, bool fp64, const double* 
     std::vector<double> b2(nI, 0.0), hrr(nI);
     std::vector<unsigned char> act(nI), act0(nI);
     IDP_CUDA_TRY(cudaMemcpyAsync(act0.data(), A.active, nI, cudaMemcpyDeviceToHost, s));
-    // |b|^2 per instance (x = 0 gives res = b)
-    auto residual = [&](std::vector<double>& out) -> int {
+    // FP64 residual res = b - A sol and its squared norm per instance; the
+    // norms are copied to pinned host memory, valid after the next
+    // synchronisation of the stream (sync = true waits here)
+    double* hres = W.pinned_doubles(nI);
+    if (!hres) return IDP_ERR_CUDA;
+    auto residual_async = [&]() -> int {
         if (fp64)
             (::idp::count_launch(), k_residual64<double><<<grid_for(8 * A.V, kBlock), kBlock, 0, s>>>(A.V, A.vinst, A.active, A.rowptr, A.colidx,
                                                                     W[W_BSR_VAL].as<double>(), trp, tcol,
@@ -1412,12 +1416,22 @@ int pcg_solve(Arena& A, Work& W, const ContactSet& cs, bool fp64, const double* 
                                                                    W[W_TAIL_VAL].as<float>(), A.dbc, rhs, sol, res));
         (::idp::count_launch(), k_norm2_chunks<<<A.n_vert_chunks, kBlock, 0, s>>>(A.vert_chunks, A.active, res, part));
         if (chunk_reduce_off(A, A.vert_chunk_off, part, inst_rr, false, s)) return IDP_ERR_CUDA;
-        IDP_CUDA_TRY(cudaMemcpyAsync(out.data(), inst_rr, sizeof(double) * nI, cudaMemcpyDeviceToHost, s));
-        IDP_CUDA_TRY(cudaStreamSynchronize(s));
+        IDP_CUDA_TRY(cudaMemcpyAsync(hres, inst_rr, sizeof(double) * nI, cudaMemcpyDeviceToHost, s));
         return IDP_OK;
     };
-    int rc = residual(b2);
+    auto residual = [&](std::vector<double>& out) -> int {
+        int r = residual_async();
+        if (r) return r;
+        IDP_CUDA_TRY(cudaStreamSynchronize(s));
+        out.assign(hres, hres + nI);
+        return IDP_OK;
+    };
+    // |b|^2 (x = 0 gives res = b); read after the first sweep, whose own
+    // synchronisation brings it back (every active instance runs sweep 0)
+    int rc = residual_async();
     if (rc) return rc;
+    bool b2_pending = true;
+    bool hrr_current = false;
     const int max_refine = fp64 ? 1 : 8;
     const double inner_tol = fp64 ? rel_tol : std::max(rel_tol, 2e-3);
     std::vector<double> prev(nI, 0.0);
@@ -1426,20 +1440,30 @@ int pcg_solve(Arena& A, Work& W, const ContactSet& cs, bool fp64, const double* 
         // improving (the FP32 operator cannot resolve them), stop refining
         bool any = false;
         if (ref > 0) {
+            if (b2_pending) {  // the first sweep synchronised the stream
+                b2.assign(hres, hres + nI);
+                b2_pending = false;
+                for (int i = 0; i < nI; ++i) prev[i] = b2[i];
+            }
             rc = residual(hrr);
             if (rc) return rc;
+            hrr_current = true;
+            for (int i = 0; i < nI; ++i) {
+                const double ti = tol_host ? std::max(rel_tol, tol_host[i]) : rel_tol;
+                const bool stalled = act[i] && hrr[i] > 0.25 * prev[i];
+                act[i] = act[i] && b2[i] > 0 && hrr[i] > ti * ti * b2[i] && !stalled;
+                relres_out[i] = b2[i] > 0 ? std::sqrt(hrr[i] / b2[i]) : 0.0;
+                prev[i] = hrr[i];
+                any |= act[i] != 0;
+            }
         } else {
-            hrr = b2;
-        }
-        for (int i = 0; i < nI; ++i) {
-            const double ti = tol_host ? std::max(rel_tol, tol_host[i]) : rel_tol;
-            const bool stalled = ref > 0 && act[i] && hrr[i] > 0.25 * prev[i];
-            act[i] = act0[i] && b2[i] > 0 && hrr[i] > ti * ti * b2[i] && (ref == 0 || act[i]) && !stalled;
-            relres_out[i] = b2[i] > 0 ? std::sqrt(hrr[i] / b2[i]) : 0.0;
-            prev[i] = hrr[i];
-            any |= act[i] != 0;
+            for (int i = 0; i < nI; ++i) {
+                act[i] = act0[i];
+                any |= act[i] != 0;
+            }
         }
         if (!any) break;
+        hrr_current = false;
         IDP_CUDA_TRY(cudaMemcpyAsync(A.active, act.data(), nI, cudaMemcpyHostToDevice, s));
         std::vector<int> its;
         if (fp64) {
@@ -1458,8 +1482,14 @@ int pcg_solve(Arena& A, Work& W, const ContactSet& cs, bool fp64, const double* 
     }
     IDP_CUDA_TRY(cudaMemcpyAsync(A.active, act0.data(), nI, cudaMemcpyHostToDevice, s));
     if (rc) return rc;
-    rc = residual(hrr);
-    if (rc) return rc;
+    if (b2_pending) {
+        IDP_CUDA_TRY(cudaStreamSynchronize(s));
+        b2.assign(hres, hres + nI);
+    }
+    if (!hrr_current) {
+        rc = residual(hrr);
+        if (rc) return rc;
+    }
     for (int i = 0; i < nI; ++i) relres_out[i] = b2[i] > 0 ? std::sqrt(hrr[i] / b2[i]) : 0.0;
     return IDP_OK;
 }

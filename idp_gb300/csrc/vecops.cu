@@ -6,6 +6,11 @@ namespace idp {
 
 namespace {
 
+__global__ void k_fill_value(long n, double v, double* __restrict__ a) {
+    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) a[i] = v;
+}
+
 __global__ void k_neg(long n, const double* __restrict__ a, double* __restrict__ o) {
     long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) o[i] = -a[i];
@@ -67,6 +72,12 @@ __global__ void k_kappa_check(long C, const int4* __restrict__ cons, const int* 
 }
 
 }  // namespace
+
+int vec_fill(double* a, long n, double v, cudaStream_t s) {
+    if (n <= 0) return IDP_OK;
+    (::idp::count_launch(), k_fill_value<<<grid_for(n), kBlock, 0, s>>>(n, v, a));
+    return cudaGetLastError() == cudaSuccess ? IDP_OK : IDP_ERR_CUDA;
+}
 
 int vec_neg(long n, const double* a, double* out, cudaStream_t s) {
     (::idp::count_launch(), k_neg<<<grid_for(n), kBlock, 0, s>>>(n, a, out));
