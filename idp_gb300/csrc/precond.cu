@@ -55,57 +55,149 @@ __global__ void k_cl_gather(int ncl, const int* __restrict__ off, const int* __r
     }
 }
 
-// Factor every block: K_c = L L^T (right-looking Cholesky in place, the
-// pivot column staged in shared memory, each warp updating whole rows of the
-// trailing triangle with coalesced accesses), then Y = L^{-1} into Ybuf by
-// forward substitution on the identity, all columns in lock-step (thread c
-// owns column c; row k of Y is read coalesced, L[i][k] is a broadcast).
-// The PCG applies K_c^{-1} = Y^T Y as z = Y^T (Y r). ok[c] = 0 when a pivot
-// is not positive (the block then falls back to 3x3 inverses).
-constexpr int kInvThreads = 1024;
+// Factor every block, one CTA per block, in 32-wide panels:
+//  Cholesky K_c = L L^T (right-looking, in place): the diagonal 32x32 tile is
+//  factored by one warp in shared memory, the panel below it is solved row by
+//  row (thread per row) into shared memory, and the trailing lower triangle
+//  takes the rank-32 update from the staged panel (padded rows, no bank
+//  conflicts);
+//  Y = L^{-1} by block rows: for rows i0..i0+31 every thread owns a column and
+//  keeps the 32 row sums in registers while streaming the column of the rows
+//  above, then solves with the diagonal tile.
+// The PCG applies K_c^{-1} = Y^T Y as z = Y^T (Y r). ok[c] = 0 when a pivot is
+// not positive (the block then falls back to 3x3 inverses).
+constexpr int kInvThreads = 256;
+constexpr int kTB = 32;
+constexpr int kNMax = 3 * kClusterCap;
+
+template <class T>
+size_t invert_smem_bytes() {
+    const size_t pan = (size_t)kNMax * (kTB + 1), rows = (size_t)kTB * (kNMax + 1);
+    return sizeof(T) * ((pan > rows ? pan : rows) + (size_t)kTB * (kTB + 1)) + 64;
+}
 
 template <class T>
 __global__ void __launch_bounds__(kInvThreads) k_cl_invert(int ncl, const int* __restrict__ off,
                                                            const long long* __restrict__ doff, T* __restrict__ K,
                                                            T* __restrict__ Ybuf, int* __restrict__ ok) {
-    __shared__ T colj[3 * kClusterCap];
+    extern __shared__ __align__(16) unsigned char inv_smem[];
+    T* big = reinterpret_cast<T*>(inv_smem);                                  // panel or row tile
+    T* dsm = big + (kNMax * (kTB + 1) > kTB * (kNMax + 1) ? kNMax * (kTB + 1) : kTB * (kNMax + 1));  // TB x (TB+1)
+    __shared__ int fail;
     const int c = blockIdx.x;
     const int N = 3 * (off[c + 1] - off[c]);
     T* L = K + doff[c];
     T* Y = Ybuf + doff[c];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int j = 0; j < N; ++j) {
-        const T d = L[(long)j * N + j];
-        if (!(d > T(0))) {  // every thread sees the same pivot
-            if (threadIdx.x == 0) ok[c] = 0;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = kInvThreads / 32;
+    if (tid == 0) fail = 0;
+    __syncthreads();
+    // ---- Cholesky
+    for (int k0 = 0; k0 < N; k0 += kTB) {
+        const int kw = min(kTB, N - k0);
+        for (int e = tid; e < kw * kw; e += kInvThreads) {
+            const int r = e / kw, q = e % kw;
+            dsm[r * (kTB + 1) + q] = L[(long)(k0 + r) * N + k0 + q];
+        }
+        __syncthreads();
+        if (warp == 0) {
+            for (int j = 0; j < kw; ++j) {
+                const T d = dsm[j * (kTB + 1) + j];
+                if (!(d > T(0))) {
+                    if (lane == 0) fail = 1;
+                    break;
+                }
+                const T ljj = sqrt(d);
+                __syncwarp();
+                if (lane == j) dsm[j * (kTB + 1) + j] = ljj;
+                if (lane > j && lane < kw) dsm[lane * (kTB + 1) + j] /= ljj;
+                __syncwarp();
+                if (lane > j && lane < kw) {
+                    const T lij = dsm[lane * (kTB + 1) + j];
+                    for (int q = j + 1; q <= lane; ++q) dsm[lane * (kTB + 1) + q] -= lij * dsm[q * (kTB + 1) + j];
+                }
+                __syncwarp();
+            }
+        }
+        __syncthreads();
+        if (fail) {
+            if (tid == 0) ok[c] = 0;
             return;
         }
-        const T ljj = sqrt(d);
-        for (int i = j + threadIdx.x; i < N; i += blockDim.x) {
-            const T v = i == j ? ljj : L[(long)i * N + j] / ljj;
-            L[(long)i * N + j] = v;
-            colj[i] = v;
+        for (int e = tid; e < kw * kw; e += kInvThreads) {
+            const int r = e / kw, q = e % kw;
+            if (q <= r) L[(long)(k0 + r) * N + k0 + q] = dsm[r * (kTB + 1) + q];
+        }
+        // panel rows below: x L_kk^T = a, staged in big[(i - k0 - kw) * (kTB + 1) + q]
+        const int m0 = k0 + kw, m = N - m0;
+        for (int ri = tid; ri < m; ri += kInvThreads) {
+            const long i = m0 + ri;
+            T x[kTB];
+#pragma unroll
+            for (int q = 0; q < kTB; ++q) {
+                if (q < kw) {
+                    T a = L[i * N + k0 + q];
+                    for (int t = 0; t < q; ++t) a -= x[t] * dsm[q * (kTB + 1) + t];
+                    x[q] = a / dsm[q * (kTB + 1) + q];
+                    big[ri * (kTB + 1) + q] = x[q];
+                    L[i * N + k0 + q] = x[q];
+                }
+            }
         }
         __syncthreads();
-        for (int i = j + 1 + warp; i < N; i += nw) {
-            const T lij = colj[i];
-            T* Li = L + (long)i * N;
-            for (int k = j + 1 + lane; k <= i; k += 32) Li[k] -= lij * colj[k];
+        // trailing lower triangle: A[i][j] -= panel_i . panel_j
+        for (int ri = warp; ri < m; ri += nw) {
+            const T* pi = big + ri * (kTB + 1);
+            T* Ai = L + (long)(m0 + ri) * N + m0;
+            for (int rj = lane; rj <= ri; rj += 32) {
+                const T* pj = big + rj * (kTB + 1);
+                T acc = 0;
+#pragma unroll 8
+                for (int q = 0; q < kw; ++q) acc += pi[q] * pj[q];
+                Ai[rj] -= acc;
+            }
         }
         __syncthreads();
     }
-    // Y = L^{-1}: row i of Y from rows k < i (columns c <= k are nonzero)
-    for (int i = 0; i < N; ++i) {
-        const T* Li = L + (long)i * N;
-        const T inv = T(1) / Li[i];
-        for (int col = threadIdx.x; col < N; col += blockDim.x) {
-            T acc = col == i ? T(1) : T(0);
-            for (int k = col; k < i; ++k) acc -= Li[k] * Y[(long)k * N + col];
-            Y[(long)i * N + col] = col <= i ? acc * inv : T(0);
+    // ---- Y = L^{-1}, block row by block row
+    for (int i0 = 0; i0 < N; i0 += kTB) {
+        const int iw = min(kTB, N - i0);
+        const int ncol = i0 + iw;
+        // rows i0..i0+iw of L (columns < i0) and the diagonal tile
+        for (int e = tid; e < iw * ncol; e += kInvThreads) {
+            const int r = e / ncol, k = e % ncol;
+            const T v = L[(long)(i0 + r) * N + k];
+            if (k < i0) big[r * (kNMax + 1) + k] = v;
+            else dsm[r * (kTB + 1) + (k - i0)] = v;
+        }
+        __syncthreads();
+        for (int col = tid; col < ncol; col += kInvThreads) {
+            T acc[kTB];
+#pragma unroll
+            for (int r = 0; r < kTB; ++r) acc[r] = T(0);
+            for (int k = col; k < i0; ++k) {
+                const T ykc = Y[(long)k * N + col];
+#pragma unroll
+                for (int r = 0; r < kTB; ++r) acc[r] += big[r * (kNMax + 1) + k] * ykc;
+            }
+#pragma unroll
+            for (int r = 0; r < kTB; ++r) {
+                if (r < iw) {
+                    T v = (col == i0 + r ? T(1) : T(0)) - acc[r];
+                    for (int t = 0; t < r; ++t) v -= dsm[r * (kTB + 1) + t] * acc[t];
+                    v /= dsm[r * (kTB + 1) + r];
+                    acc[r] = v;  // acc[r] now holds y(i0 + r, col)
+                    Y[(long)(i0 + r) * N + col] = col <= i0 + r ? v : T(0);
+                }
+            }
+        }
+        // columns right of the tile stay zero (Y is lower triangular)
+        for (int e = tid; e < iw * (N - ncol); e += kInvThreads) {
+            const int r = e / (N - ncol), q = ncol + e % (N - ncol);
+            Y[(long)(i0 + r) * N + q] = T(0);
         }
         __syncthreads();
     }
-    if (threadIdx.x == 0) ok[c] = 1;
+    if (tid == 0) ok[c] = 1;
 }
 
 struct DSU {
@@ -300,13 +392,27 @@ int build_contact_clusters(Arena& A, Work& W, const ContactSet& cs, bool fp64, c
         (::idp::count_launch(), k_cl_gather<double><<<ncl, 256, 0, s>>>(ncl, cl.off, cl.vert, cl.vcl, cl.vloc, cl.doff, A.rowptr, A.colidx,
                                                   W[W_BSR_VAL].as<double>(), trp, tcol, W[W_TAIL_VAL].as<double>(),
                                                   A.dbc, K));
-        (::idp::count_launch(), k_cl_invert<double><<<ncl, kInvThreads, 0, s>>>(ncl, cl.off, cl.doff, K, K + cl.dense, okp));
+        static bool attr_d = false;
+        if (!attr_d) {
+            IDP_CUDA_TRY(cudaFuncSetAttribute(k_cl_invert<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)invert_smem_bytes<double>()));
+            attr_d = true;
+        }
+        (::idp::count_launch(), k_cl_invert<double><<<ncl, kInvThreads, invert_smem_bytes<double>(), s>>>(
+                                    ncl, cl.off, cl.doff, K, K + cl.dense, okp));
     } else {
         float* K = W[W_CL_DENSE].as<float>();
         (::idp::count_launch(), k_cl_gather<float><<<ncl, 256, 0, s>>>(ncl, cl.off, cl.vert, cl.vcl, cl.vloc, cl.doff, A.rowptr, A.colidx,
                                                  W[W_BSR_VAL].as<float>(), trp, tcol, W[W_TAIL_VAL].as<float>(), A.dbc,
                                                  K));
-        (::idp::count_launch(), k_cl_invert<float><<<ncl, kInvThreads, 0, s>>>(ncl, cl.off, cl.doff, K, K + cl.dense, okp));
+        static bool attr_f = false;
+        if (!attr_f) {
+            IDP_CUDA_TRY(cudaFuncSetAttribute(k_cl_invert<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)invert_smem_bytes<float>()));
+            attr_f = true;
+        }
+        (::idp::count_launch(), k_cl_invert<float><<<ncl, kInvThreads, invert_smem_bytes<float>(), s>>>(
+                                    ncl, cl.off, cl.doff, K, K + cl.dense, okp));
     }
     return cudaGetLastError() == cudaSuccess ? IDP_OK : IDP_ERR_CUDA;
 }
