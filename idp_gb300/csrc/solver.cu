@@ -147,50 +147,21 @@ __device__ double cta_sum(double v) {
     return r;
 }
 
-// FP64 residual res = b - A x64: 8 lanes per block row (4 rows per warp),
-// FP64 accumulation of the stored (FP32 or FP64) operator against the FP64
-// solution; the squared norm is reduced afterwards per vertex chunk
+// FP64 residual res = b - A x64 (FP32/FP64 matrix, FP64 accumulation), one
+// thread per block row in small CTAs (the FP64 pipe, not memory, limits it);
+// the squared norm is reduced afterwards per vertex chunk
 template <class T>
 __global__ void k_residual64(long V, const int* __restrict__ vinst, const unsigned char* __restrict__ active,
                              const int* __restrict__ rowptr, const int* __restrict__ colidx, const T* __restrict__ val,
                              const int* __restrict__ trp, const int* __restrict__ tcol, const T* __restrict__ tval,
                              const unsigned char* __restrict__ dbc, const double* __restrict__ b,
                              const double* __restrict__ x, double* __restrict__ res) {
-    const int lane = threadIdx.x & 31, l8 = lane & 7;
-    const long v = (((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 4 + (lane >> 3);
-    const bool act = v < V && active[vinst[v]];
-    const bool fixed = act && dbc[v];
-    double a0 = 0, a1 = 0, a2 = 0;
-    if (act && !fixed) {
-        const int k1 = rowptr[v + 1];
-        for (int k = rowptr[v] + l8; k < k1; k += 8) {
-            const int c = colidx[k];
-            const T* m = val + 9L * k;
-            const double x0 = x[3 * c], x1 = x[3 * c + 1], x2 = x[3 * c + 2];
-            a0 += (double)m[0] * x0 + (double)m[1] * x1 + (double)m[2] * x2;
-            a1 += (double)m[3] * x0 + (double)m[4] * x1 + (double)m[5] * x2;
-            a2 += (double)m[6] * x0 + (double)m[7] * x1 + (double)m[8] * x2;
-        }
-        const int t1 = trp[v + 1];
-        for (int k = trp[v] + l8; k < t1; k += 8) {
-            const int c = tcol[k];
-            if (dbc[c]) continue;
-            const T* m = tval + 9L * k;
-            const double x0 = x[3 * c], x1 = x[3 * c + 1], x2 = x[3 * c + 2];
-            a0 += (double)m[0] * x0 + (double)m[1] * x1 + (double)m[2] * x2;
-            a1 += (double)m[3] * x0 + (double)m[4] * x1 + (double)m[5] * x2;
-            a2 += (double)m[6] * x0 + (double)m[7] * x1 + (double)m[8] * x2;
-        }
-    }
-    for (int o = 4; o > 0; o >>= 1) {
-        a0 += __shfl_xor_sync(0xffffffffu, a0, o);
-        a1 += __shfl_xor_sync(0xffffffffu, a1, o);
-        a2 += __shfl_xor_sync(0xffffffffu, a2, o);
-    }
-    if (act && l8 < 3) {
-        const double y = l8 == 0 ? a0 : (l8 == 1 ? a1 : a2);
-        res[3 * v + l8] = fixed ? 0.0 : b[3 * v + l8] - y;
-    }
+    long v = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= V || !active[vinst[v]]) return;
+    double y[3];
+    spmv_row<T, double, double>(v, rowptr, colidx, val, trp, tcol, tval, dbc, x, y);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) res[3 * v + d] = dbc[v] ? 0.0 : b[3 * v + d] - y[d];
 }
 
 __global__ void k_norm2_chunks(const Chunk* __restrict__ chunks, const unsigned char* __restrict__ active,
@@ -1407,11 +1378,11 @@ int pcg_solve(Arena& A, Work& W, const ContactSet& cs, bool fp64, const double* 
     if (!hres) return IDP_ERR_CUDA;
     auto residual_async = [&]() -> int {
         if (fp64)
-            (::idp::count_launch(), k_residual64<double><<<grid_for(8 * A.V, kBlock), kBlock, 0, s>>>(A.V, A.vinst, A.active, A.rowptr, A.colidx,
+            (::idp::count_launch(), k_residual64<double><<<grid_for(A.V, 64), 64, 0, s>>>(A.V, A.vinst, A.active, A.rowptr, A.colidx,
                                                                     W[W_BSR_VAL].as<double>(), trp, tcol,
                                                                     W[W_TAIL_VAL].as<double>(), A.dbc, rhs, sol, res));
         else
-            (::idp::count_launch(), k_residual64<float><<<grid_for(8 * A.V, kBlock), kBlock, 0, s>>>(A.V, A.vinst, A.active, A.rowptr, A.colidx,
+            (::idp::count_launch(), k_residual64<float><<<grid_for(A.V, 64), 64, 0, s>>>(A.V, A.vinst, A.active, A.rowptr, A.colidx,
                                                                    W[W_BSR_VAL].as<float>(), trp, tcol,
                                                                    W[W_TAIL_VAL].as<float>(), A.dbc, rhs, sol, res));
         (::idp::count_launch(), k_norm2_chunks<<<A.n_vert_chunks, kBlock, 0, s>>>(A.vert_chunks, A.active, res, part));
