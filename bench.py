@@ -67,6 +67,11 @@ def parse():
     ap.add_argument("--instances", type=int, default=256)
     ap.add_argument("--mode", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--max-newton", type=int, default=2000)
+    ap.add_argument("--newton-budget", type=int, default=0,
+                    help="batch/bar workloads: stop every instance after this many Newton iterations and report "
+                         "Newton iterations/s (0 = solve to convergence, report solves/s)")
+    ap.add_argument("--fp64-sample", type=int, default=16,
+                    help="batch/bar workloads: instances re-solved one at a time on the FP64 path")
     ap.add_argument("--cpu-sample-s", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
@@ -189,10 +194,12 @@ def ncu_traffic():
         return None
 
 
-def cpu_baseline(probs, budget_s):
-    """Oracle (FP64, direct solve) on a bounded sample: full solves of the
-    smallest instances until the budget is spent; throughput extrapolated to
-    the workload by tet count."""
+def cpu_baseline(probs, budget_s, newton_budget=0):
+    """Oracle (FP64, direct solve) on a bounded sample: solves of the
+    smallest instances (capped at newton_budget Newton iterations when it is
+    set) until the time budget is spent; throughput extrapolated to the
+    workload by tet count (solves/s, or Newton iterations/s summed over the
+    workload's instances when newton_budget is set)."""
     import numpy as np
 
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -206,7 +213,7 @@ def cpu_baseline(probs, budget_s):
         T = p["tets"].shape[0]
         pb = O.Problem(X=p["X"].copy(), X0=p["X"], tets=p["tets"], mass=p["mass"], lam=np.full(T, p["lam"]),
                        mu=np.full(T, p["mu"]), h=0.1, dHat2=p["dHat2"], kappa=[p["kappa"], p["kappa_max"], 0.0],
-                       v=(p["target"] - p["X"]) / 0.1, tol=1e-3, max_iters=2000)
+                       v=(p["target"] - p["X"]) / 0.1, tol=1e-3, max_iters=newton_budget or 2000)
         t0 = time.perf_counter()
         iters += O.advance_one_step(pb)
         t_used += time.perf_counter() - t0
@@ -216,10 +223,16 @@ def cpu_baseline(probs, budget_s):
             break
     mean_tets = sum(p["tets"].shape[0] for p in probs) / len(probs)
     rate = tets_done / t_used / mean_tets  # workload solves per second
+    unit = UNIT
+    if newton_budget:
+        # Newton iterations per second at the mean instance size
+        rate = iters / t_used * (tets_done / solved) / mean_tets
+        unit = "newton_iters/s"
     cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
-    return {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"oracle full solves of the {solved} smallest instance(s) ({tets_done} tets, {iters} Newton "
-                      f"iterations, {t_used:.1f} s); solves/s scaled to the mean instance ({mean_tets:.0f} tets)"}
+    return {"value": rate, "unit": unit, "cores": cores, "kind": "port",
+            "sample": (f"oracle {'solves capped at %d Newton iterations' % newton_budget if newton_budget else 'full solves'}"
+                       f" of the {solved} smallest instance(s) ({tets_done} tets, {iters} Newton iterations, "
+                       f"{t_used:.1f} s); scaled to the mean instance ({mean_tets:.0f} tets)")}
 
 
 H = 0.1
@@ -381,7 +394,7 @@ def run_flow(args):
     lat = [r["latency_ms"] for r in results]
     newton = [r["newton_iters"] for r in results]
     out = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "metric": metric, "value": value, "unit": unit, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32+f64" if mode == idp.MODE_MIXED else "f64", "data": "synthetic",
         "config": {"workload": desc, "tets": int(p["tets"].shape[0]), "verts": V, "mode": args.mode,
@@ -405,6 +418,9 @@ def run_flow(args):
         "clocks": clocks.summary(),
         "wall_ms_per_step": 1000 * statistics.mean(wall),
     }
+    if fp64_single:
+        ref = fp64_single["newton_iters_per_s"] if budget > 0 else fp64_single["solves_per_s"]
+        out["mixed_batched_over_fp64_one_at_a_time"] = (value / ref) if ref else None
     if not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline_flow(int(p["tets"].shape[0]), args.flow_step, args.cpu_sample_s)
     print(json.dumps(out), flush=True)
@@ -428,18 +444,24 @@ def run_reference(args):
         for _ in range(args.warmup + args.steps):
             bl = cpu_baseline_flow(int(tets.shape[0]), args.flow_step, per_step)
             vals.append(bl["value"])
-    else:
+    metric, unit = METRIC, UNIT
+    if args.workload != "blob":
         probs, desc = make_workload(args, seed=0)
+        if args.newton_budget > 0:
+            desc += f"; first {args.newton_budget} Newton iterations of every instance from the rest state"
+            metric = "Newton iterations/s (summed over instances), mixed batched vs FP64 one at a time"
+            unit = "newton_iters/s"
+        per_step = min(args.cpu_sample_s, 150.0 / max(1, args.warmup + args.steps))
         for _ in range(args.warmup + args.steps):
-            bl = cpu_baseline(probs, args.cpu_sample_s)
+            bl = cpu_baseline(probs, per_step, args.newton_budget)
             vals.append(bl["value"])
     v = statistics.mean(vals[args.warmup:]) if args.steps else vals[-1]
-    out = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+    out = {"impl": "reference", "metric": metric, "value": v, "unit": unit, "n_gpus": args.gpus,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / v if v else None,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
            "config": {"workload": desc, "instances": len(probs)},
            "cpu_baseline": dict(bl, value=v),
-           "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+           "e2e": {"value": v, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
            "note": "reference CPU path = oracle port (the reference does not build here: Eigen, CHOLMOD, Boost "
                    "and Kokkos are absent)"}
     print(json.dumps(out))
@@ -459,7 +481,11 @@ def run_gpu(args):
     torch.cuda.set_device(local)
     # replicas: every rank solves its own copy of the workload (seeded by rank)
     probs, desc = make_workload(args, seed=rank)
-    ctx = idp.Context(h=0.1, newton_tol=1e-3, max_newton=args.max_newton, mode=mode, device=local)
+    budget = args.newton_budget
+    max_newton = budget if budget > 0 else args.max_newton
+    if budget > 0:
+        desc += f"; first {budget} Newton iterations of every instance from the rest state"
+    ctx = idp.Context(h=0.1, newton_tol=1e-3, max_newton=max_newton, mode=mode, device=local)
     for i, p in enumerate(probs):
         ctx.add_instance(p["X"], p["tets"], p["mass"], p["lam"], p["mu"], p["dHat2"], p["kappa"], p["kappa_max"])
         ctx.set_velocity(i, (p["target"] - p["X"]) / 0.1)
@@ -495,7 +521,20 @@ def run_gpu(args):
             lat += [r["latency_ms"] for r in results]
     barrier()
     step_ms = max_over_ranks(statistics.mean(dev_ms), world)
-    value = world * nI / (step_ms / 1000.0)
+    iters_step = sum(r["newton_iters"] for r in results)
+    metric, unit = METRIC, UNIT
+    if budget > 0:
+        metric = "Newton iterations/s (summed over instances), mixed batched vs FP64 one at a time"
+        unit = "newton_iters/s"
+        value = world * iters_step / (step_ms / 1000.0)
+    else:
+        value = world * nI / (step_ms / 1000.0)
+    # exact intersection check and inversion status of every instance's result
+    counts = ctx.intersection_counts()
+    injective = {"checked": nI, "intersection_free": int((counts == 0).sum()),
+                 "inverted": sum(1 for r in results if r["status"] == idp.IDP_ERR_INVERTED)}
+    fp64_single = fp64_one_at_a_time(idp, probs, results, args.fp64_sample, max_newton, budget, local) \
+        if rank == 0 and mode == idp.MODE_MIXED and args.fp64_sample > 0 else None
 
     # ---- end to end with host buffers (pinned), copies inside the timed region
     Xh = [torch.from_numpy(np.ascontiguousarray(p["X"])).pin_memory() for p in probs]
@@ -514,7 +553,7 @@ def run_gpu(args):
             ctx.state_ptr(i, Xo[i].data_ptr())
         e2e_wall.append(time.perf_counter() - t0)
     e2e_s = max_over_ranks(statistics.mean(e2e_wall), world)
-    e2e_val = world * nI / e2e_s
+    e2e_val = world * (iters_step if budget > 0 else nI) / e2e_s
     h2d = 2 * 3 * total_verts * 8
     d2h = 3 * total_verts * 8
 
@@ -528,28 +567,70 @@ def run_gpu(args):
         status[str(r["status"])] = status.get(str(r["status"]), 0) + 1
     newton = [r["newton_iters"] for r in results]
     out = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "metric": metric, "value": value, "unit": unit, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32+f64" if mode == idp.MODE_MIXED else "f64", "data": "synthetic",
         "config": {"workload": desc, "instances": nI, "total_tets": total_tets, "mode": args.mode,
                    "parallelism": f"replicas{world}", "l2": "inputs larger than L2 (arena %.0f MB)" % (
                        (total_tets * 112 + total_verts * 24 * 6) / 1e6)},
         "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
-        "newton_iters": {"mean": float(np.mean(newton)), "max": int(np.max(newton))},
+        "newton_iters": {"mean": float(np.mean(newton)), "max": int(np.max(newton)), "total": int(iters_step)},
         "status_counts": status,
-        "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "injective": injective,
+        "fp64_one_at_a_time": fp64_single,
+        "e2e": {"value": e2e_val, "unit": unit, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None,
                      "traffic": traffic.get("bytes_per_launch") if traffic else None,
-                     "kernel": "k_pcg_cta (persistent block-Jacobi PCG, one CTA per instance)",
+                     "kernel": "k_pcg_cluster (block-Jacobi + contact-block PCG, one thread-block cluster per "
+                               "instance)",
                      "peak_source": peak_kind},
         "gpu_launches": launches,
         "clocks": clocks.summary(),
         "wall_ms_per_step": 1000 * statistics.mean(wall),
     }
+    if fp64_single:
+        ref = fp64_single["newton_iters_per_s"] if budget > 0 else fp64_single["solves_per_s"]
+        out["mixed_batched_over_fp64_one_at_a_time"] = (value / ref) if ref else None
     if not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline(probs, args.cpu_sample_s)
+        out["cpu_baseline"] = cpu_baseline(probs, args.cpu_sample_s, budget)
     print(json.dumps(out))
+
+
+def fp64_one_at_a_time(idp, probs, results, sample, max_newton, budget, device):
+    """The plain FP64 path, one instance per context and call, on `sample`
+    instances spread evenly over the batch (same start state and Newton
+    budget as the batched mixed run); Newton iterations/s and solves/s from
+    the library's device time, and the relative energy difference of the
+    batched mixed results on the same instances."""
+    import numpy as np
+
+    nI = len(probs)
+    idx = sorted(set(np.linspace(0, nI - 1, min(sample, nI)).round().astype(int).tolist()))
+    ms = its = 0.0
+    solved = 0
+    rel = []
+    for i in idx:
+        p = probs[i]
+        c = idp.Context(h=0.1, newton_tol=1e-3, max_newton=max_newton, mode=idp.MODE_FP64, device=device)
+        c.add_instance(p["X"], p["tets"], p["mass"], p["lam"], p["mu"], p["dHat2"], p["kappa"], p["kappa_max"])
+        c.set_velocity(0, (p["target"] - p["X"]) / 0.1)
+        c.commit()
+        c.save_state()
+        c.advance(check=False)  # warm-up: grows the work buffers
+        c.restore_state()
+        _, r = c.advance(check=False)
+        ms += c.stats()["total_ms"]
+        its += r[0]["newton_iters"]
+        solved += r[0]["status"] in (idp.IDP_OK, idp.IDP_WARN_ITER_CAP)
+        e64, em = r[0]["energy"], results[i]["energy"]
+        rel.append(abs(em - e64) / max(abs(e64), 1e-300))
+        c.close()
+    out = {"instances": idx if len(idx) <= 32 else len(idx), "newton_iters": int(its), "ms": ms,
+           "newton_iters_per_s": its / (ms / 1000.0) if ms > 0 else None,
+           "solves_per_s": (len(idx) / (ms / 1000.0)) if budget == 0 and ms > 0 else None,
+           "converged": solved, "rel_energy_diff_mixed_batched": {"max": max(rel), "mean": float(np.mean(rel))}}
+    return out
 
 
 def main():

@@ -26,6 +26,7 @@ IDP_ERR_ZERO_STEP = 6
 IDP_ERR_NONPOSITIVE_DIST = 7
 IDP_ERR_STATE = 8
 IDP_WARN_ITER_CAP = 9
+IDP_ERR_INTERSECTION = 10
 MODE_FP64 = 0
 MODE_MIXED = 1
 
@@ -35,7 +36,8 @@ EXPORTS = [
     "idp_set_positions", "idp_commit", "idp_advance", "idp_get_state", "idp_instance_info", "idp_get_surface",
     "idp_eval_energy", "idp_eval_gradient", "idp_constraint_set", "idp_ccd_stepsize", "idp_hessian_apply",
     "idp_newton_direction", "idp_get_stats", "idp_save_state", "idp_restore_state",
-    "idp_set_normal_flow", "idp_set_kappa", "idp_tet_energy_noalloc",
+    "idp_set_normal_flow", "idp_set_kappa", "idp_tet_energy_noalloc", "idp_check_intersection",
+    "idp_check_intersection_all",
 ]
 
 
@@ -43,7 +45,7 @@ class Params(C.Structure):
     _fields_ = [("h", C.c_double), ("newton_tol", C.c_double), ("max_newton", C.c_int), ("mode", C.c_int),
                 ("pcg_rel_tol", C.c_double), ("pcg_max_iters", C.c_int), ("thickness", C.c_double),
                 ("device", C.c_int), ("pcg_grid_min_vertices", C.c_int), ("pcg_grid_cta_vertices", C.c_int),
-                ("contact_block_vertices", C.c_int)]
+                ("contact_block_vertices", C.c_int), ("verify_iterates", C.c_int)]
 
 
 class Result(C.Structure):
@@ -59,7 +61,8 @@ class Stats(C.Structure):
     _fields_ = [("pcg_ms", C.c_double), ("pcg_bytes", C.c_double), ("pcg_iters", C.c_longlong),
                 ("pcg_launches", C.c_int), ("tet_ms", C.c_double), ("contact_ms", C.c_double), ("ccd_ms", C.c_double),
                 ("total_ms", C.c_double), ("kernel_launches", C.c_longlong), ("barrier_ms", C.c_double),
-                ("assembly_ms", C.c_double), ("fp64_fallbacks", C.c_int)]
+                ("assembly_ms", C.c_double), ("fp64_fallbacks", C.c_int), ("verify_checks", C.c_longlong),
+                ("verify_failures", C.c_longlong)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -111,6 +114,8 @@ def load(path: str | None = None):
     L.idp_hessian_apply.argtypes = [C.c_void_p, C.c_int, _dp, _dp, _dp]
     L.idp_newton_direction.argtypes = [C.c_void_p, C.c_int, _dp, _dp, C.POINTER(C.c_int), _dp]
     L.idp_get_stats.argtypes = [C.c_void_p, C.POINTER(Stats)]
+    L.idp_check_intersection.argtypes = [C.c_void_p, C.c_int, _dp, C.c_int, _ip, C.POINTER(C.c_int)]
+    L.idp_check_intersection_all.argtypes = [C.c_void_p, _ip]
     L.idp_save_state.argtypes = [C.c_void_p]
     L.idp_restore_state.argtypes = [C.c_void_p]
     _lib = L
@@ -293,6 +298,27 @@ class Context:
         rc = load().idp_ccd_stepsize(self._h, i, _pd(X), _pd(d), C.byref(a))
         self._check(rc, "idp_ccd_stepsize", ok=(IDP_OK, IDP_WARN_ITER_CAP))
         return a.value, rc
+
+    def intersections(self, i, X=None, cap=1024):
+        """Intersecting (triangle, edge) pairs of instance i's surface at X
+        (None: its current state), as surface-list indices, sorted."""
+        Xa = None if X is None else _f64(X)
+        n = C.c_int()
+        while True:
+            buf = np.zeros((max(cap, 1), 2), np.int32)
+            rc = load().idp_check_intersection(self._h, i, None if Xa is None else _pd(Xa), cap, _pi(buf),
+                                               C.byref(n))
+            if rc == IDP_ERR_CAPACITY:
+                cap = n.value + 16
+                continue
+            self._check(rc, "idp_check_intersection")
+            return buf[: n.value].copy()
+
+    def intersection_counts(self):
+        """Number of intersecting pairs of every instance at its current state."""
+        out = np.zeros(len(self._V), np.int32)
+        self._check(load().idp_check_intersection_all(self._h, _pi(out)), "idp_check_intersection_all")
+        return out
 
     def hessian_apply(self, i, X, x):
         X, x = _f64(X), _f64(x)

@@ -17,6 +17,7 @@
 #include "engine.hpp"
 #include "grid.cuh"
 #include "geom.cuh"
+#include "predicates.cuh"
 #include "prims.cuh"
 
 namespace idp {
@@ -534,6 +535,52 @@ __global__ void k_inst_offsets(int nI, const uint32_t* __restrict__ count, const
     off[i] = (int)lo;
 }
 
+// ---- intersection check (Check_Edge_Tri_Intersect, FEM/IPC.h:2444-2517):
+// one lane group per surface triangle walks the cells of the triangle's box
+// in the edge grid; each (triangle, edge) pair is tested once (lowest shared
+// cell) after the reference's exclusions (shared vertex; triangle and edge
+// all DBC), an AABB overlap test and the exact segment-triangle test
+__global__ void k_query_tri_edges(long nT, const int* __restrict__ tris, const int* __restrict__ tinst,
+                                  const unsigned char* __restrict__ active, const double* __restrict__ X,
+                                  const unsigned char* __restrict__ dbc, const int2* __restrict__ edges,
+                                  const BoxI* __restrict__ tbox, const BoxI* __restrict__ ebox,
+                                  const GridP* __restrict__ gp, CellHash cells, const uint32_t* __restrict__ cstart,
+                                  const uint32_t* __restrict__ entries, Cand* __restrict__ out, unsigned int* counter,
+                                  long cap, unsigned int* __restrict__ inst_count) {
+    const long f = ((long)blockIdx.x * blockDim.x + threadIdx.x) / kQueryLanes;
+    if (f >= nT) return;  // the whole group leaves together
+    const int inst = tinst[f];
+    if (!active[inst]) return;
+    const int t0 = tris[3 * f], t1 = tris[3 * f + 1], t2 = tris[3 * f + 2];
+    const double ta[3] = {X[3 * t0], X[3 * t0 + 1], X[3 * t0 + 2]};
+    const double tb[3] = {X[3 * t1], X[3 * t1 + 1], X[3 * t1 + 2]};
+    const double tc[3] = {X[3 * t2], X[3 * t2 + 1], X[3 * t2 + 2]};
+    double tmin[3], tmax[3];
+    for (int d = 0; d < 3; ++d) {
+        tmin[d] = fmin(fmin(ta[d], tb[d]), tc[d]);
+        tmax[d] = fmax(fmax(ta[d], tb[d]), tc[d]);
+    }
+    const bool tdbc = dbc[t0] && dbc[t1] && dbc[t2];
+    const BoxI qb = tbox[f];
+    const GridP g = gp[inst];
+    group_walk_emit<kQueryLanes>(qb, inst, g, cells, cstart, entries, out, counter, cap,
+                   [&](uint32_t ent, int cx, int cy, int cz, Cand& c) -> bool {
+                       const int eJ = (int)ent;
+                       if (!is_first_shared(qb, ebox[eJ], cx, cy, cz)) return false;
+                       const int2 m = edges[eJ];
+                       if (m.x == t0 || m.x == t1 || m.x == t2 || m.y == t0 || m.y == t1 || m.y == t2) return false;
+                       if (tdbc && dbc[m.x] && dbc[m.y]) return false;
+                       const double e0[3] = {X[3 * m.x], X[3 * m.x + 1], X[3 * m.x + 2]};
+                       const double e1[3] = {X[3 * m.y], X[3 * m.y + 1], X[3 * m.y + 2]};
+                       for (int d = 0; d < 3; ++d)
+                           if (fmax(e0[d], e1[d]) < tmin[d] || fmin(e0[d], e1[d]) > tmax[d]) return false;
+                       if (!pred::seg_tri_intersect(e0, e1, ta, tb, tc)) return false;
+                       atomicAdd(inst_count + inst, 1u);
+                       c = {(int)f, eJ};
+                       return true;
+                   });
+}
+
 __global__ void k_min_dist2(long C, const int4* __restrict__ cons, const int* __restrict__ cinst,
                             const unsigned char* __restrict__ active, const double* __restrict__ X,
                             double* __restrict__ dist2, double* __restrict__ inst_min) {
@@ -722,25 +769,34 @@ int grids_build(Work& W, int set, const BoxI* tbox, long nt, const int* tinst, c
     return IDP_OK;
 }
 
-int build_constraint_set(Arena& A, Work& W, const double* X, ContactSet& cs, cudaStream_t s) {
+// per-instance grid over the surface at X and the integer boxes of every
+// surface triangle and edge in it
+static int surface_boxes(Arena& A, Work& W, const double* X, GridP*& gp, BoxI*& tbox, BoxI*& ebox, cudaStream_t s) {
     const int nI = A.nI;
-    // 1. per-instance grid parameters
     if (W[W_BBOX].ensure(sizeof(unsigned long long) * 6 * nI) || W[W_GRIDP].ensure(sizeof(GridP) * nI))
         return IDP_ERR_CUDA;
     unsigned long long* bb = W[W_BBOX].as<unsigned long long>();
-    GridP* gp = W[W_GRIDP].as<GridP>();
+    gp = W[W_GRIDP].as<GridP>();
     (::idp::count_launch(), k_bbox_init<<<grid_for(6 * nI), kBlock, 0, s>>>(nI, bb));
     if (A.Sn) (::idp::count_launch(), k_bbox<<<grid_for(A.Sn), kBlock, 0, s>>>(A.Sn, A.snode, A.sn_inst, A.active, X, bb));
     (::idp::count_launch(), k_grid_params<<<grid_for(nI), kBlock, 0, s>>>(nI, bb, A.cell, A.dHat2, A.thickness, A.active, gp));
-    // 2. triangle and edge boxes + grids
     long St = A.St > 0 ? A.St : 1, Se = A.Se > 0 ? A.Se : 1;
     if (W[W_BOX_A].ensure(sizeof(BoxI) * St) || W[W_BOX_B].ensure(sizeof(BoxI) * Se)) return IDP_ERR_CUDA;
-    BoxI* tbox = W[W_BOX_A].as<BoxI>();
-    BoxI* ebox = W[W_BOX_B].as<BoxI>();
+    tbox = W[W_BOX_A].as<BoxI>();
+    ebox = W[W_BOX_B].as<BoxI>();
     if (A.St) (::idp::count_launch(), k_prim_boxes<3><<<grid_for(A.St), kBlock, 0, s>>>(A.St, A.stri, A.st_inst, A.active, X, gp, tbox));
     if (A.Se)
         (::idp::count_launch(), k_prim_boxes<2><<<grid_for(A.Se), kBlock, 0, s>>>(A.Se, reinterpret_cast<const int*>(A.sedge), A.se_inst,
                                                            A.active, X, gp, ebox));
+    return IDP_OK;
+}
+
+int build_constraint_set(Arena& A, Work& W, const double* X, ContactSet& cs, cudaStream_t s) {
+    const int nI = A.nI;
+    // 1-2. per-instance grid parameters, triangle and edge boxes
+    GridP* gp = nullptr;
+    BoxI *tbox = nullptr, *ebox = nullptr;
+    if (int r = surface_boxes(A, W, X, gp, tbox, ebox, s)) return r;
     // 3. grids and candidates: PT in [0, cap_pt), EE in [cap_pt, cap_pt +
     // cap_ee); one host round trip reads both counts and the grids' overflow
     // flag (ccount[2])
@@ -856,6 +912,46 @@ int build_constraint_set(Arena& A, Work& W, const double* X, ContactSet& cs, cud
             cs.d_off = W[W_CONS_OFF].as<int>();
             return IDP_OK;
         }
+    }
+    return IDP_ERR_CAPACITY;
+}
+
+int edge_tri_intersections(Arena& A, Work& W, const double* X, unsigned int* inst_count, const int2** pairs,
+                           long* npairs, cudaStream_t s) {
+    const int nI = A.nI;
+    GridP* gp = nullptr;
+    BoxI *tbox = nullptr, *ebox = nullptr;
+    if (int r = surface_boxes(A, W, X, gp, tbox, ebox, s)) return r;
+    uint32_t* hp = W.pinned();
+    if (!hp || W[W_CAND_CNT].ensure(64)) return IDP_ERR_CUDA;
+    unsigned int* ccount = W[W_CAND_CNT].as<unsigned int>();
+    long cap = std::max<long>(W.isect_cap, 1024);
+    for (int attempt = 0; attempt < 6; ++attempt) {
+        BoxGrid gt, ge;
+        IDP_CUDA_TRY(cudaMemsetAsync(ccount, 0, 3 * sizeof(unsigned int), s));
+        IDP_CUDA_TRY(cudaMemsetAsync(inst_count, 0, sizeof(unsigned int) * nI, s));
+        if (int r = grids_build(W, 0, tbox, A.St, A.st_inst, ebox, A.Se, A.se_inst, A.active, gp, nI, ccount + 2, gt,
+                                ge, s))
+            return r;
+        if (W[W_CAND].ensure(sizeof(Cand) * cap)) return IDP_ERR_CUDA;
+        Cand* out = W[W_CAND].as<Cand>();
+        if (A.St)
+            (::idp::count_launch(),
+             k_query_tri_edges<<<grid_for(kQueryLanes * A.St), kBlock, 0, s>>>(
+                 A.St, A.stri, A.st_inst, A.active, X, A.dbc, A.sedge, tbox, ebox, gp, ge.cells, ge.cell_start,
+                 ge.entries, out, ccount, cap, inst_count));
+        IDP_CUDA_TRY(cudaMemcpyAsync(hp + 2, ccount, 3 * sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
+        IDP_CUDA_TRY(cudaStreamSynchronize(s));
+        if (grids_overflowed(W, 0, hp[4])) continue;
+        const long n = hp[2];
+        if (n > cap) {
+            cap = n + n / 2 + 1024;
+            W.isect_cap = cap;
+            continue;
+        }
+        *pairs = reinterpret_cast<const int2*>(out);
+        *npairs = n;
+        return IDP_OK;
     }
     return IDP_ERR_CAPACITY;
 }

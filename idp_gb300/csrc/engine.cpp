@@ -167,7 +167,7 @@ void build_chunks(const std::vector<int>& off, std::vector<Chunk>& ch, std::vect
 
 // per-instance device scalar layout inside ctx->inst_buf
 enum { S_ETET, S_EINERT, S_EBAR, S_MIND, S_NORM2, S_TOL, S_NUMD };
-enum { SI_BAD, SI_BADB, SI_KFLAG, SI_CCDF, S_NUMI };
+enum { SI_BAD, SI_BADB, SI_KFLAG, SI_CCDF, SI_ISECT, S_NUMI };
 
 double* dsc(idp_ctx* c, int k) { return c->inst_buf.as<double>() + (long)k * c->A.nI; }
 int* isc(idp_ctx* c, int k) { return reinterpret_cast<int*>(c->inst_buf.as<double>() + (long)S_NUMD * c->A.nI) + (long)k * c->A.nI; }
@@ -319,6 +319,7 @@ void idp_default_params(idp_params* p) {
     p->pcg_grid_min_vertices = 0;
     p->pcg_grid_cta_vertices = 0;
     p->contact_block_vertices = 0;
+    p->verify_iterates = 0;
 }
 
 const char* idp_status_str(int s) {
@@ -333,6 +334,7 @@ const char* idp_status_str(int s) {
         case IDP_ERR_NONPOSITIVE_DIST: return "non-positive constraint distance";
         case IDP_ERR_STATE: return "call out of order";
         case IDP_WARN_ITER_CAP: return "ACCD iteration cap reached (step still conservative)";
+        case IDP_ERR_INTERSECTION: return "accepted iterate has an edge-triangle intersection";
         default: return "unknown status";
     }
 }
@@ -915,6 +917,22 @@ int idp_advance(idp_ctx* c, idp_result* results) {
         for (int i = 0; i < nI; ++i)
             if (mask[i] && acc_trial[i] != last_trial) fresh = false;
         if (!fresh && (rc = build_cs(A.X))) return rc;
+        // exact intersection check of every accepted iterate (optional)
+        if (c->P.verify_iterates) {
+            const int2* pairs = nullptr;
+            long npairs = 0;
+            unsigned int* cnt = reinterpret_cast<unsigned int*>(isc(c, SI_ISECT));
+            if ((rc = edge_tri_intersections(A, W, A.X, cnt, &pairs, &npairs, s))) return rc;
+            if ((rc = fetch(c, isc(c, SI_ISECT), hi))) return rc;
+            for (int i = 0; i < nI; ++i) {
+                if (!mask[i]) continue;
+                W.stats.verify_checks += 1;
+                if (hi[i] != 0) {
+                    W.stats.verify_failures += 1;
+                    st[i].status = IDP_ERR_INTERSECTION;
+                }
+            }
+        }
         for (int i = 0; i < nI; ++i)
             if (mask[i]) {
                 st[i].Eprev = Eacc[i];
@@ -966,7 +984,9 @@ int idp_advance(idp_ctx* c, idp_result* results) {
             if (S.use_gd) L2m = c->P.newton_tol * 10;
             // switch to gradient descent after a vanishing step (IMPLICIT_EULER.h:682-699)
             S.use_gd = (S.alpha < 1e-8 && S.feasible_alpha > 1e-8);
-            if (S.status == IDP_ERR_ZERO_STEP || S.status == IDP_ERR_NONPOSITIVE_DIST) S.active = false;
+            if (S.status == IDP_ERR_ZERO_STEP || S.status == IDP_ERR_NONPOSITIVE_DIST ||
+                S.status == IDP_ERR_INTERSECTION)
+                S.active = false;
             else if (S.nres == 3 && L2m <= c->P.newton_tol) S.active = false;
             else if (S.iters >= c->P.max_newton) {
                 S.active = false;
@@ -1197,6 +1217,61 @@ int idp_constraint_set(idp_ctx* c, int i, const double* X, int cap, int32_t* con
             }
         }
     }
+    return IDP_OK;
+}
+
+int idp_check_intersection(idp_ctx* c, int i, const double* X, int cap, int32_t* pairs, int* count) {
+    if (!c || !c->committed) return IDP_ERR_STATE;
+    if (i < 0 || i >= c->A.nI || cap < 0) return IDP_ERR_INVALID_ARG;
+    int rc;
+    const double* Xp = c->A.X;
+    if (X) {
+        if ((rc = prep_one(c, i, X))) return rc;
+        Xp = c->A.Xprev;
+    } else {
+        cudaSetDevice(c->P.device);
+        std::vector<unsigned char> m(c->A.nI, 0);
+        m[i] = 1;
+        if ((rc = set_mask(c, m))) return rc;
+    }
+    const int2* dp = nullptr;
+    long n = 0;
+    if ((rc = edge_tri_intersections(c->A, c->W, Xp, reinterpret_cast<unsigned int*>(isc(c, SI_ISECT)), &dp, &n,
+                                     c->s)))
+        return rc;
+    if (count) *count = (int)n;
+    if (n > cap) return IDP_ERR_CAPACITY;
+    if (n > 0 && pairs) {
+        std::vector<int32_t> h(2 * n);
+        IDP_CUDA_TRY(cudaMemcpyAsync(h.data(), dp, sizeof(int2) * n, cudaMemcpyDeviceToHost, c->s));
+        IDP_CUDA_TRY(cudaStreamSynchronize(c->s));
+        const int t0 = c->A.st_off[i], e0 = c->A.se_off[i];
+        std::vector<std::pair<int, int>> v(n);
+        for (long k = 0; k < n; ++k) v[k] = {h[2 * k] - t0, h[2 * k + 1] - e0};
+        std::sort(v.begin(), v.end());
+        for (long k = 0; k < n; ++k) {
+            pairs[2 * k] = v[k].first;
+            pairs[2 * k + 1] = v[k].second;
+        }
+    }
+    return IDP_OK;
+}
+
+int idp_check_intersection_all(idp_ctx* c, int32_t* counts) {
+    if (!c || !c->committed) return IDP_ERR_STATE;
+    if (!counts) return IDP_ERR_INVALID_ARG;
+    cudaSetDevice(c->P.device);
+    int rc;
+    std::vector<unsigned char> m(c->A.nI, 1);
+    if ((rc = set_mask(c, m))) return rc;
+    const int2* dp = nullptr;
+    long n = 0;
+    if ((rc = edge_tri_intersections(c->A, c->W, c->A.X, reinterpret_cast<unsigned int*>(isc(c, SI_ISECT)), &dp, &n,
+                                     c->s)))
+        return rc;
+    std::vector<int> h;
+    if ((rc = fetch(c, isc(c, SI_ISECT), h))) return rc;
+    std::copy(h.begin(), h.end(), counts);
     return IDP_OK;
 }
 

@@ -218,6 +218,7 @@ struct Work {
         int max_n = 0;
     } cl;
     long cand_cap_pt = 0, cand_cap_ee = 0;   // candidate list capacities (grown on overflow)
+    long isect_cap = 0;                      // intersecting-pair list capacity
     long ccd_cap_pt = 0, ccd_cap_ee = 0;
     // dense cell tables of the two broad phases (0: constraint set, 1: CCD):
     // capacities from the last synchronised build, reused without a round trip
@@ -276,6 +277,14 @@ struct ContactSet {
 int build_constraint_set(Arena& A, Work& W, const double* X, ContactSet& cs, cudaStream_t s);
 int constraint_min_dist2(Arena& A, Work& W, const double* X, const int4* cons, const int* cinst, long C,
                          double* dist2, double* inst_min, cudaStream_t s);
+// Edge-triangle intersections of the surfaces of the active instances at X
+// (Check_Edge_Tri_Intersect, FEM/IPC.h:2444-2517, exact predicates):
+// inst_count[nI] (device) receives each instance's number of intersecting
+// pairs; *pairs (device, valid until the next broad phase) the *npairs pairs
+// (arena triangle index, arena edge index) in no particular order.
+// Synchronises the stream.
+int edge_tri_intersections(Arena& A, Work& W, const double* X, unsigned int* inst_count, const int2** pairs,
+                           long* npairs, cudaStream_t s);
 
 // barrier.cu
 int barrier_energy(Arena& A, Work& W, const double* X, const ContactSet& cs, double* inst_E, int* inst_bad,

@@ -32,6 +32,9 @@ extern "C" {
 #define IDP_ERR_NONPOSITIVE_DIST 7  /* barrier at d <= 0 (IPC.h:925-928 exits)    */
 #define IDP_ERR_STATE 8             /* call out of order (e.g. advance before commit) */
 #define IDP_WARN_ITER_CAP 9         /* an ACCD loop hit its cap; step still safe  */
+#define IDP_ERR_INTERSECTION 10     /* an accepted iterate failed the exact
+                                       edge-triangle intersection check (only
+                                       with idp_params.verify_iterates)          */
 
 #define IDP_MODE_FP64 0   /* plain FP64 path: FP64 Hessians, BSR and PCG          */
 #define IDP_MODE_MIXED 1  /* FP32 Hessians/BSR/PCG + FP64 residual refinement   */
@@ -55,6 +58,13 @@ typedef struct idp_params {
     int contact_block_vertices; /* largest group of contact-coupled vertices the
                              preconditioner inverts as one dense block (2..192);
                              0 = default (192)                                        */
+    int verify_iterates;  /* nonzero: after every accepted Newton step, check each
+                             instance's surface for edge-triangle intersections with
+                             exact predicates (Check_Edge_Tri_Intersect,
+                             FEM/IPC.h:2444-2517, which the reference keeps as a
+                             diagnostic); an instance that fails stops with
+                             IDP_ERR_INTERSECTION. Positive tet volumes are already
+                             enforced by the line search. 0 = off (default)          */
 } idp_params;
 
 typedef struct idp_result {
@@ -87,6 +97,8 @@ typedef struct idp_stats {
     double barrier_ms;      /* barrier gradient / Hessian kernels                 */
     double assembly_ms;     /* BSR assembly and contact-block factorisation       */
     int fp64_fallbacks;     /* mixed-mode directions re-solved in FP64            */
+    long long verify_checks;   /* iterates checked for intersections (verify_iterates) */
+    long long verify_failures; /* of those, iterates with an intersecting pair      */
 } idp_stats;
 
 /* Defaults: h=0.1, newton_tol=1e-3, max_newton=2000, mode=MIXED,
@@ -192,6 +204,19 @@ int idp_ccd_stepsize(idp_ctx* ctx, int inst, const double* X, const double* dir,
  * Compute_IncPotential_Hessian, INC_POTENTIAL.h:277-395) times a vector:
  * y = H x (3V). Uses the precision of the context's mode. */
 int idp_hessian_apply(idp_ctx* ctx, int inst, const double* X, const double* x, double* y);
+
+/* Edge-triangle intersections of instance inst's surface at X (V x 3; NULL =
+ * the instance's current state): Check_Edge_Tri_Intersect (FEM/IPC.h:2444-2517)
+ * with segTriIntersect (FEM/IPC.h:2390-2442) decided by exact orientation
+ * predicates. Pairs are (triangle, edge) indices into the idp_get_surface
+ * lists, sorted; *count receives their number, at most cap are written
+ * (IDP_ERR_CAPACITY if cap is too small). 0 pairs = intersection-free. */
+int idp_check_intersection(idp_ctx* ctx, int inst, const double* X, int cap, int32_t* pairs, int* count);
+
+/* The same check on every instance at its current state; counts[i] receives
+ * instance i's number of intersecting pairs (no counterpart in the reference,
+ * which checks one mesh per call). */
+int idp_check_intersection_all(idp_ctx* ctx, int32_t* counts);
 
 /* Solve H p = -g at X with the context's PCG (mixed or FP64); returns PCG
  * iterations in *iters and the final relative residual in *relres. */

@@ -1104,4 +1104,134 @@ void ora_normal_flow(int V, int nT, const int* tris, const double* X, double ste
     }
 }
 
+// ---------------------------------------------------------------------------
+// Intersection check: Check_Edge_Tri_Intersect (FEM/IPC.h:2444-2517) with
+// segTriIntersect (FEM/IPC.h:2390-2442). The reference decides the plane side
+// with orient3d under USE_PREDICATES and the crossing point with an LU solve;
+// this restatement decides both with exact orientation signs: the segment
+// must cross the plane strictly, and the line through it must pass no
+// triangle edge on the outside (no two strictly opposite edge orientations).
+// Every triangle is tested against every edge whose AABB overlaps its own
+// (the reference's spatial hash only prunes pairs that cannot intersect),
+// after the reference's exclusions: shared vertex, all five vertices DBC.
+// ---------------------------------------------------------------------------
+}  // extern "C"
+
+namespace {
+
+// exact sign of det[a-d; b-d; c-d]: each difference is split exactly into two
+// doubles (two-difference), the determinant's six signed triple products of
+// differences expand into 48 triple products of doubles, each of which is
+// split exactly into four doubles (fused multiply-add products), and the 192
+// terms are summed into a nonoverlapping expansion whose largest component
+// carries the sign (Shewchuk's grow-expansion, Discrete Comput. Geom. 18, 1997)
+void xsum(double a, double b, double& x, double& y) {
+    x = a + b;
+    double bv = x - a, av = x - bv;
+    y = (a - av) + (b - bv);
+}
+
+void xgrow(std::vector<double>& e, double b) {
+    double q = b;
+    size_t m = 0;
+    for (size_t i = 0; i < e.size(); ++i) {
+        double hh;
+        xsum(q, e[i], q, hh);
+        if (hh != 0.0) e[m++] = hh;
+    }
+    e.resize(m);
+    if (q != 0.0) e.push_back(q);
+}
+
+int exact_orient3d(const double* a, const double* b, const double* c, const double* d) {
+    double D[3][3][2];  // D[row][axis] = (hi, lo) of (p - d)
+    const double* P[3] = {a, b, c};
+    for (int r = 0; r < 3; ++r)
+        for (int k = 0; k < 3; ++k) {
+            double x = P[r][k] - d[k];
+            double bv = P[r][k] - x, av = x + bv;
+            D[r][k][0] = x;
+            D[r][k][1] = (P[r][k] - av) + (bv - d[k]);
+        }
+    static const int perm[6][3] = {{0, 1, 2}, {1, 2, 0}, {2, 0, 1}, {0, 2, 1}, {2, 1, 0}, {1, 0, 2}};
+    static const double sgn[6] = {1, 1, 1, -1, -1, -1};
+    std::vector<double> e;
+    e.reserve(200);
+    for (int p = 0; p < 6; ++p)
+        for (int i = 0; i < 2; ++i)
+            for (int j = 0; j < 2; ++j)
+                for (int k = 0; k < 2; ++k) {
+                    const double u = D[0][perm[p][0]][i], v = D[1][perm[p][1]][j], w = D[2][perm[p][2]][k];
+                    const double x = u * v, y = std::fma(u, v, -x);
+                    const double x1 = x * w, y1 = std::fma(x, w, -x1);
+                    const double x2 = y * w, y2 = std::fma(y, w, -x2);
+                    xgrow(e, sgn[p] * y2);
+                    xgrow(e, sgn[p] * x2);
+                    xgrow(e, sgn[p] * y1);
+                    xgrow(e, sgn[p] * x1);
+                }
+    if (e.empty()) return 0;
+    return e.back() > 0 ? 1 : -1;
+}
+
+bool seg_tri_exact(const double* e0, const double* e1, const double* t0, const double* t1, const double* t2) {
+    int o0 = exact_orient3d(t0, t1, t2, e0), o1 = exact_orient3d(t0, t1, t2, e1);
+    if (o0 == 0 || o1 == 0 || o0 == o1) return false;
+    int s[3] = {exact_orient3d(e0, e1, t0, t1), exact_orient3d(e0, e1, t1, t2), exact_orient3d(e0, e1, t2, t0)};
+    bool pos = false, neg = false;
+    for (int k = 0; k < 3; ++k) {
+        pos |= s[k] > 0;
+        neg |= s[k] < 0;
+    }
+    return !(pos && neg);
+}
+
+}  // namespace
+
+extern "C" {
+
+int ora_orient3d(const double* a, const double* b, const double* c, const double* d) {
+    return exact_orient3d(a, b, c, d);
+}
+
+// Writes up to cap (triangle, edge) pairs, sorted; returns their number.
+long ora_edge_tri_intersections(int nT, const int* tris, int nE, const int* edges, const double* X,
+                                const unsigned char* dbc, long cap, int* pairs) {
+    std::vector<double> emin(3 * (size_t)nE), emax(3 * (size_t)nE);
+    for (int e = 0; e < nE; ++e)
+        for (int k = 0; k < 3; ++k) {
+            emin[3 * e + k] = std::min(X[3 * edges[2 * e] + k], X[3 * edges[2 * e + 1] + k]);
+            emax[3 * e + k] = std::max(X[3 * edges[2 * e] + k], X[3 * edges[2 * e + 1] + k]);
+        }
+    std::vector<std::vector<int>> hit(nT);
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int f = 0; f < nT; ++f) {
+        const int* t = tris + 3 * f;
+        double tmin[3], tmax[3];
+        for (int k = 0; k < 3; ++k) {
+            tmin[k] = std::min(std::min(X[3 * t[0] + k], X[3 * t[1] + k]), X[3 * t[2] + k]);
+            tmax[k] = std::max(std::max(X[3 * t[0] + k], X[3 * t[1] + k]), X[3 * t[2] + k]);
+        }
+        for (int e = 0; e < nE; ++e) {
+            const int a = edges[2 * e], b = edges[2 * e + 1];
+            if (a == t[0] || a == t[1] || a == t[2] || b == t[0] || b == t[1] || b == t[2]) continue;
+            if (dbc[a] && dbc[b] && dbc[t[0]] && dbc[t[1]] && dbc[t[2]]) continue;
+            bool sep = false;
+            for (int k = 0; k < 3; ++k) sep |= emax[3 * e + k] < tmin[k] || emin[3 * e + k] > tmax[k];
+            if (sep) continue;
+            if (seg_tri_exact(X + 3 * a, X + 3 * b, X + 3 * t[0], X + 3 * t[1], X + 3 * t[2])) hit[f].push_back(e);
+        }
+    }
+    long n = 0;
+    for (int f = 0; f < nT; ++f)
+        for (int e : hit[f]) {
+            if (n < cap) {
+                pairs[2 * n] = f;
+                pairs[2 * n + 1] = e;
+            }
+            ++n;
+        }
+    return n;
+}
+
 }  // extern "C"

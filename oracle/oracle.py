@@ -55,6 +55,9 @@ def lib():
         L.ora_type_ee.restype = C.c_int
         L.ora_dist_pt_unclassified.restype = C.c_double
         L.ora_dist_ee_unclassified.restype = C.c_double
+        L.ora_orient3d.restype = C.c_int
+        L.ora_edge_tri_intersections.restype = C.c_long
+        L.ora_edge_tri_intersections.argtypes = [C.c_int, _ip, C.c_int, _ip, _dp, _up, C.c_long, _ip]
         _lib = L
     return _lib
 
@@ -175,6 +178,27 @@ def ccd_stepsize(X, dirn, surf, dbc, alpha=1.0, thickness=0.0):
                                 surf["tris"].shape[0], _i(surf["tris"]), _u(dbc), _d(f64(X)), _d(f64(dirn)),
                                 C.c_double(thickness), C.byref(a))
     return a.value, rc
+
+
+def orient3d(a, b, c, d):
+    """Exact sign of det[a-d; b-d; c-d]."""
+    return lib().ora_orient3d(_d(f64(a)), _d(f64(b)), _d(f64(c)), _d(f64(d)))
+
+
+def edge_tri_intersections(X, surf, dbc=None):
+    """Intersecting (triangle, edge) pairs of a surface at X, sorted
+    (Check_Edge_Tri_Intersect, FEM/IPC.h:2444-2517, exact predicates)."""
+    tris, edges = i32(surf["tris"]), i32(surf["edges"])
+    X = f64(X)
+    dbc = np.zeros(X.shape[0], np.uint8) if dbc is None else np.ascontiguousarray(dbc, np.uint8)
+    cap = 1024
+    while True:
+        out = np.zeros((cap, 2), np.int32)
+        n = lib().ora_edge_tri_intersections(tris.shape[0], _i(tris), edges.shape[0], _i(edges), _d(X), _u(dbc), cap,
+                                             _i(out))
+        if n <= cap:
+            return out[:n].copy()
+        cap = n
 
 
 def kappa_init(mean_mass_diag, dHat2, stiff_mult=1.0):
