@@ -56,7 +56,13 @@ def parse():
     ap.add_argument("--steps", type=int, default=17)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="blob", choices=["blob", "batch256", "bar"])
+    ap.add_argument("--workload", default="blob", choices=["blob", "batch256", "bar", "serve"])
+    ap.add_argument("--rate", type=float, default=200.0, help="serve: Poisson arrival rate (jobs/s)")
+    ap.add_argument("--duration", type=float, default=4.0, help="serve: seconds of arrivals")
+    ap.add_argument("--serve-workers", type=int, default=4)
+    ap.add_argument("--serve-batch", type=int, default=8)
+    ap.add_argument("--hbm-budget-gb", type=float, default=150.0)
+    ap.add_argument("--serve-newton-cap", type=int, default=30)
     ap.add_argument("--blob-n", type=int, default=64)
     ap.add_argument("--flow-step", type=float, default=0.05)
     ap.add_argument("--no-fp64", action="store_true")
@@ -430,6 +436,10 @@ def run_reference(args):
     rank, world, local = dist_env()
     if rank != 0:
         return
+    if args.workload == "serve":
+        print(json.dumps({"impl": "reference", "unavailable": "the reference has no request server (one scene per "
+                          "Python call); its CPU path is timed on the blob and batch workloads"}))
+        return
     vals = []
     bl = None
     if args.workload == "blob":
@@ -632,10 +642,149 @@ def fp64_one_at_a_time(idp, probs, results, sample, max_newton, budget, device):
     return out
 
 
+def serve_pool(seed=0):
+    """Config-4 style job pool: 8 bars (tet counts log-uniform in [2k, 50k],
+    bend U[1.5pi, 2.5pi], the config-0 target) and 8 blobs (tet counts
+    log-uniform in [2k, 100k], one normal-flow step of 0.05)."""
+    import numpy as np
+    from idp_gb300 import meshgen
+    from idp_gb300.api import initialize_oipc
+
+    rng = np.random.default_rng(seed)
+    pool = []
+    for it in meshgen.bar_batch(8, 2_000, 50_000, seed=seed):
+        pool.append(dict(kind="bar", X=it["X"], tets=it["tets"], v=(it["target"] - it["X"]) / 0.1, flow=0.0))
+    for k in range(8):
+        t = math.exp(rng.uniform(math.log(2_000), math.log(100_000)))
+        n = max(8, int(round((t / 0.84) ** (1.0 / 3.0))))
+        X, tets, _ = meshgen.blob(n=n, lmax=8, amp=0.3, seed=seed * 100 + k)
+        pool.append(dict(kind="blob", X=X, tets=tets, v=None, flow=0.05))
+    for p in pool:
+        X, tets = p["X"], p["tets"]
+        p["mass"] = meshgen.lumped_mass(X, tets, 1000.0)
+        p["lam"], p["mu"] = meshgen.lame(1e4, 0.3)
+        diag = float(np.linalg.norm(X.max(0) - X.min(0)))
+        p["dHat2"] = (1e-3 * diag) ** 2
+        p["kappa"], p["kappa_max"] = initialize_oipc(float(p["mass"].mean()), p["dHat2"])
+    return pool
+
+
+def run_serve(args):
+    """Served request stream (config 4, scaled): Poisson arrivals at --rate for
+    --duration seconds, each a job drawn from serve_pool(); the continuous-
+    batching server (idp_server_*) solves them in mixed precision. The
+    reference point is the plain FP64 path one job at a time: every pool
+    job's FP64 service time is measured once and the same arrival sequence is
+    replayed through a single FIFO server."""
+    import numpy as np
+    import torch
+    import idp_gb300 as idp
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    pool = serve_pool(seed=rank)
+    rng = np.random.default_rng(1000 + rank)
+    arr, t = [], 0.0
+    while True:
+        t += rng.exponential(1.0 / args.rate)
+        if t > args.duration:
+            break
+        arr.append((t, int(rng.integers(len(pool)))))
+    params = dict(h=0.1, newton_tol=1e-3, max_newton=args.serve_newton_cap, device=local)
+    # FP64 one at a time: service time of every pool job (wall time of one
+    # context's add + commit + solve + read back, after a warm-up solve)
+    svc, e64 = [], []
+    for p in pool:
+        for rep in range(2):
+            t0 = time.perf_counter()
+            c = idp.Context(mode=idp.MODE_FP64, **params)
+            c.add_instance(p["X"], p["tets"], p["mass"], p["lam"], p["mu"], p["dHat2"], p["kappa"], p["kappa_max"])
+            if p["v"] is not None:
+                c.set_velocity(0, p["v"])
+            c.commit()
+            if p["flow"]:
+                c.set_normal_flow(0, p["flow"])
+            _, r = c.advance(check=False)
+            c.state(0)
+            c.close()
+            dt = time.perf_counter() - t0
+        svc.append(dt)
+        e64.append(r[0])
+    t_free, lat64 = 0.0, []
+    for ta, k in arr:
+        start = max(ta, t_free)
+        t_free = start + svc[k]
+        lat64.append(t_free - ta)
+    thr64 = len(arr) / (t_free - arr[0][0]) if arr else 0.0
+    # warm-up of the server's worker contexts on the pool, then the stream
+    srv = idp.Server(args.hbm_budget_gb * 1e9, workers=args.serve_workers, max_batch=args.serve_batch,
+                     mode=idp.MODE_MIXED, **params)
+
+    def submit(p):
+        return srv.submit(p["X"], p["tets"], p["mass"], p["lam"], p["mu"], p["dHat2"], p["kappa"], p["kappa_max"],
+                          v=p["v"], normal_flow=p["flow"])
+
+    for _ in range(max(1, args.warmup)):
+        for jid in [submit(p) for p in pool]:
+            srv.wait(jid)
+    ids = []
+    with ClockSampler(local) as clocks:
+        t0 = time.perf_counter()
+        for ta, k in arr:
+            d = ta - (time.perf_counter() - t0)
+            if d > 0:
+                time.sleep(d)
+            ids.append((submit(pool[k]), k))
+        srv.drain()
+    infos = [(srv.wait(j)[0], k) for j, k in ids]
+    st = srv.stats()
+    srv.close()
+    lat = [i["done_ms"] - i["submit_ms"] for i, _ in infos]
+    span_s = (max(i["done_ms"] for i, _ in infos) - min(i["submit_ms"] for i, _ in infos)) / 1000.0
+    thr = len(infos) / span_s
+    status, rel = {}, []
+    for i, k in infos:
+        status[str(i["status"])] = status.get(str(i["status"]), 0) + 1
+        r64 = e64[k]
+        if i["status"] == idp.IDP_OK and r64["status"] == idp.IDP_OK:
+            rel.append(abs(i["result"]["energy"] - r64["energy"]) / abs(r64["energy"]))
+    if rank != 0:
+        return
+    kinds = {"bar": sum(1 for _, k in arr if pool[k]["kind"] == "bar"),
+             "blob": sum(1 for _, k in arr if pool[k]["kind"] == "blob")}
+    out = {
+        "metric": METRIC + " (served request stream)", "value": thr, "unit": UNIT, "n_gpus": 1,
+        "steps": len(infos), "warmup": args.warmup, "ms_per_step": 1000.0 / thr if thr else None,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+        "config": {"workload": f"serve: Poisson arrivals {args.rate:g}/s for {args.duration:g} s, jobs drawn from "
+                               "8 bars (2k-50k tets, bend U[1.5pi,2.5pi]) and 8 blobs (2k-100k tets, one normal-flow "
+                               f"step 0.05), Newton cap {args.serve_newton_cap} per job",
+                   "jobs": len(infos), "kinds": kinds, "workers": args.serve_workers, "max_batch": args.serve_batch,
+                   "hbm_budget_gb": args.hbm_budget_gb, "l2": "no flush; jobs are independent solves"},
+        "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
+        "status_counts": status,
+        "server": st,
+        "fp64_one_at_a_time": {"value": thr64, "unit": UNIT,
+                               "latency_ms": {"p50": 1000 * float(np.percentile(lat64, 50)),
+                                              "p99": 1000 * float(np.percentile(lat64, 99))},
+                               "basis": "FIFO replay of the same arrivals with each pool job's measured FP64 "
+                                        "service time (one context per job)"},
+        "served_over_fp64_one_at_a_time": thr / thr64 if thr64 else None,
+        "rel_energy_diff_vs_fp64": {"max": max(rel) if rel else None, "converged_jobs": len(rel)},
+        "e2e": {"value": thr, "unit": UNIT,
+                "h2d_bytes_per_step": float(np.mean([pool[k]["X"].size * 8 * 2 for _, k in arr])),
+                "d2h_bytes_per_step": float(np.mean([pool[k]["X"].size * 8 * 2 for _, k in arr]))},
+        "clocks": clocks.summary(),
+    }
+    print(json.dumps(out))
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "serve":
+        run_serve(args)
     elif args.workload == "blob":
         run_flow(args)
     else:

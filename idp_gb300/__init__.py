@@ -37,7 +37,9 @@ EXPORTS = [
     "idp_eval_energy", "idp_eval_gradient", "idp_constraint_set", "idp_ccd_stepsize", "idp_hessian_apply",
     "idp_newton_direction", "idp_get_stats", "idp_save_state", "idp_restore_state",
     "idp_set_normal_flow", "idp_set_kappa", "idp_tet_energy_noalloc", "idp_check_intersection",
-    "idp_check_intersection_all",
+    "idp_check_intersection_all", "idp_reset", "idp_device_bytes", "idp_job_footprint", "idp_server_create",
+    "idp_server_create_simulated", "idp_server_submit", "idp_server_wait", "idp_server_drain",
+    "idp_server_get_stats", "idp_server_destroy",
 ]
 
 
@@ -63,6 +65,31 @@ class Stats(C.Structure):
                 ("total_ms", C.c_double), ("kernel_launches", C.c_longlong), ("barrier_ms", C.c_double),
                 ("assembly_ms", C.c_double), ("fp64_fallbacks", C.c_int), ("verify_checks", C.c_longlong),
                 ("verify_failures", C.c_longlong)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class JobDesc(C.Structure):
+    _fields_ = [("V", C.c_int), ("X", C.c_void_p), ("X0", C.c_void_p), ("T", C.c_int), ("tets", C.c_void_p),
+                ("mass", C.c_void_p), ("lam", C.c_void_p), ("mu", C.c_void_p), ("nDBC", C.c_int),
+                ("dbc_idx", C.c_void_p), ("dHat2", C.c_double), ("kappa", C.c_double), ("kappa_max", C.c_double),
+                ("v", C.c_void_p), ("normal_flow", C.c_double), ("X_out", C.c_void_p), ("v_out", C.c_void_p)]
+
+
+class JobInfo(C.Structure):
+    _fields_ = [("status", C.c_int), ("result", Result), ("submit_ms", C.c_double), ("admit_ms", C.c_double),
+                ("done_ms", C.c_double), ("cohort", C.c_int), ("cohort_size", C.c_int), ("footprint", C.c_double)]
+
+    def as_dict(self):
+        d = {k: getattr(self, k) for k, _ in self._fields_ if k != "result"}
+        d["result"] = self.result.as_dict()
+        return d
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_longlong), ("completed", C.c_longlong), ("cohorts", C.c_longlong),
+                ("peak_resident", C.c_double), ("peak_concurrency", C.c_int), ("device_bytes", C.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -116,6 +143,19 @@ def load(path: str | None = None):
     L.idp_get_stats.argtypes = [C.c_void_p, C.POINTER(Stats)]
     L.idp_check_intersection.argtypes = [C.c_void_p, C.c_int, _dp, C.c_int, _ip, C.POINTER(C.c_int)]
     L.idp_check_intersection_all.argtypes = [C.c_void_p, _ip]
+    L.idp_reset.argtypes = [C.c_void_p]
+    L.idp_device_bytes.argtypes = [C.c_void_p, C.POINTER(C.c_size_t)]
+    L.idp_job_footprint.restype = C.c_double
+    L.idp_job_footprint.argtypes = [C.c_int, C.c_int]
+    L.idp_server_create.restype = C.c_void_p
+    L.idp_server_create.argtypes = [C.POINTER(Params), C.c_double, C.c_int, C.c_int, C.POINTER(C.c_int)]
+    L.idp_server_create_simulated.restype = C.c_void_p
+    L.idp_server_create_simulated.argtypes = [C.c_double, C.c_int, C.c_int, C.c_double, C.POINTER(C.c_int)]
+    L.idp_server_submit.argtypes = [C.c_void_p, C.POINTER(JobDesc)]
+    L.idp_server_wait.argtypes = [C.c_void_p, C.c_int, C.POINTER(JobInfo)]
+    L.idp_server_drain.argtypes = [C.c_void_p]
+    L.idp_server_get_stats.argtypes = [C.c_void_p, C.POINTER(ServerStats)]
+    L.idp_server_destroy.argtypes = [C.c_void_p]
     L.idp_save_state.argtypes = [C.c_void_p]
     L.idp_restore_state.argtypes = [C.c_void_p]
     _lib = L
@@ -218,6 +258,17 @@ class Context:
     def commit(self):
         self._check(load().idp_commit(self._h), "idp_commit")
         self.committed = True
+
+    def reset(self):
+        """Drop the instances, keep the device buffers for the next set."""
+        self._check(load().idp_reset(self._h), "idp_reset")
+        self._V = []
+        self.committed = False
+
+    def device_bytes(self):
+        n = C.c_size_t()
+        self._check(load().idp_device_bytes(self._h, C.byref(n)), "idp_device_bytes")
+        return n.value
 
     def advance(self, check=True):
         res = (Result * len(self._V))()
@@ -333,3 +384,80 @@ class Context:
         self._check(load().idp_newton_direction(self._h, i, _pd(X), _pd(p), C.byref(it), C.byref(rel)),
                     "idp_newton_direction")
         return p, it.value, rel.value
+
+
+def job_footprint(V, T):
+    """Admission estimate (bytes) of one job's device memory."""
+    return load().idp_job_footprint(int(V), int(T))
+
+
+class Server:
+    """Continuous-batching request server (idp_server_*): jobs queue in
+    arrival order; worker threads, each with its own context and stream,
+    admit cohorts under the memory budget and solve them concurrently."""
+
+    def __init__(self, hbm_budget, workers=2, max_batch=8, simulated_ms_per_kvertex=None, **params):
+        L = load()
+        st = C.c_int()
+        if simulated_ms_per_kvertex is not None:
+            self._h = L.idp_server_create_simulated(float(hbm_budget), int(workers), int(max_batch),
+                                                    float(simulated_ms_per_kvertex), C.byref(st))
+        else:
+            p = default_params(**params)
+            self._h = L.idp_server_create(C.byref(p), float(hbm_budget), int(workers), int(max_batch), C.byref(st))
+        if not self._h:
+            raise IDPError(st.value, "idp_server_create")
+        self._keep = {}
+
+    def submit(self, X, tets, mass, lam, mu, dHat2, kappa, kappa_max, v=None, normal_flow=0.0, X0=None,
+               dbc_idx=None):
+        """Queue one job; returns its id. Output buffers are kept until wait()."""
+        X, tets, mass = _f64(X).reshape(-1, 3), _i32(tets).reshape(-1, 4), _f64(mass)
+        V, T = X.shape[0], tets.shape[0]
+        lam = _f64(np.broadcast_to(lam, (T,)))
+        mu = _f64(np.broadcast_to(mu, (T,)))
+        X0 = None if X0 is None else _f64(X0).reshape(-1, 3)
+        v = None if v is None else _f64(v).reshape(-1, 3)
+        dbc = None if dbc_idx is None else _i32(dbc_idx)
+        Xo, vo = np.zeros((V, 3)), np.zeros((V, 3))
+        ptr = lambda a: None if a is None else a.ctypes.data
+        d = JobDesc(V, ptr(X), ptr(X0), T, ptr(tets), ptr(mass), ptr(lam), ptr(mu), 0 if dbc is None else dbc.size,
+                    ptr(dbc), float(dHat2), float(kappa), float(kappa_max), ptr(v), float(normal_flow), ptr(Xo),
+                    ptr(vo))
+        jid = load().idp_server_submit(self._h, C.byref(d))
+        if jid < 0:
+            raise IDPError(-jid, "idp_server_submit")
+        self._keep[jid] = (Xo, vo)
+        return jid
+
+    def wait(self, jid):
+        """Block until job jid completes: (info dict, X, v)."""
+        info = JobInfo()
+        rc = load().idp_server_wait(self._h, int(jid), C.byref(info))
+        if rc:
+            raise IDPError(rc, "idp_server_wait")
+        Xo, vo = self._keep.pop(jid)
+        return info.as_dict(), Xo, vo
+
+    def drain(self):
+        rc = load().idp_server_drain(self._h)
+        if rc:
+            raise IDPError(rc, "idp_server_drain")
+
+    def stats(self):
+        st = ServerStats()
+        rc = load().idp_server_get_stats(self._h, C.byref(st))
+        if rc:
+            raise IDPError(rc, "idp_server_get_stats")
+        return st.as_dict()
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().idp_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -24,8 +24,8 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relax
           "-Xcompiler", "-Wall", "-Xcompiler", "-Wno-unused-function", "-I", INCLUDE]
 EXACT_FP64 = {"contact.cu", "ccd.cu", "flow.cu"}
 UNITS = ["prims.cu", "tet.cu", "contact.cu", "barrier.cu", "ccd.cu", "solver.cu", "precond.cu", "vecops.cu",
-         "flow.cu", "engine.cpp"]
-HEADERS = ["common.cuh", "prims.cuh", "geom.cuh", "grid.cuh", "engine.hpp"]
+         "flow.cu", "engine.cpp", "server.cpp"]
+HEADERS = ["common.cuh", "prims.cuh", "geom.cuh", "grid.cuh", "engine.hpp", "predicates.cuh"]
 
 
 def nvcc():
@@ -65,7 +65,7 @@ def build(verbose=False, extra=()):
         raise RuntimeError("nvcc failed:\n" + "\n".join(errs))
     objs = [o for o, _ in results]
     if not os.path.exists(LIB) or os.path.getmtime(LIB) < max(os.path.getmtime(o) for o in objs):
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lpthread"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

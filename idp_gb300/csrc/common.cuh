@@ -20,7 +20,7 @@ constexpr int kBlock = 256;
 
 // host-side count of kernel launches made by this library (every launch
 // site is written as (count_launch(), kernel<<<...>>>(...)))
-extern long long g_launch_count;
+extern thread_local long long g_launch_count;  // per host thread (one thread drives a context at a time)
 inline void count_launch() { ++g_launch_count; }
 
 inline int grid_for(long n, int block = kBlock) {

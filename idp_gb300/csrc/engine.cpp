@@ -22,7 +22,7 @@
 
 using namespace idp;
 
-long long idp::g_launch_count = 0;
+thread_local long long idp::g_launch_count = 0;
 
 int DBuf::ensure(size_t n) {
     if (n <= bytes && p) return 0;
@@ -50,7 +50,8 @@ struct idp_ctx {
     std::vector<InstState> st;
     Arena A;
     Work W;
-    std::vector<DBuf> owned;  // arena storage
+    std::vector<DBuf> owned;  // arena storage (reused in order by the next commit after idp_reset)
+    size_t owned_next = 0;
     bool committed = false;
     ContactSet cs;
     long prevC = 0;
@@ -65,8 +66,8 @@ namespace {
 
 template <class T>
 int upload(idp_ctx* c, T*& dst, const std::vector<T>& src) {
-    c->owned.emplace_back();
-    DBuf& b = c->owned.back();
+    if (c->owned_next == c->owned.size()) c->owned.emplace_back();
+    DBuf& b = c->owned[c->owned_next++];
     if (b.ensure(sizeof(T) * (src.size() + 1))) return IDP_ERR_CUDA;
     dst = b.as<T>();
     if (!src.empty() && cudaMemcpy(dst, src.data(), sizeof(T) * src.size(), cudaMemcpyHostToDevice) != cudaSuccess)
@@ -372,6 +373,33 @@ void idp_destroy(idp_ctx* c) {
     c->snap.release();
     cudaStreamDestroy(c->s);
     delete c;
+}
+
+int idp_reset(idp_ctx* c) {
+    if (!c) return IDP_ERR_INVALID_ARG;
+    cudaSetDevice(c->P.device);
+    IDP_CUDA_TRY(cudaStreamSynchronize(c->s));
+    c->inst.clear();
+    c->st.clear();
+    c->A = Arena();
+    c->owned_next = 0;
+    c->committed = false;
+    c->cs = ContactSet();
+    c->prevC = 0;
+    c->has_snap = false;
+    c->snap_kappa.clear();
+    c->W.stats = idp_stats{};
+    c->W.dense_ready[0] = c->W.dense_ready[1] = false;
+    return IDP_OK;
+}
+
+int idp_device_bytes(idp_ctx* c, size_t* bytes) {
+    if (!c || !bytes) return IDP_ERR_INVALID_ARG;
+    size_t n = c->inst_buf.bytes + c->vel.bytes + c->snap.bytes;
+    for (const DBuf& b : c->owned) n += b.bytes;
+    for (const DBuf& b : c->W.b) n += b.bytes;
+    *bytes = n;
+    return IDP_OK;
 }
 
 int idp_add_instance(idp_ctx* c, int V, const double* X, const double* X0, int T, const int32_t* tets,

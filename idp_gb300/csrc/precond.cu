@@ -14,6 +14,7 @@
 #include <deque>
 #include <numeric>
 #include <vector>
+#include <atomic>
 #include "engine.hpp"
 
 namespace idp {
@@ -392,11 +393,11 @@ int build_contact_clusters(Arena& A, Work& W, const ContactSet& cs, bool fp64, c
         (::idp::count_launch(), k_cl_gather<double><<<ncl, 256, 0, s>>>(ncl, cl.off, cl.vert, cl.vcl, cl.vloc, cl.doff, A.rowptr, A.colidx,
                                                   W[W_BSR_VAL].as<double>(), trp, tcol, W[W_TAIL_VAL].as<double>(),
                                                   A.dbc, K));
-        static bool attr_d = false;
-        if (!attr_d) {
+        static std::atomic<bool> attr_d{false};
+        if (!attr_d.load()) {
             IDP_CUDA_TRY(cudaFuncSetAttribute(k_cl_invert<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                               (int)invert_smem_bytes<double>()));
-            attr_d = true;
+            attr_d.store(true);
         }
         (::idp::count_launch(), k_cl_invert<double><<<ncl, kInvThreads, invert_smem_bytes<double>(), s>>>(
                                     ncl, cl.off, cl.doff, K, K + cl.dense, okp));
@@ -405,11 +406,11 @@ int build_contact_clusters(Arena& A, Work& W, const ContactSet& cs, bool fp64, c
         (::idp::count_launch(), k_cl_gather<float><<<ncl, 256, 0, s>>>(ncl, cl.off, cl.vert, cl.vcl, cl.vloc, cl.doff, A.rowptr, A.colidx,
                                                  W[W_BSR_VAL].as<float>(), trp, tcol, W[W_TAIL_VAL].as<float>(), A.dbc,
                                                  K));
-        static bool attr_f = false;
-        if (!attr_f) {
+        static std::atomic<bool> attr_f{false};
+        if (!attr_f.load()) {
             IDP_CUDA_TRY(cudaFuncSetAttribute(k_cl_invert<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                               (int)invert_smem_bytes<float>()));
-            attr_f = true;
+            attr_f.store(true);
         }
         (::idp::count_launch(), k_cl_invert<float><<<ncl, kInvThreads, invert_smem_bytes<float>(), s>>>(
                                     ncl, cl.off, cl.doff, K, K + cl.dense, okp));

@@ -13,6 +13,7 @@
 // its own scalars and stops on its own). Mixed mode runs PCG in FP32 and
 // recovers the direction by iterative refinement against an FP64 residual
 // r = b - A x (FP32 matrix, FP64 accumulation); FP64 mode runs PCG in FP64.
+#include <atomic>
 #include <cooperative_groups.h>
 #include "engine.hpp"
 #include "prims.cuh"
@@ -1172,10 +1173,10 @@ static int pcg_inner(Arena& A, Work& W, const double* b, double rel_tol, int max
         std::vector<int> flat;
         for (int k = 0; k < 5; ++k) flat.insert(flat.end(), by_size[k].begin(), by_size[k].end());
         IDP_CUDA_TRY(cudaMemcpyAsync(d_list, flat.data(), sizeof(int) * flat.size(), cudaMemcpyHostToDevice, s));
-        static bool attr_set[2] = {false, false};
-        if (!attr_set[sizeof(T) == 8]) {
+        static std::atomic<bool> attr_set{false};  // one per instantiation
+        if (!attr_set.load()) {
             cudaFuncSetAttribute(k_pcg_cluster<T>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-            attr_set[sizeof(T) == 8] = true;
+            attr_set.store(true);
         }
         ClusterPC<T> pcb;
         pcb.vcl = W.cl.vcl;
@@ -1232,8 +1233,8 @@ static int pcg_inner(Arena& A, Work& W, const double* b, double rel_tol, int max
         return IDP_OK;
     }
     // large instances: grid-wide PCG, in waves of at most gmax CTAs
-    static int gmax_cache[2] = {0, 0};
-    int& gmax = gmax_cache[sizeof(T) == 8];
+    static std::atomic<int> gmax_cache{0};  // one per instantiation
+    int gmax = gmax_cache.load();
     if (!gmax) {
         int dev = 0, nsm = 0, per = 0;
         IDP_CUDA_TRY(cudaGetDevice(&dev));
@@ -1242,6 +1243,7 @@ static int pcg_inner(Arena& A, Work& W, const double* b, double rel_tol, int max
         IDP_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pcg_grid<T>, GP_THREADS, kGridSmem));
         gmax = nsm * per;
         if (gmax <= 0) return IDP_ERR_CUDA;
+        gmax_cache.store(gmax);
     }
     const long vper = W.grid_vper;
     std::vector<GridCta> plan;

@@ -15,6 +15,7 @@
 #ifndef IDP_GB300_H
 #define IDP_GB300_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -205,6 +206,15 @@ int idp_ccd_stepsize(idp_ctx* ctx, int inst, const double* X, const double* dir,
  * y = H x (3V). Uses the precision of the context's mode. */
 int idp_hessian_apply(idp_ctx* ctx, int inst, const double* X, const double* x, double* y);
 
+/* Clear the context's instances so a new set can be added and committed,
+ * keeping its device buffers (grow-only): the next commit and solve reuse them
+ * instead of allocating. No counterpart in the reference, whose simulator
+ * object is built once per scene. */
+int idp_reset(idp_ctx* ctx);
+
+/* Device memory the context holds (arena and work buffers), in bytes. */
+int idp_device_bytes(idp_ctx* ctx, size_t* bytes);
+
 /* Edge-triangle intersections of instance inst's surface at X (V x 3; NULL =
  * the instance's current state): Check_Edge_Tri_Intersect (FEM/IPC.h:2444-2517)
  * with segTriIntersect (FEM/IPC.h:2390-2442) decided by exact orientation
@@ -217,6 +227,92 @@ int idp_check_intersection(idp_ctx* ctx, int inst, const double* X, int cap, int
  * instance i's number of intersecting pairs (no counterpart in the reference,
  * which checks one mesh per call). */
 int idp_check_intersection_all(idp_ctx* ctx, int32_t* counts);
+
+/* ---------------------------------------------------------------------------
+ * Request server: continuous batching of independent solves on one GPU.
+ * No counterpart in the reference, which advances one scene per Python call
+ * (Python/Drivers/FEMDiscreteShellBase.py:333-361).
+ *
+ * Jobs (one mesh and its predictor each) are queued in arrival order. A pool
+ * of worker threads, each driving its own context and CUDA stream, forms a
+ * cohort from the head of the queue whenever it is free: as many jobs as fit
+ * under the memory budget (sum of admitted footprints) and max_batch, solved
+ * together in one arena (idp_advance); cohorts of different workers run on
+ * the device at the same time. A job that arrives while cohorts are running
+ * is admitted by the next free worker as soon as memory allows, so new work
+ * joins the device between the running cohorts' Newton iterations. Worker
+ * contexts keep their buffers between cohorts (idp_reset) while the total
+ * they hold stays under the budget. A job's result does not depend on the
+ * cohort it ran in (per-instance reductions are fixed-order).
+ * ------------------------------------------------------------------------- */
+typedef struct idp_server idp_server;
+
+typedef struct idp_job_desc {
+    int V;                  /* mesh, as idp_add_instance                                */
+    const double* X;
+    const double* X0;       /* rest shape (NULL = X)                                    */
+    int T;
+    const int32_t* tets;
+    const double* mass;
+    const double* lam;      /* T values                                                 */
+    const double* mu;       /* T values                                                 */
+    int nDBC;
+    const int32_t* dbc_idx;
+    double dHat2, kappa, kappa_max;
+    const double* v;        /* initial velocity (3V; NULL = zero): x_tilde = x + h v    */
+    double normal_flow;     /* nonzero: predictor of idp_set_normal_flow(step) instead  */
+    double* X_out;          /* 3V host buffer written when the job completes (or NULL)  */
+    double* v_out;          /* 3V host buffer written when the job completes (or NULL)  */
+} idp_job_desc;
+
+typedef struct idp_job_info {
+    int status;             /* IDP_* of the job                                         */
+    idp_result result;      /* as idp_advance reports it                                */
+    double submit_ms;       /* server clock: ms since idp_server_create                 */
+    double admit_ms;        /* when a worker took it                                    */
+    double done_ms;         /* when its result was written                              */
+    int cohort;             /* id of the cohort it ran in                               */
+    int cohort_size;        /* jobs in that cohort                                      */
+    double footprint;       /* admission estimate, bytes                                */
+} idp_job_info;
+
+typedef struct idp_server_stats {
+    long long submitted, completed, cohorts;
+    double peak_resident;   /* largest sum of admitted footprints                      */
+    int peak_concurrency;   /* most cohorts on the device at once                       */
+    double device_bytes;    /* device memory the worker contexts hold now               */
+} idp_server_stats;
+
+/* Admission estimate of one job's device memory (arena, matrix, solver and
+ * broad-phase buffers), bytes. */
+double idp_job_footprint(int V, int T);
+
+/* p: solver parameters of every job (NULL = defaults); hbm_budget: bytes the
+ * admitted jobs' footprints may sum to; workers: concurrent cohorts (>= 1);
+ * max_batch: jobs per cohort (>= 1). */
+idp_server* idp_server_create(const idp_params* p, double hbm_budget, int workers, int max_batch, int* status);
+
+/* Scheduler only, no device work: a cohort "runs" for ms_per_kvertex per
+ * thousand vertices it holds and every job completes with IDP_OK and its
+ * input positions. For testing admission and scheduling without a GPU. */
+idp_server* idp_server_create_simulated(double hbm_budget, int workers, int max_batch, double ms_per_kvertex,
+                                        int* status);
+
+/* Queue a job (inputs are copied; X_out / v_out must stay valid until the job
+ * completes). Returns the job id (>= 0) or -IDP_ERR_* (a footprint above the
+ * whole budget is IDP_ERR_CAPACITY). Thread-safe. */
+int idp_server_submit(idp_server* s, const idp_job_desc* job);
+
+/* Block until the job completes; info (may be NULL) receives its record. */
+int idp_server_wait(idp_server* s, int job, idp_job_info* info);
+
+/* Block until every submitted job has completed. */
+int idp_server_drain(idp_server* s);
+
+int idp_server_get_stats(idp_server* s, idp_server_stats* out);
+
+/* Finishes the queued jobs, stops the workers and frees their contexts. */
+void idp_server_destroy(idp_server* s);
 
 /* Solve H p = -g at X with the context's PCG (mixed or FP64); returns PCG
  * iterations in *iters and the final relative residual in *relres. */
