@@ -56,7 +56,10 @@ def parse():
     ap.add_argument("--steps", type=int, default=17)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="blob", choices=["blob", "batch256", "bar", "serve"])
+    ap.add_argument("--workload", default="blob", choices=["blob", "batch256", "bar", "serve", "anim"])
+    ap.add_argument("--frames", type=int, default=120, help="anim: keyframes solved")
+    ap.add_argument("--frame-stride", type=int, default=1, help="anim: keyframe step")
+    ap.add_argument("--anim-n", type=int, default=22, help="anim: cells across the cylinder's diameter")
     ap.add_argument("--rate", type=float, default=200.0, help="serve: Poisson arrival rate (jobs/s)")
     ap.add_argument("--duration", type=float, default=4.0, help="serve: seconds of arrivals")
     ap.add_argument("--serve-workers", type=int, default=4)
@@ -436,9 +439,10 @@ def run_reference(args):
     rank, world, local = dist_env()
     if rank != 0:
         return
-    if args.workload == "serve":
-        print(json.dumps({"impl": "reference", "unavailable": "the reference has no request server (one scene per "
-                          "Python call); its CPU path is timed on the blob and batch workloads"}))
+    if args.workload in ("serve", "anim"):
+        print(json.dumps({"impl": "reference", "unavailable": f"{args.workload}: not timed on the CPU port (a "
+                          "300k-tet or served sequence takes hours there); its CPU path is timed on the blob and "
+                          "batch workloads"}))
         return
     vals = []
     bl = None
@@ -779,12 +783,86 @@ def run_serve(args):
     print(json.dumps(out))
 
 
+def run_anim(args):
+    """Animation-fix sequence (config 2): a tet cylinder (radius 0.2, length
+    3) follows keyframes bent by 2.4 pi sin(2 pi t/120) and twisted by
+    pi cos(2 pi t/60); each keyframe is solved to the nearest injective
+    configuration (x_tilde = keyframe, h = 0.1, i.e. the config-0 energy with
+    weight 1e2 m), warm-started from the previous frame's result."""
+    import numpy as np
+    import torch
+    import idp_gb300 as idp
+    from idp_gb300 import meshgen
+    from idp_gb300.api import initialize_oipc
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    X0, tets = meshgen.cylinder(n_cross=args.anim_n)
+    mass = meshgen.lumped_mass(X0, tets, 1000.0)
+    lam, mu = meshgen.lame(1e4, 0.3)
+    diag = float(np.linalg.norm(X0.max(0) - X0.min(0)))
+    dHat2 = (1e-3 * diag) ** 2
+    k, km = initialize_oipc(float(mass.mean()), dHat2)
+    mode = idp.MODE_MIXED if args.mode == "mixed" else idp.MODE_FP64
+    ctx = idp.Context(h=0.1, newton_tol=1e-3, max_newton=args.max_newton, mode=mode, device=local)
+    ctx.add_instance(X0, tets, mass, lam, mu, dHat2, k, km)
+    ctx.commit()
+    frames = [(args.frame_stride * f) % 120 for f in range(args.frames)]
+    rows = []
+    Xc = X0.copy()
+    with ClockSampler(local) as clocks:
+        for t in frames:
+            tgt = meshgen.anim_keyframe(X0, t)
+            t0 = time.perf_counter()
+            ctx.set_velocity(0, (tgt - Xc) / 0.1)
+            rc, res = ctx.advance(check=False)
+            Xc, _, _ = ctx.state(0)
+            wall = time.perf_counter() - t0
+            st = ctx.stats()
+            dev = np.linalg.norm(Xc - tgt, axis=1)
+            rows.append(dict(frame=t, ms=st["total_ms"], wall_ms=1000 * wall, newton=res[0]["newton_iters"],
+                             status=res[0]["status"], dev_max=float(dev.max()), dev_mean=float(dev.mean()),
+                             penetrating_target=abs(math.sin(2 * math.pi * t / 120)) * 2.4 > 2.0,
+                             launches=st["kernel_launches"]))
+    isect = int(ctx.intersection_counts()[0])
+    if rank != 0:
+        return
+    ms = [r["ms"] for r in rows]
+    status = {}
+    for r in rows:
+        status[str(r["status"])] = status.get(str(r["status"]), 0) + 1
+    pen = [r for r in rows if r["penetrating_target"]]
+    out = {
+        "metric": "per-frame solve time and max/mean vertex deviation from the keyframe (animation-fix sequence)",
+        "value": 1000.0 * len(rows) / sum(ms), "unit": "frames/s", "n_gpus": 1, "steps": len(rows), "warmup": 0,
+        "ms_per_step": statistics.mean(ms), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+f64" if mode == idp.MODE_MIXED else "f64", "data": "synthetic",
+        "config": {"workload": f"anim: tet cylinder r=0.2 L=3 ({tets.shape[0]} tets, {X0.shape[0]} verts), keyframes "
+                               f"{frames[0]}..{frames[-1]} step {args.frame_stride}, bend 2.4pi sin(2pi t/120), twist "
+                               f"pi cos(2pi t/60), warm-started, Newton cap {args.max_newton}",
+                   "mode": args.mode, "l2": "inputs larger than L2; no flush"},
+        "frame_ms": {"mean": statistics.mean(ms), "p50": float(np.percentile(ms, 50)),
+                     "p99": float(np.percentile(ms, 99)), "max": max(ms)},
+        "deviation": {"max": max(r["dev_max"] for r in rows), "mean": statistics.mean(r["dev_mean"] for r in rows),
+                      "max_penetrating_frames": max((r["dev_max"] for r in pen), default=None)},
+        "newton_iters": {"mean": statistics.mean(r["newton"] for r in rows), "max": max(r["newton"] for r in rows)},
+        "penetrating_keyframes": len(pen), "status_counts": status,
+        "final_state_intersections": isect,
+        "gpu_launches": sum(r["launches"] for r in rows),
+        "clocks": clocks.summary(),
+        "frames": [{k: (round(v, 4) if isinstance(v, float) else v) for k, v in r.items()} for r in rows],
+    }
+    print(json.dumps(out))
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "serve":
         run_serve(args)
+    elif args.workload == "anim":
+        run_anim(args)
     elif args.workload == "blob":
         run_flow(args)
     else:

@@ -9,6 +9,8 @@ workloads (host-side input generation; numpy only).
 * ``blob``: a star-shaped body r(u) = 1 + a * sum of real spherical harmonics,
   tetrahedralised on a background cube grid (cubes whose centre is inside).
 * ``bar_batch``: many bars with log-uniform tet counts, for batched solves.
+* ``cylinder`` / ``anim_keyframe``: the animation-fix sequence's tet cylinder
+  and its bent and twisted keyframes.
 
 The reference reads these shapes from .vtk/.obj files
 (``Python/Drivers/FEMDiscreteShellBase.py:184-188``); here they are generated
@@ -155,6 +157,57 @@ def blob(n=64, lmax=8, amp=0.3, seed=0):
     X, tets = _compact(Xlat, tets)
     tets = _orient(X, tets)
     return X, tets.astype(np.int32), h
+
+
+def cylinder(radius=0.2, length=3.0, n_cross=22, n_len=None):
+    """Solid cylinder along z (axis x = y = 0, z in [0, length]) on a cube
+    grid of n_cross cells across the diameter: every cube whose centre lies
+    within the radius is split into 5 tets. n_len defaults to cubes of equal
+    edge. At n_cross=22 (n_len=165) this gives 316,800 tets and 71,214 vertices."""
+    h = 2 * radius / n_cross
+    n_len = n_len or int(round(length / h))
+    gx = np.linspace(-radius, radius, n_cross + 1)
+    gz = np.linspace(0.0, length, n_len + 1)
+    cx = (gx[:-1] + gx[1:]) / 2
+    cz = (gz[:-1] + gz[1:]) / 2
+    CX, CY, _ = np.meshgrid(cx, cx, cz, indexing="ij")
+    inside = CX ** 2 + CY ** 2 < radius ** 2
+    Xlat = np.stack(np.meshgrid(gx, gx, gz, indexing="ij"), -1).reshape(-1, 3)
+    tets = cube_grid_tets(inside)
+    X, tets = _compact(Xlat, tets)
+    tets = _orient(X, tets)
+    return X, tets.astype(np.int32)
+
+
+def bend_twist_target(X, angle, twist, length):
+    """Centreline (the z axis, arc length s = z) bent in the x-z plane to a
+    circular arc of total angle ``angle`` (either sign; arc length kept) and
+    cross-sections twisted by twist * s / length. A point at offset (ox, oy)
+    from the axis goes to c(s) + ox N(s) + oy y, with tangent T = (sin ks, 0,
+    cos ks), normal N = (cos ks, 0, -sin ks), k = angle / length; (N, y, T)
+    is right-handed, so tets keep their orientation while |k| * radius < 1."""
+    s = X[:, 2]
+    ph = twist * s / length
+    ox = X[:, 0] * np.cos(ph) - X[:, 1] * np.sin(ph)
+    oy = X[:, 0] * np.sin(ph) + X[:, 1] * np.cos(ph)
+    k = angle / length
+    if abs(k) < 1e-12:
+        c = np.stack([np.zeros_like(s), np.zeros_like(s), s], -1)
+        N = np.array([1.0, 0.0, 0.0])[None, :]
+    else:
+        ks = k * s
+        c = np.stack([2.0 * np.sin(ks / 2) ** 2 / k, np.zeros_like(s), np.sin(ks) / k], -1)
+        N = np.stack([np.cos(ks), np.zeros_like(s), -np.sin(ks)], -1)
+    return c + ox[:, None] * N + oy[:, None] * np.array([0.0, 1.0, 0.0])
+
+
+def anim_keyframe(X, t, length=3.0, frames=120):
+    """Keyframe t of the animation-fix sequence: bend 2.4 pi sin(2 pi t /
+    frames) and twist pi cos(2 pi t / (frames / 2)); frames whose bend
+    exceeds 2 pi in magnitude self-penetrate."""
+    ang = 2.4 * math.pi * math.sin(2 * math.pi * t / frames)
+    tw = math.pi * math.cos(2 * math.pi * t / (frames / 2))
+    return bend_twist_target(X, ang, tw, length)
 
 
 def bar_dims_for_tets(target_tets: float):
