@@ -824,6 +824,8 @@ def run_anim(args):
                              status=res[0]["status"], dev_max=float(dev.max()), dev_mean=float(dev.mean()),
                              penetrating_target=abs(math.sin(2 * math.pi * t / 120)) * 2.4 > 2.0,
                              launches=st["kernel_launches"]))
+            print(f"frame {t}: {st['total_ms']:.1f} ms, {res[0]['newton_iters']} Newton, status "
+                  f"{res[0]['status']}, deviation max {dev.max():.4f}", file=sys.stderr, flush=True)
     isect = int(ctx.intersection_counts()[0])
     if rank != 0:
         return
