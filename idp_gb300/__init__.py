@@ -39,7 +39,7 @@ EXPORTS = [
     "idp_set_normal_flow", "idp_set_kappa", "idp_tet_energy_noalloc", "idp_check_intersection",
     "idp_check_intersection_all", "idp_reset", "idp_device_bytes", "idp_job_footprint", "idp_server_create",
     "idp_server_create_simulated", "idp_server_submit", "idp_server_wait", "idp_server_drain",
-    "idp_server_get_stats", "idp_server_destroy",
+    "idp_server_get_stats", "idp_server_destroy", "idp_add_shell_instance",
 ]
 
 
@@ -124,6 +124,8 @@ def load(path: str | None = None):
     L.idp_add_instance.argtypes = [C.c_void_p, C.c_int, _dp, _dp, C.c_int, _ip, _dp, _dp, _dp, C.c_int, _ip,
                                    C.c_double, C.c_double, C.c_double]
     L.idp_set_velocity.argtypes = [C.c_void_p, C.c_int, _dp]
+    L.idp_add_shell_instance.argtypes = [C.c_void_p, C.c_int, _dp, C.c_int, _ip, C.c_double, C.c_double, C.c_int,
+                                         _ip, C.c_double, C.c_double, C.c_double]
     L.idp_set_positions.argtypes = [C.c_void_p, C.c_int, _dp]
     L.idp_set_normal_flow.argtypes = [C.c_void_p, C.c_int, C.c_double]
     L.idp_set_kappa.argtypes = [C.c_void_p, C.c_int, _dp]
@@ -233,6 +235,19 @@ class Context:
                                     dbc.size, _pi(dbc), float(dHat2), float(kappa), float(kappa_max))
         if r < 0:
             raise IDPError(-r, "idp_add_instance")
+        self._V.append(V)
+        return r
+
+    def add_shell_instance(self, X, faces, density, thickness, dHat2, kappa, kappa_max, dbc_idx=None):
+        """Triangle shell advanced in flow mode (Laplacian flow energy)."""
+        X, faces = _f64(X).reshape(-1, 3), _i32(faces).reshape(-1, 3)
+        V = X.shape[0]
+        dbc = _i32(np.zeros(0) if dbc_idx is None else dbc_idx)
+        r = load().idp_add_shell_instance(self._h, V, _pd(X), faces.shape[0], _pi(faces), float(density),
+                                          float(thickness), dbc.size, _pi(dbc), float(dHat2), float(kappa),
+                                          float(kappa_max))
+        if r < 0:
+            raise IDPError(-r, "idp_add_shell_instance")
         self._V.append(V)
         return r
 

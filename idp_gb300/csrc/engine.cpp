@@ -17,6 +17,7 @@
 #include <cstring>
 #include <map>
 #include <numeric>
+#include <set>
 #include <vector>
 #include "engine.hpp"
 
@@ -219,6 +220,7 @@ int eval_energy(idp_ctx* c, const double* X, bool with_barrier, std::vector<doub
     IDP_CUDA_TRY(cudaMemsetAsync(dsc(c, S_EBAR), 0, sizeof(double) * nI, c->s));
     c->W.timer.start(PhaseTimer::TET, c->s);
     int rc = tet_energy(A, c->W, X, h2, dsc(c, S_ETET), isc(c, SI_BAD), c->s);
+    if (!rc) rc = flow_energy(A, c->W, X, dsc(c, S_ETET), c->s);
     c->W.timer.stop(c->s);
     if (rc) return rc;
     rc = vec_inertia(A, c->W, X, dsc(c, S_EINERT), nullptr, c->s);
@@ -257,6 +259,7 @@ int eval_gradient(idp_ctx* c, const double* X) {
     c->W.timer.stop(c->s);
     if (rc) return rc;
     rc = grad_gather_tet(A, c->W, X, A.g, c->s);
+    if (!rc) rc = flow_gradient(A, X, A.g, c->s);
     if (rc) return rc;
     c->W.timer.start(PhaseTimer::BARRIER, c->s);
     rc = barrier_gradient(A, c->W, X, c->cs, A.g, c->s);
@@ -440,10 +443,91 @@ int idp_add_instance(idp_ctx* c, int V, const double* X, const double* X0, int T
     return (int)c->inst.size() - 1;
 }
 
+// Triangle shell in flow mode: Initialize_Discrete_Shell's face filter,
+// lumped mass and element volumes (FEM/Shell/DISCRETE_SHELL.h:238-333) and
+// Find_Surface_Primitives (Utils/MESHIO.h:728-766) for the contact surface.
+int idp_add_shell_instance(idp_ctx* c, int V, const double* X, int F, const int32_t* faces, double density,
+                           double thickness, int nDBC, const int32_t* dbc_idx, double dHat2, double kappa,
+                           double kappa_max) {
+    if (!c) return -IDP_ERR_INVALID_ARG;
+    if (c->committed) return -IDP_ERR_STATE;
+    if (V <= 0 || F <= 0 || !X || !faces || !(density > 0) || !(thickness > 0) || !(dHat2 > 0))
+        return -IDP_ERR_INVALID_ARG;
+    HostInstance h;
+    h.shell = true;
+    h.V = V;
+    h.T = 0;
+    h.X.assign(X, X + 3 * (long)V);
+    h.X0 = h.X;
+    h.mass.assign(V, 0.0);
+    for (int f = 0; f < F; ++f) {
+        const int* t = faces + 3 * f;
+        for (int k = 0; k < 3; ++k)
+            if (t[k] < 0 || t[k] >= V) return -IDP_ERR_INVALID_ARG;
+        double e1[3], e2[3];
+        for (int d = 0; d < 3; ++d) {
+            e1[d] = X[3 * t[1] + d] - X[3 * t[0] + d];
+            e2[d] = X[3 * t[2] + d] - X[3 * t[0] + d];
+        }
+        const double a = e1[0] * e1[0] + e1[1] * e1[1] + e1[2] * e1[2];
+        const double b = e1[0] * e2[0] + e1[1] * e2[1] + e1[2] * e2[2];
+        const double cc = e2[0] * e2[0] + e2[1] * e2[1] + e2[2] * e2[2];
+        if (a * cc - b * b == 0.0) continue;  // singular first fundamental form
+        const double n[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
+        const double area = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]) / 2;
+        const double mp = area * thickness * density / 3;
+        for (int k = 0; k < 3; ++k) {
+            h.faces.push_back(t[k]);
+            h.mass[t[k]] += mp;
+        }
+        h.fvol.push_back(area * thickness);
+    }
+    if (h.faces.empty()) return -IDP_ERR_INVALID_ARG;
+    std::vector<char> used(V, 0);
+    for (int v : h.faces) used[v] = 1;
+    for (int v = 0; v < V; ++v)
+        if (!used[v]) return -IDP_ERR_INVALID_ARG;  // every vertex needs a face (mass, diagonal block)
+    h.dbc.assign(V, 0);
+    for (int k = 0; k < nDBC; ++k) {
+        if (!dbc_idx || dbc_idx[k] < 0 || dbc_idx[k] >= V) return -IDP_ERR_INVALID_ARG;
+        h.dbc[dbc_idx[k]] = 1;
+    }
+    h.v.assign(3 * (long)V, 0.0);
+    h.dHat2 = dHat2;
+    h.kappa = kappa;
+    h.kappa_max = kappa_max;
+    // surface primitives: every face, edges in set order with the first
+    // orientation unless the reverse is present, nodes ascending
+    std::set<std::pair<int, int>> es;
+    for (size_t f = 0; f < h.faces.size(); f += 3) {
+        const int t[3] = {h.faces[f], h.faces[f + 1], h.faces[f + 2]};
+        for (int k = 0; k < 3; ++k) {
+            const int a = t[k], b = t[(k + 1) % 3];
+            if (!es.count({b, a})) es.insert({a, b});
+        }
+    }
+    h.tris = h.faces;
+    for (auto& e : es) {
+        h.edges.push_back(e.first);
+        h.edges.push_back(e.second);
+    }
+    for (int v = 0; v < V; ++v) h.nodes.push_back(v);
+    double sl = 0;
+    for (size_t e = 0; e + 1 < h.edges.size(); e += 2) {
+        const double* a = &h.X0[3 * h.edges[e]];
+        const double* b = &h.X0[3 * h.edges[e + 1]];
+        sl += std::sqrt((a[0] - b[0]) * (a[0] - b[0]) + (a[1] - b[1]) * (a[1] - b[1]) + (a[2] - b[2]) * (a[2] - b[2]));
+    }
+    h.rest_mean_edge = h.edges.empty() ? 1.0 : sl / (h.edges.size() / 2);
+    c->inst.push_back(std::move(h));
+    return (int)c->inst.size() - 1;
+}
+
 int idp_set_velocity(idp_ctx* c, int i, const double* v) {
     if (!c || i < 0 || i >= (int)c->inst.size() || !v) return IDP_ERR_INVALID_ARG;
     HostInstance& h = c->inst[i];
     h.v.assign(v, v + 3 * (long)h.V);
+    h.vel_set = true;
     if (c->committed) {
         long o = 3L * c->A.v_off[i];
         IDP_CUDA_TRY(cudaMemcpyAsync(c->vel.as<double>() + o, v, sizeof(double) * 3 * h.V, cudaMemcpyHostToDevice, c->s));
@@ -459,6 +543,8 @@ int idp_set_normal_flow(idp_ctx* c, int i, double step) {
     if (c->A.nI == 0) return IDP_OK;
     int rc = normal_flow_velocity(c->A, i, step, c->P.h, c->vel.as<double>(), c->s);
     if (rc) return rc;
+    for (int k = 0; k < (int)c->inst.size(); ++k)
+        if (i < 0 || k == i) c->inst[k].vel_set = true;
     IDP_CUDA_TRY(cudaStreamSynchronize(c->s));
     return IDP_OK;
 }
@@ -485,6 +571,7 @@ int idp_commit(idp_ctx* c) {
     A.nI = nI;
     A.v_off.assign(nI + 1, 0);
     A.t_off.assign(nI + 1, 0);
+    A.f_off.assign(nI + 1, 0);
     A.sn_off.assign(nI + 1, 0);
     A.se_off.assign(nI + 1, 0);
     A.st_off.assign(nI + 1, 0);
@@ -492,6 +579,7 @@ int idp_commit(idp_ctx* c) {
         const HostInstance& h = c->inst[i];
         A.v_off[i + 1] = A.v_off[i] + h.V;
         A.t_off[i + 1] = A.t_off[i] + h.T;
+        A.f_off[i + 1] = A.f_off[i] + (int)h.fvol.size();
         A.sn_off[i + 1] = A.sn_off[i] + (int)h.nodes.size();
         A.se_off[i + 1] = A.se_off[i] + (int)h.edges.size() / 2;
         A.st_off[i + 1] = A.st_off[i] + (int)h.tris.size() / 3;
@@ -501,9 +589,12 @@ int idp_commit(idp_ctx* c) {
     A.Sn = A.sn_off[nI];
     A.Se = A.se_off[nI];
     A.St = A.st_off[nI];
+    A.F = A.f_off[nI];
+    A.h = c->P.h;
     std::vector<double> X, X0, mass, vol, lam, mu, IB, vel, dHat2, kappa, thick, cell;
     std::vector<unsigned char> dbc;
-    std::vector<int> vinst, snode, sedge, stri, sn_inst, se_inst, st_inst, v2s(A.V, -1);
+    std::vector<int> vinst, snode, sedge, stri, sn_inst, se_inst, st_inst, v2s(A.V, -1), face;
+    std::vector<double> fvol;
     std::vector<int4> tet;
     for (int i = 0; i < nI; ++i) {
         const HostInstance& h = c->inst[i];
@@ -532,6 +623,8 @@ int idp_commit(idp_ctx* c) {
             for (int r = 0; r < 3; ++r)
                 for (int q = 0; q < 3; ++q) IB.push_back(Cf[q * 3 + r] / J);
         }
+        for (int v : h.faces) face.push_back(v + vo);
+        fvol.insert(fvol.end(), h.fvol.begin(), h.fvol.end());
         for (size_t k = 0; k < h.nodes.size(); ++k) {
             v2s[h.nodes[k] + vo] = (int)snode.size();
             snode.push_back(h.nodes[k] + vo);
@@ -598,10 +691,28 @@ int idp_commit(idp_ctx* c) {
     rc |= upload(c, A.vert_chunks, vch);
     rc |= upload(c, A.tet_chunk_off, tco);
     rc |= upload(c, A.vert_chunk_off, vco);
+    // shell faces (flow mode): faces, volumes, chunks, vertex -> face lists
+    {
+        std::vector<Chunk> fch;
+        std::vector<int> fco;
+        build_chunks(A.f_off, fch, fco);
+        A.n_face_chunks = (int)fch.size();
+        rc |= upload(c, A.face, face);
+        rc |= upload(c, A.fvol, fvol);
+        rc |= upload(c, A.face_chunks, fch);
+        rc |= upload(c, A.face_chunk_off, fco);
+        std::vector<int> vfp(A.V + 1, 0), vf(face.size());
+        for (int v : face) vfp[v + 1]++;
+        for (long v = 0; v < A.V; ++v) vfp[v + 1] += vfp[v];
+        std::vector<int> fill(vfp.begin(), vfp.end() - 1);
+        for (size_t k = 0; k < face.size(); ++k) vf[fill[face[k]]++] = (int)k;  // face * 3 + corner
+        rc |= upload(c, A.vert_face_ptr, vfp);
+        rc |= upload(c, A.vert_face, vf);
+    }
     // BSR pattern of the tet stencil + contributor lists (fixed order)
     {
         std::vector<std::pair<long, int>> keys;  // (row*V + col, code)
-        keys.reserve(16 * A.T);
+        keys.reserve(16 * A.T + 9 * A.F);
         for (long t = 0; t < A.T; ++t) {
             int v[4] = {tet[t].x, tet[t].y, tet[t].z, tet[t].w};
             for (int a = 0; a < 4; ++a)
@@ -612,6 +723,11 @@ int idp_commit(idp_ctx* c) {
                     keys.push_back({(long)v[a] * A.V + v[b], code});
                 }
         }
+        // shell faces: -(2 f + diagonal) - 1 (flow Hessian, INC_POTENTIAL.h:323-339)
+        for (long f = 0; f < A.F; ++f)
+            for (int a = 0; a < 3; ++a)
+                for (int b = 0; b < 3; ++b)
+                    keys.push_back({(long)face[3 * f + a] * A.V + face[3 * f + b], -(int)(2 * f + (a == b ? 1 : 0)) - 1});
         std::stable_sort(keys.begin(), keys.end(),
                          [](const std::pair<long, int>& x, const std::pair<long, int>& y) { return x.first < y.first; });
         std::vector<int> rowptr(A.V + 1, 0), colidx, brow, src_ptr, src, diag(A.V, -1);
@@ -734,6 +850,15 @@ int idp_advance(idp_ctx* c, idp_result* results) {
     };
     std::vector<unsigned char> all(nI, 1), mask(nI, 0);
     if ((rc = set_mask(c, all))) return rc;
+    // flow mode zeroes a shell's velocity before the predictor
+    // (IMPLICIT_EULER.h:207-209); a predictor set for this step (normal flow)
+    // is kept
+    for (int i = 0; i < nI; ++i) {
+        HostInstance& hi0 = c->inst[i];
+        if (hi0.shell && !hi0.vel_set)
+            IDP_CUDA_TRY(cudaMemsetAsync(c->vel.as<double>() + 3L * A.v_off[i], 0, sizeof(double) * 3 * hi0.V, s));
+        hi0.vel_set = false;
+    }
     // x^n and x_tilde = x^n + h v (IMPLICIT_EULER.h:195-216)
     IDP_CUDA_TRY(cudaMemcpyAsync(A.Xn, A.X, sizeof(double) * 3 * A.V, cudaMemcpyDeviceToDevice, s));
     if ((rc = vec_xtilde(A, A.X, c->vel.as<double>(), h, A.Xtilde, s))) return rc;
@@ -902,6 +1027,7 @@ int idp_advance(idp_ctx* c, idp_result* results) {
             IDP_CUDA_TRY(cudaMemsetAsync(dsc(c, S_EBAR), 0, sizeof(double) * nI, s));
             W.timer.start(PhaseTimer::TET, s);
             if ((rc = tet_energy(A, W, A.X, h * h, dsc(c, S_ETET), isc(c, SI_BAD), s))) return rc;
+            if ((rc = flow_energy(A, W, A.X, dsc(c, S_ETET), s))) return rc;
             W.timer.stop(s);
             if ((rc = vec_inertia(A, W, A.X, dsc(c, S_EINERT), nullptr, s))) return rc;
             for (int i = 0; i < nI; ++i) st[i].ls_trials += srch[i];
@@ -1019,6 +1145,8 @@ int idp_advance(idp_ctx* c, idp_result* results) {
             else if (S.iters >= c->P.max_newton) {
                 S.active = false;
                 S.status = IDP_ERR_NOT_CONVERGED;
+            } else if (c->inst[i].shell && c->cs.off[i + 1] == c->cs.off[i]) {
+                S.active = false;  // flow mode without contacts: one Newton step (IMPLICIT_EULER.h:850-854)
             }
             if (!S.active) latency[i] = now_ms();
         }

@@ -33,6 +33,12 @@ struct HostInstance {
     // surface in reference order (local ids)
     std::vector<int> tris, edges, nodes;
     double rest_mean_edge = 0;
+    // triangle shell advanced in flow mode (no tets): faces double as the
+    // elements of the flow energy, fvol = area * thickness per face
+    bool shell = false;
+    std::vector<int> faces;
+    std::vector<double> fvol;
+    bool vel_set = false;  // predictor velocity given since the last advance
 };
 
 // per-instance Newton state kept on the host
@@ -107,6 +113,17 @@ struct Arena {
     int* brow = nullptr;                          // row (vertex) of every BSR block
     int *tet_chunk_off = nullptr, *vert_chunk_off = nullptr;  // nI+1 chunk ranges
     int* v2s = nullptr;                           // vertex -> surface node (or -1)
+    // ---- triangle shells in flow mode (faces are elements; global vertex ids)
+    long F = 0;
+    std::vector<int> f_off;                       // host, nI+1
+    int* face = nullptr;                          // 3F
+    double* fvol = nullptr;                       // F: area * thickness
+    Chunk* face_chunks = nullptr;
+    int n_face_chunks = 0;
+    int* face_chunk_off = nullptr;                // nI+1
+    int* vert_face_ptr = nullptr;                 // per vertex: list of face*3+corner, ascending
+    int* vert_face = nullptr;
+    double h = 0.1;                               // time step (flow Hessian coefficient)
 };
 
 // CUDA-event timing of the engine's phases on the context stream; elapsed
@@ -262,6 +279,10 @@ struct Params {
 };
 
 // ---------------------------------------------------------------- launchers
+// shell.cu: flow energy of triangle shells (INC_POTENTIAL.h:53-73, 191-211)
+int flow_energy(Arena& A, Work& W, const double* X, double* inst_E, cudaStream_t s);  // accumulates
+int flow_gradient(Arena& A, const double* X, double* g, cudaStream_t s);              // accumulates
+
 // tet.cu
 int tet_energy(Arena& A, Work& W, const double* X, double w_h2, double* inst_E, int* inst_bad, cudaStream_t s);
 int tet_detcheck(Arena& A, Work& W, const double* X, int* inst_bad, cudaStream_t s);

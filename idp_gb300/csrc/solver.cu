@@ -37,7 +37,8 @@ __global__ void k_assemble_tet(long B, const int* __restrict__ src_ptr, const in
                                const T* __restrict__ tet_hess, const int* __restrict__ brow,
                                const int* __restrict__ colidx, const double* __restrict__ mass,
                                const unsigned char* __restrict__ dbc, const int* __restrict__ vinst,
-                               const unsigned char* __restrict__ active, T* __restrict__ val) {
+                               const unsigned char* __restrict__ active, const double* __restrict__ fvol, double h,
+                               T* __restrict__ val) {
     long b = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= B) return;
     int row = brow[b], col = colidx[b];
@@ -47,6 +48,15 @@ __global__ void k_assemble_tet(long B, const int* __restrict__ src_ptr, const in
     for (int q = 0; q < 9; ++q) acc[q] = T(0);
     for (int k = src_ptr[b]; k < src_ptr[b + 1]; ++k) {
         int code = src[k];
+        if (code < 0) {
+            // shell face in flow mode: -h L (INC_POTENTIAL.h:323-339),
+            // 2 h vol/6 I on the diagonal, -h vol/6 I off it
+            const int cf = -code - 1;
+            const double w = h * fvol[cf >> 1] / 6.0;
+            const T d = (T)((cf & 1) ? 2.0 * w : -w);
+            acc[0] += d; acc[4] += d; acc[8] += d;
+            continue;
+        }
 #pragma unroll
         for (int q = 0; q < 9; ++q) acc[q] += blk_get(tet_hess, code, q);
     }
@@ -1100,14 +1110,14 @@ int assemble(Arena& A, Work& W, const ContactSet& cs, bool fp64, cudaStream_t s)
     const int* tcol = W[W_TAIL_COL].as<int>();
     if (fp64) {
         (::idp::count_launch(), k_assemble_tet<double><<<grid_for(A.B), kBlock, 0, s>>>(A.B, A.src_ptr, A.src, W[W_TET_HESS].as<double>(), A.brow,
-                                                                A.colidx, A.mass, A.dbc, A.vinst, A.active,
+                                                                A.colidx, A.mass, A.dbc, A.vinst, A.active, A.fvol, A.h,
                                                                 W[W_BSR_VAL].as<double>()));
         (::idp::count_launch(), k_diag_inv<double><<<grid_for(A.V), kBlock, 0, s>>>(A.V, A.diagblk, W[W_BSR_VAL].as<double>(), trp, tcol,
                                                             W[W_TAIL_VAL].as<double>(), A.dbc, A.vinst, A.active,
                                                             W[W_DIAG_INV].as<double>()));
     } else {
         (::idp::count_launch(), k_assemble_tet<float><<<grid_for(A.B), kBlock, 0, s>>>(A.B, A.src_ptr, A.src, W[W_TET_HESS].as<float>(), A.brow,
-                                                               A.colidx, A.mass, A.dbc, A.vinst, A.active,
+                                                               A.colidx, A.mass, A.dbc, A.vinst, A.active, A.fvol, A.h,
                                                                W[W_BSR_VAL].as<float>()));
         (::idp::count_launch(), k_diag_inv<float><<<grid_for(A.V), kBlock, 0, s>>>(A.V, A.diagblk, W[W_BSR_VAL].as<float>(), trp, tcol,
                                                            W[W_TAIL_VAL].as<float>(), A.dbc, A.vinst, A.active,

@@ -11,6 +11,8 @@ workloads (host-side input generation; numpy only).
 * ``bar_batch``: many bars with log-uniform tet counts, for batched solves.
 * ``cylinder`` / ``anim_keyframe``: the animation-fix sequence's tet cylinder
   and its bent and twisted keyframes.
+* ``shell_from_tets``: the boundary of a tet mesh as a closed triangle shell
+  (flow-mode workloads).
 
 The reference reads these shapes from .vtk/.obj files
 (``Python/Drivers/FEMDiscreteShellBase.py:184-188``); here they are generated
@@ -208,6 +210,20 @@ def anim_keyframe(X, t, length=3.0, frames=120):
     ang = 2.4 * math.pi * math.sin(2 * math.pi * t / frames)
     tw = math.pi * math.cos(2 * math.pi * t / (frames / 2))
     return bend_twist_target(X, ang, tw, length)
+
+
+def shell_from_tets(X, tets):
+    """Boundary of a tet mesh as a closed triangle shell: faces that belong to
+    one tet only, oriented outward, over the compacted boundary vertices."""
+    outward = np.array([[1, 2, 3], [0, 3, 2], [0, 1, 3], [0, 2, 1]])
+    F = tets[:, outward].reshape(-1, 3)
+    key = np.sort(F, axis=1)
+    _, inv, cnt = np.unique(key, axis=0, return_inverse=True, return_counts=True)
+    F = F[cnt[inv.reshape(-1)] == 1]
+    used = np.unique(F)
+    remap = -np.ones(X.shape[0], dtype=np.int64)
+    remap[used] = np.arange(used.size)
+    return X[used].copy(), remap[F].astype(np.int32)
 
 
 def bar_dims_for_tets(target_tets: float):

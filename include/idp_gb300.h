@@ -128,6 +128,21 @@ int idp_add_instance(idp_ctx* ctx, int V, const double* X, const double* X0, int
 
 /* Velocity v (3V); x_tilde = x + h v (IMPLICIT_EULER.h:195-216, no body force).
  * MeshIO.Load_Velocity_X0 (Utils/MESHIO.h:986-1004) sets v = (target - x)/h. */
+/* Add a triangle shell advanced in flow mode (the Laplacian flow energy of
+ * Advance_One_Step_IE_Flow, FEM/Shell/DISCRETE_SHELL.h:1113, with
+ * INC_POTENTIAL.h:53-73,191-211,323-339) with offset-IPC self-contact.
+ * faces int32[3F]; faces with a singular first fundamental form are dropped,
+ * mass and element volumes follow Initialize_Discrete_Shell
+ * (DISCRETE_SHELL.h:238-333: area * thickness * density / 3 per corner,
+ * area * thickness per face); the contact surface is Find_Surface_Primitives
+ * (Utils/MESHIO.h:728-766). In idp_advance the instance's velocity is zeroed
+ * before the predictor unless idp_set_velocity or idp_set_normal_flow gave
+ * one for this step, and without contacts it stops after one Newton step
+ * (IMPLICIT_EULER.h:207-209, 850-854). Returns the instance index or -IDP_*. */
+int idp_add_shell_instance(idp_ctx* ctx, int V, const double* X, int F, const int32_t* faces, double density,
+                           double thickness, int nDBC, const int32_t* dbc_idx, double dHat2, double kappa,
+                           double kappa_max);
+
 int idp_set_velocity(idp_ctx* ctx, int inst, const double* v);
 /* Current positions (3V), e.g. a warm start between frames. */
 int idp_set_positions(idp_ctx* ctx, int inst, const double* X);

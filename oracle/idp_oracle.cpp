@@ -1190,6 +1190,118 @@ bool seg_tri_exact(const double* e0, const double* e1, const double* t0, const d
 
 extern "C" {
 
+// ---------------------------------------------------------------------------
+// Triangle shells in flow mode (Advance_One_Step_IE_Flow,
+// FEM/Shell/DISCRETE_SHELL.h:1113).
+// ---------------------------------------------------------------------------
+
+// Initialize_Discrete_Shell (FEM/Shell/DISCRETE_SHELL.h:238-333): faces whose
+// first fundamental form is singular are dropped (keep[f] = 0); lumped mass
+// area * thickness * rho / 3 per corner; element volume area * thickness.
+// Returns the number of faces kept.
+int ora_shell_init(int V, int F, const int* faces, const double* X, double rho, double thickness,
+                   unsigned char* keep, double* mass, double* vol) {
+    for (int v = 0; v < V; ++v) mass[v] = 0.0;
+    int kept = 0;
+    for (int f = 0; f < F; ++f) {
+        const int* t = faces + 3 * f;
+        double e1[3], e2[3];
+        for (int d = 0; d < 3; ++d) {
+            e1[d] = X[3 * t[1] + d] - X[3 * t[0] + d];
+            e2[d] = X[3 * t[2] + d] - X[3 * t[0] + d];
+        }
+        const double a = e1[0] * e1[0] + e1[1] * e1[1] + e1[2] * e1[2];
+        const double b = e1[0] * e2[0] + e1[1] * e2[1] + e1[2] * e2[2];
+        const double c = e2[0] * e2[0] + e2[1] * e2[1] + e2[2] * e2[2];
+        keep[f] = (a * c - b * b) != 0.0;
+        vol[f] = 0.0;
+        if (!keep[f]) continue;
+        ++kept;
+        const double n[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
+        const double area = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]) / 2;
+        const double mp = area * thickness * rho / 3;
+        for (int k = 0; k < 3; ++k) mass[t[k]] += mp;
+        vol[f] = area * thickness;
+    }
+    return kept;
+}
+
+// Find_Surface_Primitives (Utils/MESHIO.h:728-766): every face is a surface
+// triangle (in order); an edge is kept in its first orientation unless its
+// reverse is already in the set; edges in set order (lexicographic); nodes
+// every referenced vertex, ascending. Returns 0, or -1 if a capacity is short.
+int ora_shell_surface(int V, int F, const int* faces, int capEdge, int* edges, int* nEdge, int* nodes, int* nNode) {
+    std::set<std::pair<int, int>> es;
+    std::vector<char> used(V, 0);
+    for (int f = 0; f < F; ++f) {
+        const int* t = faces + 3 * f;
+        const int p[3][2] = {{t[0], t[1]}, {t[1], t[2]}, {t[2], t[0]}};
+        for (auto& e : p)
+            if (!es.count({e[1], e[0]})) es.insert({e[0], e[1]});
+        used[t[0]] = used[t[1]] = used[t[2]] = 1;
+    }
+    if ((int)es.size() > capEdge) return -1;
+    int k = 0;
+    for (auto& e : es) {
+        edges[2 * k] = e.first;
+        edges[2 * k + 1] = e.second;
+        ++k;
+    }
+    *nEdge = k;
+    int m = 0;
+    for (int v = 0; v < V; ++v)
+        if (used[v]) nodes[m++] = v;
+    *nNode = m;
+    return 0;
+}
+
+// Lx of the flow energy (FEM/Shell/INC_POTENTIAL.h:53-66): per face, vertex i
+// gains vol/6 (x_{i+1} + x_{i+2} - 2 x_i)
+static void flow_Lx(int V, int F, const int* faces, const double* vol, const double* X, std::vector<double>& Lx) {
+    Lx.assign(3 * (size_t)V, 0.0);
+    for (int f = 0; f < F; ++f) {
+        const int* t = faces + 3 * f;
+        for (int i = 0; i < 3; ++i)
+            for (int d = 0; d < 3; ++d)
+                Lx[3 * t[i] + d] += vol[f] / 6 * (X[3 * t[(i + 1) % 3] + d] + X[3 * t[(i + 2) % 3] + d] - 2 * X[3 * t[i] + d]);
+    }
+}
+
+// flow energy -h/2 x^T L x (INC_POTENTIAL.h:53-73)
+double ora_flow_energy(int V, int F, const int* faces, const double* vol, const double* X, double h) {
+    std::vector<double> Lx;
+    flow_Lx(V, F, faces, vol, X, Lx);
+    double e = 0;
+    for (int v = 0; v < V; ++v)
+        for (int d = 0; d < 3; ++d) e += -h * 0.5 * X[3 * v + d] * Lx[3 * v + d];
+    return e;
+}
+
+// flow gradient -h L x (INC_POTENTIAL.h:191-211), added to g
+void ora_flow_gradient(int V, int F, const int* faces, const double* vol, const double* X, double h, double* g) {
+    std::vector<double> Lx;
+    flow_Lx(V, F, faces, vol, X, Lx);
+    for (size_t k = 0; k < Lx.size(); ++k) g[k] += -h * Lx[k];
+}
+
+// flow Hessian triplets (INC_POTENTIAL.h:323-339): 27 per face (rows, cols, vals)
+void ora_flow_hessian(int F, const int* faces, const double* vol, double h, int* rows, int* cols, double* vals) {
+    for (int f = 0; f < F; ++f) {
+        const int* t = faces + 3 * f;
+        for (int i = 0; i < 3; ++i)
+            for (int d = 0; d < 3; ++d) {
+                const long b = (long)f * 27 + i * 9 + d * 3;
+                rows[b] = rows[b + 1] = rows[b + 2] = 3 * t[i] + d;
+                cols[b] = 3 * t[(i + 1) % 3] + d;
+                cols[b + 1] = 3 * t[(i + 2) % 3] + d;
+                cols[b + 2] = 3 * t[i] + d;
+                vals[b] = -h * vol[f] / 6;
+                vals[b + 1] = -h * vol[f] / 6;
+                vals[b + 2] = 2 * h * vol[f] / 6;
+            }
+    }
+}
+
 int ora_orient3d(const double* a, const double* b, const double* c, const double* d) {
     return exact_orient3d(a, b, c, d);
 }

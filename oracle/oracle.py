@@ -56,6 +56,9 @@ def lib():
         L.ora_dist_pt_unclassified.restype = C.c_double
         L.ora_dist_ee_unclassified.restype = C.c_double
         L.ora_orient3d.restype = C.c_int
+        L.ora_shell_init.restype = C.c_int
+        L.ora_shell_surface.restype = C.c_int
+        L.ora_flow_energy.restype = C.c_double
         L.ora_edge_tri_intersections.restype = C.c_long
         L.ora_edge_tri_intersections.argtypes = [C.c_int, _ip, C.c_int, _ip, _dp, _up, C.c_long, _ip]
         _lib = L
@@ -180,6 +183,51 @@ def ccd_stepsize(X, dirn, surf, dbc, alpha=1.0, thickness=0.0):
     return a.value, rc
 
 
+def shell_init(X, faces, rho, thickness):
+    """Face filter, lumped mass and element volumes of a triangle shell
+    (Initialize_Discrete_Shell, DISCRETE_SHELL.h:238-333): (keep, mass, vol)."""
+    X, faces = f64(X), i32(faces)
+    V, F = X.shape[0], faces.shape[0]
+    keep, mass, vol = np.zeros(F, np.uint8), np.zeros(V), np.zeros(F)
+    lib().ora_shell_init(V, F, _i(faces), _d(X), C.c_double(rho), C.c_double(thickness), _u(keep), _d(mass),
+                         _d(vol))
+    return keep.astype(bool), mass, vol
+
+
+def shell_surface(V, faces):
+    """Find_Surface_Primitives (MESHIO.h:728-766) of a triangle shell."""
+    faces = i32(faces)
+    F = faces.shape[0]
+    edges, nodes = np.zeros((3 * F, 2), np.int32), np.zeros(V, np.int32)
+    ne, nn = C.c_int(), C.c_int()
+    rc = lib().ora_shell_surface(V, F, _i(faces), 3 * F, _i(edges), C.byref(ne), _i(nodes), C.byref(nn))
+    assert rc == 0
+    return {"tris": faces.copy(), "edges": edges[: ne.value].copy(), "nodes": nodes[: nn.value].copy()}
+
+
+def flow_energy(X, faces, vol, h):
+    X, faces = f64(X), i32(faces)
+    return lib().ora_flow_energy(X.shape[0], faces.shape[0], _i(faces), _d(f64(vol)), _d(X), C.c_double(h))
+
+
+def flow_gradient(X, faces, vol, h):
+    X, faces = f64(X), i32(faces)
+    g = np.zeros(X.size)
+    lib().ora_flow_gradient(X.shape[0], faces.shape[0], _i(faces), _d(f64(vol)), _d(X), C.c_double(h), _d(g))
+    return g
+
+
+def flow_hessian(n_dof, faces, vol, h):
+    """-h L as scipy CSR (INC_POTENTIAL.h:323-339)."""
+    import scipy.sparse as sp
+
+    faces = i32(faces)
+    F = faces.shape[0]
+    r, c, v = np.zeros(27 * F, np.int32), np.zeros(27 * F, np.int32), np.zeros(27 * F)
+    lib().ora_flow_hessian(F, _i(faces), _d(f64(vol)), C.c_double(h), _i(r), _i(c), _d(v))
+    return sp.coo_matrix((v, (r, c)), shape=(n_dof, n_dof)).tocsr()
+
+
 def orient3d(a, b, c, d):
     """Exact sign of det[a-d; b-d; c-d]."""
     return lib().ora_orient3d(_d(f64(a)), _d(f64(b)), _d(f64(c)), _d(f64(d)))
@@ -257,21 +305,33 @@ class Problem:
     vol: np.ndarray = None
     surf: dict = None
     log: list = field(default_factory=list)
+    faces: np.ndarray = None  # (F,3) shell faces: flow mode (Advance_One_Step_IE_Flow)
+    fvol: np.ndarray = None   # (F,) shell element volumes (area * thickness)
+
+    @property
+    def flow(self):
+        return self.faces is not None
 
     def __post_init__(self):
         self.X = f64(self.X).copy()
         self.X0 = f64(self.X0)
+        if self.flow:
+            self.faces = i32(self.faces)
+            self.tets = np.zeros((0, 4), np.int32)
         self.tets = i32(self.tets)
         if self.dbc is None:
             self.dbc = np.zeros(self.X.shape[0], np.uint8)
-        if self.IB is None:
+        if self.IB is None and not self.flow:
             self.IB, self.vol = tet_rest(self.X0, self.tets)
 
 
 def _energy(pb, X, Xtilde, with_barrier, cons, info):
     """Compute_IncPotential (INC_POTENTIAL.h:15-152); None when a tet inverts."""
     h2 = pb.h * pb.h
-    E = tet_energy(X, pb.tets, pb.IB, pb.vol, pb.lam, pb.mu, h2)
+    if pb.flow:  # INC_POTENTIAL.h:53-73
+        E = flow_energy(X, pb.faces, pb.fvol, pb.h)
+    else:
+        E = tet_energy(X, pb.tets, pb.IB, pb.vol, pb.lam, pb.mu, h2)
     if E is None:
         return None
     dx = (X - Xtilde)
@@ -284,7 +344,10 @@ def _energy(pb, X, Xtilde, with_barrier, cons, info):
 def _gradient(pb, X, Xtilde, cons, info):
     """Compute_IncPotential_Gradient (INC_POTENTIAL.h:154-275)."""
     h2 = pb.h * pb.h
-    g = tet_gradient(X, pb.tets, pb.IB, pb.vol, pb.lam, pb.mu, h2)
+    if pb.flow:  # INC_POTENTIAL.h:191-211
+        g = flow_gradient(X, pb.faces, pb.fvol, pb.h)
+    else:
+        g = tet_gradient(X, pb.tets, pb.IB, pb.vol, pb.lam, pb.mu, h2)
     g += (pb.mass[:, None] * (X - Xtilde)).reshape(-1)
     g += barrier_gradient(cons, info, X, pb.X0, pb.dHat2, pb.kappa[0], pb.thickness)
     return g
@@ -296,12 +359,16 @@ def _hessian(pb, X, cons, info):
 
     n = X.size
     h2 = pb.h * pb.h
-    He = tet_hessian(X, pb.tets, pb.IB, pb.vol, pb.lam, pb.mu, h2, True)
-    dofs = (3 * pb.tets[:, :, None] + np.arange(3)).reshape(-1, 12)
-    rows = np.repeat(dofs[:, :, None], 12, axis=2).reshape(-1)
-    cols = np.repeat(dofs[:, None, :], 12, axis=1).reshape(-1)
-    vals = He.reshape(-1)
-    R, Cc, Vv = [rows], [cols], [vals]
+    if pb.flow:  # INC_POTENTIAL.h:323-339
+        Hf = flow_hessian(n, pb.faces, pb.fvol, pb.h).tocoo()
+        R, Cc, Vv = [Hf.row], [Hf.col], [Hf.data]
+    else:
+        He = tet_hessian(X, pb.tets, pb.IB, pb.vol, pb.lam, pb.mu, h2, True)
+        dofs = (3 * pb.tets[:, :, None] + np.arange(3)).reshape(-1, 12)
+        rows = np.repeat(dofs[:, :, None], 12, axis=2).reshape(-1)
+        cols = np.repeat(dofs[:, None, :], 12, axis=1).reshape(-1)
+        vals = He.reshape(-1)
+        R, Cc, Vv = [rows], [cols], [vals]
     if cons.shape[0]:
         verts, Hb = barrier_hessian(cons, info, X, pb.X0, pb.dHat2, pb.kappa[0], pb.thickness, True)
         for nv in (2, 3, 4):
@@ -333,10 +400,12 @@ def advance_one_step(pb: Problem, Xtilde=None, verbose=False):
 
     h = pb.h
     Xn = pb.X.copy()
+    if pb.flow:
+        pb.v[:] = 0.0                     # IMPLICIT_EULER.h:207-209
     if Xtilde is None:
         Xtilde = Xn + h * pb.v            # IMPLICIT_EULER.h:195-216 (no body force)
-    if pb.surf is None:
-        pb.surf = surface(pb.X0, pb.tets)  # IMPLICIT_EULER.h:235-241
+    if pb.surf is None:                   # IMPLICIT_EULER.h:235-241
+        pb.surf = shell_surface(pb.X.shape[0], pb.faces) if pb.flow else surface(pb.X0, pb.tets)
     surf, dbc = pb.surf, pb.dbc
     nDBC = int(dbc.sum())
     X = pb.X
@@ -428,6 +497,8 @@ def advance_one_step(pb: Problem, Xtilde=None, verbose=False):
         if verbose:
             print(f"it {it} E {Eprev:.12e} res {L2:.3e} alpha {alpha*2:.3e} C {cons.shape[0]} kappa {pb.kappa[0]:.3e}")
         if (len(res_record) == 3 and L2m <= pb.tol) or it >= pb.max_iters:
+            break
+        if pb.flow and cons.shape[0] == 0:  # IMPLICIT_EULER.h:850-854
             break
     pb.v = (X - Xn) / h                     # IMPLICIT_EULER.h:882-888
     pb.last_stats = stats

@@ -252,3 +252,64 @@ def test_normal_flow_outward_unit(oracle):
     assert np.allclose(np.linalg.norm(v[on], axis=1) * h, 0.05)
     assert np.all(v[~on] == 0)
     assert np.all(np.einsum("ij,ij->i", v[on], X[on] - X.mean(0)) > 0)
+
+
+# ---------------------------------------------------------------- shells, flow mode
+def _shell(n=12, seed=1):
+    import sys, os
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    from idp_gb300 import meshgen
+
+    X, T, _ = meshgen.blob(n=n, lmax=4, seed=seed)
+    return meshgen.shell_from_tets(X, T)
+
+
+def test_flow_energy_forms_agree(oracle):
+    """-h/2 x^T L x (INC_POTENTIAL.h:53-73) equals the edge form
+    h/12 sum vol (|x0-x1|^2 + |x1-x2|^2 + |x2-x0|^2); its gradient is -h L x."""
+    X, F = _shell()
+    keep, mass, vol = oracle.shell_init(X, F, 1000.0, 0.01)
+    assert keep.all()
+    rng = np.random.default_rng(0)
+    Y = X + 0.01 * rng.normal(size=X.shape)
+    h = 0.5
+    e_ref = oracle.flow_energy(Y, F, vol, h)
+    d = lambda a, b: ((Y[F[:, a]] - Y[F[:, b]]) ** 2).sum(1)
+    e_edge = float((h / 12 * vol * (d(0, 1) + d(1, 2) + d(2, 0))).sum())
+    assert e_ref == pytest.approx(e_edge, rel=1e-12)
+    g = oracle.flow_gradient(Y, F, vol, h)
+    f = lambda z: oracle.flow_energy(z.reshape(-1, 3), F, vol, h)
+    idx = rng.choice(Y.size, 12, replace=False)
+    gfd = np.array([(f(Y.reshape(-1) + 1e-6 * np.eye(Y.size)[i]) - f(Y.reshape(-1) - 1e-6 * np.eye(Y.size)[i])) / 2e-6
+                    for i in idx])
+    assert np.allclose(gfd, g[idx], rtol=1e-5, atol=1e-10)
+
+
+def test_shell_surface_and_mass(oracle):
+    X, F = _shell()
+    s = oracle.shell_surface(X.shape[0], F)
+    assert X.shape[0] - len(s["edges"]) + F.shape[0] == 2  # closed genus-0 surface
+    assert np.array_equal(s["tris"], F)
+    assert np.array_equal(s["nodes"], np.arange(X.shape[0]))
+    assert sorted(map(tuple, s["edges"].tolist())) == list(map(tuple, s["edges"].tolist()))
+    keep, mass, vol = oracle.shell_init(X, F, 1000.0, 0.01)
+    assert mass.sum() == pytest.approx(1000.0 * vol.sum(), rel=1e-12)
+
+
+def test_flow_step_contact_free_is_one_newton_step(oracle):
+    """Flow mode without contacts: one Newton step solves the quadratic
+    exactly (IMPLICIT_EULER.h:850-854)."""
+    X, F = _shell()
+    keep, mass, vol = oracle.shell_init(X, F, 1000.0, 0.01)
+    h = 0.5
+    diag = float(np.linalg.norm(X.max(0) - X.min(0)))
+    dHat2 = (1e-3 * diag) ** 2
+    k, km = oracle.kappa_init(float(mass.mean()), dHat2)
+    pb = oracle.Problem(X=X.copy(), X0=X.copy(), tets=None, mass=mass, lam=None, mu=None, h=h, dHat2=dHat2,
+                        kappa=[k, km, 0.0], v=np.zeros_like(X), faces=F, fvol=vol)
+    Xt = X + oracle.normal_flow_velocity(X, F, 0.005, h) * h
+    it = oracle.advance_one_step(pb, Xtilde=Xt)
+    assert it == 1
+    # the result minimises E: gradient vanishes
+    g = oracle.flow_gradient(pb.X, F, vol, h) + (mass[:, None] * (pb.X - Xt)).reshape(-1)
+    assert np.linalg.norm(g) < 1e-8 * np.linalg.norm((mass[:, None] * (X - Xt)).reshape(-1))
