@@ -403,7 +403,7 @@ def run_flow(args):
     lat = [r["latency_ms"] for r in results]
     newton = [r["newton_iters"] for r in results]
     out = {
-        "metric": metric, "value": value, "unit": unit, "n_gpus": world, "steps": args.steps,
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32+f64" if mode == idp.MODE_MIXED else "f64", "data": "synthetic",
         "config": {"workload": desc, "tets": int(p["tets"].shape[0]), "verts": V, "mode": args.mode,
@@ -427,9 +427,6 @@ def run_flow(args):
         "clocks": clocks.summary(),
         "wall_ms_per_step": 1000 * statistics.mean(wall),
     }
-    if fp64_single:
-        ref = fp64_single["newton_iters_per_s"] if budget > 0 else fp64_single["solves_per_s"]
-        out["mixed_batched_over_fp64_one_at_a_time"] = (value / ref) if ref else None
     if not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline_flow(int(p["tets"].shape[0]), args.flow_step, args.cpu_sample_s)
     print(json.dumps(out), flush=True)
