@@ -102,6 +102,65 @@ class DiscreteShell:
         return res[0]["newton_iters"]
 
 
+class _FlowCache:
+    ctx = None
+    key = None
+
+
+def _flow_context_for(Elem, X, nodeAttr, elasticityAttr, dHat2, kappaVec, DBC, h, NewtonTol, thickness, mode):
+    Elem = np.asarray(Elem, dtype=np.int32).reshape(-1, 3)
+    key = (id(Elem), Elem.shape, X.shape, float(dHat2), float(h), float(NewtonTol), float(thickness), mode)
+    if _FlowCache.key == key and _FlowCache.ctx is not None:
+        return _FlowCache.ctx
+    # shell thickness and density back from the element volumes (area *
+    # thickness) and lumped masses of Initialize_Discrete_Shell
+    X0 = np.asarray(nodeAttr["x0"], dtype=np.float64).reshape(-1, 3)
+    area = np.linalg.norm(np.cross(X0[Elem[:, 1]] - X0[Elem[:, 0]], X0[Elem[:, 2]] - X0[Elem[:, 0]]), axis=1) / 2
+    vol = np.asarray(elasticityAttr["vol"], dtype=np.float64)
+    shell_t = float(vol[0] / area[0])
+    rho = float(np.sum(nodeAttr["m"]) / np.sum(vol))
+    ctx = Context(h=h, newton_tol=NewtonTol, thickness=thickness, mode=mode)
+    dbc_idx = None if _empty(DBC) else np.asarray(DBC)[:, 0].astype(np.int32)
+    ctx.add_shell_instance(X0, Elem, rho, shell_t, dHat2, kappaVec[0], kappaVec[1], dbc_idx=dbc_idx)
+    ctx.commit()
+    _FlowCache.ctx, _FlowCache.key = ctx, key
+    return ctx
+
+
+def _advance_flow(Elem, segs, DBC, edge2tri, edgeStencil, edgeInfo, thickness, bendingStiffMult, fiberStiffMult,
+                  fiberLimit, s, sHat, kappa_s, b, h, NewtonTol, withCollision, dHat2, kappaVec, mu, epsv2,
+                  fricIterAmt, compNodeRange, muComp, staticSolve, X, nodeAttr, M, elemAttr, elasticityAttr, tet,
+                  tetAttr, tetElasticityAttr, rod, rodInfo, rodHinge, rodHingeInfo, stitchInfo, stitchRatio, k_stitch,
+                  particle, outputFolder):
+    """Advance_One_Step_IE_Flow (DISCRETE_SHELL.h:1113): one flow-mode step of
+    a triangle shell. b is the body force of Update_Normal_Flow_Neumann
+    (magnitude * M_ii * normal), so x_tilde = x + h^2 M^-1 b with v = 0."""
+    for name, v in (("segs", segs), ("rod", rod), ("stitchInfo", stitchInfo), ("particle", particle), ("tet", tet)):
+        if not _empty(v):
+            raise NotImplementedError(f"{name}: not part of the flow-mode shell path")
+    if staticSolve or (mu and mu > 0):
+        raise NotImplementedError("staticSolve / friction: not part of the flow-mode shell path")
+    if not withCollision:
+        raise NotImplementedError("withCollision=False: the GB300 path always has IPC contact")
+    ctx = _flow_context_for(Elem, X, nodeAttr, elasticityAttr, dHat2, kappaVec, DBC, h, NewtonTol, thickness,
+                            DiscreteShell.mode)
+    ctx.set_positions(0, X)
+    m = np.asarray(nodeAttr["m"], dtype=np.float64)
+    bb = np.zeros_like(X) if b is None else np.asarray(b, dtype=np.float64).reshape(-1, 3)
+    ctx.set_velocity(0, h * bb / m[:, None])
+    rc, res = ctx.advance(check=False)
+    if rc not in (0, IDP_WARN_ITER_CAP):
+        raise IDPError(rc, "Advance_One_Step_IE_Flow")
+    Xn, v, k = ctx.state(0)
+    X[...] = Xn
+    nodeAttr["v"][...] = v
+    kappaVec[0] = k[0]
+    return res[0]["newton_iters"]
+
+
+DiscreteShell.Advance_One_Step_IE_Flow = staticmethod(_advance_flow)
+
+
 class FEM:
     DiscreteShell = DiscreteShell
 

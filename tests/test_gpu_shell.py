@@ -154,3 +154,31 @@ def test_flow_steps_with_contact(oracle, gpu_lib):
     Xg, _, _ = ctx.state(0)
     assert len(oracle.edge_tri_intersections(Xg, oracle.shell_surface(Xg.shape[0], s["F"]))) == 0
     ctx.close()
+
+
+def test_reference_shaped_flow_call(oracle, gpu_lib):
+    """FEM.DiscreteShell.Advance_One_Step_IE_Flow with the reference's
+    positional arguments (body force b = magnitude * M_ii * n from
+    Update_Normal_Flow_Neumann) gives the same step as the C-ABI calls."""
+    import idp_gb300 as idp
+    from idp_gb300.api import FEM
+
+    s = setup(oracle, [shell()])
+    X = s["X"].copy()
+    mag = 0.02
+    n = oracle.normal_flow_velocity(X, s["F"], 1.0, 1.0)  # unit normals
+    b = (mag * s["mass"][:, None] * n).reshape(-1)
+    nodeAttr = {"x0": s["X"].copy(), "v": np.zeros_like(X), "m": s["mass"].copy()}
+    elasticityAttr = {"vol": s["vol"].copy()}
+    kappaVec = [s["kappa"], s["kappa_max"], 0.0]
+    it = FEM.DiscreteShell.Advance_One_Step_IE_Flow(
+        s["F"], [], [], None, None, None, 0.0, 0.0, None, None, None, None, None, b, H, 1e-3, True, s["dHat2"],
+        kappaVec, 0.0, 0.0, 0, None, None, False, X, nodeAttr, None, None, elasticityAttr, [], None, None, [], None,
+        [], None, [], None, 0.0, [], "")
+    assert it == 1
+    ctx = gpu_ctx(idp, s, idp.MODE_MIXED)
+    ctx.set_normal_flow(0, H * H * mag)
+    ctx.advance(check=False)
+    Xg, _, _ = ctx.state(0)
+    assert np.allclose(X, Xg, rtol=0, atol=1e-12 * np.abs(Xg).max())
+    ctx.close()
