@@ -916,6 +916,8 @@ int idp_advance(idp_ctx* c, idp_result* results) {
                 if (st[i].iters == 0 || !(st[i].g0 > 0)) st[i].g0 = gn;
                 double eta = st[i].g0 > 0 ? gn / st[i].g0 : 1.0;
                 tol[i] = std::max(c->P.pcg_rel_tol, std::min(1e-2, eta));
+                // a flow-mode shell may stop after this one step: solve it fully
+                if (c->inst[i].shell) tol[i] = c->P.pcg_rel_tol;
             }
             IDP_CUDA_TRY(cudaMemcpyAsync(W.tol_inst, tol.data(), sizeof(double) * nI, cudaMemcpyHostToDevice, s));
         }
