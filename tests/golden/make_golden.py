@@ -59,6 +59,24 @@ def flow_case(seed):
     return X, tets
 
 
+def isect_case(seed):
+    """A jittered bar and its bend onto 2.2 pi turns (self-intersecting)."""
+    X, tets = meshgen.bar(3, 3, 8, size=(1.0, 1.0, 4.0), seed=seed)
+    return X, tets, meshgen.bend_target(X, angle=2.2 * math.pi)
+
+
+def shell_case(seed):
+    """The boundary of a jittered bar as a closed shell, sheared (portable
+    arithmetic only), and a perturbed state of it."""
+    X, tets = meshgen.bar(2, 3, 4, size=(1.0, 1.5, 2.0), seed=seed)
+    Xs, F = meshgen.shell_from_tets(X, tets)
+    Xs = Xs.copy()
+    Xs[:, 0] += 0.1 * Xs[:, 2]
+    rng = np.random.default_rng(100 + seed)
+    Xd = Xs + 0.01 * rng.uniform(-1.0, 1.0, Xs.shape)
+    return Xs, F, Xd
+
+
 def step_case():
     """A bar bent 1.6 pi into a ring whose ends approach (contact, no overlap)."""
     X, tets = meshgen.bar(2, 2, 6, size=(1.0, 1.0, 2.4), seed=0)
@@ -99,6 +117,17 @@ def main():
     for seed in range(2):
         X, tets = flow_case(seed)
         out[f"flow{seed}_v"] = O.normal_flow_velocity(X, O.surface(X, tets)["tris"], 0.05, 0.1)
+    for seed in range(2):
+        X, tets, Xt = isect_case(seed)
+        out[f"isect{seed}_pairs"] = O.edge_tri_intersections(Xt, O.surface(X, tets))
+    for seed in range(2):
+        Xs, F, Xd = shell_case(seed)
+        keep, mass, vol = O.shell_init(Xs, F, 1000.0, 0.01)
+        surf = O.shell_surface(Xs.shape[0], F)
+        out[f"shell{seed}_edges"] = surf["edges"]
+        out[f"shell{seed}_mass"] = mass
+        out[f"shell{seed}_flowE"] = np.array([O.flow_energy(Xd, F, vol, 0.5)])
+        out[f"shell{seed}_flowg"] = O.flow_gradient(Xd, F, vol, 0.5)
     X, tets, target = step_case()
     pr = cases.problem(X, tets)
     T = tets.shape[0]

@@ -57,6 +57,21 @@ def test_oracle_reproduces_golden(oracle):
         assert np.array_equal(v, GOLD[f"flow{seed}_v"])
 
 
+def test_oracle_reproduces_golden_isect_and_shells(oracle):
+    for seed in range(2):
+        X, tets, Xt = mg.isect_case(seed)
+        pairs = oracle.edge_tri_intersections(Xt, oracle.surface(X, tets))
+        assert len(pairs) > 0 and np.array_equal(pairs, GOLD[f"isect{seed}_pairs"])
+    for seed in range(2):
+        Xs, F, Xd = mg.shell_case(seed)
+        keep, mass, vol = oracle.shell_init(Xs, F, 1000.0, 0.01)
+        assert keep.all()
+        assert np.array_equal(oracle.shell_surface(Xs.shape[0], F)["edges"], GOLD[f"shell{seed}_edges"])
+        assert close(mass, GOLD[f"shell{seed}_mass"], 1e-12)
+        assert close(oracle.flow_energy(Xd, F, vol, 0.5), GOLD[f"shell{seed}_flowE"][0], 1e-12)
+        assert close(oracle.flow_gradient(Xd, F, vol, 0.5), GOLD[f"shell{seed}_flowg"], 1e-12)
+
+
 def test_oracle_step_reproduces_golden(oracle):
     X, tets, target = mg.step_case()
     pr = cases.problem(X, tets)
@@ -113,6 +128,23 @@ def test_gpu_reproduces_golden(gpu_lib):
         ctx.set_normal_flow(0, 0.05)
         _, v, _ = ctx.state(0)
         assert np.array_equal(v, GOLD[f"flow{seed}_v"])
+        ctx.close()
+    for seed in range(2):
+        X, tets, Xt = mg.isect_case(seed)
+        pr = cases.problem(X, tets)
+        ctx = idp.Context(h=0.1, mode=idp.MODE_MIXED)
+        ctx.add_instance(X, tets, pr["mass"], pr["lam"], pr["mu"], pr["dHat2"], pr["kappa"], pr["kappa_max"])
+        ctx.commit()
+        assert np.array_equal(ctx.intersections(0, Xt), GOLD[f"isect{seed}_pairs"])
+        ctx.close()
+    for seed in range(2):
+        Xs, F, Xd = mg.shell_case(seed)
+        ctx = idp.Context(h=0.5, mode=idp.MODE_FP64)
+        ctx.add_shell_instance(Xs, F, 1000.0, 0.01, 1e-6, 1.0, 100.0)
+        ctx.commit()
+        assert np.array_equal(ctx.surface(0)["edges"], GOLD[f"shell{seed}_edges"])
+        Ee, _, _ = ctx.energy(0, Xd)
+        assert close(Ee, GOLD[f"shell{seed}_flowE"][0], 1e-9)
         ctx.close()
     X, tets, target = mg.step_case()
     pr = cases.problem(X, tets)
