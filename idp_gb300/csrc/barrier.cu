@@ -359,12 +359,25 @@ __global__ void k_segment_sum(int nI, const int* __restrict__ off, const double*
     if (threadIdx.x == 0) out[inst] = accumulate ? out[inst] + sh[0] : sh[0];
 }
 
+// the 10 upper 3x3 blocks (a <= b) of an nv-vertex stencil's 3nv x 3nv matrix
+template <class T>
+__device__ __forceinline__ void write_upper_blocks(const T* H, int n, T* ho) {
+    const int nv = n / 3;
+    int k = 0;
+    for (int a = 0; a < 4; ++a)
+        for (int b = a; b < 4; ++b, ++k)
+            for (int d = 0; d < 3; ++d)
+                for (int e = 0; e < 3; ++e)
+                    ho[k * 9 + d * 3 + e] = (a < nv && b < nv) ? H[(3 * a + d) * n + 3 * b + e] : T(0);
+}
+
 template <class T>
 __global__ void k_barrier_gh(long C, const int4* __restrict__ cons, const int* __restrict__ cinst,
                              const unsigned char* __restrict__ active, const double* __restrict__ X,
                              const double* __restrict__ X0, const double* __restrict__ dHat2,
                              const double* __restrict__ kappa, const double* __restrict__ thick,
-                             double* __restrict__ gout, T* __restrict__ hout) {
+                             double* __restrict__ gout, T* __restrict__ hout, T* __restrict__ hloc,
+                             int* __restrict__ hn, int* __restrict__ plist, unsigned int* __restrict__ pcount) {
     long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= C) return;
     int inst = cinst[i];
@@ -382,14 +395,135 @@ __global__ void k_barrier_gh(long C, const int4* __restrict__ cons, const int* _
     int n = 3 * nv;
     T H[144];
     for (int k = 0; k < n * n; ++k) H[k] = (T)Hd[k];
-    make_pd(H, n);
-    T* ho = hout + 90 * i;
-    int k = 0;
-    for (int a = 0; a < 4; ++a)
-        for (int b = a; b < 4; ++b, ++k)
-            for (int d = 0; d < 3; ++d)
-                for (int e = 0; e < 3; ++e)
-                    ho[k * 9 + d * 3 + e] = (a < nv && b < nv) ? H[(3 * a + d) * n + 3 * b + e] : T(0);
+    if (!chol_pd(H, n)) {
+        // indefinite: projected by k_psd_warp (one warp per matrix)
+        T* hl = hloc + 144 * i;
+        for (int k = 0; k < n * n; ++k) hl[k] = H[k];
+        hn[i] = n;
+        plist[atomicAdd(pcount, 1u)] = (int)i;
+        return;
+    }
+    write_upper_blocks(H, n, hout + 90 * i);
+}
+
+// The 12x12 PSD projection of makePD (Math/UTILS.h:10-27: eigenvalues below
+// zero set to zero) for the matrices k_barrier_gh found indefinite, one warp
+// per matrix: cyclic Jacobi in round-robin (tournament) order, so each step
+// rotates n/2 disjoint index pairs at once (an odd n gets a dummy index), the
+// rotations' column, row and eigenvector updates spread over the lanes. The
+// rotation formula and the stopping test are those of make_pd; only the
+// order of the rotations differs, so the result agrees with it to rounding.
+constexpr int kPsdWarps = 8;  // warps per CTA
+
+template <class T>
+__global__ void __launch_bounds__(32 * kPsdWarps) k_psd_warp(const int* __restrict__ plist,
+                                                               const unsigned int* __restrict__ pcount,
+                                                               const T* __restrict__ hloc,
+                                                               const int* __restrict__ hn, T* __restrict__ hout) {
+    __shared__ T sA[kPsdWarps][144], sV[kPsdWarps][144], sCS[kPsdWarps][6][2], sW[kPsdWarps][12];
+    __shared__ int sPQ[kPsdWarps][6][2];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    T* A = sA[w];
+    T* Vm = sV[w];
+    const unsigned int cnt = *pcount;
+    for (unsigned int item = blockIdx.x * kPsdWarps + w; item < cnt; item += gridDim.x * kPsdWarps) {
+        const int i = plist[item];
+        const int n = hn[i];
+        const int m = n + (n & 1);  // players of the tournament
+        const int P = m / 2;         // rotations per step
+        for (int k = lane; k < n * n; k += 32) {
+            A[k] = hloc[144L * i + k];
+            Vm[k] = (k / n == k % n) ? T(1) : T(0);
+        }
+        __syncwarp();
+        for (int sweep = 0; sweep < 20; ++sweep) {
+            T off = 0, tot = 0;
+            for (int k = lane; k < n * n; k += 32) {
+                const T a = A[k];
+                tot += a * a;
+                if (k / n != k % n) off += a * a;
+            }
+            for (int o = 16; o > 0; o >>= 1) {
+                off += __shfl_xor_sync(0xffffffffu, off, o);
+                tot += __shfl_xor_sync(0xffffffffu, tot, o);
+            }
+            if (off <= (sizeof(T) == 4 ? T(1e-14) : T(1e-30)) * tot || off == T(0)) break;
+            for (int r = 0; r < m - 1; ++r) {
+                if (lane < P) {
+                    int p = lane == 0 ? r : (r + lane) % (m - 1);
+                    int q = lane == 0 ? m - 1 : (r - lane + (m - 1)) % (m - 1);
+                    if (p > q) { const int t = p; p = q; q = t; }
+                    T c = T(1), sn = T(0);
+                    if (q < n) {
+                        const T apq = A[p * n + q];
+                        if (apq != T(0)) {
+                            const T app = A[p * n + p], aqq = A[q * n + q];
+                            const T theta = (aqq - app) / (T(2) * apq);
+                            const T t = (theta >= T(0) ? T(1) : T(-1)) / (fabs(theta) + sqrt(theta * theta + T(1)));
+                            c = T(1) / sqrt(t * t + T(1));
+                            sn = t * c;
+                        }
+                    }
+                    sPQ[w][lane][0] = p;
+                    sPQ[w][lane][1] = q;
+                    sCS[w][lane][0] = c;
+                    sCS[w][lane][1] = sn;
+                }
+                __syncwarp();
+                // columns of A and of V: A <- A J, V <- V J
+                for (int t = lane; t < 2 * P * n; t += 32) {
+                    T* M = t < P * n ? A : Vm;
+                    const int u = t < P * n ? t : t - P * n;
+                    const int j = u / n, k = u % n;
+                    const int p = sPQ[w][j][0], q = sPQ[w][j][1];
+                    if (q >= n) continue;
+                    const T c = sCS[w][j][0], sn = sCS[w][j][1];
+                    const T mp = M[k * n + p], mq = M[k * n + q];
+                    M[k * n + p] = c * mp - sn * mq;
+                    M[k * n + q] = sn * mp + c * mq;
+                }
+                __syncwarp();
+                // rows of A: A <- J^T A
+                for (int t = lane; t < P * n; t += 32) {
+                    const int j = t / n, k = t % n;
+                    const int p = sPQ[w][j][0], q = sPQ[w][j][1];
+                    if (q >= n) continue;
+                    const T c = sCS[w][j][0], sn = sCS[w][j][1];
+                    const T ap = A[p * n + k], aq = A[q * n + k];
+                    A[p * n + k] = c * ap - sn * aq;
+                    A[q * n + k] = sn * ap + c * aq;
+                }
+                __syncwarp();
+            }
+        }
+        if (lane < n) sW[w][lane] = A[lane * n + lane] > T(0) ? A[lane * n + lane] : T(0);
+        __syncwarp();
+        for (int t = lane; t < n * n; t += 32) {
+            const int a = t / n, b = t % n;
+            T acc = 0;
+            for (int k = 0; k < n; ++k) acc += Vm[a * n + k] * sW[w][k] * Vm[b * n + k];
+            A[t] = acc;
+        }
+        __syncwarp();
+        // symmetric by construction up to rounding: mirror the upper triangle
+        for (int t = lane; t < n * n; t += 32) {
+            const int a = t / n, b = t % n;
+            if (a > b) A[t] = A[b * n + a];
+        }
+        __syncwarp();
+        const int nv = n / 3;
+        T* ho = hout + 90L * i;
+        for (int t = lane; t < 90; t += 32) {
+            const int blk = t / 9, d = (t % 9) / 3, e = t % 3;
+            int a = 0, b = 0, kk = blk;
+            for (a = 0; a < 4; ++a) {
+                if (kk < 4 - a) { b = a + kk; break; }
+                kk -= 4 - a;
+            }
+            ho[t] = (a < nv && b < nv) ? A[(3 * a + d) * n + 3 * b + e] : T(0);
+        }
+        __syncwarp();
+    }
 }
 
 // gradient entries: key = vertex, value = constraint*4 + slot
@@ -516,15 +650,40 @@ static int barrier_gh(Arena& A, Work& W, const double* X, const ContactSet& cs, 
     if (W[W_BG].ensure(sizeof(double) * 12 * Ca)) return IDP_ERR_CUDA;
     if (hess_mode >= 0 && W[W_BH].ensure(el * 90 * Ca)) return IDP_ERR_CUDA;
     if (C > 0) {
-        if (hess_mode == 1)
-            (::idp::count_launch(), k_barrier_gh<double><<<grid_for(C, 64), 64, 0, s>>>(C, cons, cinst, A.active, X, A.X0, A.dHat2, A.kappa,
-                                                                 A.thickness, W[W_BG].as<double>(), W[W_BH].as<double>()));
-        else if (hess_mode == 0)
-            (::idp::count_launch(), k_barrier_gh<float><<<grid_for(C, 64), 64, 0, s>>>(C, cons, cinst, A.active, X, A.X0, A.dHat2, A.kappa,
-                                                                A.thickness, W[W_BG].as<double>(), W[W_BH].as<float>()));
-        else
-            (::idp::count_launch(), k_barrier_gh<float><<<grid_for(C, 64), 64, 0, s>>>(C, cons, cinst, A.active, X, A.X0, A.dHat2, A.kappa,
-                                                                A.thickness, W[W_BG].as<double>(), nullptr));
+        if (hess_mode < 0) {
+            (::idp::count_launch(), k_barrier_gh<float><<<grid_for(C, 64), 64, 0, s>>>(
+                                        C, cons, cinst, A.active, X, A.X0, A.dHat2, A.kappa, A.thickness,
+                                        W[W_BG].as<double>(), nullptr, nullptr, nullptr, nullptr, nullptr));
+        } else {
+            // PSD scratch: local matrices (144 per constraint) | sizes | list | count
+            const size_t o_n = ((el * 144 * (size_t)Ca) + 255) & ~size_t(255);
+            const size_t o_l = o_n + ((sizeof(int) * (size_t)Ca + 255) & ~size_t(255));
+            const size_t o_c = o_l + ((sizeof(int) * (size_t)Ca + 255) & ~size_t(255));
+            if (W[W_PSD].ensure(o_c + 256)) return IDP_ERR_CUDA;
+            char* pb = W[W_PSD].as<char>();
+            int* hn = reinterpret_cast<int*>(pb + o_n);
+            int* plist = reinterpret_cast<int*>(pb + o_l);
+            unsigned int* pcount = reinterpret_cast<unsigned int*>(pb + o_c);
+            IDP_CUDA_TRY(cudaMemsetAsync(pcount, 0, sizeof(unsigned int), s));
+            const int pgrid = (int)std::min<long>((C + kPsdWarps - 1) / kPsdWarps, 8L * 152);
+            if (hess_mode == 1) {
+                (::idp::count_launch(), k_barrier_gh<double><<<grid_for(C, 64), 64, 0, s>>>(
+                                            C, cons, cinst, A.active, X, A.X0, A.dHat2, A.kappa, A.thickness,
+                                            W[W_BG].as<double>(), W[W_BH].as<double>(), reinterpret_cast<double*>(pb),
+                                            hn, plist, pcount));
+                (::idp::count_launch(), k_psd_warp<double><<<pgrid, 32 * kPsdWarps, 0, s>>>(
+                                            plist, pcount, reinterpret_cast<const double*>(pb), hn,
+                                            W[W_BH].as<double>()));
+            } else {
+                (::idp::count_launch(), k_barrier_gh<float><<<grid_for(C, 64), 64, 0, s>>>(
+                                            C, cons, cinst, A.active, X, A.X0, A.dHat2, A.kappa, A.thickness,
+                                            W[W_BG].as<double>(), W[W_BH].as<float>(), reinterpret_cast<float*>(pb),
+                                            hn, plist, pcount));
+                (::idp::count_launch(), k_psd_warp<float><<<pgrid, 32 * kPsdWarps, 0, s>>>(
+                                            plist, pcount, reinterpret_cast<const float*>(pb), hn,
+                                            W[W_BH].as<float>()));
+            }
+        }
     }
     // gradient scatter: sort (vertex, constraint*4+slot) pairs, sum runs in order
     if (g && C > 0) {
