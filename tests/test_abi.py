@@ -30,7 +30,7 @@ def test_library_exports_header_symbols(gpu_lib):
 def test_status_strings(gpu_lib):
     import idp_gb300
 
-    for code in range(10):
+    for code in range(11):
         s = idp_gb300.status_str(code)
         assert isinstance(s, str) and s and s != "unknown status"
 
