@@ -15,6 +15,7 @@
 #include <map>
 #include <memory>
 #include <mutex>
+#include <new>
 #include <thread>
 #include <vector>
 
@@ -144,8 +145,15 @@ void worker(idp_server* S, int w) {
 
         std::vector<idp_result> res;
         int rc = IDP_OK;
-        if (S->simulated) simulate_cohort(S, cohort, res);
-        else rc = solve_cohort(S, ctx, cohort, res);
+        try {
+            if (S->simulated) simulate_cohort(S, cohort, res);
+            else rc = solve_cohort(S, ctx, cohort, res);
+        } catch (const std::bad_alloc&) {
+            rc = IDP_ERR_CAPACITY;  // host memory for the cohort's arrays
+        } catch (...) {
+            rc = IDP_ERR_INVALID_ARG;
+        }
+        if (rc == IDP_OK && res.size() != cohort.size()) rc = IDP_ERR_STATE;
         size_t bytes = 0;
         if (ctx) idp_device_bytes(ctx, &bytes);
 
