@@ -1173,7 +1173,7 @@ int idp_advance(idp_ctx* c, idp_result* results) {
             W.accd_maxit = W.accd_long = W.accd_total = W.accd_pairs = 0;
             if (W.grid_prof[4]) {
                 const double n = (double)W.grid_prof[4];
-                std::fprintf(stderr, "idp grid pcg per iteration (CTA 0): spmv %.2f us, round1 %.2f us, update %.2f us, round2 %.2f us (%llu iterations)\n",
+                std::fprintf(stderr, "idp grid pcg per iteration (CTA 0): spmv %.2f us, reduction A %.2f us, update %.2f us, reduction B %.2f us (%llu iterations)\n",
                              W.grid_prof[0] / n / 1e3, W.grid_prof[1] / n / 1e3, W.grid_prof[2] / n / 1e3, W.grid_prof[3] / n / 1e3,
                              W.grid_prof[4]);
                 for (auto& v : W.grid_prof) v = 0;

@@ -1290,7 +1290,7 @@ static int pcg_inner(Arena& A, Work& W, const double* b, double rel_tol, int max
     const size_t o_ctl = (o_red + sizeof(T) * kRed * (size_t)(nI + 1) + 255) & ~size_t(255);
     const size_t o_err = o_ctl + sizeof(unsigned int) * kCtlWords * (size_t)(nI + 1);
     if (W[W_PCG_GRID].ensure(o_err + 256)) return IDP_ERR_CUDA;
-    // phase timers of CTA 0 (spmv, round 1, update, round 2, iterations) when profiling
+    // phase timers of CTA 0 (spmv, first reduction, update, second reduction, iterations) when profiling
     static const bool profiling = std::getenv("IDP_PROFILE") != nullptr;
     unsigned long long* d_prof = profiling ? reinterpret_cast<unsigned long long*>(W[W_PCG_GRID].as<char>() + o_err + 64)
                                            : nullptr;
