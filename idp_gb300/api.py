@@ -183,10 +183,23 @@ class TetIPCSim:
         self.PNIterCount = 0
         self.mode = mode
 
-    def add_object_3D(self, X, tets):
-        off = self.X.shape[0]
-        self.X = np.concatenate([self.X, np.asarray(X, float)])
-        self.tet = np.concatenate([self.tet, np.asarray(tets, np.int32) + off]).astype(np.int32)
+    def add_object_3D(self, X, tets=None, translate=(0, 0, 0), rotCenter=(0, 0, 0), rotAxis=(1, 0, 0), rotDeg=0.0,
+                      scale=(1, 1, 1)):
+        """Append a tet mesh: arrays (X, tets), or, as the reference's
+        add_object_3D(filePath, translate, rotCenter, rotAxis, rotDeg, scale)
+        (FEMDiscreteShellBase.py:184-188), a legacy VTK file path whose points
+        are then transformed. Returns the mesh counter."""
+        from . import meshio
+
+        if isinstance(X, (str, bytes)) or hasattr(X, "__fspath__"):
+            self.X, self.tet, counter = meshio.read_tet_vtk(X, self.X, self.tet)
+        else:
+            off = self.X.shape[0]
+            self.X = np.concatenate([self.X, np.asarray(X, float)])
+            self.tet = np.concatenate([self.tet, np.asarray(tets, np.int32) + off]).astype(np.int32)
+            counter = (off, self.tet.shape[0] - len(tets), self.X.shape[0], self.tet.shape[0])
+        meshio.transform_points(self.X, translate, rotCenter, rotAxis, rotDeg, scale, counter)
+        return counter
 
     def initialize_added_objects(self, velocity, p_density, E, nu):
         m = meshgen.lumped_mass(self.X, self.tet, p_density)

@@ -1,0 +1,84 @@
+"""Mesh files of the reference's drivers (idp_gb300.meshio, restating
+Utils/MESHIO.h readers and writers) on hand-written and round-tripped files."""
+import math
+
+import numpy as np
+import pytest
+
+
+def test_obj_reader_faces_quads_and_offsets(tmp_path):
+    from idp_gb300 import meshio
+
+    p = tmp_path / "m.obj"
+    p.write_text("# comment\nv 0 0 0\nv 1 0 0\nv 1 1 0\nv 0 1 0\nvn 0 0 1\nvt 0 0\n"
+                 "f 1 2 3\nf 1/1 3/3 4/4\nf 1//1 2//1 3//1 4//1\n")
+    X, F, cnt = meshio.read_tri_obj(p)
+    assert X.shape == (4, 3) and cnt == (0, 0, 4, 4)
+    # plain triangle, slash tokens, then a quad split into (0,1,2) and (0,2,3)
+    assert F.tolist() == [[0, 1, 2], [0, 2, 3], [0, 1, 2], [0, 2, 3]]
+    # appending offsets the new faces by the vertices already present
+    X2, F2, cnt2 = meshio.read_tri_obj(p, X, F)
+    assert cnt2 == (4, 4, 8, 8)
+    assert F2[4:].tolist() == (F + 4).tolist()
+
+
+def test_vtk_round_trip_and_counters(tmp_path):
+    from idp_gb300 import meshgen, meshio
+
+    X, T = meshgen.bar(2, 3, 4, seed=0)
+    p = tmp_path / "bar.vtk"
+    meshio.write_tet_vtk(p, X, T)
+    X1, T1, cnt = meshio.read_tet_vtk(p)
+    assert np.array_equal(X1, X) and np.array_equal(T1, T)
+    assert cnt == (0, 0, X.shape[0], T.shape[0])
+    X2, T2, cnt2 = meshio.read_tet_vtk(p, X1, T1)
+    assert cnt2 == (X.shape[0], T.shape[0], 2 * X.shape[0], 2 * T.shape[0])
+    assert np.array_equal(T2[T.shape[0]:], T + X.shape[0])
+    bad = tmp_path / "bad.vtk"
+    bad.write_text(p.read_text().replace(f"POINTS {X.shape[0]}", f"POINTS {X.shape[0] + 1}"))
+    with pytest.raises(ValueError):
+        meshio.read_tet_vtk(bad)
+
+
+def test_obj_round_trip(tmp_path):
+    from idp_gb300 import meshgen, meshio
+
+    X, T, _ = meshgen.blob(n=10, lmax=3, seed=0)
+    Xs, F = meshgen.shell_from_tets(X, T)
+    p = tmp_path / "s.obj"
+    meshio.write_tri_obj(p, Xs, F)
+    X1, F1, _ = meshio.read_tri_obj(p)
+    assert np.array_equal(F1, F)
+    assert np.allclose(X1, Xs, rtol=1e-6, atol=1e-7)  # %e keeps 7 significant digits
+
+
+def test_transform_points():
+    from idp_gb300 import meshio
+
+    X = np.array([[1.0, 0.0, 0.0], [2.0, 0.0, 0.0], [0.0, 0.0, 1.0]])
+    Y = meshio.transform_points(X.copy(), (0, 0, 10), (0, 0, 0), (0, 0, 1), 90.0, (2, 2, 2), (0, 0, 2, 0))
+    assert np.allclose(Y[0], [0.0, 2.0, 10.0]) and np.allclose(Y[1], [0.0, 4.0, 10.0])
+    assert np.array_equal(Y[2], X[2])  # outside the counter's range
+    # rotation about an axis through a centre keeps distances to the axis
+    rng = np.random.default_rng(0)
+    P = rng.normal(size=(20, 3))
+    Q = meshio.transform_points(P.copy(), (0, 0, 0), (1, 1, 1), (1, 2, 3), 37.0, (1, 1, 1))
+    a = np.array([1, 2, 3]) / math.sqrt(14)
+    d = lambda Z: np.linalg.norm(np.cross(Z - 1.0, a), axis=1)
+    assert np.allclose(d(P), d(Q))
+
+
+def test_tet_sim_reads_vtk(tmp_path):
+    from idp_gb300 import meshgen, meshio
+    from idp_gb300.api import TetIPCSim
+
+    X, T = meshgen.bar(2, 2, 3, seed=1)
+    p = tmp_path / "b.vtk"
+    meshio.write_tet_vtk(p, X, T)
+    sim = TetIPCSim()
+    cnt = sim.add_object_3D(str(p), (1.0, 0.0, 0.0), (0, 0, 0), (1, 0, 0), 0.0, (1, 1, 1))
+    cnt2 = sim.add_object_3D(str(p), (0.0, 5.0, 0.0), (0, 0, 0), (1, 0, 0), 0.0, (1, 1, 1))
+    assert cnt == (0, 0, X.shape[0], T.shape[0])
+    assert cnt2[0] == X.shape[0] and sim.tet.shape[0] == 2 * T.shape[0]
+    assert np.allclose(sim.X[: X.shape[0]], X + [1.0, 0.0, 0.0])
+    assert np.allclose(sim.X[X.shape[0]:], X + [0.0, 5.0, 0.0])
