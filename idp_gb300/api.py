@@ -183,22 +183,28 @@ class TetIPCSim:
         self.PNIterCount = 0
         self.mode = mode
 
-    def add_object_3D(self, X, tets=None, translate=(0, 0, 0), rotCenter=(0, 0, 0), rotAxis=(1, 0, 0), rotDeg=0.0,
-                      scale=(1, 1, 1)):
-        """Append a tet mesh: arrays (X, tets), or, as the reference's
+    def add_object_3D(self, X, *args):
+        """Append a tet mesh and return its mesh counter. Either
         add_object_3D(filePath, translate, rotCenter, rotAxis, rotDeg, scale)
-        (FEMDiscreteShellBase.py:184-188), a legacy VTK file path whose points
-        are then transformed. Returns the mesh counter."""
+        as the reference's driver (FEMDiscreteShellBase.py:184-188: a legacy
+        VTK file whose points are then transformed), or
+        add_object_3D(X, tets[, translate, rotCenter, rotAxis, rotDeg, scale])
+        with arrays."""
         from . import meshio
 
         if isinstance(X, (str, bytes)) or hasattr(X, "__fspath__"):
             self.X, self.tet, counter = meshio.read_tet_vtk(X, self.X, self.tet)
+            xf = args
         else:
-            off = self.X.shape[0]
+            tets = np.asarray(args[0], np.int32)
+            off, toff = self.X.shape[0], self.tet.shape[0]
             self.X = np.concatenate([self.X, np.asarray(X, float)])
-            self.tet = np.concatenate([self.tet, np.asarray(tets, np.int32) + off]).astype(np.int32)
-            counter = (off, self.tet.shape[0] - len(tets), self.X.shape[0], self.tet.shape[0])
-        meshio.transform_points(self.X, translate, rotCenter, rotAxis, rotDeg, scale, counter)
+            self.tet = np.concatenate([self.tet, tets + off]).astype(np.int32)
+            counter = (off, toff, self.X.shape[0], self.tet.shape[0])
+            xf = args[1:]
+        if xf:
+            translate, rotCenter, rotAxis, rotDeg, scale = xf
+            meshio.transform_points(self.X, translate, rotCenter, rotAxis, rotDeg, scale, counter)
         return counter
 
     def initialize_added_objects(self, velocity, p_density, E, nu):
