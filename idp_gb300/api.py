@@ -229,3 +229,109 @@ class TetIPCSim:
             10, None, "")
         self.PNIterCount += it
         return it
+
+
+class ShellFlowSim:
+    """The triangle-shell flow-mode slice of FEMDiscreteShellBase that the
+    normal-flow scripts drive (Projects/FEMShell/12-14_normal_flow.py):
+    add_shell_3D, initialize, initialize_OIPC, the frame loop of
+    SimulationBase (Python/Drivers/SimulationBase.py:76-103) and
+    advance_one_time_step with Update_Normal_Flow_Neumann
+    (FEMDiscreteShellBase.py:266-276, 332-340)."""
+
+    def __init__(self, precision="double", dim=3, mode=MODE_MIXED):
+        if dim != 3:
+            raise NotImplementedError("2D shells are not part of this path")
+        self.X = np.zeros((0, 3))
+        self.Elem = np.zeros((0, 3), np.int32)
+        self.dt = 0.04
+        self.frame_dt = 0.04
+        self.frame_num = 1
+        self.PNTol = 1e-3
+        self.flow = False
+        self.normalFlowMag = 0.0
+        self.withCollision = True
+        self.gravity = (0.0, 0.0, 0.0)
+        self.bendingStiffMult = 1.0
+        self.shell_density = 1000.0
+        self.shell_thickness = 0.001
+        self.dHat2 = 1e-6
+        self.kappa = [1e5, 0.0, 0.0]
+        self.thickness = 0.0  # IPC offset
+        self.DBC = None
+        self.PNIterCount = 0
+        self.mode = mode
+        self._ctx = None
+        self._ctx_h = None
+
+    def add_shell_3D(self, filePath, translate, rotCenter, rotAxis, rotDeg):
+        from . import meshio
+
+        self.X, self.Elem, counter = meshio.read_tri_obj(filePath, self.X, self.Elem)
+        meshio.transform_points(self.X, translate, rotCenter, rotAxis, rotDeg, (1.0, 1.0, 1.0), counter)
+        return counter
+
+    def _mass(self):
+        X, F = self.X, self.Elem
+        area = np.linalg.norm(np.cross(X[F[:, 1]] - X[F[:, 0]], X[F[:, 2]] - X[F[:, 0]]), axis=1) / 2
+        m = np.zeros(X.shape[0])
+        np.add.at(m, F.reshape(-1), np.repeat(area * self.shell_thickness * self.shell_density / 3, 3))
+        return m
+
+    def initialize(self, p_density, E, nu, thickness, caseI):
+        """Shell material (Initialize_Shell_Hinge_EIPC's density and
+        thickness; E and nu do not enter the flow energy); in flow mode the
+        open boundary's vertices are fixed (FEM.Boundary_Dirichlet)."""
+        self.shell_density, self.shell_thickness = float(p_density), float(thickness)
+        self.thickness = float(thickness)
+        if self.flow:
+            e = np.sort(self.Elem[:, [[0, 1], [1, 2], [2, 0]]].reshape(-1, 2), axis=1)
+            uniq, cnt = np.unique(e, axis=0, return_counts=True)
+            bnd = np.unique(uniq[cnt == 1].reshape(-1))
+            self.DBC = bnd.astype(np.int32) if bnd.size else None
+
+    def initialize_OIPC(self, thickness, offset, stiffMult=1.0):
+        """Initialize_OIPC (DISCRETE_SHELL.h:555-577): d-hat = thickness,
+        kappa from the mean lumped mass."""
+        self.dHat2 = float(thickness) ** 2
+        k, km = initialize_oipc(float(self._mass().mean()), self.dHat2, stiffMult)
+        self.kappa = [k, km, 0.0]
+        self.thickness = float(offset)
+
+    def _context(self, h):
+        if self._ctx is None or self._ctx_h != h:
+            X = self.X.copy()
+            self._ctx = Context(h=h, newton_tol=self.PNTol, thickness=self.thickness, mode=self.mode)
+            self._ctx.add_shell_instance(X, self.Elem, self.shell_density, self.shell_thickness, self.dHat2,
+                                         self.kappa[0], self.kappa[1], dbc_idx=self.DBC)
+            self._ctx.commit()
+            self._ctx_h = h
+        return self._ctx
+
+    def advance_one_time_step(self, dt):
+        if not self.flow:
+            raise NotImplementedError("shells without flow mode (membrane/bending) are not part of this path")
+        ctx = self._context(dt)
+        ctx.set_positions(0, self.X)
+        ctx.set_kappa(0, self.kappa)
+        if self.normalFlowMag != 0:
+            ctx.set_normal_flow(0, dt * dt * self.normalFlowMag)
+        rc, res = ctx.advance(check=False)
+        if rc not in (0, IDP_WARN_ITER_CAP):
+            raise IDPError(rc, "advance_one_time_step")
+        X, _, k = ctx.state(0)
+        self.X[...] = X
+        self.kappa[0] = k[0]
+        self.PNIterCount += res[0]["newton_iters"]
+        return res[0]["newton_iters"]
+
+    def advance_one_frame(self, f):
+        remain = self.frame_dt
+        while remain > 0:
+            cur = self.dt if remain > 2 * self.dt else (remain / 2 if remain > self.dt else remain)
+            self.advance_one_time_step(cur)
+            remain -= cur
+
+    def run(self):
+        for f in range(self.frame_num):
+            self.advance_one_frame(f + 1)

@@ -185,3 +185,41 @@ def test_reference_shaped_flow_call(oracle, gpu_lib):
     Xg, _, _ = ctx.state(0)
     assert np.allclose(X, Xg, rtol=0, atol=1e-12 * np.abs(Xg).max())
     ctx.close()
+
+
+def test_normal_flow_script_driver(oracle, gpu_lib, tmp_path):
+    """The normal-flow script's calls (12-14_normal_flow.py) through
+    ShellFlowSim, on a shell read from an OBJ file, give the same states as
+    the C-ABI calls they stand for."""
+    import idp_gb300 as idp
+    from idp_gb300 import meshio
+    from idp_gb300.api import ShellFlowSim
+
+    X, F = shell()
+    p = tmp_path / "blob.obj"
+    meshio.write_tri_obj(p, X, F)
+    sim = ShellFlowSim("double", 3)
+    smooth = 0.5
+    sim.normalFlowMag = 0.005
+    sim.frame_num = 2
+    sim.add_shell_3D(str(p), (0, 0, 0), (0, 0, 0), (0, 0, 0), 0)
+    sim.dt = 1.0 * smooth
+    sim.frame_dt = 1.0 * smooth
+    sim.flow = True
+    sim.normalFlowMag /= smooth * smooth
+    sim.initialize(1, 0, 0, 1, 0)
+    sim.initialize_OIPC(1e-3, 0)
+    X0 = sim.X.copy()
+    sim.run()
+    assert sim.DBC is None  # closed surface: nothing fixed
+    ctx = idp.Context(h=0.5, mode=idp.MODE_MIXED)
+    k0, km0 = idp.api.initialize_oipc(float(sim._mass().mean()), 1e-6)
+    ctx.add_shell_instance(X0, F, 1.0, 1.0, 1e-6, k0, km0)
+    ctx.commit()
+    for _ in range(2):
+        ctx.set_normal_flow(0, 0.25 * 0.005 / 0.25)
+        ctx.advance(check=False)
+    Xg, _, _ = ctx.state(0)
+    assert np.array_equal(sim.X, Xg)
+    assert not np.array_equal(Xg, X0)
+    ctx.close()
