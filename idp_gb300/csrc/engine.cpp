@@ -2,7 +2,8 @@
 // (surface primitives in the reference's order, BSR pattern, chunk tables)
 // and the batched Newton driver that restates
 // Advance_One_Step_IE_Discrete_Shell (FEM/Shell/IMPLICIT_EULER.h:151-891) and
-// Line_Search (IMPLICIT_EULER.h:9-149) for tet meshes with offset IPC.
+// Line_Search (IMPLICIT_EULER.h:9-149) for tet meshes with offset IPC, and its
+// flow-mode variant for triangle shells (Advance_One_Step_IE_Flow).
 //
 // Every instance of a context runs its own Newton iteration; the kernels of
 // one Newton iteration serve all instances that are still iterating, and an

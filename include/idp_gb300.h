@@ -1,11 +1,14 @@
 /*
  * idp_gb300 — C ABI of the GB300 injective-deformation Newton step.
  *
- * Replaces the pybind11 entry point FEM.DiscreteShell.Advance_One_Step_IE_Hinge
+ * Replaces the pybind11 entry points FEM.DiscreteShell.Advance_One_Step_IE_Hinge
  * (Library/FEM/Shell/DISCRETE_SHELL.h:1110, body
- * Library/FEM/Shell/IMPLICIT_EULER.h:151-891) for tet meshes with offset IPC
- * self-contact, and exposes the sub-steps the reference computes inside it so
- * a caller (or a test) can check each one.
+ * Library/FEM/Shell/IMPLICIT_EULER.h:151-891) for tet meshes and
+ * Advance_One_Step_IE_Flow (DISCRETE_SHELL.h:1113) for triangle shells in flow
+ * mode, both with offset IPC self-contact; exposes the sub-steps the reference
+ * computes inside them so a caller (or a test) can check each one; and adds
+ * an exact intersection check, context reuse and a request server for many
+ * independent solves.
  *
  * Conventions: positions are double[3*V] (x0,y0,z0,x1,...), tets int32[4*T]
  * with instance-local vertex ids. The caller owns every host buffer; the
