@@ -7,9 +7,14 @@ meaning for the arguments this path reads; storages are plain numpy arrays /
 dicts instead of JGSL storages. It mutates ``X`` and ``nodeAttr['v']`` in
 place and returns the Newton iteration count, like the reference.
 
+``FEM.DiscreteShell.Advance_One_Step_IE_Flow`` does the same for the flow-mode
+export (``DISCRETE_SHELL.h:1113``) over a triangle-shell instance.
+
 ``TetIPCSim`` mirrors the slice of ``FEMDiscreteShellBase`` that sets up a
 tet mesh with offset IPC (``add_object_3D``, ``initialize_added_objects``,
-``initialize_OIPC``, ``advance_one_time_step``).
+``initialize_OIPC``, ``advance_one_time_step``); ``ShellFlowSim`` the slice the
+normal-flow scripts drive (``add_shell_3D``, ``initialize``,
+``initialize_OIPC``, ``run``).
 """
 from __future__ import annotations
 
@@ -19,7 +24,7 @@ import numpy as np
 
 from . import Context, IDPError, IDP_WARN_ITER_CAP, MODE_MIXED, meshgen
 
-_UNSUPPORTED = "not part of the GB300 path (tet meshes with offset IPC only)"
+_UNSUPPORTED = "not part of the GB300 path (tet meshes, and shells in flow mode, with offset IPC)"
 
 
 def _empty(x):
