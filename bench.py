@@ -243,7 +243,8 @@ def cpu_baseline(probs, budget_s, newton_budget=0):
     return {"value": rate, "unit": unit, "cores": cores, "kind": "port",
             "sample": (f"oracle {'solves capped at %d Newton iterations' % newton_budget if newton_budget else 'full solves'}"
                        f" of the {solved} smallest instance(s) ({tets_done} tets, {iters} Newton iterations, "
-                       f"{t_used:.1f} s); scaled to the mean instance ({mean_tets:.0f} tets)")}
+                       f"{t_used:.1f} s); scaled to the mean instance ({mean_tets:.0f} tets); element and contact "
+                       "loops OpenMP on all cores, sparse LU (SciPy SuperLU) on one")}
 
 
 H = 0.1
@@ -298,7 +299,8 @@ def cpu_baseline_flow(full_tets, step, budget_s, n_small=24):
     cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
     return {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
             "sample": f"oracle first flow step of the blob at {n_small}^3 ({T} tets), {solves} solve(s), {iters} "
-                      f"Newton iterations, {t_used:.1f} s; solves/s scaled to {full_tets} tets by tet count"}
+                      f"Newton iterations, {t_used:.1f} s; solves/s scaled to {full_tets} tets by tet count; "
+                      "element and contact loops OpenMP on all cores, sparse LU (SciPy SuperLU) on one"}
 
 
 def run_flow(args):
