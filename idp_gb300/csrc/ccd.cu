@@ -8,8 +8,9 @@
 // voxel grid is replicated exactly: voxel size = mean surface-edge length,
 // span cap = alpha * mean|dir| / voxel size, grid corner = min over x and
 // x + alpha*dir minus thickness/2, floor((p - corner) / voxel) per axis. The
-// two means are fixed-order sums (prims.cuh det_sum order) so the oracle can
-// reproduce them bit for bit. A pair is tested iff the integer boxes overlap.
+// two means are summed in the reference's own order: the edge lengths as
+// Eigen's vectorised mean() adds them, |dir| by the reference's serial loop
+// (SPATIAL_HASH.h:455-475). A pair is tested iff the integer boxes overlap.
 //
 // Every pair's ACCD result is independent of the order pairs are visited (a
 // pair either finishes below the bound with its own toc, or is discarded), so
@@ -33,8 +34,92 @@ constexpr int ACCD_MAX_ITERS = 200000;
 // pairs above 1000 iterations, total iterations, pairs
 __device__ unsigned long long g_accd_stats[4];
 
-// fixed-order sum by one CTA of 256 threads (same tiling as det_sum)
-__device__ double cta_det_sum(const double* x, long n, double* scratch) {
+__global__ void k_edge_len(long nE, const int2* __restrict__ e, const double* __restrict__ X, double* __restrict__ len) {
+    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nE) return;
+    int2 v = e[i];
+    len[i] = sqrt(sqn(ld3(X, v.x) - ld3(X, v.y)));
+}
+
+__global__ void k_abs_dir(long nN, const int* __restrict__ nodes, const double* __restrict__ dir, double* __restrict__ out) {
+    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nN) return;
+    int v = nodes[i];
+    out[3 * i] = fabs(dir[3 * v]);
+    out[3 * i + 1] = fabs(dir[3 * v + 1]);
+    out[3 * i + 2] = fabs(dir[3 * v + 2]);
+}
+
+// first level of the fixed-order estimate of sum |dir| (a span cap can only
+// apply when this estimate comes near 1), one CTA per 2048-item tile of every
+// instance's |dir| segment
+__global__ void k_span_tiles(const SpanTile* __restrict__ tiles, const unsigned char* __restrict__ active,
+                             const double* __restrict__ absdir, double* __restrict__ out) {
+    __shared__ double a[256];
+    const SpanTile t = tiles[blockIdx.x];
+    if (!active[t.inst]) return;
+    const double* in = absdir + t.start;
+    double s = 0.0;
+    for (int r = 0; r < 8; ++r) {
+        long i = (long)t.k * 2048 + r * 256 + threadIdx.x;
+        if (i < t.m) s += in[i];
+    }
+    a[threadIdx.x] = s;
+    __syncthreads();
+    for (int st = 128; st > 0; st >>= 1) {
+        if (threadIdx.x < st) a[threadIdx.x] += a[threadIdx.x + st];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[blockIdx.x] = a[0];
+}
+
+// Sum of x[0..n) in the order of Eigen's vectorised redux of a dense double
+// vector on the reference's AVX build (`eLen.mean()`, SPATIAL_HASH.h:455-464;
+// Eigen/src/Core/Redux.h, LinearVectorizedTraversal over 4-lane packets):
+// lane l of accumulator 0 sums items l, l+8, ..., lane l of accumulator 1
+// items 4+l, 12+l, ... over the first 8*floor(n/8) items; the accumulators
+// are added lane by lane, one more 4-item packet is added when n mod 8 >= 4,
+// the lanes reduce as (l0 + l2) + (l1 + l3) and the last n mod 4 items follow
+// one at a time; fewer than 4 items are summed left to right. Lanes 0-7 of
+// the calling warp each carry one accumulator lane; every lane of the warp
+// must call it, and lane 0 receives the result.
+__device__ double warp_eigen_sum(const double* x, long n) {
+    const int lane = threadIdx.x & 31;
+    const long aligned = n & ~3L, aligned2 = n & ~7L;
+    double acc = 0.0;
+    if (aligned > 4) {
+        if (lane < 8) {
+#pragma unroll 8
+            for (long i = lane; i < aligned2; i += 8) acc += x[i];
+        }
+    } else if (aligned == 4 && lane < 4) {
+        acc = x[lane];
+    }
+    const double hi = __shfl_down_sync(0xffffffffu, acc, 4);
+    if (aligned > 4 && lane < 4) {
+        acc = acc + hi;
+        if (aligned > aligned2) acc = acc + x[aligned2 + lane];
+    }
+    const double l1 = __shfl_down_sync(0xffffffffu, acc, 1);
+    const double l2 = __shfl_down_sync(0xffffffffu, acc, 2);
+    const double l3 = __shfl_down_sync(0xffffffffu, acc, 3);
+    double res = 0.0;
+    if (lane == 0) {
+        if (aligned == 0) {
+            if (n > 0) {
+                res = x[0];
+                for (long i = 1; i < n; ++i) res += x[i];
+            }
+        } else {
+            res = (acc + l2) + (l1 + l3);
+            for (long i = aligned; i < n; ++i) res += x[i];
+        }
+    }
+    return res;
+}
+
+// fixed-order sum of the tile sums (used for the span-cap estimate only)
+__device__ double cta_tree_sum(const double* x, long n, double* scratch) {
     __shared__ double a[256];
     if (n <= 0) return 0.0;
     const double* in = x;
@@ -68,70 +153,45 @@ __device__ double cta_det_sum(const double* x, long n, double* scratch) {
     }
 }
 
-__global__ void k_edge_len(long nE, const int2* __restrict__ e, const double* __restrict__ X, double* __restrict__ len) {
-    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nE) return;
-    int2 v = e[i];
-    len[i] = sqrt(sqn(ld3(X, v.x) - ld3(X, v.y)));
-}
-
-__global__ void k_abs_dir(long nN, const int* __restrict__ nodes, const double* __restrict__ dir, double* __restrict__ out) {
-    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nN) return;
-    int v = nodes[i];
-    out[3 * i] = fabs(dir[3 * v]);
-    out[3 * i + 1] = fabs(dir[3 * v + 1]);
-    out[3 * i + 2] = fabs(dir[3 * v + 2]);
-}
-
-// per instance: voxel size, span cap (SPATIAL_HASH.h:455-482)
-// first level of the fixed-order sums, one CTA per 2048-item tile of every
-// instance's edge-length and |dir| segments (tile t of a segment of length m
-// covers items 2048 t ...; same arithmetic as one tile of cta_det_sum)
-__global__ void k_span_tiles(const SpanTile* __restrict__ tiles, const unsigned char* __restrict__ active,
-                             const double* __restrict__ len, const double* __restrict__ absdir,
-                             double* __restrict__ out) {
-    __shared__ double a[256];
-    const SpanTile t = tiles[blockIdx.x];
-    if (!active[t.inst]) return;
-    const double* in = (t.kind ? absdir : len) + t.start;
-    double s = 0.0;
-    for (int r = 0; r < 8; ++r) {
-        long i = (long)t.k * 2048 + r * 256 + threadIdx.x;
-        if (i < t.m) s += in[i];
-    }
-    a[threadIdx.x] = s;
-    __syncthreads();
-    for (int st = 128; st > 0; st >>= 1) {
-        if (threadIdx.x < st) a[threadIdx.x] += a[threadIdx.x + st];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) out[blockIdx.x] = a[0];
-}
-
-// the rest of the recursion per instance: a segment of one tile is its tile
-// sum; otherwise the tile sums are summed by the same fixed-order scheme
+// per instance: voxel size and span cap (SPATIAL_HASH.h:455-482). The voxel
+// size is the Eigen-order mean edge length. pSize is the reference's serial
+// sum; it only matters when the span exceeds 1, so it is computed (by one
+// thread, 3 Sn dependent additions) only when a fixed-order estimate of the
+// span is within the two sums' rounding-error bound ((n + 32) u) of 1 or
+// above it.
 __global__ void k_span_cap(int nI, const unsigned char* __restrict__ active, const int* __restrict__ se_off,
                            const int* __restrict__ sn_off, const int* __restrict__ tile_off,
-                           const double* __restrict__ tsum, double* __restrict__ scratch, double* __restrict__ alpha,
-                           double* __restrict__ voxel_size) {
+                           const double* __restrict__ tsum, const double* __restrict__ len,
+                           const double* __restrict__ absdir, double* __restrict__ scratch,
+                           double* __restrict__ alpha, double* __restrict__ voxel_size) {
+    __shared__ double s_vsz;
     int i = blockIdx.x;
     if (!active[i]) return;
-    long ne = se_off[i + 1] - se_off[i], nn = sn_off[i + 1] - sn_off[i];
-    const int te0 = tile_off[2 * i], tn0 = tile_off[2 * i + 1], tn1 = tile_off[2 * i + 2];
-    const int nte = tn0 - te0, ntn = tn1 - tn0;
+    const long e0 = se_off[i], ne = se_off[i + 1] - se_off[i];
+    const long n0 = sn_off[i], nn = sn_off[i + 1] - sn_off[i];
+    const int tn0 = tile_off[2 * i + 1], tn1 = tile_off[2 * i + 2];
+    const int ntn = tn1 - tn0;
     double* sc = scratch + 2 * (long)tile_off[2 * i] + 8 * (long)i;
-    double vsz = 1.0;
-    if (ne) {
-        double s = nte == 1 ? tsum[te0] : cta_det_sum(tsum + te0, nte, sc);
-        vsz *= s / (double)ne;
+    if (threadIdx.x < 32) {
+        double es = warp_eigen_sum(len + e0, ne);
+        if (threadIdx.x == 0) s_vsz = ne ? 1.0 * (es / (double)ne) : 1.0;
     }
-    double ps = ntn == 0 ? 0.0 : (ntn == 1 ? tsum[tn0] : cta_det_sum(tsum + tn0, ntn, sc));
+    double ps = ntn == 0 ? 0.0 : (ntn == 1 ? tsum[tn0] : cta_tree_sum(tsum + tn0, ntn, sc));
+    __syncthreads();
     if (threadIdx.x == 0) {
-        double pSize = ps / (double)(nn * 3);
+        const double vsz = s_vsz;
+        const double cnt = (double)(nn * 3);
         double a = alpha[i];
-        double spanSize = a * pSize / vsz;
-        if (spanSize > 1) a /= spanSize;
+        const double est = a * (ps / cnt) / vsz;
+        const double bound = 1.0 - ((double)(3 * nn) + 32.0) * 2.3e-16;
+        if (!(est < bound)) {
+            const double* d = absdir + 3 * n0;
+            double pSize = 0.0;
+            for (long k = 0; k < 3 * nn; ++k) pSize += d[k];
+            pSize /= cnt;
+            const double spanSize = a * pSize / vsz;
+            if (spanSize > 1) a /= spanSize;
+        }
         alpha[i] = a;
         voxel_size[i] = vsz;
     }
@@ -602,9 +662,9 @@ int ccd_stepsize(Arena& A, Work& W, const double* X, const double* dir, double* 
     if (W[W_SPAN].ensure(sizeof(double) * (A.n_span_tiles + 1))) return IDP_ERR_CUDA;
     double* tsum = W[W_SPAN].as<double>();
     if (A.n_span_tiles > 0)
-        (::idp::count_launch(), k_span_tiles<<<A.n_span_tiles, 256, 0, s>>>(A.span_tiles, A.active, len, absdir, tsum));
+        (::idp::count_launch(), k_span_tiles<<<A.n_span_tiles, 256, 0, s>>>(A.span_tiles, A.active, absdir, tsum));
     (::idp::count_launch(), k_span_cap<<<nI, 256, 0, s>>>(nI, A.active, d_se_off, d_sn_off, A.span_tile_off, tsum,
-                                                          sumsc, alpha, vsz));
+                                                          len, absdir, sumsc, alpha, vsz));
     // grid
     if (W[W_BBOX].ensure(sizeof(unsigned long long) * 6 * nI) || W[W_GRIDP].ensure(sizeof(GridP) * nI))
         return IDP_ERR_CUDA;

@@ -778,16 +778,16 @@ int idp_commit(idp_ctx* c) {
             for (int a = 0; a < 3; ++a) vt[vfill[stri[3 * f + a]]++] = (int)f;
         rc |= upload(c, A.vtri_ptr, vtp);
         rc |= upload(c, A.vtri, vt);
-        // tiles of the CCD span sums (2048 items each) per instance
+        // tiles (2048 items each) of the fixed-order estimate of each
+        // instance's sum |dir| that decides whether the CCD span cap can apply
+        // (toff[2i] = toff[2i+1]: no edge-length tiles, the voxel size is
+        // summed in the reference's order by one warp)
         std::vector<SpanTile> tiles;
         std::vector<int> toff(2 * nI + 1, 0);
         for (int i = 0; i < nI; ++i) {
-            const int seg[2][2] = {{A.se_off[i], A.se_off[i + 1] - A.se_off[i]},
-                                   {3 * A.sn_off[i], 3 * (A.sn_off[i + 1] - A.sn_off[i])}};
-            for (int kind = 0; kind < 2; ++kind) {
-                toff[2 * i + kind] = (int)tiles.size();
-                for (int k = 0; k * 2048 < seg[kind][1]; ++k) tiles.push_back({i, kind, seg[kind][0], seg[kind][1], k});
-            }
+            const int start = 3 * A.sn_off[i], m = 3 * (A.sn_off[i + 1] - A.sn_off[i]);
+            toff[2 * i] = toff[2 * i + 1] = (int)tiles.size();
+            for (int k = 0; k * 2048 < m; ++k) tiles.push_back({i, 1, start, m, k});
         }
         toff[2 * nI] = (int)tiles.size();
         A.n_span_tiles = (int)tiles.size();

@@ -56,10 +56,11 @@ struct InstState {
     double g0 = 0;             // gradient norm at the first Newton iteration
 };
 
-// one 2048-item tile of an instance's CCD span sums (edge lengths or |dir|)
+// one 2048-item tile of the fixed-order estimate of an instance's sum |dir|
+// (the CCD span-cap test)
 struct SpanTile {
     int inst;
-    int kind;   // 0: edge lengths, 1: |dir| components
+    int kind;   // 1: |dir| components (the only kind built)
     int start;  // segment start in its array
     int m;      // segment length
     int k;      // tile index inside the segment

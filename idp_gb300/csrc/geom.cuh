@@ -27,18 +27,31 @@ __device__ __forceinline__ double d_EE(D3 ea0, D3 ea1, D3 eb0, D3 eb1) {
     return aTb * aTb / sqn(b);
 }
 
-// unpivoted LDL^T solve of the 2x2 normal equations of the PT classifier
+// Solve of the PT classifier's 2x2 normal equations (the reference's
+// `(basis * basis.transpose()).ldlt().solve(basis * (p - o))`,
+// DISTANCE_TYPE.h:46,54,62) by Eigen's LDLT with diagonal pivoting: the
+// larger diagonal entry first (ties keep the identity); D0 = m00,
+// l = m10 / D0, D1 = m11 - l * (D0 * l); forward substitution, division by
+// D_i (0 when |D_i| <= DBL_MIN), back substitution, inverse permutation.
 __device__ __forceinline__ void pt_param(D3 r0, D3 n, D3 p, D3 o, double& s, double& t) {
     D3 r1 = cross(r0, n);
     D3 q = p - o;
     double a00 = dot(r0, r0), a01 = dot(r0, r1), a11 = dot(r1, r1);
     double b0 = dot(r0, q), b1 = dot(r1, q);
-    double D0 = a00;
-    double l = a01 / D0;
-    double D1 = a11 - l * a01;
-    double y1 = b1 - l * b0;
-    t = y1 / D1;
-    s = b0 / D0 - l * t;
+    const bool piv = fabs(a11) > fabs(a00);
+    const double m00 = piv ? a11 : a00, m11 = piv ? a00 : a11;
+    double y0 = piv ? b1 : b0, y1 = piv ? b0 : b1;
+    const double D0 = m00;
+    double l = a01;
+    if (fabs(D0) > 0.0) l = a01 / D0;
+    const double D1 = m11 - l * (D0 * l);
+    y1 = y1 - l * y0;
+    const double tiny = 2.2250738585072014e-308;
+    y0 = fabs(D0) > tiny ? y0 / D0 : 0.0;
+    y1 = fabs(D1) > tiny ? y1 / D1 : 0.0;
+    y0 = y0 - l * y1;
+    s = piv ? y1 : y0;
+    t = piv ? y0 : y1;
 }
 
 __device__ inline int type_PT(D3 p, D3 t0, D3 t1, D3 t2) {

@@ -54,17 +54,36 @@ inline int type_PE(V3 p, V3 e0, V3 e1) {  // DISTANCE_TYPE.h:11-28
     return 2;
 }
 
-// 2x2 SPD solve used by the PT classifier. The reference calls Eigen's LDLT
-// (DISTANCE_TYPE.h:46); this restatement uses an unpivoted LDL^T:
-// D0 = a00, l = a10 / D0, D1 = a11 - l * a10, x1 = (b1 - l * b0) / D1,
-// x0 = b0 / D0 - l * x1.
+// 2x2 solve of the PT classifier's normal equations, restating the
+// reference's `(basis * basis.transpose()).ldlt().solve(...)`
+// (DISTANCE_TYPE.h:46,54,62) with Eigen's LDLT as published in its source
+// (Eigen/src/Cholesky/LDLT.h, ldlt_inplace<Lower>::unblocked and
+// LDLT::_solve_impl, Eigen 3.3/3.4):
+//   pivot: the larger diagonal entry goes first (|a11| > |a00|, strictly: a
+//          tie keeps the identity, as Eigen's maxCoeff keeps the first maximum);
+//   factor: D0 = m00; l = m10 / D0 (left unscaled when D0 == 0);
+//           D1 = m11 - l * (D0 * l);
+//   solve: y = P b; y1 = y1 - l * y0; y_i = y_i / D_i if |D_i| > DBL_MIN
+//          else 0; y0 = y0 - l * y1; x = P^T y.
+// The reference is compiled with -mfma under GCC's default
+// -ffp-contract=fast (its CMakeLists.txt:20), so which of its products are
+// fused into multiply-adds is the compiler's choice; this restatement rounds
+// every operation separately (built with -ffp-contract=off).
 inline void solve2(double a00, double a01, double a11, double b0, double b1, double& x0, double& x1) {
-    double D0 = a00;
-    double l = a01 / D0;
-    double D1 = a11 - l * a01;
-    double y1 = b1 - l * b0;
-    x1 = y1 / D1;
-    x0 = b0 / D0 - l * x1;
+    const bool piv = std::fabs(a11) > std::fabs(a00);
+    const double m00 = piv ? a11 : a00, m11 = piv ? a00 : a11;
+    double y0 = piv ? b1 : b0, y1 = piv ? b0 : b1;
+    const double D0 = m00;
+    double l = a01;
+    if (std::fabs(D0) > 0.0) l = a01 / D0;
+    const double D1 = m11 - l * (D0 * l);
+    y1 = y1 - l * y0;
+    const double tiny = 2.2250738585072014e-308;  // numeric_limits<double>::min()
+    y0 = std::fabs(D0) > tiny ? y0 / D0 : 0.0;
+    y1 = std::fabs(D1) > tiny ? y1 / D1 : 0.0;
+    y0 = y0 - l * y1;
+    x0 = piv ? y1 : y0;
+    x1 = piv ? y0 : y1;
 }
 
 inline void pt_param(V3 r0, V3 n, V3 p, V3 o, double& s, double& t) {

@@ -156,36 +156,51 @@ void deformation_gradient(const double* X, const int* t, const double* IB, doubl
         for (int j = 0; j < 3; ++j) F[i * 3 + j] = Ds[i * 3 + 0] * IB[0 * 3 + j] + Ds[i * 3 + 1] * IB[1 * 3 + j] + Ds[i * 3 + 2] * IB[2 * 3 + j];
 }
 
-// Fixed-order sum used for the two means of the CCD hash (mean edge length,
-// mean |dir|). The reference takes them with Eigen's mean() and a serial loop
-// (SPATIAL_HASH.h:455-475); this restatement fixes one order that a GPU can
-// reproduce: tiles of 2048 items, item t of a 256-lane tile sums items
-// t, t+256, ..., t+1792 in turn, then lanes are added pairwise with strides
-// 128, 64, ..., 1; tile sums are reduced the same way until one is left.
-double det_sum(const double* x, long n) {
+// The two means of the CCD hash in the reference's own order
+// (SPATIAL_HASH.h:455-475).
+//
+// eigen_sum: `eLen.mean()` is Eigen's sum() / size(). For a dense double
+// vector on an AVX build (the reference compiles with -mavx2,
+// CMakeLists.txt:20) Eigen's redux (Eigen/src/Core/Redux.h,
+// LinearVectorizedTraversal, storage 32-byte aligned) keeps two 4-lane
+// accumulators: lane l of the first sums items l, l+8, l+16, ... and lane l
+// of the second items 4+l, 12+l, ... over the first 8*floor(n/8) items; the
+// accumulators are added lane by lane, one more 4-item packet is added when
+// n mod 8 >= 4, the four lanes are reduced by the AVX predux as
+// (l0 + l2) + (l1 + l3) (Eigen 3.3/3.4), and the last n mod 4 items are added
+// one at a time. Fewer than 4 items are summed left to right.
+double eigen_sum(const double* x, long n) {
     if (n <= 0) return 0.0;
-    std::vector<double> cur(x, x + n);
-    while (true) {
-        long m = (long)cur.size();
-        long tiles = (m + 2047) / 2048;
-        std::vector<double> nxt(tiles);
-        for (long k = 0; k < tiles; ++k) {
-            double a[256];
-            for (int t = 0; t < 256; ++t) {
-                double s = 0.0;
-                for (int r = 0; r < 8; ++r) {
-                    long i = k * 2048 + r * 256 + t;
-                    if (i < m) s += cur[i];
-                }
-                a[t] = s;
-            }
-            for (int st = 128; st > 0; st >>= 1)
-                for (int t = 0; t < st; ++t) a[t] += a[t + st];
-            nxt[k] = a[0];
-        }
-        if (tiles == 1) return nxt[0];
-        cur.swap(nxt);
+    const long aligned = n & ~3L, aligned2 = n & ~7L;
+    double res;
+    if (aligned == 0) {
+        res = x[0];
+        for (long i = 1; i < n; ++i) res += x[i];
+        return res;
     }
+    double p0[4] = {x[0], x[1], x[2], x[3]};
+    if (aligned > 4) {
+        double p1[4] = {x[4], x[5], x[6], x[7]};
+        for (long i = 8; i < aligned2; i += 8)
+            for (int l = 0; l < 4; ++l) {
+                p0[l] += x[i + l];
+                p1[l] += x[i + 4 + l];
+            }
+        for (int l = 0; l < 4; ++l) p0[l] += p1[l];
+        if (aligned > aligned2)
+            for (int l = 0; l < 4; ++l) p0[l] += x[aligned2 + l];
+    }
+    res = (p0[0] + p0[2]) + (p0[1] + p0[3]);
+    for (long i = aligned; i < n; ++i) res += x[i];
+    return res;
+}
+
+// pSize: the reference's serial loop, |dir_x| + |dir_y| + |dir_z| of every
+// surface node in node order into one accumulator.
+double serial_sum(const double* x, long n) {
+    double s = 0.0;
+    for (long i = 0; i < n; ++i) s += x[i];
+    return s;
 }
 
 // ---------------------------------------------------------------------------
@@ -231,9 +246,9 @@ struct SpatialHash {
     void build_ccs(int V, const double* X, int nN, const int* nodes, int nE, const int* edges, int nT, const int* tris) {
         double voxelSize = 1.0;
         if (nE) {
-            double s = 0;
-            for (int e = 0; e < nE; ++e) s += std::sqrt(sq(v3(X + 3 * edges[2 * e]) - v3(X + 3 * edges[2 * e + 1])));
-            voxelSize *= s / nE;
+            std::vector<double> len(nE);
+            for (int e = 0; e < nE; ++e) len[e] = std::sqrt(sq(v3(X + 3 * edges[2 * e]) - v3(X + 3 * edges[2 * e + 1])));
+            voxelSize *= eigen_sum(len.data(), nE) / (double)nE;
         }
         V3 lo = v3(X), hi = v3(X);
         for (int i = 1; i < V; ++i) {
@@ -318,12 +333,12 @@ struct SpatialHash {
         if (nE) {
             std::vector<double> len(nE);
             for (int e = 0; e < nE; ++e) len[e] = std::sqrt(sq(v3(X + 3 * edges[2 * e]) - v3(X + 3 * edges[2 * e + 1])));
-            voxelSize *= det_sum(len.data(), nE) / (double)nE;
+            voxelSize *= eigen_sum(len.data(), nE) / (double)nE;
         }
         std::vector<double> ad(3 * (size_t)nN);
         for (int s = 0; s < nN; ++s)
             for (int d = 0; d < 3; ++d) ad[3 * s + d] = std::fabs(dir[3 * nodes[s] + d]);
-        double pSize = det_sum(ad.data(), 3L * nN) / (double)(nN * 3);
+        double pSize = serial_sum(ad.data(), 3L * nN) / (double)(nN * 3);
         double spanSize = curMaxStepSize * pSize / voxelSize;
         if (spanSize > 1) curMaxStepSize /= spanSize;
 
@@ -1064,6 +1079,35 @@ double ora_kappa_init(double meanMassDiag, double dHat2, double stiffMult, doubl
 
 // raw distance-function access for known-answer and FD tests
 int ora_type_pt(const double* p, const double* t0, const double* t1, const double* t2) { return type_PT(v3(p), v3(t0), v3(t1), v3(t2)); }
+// extend-add of a multifrontal update matrix into its parent front, lower
+// triangle only. The front (order m = k + r) is held as three column-major
+// blocks F11 (k x k), F21 (r x k), F22 (r x r); U (mu x mu, column-major)
+// goes to the front positions li (ascending): F[li[i], li[j]] += U[i, j] for
+// i >= j. Used by the oracle's sparse Cholesky (oracle/cholesky.py).
+void ora_extend_add(double* F11, double* F21, double* F22, long k, long r, const double* U, long mu, const long* li) {
+    for (long j = 0; j < mu; ++j) {
+        const long c = li[j];
+        const double* Uc = U + j * mu;
+        if (c < k) {
+            long i = j;
+            for (; i < mu && li[i] < k; ++i) F11[c * k + li[i]] += Uc[i];
+            for (; i < mu; ++i) F21[c * r + (li[i] - k)] += Uc[i];
+        } else {
+            double* Fc = F22 + (c - k) * r - k;
+            for (long i = j; i < mu; ++i) Fc[li[i]] += Uc[i];
+        }
+    }
+}
+
+// the classifier's three (s, t) edge parameters (DISTANCE_TYPE.h:46,54,62),
+// all computed, for tests of the 2x2 LDLT solve
+void ora_pt_params(const double* p, const double* t0, const double* t1, const double* t2, double* st) {
+    V3 P = v3(p), A = v3(t0), B = v3(t1), Cc = v3(t2);
+    V3 n = cross(B - A, Cc - A);
+    pt_param(B - A, n, P, A, st[0], st[1]);
+    pt_param(Cc - B, n, P, B, st[2], st[3]);
+    pt_param(A - Cc, n, P, Cc, st[4], st[5]);
+}
 int ora_type_ee(const double* a0, const double* a1, const double* b0, const double* b1) { return type_EE(v3(a0), v3(a1), v3(b0), v3(b1)); }
 double ora_dist_pt_unclassified(const double* p, const double* t0, const double* t1, const double* t2) { return d_PT_unclassified(v3(p), v3(t0), v3(t1), v3(t2)); }
 double ora_dist_ee_unclassified(const double* a0, const double* a1, const double* b0, const double* b1) { return d_EE_unclassified(v3(a0), v3(a1), v3(b0), v3(b1)); }

@@ -6,7 +6,8 @@ Only tests/, ``__graft_entry__.smoke()`` and the cpu_baseline leg of
 bench.py import this module; the product never does.
 
 Parity status: UNPINNED (the reference ships no tests or golden vectors and
-cannot be built here). The linear solve uses scipy's sparse LU in place of
+cannot be built here). The linear solve is a sparse Cholesky of our own
+(``oracle/cholesky.py``, multifrontal with nested dissection) in place of
 CHOLMOD (``Math/DIRECT_SOLVER.h:13-65``).
 """
 from __future__ import annotations
@@ -20,6 +21,11 @@ from collections import deque
 from dataclasses import dataclass, field
 
 import numpy as np
+
+try:
+    from . import cholesky
+except ImportError:  # imported as a top-level module (oracle/ on sys.path)
+    import cholesky
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB = os.path.join(_HERE, "libidp_oracle.so")
@@ -396,8 +402,6 @@ def advance_one_step(pb: Problem, Xtilde=None, verbose=False):
     """Advance_One_Step_IE_Discrete_Shell<double,3,false,false,false>
     (FEM/Shell/IMPLICIT_EULER.h:151-891) for tets with fixed DBC, no friction.
     Returns the Newton iteration count; pb.X and pb.v are updated."""
-    import scipy.sparse.linalg as spla
-
     h = pb.h
     Xn = pb.X.copy()
     if pb.flow:
@@ -424,13 +428,9 @@ def advance_one_step(pb: Problem, Xtilde=None, verbose=False):
         if not use_gd:
             Hm = _hessian(pb, X, cons, info)
             t0 = time.perf_counter()
-            try:
-                sol = spla.spsolve(Hm.tocsc(), rhs, permc_spec="MMD_AT_PLUS_A")
-                ok = np.all(np.isfinite(sol))
-            except Exception:
-                ok = False
+            sol = cholesky.solve_spd(Hm, rhs, X)  # Solve_Direct (DIRECT_SOLVER.h:13-65)
             stats["t_solve"] += time.perf_counter() - t0
-            if not ok:
+            if sol is None:  # not positive definite: gradient descent (IMPLICIT_EULER.h:519-546)
                 use_gd = True
                 sol = rhs.copy()
         else:
