@@ -73,6 +73,8 @@ __global__ void k_span_tiles(const SpanTile* __restrict__ tiles, const unsigned 
     if (threadIdx.x == 0) out[blockIdx.x] = a[0];
 }
 
+constexpr int kStageTile = 1024;  // items staged in shared memory per step (multiple of 8)
+
 // Sum of x[0..n) in the order of Eigen's vectorised redux of a dense double
 // vector on the reference's AVX build (`eLen.mean()`, SPATIAL_HASH.h:455-464;
 // Eigen/src/Core/Redux.h, LinearVectorizedTraversal over 4-lane packets):
@@ -80,42 +82,73 @@ __global__ void k_span_tiles(const SpanTile* __restrict__ tiles, const unsigned 
 // items 4+l, 12+l, ... over the first 8*floor(n/8) items; the accumulators
 // are added lane by lane, one more 4-item packet is added when n mod 8 >= 4,
 // the lanes reduce as (l0 + l2) + (l1 + l3) and the last n mod 4 items follow
-// one at a time; fewer than 4 items are summed left to right. Lanes 0-7 of
-// the calling warp each carry one accumulator lane; every lane of the warp
-// must call it, and lane 0 receives the result.
-__device__ double warp_eigen_sum(const double* x, long n) {
-    const int lane = threadIdx.x & 31;
+// one at a time; fewer than 4 items are summed left to right. The whole CTA
+// stages the items through shared memory (double-buffered tiles); threads
+// 0-7 carry the eight accumulator lanes. Every thread must call it; thread 0
+// receives the result.
+__device__ double cta_eigen_sum(const double* __restrict__ x, long n, double (*buf)[kStageTile]) {
+    const int tid = threadIdx.x;
     const long aligned = n & ~3L, aligned2 = n & ~7L;
     double acc = 0.0;
     if (aligned > 4) {
-        if (lane < 8) {
+        for (long base = 0, k = 0; base < aligned2; base += kStageTile, ++k) {
+            double* t = buf[k & 1];
+            const long m = min((long)kStageTile, aligned2 - base);
+            for (long i = tid; i < m; i += blockDim.x) t[i] = x[base + i];
+            __syncthreads();
+            if (tid < 8) {
 #pragma unroll 8
-            for (long i = lane; i < aligned2; i += 8) acc += x[i];
+                for (long i = tid; i < m; i += 8) acc += t[i];
+            }
         }
-    } else if (aligned == 4 && lane < 4) {
-        acc = x[lane];
+        __syncthreads();
+    } else if (aligned == 4 && tid < 4) {
+        acc = x[tid];
     }
-    const double hi = __shfl_down_sync(0xffffffffu, acc, 4);
-    if (aligned > 4 && lane < 4) {
-        acc = acc + hi;
-        if (aligned > aligned2) acc = acc + x[aligned2 + lane];
-    }
-    const double l1 = __shfl_down_sync(0xffffffffu, acc, 1);
-    const double l2 = __shfl_down_sync(0xffffffffu, acc, 2);
-    const double l3 = __shfl_down_sync(0xffffffffu, acc, 3);
+    __shared__ double lanes[8];
+    if (tid < 8) lanes[tid] = acc;
+    __syncthreads();
     double res = 0.0;
-    if (lane == 0) {
+    if (tid == 0) {
         if (aligned == 0) {
             if (n > 0) {
                 res = x[0];
                 for (long i = 1; i < n; ++i) res += x[i];
             }
         } else {
-            res = (acc + l2) + (l1 + l3);
+            double p[4] = {lanes[0], lanes[1], lanes[2], lanes[3]};
+            if (aligned > 4) {
+                for (int l = 0; l < 4; ++l) p[l] = p[l] + lanes[4 + l];
+                if (aligned > aligned2)
+                    for (int l = 0; l < 4; ++l) p[l] = p[l] + x[aligned2 + l];
+            }
+            res = (p[0] + p[2]) + (p[1] + p[3]);
             for (long i = aligned; i < n; ++i) res += x[i];
         }
     }
+    __syncthreads();
     return res;
+}
+
+// x[0] + x[1] + ... + x[n-1] added left to right into one accumulator (the
+// reference's serial loop), the items staged through shared memory by the
+// whole CTA while thread 0 adds the previous tile. Every thread must call
+// it; thread 0 receives the result.
+__device__ double cta_serial_sum(const double* __restrict__ x, long n, double (*buf)[kStageTile]) {
+    const int tid = threadIdx.x;
+    double acc = 0.0;
+    for (long base = 0, k = 0; base < n; base += kStageTile, ++k) {
+        double* t = buf[k & 1];
+        const long m = min((long)kStageTile, n - base);
+        for (long i = tid; i < m; i += blockDim.x) t[i] = x[base + i];
+        __syncthreads();
+        if (tid == 0) {
+#pragma unroll 8
+            for (long i = 0; i < m; ++i) acc += t[i];
+        }
+    }
+    __syncthreads();
+    return acc;
 }
 
 // fixed-order sum of the tile sums (used for the span-cap estimate only)
@@ -164,7 +197,8 @@ __global__ void k_span_cap(int nI, const unsigned char* __restrict__ active, con
                            const double* __restrict__ tsum, const double* __restrict__ len,
                            const double* __restrict__ absdir, double* __restrict__ scratch,
                            double* __restrict__ alpha, double* __restrict__ voxel_size) {
-    __shared__ double s_vsz;
+    __shared__ double buf[2][kStageTile];
+    __shared__ double s_vsz, s_est;
     int i = blockIdx.x;
     if (!active[i]) return;
     const long e0 = se_off[i], ne = se_off[i + 1] - se_off[i];
@@ -172,26 +206,26 @@ __global__ void k_span_cap(int nI, const unsigned char* __restrict__ active, con
     const int tn0 = tile_off[2 * i + 1], tn1 = tile_off[2 * i + 2];
     const int ntn = tn1 - tn0;
     double* sc = scratch + 2 * (long)tile_off[2 * i] + 8 * (long)i;
-    if (threadIdx.x < 32) {
-        double es = warp_eigen_sum(len + e0, ne);
-        if (threadIdx.x == 0) s_vsz = ne ? 1.0 * (es / (double)ne) : 1.0;
-    }
-    double ps = ntn == 0 ? 0.0 : (ntn == 1 ? tsum[tn0] : cta_tree_sum(tsum + tn0, ntn, sc));
-    __syncthreads();
+    const double es = cta_eigen_sum(len + e0, ne, buf);
+    const double ps = ntn == 0 ? 0.0 : (ntn == 1 ? tsum[tn0] : cta_tree_sum(tsum + tn0, ntn, sc));
+    const double cnt = (double)(nn * 3);
     if (threadIdx.x == 0) {
-        const double vsz = s_vsz;
-        const double cnt = (double)(nn * 3);
-        double a = alpha[i];
-        const double est = a * (ps / cnt) / vsz;
-        const double bound = 1.0 - ((double)(3 * nn) + 32.0) * 2.3e-16;
-        if (!(est < bound)) {
-            const double* d = absdir + 3 * n0;
-            double pSize = 0.0;
-            for (long k = 0; k < 3 * nn; ++k) pSize += d[k];
+        s_vsz = ne ? 1.0 * (es / (double)ne) : 1.0;
+        s_est = alpha[i] * (ps / cnt) / s_vsz;
+    }
+    __syncthreads();
+    const double vsz = s_vsz;
+    double a = alpha[i];
+    const double bound = 1.0 - ((double)(3 * nn) + 32.0) * 2.3e-16;
+    if (!(s_est < bound)) {
+        double pSize = cta_serial_sum(absdir + 3 * n0, 3 * nn, buf);
+        if (threadIdx.x == 0) {
             pSize /= cnt;
             const double spanSize = a * pSize / vsz;
             if (spanSize > 1) a /= spanSize;
         }
+    }
+    if (threadIdx.x == 0) {
         alpha[i] = a;
         voxel_size[i] = vsz;
     }
@@ -528,7 +562,10 @@ __device__ int accd_pt(D3 p, D3 t0, D3 t1, D3 t2, D3 dp, D3 dt0, D3 dt1, D3 dt2,
     for (its = 0; its < ACCD_MAX_ITERS; ++its) {
         double tocLB = (1 - eta) * (dist2_cur - th2) / ((dist_cur + thickness) * maxDispMag);
         p = p + tocLB * dp; t0 = t0 + tocLB * dt0; t1 = t1 + tocLB * dt1; t2 = t2 + tocLB * dt2;
-        dist2_cur = d_PT_unclassified(p, t0, t1, t2);
+        // short chains share the FP64 pipe with many others: evaluate only the
+        // branch taken; a chain past ACCD_POLL iterations is one of the few
+        // long ones that decide the launch time: evaluate for latency
+        dist2_cur = its < ACCD_POLL ? d_PT_unclassified(p, t0, t1, t2) : d_PT_unclassified_ilp(p, t0, t1, t2);
         dist_cur = sqrt(dist2_cur);
         if (toc != 0 && ((dist2_cur - th2) / (dist_cur + thickness) < gap)) return 1;
         toc += tocLB;

@@ -781,7 +781,7 @@ int idp_commit(idp_ctx* c) {
         // tiles (2048 items each) of the fixed-order estimate of each
         // instance's sum |dir| that decides whether the CCD span cap can apply
         // (toff[2i] = toff[2i+1]: no edge-length tiles, the voxel size is
-        // summed in the reference's order by one warp)
+        // summed in the reference's order by the instance's CTA)
         std::vector<SpanTile> tiles;
         std::vector<int> toff(2 * nI + 1, 0);
         for (int i = 0; i < nI; ++i) {

@@ -112,6 +112,30 @@ __device__ inline double d_PT_unclassified(D3 p, D3 t0, D3 t1, D3 t2) {
         default: return d_PT(p, t0, t1, t2);
     }
 }
+// The same value as d_PT_unclassified, scheduled for a single long-running
+// thread: the classifier's three 2x2 solves and all seven candidate
+// distances are independent of one another, so they are all evaluated (their
+// divisions overlap) and the classifier's decision then selects one. Every
+// operation of the selected branch is the one d_PT_unclassified performs, so
+// the result is bit-identical; the unselected values (which may be inf or
+// NaN on degenerate inputs) are discarded.
+__device__ inline double d_PT_unclassified_ilp(D3 p, D3 t0, D3 t1, D3 t2) {
+    D3 n = cross(t1 - t0, t2 - t0);
+    double s0, u0, s1, u1, s2, u2;
+    pt_param(t1 - t0, n, p, t0, s0, u0);
+    pt_param(t2 - t1, n, p, t1, s1, u1);
+    pt_param(t0 - t2, n, p, t2, s2, u2);
+    const double dpp0 = d_PP(p, t0), dpp1 = d_PP(p, t1), dpp2 = d_PP(p, t2);
+    const double dpe0 = d_PE(p, t0, t1), dpe1 = d_PE(p, t1, t2), dpe2 = d_PE(p, t2, t0);
+    const double dpt = d_PT(p, t0, t1, t2);
+    if (s0 > 0.0 && s0 < 1.0 && u0 >= 0.0) return dpe0;
+    if (s1 > 0.0 && s1 < 1.0 && u1 >= 0.0) return dpe1;
+    if (s2 > 0.0 && s2 < 1.0 && u2 >= 0.0) return dpe2;
+    if (s0 <= 0.0 && s2 >= 1.0) return dpp0;
+    if (s1 <= 0.0 && s0 >= 1.0) return dpp1;
+    if (s2 <= 0.0 && s1 >= 1.0) return dpp2;
+    return dpt;
+}
 __device__ inline double d_EE_unclassified(D3 ea0, D3 ea1, D3 eb0, D3 eb1) {
     switch (type_EE(ea0, ea1, eb0, eb1)) {
         case 0: return d_PP(ea0, eb0);

@@ -623,15 +623,26 @@ __device__ __forceinline__ bool inst_round(unsigned int* ctl, T* red, T* part, i
     }
     __syncthreads();
     if (sh_i[0]) {
-        if (reduce && threadIdx.x < 32) {
+        if (reduce) {
+            // every thread of the completing CTA loads its share of the
+            // partials at once (one L2 round trip), then a fixed-order tree:
+            // lanes by shuffles, warps in order
+            __shared__ T wred[GP_THREADS / 32][kRed];
             __threadfence();
             T acc[kRed] = {};
-            for (int c = threadIdx.x; c < nc; c += 32)
+            for (int c = threadIdx.x; c < nc; c += GP_THREADS)
                 for (int j = 0; j < kRed; ++j) acc[j] += __ldcg(part + kRed * (c0 + c) + j);
             for (int o = 16; o > 0; o >>= 1)
                 for (int j = 0; j < kRed; ++j) acc[j] += __shfl_xor_sync(0xffffffffu, acc[j], o);
+            if ((threadIdx.x & 31) == 0)
+                for (int j = 0; j < kRed; ++j) wred[threadIdx.x >> 5][j] = acc[j];
+            __syncthreads();
             if (threadIdx.x == 0)
-                for (int j = 0; j < kRed; ++j) red[j] = acc[j];
+                for (int j = 0; j < kRed; ++j) {
+                    T t = wred[0][j];
+                    for (int w = 1; w < GP_THREADS / 32; ++w) t += wred[w][j];
+                    red[j] = t;
+                }
         }
         if (threadIdx.x == 0) {
             __threadfence();

@@ -15,6 +15,7 @@
 // blocks [[l+r, l-r], [l-r, l+r]]. Each mode Q contributes
 // lambda * g g^T with g = dF/dx^T vec(Q), computed as Q * IB^T.
 #include <mutex>
+#include <cuda.h>
 #include "engine.hpp"
 #include "prims.cuh"
 
@@ -408,10 +409,43 @@ __global__ void k_tet_energy_noalloc_sum(int nchunks, const unsigned char* __res
     *inverted = *bad_flag;
 }
 
-// device address of the scratch array, looked up once per device
+// Device address of the scratch array, looked up once per device and
+// context: a context that is destroyed and re-created (cudaDeviceReset, or a
+// primary context released and retained again) reloads the module, so the
+// cached address is keyed on the driver's unique id of the current context
+// (cuCtxGetId), reached through the runtime's driver entry-point query so
+// that the library needs no link to libcuda.
 constexpr int kNoAllocMaxDevices = 64;
 std::mutex g_noalloc_mu;
 unsigned char* g_noalloc_addr[kNoAllocMaxDevices] = {};
+unsigned long long g_noalloc_ctx[kNoAllocMaxDevices] = {};
+
+typedef CUresult (*PfnCtxGetCurrent)(CUcontext*);
+typedef CUresult (*PfnCtxGetId)(CUcontext, unsigned long long*);
+
+// unique id of the calling thread's current context + 1 (0: none current, or
+// the driver entry points are unavailable); call with g_noalloc_mu held
+unsigned long long current_context_key() {
+    static bool looked_up = false;
+    static PfnCtxGetCurrent get_current = nullptr;
+    static PfnCtxGetId get_id = nullptr;
+    if (!looked_up) {
+        looked_up = true;
+        cudaDriverEntryPointQueryResult q;
+        void* f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<PfnCtxGetCurrent>(f);
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<PfnCtxGetId>(f);
+    }
+    CUcontext c = nullptr;
+    unsigned long long id = 0;
+    if (!get_current || !get_id || get_current(&c) != CUDA_SUCCESS || !c || get_id(c, &id) != CUDA_SUCCESS) return 0;
+    return id + 1;
+}
 
 }  // namespace
 
@@ -429,12 +463,16 @@ extern "C" int idp_tet_energy_noalloc(int T, const int32_t* tets, const double* 
     unsigned char* scratch = nullptr;
     {
         std::lock_guard<std::mutex> lock(g_noalloc_mu);
-        if (!g_noalloc_addr[dev]) {
-            // first call on this device: the symbol's device address (the
-            // name itself is only a host-side stand-in)
+        const unsigned long long key = current_context_key();
+        if (!g_noalloc_addr[dev] || key == 0 || key != g_noalloc_ctx[dev]) {
+            // set-up, the first call on this device and context: the
+            // symbol's device address (the name itself is only a host-side
+            // stand-in); the lookup also makes the device's primary context
+            // current when no context was yet
             void* p = nullptr;
             if (cudaGetSymbolAddress(&p, g_tet_energy_scratch) != cudaSuccess || !p) return IDP_ERR_CUDA;
             g_noalloc_addr[dev] = static_cast<unsigned char*>(p);
+            g_noalloc_ctx[dev] = current_context_key();
         }
         scratch = g_noalloc_addr[dev];
     }

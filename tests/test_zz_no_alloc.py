@@ -7,8 +7,9 @@ synchronisation of cudaMalloc/cudaFree). Its scratch is one fixed array in
 the library shared by every call, so this file checks two calls in a row
 (the second must not see the first one's leftovers, in particular the
 inversion flag) against the context entry point idp_eval_energy, whose
-elastic term is the same quantity. The file name makes pytest collect it
-last.
+elastic term is the same quantity, and against the CPU oracle's elastic
+energy; and that a run of calls leaves the device's free memory unchanged.
+The file name makes pytest collect it last.
 """
 import ctypes as C
 import math
@@ -33,7 +34,7 @@ def _dev(torch, a, dtype):
     return torch.from_numpy(np.ascontiguousarray(a, dtype=dtype)).cuda()
 
 
-def test_tet_energy_noalloc_matches_context_entry(gpu_lib):
+def test_tet_energy_noalloc_matches_context_entry(gpu_lib, oracle):
     import torch
 
     import idp_gb300 as idp
@@ -69,13 +70,28 @@ def test_tet_energy_noalloc_matches_context_entry(gpu_lib):
     rng = np.random.default_rng(11)
     bent = meshgen.bend_target(X0, angle=0.8 * math.pi, radius=1.2)
     shaken = X0 + rng.uniform(-0.02, 0.02, X0.shape)
-    # two calls in a row, each against the context entry point
+    # two calls in a row, each against the context entry point and the oracle
+    lam_t, mu_t = np.full(T, pr["lam"]), np.full(T, pr["mu"])
     for X in (bent, shaken):
         e, bad = call(X)
         ref = ctx.energy(0, X)
         assert ref is not None
         assert bad == 0
         assert abs(e - ref[0]) <= TOL * abs(ref[0]), (e, ref[0])
+        e_or = oracle.tet_energy(X, tets, np.ascontiguousarray(IB.reshape(-1, 3, 3)), vol, lam_t, mu_t, h * h)
+        assert abs(e - e_or) <= TOL * abs(e_or), (e, e_or)
+
+    # no device allocation: free memory unchanged over a run of calls
+    d_X = _dev(torch, shaken, np.float64)
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    for _ in range(20):
+        rc = gpu_lib.idp_tet_energy_noalloc(T, d_tets.data_ptr(), d_X.data_ptr(), d_IB.data_ptr(), d_vol.data_ptr(),
+                                            d_lam.data_ptr(), d_mu.data_ptr(), h * h, energy.data_ptr(),
+                                            inverted.data_ptr(), stream)
+        assert rc == idp.IDP_OK
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
 
     # an inverted configuration raises the flag; the next call starts clean
     mirrored = X0 * np.array([-1.0, 1.0, 1.0])
