@@ -19,17 +19,20 @@ steps and K timed steps continue one flow sequence (20 steps for K=17, W=3).
   the timed region (host wall clock around synchronous calls).
 * roofline: the cluster PCG kernel (dominant), algorithmic bytes per launch /
   event time, against MEASURED_PEAKS.json hbm_gbs.
-* cpu_baseline: the CPU oracle (FP64, sparse LU) running the first flow step
-  of the same blob at 24^3 resolution (bounded sample), solves/s scaled to
-  the full blob by tet count.
+* cpu_baseline and oracle_check: the CPU oracle (FP64, sparse Cholesky)
+  solving the first timed step(s) of the same full-size blob from the GPU's
+  start states (at least one step, more while --cpu-sample-s lasts): its
+  solves/s, and the GPU energies' relative error against it per step.
+* constraints_per_step: the constraint-set size at the end of each step.
 
 ``--workload batch256`` (256 bars, tet counts log-uniform in [1k, 50k]) and
 ``--workload bar`` (6x6x24 bar, bend 2.2pi) time one batched solve per step
 from a restored device snapshot instead.
 
 ``--impl reference`` times the reference's CPU path (the oracle port: the
-reference does not build in this environment) on the same metric, one
-bounded sample per step.
+reference does not build in this environment) on the same metric: on the
+blob, full-size flow steps from the rest state (at least one, as many as
+about 2.5 minutes allow; "steps" is the number that ran).
 """
 from __future__ import annotations
 
@@ -83,7 +86,8 @@ def parse():
                          "Newton iterations/s (0 = solve to convergence, report solves/s)")
     ap.add_argument("--fp64-sample", type=int, default=16,
                     help="batch/bar workloads: instances re-solved one at a time on the FP64 path")
-    ap.add_argument("--cpu-sample-s", type=float, default=20.0)
+    ap.add_argument("--cpu-sample-s", type=float, default=20.0,
+                    help="CPU baseline budget (at least one full solve runs)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
 
@@ -269,38 +273,42 @@ def blob_desc(p, n, step):
             f"E=1e4 nu=0.3 rho=1e3, dhat=1e-3 bbox diag")
 
 
-def cpu_baseline_flow(full_tets, step, budget_s, n_small=24):
-    """Oracle (FP64, direct solve) running the first normal-flow step of the
-    same blob at n_small^3 resolution, repeated while the budget lasts;
-    solves/s scaled to the full blob by tet count (linear, which favours the
-    CPU: its sparse LU grows faster than linearly)."""
+def oracle_flow_steps(p, starts, step, budget_s, tol=1e-3):
+    """The oracle (FP64, sparse Cholesky) solving normal-flow steps of the
+    full blob: step k starts from starts[k] = (X, kappa[3]) (the next start
+    is the oracle's own result when starts[k+1] is None), at least one step,
+    more while the time budget lasts. Returns per-step results and the
+    time spent in the steps."""
     import numpy as np
 
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
 
     O.build()
-    p = blob_problem(n_small)
     T = p["tets"].shape[0]
     surf = O.surface(p["X"], p["tets"])
-    v = O.normal_flow_velocity(p["X"], surf["tris"], step, H)
-    t_used, solves, iters = 0.0, 0, 0
-    while True:
-        pb = O.Problem(X=p["X"].copy(), X0=p["X"], tets=p["tets"], mass=p["mass"], lam=np.full(T, p["lam"]),
-                       mu=np.full(T, p["mu"]), h=H, dHat2=p["dHat2"], kappa=[p["kappa"], p["kappa_max"], 0.0],
-                       v=v.copy(), tol=1e-3, max_iters=500)
+    out, t_used = [], 0.0
+    X, kap = None, None
+    for k, st in enumerate(starts):
+        if st is not None:
+            X, kap = st[0], st[1]
+        v = O.normal_flow_velocity(X, surf["tris"], step, H)
+        pb = O.Problem(X=X.copy(), X0=p["X"], tets=p["tets"], mass=p["mass"], lam=np.full(T, p["lam"]),
+                       mu=np.full(T, p["mu"]), h=H, dHat2=p["dHat2"], kappa=[kap[0], kap[1], 0.0], v=v, tol=tol,
+                       max_iters=500)
+        pb.surf = surf
         t0 = time.perf_counter()
-        iters += O.advance_one_step(pb)
+        it = O.advance_one_step(pb)
         t_used += time.perf_counter() - t0
-        solves += 1
+        out.append(dict(energy=pb.last_energy, newton_iters=it, constraints=int(pb.log[-1]["ncons"])))
+        X, kap = pb.X.copy(), [pb.kappa[0], pb.kappa[1], 0.0]
         if t_used >= budget_s:
             break
-    rate = solves * T / t_used / full_tets
-    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
-    return {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"oracle first flow step of the blob at {n_small}^3 ({T} tets), {solves} solve(s), {iters} "
-                      f"Newton iterations, {t_used:.1f} s; solves/s scaled to {full_tets} tets by tet count; "
-                      "element and contact loops OpenMP on all cores, sparse LU (SciPy SuperLU) on one"}
+    return out, t_used
+
+
+def cpu_cores():
+    return int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
 
 
 def run_flow(args):
@@ -370,7 +378,7 @@ def run_flow(args):
     fp64 = None
     if not args.no_fp64 and mode == idp.MODE_MIXED:
         cd = make_ctx(idp.MODE_FP64, timed_arm=False)
-        d_ms, rel = [], []
+        d_ms, rel, energies64 = [], [], []
         for k, (Xs, vs, ks) in enumerate(starts):
             cd.set_positions(0, Xs)
             cd.set_kappa(0, ks)
@@ -378,8 +386,10 @@ def run_flow(args):
             _, rd = cd.advance(check=False)
             d_ms.append(cd.stats()["total_ms"])
             Em, Ed = results[k]["energy"], rd[0]["energy"]
+            energies64.append(Ed)
             rel.append(abs(Em - Ed) / max(abs(Ed), 1e-300))
         fp64 = {"solves_per_s": len(d_ms) / (sum(d_ms) / 1000.0), "ms_per_step": statistics.mean(d_ms),
+                "energies": energies64,
                 "rel_energy_err_max": max(rel), "rel_energy_err_mean": statistics.mean(rel),
                 "mixed_speedup": (sum(d_ms) / total_ms) if total_ms > 0 else None}
         cd.close()
@@ -431,8 +441,32 @@ def run_flow(args):
         "clocks": clocks.summary(),
         "wall_ms_per_step": 1000 * statistics.mean(wall),
     }
+    cons = [int(r["num_constraints"]) for r in results]
+    out["constraints_per_step"] = {"min": min(cons), "max": max(cons), "mean": float(np.mean(cons)),
+                                   "steps_with_contact": sum(1 for c in cons if c > 0)}
     if not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline_flow(int(p["tets"].shape[0]), args.flow_step, args.cpu_sample_s)
+        # the oracle solves the first timed steps from the same start states
+        # (full size); its time is the CPU baseline, its energies the
+        # error check of those steps
+        ores, t_or = oracle_flow_steps(p, [(X, k) for X, _, k in starts], args.flow_step, args.cpu_sample_s)
+        n = len(ores)
+        rel_m = [abs(results[k]["energy"] - ores[k]["energy"]) / abs(ores[k]["energy"]) for k in range(n)]
+        chk = {"steps": n, "first_step": args.warmup + 1, "rel_energy_err_mixed": rel_m,
+               "max": max(rel_m), "oracle_newton_iters": [o["newton_iters"] for o in ores],
+               "gpu_newton_iters": [results[k]["newton_iters"] for k in range(n)],
+               "oracle_constraints": [o["constraints"] for o in ores]}
+        if fp64 is not None:
+            chk["rel_energy_err_fp64"] = [abs(fp64["energies"][k] - ores[k]["energy"]) / abs(ores[k]["energy"])
+                                          for k in range(n)]
+        out["oracle_check"] = chk
+        out["cpu_baseline"] = {
+            "value": n / t_or, "unit": UNIT, "cores": cpu_cores(), "kind": "port",
+            "sample": f"oracle (FP64, sparse Cholesky) solving {n} full normal-flow step(s) of the same "
+                      f"{int(p['tets'].shape[0])}-tet blob (steps {args.warmup + 1}-{args.warmup + n} of the "
+                      f"sequence, from the GPU's start states), {t_or:.1f} s; element, contact and front "
+                      "assembly loops OpenMP, dense fronts multithreaded BLAS, on all cores"}
+    if fp64 is not None:
+        fp64.pop("energies", None)
     print(json.dumps(out), flush=True)
 
 
@@ -447,17 +481,31 @@ def run_reference(args):
     vals = []
     bl = None
     if args.workload == "blob":
-        import numpy as np
-        from idp_gb300 import meshgen
-
-        X, tets, _ = meshgen.blob(n=args.blob_n, lmax=8, amp=0.3, seed=0)
-        probs = [dict(X=X, tets=tets)]
-        desc = blob_desc(probs[0], args.blob_n, args.flow_step)
-        # every step is one bounded sample; the whole run stays near 2.5 min
-        per_step = min(args.cpu_sample_s, 150.0 / max(1, args.warmup + args.steps))
-        for _ in range(args.warmup + args.steps):
-            bl = cpu_baseline_flow(int(tets.shape[0]), args.flow_step, per_step)
-            vals.append(bl["value"])
+        # the full blob's flow sequence from its rest state, one full step
+        # at least, more while about 2.5 minutes last; no warm-up (nothing
+        # to warm on the CPU); steps = the steps that ran
+        p = blob_problem(args.blob_n)
+        desc = blob_desc(p, args.blob_n, args.flow_step)
+        starts = [(p["X"], [p["kappa"], p["kappa_max"], 0.0])] + [None] * max(0, args.steps - 1)
+        ores, t_or = oracle_flow_steps(p, starts, args.flow_step, 150.0)
+        n = len(ores)
+        v = n / t_or
+        out = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": n,
+               "warmup": 0, "ms_per_step": 1000.0 * t_or / n, "higher_is_better": True, "scaling": "weak",
+               "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+               "config": {"workload": desc, "tets": int(p["tets"].shape[0]), "verts": int(p["X"].shape[0])},
+               "newton_iters": [o["newton_iters"] for o in ores], "energies": [o["energy"] for o in ores],
+               "constraints": [o["constraints"] for o in ores],
+               "cpu_baseline": {"value": v, "unit": UNIT, "cores": cpu_cores(), "kind": "port",
+                                "sample": f"oracle (FP64, sparse Cholesky) solving flow steps 1-{n} of the full "
+                                          f"{int(p['tets'].shape[0])}-tet blob from its rest state, {t_or:.1f} s; "
+                                          "element, contact and front assembly loops OpenMP, dense fronts "
+                                          "multithreaded BLAS, on all cores"},
+               "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+               "note": "reference CPU path = oracle port (the reference does not build in this environment: "
+                       "Eigen, CHOLMOD, Boost and Kokkos are absent)"}
+        print(json.dumps(out))
+        return
     metric, unit = METRIC, UNIT
     if args.workload != "blob":
         probs, desc = make_workload(args, seed=0)
@@ -536,13 +584,18 @@ def run_gpu(args):
     barrier()
     step_ms = max_over_ranks(statistics.mean(dev_ms), world)
     iters_step = sum(r["newton_iters"] for r in results)
+    # a solve counts when Newton met its stopping test (IDP_OK, or
+    # IDP_WARN_ITER_CAP: converged with a capped, still conservative CCD
+    # loop); instances stopped at max_newton are reported as capped
+    conv_ok = (idp.IDP_OK, idp.IDP_WARN_ITER_CAP)
+    n_conv = sum(1 for r in results if r["status"] in conv_ok)
     metric, unit = METRIC, UNIT
     if budget > 0:
         metric = "Newton iterations/s (summed over instances), mixed batched vs FP64 one at a time"
         unit = "newton_iters/s"
         value = world * iters_step / (step_ms / 1000.0)
     else:
-        value = world * nI / (step_ms / 1000.0)
+        value = world * n_conv / (step_ms / 1000.0)
     # exact intersection check and inversion status of every instance's result
     counts = ctx.intersection_counts()
     injective = {"checked": nI, "intersection_free": int((counts == 0).sum()),
@@ -567,7 +620,7 @@ def run_gpu(args):
             ctx.state_ptr(i, Xo[i].data_ptr())
         e2e_wall.append(time.perf_counter() - t0)
     e2e_s = max_over_ranks(statistics.mean(e2e_wall), world)
-    e2e_val = world * (iters_step if budget > 0 else nI) / e2e_s
+    e2e_val = world * (iters_step if budget > 0 else n_conv) / e2e_s
     h2d = 2 * 3 * total_verts * 8
     d2h = 3 * total_verts * 8
 
@@ -589,6 +642,8 @@ def run_gpu(args):
         "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
         "newton_iters": {"mean": float(np.mean(newton)), "max": int(np.max(newton)), "total": int(iters_step)},
         "status_counts": status,
+        "converged": n_conv,
+        "capped_at_max_newton": sum(1 for r in results if r["status"] == idp.IDP_ERR_NOT_CONVERGED),
         "injective": injective,
         "fp64_one_at_a_time": fp64_single,
         "e2e": {"value": e2e_val, "unit": unit, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
@@ -635,13 +690,13 @@ def fp64_one_at_a_time(idp, probs, results, sample, max_newton, budget, device):
         _, r = c.advance(check=False)
         ms += c.stats()["total_ms"]
         its += r[0]["newton_iters"]
-        solved += r[0]["status"] in (idp.IDP_OK, idp.IDP_WARN_ITER_CAP)
+        solved += r[0]["status"] in (idp.IDP_OK, idp.IDP_WARN_ITER_CAP)  # converged solves only
         e64, em = r[0]["energy"], results[i]["energy"]
         rel.append(abs(em - e64) / max(abs(e64), 1e-300))
         c.close()
     out = {"instances": idx if len(idx) <= 32 else len(idx), "newton_iters": int(its), "ms": ms,
            "newton_iters_per_s": its / (ms / 1000.0) if ms > 0 else None,
-           "solves_per_s": (len(idx) / (ms / 1000.0)) if budget == 0 and ms > 0 else None,
+           "solves_per_s": (solved / (ms / 1000.0)) if budget == 0 and ms > 0 else None,
            "converged": solved, "rel_energy_diff_mixed_batched": {"max": max(rel), "mean": float(np.mean(rel))}}
     return out
 
@@ -719,7 +774,9 @@ def run_serve(args):
         start = max(ta, t_free)
         t_free = start + svc[k]
         lat64.append(t_free - ta)
-    thr64 = len(arr) / (t_free - arr[0][0]) if arr else 0.0
+    conv_ok = (idp.IDP_OK, idp.IDP_WARN_ITER_CAP)
+    n_conv64 = sum(1 for _, k in arr if e64[k]["status"] in conv_ok)
+    thr64 = n_conv64 / (t_free - arr[0][0]) if arr else 0.0
     # warm-up of the server's worker contexts on the pool, then the stream
     srv = idp.Server(args.hbm_budget_gb * 1e9, workers=args.serve_workers, max_batch=args.serve_batch,
                      mode=idp.MODE_MIXED, **params)
@@ -745,7 +802,10 @@ def run_serve(args):
     srv.close()
     lat = [i["done_ms"] - i["submit_ms"] for i, _ in infos]
     span_s = (max(i["done_ms"] for i, _ in infos) - min(i["submit_ms"] for i, _ in infos)) / 1000.0
-    thr = len(infos) / span_s
+    # only jobs whose Newton loop met its stopping test count as solves; the
+    # jobs stopped at the Newton cap are reported beside them
+    n_conv = sum(1 for i, _ in infos if i["status"] in conv_ok)
+    thr = n_conv / span_s
     status, rel = {}, []
     for i, k in infos:
         status[str(i["status"])] = status.get(str(i["status"]), 0) + 1
@@ -767,12 +827,15 @@ def run_serve(args):
                    "hbm_budget_gb": args.hbm_budget_gb, "l2": "no flush; jobs are independent solves"},
         "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
         "status_counts": status,
+        "converged": n_conv,
+        "capped_at_max_newton": sum(1 for i, _ in infos if i["status"] == idp.IDP_ERR_NOT_CONVERGED),
         "server": st,
         "fp64_one_at_a_time": {"value": thr64, "unit": UNIT,
                                "latency_ms": {"p50": 1000 * float(np.percentile(lat64, 50)),
                                               "p99": 1000 * float(np.percentile(lat64, 99))},
+                               "converged": n_conv64,
                                "basis": "FIFO replay of the same arrivals with each pool job's measured FP64 "
-                                        "service time (one context per job)"},
+                                        "service time (one context per job); converged jobs per second"},
         "served_over_fp64_one_at_a_time": thr / thr64 if thr64 else None,
         "rel_energy_diff_vs_fp64": {"max": max(rel) if rel else None, "converged_jobs": len(rel)},
         "e2e": {"value": thr, "unit": UNIT,

@@ -311,6 +311,7 @@ class Problem:
     vol: np.ndarray = None
     surf: dict = None
     log: list = field(default_factory=list)
+    b: np.ndarray = None      # (V,3) body force (None: zero)
     faces: np.ndarray = None  # (F,3) shell faces: flow mode (Advance_One_Step_IE_Flow)
     fvol: np.ndarray = None   # (F,) shell element volumes (area * thickness)
 
@@ -398,16 +399,22 @@ def _hessian(pb, X, cons, info):
     return H.tocsr()
 
 
-def advance_one_step(pb: Problem, Xtilde=None, verbose=False):
+def advance_one_step(pb: Problem, Xtilde=None, verbose=False, on_iter=None):
     """Advance_One_Step_IE_Discrete_Shell<double,3,false,false,false>
     (FEM/Shell/IMPLICIT_EULER.h:151-891) for tets with fixed DBC, no friction.
-    Returns the Newton iteration count; pb.X and pb.v are updated."""
+    Returns the Newton iteration count; pb.X and pb.v are updated.
+    on_iter(it, Xprev, direction, ncons) is called after each accepted
+    Newton step with the iterate the direction was computed at and the size
+    of the constraint set at that iterate."""
     h = pb.h
     Xn = pb.X.copy()
     if pb.flow:
         pb.v[:] = 0.0                     # IMPLICIT_EULER.h:207-209
-    if Xtilde is None:
-        Xtilde = Xn + h * pb.v            # IMPLICIT_EULER.h:195-216 (no body force)
+    if Xtilde is None:                    # IMPLICIT_EULER.h:195-216
+        if pb.b is None:
+            Xtilde = Xn + h * pb.v
+        else:                             # x + (h v + h^2 M^-1 b), M lumped
+            Xtilde = Xn + (h * pb.v + (h * h) * (f64(pb.b).reshape(-1, 3) / pb.mass[:, None]))
     if pb.surf is None:                   # IMPLICIT_EULER.h:235-241
         pb.surf = shell_surface(pb.X.shape[0], pb.faces) if pb.flow else surface(pb.X0, pb.tets)
     surf, dbc = pb.surf, pb.dbc
@@ -437,6 +444,7 @@ def advance_one_step(pb: Problem, Xtilde=None, verbose=False):
             sol = rhs.copy()
         # ---- Line_Search (IMPLICIT_EULER.h:9-149)
         Xprev = X.copy()
+        ncons_prev = int(cons.shape[0])
         p = sol.reshape(-1, 3)
         alpha = 1.0
         while True:
@@ -494,6 +502,8 @@ def advance_one_step(pb: Problem, Xtilde=None, verbose=False):
         else:
             use_gd = False
         pb.log.append(dict(it=it, E=Eprev, res=L2, alpha=alpha * 2, ncons=int(cons.shape[0]), kappa=pb.kappa[0]))
+        if on_iter is not None:
+            on_iter(it, Xprev, sol, ncons_prev)
         if verbose:
             print(f"it {it} E {Eprev:.12e} res {L2:.3e} alpha {alpha*2:.3e} C {cons.shape[0]} kappa {pb.kappa[0]:.3e}")
         if (len(res_record) == 3 and L2m <= pb.tol) or it >= pb.max_iters:
