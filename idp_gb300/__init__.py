@@ -39,7 +39,8 @@ EXPORTS = [
     "idp_set_normal_flow", "idp_set_kappa", "idp_tet_energy_noalloc", "idp_check_intersection",
     "idp_check_intersection_all", "idp_reset", "idp_device_bytes", "idp_job_footprint", "idp_server_create",
     "idp_server_create_simulated", "idp_server_submit", "idp_server_wait", "idp_server_drain",
-    "idp_server_get_stats", "idp_server_destroy", "idp_add_shell_instance",
+    "idp_server_get_stats", "idp_server_destroy", "idp_add_shell_instance", "idp_step_begin", "idp_step_iterate",
+    "idp_set_body_force",
 ]
 
 
@@ -89,7 +90,8 @@ class JobInfo(C.Structure):
 
 class ServerStats(C.Structure):
     _fields_ = [("submitted", C.c_longlong), ("completed", C.c_longlong), ("cohorts", C.c_longlong),
-                ("peak_resident", C.c_double), ("peak_concurrency", C.c_int), ("device_bytes", C.c_double)]
+                ("peak_resident", C.c_double), ("peak_concurrency", C.c_int), ("device_bytes", C.c_double),
+                ("peak_device", C.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -133,6 +135,9 @@ def load(path: str | None = None):
                                          C.c_void_p, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p]
     L.idp_commit.argtypes = [C.c_void_p]
     L.idp_advance.argtypes = [C.c_void_p, C.POINTER(Result)]
+    L.idp_step_begin.argtypes = [C.c_void_p]
+    L.idp_step_iterate.argtypes = [C.c_void_p, C.c_int, C.POINTER(Result), C.POINTER(C.c_int)]
+    L.idp_set_body_force.argtypes = [C.c_void_p, C.c_int, _dp]
     L.idp_get_state.argtypes = [C.c_void_p, C.c_int, _dp, _dp, _dp]
     L.idp_instance_info.argtypes = [C.c_void_p, C.c_int] + [C.POINTER(C.c_int)] * 5
     L.idp_get_surface.argtypes = [C.c_void_p, C.c_int, _ip, _ip, _ip]
@@ -255,6 +260,12 @@ class Context:
         v = _f64(v)
         self._check(load().idp_set_velocity(self._h, i, _pd(v)), "idp_set_velocity")
 
+    def set_body_force(self, i, b):
+        """Body force b (V,3) in the predictor x + (h v + h^2 M^-1 b); None removes it."""
+        bb = None if b is None else _f64(b)
+        self._check(load().idp_set_body_force(self._h, int(i), None if bb is None else _pd(bb)),
+                    "idp_set_body_force")
+
     def set_normal_flow(self, i, step):
         """x_tilde = x + step * n on surface vertices, x_tilde = x inside
         (instance i, or every instance for i = -1)."""
@@ -292,6 +303,20 @@ class Context:
         if check:
             self._check(rc, "idp_advance", ok=(IDP_OK, IDP_WARN_ITER_CAP))
         return rc, out
+
+    def step_begin(self):
+        """x^n = x, predictor and initial constraint set / energy (the first
+        part of advance)."""
+        self._check(load().idp_step_begin(self._h), "idp_step_begin")
+
+    def step_iterate(self, max_iters):
+        """At most max_iters Newton iterations; returns (rc, n_active, results)."""
+        res = (Result * len(self._V))()
+        n = C.c_int()
+        rc = load().idp_step_iterate(self._h, int(max_iters), res, C.byref(n))
+        if rc in (IDP_ERR_CUDA, IDP_ERR_STATE, IDP_ERR_INVALID_ARG, IDP_ERR_CAPACITY):
+            raise IDPError(rc, "idp_step_iterate")
+        return rc, n.value, [r.as_dict() for r in res]
 
     def save_state(self):
         self._check(load().idp_save_state(self._h), "idp_save_state")

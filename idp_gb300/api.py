@@ -55,12 +55,46 @@ class _Cache:
     key = None
 
 
+def _digest(*arrays):
+    """Content key of the arrays that define a context (not their ids: a new
+    array can reuse a freed one's address)."""
+    import hashlib
+
+    hsh = hashlib.blake2b(digest_size=16)
+    for a in arrays:
+        a = np.ascontiguousarray(a)
+        hsh.update(str((a.dtype.str, a.shape)).encode())
+        hsh.update(a.tobytes())
+    return hsh.hexdigest()
+
+
+def _dbc_indices(DBC, X=None):
+    """Vertex indices of the DBC storage (rows (index, x, y, z), the
+    reference's VECTOR_STORAGE<T, dim + 1>, IMPLICIT_EULER.h:155). Only fixed
+    DBCs are on this path: a target that differs from the vertex's position
+    (a moving DBC, solved by the reference's augmented Lagrangian,
+    Shell/DIRICHLET.h) raises NotImplementedError."""
+    if _empty(DBC):
+        return None
+    D = np.asarray(DBC, dtype=np.float64)
+    if D.ndim == 1:
+        return D.astype(np.int32)
+    idx = D[:, 0].astype(np.int32)
+    if X is not None and D.shape[1] >= 4 and not np.array_equal(D[:, 1:4], np.asarray(X)[idx]):
+        raise NotImplementedError(f"moving DBC targets: {_UNSUPPORTED}")
+    return idx
+
+
 def _context_for(tet, X, nodeAttr, tetEl, dHat2, kappaVec, DBC, h, NewtonTol, thickness, mode):
-    key = (id(tet), tet.shape, X.shape, float(dHat2), float(h), float(NewtonTol), float(thickness), mode)
+    dbc_idx = _dbc_indices(DBC, X)
+    key = (_digest(tet, nodeAttr["x0"], nodeAttr["m"], tetEl["lambda"], tetEl["mu"],
+                   np.zeros(0, np.int32) if dbc_idx is None else dbc_idx),
+           X.shape, float(dHat2), float(h), float(NewtonTol), float(thickness), mode)
     if _Cache.key == key and _Cache.ctx is not None:
         return _Cache.ctx
+    if _Cache.ctx is not None:
+        _Cache.ctx.close()
     ctx = Context(h=h, newton_tol=NewtonTol, thickness=thickness, mode=mode)
-    dbc_idx = None if _empty(DBC) else np.asarray(DBC)[:, 0].astype(np.int32)
     ctx.add_instance(X, tet, nodeAttr["m"], tetEl["lambda"], tetEl["mu"], dHat2, kappaVec[0], kappaVec[1],
                      X0=nodeAttr["x0"], dbc_idx=dbc_idx)
     ctx.commit()
@@ -90,13 +124,17 @@ class DiscreteShell:
             raise NotImplementedError(f"staticSolve: {_UNSUPPORTED}")
         if not withCollision:
             raise NotImplementedError("withCollision=False: the GB300 path always has IPC contact")
-        if b is not None and np.any(np.asarray(b) != 0):
-            raise NotImplementedError(f"body force: {_UNSUPPORTED}")
         tet = np.asarray(tet)
         ctx = _context_for(tet, X, nodeAttr, tetElasticityAttr, dHat2, kappaVec, DBC, h, NewtonTol, thickness,
                            DiscreteShell.mode)
+        # per call, as the reference reads them: positions, velocity, the
+        # kappa pair (a driver may reset it, e.g. initialize_OIPC) and the
+        # body force of the predictor (IMPLICIT_EULER.h:195-216)
         ctx.set_positions(0, X)
         ctx.set_velocity(0, nodeAttr["v"])
+        ctx.set_kappa(0, [kappaVec[0], kappaVec[1], 0.0])
+        bb = None if b is None else np.asarray(b, dtype=np.float64).reshape(-1, 3)
+        ctx.set_body_force(0, bb if bb is not None and np.any(bb != 0) else None)
         rc, res = ctx.advance(check=False)
         if rc not in (0, IDP_WARN_ITER_CAP):
             raise IDPError(rc, "Advance_One_Step_IE_Hinge")
@@ -125,7 +163,7 @@ def _flow_context_for(Elem, X, nodeAttr, elasticityAttr, dHat2, kappaVec, DBC, h
     shell_t = float(vol[0] / area[0])
     rho = float(np.sum(nodeAttr["m"]) / np.sum(vol))
     ctx = Context(h=h, newton_tol=NewtonTol, thickness=thickness, mode=mode)
-    dbc_idx = None if _empty(DBC) else np.asarray(DBC)[:, 0].astype(np.int32)
+    dbc_idx = _dbc_indices(DBC, X)
     ctx.add_shell_instance(X0, Elem, rho, shell_t, dHat2, kappaVec[0], kappaVec[1], dbc_idx=dbc_idx)
     ctx.commit()
     _FlowCache.ctx, _FlowCache.key = ctx, key

@@ -13,6 +13,7 @@
 #include <algorithm>
 #include <array>
 #include <chrono>
+#include <climits>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -62,6 +63,10 @@ struct idp_ctx {
     DBuf snap;                // saved X and v (6V)
     std::vector<double> snap_kappa;
     bool has_snap = false;
+    DBuf bacc;                // body-force accelerations M^-1 b (3V), when some instance has one
+    bool has_bacc = false;
+    bool stepping = false;    // a step is in flight (begun, instances still iterating)
+    std::chrono::steady_clock::time_point t_begin;  // the step's begin (latency origin)
 };
 
 namespace {
@@ -374,6 +379,7 @@ void idp_destroy(idp_ctx* c) {
     c->W.release();
     c->inst_buf.release();
     c->vel.release();
+    c->bacc.release();
     c->snap.release();
     cudaStreamDestroy(c->s);
     delete c;
@@ -391,6 +397,8 @@ int idp_reset(idp_ctx* c) {
     c->cs = ContactSet();
     c->prevC = 0;
     c->has_snap = false;
+    c->has_bacc = false;
+    c->stepping = false;
     c->snap_kappa.clear();
     c->W.stats = idp_stats{};
     c->W.dense_ready[0] = c->W.dense_ready[1] = false;
@@ -399,7 +407,7 @@ int idp_reset(idp_ctx* c) {
 
 int idp_device_bytes(idp_ctx* c, size_t* bytes) {
     if (!c || !bytes) return IDP_ERR_INVALID_ARG;
-    size_t n = c->inst_buf.bytes + c->vel.bytes + c->snap.bytes;
+    size_t n = c->inst_buf.bytes + c->vel.bytes + c->snap.bytes + c->bacc.bytes;
     for (const DBuf& b : c->owned) n += b.bytes;
     for (const DBuf& b : c->W.b) n += b.bytes;
     *bytes = n;
@@ -532,6 +540,39 @@ int idp_set_velocity(idp_ctx* c, int i, const double* v) {
     if (c->committed) {
         long o = 3L * c->A.v_off[i];
         IDP_CUDA_TRY(cudaMemcpyAsync(c->vel.as<double>() + o, v, sizeof(double) * 3 * h.V, cudaMemcpyHostToDevice, c->s));
+        IDP_CUDA_TRY(cudaStreamSynchronize(c->s));
+    }
+    return IDP_OK;
+}
+
+int idp_set_body_force(idp_ctx* c, int i, const double* b) {
+    if (!c || i < 0 || i >= (int)c->inst.size()) return IDP_ERR_INVALID_ARG;
+    HostInstance& h = c->inst[i];
+    if (!b) {
+        h.bacc.clear();
+    } else {
+        // a = M^-1 b with the lumped (diagonal) mass
+        std::vector<double> acc(3 * (size_t)h.V);
+        for (int v = 0; v < h.V; ++v) {
+            if (!(h.mass[v] > 0)) return IDP_ERR_INVALID_ARG;
+            for (int d = 0; d < 3; ++d) acc[3 * v + d] = b[3 * v + d] / h.mass[v];
+        }
+        h.bacc.swap(acc);
+    }
+    if (c->committed) {
+        cudaSetDevice(c->P.device);
+        const long n = 3L * c->A.V, o = 3L * c->A.v_off[i];
+        if (!c->has_bacc) {
+            if (!b) return IDP_OK;
+            if (c->bacc.ensure(sizeof(double) * (n + 3))) return IDP_ERR_CUDA;
+            IDP_CUDA_TRY(cudaMemsetAsync(c->bacc.p, 0, sizeof(double) * n, c->s));
+            c->has_bacc = true;
+        }
+        if (b)
+            IDP_CUDA_TRY(cudaMemcpyAsync(c->bacc.as<double>() + o, h.bacc.data(), sizeof(double) * 3 * h.V,
+                                         cudaMemcpyHostToDevice, c->s));
+        else
+            IDP_CUDA_TRY(cudaMemsetAsync(c->bacc.as<double>() + o, 0, sizeof(double) * 3 * h.V, c->s));
         IDP_CUDA_TRY(cudaStreamSynchronize(c->s));
     }
     return IDP_OK;
@@ -819,13 +860,160 @@ int idp_commit(idp_ctx* c) {
     else if (cudaMemcpy(c->vel.p, vel.data(), sizeof(double) * 3 * A.V, cudaMemcpyHostToDevice) != cudaSuccess)
         rc = IDP_ERR_CUDA;
     if (rc) return IDP_ERR_CUDA;
+    // body-force accelerations (only when some instance has one)
+    c->has_bacc = false;
+    for (const HostInstance& h : c->inst) c->has_bacc |= !h.bacc.empty();
+    if (c->has_bacc) {
+        std::vector<double> acc(3 * (size_t)A.V, 0.0);
+        for (int i = 0; i < nI; ++i)
+            if (!c->inst[i].bacc.empty())
+                std::copy(c->inst[i].bacc.begin(), c->inst[i].bacc.end(), acc.begin() + 3L * A.v_off[i]);
+        if (c->bacc.ensure(sizeof(double) * 3 * (A.V + 1)) ||
+            cudaMemcpy(c->bacc.p, acc.data(), sizeof(double) * 3 * A.V, cudaMemcpyHostToDevice) != cudaSuccess)
+            return IDP_ERR_CUDA;
+    }
     c->committed = true;
     return IDP_OK;
 }
 
-int idp_advance(idp_ctx* c, idp_result* results) {
+}  // extern "C"
+
+namespace idp {
+
+// milliseconds since t0 (host clock)
+static double since_ms(const std::chrono::steady_clock::time_point& t0) {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+// collect the phase timers of one call into the step's running stats
+static void collect_stats(idp_ctx* c, long long launches0) {
+    Work& W = c->W;
+    double ms[PhaseTimer::NPHASE], hms[PhaseTimer::NPHASE];
+    W.timer.collect(ms, hms);
+    if (std::getenv("IDP_PROFILE")) {
+        const char* nm[] = {"pcg", "tet", "contact", "ccd", "total", "barrier", "assembly", "linesearch"};
+        for (int k = 0; k < PhaseTimer::NPHASE; ++k)
+            std::fprintf(stderr, "idp phase %-10s device %10.3f ms  host %10.3f ms\n", nm[k], ms[k], hms[k]);
+        std::fprintf(stderr,
+                     "idp accd pairs %lld, iterations %lld, longest %lld, pairs over 1000 iterations %lld; "
+                     "contact blocks %d (max %d vertices); pcg iterations %lld; fp64 fallbacks %d\n",
+                     W.accd_pairs, W.accd_total, W.accd_maxit, W.accd_long, W.cl.n, W.cl.max_n,
+                     (long long)W.stats.pcg_iters, W.stats.fp64_fallbacks);
+        W.accd_maxit = W.accd_long = W.accd_total = W.accd_pairs = 0;
+        if (W.grid_prof[4]) {
+            const double n = (double)W.grid_prof[4];
+            std::fprintf(stderr, "idp grid pcg per iteration (CTA 0): spmv %.2f us, reduction A %.2f us, update %.2f us, reduction B %.2f us (%llu iterations)\n",
+                         W.grid_prof[0] / n / 1e3, W.grid_prof[1] / n / 1e3, W.grid_prof[2] / n / 1e3, W.grid_prof[3] / n / 1e3,
+                         W.grid_prof[4]);
+            for (auto& v : W.grid_prof) v = 0;
+        }
+    }
+    W.stats.barrier_ms += ms[PhaseTimer::BARRIER];
+    W.stats.assembly_ms += ms[PhaseTimer::ASSEMBLY];
+    W.stats.pcg_ms += ms[PhaseTimer::PCG];
+    W.stats.tet_ms += ms[PhaseTimer::TET];
+    W.stats.contact_ms += ms[PhaseTimer::CONTACT];
+    W.stats.ccd_ms += ms[PhaseTimer::CCD];
+    W.stats.total_ms += ms[PhaseTimer::TOTAL];
+    W.stats.kernel_launches += g_launch_count - launches0;
+}
+
+// Start one implicit-Euler step of the instances in `which` (the others keep
+// their state): x^n = x, predictor x_tilde = x + h v (+ h^2 M^-1 b with a body
+// force; IMPLICIT_EULER.h:195-216; a flow-mode shell's velocity is zeroed
+// first unless a predictor was set for this step, :207-209), and the initial
+// constraint set and energy (:418-434). The step's stats start here.
+int step_begin(idp_ctx* c, const std::vector<unsigned char>& which) {
     if (!c) return IDP_ERR_INVALID_ARG;
     if (!c->committed) return IDP_ERR_STATE;
+    cudaSetDevice(c->P.device);
+    Arena& A = c->A;
+    Work& W = c->W;
+    const int nI = A.nI;
+    const double h = c->P.h;
+    cudaStream_t s = c->s;
+    int rc;
+    W.timer.reset();
+    W.stats = idp_stats{};
+    const long long launches0 = g_launch_count;
+    W.timer.start(PhaseTimer::TOTAL, s);
+    c->t_begin = std::chrono::steady_clock::now();
+    if ((rc = set_mask(c, which))) return rc;
+    for (int i = 0; i < nI; ++i) {
+        if (!which[i]) continue;
+        HostInstance& hi0 = c->inst[i];
+        if (hi0.shell && !hi0.vel_set)
+            IDP_CUDA_TRY(cudaMemsetAsync(c->vel.as<double>() + 3L * A.v_off[i], 0, sizeof(double) * 3 * hi0.V, s));
+        hi0.vel_set = false;
+    }
+    if ((rc = vec_copy_masked(A, A.active, A.X, A.Xn, s))) return rc;
+    if ((rc = vec_xtilde(A, A.X, c->vel.as<double>(), h, A.Xtilde, s, c->has_bacc ? c->bacc.as<double>() : nullptr)))
+        return rc;
+    std::vector<InstState>& st = c->st;
+    for (int i = 0; i < nI; ++i) {
+        if (!which[i]) continue;
+        InstState& S = st[i];
+        double k = S.kappa, km = S.kappa_max;
+        S = InstState();
+        S.kappa = k;
+        S.kappa_max = km;
+        S.active = true;
+        S.finalized = false;
+        S.min_alpha = 1.0;
+    }
+    std::vector<double> kap(nI);
+    for (int i = 0; i < nI; ++i) kap[i] = st[i].kappa;
+    IDP_CUDA_TRY(cudaMemcpyAsync(A.kappa, kap.data(), sizeof(double) * nI, cudaMemcpyHostToDevice, s));
+    W.timer.start(PhaseTimer::CONTACT, s);
+    rc = build_constraint_set(A, W, A.X, c->cs, s);
+    W.timer.stop(s);
+    if (rc) return rc;
+    std::vector<double> E;
+    std::vector<int> bad;
+    if ((rc = eval_energy(c, A.X, true, E, bad))) return rc;
+    for (int i = 0; i < nI; ++i) {
+        if (!which[i]) continue;
+        st[i].Eprev = E[i];
+        st[i].ncons = c->cs.off[i + 1] - c->cs.off[i];
+        if (bad[i] == 1) { st[i].status = IDP_ERR_INVERTED; st[i].active = false; }
+        if (bad[i] == 2) { st[i].status = IDP_ERR_NONPOSITIVE_DIST; st[i].active = false; }
+    }
+    W.timer.stop(s);
+    IDP_CUDA_TRY(cudaStreamSynchronize(s));
+    collect_stats(c, launches0);
+    c->stepping = true;
+    return IDP_OK;
+}
+
+// Rebuild the constraint set and the previous-iterate set at the current
+// positions of every iterating instance. After instances were resumed into a
+// re-packed arena this restores what the end of their last Newton iteration
+// had left: both sets are functions of the positions alone.
+int step_prepare_resumed(idp_ctx* c) {
+    Arena& A = c->A;
+    const int nI = A.nI;
+    std::vector<unsigned char> m(nI, 0);
+    std::vector<double> kap(nI);
+    for (int i = 0; i < nI; ++i) {
+        m[i] = c->st[i].active ? 1 : 0;
+        kap[i] = c->st[i].kappa;
+    }
+    int rc;
+    IDP_CUDA_TRY(cudaMemcpyAsync(A.kappa, kap.data(), sizeof(double) * nI, cudaMemcpyHostToDevice, c->s));
+    if ((rc = set_mask(c, m))) return rc;
+    if ((rc = build_constraint_set(A, c->W, A.X, c->cs, c->s))) return rc;
+    if ((rc = save_prev_set(c, A.X))) return rc;
+    IDP_CUDA_TRY(cudaStreamSynchronize(c->s));
+    c->stepping = true;
+    return IDP_OK;
+}
+
+// At most max_iters Newton iterations (IMPLICIT_EULER.h:436-876) of every
+// instance still iterating. Instances that stop have their velocity
+// v = (x - x^n) / h (:882-888) written at the end of the call.
+int step_iterate(idp_ctx* c, int max_iters, idp_result* results, int* n_active) {
+    if (!c) return IDP_ERR_INVALID_ARG;
+    if (!c->committed || !c->stepping) return IDP_ERR_STATE;
     cudaSetDevice(c->P.device);
     Arena& A = c->A;
     Work& W = c->W;
@@ -835,67 +1023,28 @@ int idp_advance(idp_ctx* c, idp_result* results) {
     cudaStream_t s = c->s;
     int rc;
     W.timer.reset();
-    W.stats = idp_stats{};
     const long long launches0 = g_launch_count;
     W.timer.start(PhaseTimer::TOTAL, s);
-    const auto t_start = std::chrono::steady_clock::now();
-    std::vector<double> latency(nI, 0.0);
-    auto now_ms = [&]() {
-        return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
-    };
     auto build_cs = [&](const double* Xp) {
         W.timer.start(PhaseTimer::CONTACT, s);
         int r = build_constraint_set(A, W, Xp, c->cs, s);
         W.timer.stop(s);
         return r;
     };
-    std::vector<unsigned char> all(nI, 1), mask(nI, 0);
-    if ((rc = set_mask(c, all))) return rc;
-    // flow mode zeroes a shell's velocity before the predictor
-    // (IMPLICIT_EULER.h:207-209); a predictor set for this step (normal flow)
-    // is kept
-    for (int i = 0; i < nI; ++i) {
-        HostInstance& hi0 = c->inst[i];
-        if (hi0.shell && !hi0.vel_set)
-            IDP_CUDA_TRY(cudaMemsetAsync(c->vel.as<double>() + 3L * A.v_off[i], 0, sizeof(double) * 3 * hi0.V, s));
-        hi0.vel_set = false;
-    }
-    // x^n and x_tilde = x^n + h v (IMPLICIT_EULER.h:195-216)
-    IDP_CUDA_TRY(cudaMemcpyAsync(A.Xn, A.X, sizeof(double) * 3 * A.V, cudaMemcpyDeviceToDevice, s));
-    if ((rc = vec_xtilde(A, A.X, c->vel.as<double>(), h, A.Xtilde, s))) return rc;
+    std::vector<unsigned char> mask(nI, 0);
     std::vector<InstState>& st = c->st;
-    for (int i = 0; i < nI; ++i) {
-        InstState& S = st[i];
-        double k = S.kappa, km = S.kappa_max;
-        S = InstState();
-        S.kappa = k;
-        S.kappa_max = km;
-        S.active = true;
-        S.min_alpha = 1.0;
-    }
     std::vector<double> kap(nI);
     for (int i = 0; i < nI; ++i) kap[i] = st[i].kappa;
-    IDP_CUDA_TRY(cudaMemcpyAsync(A.kappa, kap.data(), sizeof(double) * nI, cudaMemcpyHostToDevice, s));
     std::vector<int> nDBC(nI, 0), nvert(nI);
     for (int i = 0; i < nI; ++i) {
         for (unsigned char d : c->inst[i].dbc) nDBC[i] += d;
         nvert[i] = c->inst[i].V;
     }
-    // initial constraint set and energy (IMPLICIT_EULER.h:418-434)
-    if ((rc = build_cs(A.X))) return rc;
     std::vector<double> E;
     std::vector<int> bad;
-    if ((rc = eval_energy(c, A.X, true, E, bad))) return rc;
-    for (int i = 0; i < nI; ++i) {
-        st[i].Eprev = E[i];
-        if (bad[i] == 1) { st[i].status = IDP_ERR_INVERTED; st[i].active = false; }
-        if (bad[i] == 2) { st[i].status = IDP_ERR_NONPOSITIVE_DIST; st[i].active = false; }
-    }
-    c->prevC = 0;
-    bool have_prev = false;
     std::vector<double> hv;
     std::vector<int> hi;
-    while (true) {
+    for (int round = 0; round < max_iters; ++round) {
         bool any = false;
         for (int i = 0; i < nI; ++i) {
             mask[i] = st[i].active ? 1 : 0;
@@ -1099,6 +1248,8 @@ int idp_advance(idp_ctx* c, idp_result* results) {
             }
         // ---- kappa adaptation (IMPLICIT_EULER.h:566-595) and the direction
         // norm of the stopping test, read back together
+        bool have_prev = false;
+        for (int i = 0; i < nI; ++i) have_prev |= mask[i] && st[i].have_prev;
         IDP_CUDA_TRY(cudaMemsetAsync(isc(c, SI_KFLAG), 0, sizeof(int) * nI, s));
         if (have_prev && c->prevC > 0)
             if ((rc = kappa_check(A, W, A.X, W[W_PREV_CONS].as<int4>(), W[W_PREV_INST].as<int>(),
@@ -1111,7 +1262,7 @@ int idp_advance(idp_ctx* c, idp_result* results) {
             std::vector<unsigned char> km(nI, 0);
             bool anyk = false;
             for (int i = 0; i < nI; ++i)
-                if (mask[i] && ksc.flag(SI_KFLAG, i) && st[i].kappa < st[i].kappa_max) {
+                if (mask[i] && st[i].have_prev && ksc.flag(SI_KFLAG, i) && st[i].kappa < st[i].kappa_max) {
                     st[i].kappa *= 2;
                     km[i] = 1;
                     anyk = true;
@@ -1127,12 +1278,14 @@ int idp_advance(idp_ctx* c, idp_result* results) {
             }
         }
         if ((rc = save_prev_set(c, A.X))) return rc;
-        have_prev = true;
+        for (int i = 0; i < nI; ++i)
+            if (mask[i]) st[i].have_prev = true;
         // ---- stopping criterion (IMPLICIT_EULER.h:647-676, 759, 855)
         for (int i = 0; i < nI; ++i) {
             if (!mask[i]) continue;
             InstState& S = st[i];
             double L2 = std::sqrt(ksc.d(S_NORM2, i) / (nvert[i] - nDBC[i])) / h;
+            S.ncons = c->cs.off[i + 1] - c->cs.off[i];
             S.iters += 1;
             S.last_res = L2;
             if (S.nres < 3) S.res[S.nres++] = L2;
@@ -1151,44 +1304,35 @@ int idp_advance(idp_ctx* c, idp_result* results) {
             } else if (c->inst[i].shell && c->cs.off[i + 1] == c->cs.off[i]) {
                 S.active = false;  // flow mode without contacts: one Newton step (IMPLICIT_EULER.h:850-854)
             }
-            if (!S.active) latency[i] = now_ms();
+            if (!S.active) S.latency_ms = since_ms(c->t_begin);
         }
     }
-    // v = (x - x^n) / h (IMPLICIT_EULER.h:882-888)
-    if ((rc = set_mask(c, all))) return rc;
-    if ((rc = vec_velocity(A, A.X, A.Xn, h, c->vel.as<double>(), s))) return rc;
+    // instances that stopped (in this call, or already at the step's begin):
+    // velocity v = (x - x^n) / h (IMPLICIT_EULER.h:882-888)
+    std::vector<unsigned char> fin(nI, 0);
+    bool any_fin = false;
+    int left = 0;
+    for (int i = 0; i < nI; ++i) {
+        if (st[i].active) {
+            ++left;
+            continue;
+        }
+        if (!st[i].finalized) {
+            fin[i] = 1;
+            any_fin = true;
+            st[i].finalized = true;
+            if (!(st[i].latency_ms > 0)) st[i].latency_ms = since_ms(c->t_begin);
+        }
+    }
+    if (any_fin) {
+        if ((rc = set_mask(c, fin))) return rc;
+        if ((rc = vec_velocity(A, A.X, A.Xn, h, c->vel.as<double>(), s))) return rc;
+    }
     W.timer.stop(s);
     IDP_CUDA_TRY(cudaStreamSynchronize(s));
-    {
-        double ms[PhaseTimer::NPHASE], hms[PhaseTimer::NPHASE];
-        W.timer.collect(ms, hms);
-        if (std::getenv("IDP_PROFILE")) {
-            const char* nm[] = {"pcg", "tet", "contact", "ccd", "total", "barrier", "assembly", "linesearch"};
-            for (int k = 0; k < PhaseTimer::NPHASE; ++k)
-                std::fprintf(stderr, "idp phase %-10s device %10.3f ms  host %10.3f ms\n", nm[k], ms[k], hms[k]);
-            std::fprintf(stderr,
-                         "idp accd pairs %lld, iterations %lld, longest %lld, pairs over 1000 iterations %lld; "
-                         "contact blocks %d (max %d vertices); pcg iterations %lld; fp64 fallbacks %d\n",
-                         W.accd_pairs, W.accd_total, W.accd_maxit, W.accd_long, W.cl.n, W.cl.max_n,
-                         (long long)W.stats.pcg_iters, W.stats.fp64_fallbacks);
-            W.accd_maxit = W.accd_long = W.accd_total = W.accd_pairs = 0;
-            if (W.grid_prof[4]) {
-                const double n = (double)W.grid_prof[4];
-                std::fprintf(stderr, "idp grid pcg per iteration (CTA 0): spmv %.2f us, reduction A %.2f us, update %.2f us, reduction B %.2f us (%llu iterations)\n",
-                             W.grid_prof[0] / n / 1e3, W.grid_prof[1] / n / 1e3, W.grid_prof[2] / n / 1e3, W.grid_prof[3] / n / 1e3,
-                             W.grid_prof[4]);
-                for (auto& v : W.grid_prof) v = 0;
-            }
-        }
-        W.stats.barrier_ms = ms[PhaseTimer::BARRIER];
-        W.stats.assembly_ms = ms[PhaseTimer::ASSEMBLY];
-        W.stats.pcg_ms = ms[PhaseTimer::PCG];
-        W.stats.tet_ms = ms[PhaseTimer::TET];
-        W.stats.contact_ms = ms[PhaseTimer::CONTACT];
-        W.stats.ccd_ms = ms[PhaseTimer::CCD];
-        W.stats.total_ms = ms[PhaseTimer::TOTAL];
-        W.stats.kernel_launches = g_launch_count - launches0;
-    }
+    collect_stats(c, launches0);
+    if (left == 0) c->stepping = false;
+    if (n_active) *n_active = left;
     int worst = IDP_OK;
     for (int i = 0; i < nI; ++i) {
         if (results) {
@@ -1197,16 +1341,68 @@ int idp_advance(idp_ctx* c, idp_result* results) {
             r.newton_iters = st[i].iters;
             r.pcg_iters = st[i].pcg_iters;
             r.ls_trials = st[i].ls_trials;
-            r.num_constraints = c->cs.off.size() > (size_t)i + 1 ? c->cs.off[i + 1] - c->cs.off[i] : 0;
+            r.num_constraints = st[i].ncons;
             r.energy = st[i].Eprev;
             r.kappa = st[i].kappa;
             r.residual = st[i].last_res;
             r.min_alpha = st[i].min_alpha;
-            r.latency_ms = latency[i] > 0 ? latency[i] : now_ms();
+            r.latency_ms = st[i].active ? since_ms(c->t_begin) : st[i].latency_ms;
         }
-        if (st[i].status != IDP_OK && st[i].status != IDP_WARN_ITER_CAP && worst == IDP_OK) worst = st[i].status;
+        if (!st[i].active && st[i].status != IDP_OK && st[i].status != IDP_WARN_ITER_CAP && worst == IDP_OK)
+            worst = st[i].status;
     }
     return worst;
+}
+
+int snapshot_instance(idp_ctx* c, int i, InstSnapshot& out) {
+    if (!c || !c->committed || i < 0 || i >= c->A.nI) return IDP_ERR_INVALID_ARG;
+    const long o = 3L * c->A.v_off[i], n = 3L * c->inst[i].V;
+    out.st = c->st[i];
+    out.X.resize(n);
+    out.Xn.resize(n);
+    out.Xt.resize(n);
+    IDP_CUDA_TRY(cudaMemcpyAsync(out.X.data(), c->A.X + o, sizeof(double) * n, cudaMemcpyDeviceToHost, c->s));
+    IDP_CUDA_TRY(cudaMemcpyAsync(out.Xn.data(), c->A.Xn + o, sizeof(double) * n, cudaMemcpyDeviceToHost, c->s));
+    IDP_CUDA_TRY(cudaMemcpyAsync(out.Xt.data(), c->A.Xtilde + o, sizeof(double) * n, cudaMemcpyDeviceToHost, c->s));
+    IDP_CUDA_TRY(cudaStreamSynchronize(c->s));
+    return IDP_OK;
+}
+
+bool instance_active(idp_ctx* c, int i) {
+    return c && i >= 0 && i < (int)c->st.size() && c->st[i].active;
+}
+
+int resume_instance(idp_ctx* c, int i, const InstSnapshot& in) {
+    if (!c || !c->committed || i < 0 || i >= c->A.nI) return IDP_ERR_INVALID_ARG;
+    const long o = 3L * c->A.v_off[i], n = 3L * c->inst[i].V;
+    if ((long)in.X.size() != n || (long)in.Xn.size() != n || (long)in.Xt.size() != n) return IDP_ERR_INVALID_ARG;
+    IDP_CUDA_TRY(cudaMemcpyAsync(c->A.X + o, in.X.data(), sizeof(double) * n, cudaMemcpyHostToDevice, c->s));
+    IDP_CUDA_TRY(cudaMemcpyAsync(c->A.Xn + o, in.Xn.data(), sizeof(double) * n, cudaMemcpyHostToDevice, c->s));
+    IDP_CUDA_TRY(cudaMemcpyAsync(c->A.Xtilde + o, in.Xt.data(), sizeof(double) * n, cudaMemcpyHostToDevice, c->s));
+    IDP_CUDA_TRY(cudaStreamSynchronize(c->s));
+    c->st[i] = in.st;
+    return IDP_OK;
+}
+
+}  // namespace idp
+
+extern "C" {
+
+int idp_step_begin(idp_ctx* c) {
+    if (!c) return IDP_ERR_INVALID_ARG;
+    return idp::step_begin(c, std::vector<unsigned char>(c->A.nI, 1));
+}
+
+int idp_step_iterate(idp_ctx* c, int max_iters, idp_result* results, int* n_active) {
+    if (max_iters < 0) return IDP_ERR_INVALID_ARG;
+    return idp::step_iterate(c, max_iters, results, n_active);
+}
+
+int idp_advance(idp_ctx* c, idp_result* results) {
+    int rc = idp_step_begin(c);
+    if (rc) return rc;
+    // the stats of idp_advance cover its begin and every Newton iteration
+    return idp::step_iterate(c, INT_MAX, results, nullptr);
 }
 
 int idp_save_state(idp_ctx* c) {
@@ -1310,7 +1506,8 @@ static int prep_one(idp_ctx* c, int i, const double* X) {
     long o = 3L * c->A.v_off[i];
     IDP_CUDA_TRY(cudaMemcpyAsync(c->A.Xprev + o, X, sizeof(double) * 3 * c->inst[i].V, cudaMemcpyHostToDevice, c->s));
     // x_tilde from the instance's current positions and velocity
-    rc = vec_xtilde(c->A, c->A.X, c->vel.as<double>(), c->P.h, c->A.Xtilde, c->s);
+    rc = vec_xtilde(c->A, c->A.X, c->vel.as<double>(), c->P.h, c->A.Xtilde, c->s,
+                    c->has_bacc ? c->bacc.as<double>() : nullptr);
     if (rc) return rc;
     std::vector<double> kap(c->A.nI);
     for (int k = 0; k < c->A.nI; ++k) kap[k] = c->st[k].kappa;

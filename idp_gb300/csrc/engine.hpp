@@ -39,6 +39,7 @@ struct HostInstance {
     std::vector<int> faces;
     std::vector<double> fvol;
     bool vel_set = false;  // predictor velocity given since the last advance
+    std::vector<double> bacc;  // body-force acceleration M^-1 b (3V; empty = none)
 };
 
 // per-instance Newton state kept on the host
@@ -54,6 +55,10 @@ struct InstState {
     double kappa = 0, kappa_max = 0;
     double min_alpha = 1;
     double g0 = 0;             // gradient norm at the first Newton iteration
+    bool have_prev = false;    // a previous iterate's constraint set exists (kappa test)
+    bool finalized = true;     // stopped and its velocity written
+    double latency_ms = 0;     // host time from the step's begin until it stopped
+    int ncons = 0;             // constraint-set size at its latest iterate
 };
 
 // one 2048-item tile of the fixed-order estimate of an instance's sum |dir|
@@ -125,6 +130,15 @@ struct Arena {
     int* vert_face_ptr = nullptr;                 // per vertex: list of face*3+corner, ascending
     int* vert_face = nullptr;
     double h = 0.1;                               // time step (flow Hessian coefficient)
+};
+
+// In-flight state of one instance in the middle of a step, enough to resume
+// its Newton loop in another arena (the request server re-packs a worker's
+// arena when new jobs join): positions, step-start positions, predictor and
+// the host-side Newton state. The constraint sets are rebuilt from X.
+struct InstSnapshot {
+    InstState st;
+    std::vector<double> X, Xn, Xt;
 };
 
 // CUDA-event timing of the engine's phases on the context stream; elapsed
@@ -279,6 +293,16 @@ struct Params {
     idp_params p;
 };
 
+// ---------------------------------------------------------------- stepping (engine.cpp)
+// idp_advance = step_begin(all) + step_iterate(until none is left); the
+// request server drives the parts itself.
+int step_begin(idp_ctx* c, const std::vector<unsigned char>& which);
+int step_iterate(idp_ctx* c, int max_iters, idp_result* results, int* n_active);
+int step_prepare_resumed(idp_ctx* c);
+int snapshot_instance(idp_ctx* c, int i, InstSnapshot& out);
+int resume_instance(idp_ctx* c, int i, const InstSnapshot& in);
+bool instance_active(idp_ctx* c, int i);  // still iterating in the step in flight
+
 // ---------------------------------------------------------------- launchers
 // shell.cu: flow energy of triangle shells (INC_POTENTIAL.h:53-73, 191-211)
 int flow_energy(Arena& A, Work& W, const double* X, double* inst_E, cudaStream_t s);  // accumulates
@@ -342,7 +366,9 @@ int vec_fill(double* a, long n, double v, cudaStream_t s);
 int vec_copy_masked(Arena& A, const unsigned char* mask, const double* src, double* dst, cudaStream_t s);
 int vec_dir_norm2(Arena& A, Work& W, const double* dir, double* inst_out, cudaStream_t s);
 int vec_velocity(Arena& A, const double* X, const double* Xn, double h, double* v, cudaStream_t s);
-int vec_xtilde(Arena& A, const double* X, const double* v, double h, double* Xt, cudaStream_t s);
+// x_tilde = x + h v, or x + (h v + h^2 acc) with a body force (acc = M^-1 b)
+int vec_xtilde(Arena& A, const double* X, const double* v, double h, double* Xt, cudaStream_t s,
+               const double* acc = nullptr);
 int kappa_check(Arena& A, Work& W, const double* X, const int4* cons, const int* cinst, const double* d2prev, long C,
                 int* inst_flag, cudaStream_t s);
 

@@ -1,12 +1,22 @@
 // Request server: continuous batching of independent Newton-step solves on
-// one GPU (the C ABI's idp_server_*). Host-only C++: a FIFO of jobs, an
-// admission rule on the sum of the admitted jobs' memory footprints, and a
-// pool of worker threads; each worker owns one context (one CUDA stream and
-// one device arena) and solves one cohort at a time, so cohorts of different
-// workers overlap on the device. New jobs are admitted whenever a worker is
-// free and the budget allows, i.e. while other cohorts are between Newton
-// iterations. The reference has no counterpart: its Python driver advances
-// one scene per call (Python/Drivers/FEMDiscreteShellBase.py:333-361).
+// one GPU (the C ABI's idp_server_*). Host C++: a FIFO of jobs, an admission
+// rule on device memory, and a pool of worker threads; each worker owns one
+// context (one CUDA stream and one device arena) holding the jobs it is
+// solving. A worker advances its jobs a few Newton iterations at a time
+// (step_iterate); between those chunks it releases every job that finished
+// (its result is written at once) and admits jobs from the head of the queue
+// into its running arena: the jobs still iterating are snapshotted, the
+// arena is rebuilt with them and the new jobs, and their Newton loops resume
+// where they were. Workers run concurrently on their own streams. The
+// reference has no counterpart: its Python driver advances one scene per
+// call (Python/Drivers/FEMDiscreteShellBase.py:333-361).
+//
+// Memory: a worker occupies max(bytes its context holds, footprints of its
+// unfinished jobs); a job is admitted only while the sum of that over all
+// workers, with the job added to the admitting worker, stays within the
+// budget. An idle worker's context counts too: when the head job does not fit
+// and some idle worker holds memory, the idle workers are asked to give
+// their contexts back.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -19,7 +29,7 @@
 #include <thread>
 #include <vector>
 
-#include "idp_gb300.h"
+#include "engine.hpp"
 
 namespace {
 
@@ -34,10 +44,16 @@ struct Job {
     double* v_out = nullptr;
     double footprint = 0;
     bool done = false;
+    int sim_left = 0;  // simulated mode: Newton iterations still to run
     idp_job_info info{};
 };
 
 using Clock = std::chrono::steady_clock;
+
+// simulated mode: a job of V vertices needs 2 + V/1000 Newton iterations; an
+// iteration of a worker costs ms_per_kvertex / 10 per thousand vertices of
+// its unfinished jobs
+int sim_iters(int V) { return 2 + V / 1000; }
 
 }  // namespace
 
@@ -45,6 +61,7 @@ struct idp_server {
     idp_params P{};
     double budget = 0;
     int max_batch = 1;
+    int chunk = 4;                // Newton iterations between admission points
     bool simulated = false;
     double sim_ms_per_kvertex = 0;
     std::mutex mu;
@@ -53,149 +70,267 @@ struct idp_server {
     std::map<int, std::unique_ptr<Job>> jobs;
     int next_id = 0;
     int next_cohort = 0;
-    double resident = 0;          // sum of footprints of admitted, unfinished jobs
     std::vector<double> held;     // device bytes each worker's context holds
+    std::vector<double> res;      // footprints of each worker's unfinished jobs
+    std::vector<int> live;        // each worker's unfinished jobs
+    bool release_req = false;     // the head job waits for idle workers' memory
     bool stop = false;
-    int running = 0;
     idp_server_stats st{};
     std::vector<std::thread> threads;
     Clock::time_point t0 = Clock::now();
 
     double now_ms() const { return std::chrono::duration<double, std::milli>(Clock::now() - t0).count(); }
-    bool admissible() const { return !pending.empty() && resident + pending.front()->footprint <= budget; }
+    double occupied(int w, double extra) const { return std::max(held[w], res[w] + extra); }
+    // device memory in use if worker w took `extra` more bytes of jobs
+    double total_with(int w, double extra) const {
+        double t = 0;
+        for (size_t k = 0; k < held.size(); ++k) t += occupied((int)k, (int)k == w ? extra : 0.0);
+        return t;
+    }
+    bool head_fits(int w) const {
+        return !pending.empty() && live[w] < max_batch && total_with(w, pending.front()->footprint) <= budget;
+    }
+    void note_peaks() {
+        double r = 0;
+        int running = 0;
+        for (size_t k = 0; k < res.size(); ++k) {
+            r += res[k];
+            running += live[k] > 0;
+        }
+        st.peak_resident = std::max(st.peak_resident, r);
+        st.peak_device = std::max(st.peak_device, total_with(-1, 0.0));
+        st.peak_concurrency = std::max(st.peak_concurrency, running);
+    }
 };
 
 namespace {
 
-// One cohort on a worker's context: add, commit, predictors, advance, read back.
-int solve_cohort(idp_server* S, idp_ctx*& ctx, std::vector<Job*>& cohort, std::vector<idp_result>& res) {
-    int rc = IDP_OK;
-    if (!ctx) {
-        ctx = idp_create(&S->P, &rc);
-        if (!ctx) return rc ? rc : IDP_ERR_CUDA;
-    } else if ((rc = idp_reset(ctx))) {
+// A worker's arena and the jobs in it, in arena order; slots of finished jobs
+// stay (inactive) until the next re-pack.
+struct Slots {
+    idp_ctx* ctx = nullptr;
+    std::vector<Job*> job;
+    std::vector<char> live;
+    std::vector<idp_result> res;
+    double sim_bytes = 0;  // simulated mode: bytes the arena would hold
+};
+
+// Rebuild the worker's arena with its unfinished jobs (resumed where their
+// Newton loops were) followed by the new jobs (begun).
+int repack(idp_server* S, Slots& W, const std::vector<Job*>& fresh) {
+    std::vector<Job*> keep;
+    std::vector<idp::InstSnapshot> snaps;
+    int rc;
+    for (size_t k = 0; k < W.job.size(); ++k)
+        if (W.live[k]) {
+            keep.push_back(W.job[k]);
+            if (!S->simulated) {
+                snaps.emplace_back();
+                if ((rc = idp::snapshot_instance(W.ctx, (int)k, snaps.back()))) return rc;
+            }
+        }
+    W.job = keep;
+    W.job.insert(W.job.end(), fresh.begin(), fresh.end());
+    W.live.assign(W.job.size(), 1);
+    W.res.assign(W.job.size(), idp_result{});
+    if (S->simulated) {
+        double fp = 0;
+        for (Job* j : W.job) fp += j->footprint;
+        W.sim_bytes = std::max(W.sim_bytes, fp);  // grow-only, as a real context
+        return IDP_OK;
+    }
+    if (!W.ctx) {
+        W.ctx = idp_create(&S->P, &rc);
+        if (!W.ctx) return rc ? rc : IDP_ERR_CUDA;
+    } else if ((rc = idp_reset(W.ctx))) {
         return rc;
     }
-    for (Job* j : cohort) {
-        int k = idp_add_instance(ctx, j->V, j->X.data(), j->X0.data(), j->T, j->tets.data(), j->mass.data(),
+    for (Job* j : W.job) {
+        int k = idp_add_instance(W.ctx, j->V, j->X.data(), j->X0.data(), j->T, j->tets.data(), j->mass.data(),
                                  j->lam.data(), j->mu.data(), j->nDBC, j->dbc.empty() ? nullptr : j->dbc.data(),
                                  j->dHat2, j->kappa, j->kappa_max);
         if (k < 0) return -k;
-        if (j->has_v && (rc = idp_set_velocity(ctx, k, j->v.data()))) return rc;
+        if (k >= (int)keep.size() && j->has_v && (rc = idp_set_velocity(W.ctx, k, j->v.data()))) return rc;
     }
-    if ((rc = idp_commit(ctx))) return rc;
-    for (size_t k = 0; k < cohort.size(); ++k)
-        if (cohort[k]->normal_flow != 0 && (rc = idp_set_normal_flow(ctx, (int)k, cohort[k]->normal_flow))) return rc;
-    res.assign(cohort.size(), idp_result{});
-    rc = idp_advance(ctx, res.data());
-    if (rc == IDP_ERR_CUDA || rc == IDP_ERR_CAPACITY || rc == IDP_ERR_STATE || rc == IDP_ERR_INVALID_ARG) return rc;
-    for (size_t k = 0; k < cohort.size(); ++k) {
-        Job* j = cohort[k];
-        if (j->X_out || j->v_out) {
-            int r = idp_get_state(ctx, (int)k, j->X_out, j->v_out, nullptr);
-            if (r) return r;
+    if ((rc = idp_commit(W.ctx))) return rc;
+    for (size_t k = 0; k < keep.size(); ++k)
+        if ((rc = idp::resume_instance(W.ctx, (int)k, snaps[k]))) return rc;
+    std::vector<unsigned char> which(W.job.size(), 0);
+    for (size_t k = keep.size(); k < W.job.size(); ++k) {
+        which[k] = 1;
+        Job* j = W.job[k];
+        if (j->normal_flow != 0 && (rc = idp_set_normal_flow(W.ctx, (int)k, j->normal_flow))) return rc;
+    }
+    if ((rc = idp::step_begin(W.ctx, which))) return rc;
+    return idp::step_prepare_resumed(W.ctx);
+}
+
+// One chunk of Newton iterations of the worker's live jobs.
+int iterate(idp_server* S, Slots& W) {
+    if (S->simulated) {
+        double kv = 0;
+        for (size_t k = 0; k < W.job.size(); ++k)
+            if (W.live[k]) kv += W.job[k]->V / 1000.0;
+        int n = 0;
+        for (size_t k = 0; k < W.job.size(); ++k)
+            if (W.live[k]) n = std::max(n, std::min(S->chunk, W.job[k]->sim_left));
+        std::this_thread::sleep_for(std::chrono::duration<double, std::milli>(S->sim_ms_per_kvertex * kv * n / 10.0));
+        for (size_t k = 0; k < W.job.size(); ++k) {
+            if (!W.live[k]) continue;
+            Job* j = W.job[k];
+            j->sim_left -= std::min(n, j->sim_left);
+            W.res[k].newton_iters = sim_iters(j->V) - j->sim_left;
+            W.res[k].status = j->sim_left > 0 ? IDP_ERR_NOT_CONVERGED : IDP_OK;
         }
+        return IDP_OK;
     }
+    int left = 0;
+    const int rc = idp::step_iterate(W.ctx, S->chunk, W.res.data(), &left);
+    if (rc == IDP_ERR_CUDA || rc == IDP_ERR_CAPACITY || rc == IDP_ERR_STATE || rc == IDP_ERR_INVALID_ARG) return rc;
     return IDP_OK;
 }
 
-void simulate_cohort(idp_server* S, std::vector<Job*>& cohort, std::vector<idp_result>& res) {
-    double kv = 0;
-    for (Job* j : cohort) kv += j->V / 1000.0;
-    std::this_thread::sleep_for(std::chrono::duration<double, std::milli>(S->sim_ms_per_kvertex * kv));
-    res.assign(cohort.size(), idp_result{});
-    for (size_t k = 0; k < cohort.size(); ++k) {
-        Job* j = cohort[k];
-        res[k].status = IDP_OK;
-        res[k].newton_iters = 1;
-        if (j->X_out) std::copy(j->X.begin(), j->X.end(), j->X_out);
-        if (j->v_out) std::fill(j->v_out, j->v_out + 3 * (size_t)j->V, 0.0);
-    }
+// true when slot k's job stopped iterating
+bool finished(idp_server* S, Slots& W, size_t k) {
+    if (S->simulated) return W.job[k]->sim_left <= 0;
+    return !idp::instance_active(W.ctx, (int)k);
+}
+
+void release_inputs(Job* j) {
+    std::vector<double>().swap(j->X);
+    std::vector<double>().swap(j->X0);
+    std::vector<double>().swap(j->mass);
+    std::vector<double>().swap(j->lam);
+    std::vector<double>().swap(j->mu);
+    std::vector<double>().swap(j->v);
+    std::vector<int32_t>().swap(j->tets);
+    std::vector<int32_t>().swap(j->dbc);
+}
+
+double held_bytes(idp_server* S, Slots& W) {
+    if (S->simulated) return W.sim_bytes;
+    size_t bytes = 0;
+    if (W.ctx) idp_device_bytes(W.ctx, &bytes);
+    return (double)bytes;
+}
+
+void drop_context(Slots& W) {
+    if (W.ctx) idp_destroy(W.ctx);
+    W.ctx = nullptr;
+    W.sim_bytes = 0;
+    W.job.clear();
+    W.live.clear();
+    W.res.clear();
 }
 
 void worker(idp_server* S, int w) {
-    idp_ctx* ctx = nullptr;
+    Slots W;
     std::unique_lock<std::mutex> lk(S->mu);
     while (true) {
-        S->cv_work.wait(lk, [&] { return S->admissible() || (S->stop && S->pending.empty()); });
-        if (S->pending.empty()) break;  // stopping, nothing left
-        // cohort: jobs from the head of the queue while they fit
-        std::vector<Job*> cohort;
+        S->cv_work.wait(lk, [&] {
+            return S->live[w] > 0 || S->head_fits(w) || (S->release_req && S->live[w] == 0 && S->held[w] > 0) ||
+                   (S->stop && S->pending.empty());
+        });
+        if (S->live[w] == 0 && S->pending.empty() && S->stop) break;
+        if (S->live[w] == 0 && !S->head_fits(w)) {
+            // idle, asked to give its memory back
+            lk.unlock();
+            drop_context(W);
+            lk.lock();
+            S->held[w] = 0;
+            S->cv_work.notify_all();
+            continue;
+        }
+        // admission at the queue head, between Newton iterations
+        std::vector<Job*> fresh;
         double fp = 0;
-        while (!S->pending.empty() && (int)cohort.size() < S->max_batch &&
-               S->resident + fp + S->pending.front()->footprint <= S->budget) {
+        while (!S->pending.empty() && S->live[w] + (int)fresh.size() < S->max_batch &&
+               S->total_with(w, fp + S->pending.front()->footprint) <= S->budget) {
             fp += S->pending.front()->footprint;
-            cohort.push_back(S->pending.front());
+            fresh.push_back(S->pending.front());
             S->pending.pop_front();
         }
-        S->resident += fp;
-        S->st.peak_resident = std::max(S->st.peak_resident, S->resident);
-        S->running += 1;
-        S->st.peak_concurrency = std::max(S->st.peak_concurrency, S->running);
-        const int cid = S->next_cohort++;
-        S->st.cohorts += 1;
-        const double t_admit = S->now_ms();
-        for (Job* j : cohort) {
-            j->info.admit_ms = t_admit;
-            j->info.cohort = cid;
-            j->info.cohort_size = (int)cohort.size();
+        if (!fresh.empty()) {
+            S->res[w] += fp;
+            S->live[w] += (int)fresh.size();
+            S->release_req = false;
+            const int cid = S->next_cohort++;
+            S->st.cohorts += 1;
+            const double t_admit = S->now_ms();
+            for (Job* j : fresh) {
+                j->info.admit_ms = t_admit;
+                j->info.cohort = cid;
+                j->sim_left = sim_iters(j->V);
+            }
+            S->note_peaks();
+        }
+        // the head job waits for memory that idle workers hold: ask them
+        if (!S->pending.empty() && fresh.empty() && !S->head_fits(w)) {
+            for (size_t k = 0; k < S->held.size(); ++k)
+                if ((int)k != w && S->live[k] == 0 && S->held[k] > 0) S->release_req = true;
+            if (S->release_req) S->cv_work.notify_all();
         }
         if (!S->pending.empty()) S->cv_work.notify_one();  // another worker may take the rest
         lk.unlock();
 
-        std::vector<idp_result> res;
         int rc = IDP_OK;
         try {
-            if (S->simulated) simulate_cohort(S, cohort, res);
-            else rc = solve_cohort(S, ctx, cohort, res);
+            if (!fresh.empty()) rc = repack(S, W, fresh);
+            for (Job* j : fresh) j->info.cohort_size = (int)W.job.size();
+            if (rc == IDP_OK) rc = iterate(S, W);
         } catch (const std::bad_alloc&) {
-            rc = IDP_ERR_CAPACITY;  // host memory for the cohort's arrays
+            rc = IDP_ERR_CAPACITY;  // host memory for the jobs' arrays
         } catch (...) {
             rc = IDP_ERR_INVALID_ARG;
         }
-        if (rc == IDP_OK && res.size() != cohort.size()) rc = IDP_ERR_STATE;
-        size_t bytes = 0;
-        if (ctx) idp_device_bytes(ctx, &bytes);
+        // results of the jobs that stopped (all live jobs on an error)
+        std::vector<size_t> done;
+        for (size_t k = 0; k < W.job.size(); ++k)
+            if (W.live[k] && (rc != IDP_OK || finished(S, W, k))) done.push_back(k);
+        std::vector<int> out_rc(done.size(), IDP_OK);
+        for (size_t d = 0; d < done.size(); ++d) {
+            Job* j = W.job[done[d]];
+            if (rc == IDP_OK && !S->simulated && (j->X_out || j->v_out))
+                out_rc[d] = idp_get_state(W.ctx, (int)done[d], j->X_out, j->v_out, nullptr);
+            if (rc == IDP_OK && S->simulated) {
+                if (j->X_out) std::copy(j->X.begin(), j->X.end(), j->X_out);
+                if (j->v_out) std::fill(j->v_out, j->v_out + 3 * (size_t)j->V, 0.0);
+            }
+        }
+        const double bytes = held_bytes(S, W);
 
         lk.lock();
         const double t_done = S->now_ms();
-        for (size_t k = 0; k < cohort.size(); ++k) {
-            Job* j = cohort[k];
-            j->info.result = rc == IDP_OK ? res[k] : idp_result{};
-            j->info.status = rc == IDP_OK ? res[k].status : rc;
-            j->info.result.status = j->info.status;
+        for (size_t d = 0; d < done.size(); ++d) {
+            const size_t k = done[d];
+            Job* j = W.job[k];
+            const int status = rc != IDP_OK ? rc : (out_rc[d] != IDP_OK ? out_rc[d] : W.res[k].status);
+            j->info.result = rc == IDP_OK ? W.res[k] : idp_result{};
+            j->info.status = status;
+            j->info.result.status = status;
+            j->info.result.latency_ms = t_done - j->info.admit_ms;
             j->info.done_ms = t_done;
             j->done = true;
-            // the record stays for idp_server_wait; the inputs are no longer needed
-            std::vector<double>().swap(j->X);
-            std::vector<double>().swap(j->X0);
-            std::vector<double>().swap(j->mass);
-            std::vector<double>().swap(j->lam);
-            std::vector<double>().swap(j->mu);
-            std::vector<double>().swap(j->v);
-            std::vector<int32_t>().swap(j->tets);
-            std::vector<int32_t>().swap(j->dbc);
+            W.live[k] = 0;
+            S->res[w] -= j->footprint;
+            S->live[w] -= 1;
+            S->st.completed += 1;
+            release_inputs(j);
         }
-        S->resident -= fp;
-        S->running -= 1;
-        S->st.completed += (long long)cohort.size();
-        // keep the context's buffers for the next cohort while all workers'
-        // contexts together stay under the budget
-        S->held[w] = (double)bytes;
-        double total = 0;
-        for (double h : S->held) total += h;
-        if (ctx && (total > S->budget || rc == IDP_ERR_CUDA)) {
+        if (S->live[w] == 0) S->res[w] = 0;  // no rounding residue
+        S->held[w] = bytes;
+        S->note_peaks();
+        if (rc == IDP_ERR_CUDA || (S->live[w] == 0 && S->total_with(-1, 0.0) > S->budget)) {
             lk.unlock();
-            idp_destroy(ctx);
-            ctx = nullptr;
+            drop_context(W);
             lk.lock();
             S->held[w] = 0;
         }
-        S->cv_done.notify_all();
+        if (!done.empty()) S->cv_done.notify_all();
         S->cv_work.notify_all();
     }
     lk.unlock();
-    if (ctx) idp_destroy(ctx);
+    drop_context(W);
 }
 
 idp_server* make_server(double budget, int workers, int max_batch) {
@@ -205,6 +340,8 @@ idp_server* make_server(double budget, int workers, int max_batch) {
     S->budget = budget;
     S->max_batch = max_batch;
     S->held.assign(workers, 0.0);
+    S->res.assign(workers, 0.0);
+    S->live.assign(workers, 0);
     return S;
 }
 

@@ -57,6 +57,18 @@ __global__ void k_xtilde(long V, const int* __restrict__ vinst, const unsigned c
     for (int d = 0; d < 3; ++d) Xt[3 * i + d] = X[3 * i + d] + h * v[3 * i + d];
 }
 
+// with a body force (IMPLICIT_EULER.h:195-216): x_tilde = x + (h v + h^2 a),
+// a = M^-1 b, each operation rounded on its own in the reference's order
+__global__ void k_xtilde_b(long V, const int* __restrict__ vinst, const unsigned char* __restrict__ active,
+                           const double* __restrict__ X, const double* __restrict__ v, const double* __restrict__ a,
+                           double h, double* __restrict__ Xt) {
+    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= V || !active[vinst[i]]) return;
+    const double h2 = __dmul_rn(h, h);
+    for (int d = 0; d < 3; ++d)
+        Xt[3 * i + d] = __dadd_rn(X[3 * i + d], __dadd_rn(__dmul_rn(h, v[3 * i + d]), __dmul_rn(h2, a[3 * i + d])));
+}
+
 // kappa adaptation test of IMPLICIT_EULER.h:566-595 over the previous set
 __global__ void k_kappa_check(long C, const int4* __restrict__ cons, const int* __restrict__ cinst,
                               const unsigned char* __restrict__ active, const double* __restrict__ X,
@@ -101,8 +113,11 @@ int vec_velocity(Arena& A, const double* X, const double* Xn, double h, double* 
     return cudaGetLastError() == cudaSuccess ? IDP_OK : IDP_ERR_CUDA;
 }
 
-int vec_xtilde(Arena& A, const double* X, const double* v, double h, double* Xt, cudaStream_t s) {
-    (::idp::count_launch(), k_xtilde<<<grid_for(A.V), kBlock, 0, s>>>(A.V, A.vinst, A.active, X, v, h, Xt));
+int vec_xtilde(Arena& A, const double* X, const double* v, double h, double* Xt, cudaStream_t s, const double* acc) {
+    if (acc)
+        (::idp::count_launch(), k_xtilde_b<<<grid_for(A.V), kBlock, 0, s>>>(A.V, A.vinst, A.active, X, v, acc, h, Xt));
+    else
+        (::idp::count_launch(), k_xtilde<<<grid_for(A.V), kBlock, 0, s>>>(A.V, A.vinst, A.active, X, v, h, Xt));
     return cudaGetLastError() == cudaSuccess ? IDP_OK : IDP_ERR_CUDA;
 }
 

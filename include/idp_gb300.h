@@ -129,8 +129,6 @@ int idp_add_instance(idp_ctx* ctx, int V, const double* X, const double* X0, int
                      const double* mass, const double* lam, const double* mu, int nDBC, const int32_t* dbc_idx,
                      double dHat2, double kappa, double kappa_max);
 
-/* Velocity v (3V); x_tilde = x + h v (IMPLICIT_EULER.h:195-216, no body force).
- * MeshIO.Load_Velocity_X0 (Utils/MESHIO.h:986-1004) sets v = (target - x)/h. */
 /* Add a triangle shell advanced in flow mode (the Laplacian flow energy of
  * Advance_One_Step_IE_Flow, FEM/Shell/DISCRETE_SHELL.h:1113, with
  * INC_POTENTIAL.h:53-73,191-211,323-339) with offset-IPC self-contact.
@@ -146,7 +144,16 @@ int idp_add_shell_instance(idp_ctx* ctx, int V, const double* X, int F, const in
                            double thickness, int nDBC, const int32_t* dbc_idx, double dHat2, double kappa,
                            double kappa_max);
 
+/* Velocity v (3V); x_tilde = x + h v (IMPLICIT_EULER.h:195-216; a body force
+ * adds h^2 M^-1 b, idp_set_body_force). MeshIO.Load_Velocity_X0
+ * (Utils/MESHIO.h:986-1004) sets v = (target - x)/h. */
 int idp_set_velocity(idp_ctx* ctx, int inst, const double* v);
+/* Body force b (3V) of one instance, the `b` argument of
+ * Advance_One_Step_IE_Hinge: the predictor becomes
+ * x_tilde = x + (h v + h^2 M^-1 b) (IMPLICIT_EULER.h:195-216; M is the lumped
+ * mass, so M^-1 b = b / m per vertex). Kept for every following step until
+ * changed; b = NULL removes it. Before or after idp_commit. */
+int idp_set_body_force(idp_ctx* ctx, int inst, const double* b);
 /* Current positions (3V), e.g. a warm start between frames. */
 int idp_set_positions(idp_ctx* ctx, int inst, const double* X);
 
@@ -170,6 +177,21 @@ int idp_commit(idp_ctx* ctx);
  * (FEM/Shell/DISCRETE_SHELL.h:1110 -> IMPLICIT_EULER.h:151-891).
  * results: array of idp_result, one per instance (may be NULL). */
 int idp_advance(idp_ctx* ctx, idp_result* results);
+
+/* The same step in bounded parts, for callers that interleave other work
+ * between Newton iterations (the request server admits new meshes there):
+ * idp_step_begin does what idp_advance does first (x^n = x, the predictor
+ * x_tilde, the initial constraint set and energy, IMPLICIT_EULER.h:195-216,
+ * 418-434); idp_step_iterate then runs at most max_iters Newton iterations
+ * of the instances still iterating (IMPLICIT_EULER.h:436-876). An instance
+ * that stops has its velocity and result final at the end of the call;
+ * *n_active (may be NULL) receives how many are still iterating, and results
+ * (may be NULL) one idp_result per instance. idp_advance = idp_step_begin,
+ * then idp_step_iterate until none is left; the parts give the same results
+ * bit for bit. idp_get_stats covers the step since its begin. The reference
+ * runs the whole loop in one call. */
+int idp_step_begin(idp_ctx* ctx);
+int idp_step_iterate(idp_ctx* ctx, int max_iters, idp_result* results, int* n_active);
 
 /* Device-side checkpoint of every instance's positions, velocity and kappa
  * (the reference restarts from OBJ files instead,
@@ -252,16 +274,19 @@ int idp_check_intersection_all(idp_ctx* ctx, int32_t* counts);
  * (Python/Drivers/FEMDiscreteShellBase.py:333-361).
  *
  * Jobs (one mesh and its predictor each) are queued in arrival order. A pool
- * of worker threads, each driving its own context and CUDA stream, forms a
- * cohort from the head of the queue whenever it is free: as many jobs as fit
- * under the memory budget (sum of admitted footprints) and max_batch, solved
- * together in one arena (idp_advance); cohorts of different workers run on
- * the device at the same time. A job that arrives while cohorts are running
- * is admitted by the next free worker as soon as memory allows, so new work
- * joins the device between the running cohorts' Newton iterations. Worker
- * contexts keep their buffers between cohorts (idp_reset) while the total
- * they hold stays under the budget. A job's result does not depend on the
- * cohort it ran in (per-instance reductions are fixed-order).
+ * of worker threads, each driving its own context and CUDA stream, solves
+ * the jobs it holds a few Newton iterations at a time. Between those chunks a
+ * worker writes the result of every job that finished (at once, not when the
+ * slowest job it holds finishes) and admits jobs from the head of the queue
+ * into its running arena (max_batch jobs at most): the jobs still iterating
+ * are carried over to a rebuilt arena with the new ones and their Newton
+ * loops continue where they were. Workers run on the device at the same
+ * time. Admission keeps the sum over workers of max(device bytes the worker's
+ * context holds, footprints of its unfinished jobs) within the budget; idle
+ * workers give their contexts back when the head job needs that memory.
+ * A job's result does not depend on the jobs it ran with (per-instance
+ * reductions are fixed-order, and a carried-over instance resumes with its
+ * exact state).
  * ------------------------------------------------------------------------- */
 typedef struct idp_server idp_server;
 
@@ -295,10 +320,13 @@ typedef struct idp_job_info {
 } idp_job_info;
 
 typedef struct idp_server_stats {
-    long long submitted, completed, cohorts;
-    double peak_resident;   /* largest sum of admitted footprints                      */
-    int peak_concurrency;   /* most cohorts on the device at once                       */
+    long long submitted, completed, cohorts; /* cohorts: admission events           */
+    double peak_resident;   /* largest sum of the footprints of admitted, unfinished jobs */
+    int peak_concurrency;   /* most workers with unfinished jobs at once                */
     double device_bytes;    /* device memory the worker contexts hold now               */
+    double peak_device;     /* largest sum over workers of max(bytes the context holds,
+                               footprints of its unfinished jobs): what admission keeps
+                               within the budget                                        */
 } idp_server_stats;
 
 /* Admission estimate of one job's device memory (arena, matrix, solver and
@@ -310,9 +338,12 @@ double idp_job_footprint(int V, int T);
  * max_batch: jobs per cohort (>= 1). */
 idp_server* idp_server_create(const idp_params* p, double hbm_budget, int workers, int max_batch, int* status);
 
-/* Scheduler only, no device work: a cohort "runs" for ms_per_kvertex per
- * thousand vertices it holds and every job completes with IDP_OK and its
- * input positions. For testing admission and scheduling without a GPU. */
+/* Scheduler only, no device work: a job of V vertices "needs" 2 + V/1000
+ * Newton iterations, an iteration of a worker takes ms_per_kvertex / 10 per
+ * thousand vertices of its unfinished jobs, a worker's context "holds" the
+ * largest sum of footprints its arena had (grow-only, as real contexts), and
+ * every job completes with IDP_OK and its input positions. For testing
+ * admission and scheduling without a GPU. */
 idp_server* idp_server_create_simulated(double hbm_budget, int workers, int max_batch, double ms_per_kvertex,
                                         int* status);
 

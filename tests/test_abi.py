@@ -58,3 +58,18 @@ def test_reference_shaped_shim_rejects_unsupported_inputs(gpu_lib):
     args[0] = np.zeros((3, 3))  # shell elements are not part of this path
     with pytest.raises(NotImplementedError):
         FEM.DiscreteShell.Advance_One_Step_IE_Hinge(*args)
+
+
+def test_reference_shaped_shim_rejects_moving_dbc(gpu_lib):
+    """A DBC target away from the vertex's position is a moving DBC (the
+    reference's augmented Lagrangian), which this path does not solve: the
+    shim says so instead of fixing the vertex where it is."""
+    import numpy as np
+    import pytest
+    from idp_gb300.api import _dbc_indices
+
+    X = np.arange(12, dtype=float).reshape(4, 3)
+    assert list(_dbc_indices(np.array([[1, 3.0, 4.0, 5.0]]), X)) == [1]
+    with pytest.raises(NotImplementedError):
+        _dbc_indices(np.array([[1, 3.0, 4.0, 5.5]]), X)
+    assert _dbc_indices(None, X) is None

@@ -115,3 +115,84 @@ def test_reset_context_matches_fresh(gpu_lib):
             assert res[i]["energy"] == r0["energy"] and np.array_equal(X, X0), (sel, k)
         ctx.reset()
     ctx.close()
+
+
+def test_bounded_steps_match_advance(gpu_lib):
+    """idp_step_begin + idp_step_iterate in chunks of 3 Newton iterations gives
+    idp_advance's results bit for bit, batch and all."""
+    import idp_gb300 as idp
+
+    pool = job_pool()
+    sel = [1, 4, 2]
+
+    def ctx_for():
+        ctx = idp.Context(h=0.1, mode=idp.MODE_MIXED, max_newton=40)
+        for i, k in enumerate(sel):
+            j = pool[k]
+            pr = j["pr"]
+            ctx.add_instance(j["X"], j["tets"], pr["mass"], pr["lam"], pr["mu"], pr["dHat2"], pr["kappa"],
+                             pr["kappa_max"])
+            if j["v"] is not None:
+                ctx.set_velocity(i, j["v"])
+        ctx.commit()
+        for i, k in enumerate(sel):
+            if pool[k]["flow"]:
+                ctx.set_normal_flow(i, pool[k]["flow"])
+        return ctx
+
+    a = ctx_for()
+    _, ra = a.advance(check=False)
+    b = ctx_for()
+    b.step_begin()
+    chunks, left = 0, 1
+    while left:
+        _, left, rb = b.step_iterate(3)
+        chunks += 1
+    assert chunks > 2
+    for i in range(len(sel)):
+        assert ra[i]["newton_iters"] == rb[i]["newton_iters"] and ra[i]["energy"] == rb[i]["energy"]
+        Xa, va, ka = a.state(i)
+        Xb, vb, kb = b.state(i)
+        assert np.array_equal(Xa, Xb) and np.array_equal(va, vb) and np.array_equal(ka, kb)
+    a.close()
+    b.close()
+
+
+def test_job_joins_a_running_arena(gpu_lib):
+    """One worker: a short flow job submitted while a long bar solve is
+    iterating joins that worker's arena between Newton iterations, is released
+    when it converges (well before the bar), and both results equal the
+    results of solving each job alone."""
+    import time
+
+    import idp_gb300 as idp
+
+    pool = job_pool()
+    max_newton = 120
+    bar, blob = pool[1], pool[5]
+    alone_bar = solve_alone(idp, bar, max_newton)
+    alone_blob = solve_alone(idp, blob, max_newton)
+    assert alone_bar[0]["newton_iters"] > 3 * alone_blob[0]["newton_iters"]
+    srv = idp.Server(hbm_budget=8e9, workers=1, max_batch=4, h=0.1, mode=idp.MODE_MIXED, max_newton=max_newton)
+    pr = bar["pr"]
+    jb = srv.submit(bar["X"], bar["tets"], pr["mass"], pr["lam"], pr["mu"], pr["dHat2"], pr["kappa"],
+                    pr["kappa_max"], v=bar["v"])
+    t0 = time.time()
+    while srv.stats()["cohorts"] < 1 and time.time() - t0 < 30:
+        time.sleep(0.005)
+    time.sleep(0.2)
+    pr = blob["pr"]
+    jf = srv.submit(blob["X"], blob["tets"], pr["mass"], pr["lam"], pr["mu"], pr["dHat2"], pr["kappa"],
+                    pr["kappa_max"], normal_flow=blob["flow"])
+    info_f, Xf, vf = srv.wait(jf)
+    info_b, Xb, vb = srv.wait(jb)
+    assert info_b["admit_ms"] < info_f["admit_ms"] < info_b["done_ms"]
+    assert info_f["cohort_size"] == 2  # admitted into the bar's running arena
+    assert info_f["done_ms"] < info_b["done_ms"]
+    for info, X, v, alone in ((info_b, Xb, vb, alone_bar), (info_f, Xf, vf, alone_blob)):
+        r0, X0, v0, _ = alone
+        assert info["status"] == r0["status"]
+        assert info["result"]["newton_iters"] == r0["newton_iters"]
+        assert info["result"]["energy"] == r0["energy"]
+        assert np.array_equal(X, X0) and np.array_equal(v, v0)
+    srv.close()
