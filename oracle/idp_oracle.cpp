@@ -23,6 +23,7 @@
 #include <algorithm>
 #include "geom.hpp"
 #include "deriv.hpp"
+#include "shell.hpp"
 
 using namespace ora;
 
@@ -1122,6 +1123,116 @@ void ora_dist_derivs(int kind, const double* x, double* d, double* g, double* H)
     }
 }
 void ora_make_pd(int n, double* A) { make_pd(n, A); }
+
+// ---------------------------------------------------------------------------
+// Discrete-shell elasticity of the Hinge path (oracle/shell.hpp)
+// ---------------------------------------------------------------------------
+
+// rest data of every face: inverse of the rest first fundamental form, its
+// determinant, vol = area * thickness, lambda = E nu / (1 - nu^2),
+// mu = E / (2 (1 + nu)) (DISCRETE_SHELL.h:132-170, 328-342); 7 doubles per face
+void ora_membrane_rest(int F, const int* faces, const double* X0, double thickness, double E, double nu,
+                       double* mem) {
+    const double lam = E * nu / (1.0 - nu * nu), mu = E / (2.0 * (1.0 + nu));
+    for (int f = 0; f < F; ++f) {
+        const V3 x1 = v3(X0 + 3 * faces[3 * f]), x2 = v3(X0 + 3 * faces[3 * f + 1]), x3 = v3(X0 + 3 * faces[3 * f + 2]);
+        const V3 e01 = x2 - x1, e02 = x3 - x1;
+        const double a00 = sq(e01), a01 = dot(e01, e02), a11 = sq(e02);
+        const double det = a00 * a11 - a01 * a01;
+        double* m = mem + 7 * f;
+        m[0] = a11 / det;
+        m[1] = -a01 / det;
+        m[2] = a00 / det;
+        m[3] = m[0] * m[2] - m[1] * m[1];
+        m[4] = std::sqrt(sq(cross(e01, e02))) / 2 * thickness;
+        m[5] = lam;
+        m[6] = mu;
+    }
+}
+
+static MemFace mem_at(const double* m) { return MemFace{m[0], m[1], m[2], m[3], m[4], m[5], m[6]}; }
+
+// membrane energy of every face (summed in face order); gradient added into
+// g (3V, may be null); element Hessians H (F x 81, may be null), projected
+// to PSD when project (MEMBRANE.h:125-322)
+double ora_membrane(int F, const int* faces, const double* X, const double* mem, double w, double* g, double* H,
+                    int project) {
+    double E = 0;
+    for (int f = 0; f < F; ++f) {
+        const int* t = faces + 3 * f;
+        double ge[9];
+        E += membrane_face(v3(X + 3 * t[0]), v3(X + 3 * t[1]), v3(X + 3 * t[2]), mem_at(mem + 7 * f), w,
+                           g ? ge : nullptr, H ? H + 81L * f : nullptr);
+        if (g)
+            for (int a = 0; a < 3; ++a)
+                for (int d = 0; d < 3; ++d) g[3 * t[a] + d] += ge[3 * a + d];
+        if (H && project) make_pd(9, H + 81L * f);
+    }
+    return E;
+}
+
+// hinge stencils (x0, x1, x2, x3) of the surface edges in their order and
+// (thetabar, ebar, hbar) at X0 (DISCRETE_SHELL.h:172-212): for edge (a, b),
+// x0 follows b in the face holding the directed edge a->b, x1 = a, x2 = b,
+// x3 follows a in the face holding b->a; boundary edges have no hinge.
+int ora_shell_hinges(int V, int F, const int* faces, const double* X0, int nE, const int* edges, int* hinges,
+                     double* info) {
+    (void)V;
+    std::map<std::pair<int, int>, int> e2t;
+    for (int f = 0; f < F; ++f)
+        for (int k = 0; k < 3; ++k) e2t[{faces[3 * f + k], faces[3 * f + (k + 1) % 3]}] = f;
+    int n = 0;
+    for (int e = 0; e < nE; ++e) {
+        const int a = edges[2 * e], b = edges[2 * e + 1];
+        auto it = e2t.find({a, b});
+        if (it == e2t.end()) continue;
+        const int* t = faces + 3 * it->second;
+        int v0 = -1;
+        for (int j = 0; j < 3; ++j)
+            if (t[j] == b) v0 = t[(j + 1) % 3];
+        auto jt = e2t.find({b, a});
+        if (jt == e2t.end()) continue;
+        const int* o = faces + 3 * jt->second;
+        int v3i = 0;
+        for (int j = 0; j < 3; ++j)
+            if (o[j] == a) v3i = o[(j + 1) % 3];
+        int* hh = hinges + 4 * n;
+        hh[0] = v0; hh[1] = a; hh[2] = b; hh[3] = v3i;
+        const V3 X0_ = v3(X0 + 3 * v0), X1 = v3(X0 + 3 * a), X2 = v3(X0 + 3 * b), X3 = v3(X0 + 3 * v3i);
+        double* in = info + 3 * n;
+        in[0] = dihedral_angle(X0_, X1, X2, X3);
+        in[1] = std::sqrt(sq(X1 - X2));
+        const V3 n1 = cross(X1 - X0_, X2 - X0_), n2 = cross(X2 - X3, X1 - X3);
+        in[2] = (std::sqrt(sq(n1)) + std::sqrt(sq(n2))) / (in[1] * 6);
+        ++n;
+    }
+    return n;
+}
+
+// bending energy of every hinge (hinge order); gradient into g (may be null);
+// element Hessians H (Hn x 144, may be null), projected when project
+double ora_bending(int Hn, const int* hinges, const double* info, double k, const double* X, double w, double* g,
+                   double* H, int project) {
+    double E = 0;
+    for (int i = 0; i < Hn; ++i) {
+        const int* hh = hinges + 4 * i;
+        const double* in = info + 3 * i;
+        double ge[12];
+        E += bending_hinge(v3(X + 3 * hh[0]), v3(X + 3 * hh[1]), v3(X + 3 * hh[2]), v3(X + 3 * hh[3]), in[0], in[1],
+                           in[2], k, w, g ? ge : nullptr, H ? H + 144L * i : nullptr);
+        if (g)
+            for (int a = 0; a < 4; ++a)
+                for (int d = 0; d < 3; ++d) g[3 * hh[a] + d] += ge[3 * a + d];
+        if (H && project) make_pd(12, H + 144L * i);
+    }
+    return E;
+}
+
+double ora_dihedral(const double* x, double* g, double* H) {
+    const V3 a = v3(x), b = v3(x + 3), c = v3(x + 6), d = v3(x + 9);
+    dihedral_derivs(a, b, c, d, g, H);
+    return dihedral_angle(a, b, c, d);
+}
 
 // Normal-flow predictor shift (Update_Normal_Flow_Neumann,
 // FEM/Shell/DISCRETE_SHELL.h:359-395): b_v += cross(X2-X1, X3-X1) over the

@@ -39,7 +39,7 @@ _up = C.POINTER(C.c_ubyte)
 def build(force=False):
     """Compile the oracle with its Makefile (g++ -ffp-contract=off)."""
     if force or not os.path.exists(_LIB) or os.path.getmtime(_LIB) < max(
-        os.path.getmtime(os.path.join(_HERE, f)) for f in ("idp_oracle.cpp", "geom.hpp", "deriv.hpp")
+        os.path.getmtime(os.path.join(_HERE, f)) for f in ("idp_oracle.cpp", "geom.hpp", "deriv.hpp", "shell.hpp")
     ):
         subprocess.run(["make", "-s", "-C", _HERE], check=True)
     return _LIB
@@ -67,6 +67,10 @@ def lib():
         L.ora_flow_energy.restype = C.c_double
         L.ora_edge_tri_intersections.restype = C.c_long
         L.ora_edge_tri_intersections.argtypes = [C.c_int, _ip, C.c_int, _ip, _dp, _up, C.c_long, _ip]
+        L.ora_membrane.restype = C.c_double
+        L.ora_bending.restype = C.c_double
+        L.ora_dihedral.restype = C.c_double
+        L.ora_shell_hinges.restype = C.c_int
         _lib = L
     return _lib
 
@@ -234,6 +238,59 @@ def flow_hessian(n_dof, faces, vol, h):
     return sp.coo_matrix((v, (r, c)), shape=(n_dof, n_dof)).tocsr()
 
 
+def membrane_rest(X0, faces, thickness, E, nu):
+    """Per-face rest data of the NH membrane (F, 7): inverse rest first
+    fundamental form (00, 01, 11), its determinant, vol, lambda, mu."""
+    X0, faces = f64(X0), i32(faces)
+    mem = np.zeros((faces.shape[0], 7))
+    lib().ora_membrane_rest(faces.shape[0], _i(faces), _d(X0), C.c_double(thickness), C.c_double(E), C.c_double(nu),
+                            _d(mem))
+    return mem
+
+
+def membrane(X, faces, mem, w, grad=False, hess=False, project=True):
+    """Membrane energy (and gradient 3V, element Hessians F x 9 x 9)."""
+    X, faces = f64(X), i32(faces)
+    g = np.zeros(X.size) if grad else None
+    H = np.zeros((faces.shape[0], 9, 9)) if hess else None
+    E = lib().ora_membrane(faces.shape[0], _i(faces), _d(X), _d(f64(mem)), C.c_double(w),
+                           _d(g) if grad else None, _d(H) if hess else None, int(project))
+    return E, g, H
+
+
+def shell_hinges(X0, faces, edges):
+    """Hinge stencils (Hn, 4) and rest data (thetabar, ebar, hbar) of a shell."""
+    X0, faces, edges = f64(X0), i32(faces), i32(edges)
+    hin = np.zeros((edges.shape[0], 4), np.int32)
+    info = np.zeros((edges.shape[0], 3))
+    n = lib().ora_shell_hinges(X0.shape[0], faces.shape[0], _i(faces), _d(X0), edges.shape[0], _i(edges), _i(hin),
+                               _d(info))
+    return hin[:n].copy(), info[:n].copy()
+
+
+def bending(X, hinges, info, k, w, grad=False, hess=False, project=True):
+    """Hinge bending energy (and gradient 3V, element Hessians Hn x 12 x 12)."""
+    X, hinges = f64(X), i32(hinges)
+    g = np.zeros(X.size) if grad else None
+    H = np.zeros((hinges.shape[0], 12, 12)) if hess else None
+    E = lib().ora_bending(hinges.shape[0], _i(hinges), _d(f64(info)), C.c_double(k), _d(X), C.c_double(w),
+                          _d(g) if grad else None, _d(H) if hess else None, int(project))
+    return E, g, H
+
+
+def dihedral(x):
+    """Dihedral angle of a hinge (4 x 3) with its gradient (12) and Hessian (12 x 12)."""
+    x = f64(x).reshape(-1)
+    g, H = np.zeros(12), np.zeros(144)
+    t = lib().ora_dihedral(_d(x), _d(g), _d(H))
+    return t, g, H.reshape(12, 12)
+
+
+def hinge_stiffness(E, nu, thickness, mult=1.0):
+    """k = E t^3 / (24 (1 - nu^2)) times bendingStiffMult (DISCRETE_SHELL.h:344-349)."""
+    return mult * E * thickness ** 3 / (24.0 * (1.0 - nu * nu))
+
+
 def orient3d(a, b, c, d):
     """Exact sign of det[a-d; b-d; c-d]."""
     return lib().ora_orient3d(_d(f64(a)), _d(f64(b)), _d(f64(c)), _d(f64(d)))
@@ -314,21 +371,29 @@ class Problem:
     b: np.ndarray = None      # (V,3) body force (None: zero)
     faces: np.ndarray = None  # (F,3) shell faces: flow mode (Advance_One_Step_IE_Flow)
     fvol: np.ndarray = None   # (F,) shell element volumes (area * thickness)
+    mem: np.ndarray = None    # (F,7) membrane rest data: an elastic shell (Hinge path) instead of flow mode
+    hinges: np.ndarray = None  # (Hn,4) hinge stencils of an elastic shell
+    hinfo: np.ndarray = None  # (Hn,3) thetabar, ebar, hbar
+    kbend: float = 0.0        # hinge stiffness k
 
     @property
     def flow(self):
-        return self.faces is not None
+        return self.faces is not None and self.mem is None
+
+    @property
+    def elastic_shell(self):
+        return self.faces is not None and self.mem is not None
 
     def __post_init__(self):
         self.X = f64(self.X).copy()
         self.X0 = f64(self.X0)
-        if self.flow:
+        if self.faces is not None:
             self.faces = i32(self.faces)
             self.tets = np.zeros((0, 4), np.int32)
         self.tets = i32(self.tets)
         if self.dbc is None:
             self.dbc = np.zeros(self.X.shape[0], np.uint8)
-        if self.IB is None and not self.flow:
+        if self.IB is None and self.faces is None:
             self.IB, self.vol = tet_rest(self.X0, self.tets)
 
 
@@ -337,6 +402,10 @@ def _energy(pb, X, Xtilde, with_barrier, cons, info):
     h2 = pb.h * pb.h
     if pb.flow:  # INC_POTENTIAL.h:53-73
         E = flow_energy(X, pb.faces, pb.fvol, pb.h)
+    elif pb.elastic_shell:  # INC_POTENTIAL.h: membrane + hinge bending
+        E = membrane(X, pb.faces, pb.mem, h2)[0] + bending(X, pb.hinges, pb.hinfo, pb.kbend, h2)[0]
+        if not np.isfinite(E):
+            return None
     else:
         E = tet_energy(X, pb.tets, pb.IB, pb.vol, pb.lam, pb.mu, h2)
     if E is None:
@@ -353,6 +422,8 @@ def _gradient(pb, X, Xtilde, cons, info):
     h2 = pb.h * pb.h
     if pb.flow:  # INC_POTENTIAL.h:191-211
         g = flow_gradient(X, pb.faces, pb.fvol, pb.h)
+    elif pb.elastic_shell:
+        g = membrane(X, pb.faces, pb.mem, h2, grad=True)[1] + bending(X, pb.hinges, pb.hinfo, pb.kbend, h2, grad=True)[1]
     else:
         g = tet_gradient(X, pb.tets, pb.IB, pb.vol, pb.lam, pb.mu, h2)
     g += (pb.mass[:, None] * (X - Xtilde)).reshape(-1)
@@ -369,6 +440,15 @@ def _hessian(pb, X, cons, info):
     if pb.flow:  # INC_POTENTIAL.h:323-339
         Hf = flow_hessian(n, pb.faces, pb.fvol, pb.h).tocoo()
         R, Cc, Vv = [Hf.row], [Hf.col], [Hf.data]
+    elif pb.elastic_shell:
+        R, Cc, Vv = [], [], []
+        for st, Hs in ((pb.faces, membrane(X, pb.faces, pb.mem, h2, hess=True)[2]),
+                       (pb.hinges, bending(X, pb.hinges, pb.hinfo, pb.kbend, h2, hess=True)[2])):
+            k = 3 * st.shape[1]
+            dofs = (3 * st[:, :, None] + np.arange(3)).reshape(-1, k)
+            R.append(np.repeat(dofs[:, :, None], k, axis=2).reshape(-1))
+            Cc.append(np.repeat(dofs[:, None, :], k, axis=1).reshape(-1))
+            Vv.append(Hs.reshape(-1))
     else:
         He = tet_hessian(X, pb.tets, pb.IB, pb.vol, pb.lam, pb.mu, h2, True)
         dofs = (3 * pb.tets[:, :, None] + np.arange(3)).reshape(-1, 12)
@@ -416,7 +496,7 @@ def advance_one_step(pb: Problem, Xtilde=None, verbose=False, on_iter=None):
         else:                             # x + (h v + h^2 M^-1 b), M lumped
             Xtilde = Xn + (h * pb.v + (h * h) * (f64(pb.b).reshape(-1, 3) / pb.mass[:, None]))
     if pb.surf is None:                   # IMPLICIT_EULER.h:235-241
-        pb.surf = shell_surface(pb.X.shape[0], pb.faces) if pb.flow else surface(pb.X0, pb.tets)
+        pb.surf = shell_surface(pb.X.shape[0], pb.faces) if pb.faces is not None else surface(pb.X0, pb.tets)
     surf, dbc = pb.surf, pb.dbc
     nDBC = int(dbc.sum())
     X = pb.X
