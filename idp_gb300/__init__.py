@@ -40,7 +40,7 @@ EXPORTS = [
     "idp_check_intersection_all", "idp_reset", "idp_device_bytes", "idp_job_footprint", "idp_server_create",
     "idp_server_create_simulated", "idp_server_submit", "idp_server_wait", "idp_server_drain",
     "idp_server_get_stats", "idp_server_destroy", "idp_add_shell_instance", "idp_step_begin", "idp_step_iterate",
-    "idp_set_body_force",
+    "idp_set_body_force", "idp_add_elastic_shell_instance",
 ]
 
 
@@ -138,6 +138,9 @@ def load(path: str | None = None):
     L.idp_step_begin.argtypes = [C.c_void_p]
     L.idp_step_iterate.argtypes = [C.c_void_p, C.c_int, C.POINTER(Result), C.POINTER(C.c_int)]
     L.idp_set_body_force.argtypes = [C.c_void_p, C.c_int, _dp]
+    L.idp_add_elastic_shell_instance.argtypes = [C.c_void_p, C.c_int, _dp, _dp, C.c_int, _ip, _dp, C.c_double,
+                                                 C.c_double, C.c_double, C.c_double, C.c_double, C.c_int, _ip,
+                                                 C.c_double, C.c_double, C.c_double]
     L.idp_get_state.argtypes = [C.c_void_p, C.c_int, _dp, _dp, _dp]
     L.idp_instance_info.argtypes = [C.c_void_p, C.c_int] + [C.POINTER(C.c_int)] * 5
     L.idp_get_surface.argtypes = [C.c_void_p, C.c_int, _ip, _ip, _ip]
@@ -253,6 +256,26 @@ class Context:
                                           float(kappa_max))
         if r < 0:
             raise IDPError(-r, "idp_add_shell_instance")
+        self._V.append(V)
+        return r
+
+    def add_elastic_shell_instance(self, X, faces, density, E, nu, thickness, dHat2, kappa, kappa_max,
+                                   bending_mult=1.0, X0=None, dbc_idx=None, mass=None):
+        """Elastic triangle shell (neo-Hookean membrane + hinge bending);
+        mass (V) overrides the lumped masses from density."""
+        X, faces = _f64(X).reshape(-1, 3), _i32(faces).reshape(-1, 3)
+        V = X.shape[0]
+        X0 = X if X0 is None else _f64(X0).reshape(-1, 3)
+        dbc = _i32(np.zeros(0) if dbc_idx is None else dbc_idx)
+        m = None if mass is None else _f64(mass)
+        if m is not None and m.size != V:
+            raise ValueError("mass: one value per vertex")
+        r = load().idp_add_elastic_shell_instance(self._h, V, _pd(X), _pd(X0), faces.shape[0], _pi(faces),
+                                                  None if m is None else _pd(m), float(density), float(E), float(nu),
+                                                  float(thickness), float(bending_mult), dbc.size, _pi(dbc),
+                                                  float(dHat2), float(kappa), float(kappa_max))
+        if r < 0:
+            raise IDPError(-r, "idp_add_elastic_shell_instance")
         self._V.append(V)
         return r
 

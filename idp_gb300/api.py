@@ -7,6 +7,9 @@ meaning for the arguments this path reads; storages are plain numpy arrays /
 dicts instead of JGSL storages. It mutates ``X`` and ``nodeAttr['v']`` in
 place and returns the Newton iteration count, like the reference.
 
+With shell elements (``Elem``) it advances an elastic triangle shell
+(membrane + hinge bending) instead of a tet mesh.
+
 ``FEM.DiscreteShell.Advance_One_Step_IE_Flow`` does the same for the flow-mode
 export (``DISCRETE_SHELL.h:1113``) over a triangle-shell instance.
 
@@ -24,7 +27,7 @@ import numpy as np
 
 from . import Context, IDPError, IDP_WARN_ITER_CAP, MODE_MIXED, meshgen
 
-_UNSUPPORTED = "not part of the GB300 path (tet meshes, and shells in flow mode, with offset IPC)"
+_UNSUPPORTED = "not part of the GB300 path (tet meshes and triangle shells with offset IPC)"
 
 
 def _empty(x):
@@ -102,6 +105,59 @@ def _context_for(tet, X, nodeAttr, tetEl, dHat2, kappaVec, DBC, h, NewtonTol, th
     return ctx
 
 
+def shell_material(Elem, nodeAttr, elemAttr, elasticityAttr, bendingStiffMult):
+    """The elastic-shell material behind the storages Initialize_Discrete_Shell
+    fills (FEM/Shell/DISCRETE_SHELL.h:218-357): thickness = vol / area of the
+    first face, nu = lambda / (lambda + 2 mu) and E = 2 mu (1 + nu) from
+    lambda = E nu / (1 - nu^2), mu = E / (2 (1 + nu)), the bending multiplier
+    that gives the hinge stiffness k = bendingStiffMult * elemAttr P[0](0, 0)
+    (BENDING.h:54) from E thickness^3 / (24 (1 - nu^2)), and the lumped masses
+    (nodeAttr m). Raises ValueError where the faces do not share one material."""
+    F = np.asarray(Elem, dtype=np.int32).reshape(-1, 3)
+    X0 = np.asarray(nodeAttr["x0"], dtype=np.float64).reshape(-1, 3)
+    vol = np.asarray(elasticityAttr["vol"], dtype=np.float64).reshape(-1)
+    lam = np.asarray(elasticityAttr["lambda"], dtype=np.float64).reshape(-1)
+    mu = np.asarray(elasticityAttr["mu"], dtype=np.float64).reshape(-1)
+    if not (vol.size == lam.size == mu.size == F.shape[0]) or F.shape[0] == 0:
+        raise ValueError("elasticityAttr: one (vol, lambda, mu) per shell element")
+    if np.any(lam != lam[0]) or np.any(mu != mu[0]):
+        raise NotImplementedError(f"per-element shell materials: {_UNSUPPORTED}")
+    area = np.linalg.norm(np.cross(X0[F[:, 1]] - X0[F[:, 0]], X0[F[:, 2]] - X0[F[:, 0]]), axis=1) / 2
+    t = float(vol[0] / area[0])
+    if not np.allclose(vol, area * t, rtol=1e-12, atol=0):
+        raise NotImplementedError(f"per-element shell thickness: {_UNSUPPORTED}")
+    nu = float(lam[0] / (lam[0] + 2 * mu[0]))
+    E = float(2 * mu[0] * (1 + nu))
+    P = np.asarray(elemAttr["P"], dtype=np.float64)
+    k = float(P.reshape(-1)[0]) if P.size else 0.0
+    kd = E * t ** 3 / (24.0 * (1.0 - nu * nu))
+    m = np.asarray(nodeAttr["m"], dtype=np.float64).reshape(-1)
+    return dict(E=E, nu=nu, thickness=t, bending_mult=float(bendingStiffMult) * k / kd,
+                density=float(np.sum(m) / np.sum(vol)), mass=m)
+
+
+def _shell_context_for(Elem, X, nodeAttr, elemAttr, elasticityAttr, bendingStiffMult, dHat2, kappaVec, DBC, h,
+                       NewtonTol, thickness, mode):
+    dbc_idx = _dbc_indices(DBC, X)
+    P = np.asarray(elemAttr["P"], dtype=np.float64)
+    key = ("shell", _digest(np.asarray(Elem, dtype=np.int32), nodeAttr["x0"], nodeAttr["m"], elasticityAttr["vol"],
+                            elasticityAttr["lambda"], elasticityAttr["mu"], P.reshape(-1)[:1],
+                            np.zeros(0, np.int32) if dbc_idx is None else dbc_idx),
+           float(bendingStiffMult), X.shape, float(dHat2), float(h), float(NewtonTol), float(thickness), mode)
+    if _Cache.key == key and _Cache.ctx is not None:
+        return _Cache.ctx
+    if _Cache.ctx is not None:
+        _Cache.ctx.close()
+    mat = shell_material(Elem, nodeAttr, elemAttr, elasticityAttr, bendingStiffMult)
+    ctx = Context(h=h, newton_tol=NewtonTol, thickness=thickness, mode=mode)
+    ctx.add_elastic_shell_instance(X, Elem, mat["density"], mat["E"], mat["nu"], mat["thickness"], dHat2,
+                                   kappaVec[0], kappaVec[1], bending_mult=mat["bending_mult"], X0=nodeAttr["x0"],
+                                   dbc_idx=dbc_idx, mass=mat["mass"])
+    ctx.commit()
+    _Cache.ctx, _Cache.key = ctx, key
+    return ctx
+
+
 class DiscreteShell:
     mode = MODE_MIXED
 
@@ -112,10 +168,13 @@ class DiscreteShell:
                                   nodeAttr, M, elemAttr, elasticityAttr, tet, tetAttr, tetElasticityAttr, rod,
                                   rodInfo, rodHinge, rodHingeInfo, stitchInfo, stitchRatio, k_stitch, particle,
                                   outputFolder):
-        """One implicit-Euler step; X (V,3) and nodeAttr['v'] are updated in
+        """One implicit-Euler step of a tet mesh (tet, tetElasticityAttr) or
+        of an elastic triangle shell (Elem with elemAttr, elasticityAttr and
+        the rest data of nodeAttr['x0'] that Initialize_Discrete_Shell made;
+        the hinge stencils are rebuilt from it on the device, so edgeStencil
+        and edgeInfo are not read); X (V,3) and nodeAttr['v'] are updated in
         place, kappaVec[0] receives the adapted kappa. Returns Newton iterations."""
-        for name, v in (("Elem", Elem), ("segs", segs), ("rod", rod), ("stitchInfo", stitchInfo),
-                        ("particle", particle)):
+        for name, v in (("segs", segs), ("rod", rod), ("stitchInfo", stitchInfo), ("particle", particle)):
             if not _empty(v):
                 raise NotImplementedError(f"{name}: {_UNSUPPORTED}")
         if mu and mu > 0:
@@ -124,9 +183,16 @@ class DiscreteShell:
             raise NotImplementedError(f"staticSolve: {_UNSUPPORTED}")
         if not withCollision:
             raise NotImplementedError("withCollision=False: the GB300 path always has IPC contact")
-        tet = np.asarray(tet)
-        ctx = _context_for(tet, X, nodeAttr, tetElasticityAttr, dHat2, kappaVec, DBC, h, NewtonTol, thickness,
-                           DiscreteShell.mode)
+        if not _empty(Elem) and not _empty(tet):
+            raise NotImplementedError(f"shells and tets in one call: {_UNSUPPORTED}")
+        if not _empty(Elem):
+            if _empty(elemAttr) or _empty(elasticityAttr):
+                raise ValueError("shell elements need elemAttr and elasticityAttr (Initialize_Discrete_Shell)")
+            ctx = _shell_context_for(Elem, X, nodeAttr, elemAttr, elasticityAttr, bendingStiffMult, dHat2, kappaVec,
+                                     DBC, h, NewtonTol, thickness, DiscreteShell.mode)
+        else:
+            ctx = _context_for(np.asarray(tet), X, nodeAttr, tetElasticityAttr, dHat2, kappaVec, DBC, h, NewtonTol,
+                               thickness, DiscreteShell.mode)
         # per call, as the reference reads them: positions, velocity, the
         # kappa pair (a driver may reset it, e.g. initialize_OIPC) and the
         # body force of the predictor (IMPLICIT_EULER.h:195-216)
@@ -275,12 +341,13 @@ class TetIPCSim:
 
 
 class ShellFlowSim:
-    """The triangle-shell flow-mode slice of FEMDiscreteShellBase that the
-    normal-flow scripts drive (Projects/FEMShell/12-14_normal_flow.py):
-    add_shell_3D, initialize, initialize_OIPC, the frame loop of
-    SimulationBase (Python/Drivers/SimulationBase.py:76-103) and
-    advance_one_time_step with Update_Normal_Flow_Neumann
-    (FEMDiscreteShellBase.py:266-276, 332-340)."""
+    """The triangle-shell slice of FEMDiscreteShellBase: what the normal-flow
+    scripts drive (Projects/FEMShell/12-14_normal_flow.py) — add_shell_3D,
+    initialize, initialize_OIPC, the frame loop of SimulationBase
+    (Python/Drivers/SimulationBase.py:76-103) and advance_one_time_step with
+    Update_Normal_Flow_Neumann (FEMDiscreteShellBase.py:266-276, 332-340) —
+    and, with flow off, the elastic shell's Hinge step with gravity
+    (FEMDiscreteShellBase.py:300-361)."""
 
     def __init__(self, precision="double", dim=3, mode=MODE_MIXED):
         if dim != 3:
@@ -297,6 +364,8 @@ class ShellFlowSim:
         self.gravity = (0.0, 0.0, 0.0)
         self.bendingStiffMult = 1.0
         self.shell_density = 1000.0
+        self.shell_E = 1e5
+        self.shell_nu = 0.4
         self.shell_thickness = 0.001
         self.dHat2 = 1e-6
         self.kappa = [1e5, 0.0, 0.0]
@@ -322,10 +391,11 @@ class ShellFlowSim:
         return m
 
     def initialize(self, p_density, E, nu, thickness, caseI):
-        """Shell material (Initialize_Shell_Hinge_EIPC's density and
+        """Shell material (Initialize_Shell_Hinge_EIPC's density, E, nu and
         thickness; E and nu do not enter the flow energy); in flow mode the
         open boundary's vertices are fixed (FEM.Boundary_Dirichlet)."""
         self.shell_density, self.shell_thickness = float(p_density), float(thickness)
+        self.shell_E, self.shell_nu = float(E), float(nu)
         self.thickness = float(thickness)
         if self.flow:
             e = np.sort(self.Elem[:, [[0, 1], [1, 2], [2, 0]]].reshape(-1, 2), axis=1)
@@ -344,20 +414,36 @@ class ShellFlowSim:
     def _context(self, h):
         if self._ctx is None or self._ctx_h != h:
             X = self.X.copy()
+            v = None
+            if self._ctx is not None:  # a new step size keeps the elastic shell's rest shape and velocity
+                v = self._ctx.state(0)[1]
+                self._ctx.close()
+            else:
+                self._X0 = X.copy()
             self._ctx = Context(h=h, newton_tol=self.PNTol, thickness=self.thickness, mode=self.mode)
-            self._ctx.add_shell_instance(X, self.Elem, self.shell_density, self.shell_thickness, self.dHat2,
-                                         self.kappa[0], self.kappa[1], dbc_idx=self.DBC)
+            if self.flow:
+                self._ctx.add_shell_instance(X, self.Elem, self.shell_density, self.shell_thickness, self.dHat2,
+                                             self.kappa[0], self.kappa[1], dbc_idx=self.DBC)
+            else:
+                self._ctx.add_elastic_shell_instance(X, self.Elem, self.shell_density, self.shell_E, self.shell_nu,
+                                                     self.shell_thickness, self.dHat2, self.kappa[0], self.kappa[1],
+                                                     bending_mult=self.bendingStiffMult, X0=self._X0,
+                                                     dbc_idx=self.DBC)
+                if v is not None:
+                    self._ctx.set_velocity(0, v)
+                if any(g != 0 for g in self.gravity):  # b = M g (Initialize_Discrete_Shell)
+                    self._ctx.set_body_force(0, self._mass()[:, None] * np.asarray(self.gravity, float)[None, :])
             self._ctx.commit()
             self._ctx_h = h
         return self._ctx
 
     def advance_one_time_step(self, dt):
-        if not self.flow:
-            raise NotImplementedError("shells without flow mode (membrane/bending) are not part of this path")
+        """Advance_One_Step_IE_Flow with the normal-flow predictor in flow
+        mode, Advance_One_Step_IE_Hinge of the elastic shell otherwise."""
         ctx = self._context(dt)
         ctx.set_positions(0, self.X)
         ctx.set_kappa(0, self.kappa)
-        if self.normalFlowMag != 0:
+        if self.flow and self.normalFlowMag != 0:
             ctx.set_normal_flow(0, dt * dt * self.normalFlowMag)
         rc, res = ctx.advance(check=False)
         if rc not in (0, IDP_WARN_ITER_CAP):

@@ -227,6 +227,7 @@ int eval_energy(idp_ctx* c, const double* X, bool with_barrier, std::vector<doub
     c->W.timer.start(PhaseTimer::TET, c->s);
     int rc = tet_energy(A, c->W, X, h2, dsc(c, S_ETET), isc(c, SI_BAD), c->s);
     if (!rc) rc = flow_energy(A, c->W, X, dsc(c, S_ETET), c->s);
+    if (!rc) rc = shell_energy(A, c->W, X, h2, dsc(c, S_ETET), c->s);
     c->W.timer.stop(c->s);
     if (rc) return rc;
     rc = vec_inertia(A, c->W, X, dsc(c, S_EINERT), nullptr, c->s);
@@ -266,6 +267,7 @@ int eval_gradient(idp_ctx* c, const double* X) {
     if (rc) return rc;
     rc = grad_gather_tet(A, c->W, X, A.g, c->s);
     if (!rc) rc = flow_gradient(A, X, A.g, c->s);
+    if (!rc) rc = shell_gradient(A, c->W, X, h2, A.g, c->s);
     if (rc) return rc;
     c->W.timer.start(PhaseTimer::BARRIER, c->s);
     rc = barrier_gradient(A, c->W, X, c->cs, A.g, c->s);
@@ -279,6 +281,7 @@ int eval_hessian(idp_ctx* c, const double* X, bool force_fp64 = false) {
     bool fp64 = force_fp64 || c->P.mode == IDP_MODE_FP64;
     c->W.timer.start(PhaseTimer::TET, c->s);
     int rc = tet_hessian(A, c->W, X, c->P.h * c->P.h, fp64, c->s);
+    if (!rc) rc = shell_hessian(A, c->W, X, c->P.h * c->P.h, fp64, c->s);
     c->W.timer.stop(c->s);
     if (rc) return rc;
     c->W.timer.start(PhaseTimer::BARRIER, c->s);
@@ -452,17 +455,16 @@ int idp_add_instance(idp_ctx* c, int V, const double* X, const double* X0, int T
     return (int)c->inst.size() - 1;
 }
 
-// Triangle shell in flow mode: Initialize_Discrete_Shell's face filter,
-// lumped mass and element volumes (FEM/Shell/DISCRETE_SHELL.h:238-333) and
+// Triangle shell common to flow mode and elastic shells, at its rest
+// positions X: Initialize_Discrete_Shell's face filter, lumped mass and
+// element volumes (FEM/Shell/DISCRETE_SHELL.h:238-333) and
 // Find_Surface_Primitives (Utils/MESHIO.h:728-766) for the contact surface.
-int idp_add_shell_instance(idp_ctx* c, int V, const double* X, int F, const int32_t* faces, double density,
-                           double thickness, int nDBC, const int32_t* dbc_idx, double dHat2, double kappa,
-                           double kappa_max) {
-    if (!c) return -IDP_ERR_INVALID_ARG;
-    if (c->committed) return -IDP_ERR_STATE;
+// Returns 0 or -IDP_*.
+static int build_shell(HostInstance& h, int V, const double* X, int F, const int32_t* faces, double density,
+                       double thickness, int nDBC, const int32_t* dbc_idx, double dHat2, double kappa,
+                       double kappa_max) {
     if (V <= 0 || F <= 0 || !X || !faces || !(density > 0) || !(thickness > 0) || !(dHat2 > 0))
         return -IDP_ERR_INVALID_ARG;
-    HostInstance h;
     h.shell = true;
     h.V = V;
     h.T = 0;
@@ -528,6 +530,132 @@ int idp_add_shell_instance(idp_ctx* c, int V, const double* X, int F, const int3
         sl += std::sqrt((a[0] - b[0]) * (a[0] - b[0]) + (a[1] - b[1]) * (a[1] - b[1]) + (a[2] - b[2]) * (a[2] - b[2]));
     }
     h.rest_mean_edge = h.edges.empty() ? 1.0 : sl / (h.edges.size() / 2);
+    return 0;
+}
+
+// Triangle shell in flow mode (Advance_One_Step_IE_Flow).
+int idp_add_shell_instance(idp_ctx* c, int V, const double* X, int F, const int32_t* faces, double density,
+                           double thickness, int nDBC, const int32_t* dbc_idx, double dHat2, double kappa,
+                           double kappa_max) {
+    if (!c) return -IDP_ERR_INVALID_ARG;
+    if (c->committed) return -IDP_ERR_STATE;
+    HostInstance h;
+    int r = build_shell(h, V, X, F, faces, density, thickness, nDBC, dbc_idx, dHat2, kappa, kappa_max);
+    if (r) return r;
+    c->inst.push_back(std::move(h));
+    return (int)c->inst.size() - 1;
+}
+
+// Dihedral angle of the hinge (x0, x1, x2, x3) with hinge edge x1-x2
+// (Math/DIHEDRAL_ANGLE.h:10-24).
+static double dihedral_host(const double* x0, const double* x1, const double* x2, const double* x3) {
+    double a[3], b[3], c3[3], d[3];
+    for (int k = 0; k < 3; ++k) {
+        a[k] = x1[k] - x0[k];
+        b[k] = x2[k] - x0[k];
+        c3[k] = x2[k] - x3[k];
+        d[k] = x1[k] - x3[k];
+    }
+    const double n1[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]};
+    const double n2[3] = {c3[1] * d[2] - c3[2] * d[1], c3[2] * d[0] - c3[0] * d[2], c3[0] * d[1] - c3[1] * d[0]};
+    const double n11 = n1[0] * n1[0] + n1[1] * n1[1] + n1[2] * n1[2];
+    const double n22 = n2[0] * n2[0] + n2[1] * n2[1] + n2[2] * n2[2];
+    double cth = (n1[0] * n2[0] + n1[1] * n2[1] + n1[2] * n2[2]) / std::sqrt(n11 * n22);
+    cth = std::max(-1.0, std::min(1.0, cth));
+    double t = std::acos(cth);
+    const double m[3] = {n2[1] * n1[2] - n2[2] * n1[1], n2[2] * n1[0] - n2[0] * n1[2], n2[0] * n1[1] - n2[1] * n1[0]};
+    if (m[0] * (x1[0] - x2[0]) + m[1] * (x1[1] - x2[1]) + m[2] * (x1[2] - x2[2]) < 0) t = -t;
+    return t;
+}
+
+// Elastic triangle shell of the Hinge path: neo-Hookean membrane per face and
+// hinge bending per interior edge, with the rest data of
+// Compute_Discrete_Shell_Inv_Basis and the stiffness of
+// Initialize_Discrete_Shell (DISCRETE_SHELL.h:132-216,218-357).
+int idp_add_elastic_shell_instance(idp_ctx* c, int V, const double* X, const double* X0, int F,
+                                   const int32_t* faces, const double* mass, double density, double E, double nu,
+                                   double thickness, double bending_mult, int nDBC, const int32_t* dbc_idx,
+                                   double dHat2, double kappa, double kappa_max) {
+    if (!c) return -IDP_ERR_INVALID_ARG;
+    if (c->committed) return -IDP_ERR_STATE;
+    if (!(E > 0) || !(nu > -1.0 && nu < 0.5) || !(bending_mult >= 0)) return -IDP_ERR_INVALID_ARG;
+    if (!X0) X0 = X;
+    HostInstance h;
+    int r = build_shell(h, V, X0, F, faces, density, thickness, nDBC, dbc_idx, dHat2, kappa, kappa_max);
+    if (r) return r;
+    if (!X) return -IDP_ERR_INVALID_ARG;
+    if (mass) {
+        for (int v = 0; v < V; ++v)
+            if (!(mass[v] > 0)) return -IDP_ERR_INVALID_ARG;
+        h.mass.assign(mass, mass + V);
+    }
+    h.X.assign(X, X + 3 * (long)V);
+    h.elastic = true;
+    h.fvol.clear();  // no flow energy
+    const double lam = E * nu / (1.0 - nu * nu), mu = E / (2.0 * (1.0 + nu));
+    const size_t nf = h.faces.size() / 3;
+    for (size_t f = 0; f < nf; ++f) {
+        const double* x1 = &h.X0[3 * h.faces[3 * f]];
+        const double* x2 = &h.X0[3 * h.faces[3 * f + 1]];
+        const double* x3 = &h.X0[3 * h.faces[3 * f + 2]];
+        double e1[3], e2[3];
+        for (int d = 0; d < 3; ++d) {
+            e1[d] = x2[d] - x1[d];
+            e2[d] = x3[d] - x1[d];
+        }
+        const double a00 = e1[0] * e1[0] + e1[1] * e1[1] + e1[2] * e1[2];
+        const double a01 = e1[0] * e2[0] + e1[1] * e2[1] + e1[2] * e2[2];
+        const double a11 = e2[0] * e2[0] + e2[1] * e2[1] + e2[2] * e2[2];
+        const double det = a00 * a11 - a01 * a01;
+        const double n[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
+        const double i00 = a11 / det, i01 = -a01 / det, i11 = a00 / det;
+        const double vals[7] = {i00, i01, i11, i00 * i11 - i01 * i01,
+                                std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]) / 2 * thickness, lam, mu};
+        h.mem.insert(h.mem.end(), vals, vals + 7);
+    }
+    // hinges of the surface edges in their order: x0 follows x2 in the face
+    // holding the directed edge x1->x2, x3 follows x1 in the face holding
+    // x2->x1 (DISCRETE_SHELL.h:172-212); boundary edges have none
+    std::map<std::pair<int, int>, int> e2t;
+    for (size_t f = 0; f < nf; ++f)
+        for (int k = 0; k < 3; ++k) e2t[{h.faces[3 * f + k], h.faces[3 * f + (k + 1) % 3]}] = (int)f;
+    const double kb = bending_mult * E * thickness * thickness * thickness / (24.0 * (1.0 - nu * nu));
+    for (size_t e = 0; e + 1 < h.edges.size(); e += 2) {
+        const int a = h.edges[e], b = h.edges[e + 1];
+        auto it = e2t.find({a, b});
+        if (it == e2t.end()) continue;
+        auto jt = e2t.find({b, a});
+        if (jt == e2t.end()) continue;
+        const int* t = &h.faces[3 * it->second];
+        const int* o = &h.faces[3 * jt->second];
+        int v0 = -1, v3 = -1;
+        for (int j = 0; j < 3; ++j) {
+            if (t[j] == b) v0 = t[(j + 1) % 3];
+            if (o[j] == a) v3 = o[(j + 1) % 3];
+        }
+        const double* P0 = &h.X0[3 * v0];
+        const double* P1 = &h.X0[3 * a];
+        const double* P2 = &h.X0[3 * b];
+        const double* P3 = &h.X0[3 * v3];
+        const double thb = dihedral_host(P0, P1, P2, P3);
+        double d12[3], a1[3], b1[3], c1[3], dd[3];
+        for (int d = 0; d < 3; ++d) {
+            d12[d] = P1[d] - P2[d];
+            a1[d] = P1[d] - P0[d];
+            b1[d] = P2[d] - P0[d];
+            c1[d] = P2[d] - P3[d];
+            dd[d] = P1[d] - P3[d];
+        }
+        const double ebar = std::sqrt(d12[0] * d12[0] + d12[1] * d12[1] + d12[2] * d12[2]);
+        const double n1[3] = {a1[1] * b1[2] - a1[2] * b1[1], a1[2] * b1[0] - a1[0] * b1[2], a1[0] * b1[1] - a1[1] * b1[0]};
+        const double n2[3] = {c1[1] * dd[2] - c1[2] * dd[1], c1[2] * dd[0] - c1[0] * dd[2], c1[0] * dd[1] - c1[1] * dd[0]};
+        const double hbar = (std::sqrt(n1[0] * n1[0] + n1[1] * n1[1] + n1[2] * n1[2]) +
+                             std::sqrt(n2[0] * n2[0] + n2[1] * n2[1] + n2[2] * n2[2])) / (ebar * 6);
+        const int st[4] = {v0, a, b, v3};
+        h.hinges.insert(h.hinges.end(), st, st + 4);
+        h.hk.push_back(thb);
+        h.hk.push_back(kb * ebar / hbar);
+    }
     c->inst.push_back(std::move(h));
     return (int)c->inst.size() - 1;
 }
@@ -614,6 +742,8 @@ int idp_commit(idp_ctx* c) {
     A.v_off.assign(nI + 1, 0);
     A.t_off.assign(nI + 1, 0);
     A.f_off.assign(nI + 1, 0);
+    A.fm_off.assign(nI + 1, 0);
+    A.hn_off.assign(nI + 1, 0);
     A.sn_off.assign(nI + 1, 0);
     A.se_off.assign(nI + 1, 0);
     A.st_off.assign(nI + 1, 0);
@@ -622,6 +752,8 @@ int idp_commit(idp_ctx* c) {
         A.v_off[i + 1] = A.v_off[i] + h.V;
         A.t_off[i + 1] = A.t_off[i] + h.T;
         A.f_off[i + 1] = A.f_off[i] + (int)h.fvol.size();
+        A.fm_off[i + 1] = A.fm_off[i] + (int)(h.mem.size() / 7);
+        A.hn_off[i + 1] = A.hn_off[i] + (int)(h.hinges.size() / 4);
         A.sn_off[i + 1] = A.sn_off[i] + (int)h.nodes.size();
         A.se_off[i + 1] = A.se_off[i] + (int)h.edges.size() / 2;
         A.st_off[i + 1] = A.st_off[i] + (int)h.tris.size() / 3;
@@ -632,12 +764,15 @@ int idp_commit(idp_ctx* c) {
     A.Se = A.se_off[nI];
     A.St = A.st_off[nI];
     A.F = A.f_off[nI];
+    A.Fm = A.fm_off[nI];
+    A.Hn = A.hn_off[nI];
     A.h = c->P.h;
     std::vector<double> X, X0, mass, vol, lam, mu, IB, vel, dHat2, kappa, thick, cell;
     std::vector<unsigned char> dbc;
     std::vector<int> vinst, snode, sedge, stri, sn_inst, se_inst, st_inst, v2s(A.V, -1), face;
-    std::vector<double> fvol;
-    std::vector<int4> tet;
+    std::vector<double> fvol, mem, hk;
+    std::vector<int> mface, finst, hinst;
+    std::vector<int4> tet, hinge;
     for (int i = 0; i < nI; ++i) {
         const HostInstance& h = c->inst[i];
         int vo = A.v_off[i];
@@ -665,8 +800,20 @@ int idp_commit(idp_ctx* c) {
             for (int r = 0; r < 3; ++r)
                 for (int q = 0; q < 3; ++q) IB.push_back(Cf[q * 3 + r] / J);
         }
-        for (int v : h.faces) face.push_back(v + vo);
-        fvol.insert(fvol.end(), h.fvol.begin(), h.fvol.end());
+        if (h.flow()) {
+            for (int v : h.faces) face.push_back(v + vo);
+            fvol.insert(fvol.end(), h.fvol.begin(), h.fvol.end());
+        }
+        if (h.elastic) {
+            for (int v : h.faces) mface.push_back(v + vo);
+            mem.insert(mem.end(), h.mem.begin(), h.mem.end());
+            finst.insert(finst.end(), h.mem.size() / 7, i);
+            for (size_t k = 0; k < h.hinges.size(); k += 4)
+                hinge.push_back(make_int4(h.hinges[k] + vo, h.hinges[k + 1] + vo, h.hinges[k + 2] + vo,
+                                          h.hinges[k + 3] + vo));
+            hk.insert(hk.end(), h.hk.begin(), h.hk.end());
+            hinst.insert(hinst.end(), h.hinges.size() / 4, i);
+        }
         for (size_t k = 0; k < h.nodes.size(); ++k) {
             v2s[h.nodes[k] + vo] = (int)snode.size();
             snode.push_back(h.nodes[k] + vo);
@@ -751,6 +898,40 @@ int idp_commit(idp_ctx* c) {
         rc |= upload(c, A.vert_face_ptr, vfp);
         rc |= upload(c, A.vert_face, vf);
     }
+    // elastic shells: membrane faces, hinges, chunks, vertex -> element
+    // gradient slots (faces ascending, then hinges ascending)
+    {
+        std::vector<Chunk> mch, hch;
+        std::vector<int> mco, hco;
+        build_chunks(A.fm_off, mch, mco);
+        build_chunks(A.hn_off, hch, hco);
+        A.n_mface_chunks = (int)mch.size();
+        A.n_hinge_chunks = (int)hch.size();
+        rc |= upload(c, A.mface, mface);
+        rc |= upload(c, A.mem, mem);
+        rc |= upload(c, A.finst, finst);
+        rc |= upload(c, A.mface_chunks, mch);
+        rc |= upload(c, A.mface_chunk_off, mco);
+        rc |= upload(c, A.hinge, hinge);
+        rc |= upload(c, A.hk, hk);
+        rc |= upload(c, A.hinst, hinst);
+        rc |= upload(c, A.hinge_chunks, hch);
+        rc |= upload(c, A.hinge_chunk_off, hco);
+        std::vector<int> vsp(A.V + 1, 0);
+        for (int v : mface) vsp[v + 1]++;
+        for (const int4& q : hinge) {
+            vsp[q.x + 1]++; vsp[q.y + 1]++; vsp[q.z + 1]++; vsp[q.w + 1]++;
+        }
+        for (long v = 0; v < A.V; ++v) vsp[v + 1] += vsp[v];
+        std::vector<int> vs(vsp[A.V]), fill(vsp.begin(), vsp.end() - 1);
+        for (size_t k = 0; k < mface.size(); ++k) vs[fill[mface[k]]++] = (int)k;  // face * 3 + corner
+        for (size_t k = 0; k < hinge.size(); ++k) {
+            const int v[4] = {hinge[k].x, hinge[k].y, hinge[k].z, hinge[k].w};
+            for (int a = 0; a < 4; ++a) vs[fill[v[a]]++] = (int)(mface.size() + 4 * k + a);
+        }
+        rc |= upload(c, A.vshell_ptr, vsp);
+        rc |= upload(c, A.vshell, vs);
+    }
     // BSR pattern of the tet stencil + contributor lists (fixed order)
     {
         std::vector<std::pair<long, int>> keys;  // (row*V + col, code)
@@ -770,6 +951,24 @@ int idp_commit(idp_ctx* c) {
             for (int a = 0; a < 3; ++a)
                 for (int b = 0; b < 3; ++b)
                     keys.push_back({(long)face[3 * f + a] * A.V + face[3 * f + b], -(int)(2 * f + (a == b ? 1 : 0)) - 1});
+        // elastic-shell element blocks, stored after the tets' 10 per tet:
+        // 6 per membrane face, 10 per hinge (upper blocks, a <= b)
+        for (long f = 0; f < A.Fm; ++f)
+            for (int a = 0; a < 3; ++a)
+                for (int b = 0; b < 3; ++b) {
+                    const int lo = std::min(a, b), hi = std::max(a, b);
+                    const long k = 10 * A.T + 6 * f + lo * 3 - lo * (lo - 1) / 2 + (hi - lo);
+                    keys.push_back({(long)mface[3 * f + a] * A.V + mface[3 * f + b], (int)(k * 2 + (a > b ? 1 : 0))});
+                }
+        for (long q = 0; q < A.Hn; ++q) {
+            const int v[4] = {hinge[q].x, hinge[q].y, hinge[q].z, hinge[q].w};
+            for (int a = 0; a < 4; ++a)
+                for (int b = 0; b < 4; ++b) {
+                    const int lo = std::min(a, b), hi = std::max(a, b);
+                    const long k = 10 * A.T + 6 * A.Fm + 10 * q + lo * 4 - lo * (lo - 1) / 2 + (hi - lo);
+                    keys.push_back({(long)v[a] * A.V + v[b], (int)(k * 2 + (a > b ? 1 : 0))});
+                }
+        }
         std::stable_sort(keys.begin(), keys.end(),
                          [](const std::pair<long, int>& x, const std::pair<long, int>& y) { return x.first < y.first; });
         std::vector<int> rowptr(A.V + 1, 0), colidx, brow, src_ptr, src, diag(A.V, -1);
@@ -942,7 +1141,7 @@ int step_begin(idp_ctx* c, const std::vector<unsigned char>& which) {
     for (int i = 0; i < nI; ++i) {
         if (!which[i]) continue;
         HostInstance& hi0 = c->inst[i];
-        if (hi0.shell && !hi0.vel_set)
+        if (hi0.flow() && !hi0.vel_set)
             IDP_CUDA_TRY(cudaMemsetAsync(c->vel.as<double>() + 3L * A.v_off[i], 0, sizeof(double) * 3 * hi0.V, s));
         hi0.vel_set = false;
     }
@@ -1067,7 +1266,7 @@ int step_iterate(idp_ctx* c, int max_iters, idp_result* results, int* n_active) 
                 double eta = st[i].g0 > 0 ? gn / st[i].g0 : 1.0;
                 tol[i] = std::max(c->P.pcg_rel_tol, std::min(1e-2, eta));
                 // a flow-mode shell may stop after this one step: solve it fully
-                if (c->inst[i].shell) tol[i] = c->P.pcg_rel_tol;
+                if (c->inst[i].flow()) tol[i] = c->P.pcg_rel_tol;
             }
             IDP_CUDA_TRY(cudaMemcpyAsync(W.tol_inst, tol.data(), sizeof(double) * nI, cudaMemcpyHostToDevice, s));
         }
@@ -1180,6 +1379,7 @@ int step_iterate(idp_ctx* c, int max_iters, idp_result* results, int* n_active) 
             W.timer.start(PhaseTimer::TET, s);
             if ((rc = tet_energy(A, W, A.X, h * h, dsc(c, S_ETET), isc(c, SI_BAD), s))) return rc;
             if ((rc = flow_energy(A, W, A.X, dsc(c, S_ETET), s))) return rc;
+            if ((rc = shell_energy(A, W, A.X, h * h, dsc(c, S_ETET), s))) return rc;
             W.timer.stop(s);
             if ((rc = vec_inertia(A, W, A.X, dsc(c, S_EINERT), nullptr, s))) return rc;
             for (int i = 0; i < nI; ++i) st[i].ls_trials += srch[i];
@@ -1204,7 +1404,7 @@ int step_iterate(idp_ctx* c, int max_iters, idp_result* results, int* n_active) 
                     continue;
                 }
                 const double Ei = sc.d(S_ETET, i) + sc.d(S_EINERT, i) + sc.d(S_EBAR, i);
-                bool ok = sc.flag(SI_BADB, i) == 0 && !(Ei > st[i].Eprev);
+                bool ok = sc.flag(SI_BADB, i) == 0 && std::isfinite(Ei) && !(Ei > st[i].Eprev);
                 alpha[i] /= 2.0;
                 if (ok) {
                     srch[i] = 0;
@@ -1301,7 +1501,7 @@ int step_iterate(idp_ctx* c, int max_iters, idp_result* results, int* n_active) 
             else if (S.iters >= c->P.max_newton) {
                 S.active = false;
                 S.status = IDP_ERR_NOT_CONVERGED;
-            } else if (c->inst[i].shell && c->cs.off[i + 1] == c->cs.off[i]) {
+            } else if (c->inst[i].flow() && c->cs.off[i + 1] == c->cs.off[i]) {
                 S.active = false;  // flow mode without contacts: one Newton step (IMPLICIT_EULER.h:850-854)
             }
             if (!S.active) S.latency_ms = since_ms(c->t_begin);

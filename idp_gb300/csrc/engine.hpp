@@ -40,6 +40,14 @@ struct HostInstance {
     std::vector<double> fvol;
     bool vel_set = false;  // predictor velocity given since the last advance
     std::vector<double> bacc;  // body-force acceleration M^-1 b (3V; empty = none)
+    // elastic shell (the Hinge path's membrane + hinge bending) instead of
+    // flow mode: per face (IB^-1 00, 01, 11, det IB^-1, vol, lam, mu); per
+    // hinge its stencil (x0, x1, x2, x3) and (thetabar, k ebar / hbar)
+    bool elastic = false;
+    std::vector<double> mem;
+    std::vector<int> hinges;
+    std::vector<double> hk;
+    bool flow() const { return shell && !elastic; }
 };
 
 // per-instance Newton state kept on the host
@@ -130,6 +138,23 @@ struct Arena {
     int* vert_face_ptr = nullptr;                 // per vertex: list of face*3+corner, ascending
     int* vert_face = nullptr;
     double h = 0.1;                               // time step (flow Hessian coefficient)
+    // ---- elastic shells: membrane faces and hinges (global vertex ids)
+    long Fm = 0, Hn = 0;
+    std::vector<int> fm_off, hn_off;              // host, nI+1
+    int* mface = nullptr;                         // 3 Fm
+    double* mem = nullptr;                        // 7 Fm: IB^-1 (00, 01, 11), det IB^-1, vol, lam, mu
+    int* finst = nullptr;                         // Fm: instance of each face
+    Chunk* mface_chunks = nullptr;
+    int n_mface_chunks = 0;
+    int* mface_chunk_off = nullptr;               // nI+1
+    int4* hinge = nullptr;                        // Hn: (x0, x1, x2, x3)
+    double* hk = nullptr;                         // 2 Hn: thetabar, k ebar / hbar
+    int* hinst = nullptr;                         // Hn
+    Chunk* hinge_chunks = nullptr;
+    int n_hinge_chunks = 0;
+    int* hinge_chunk_off = nullptr;               // nI+1
+    int* vshell_ptr = nullptr;                    // per vertex: element gradient slots (3 doubles each)
+    int* vshell = nullptr;
 };
 
 // In-flight state of one instance in the middle of a step, enough to resume
@@ -221,7 +246,7 @@ enum WorkSlot {
     W_BH, W_BG, W_GENT_KEY, W_GENT_VAL, W_GENT_KEY2, W_GENT_VAL2, W_GENT_HEAD,
     W_TAIL_ROWPTR, W_TAIL_COL, W_TAIL_VAL, W_TAIL_KEYS,
     W_BSR_VAL, W_DIAG_INV, W_PCG_VEC, W_PCG_GRID, W_SPAN, W_CBASE, W_DENSE0, W_DENSE1, W_PCG_VEC64, W_CCD_TMP, W_CCD_ALPHA, W_MISC, W_MISC2,
-    W_CL_INT, W_CL_DENSE, W_CL_HOSTCONS, W_PSD,
+    W_CL_INT, W_CL_DENSE, W_CL_HOSTCONS, W_PSD, W_SHELL_GRAD,
     W_NUM
 };
 struct Work {
@@ -307,6 +332,11 @@ bool instance_active(idp_ctx* c, int i);  // still iterating in the step in flig
 // shell.cu: flow energy of triangle shells (INC_POTENTIAL.h:53-73, 191-211)
 int flow_energy(Arena& A, Work& W, const double* X, double* inst_E, cudaStream_t s);  // accumulates
 int flow_gradient(Arena& A, const double* X, double* g, cudaStream_t s);              // accumulates
+
+// shell_elastic.cu: membrane + hinge bending of elastic shells
+int shell_energy(Arena& A, Work& W, const double* X, double w_h2, double* inst_E, cudaStream_t s);  // accumulates
+int shell_gradient(Arena& A, Work& W, const double* X, double w_h2, double* g, cudaStream_t s);     // accumulates
+int shell_hessian(Arena& A, Work& W, const double* X, double w_h2, bool fp64, cudaStream_t s);
 
 // tet.cu
 int tet_energy(Arena& A, Work& W, const double* X, double w_h2, double* inst_E, int* inst_bad, cudaStream_t s);

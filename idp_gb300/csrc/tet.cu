@@ -336,7 +336,8 @@ int tet_gradient(Arena& A, Work& W, const double* X, double w_h2, double* g_corn
 
 int tet_hessian(Arena& A, Work& W, const double* X, double w_h2, bool fp64, cudaStream_t s) {
     size_t el = fp64 ? sizeof(double) : sizeof(float);
-    if (W[W_TET_HESS].ensure(el * 90 * (A.T + 1))) return IDP_ERR_CUDA;
+    // element blocks: 10 per tet, then 6 per elastic-shell face and 10 per hinge
+    if (W[W_TET_HESS].ensure(el * 9 * (10 * (A.T + 1) + 6 * A.Fm + 10 * A.Hn))) return IDP_ERR_CUDA;
     if (fp64)
         (::idp::count_launch(), k_tet_hessian<double><<<grid_for(A.T, 128), 128, 0, s>>>(A.T, nullptr, A.active, X, A.tet, A.IB, A.vol, A.lam,
                                                                   A.mu, w_h2, W[W_TET_HESS].as<double>()));

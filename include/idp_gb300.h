@@ -144,6 +144,26 @@ int idp_add_shell_instance(idp_ctx* ctx, int V, const double* X, int F, const in
                            double thickness, int nDBC, const int32_t* dbc_idx, double dHat2, double kappa,
                            double kappa_max);
 
+/* Add an elastic triangle shell of the Hinge path (Advance_One_Step_IE_Hinge
+ * with shell elements, FEM/Shell/DISCRETE_SHELL.h:1110): neo-Hookean
+ * membrane on the first fundamental form of every face
+ * (FEM/Shell/MEMBRANE.h:7-322) and hinge bending on the dihedral angle of
+ * every interior edge (FEM/Shell/BENDING.h, KL = false;
+ * Math/DIHEDRAL_ANGLE.h), with offset-IPC self-contact on all faces.
+ * X: current positions, X0: rest positions (NULL = X); faces int32[3F]
+ * (faces with a singular rest first fundamental form are dropped). mass:
+ * lumped vertex masses (V, the nodeAttr m of Initialize_Discrete_Shell), or
+ * NULL for area * thickness * density / 3 per corner; membrane lambda = E nu / (1 -
+ * nu^2), mu = E / (2 (1 + nu)), vol = area * thickness; hinge stiffness
+ * k = bending_mult * E thickness^3 / (24 (1 - nu^2)) with the rest angle,
+ * |rest edge| and (|n1| + |n2|) / (6 |edge|) of Compute_Discrete_Shell_Inv_Basis
+ * (DISCRETE_SHELL.h:132-357). Elements whose vertices are all fixed are
+ * skipped. Before idp_commit; returns the instance index or -IDP_*. */
+int idp_add_elastic_shell_instance(idp_ctx* ctx, int V, const double* X, const double* X0, int F,
+                                   const int32_t* faces, const double* mass, double density, double E, double nu,
+                                   double thickness, double bending_mult, int nDBC, const int32_t* dbc_idx,
+                                   double dHat2, double kappa, double kappa_max);
+
 /* Velocity v (3V); x_tilde = x + h v (IMPLICIT_EULER.h:195-216; a body force
  * adds h^2 M^-1 b, idp_set_body_force). MeshIO.Load_Velocity_X0
  * (Utils/MESHIO.h:986-1004) sets v = (target - x)/h. */

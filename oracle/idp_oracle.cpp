@@ -1154,12 +1154,18 @@ static MemFace mem_at(const double* m) { return MemFace{m[0], m[1], m[2], m[3], 
 
 // membrane energy of every face (summed in face order); gradient added into
 // g (3V, may be null); element Hessians H (F x 81, may be null), projected
-// to PSD when project (MEMBRANE.h:125-322)
+// to PSD when project (MEMBRANE.h:125-322); faces whose three vertices are
+// all fixed (dbc, may be null) are skipped, as in the reference
 double ora_membrane(int F, const int* faces, const double* X, const double* mem, double w, double* g, double* H,
-                    int project) {
+                    int project, const unsigned char* dbc) {
     double E = 0;
     for (int f = 0; f < F; ++f) {
         const int* t = faces + 3 * f;
+        if (dbc && dbc[t[0]] && dbc[t[1]] && dbc[t[2]]) {  // all-DBC faces are skipped (MEMBRANE.h:25)
+            if (H)
+                for (int i = 0; i < 81; ++i) H[81L * f + i] = 0.0;
+            continue;
+        }
         double ge[9];
         E += membrane_face(v3(X + 3 * t[0]), v3(X + 3 * t[1]), v3(X + 3 * t[2]), mem_at(mem + 7 * f), w,
                            g ? ge : nullptr, H ? H + 81L * f : nullptr);
@@ -1212,10 +1218,15 @@ int ora_shell_hinges(int V, int F, const int* faces, const double* X0, int nE, c
 // bending energy of every hinge (hinge order); gradient into g (may be null);
 // element Hessians H (Hn x 144, may be null), projected when project
 double ora_bending(int Hn, const int* hinges, const double* info, double k, const double* X, double w, double* g,
-                   double* H, int project) {
+                   double* H, int project, const unsigned char* dbc) {
     double E = 0;
     for (int i = 0; i < Hn; ++i) {
         const int* hh = hinges + 4 * i;
+        if (dbc && dbc[hh[0]] && dbc[hh[1]] && dbc[hh[2]] && dbc[hh[3]]) {  // BENDING.h:56-60
+            if (H)
+                for (int q = 0; q < 144; ++q) H[144L * i + q] = 0.0;
+            continue;
+        }
         const double* in = info + 3 * i;
         double ge[12];
         E += bending_hinge(v3(X + 3 * hh[0]), v3(X + 3 * hh[1]), v3(X + 3 * hh[2]), v3(X + 3 * hh[3]), in[0], in[1],

@@ -248,13 +248,16 @@ def membrane_rest(X0, faces, thickness, E, nu):
     return mem
 
 
-def membrane(X, faces, mem, w, grad=False, hess=False, project=True):
-    """Membrane energy (and gradient 3V, element Hessians F x 9 x 9)."""
+def membrane(X, faces, mem, w, grad=False, hess=False, project=True, dbc=None):
+    """Membrane energy (and gradient 3V, element Hessians F x 9 x 9); faces
+    with all three vertices fixed (dbc) are skipped."""
     X, faces = f64(X), i32(faces)
     g = np.zeros(X.size) if grad else None
     H = np.zeros((faces.shape[0], 9, 9)) if hess else None
+    d = None if dbc is None else np.ascontiguousarray(dbc, np.uint8)
     E = lib().ora_membrane(faces.shape[0], _i(faces), _d(X), _d(f64(mem)), C.c_double(w),
-                           _d(g) if grad else None, _d(H) if hess else None, int(project))
+                           _d(g) if grad else None, _d(H) if hess else None, int(project),
+                           None if d is None else _u(d))
     return E, g, H
 
 
@@ -268,13 +271,16 @@ def shell_hinges(X0, faces, edges):
     return hin[:n].copy(), info[:n].copy()
 
 
-def bending(X, hinges, info, k, w, grad=False, hess=False, project=True):
-    """Hinge bending energy (and gradient 3V, element Hessians Hn x 12 x 12)."""
+def bending(X, hinges, info, k, w, grad=False, hess=False, project=True, dbc=None):
+    """Hinge bending energy (and gradient 3V, element Hessians Hn x 12 x 12);
+    hinges with all four vertices fixed (dbc) are skipped."""
     X, hinges = f64(X), i32(hinges)
     g = np.zeros(X.size) if grad else None
     H = np.zeros((hinges.shape[0], 12, 12)) if hess else None
+    d = None if dbc is None else np.ascontiguousarray(dbc, np.uint8)
     E = lib().ora_bending(hinges.shape[0], _i(hinges), _d(f64(info)), C.c_double(k), _d(X), C.c_double(w),
-                          _d(g) if grad else None, _d(H) if hess else None, int(project))
+                          _d(g) if grad else None, _d(H) if hess else None, int(project),
+                          None if d is None else _u(d))
     return E, g, H
 
 
@@ -403,7 +409,8 @@ def _energy(pb, X, Xtilde, with_barrier, cons, info):
     if pb.flow:  # INC_POTENTIAL.h:53-73
         E = flow_energy(X, pb.faces, pb.fvol, pb.h)
     elif pb.elastic_shell:  # INC_POTENTIAL.h: membrane + hinge bending
-        E = membrane(X, pb.faces, pb.mem, h2)[0] + bending(X, pb.hinges, pb.hinfo, pb.kbend, h2)[0]
+        E = (membrane(X, pb.faces, pb.mem, h2, dbc=pb.dbc)[0]
+             + bending(X, pb.hinges, pb.hinfo, pb.kbend, h2, dbc=pb.dbc)[0])
         if not np.isfinite(E):
             return None
     else:
@@ -423,7 +430,8 @@ def _gradient(pb, X, Xtilde, cons, info):
     if pb.flow:  # INC_POTENTIAL.h:191-211
         g = flow_gradient(X, pb.faces, pb.fvol, pb.h)
     elif pb.elastic_shell:
-        g = membrane(X, pb.faces, pb.mem, h2, grad=True)[1] + bending(X, pb.hinges, pb.hinfo, pb.kbend, h2, grad=True)[1]
+        g = (membrane(X, pb.faces, pb.mem, h2, grad=True, dbc=pb.dbc)[1]
+             + bending(X, pb.hinges, pb.hinfo, pb.kbend, h2, grad=True, dbc=pb.dbc)[1])
     else:
         g = tet_gradient(X, pb.tets, pb.IB, pb.vol, pb.lam, pb.mu, h2)
     g += (pb.mass[:, None] * (X - Xtilde)).reshape(-1)
@@ -442,8 +450,8 @@ def _hessian(pb, X, cons, info):
         R, Cc, Vv = [Hf.row], [Hf.col], [Hf.data]
     elif pb.elastic_shell:
         R, Cc, Vv = [], [], []
-        for st, Hs in ((pb.faces, membrane(X, pb.faces, pb.mem, h2, hess=True)[2]),
-                       (pb.hinges, bending(X, pb.hinges, pb.hinfo, pb.kbend, h2, hess=True)[2])):
+        for st, Hs in ((pb.faces, membrane(X, pb.faces, pb.mem, h2, hess=True, dbc=pb.dbc)[2]),
+                       (pb.hinges, bending(X, pb.hinges, pb.hinfo, pb.kbend, h2, hess=True, dbc=pb.dbc)[2])):
             k = 3 * st.shape[1]
             dofs = (3 * st[:, :, None] + np.arange(3)).reshape(-1, k)
             R.append(np.repeat(dofs[:, :, None], k, axis=2).reshape(-1))

@@ -1,0 +1,149 @@
+"""Elastic triangle shells of the Hinge path (neo-Hookean membrane + hinge
+bending, with offset-IPC self-contact) on the GB300 against the oracle,
+through the C ABI: energy and gradient within 1e-9 relative, assembled
+Hessian times a vector within 1e-9 (FP64) / 2e-4 (mixed), constraint sets
+bit for bit, and whole steps (a sphere pressed flat until its caps touch)
+to the oracle's energy within 1e-6; the reference-shaped Hinge call with
+shell elements gives the direct C-ABI calls' results bit for bit."""
+import numpy as np
+import pytest
+
+import cases
+
+pytestmark = pytest.mark.gpu
+
+
+def shell_ctx(idp, X0, F, pr, mode, v=None, X=None, dbc=None, **kw):
+    ctx = idp.Context(h=0.1, mode=mode, **kw)
+    ctx.add_elastic_shell_instance(X0 if X is None else X, F, pr["density"], pr["E"], pr["nu"], pr["thickness"],
+                                   pr["dHat2"], pr["kappa"], pr["kappa_max"], X0=X0, dbc_idx=dbc)
+    if v is not None:
+        ctx.set_velocity(0, v)
+    ctx.commit()
+    return ctx
+
+
+def shell_oracle(O, X0, F, pr, v, X=None, dbc=None, tol=1e-3):
+    surf = O.shell_surface(X0.shape[0], F)
+    hin, info = O.shell_hinges(X0, F, surf["edges"])
+    k = O.hinge_stiffness(pr["E"], pr["nu"], pr["thickness"])
+    hinfo = info.copy()
+    mask = np.zeros(X0.shape[0], np.uint8)
+    if dbc is not None:
+        mask[dbc] = 1
+    pb = O.Problem(X=(X0 if X is None else X).copy(), X0=X0, tets=np.zeros((0, 4), np.int32), mass=pr["mass"],
+                   lam=np.zeros(0), mu=np.zeros(0), h=0.1, dHat2=pr["dHat2"], kappa=[pr["kappa"], pr["kappa_max"], 0.0],
+                   v=v.copy(), faces=F, mem=O.membrane_rest(X0, F, pr["thickness"], pr["E"], pr["nu"]), hinges=hin,
+                   hinfo=hinfo, kbend=k, dbc=mask, tol=tol)
+    pb.surf = surf
+    return pb
+
+
+def pressed_sphere():
+    X0, F = cases.sphere_shell(3)
+    pr = cases.shell_problem(X0, F, dHat=0.02)
+    tgt = X0 * np.array([1.0, 1.0, 0.05])  # flattened through itself
+    return X0, F, pr, (tgt - X0) / 0.1
+
+
+def test_mass_and_surface_match(oracle, gpu_lib):
+    import idp_gb300 as idp
+
+    X0, F, pr, v = pressed_sphere()
+    ctx = shell_ctx(idp, X0, F, pr, idp.MODE_FP64, v=v)
+    s = ctx.surface(0)
+    o = oracle.shell_surface(X0.shape[0], F)
+    assert np.array_equal(s["edges"], o["edges"]) and np.array_equal(s["tris"], o["tris"])
+    ctx.close()
+
+
+@pytest.mark.parametrize("mode,tol", [(0, 1e-9), (1, 2e-4)], ids=["fp64", "mixed"])
+def test_energy_gradient_hessian_parity(oracle, gpu_lib, mode, tol):
+    import idp_gb300 as idp
+
+    X0, F, pr, v = pressed_sphere()
+    rng = np.random.default_rng(4)
+    X = X0 * np.array([1.0, 1.0, 0.3]) + 0.01 * rng.normal(size=X0.shape)
+    dbc = np.arange(0, X0.shape[0], 11, dtype=np.int32)
+    X[dbc] = X0[dbc]
+    ctx = shell_ctx(idp, X0, F, pr, mode, v=v, dbc=dbc)
+    pb = shell_oracle(oracle, X0, F, pr, v, X=X, dbc=dbc)
+    xt = X0 + 0.1 * v
+    cons, info = oracle.constraint_set(X, X0, pb.surf, pb.dbc, pr["dHat2"])
+    Ee, Ei, Eb = ctx.energy(0, X)
+    E_or = oracle._energy(pb, X, xt, False, cons, info) - 0.5 * float(np.sum(pr["mass"][:, None] * (X - xt) ** 2))
+    assert Ee == pytest.approx(E_or, rel=1e-9) and E_or > 0
+    g = ctx.gradient(0, X)
+    go = oracle._gradient(pb, X, xt, cons, info)
+    go.reshape(-1, 3)[dbc] = 0
+    assert np.linalg.norm(g - go) <= 1e-9 * np.linalg.norm(go)
+    H = oracle._hessian(pb, X, cons, info)
+    for _ in range(2):
+        x = rng.normal(size=X.size)
+        y, yo = ctx.hessian_apply(0, X, x), H @ x
+        assert np.linalg.norm(y - yo) <= tol * np.linalg.norm(yo)
+    ctx.close()
+
+
+@pytest.mark.parametrize("mode", [0, 1], ids=["fp64", "mixed"])
+def test_pressed_sphere_step_matches_oracle(oracle, gpu_lib, mode):
+    """The sphere's predictor flattens it through itself: the step ends with
+    the caps in contact (constraints active), injective, at the oracle's
+    energy within 1e-6 relative."""
+    import idp_gb300 as idp
+
+    X0, F, pr, v = pressed_sphere()
+    ctx = shell_ctx(idp, X0, F, pr, mode, v=v, newton_tol=1e-5, max_newton=500)
+    rc, res = ctx.advance(check=False)
+    assert rc in (idp.IDP_OK, idp.IDP_WARN_ITER_CAP), res
+    Xg, _, _ = ctx.state(0)
+    assert len(ctx.intersections(0)) == 0
+    pb = shell_oracle(oracle, X0, F, pr, v, tol=1e-5)
+    pb.max_iters = 500
+    its = oracle.advance_one_step(pb)
+    rel = abs(res[0]["energy"] - pb.last_energy) / abs(pb.last_energy)
+    print(f"pressed sphere: GPU {res[0]['newton_iters']} iterations E {res[0]['energy']:.12e} C "
+          f"{res[0]['num_constraints']}; oracle {its} iterations E {pb.last_energy:.12e} C {pb.log[-1]['ncons']}; "
+          f"rel {rel:.2e}")
+    assert res[0]["num_constraints"] > 0
+    assert len(oracle.edge_tri_intersections(Xg, pb.surf)) == 0
+    assert rel <= 1e-6
+    ctx.close()
+
+
+def test_hinge_call_with_shell_elements_matches_c_abi(oracle, gpu_lib):
+    """Advance_One_Step_IE_Hinge with the shell's elements, element attributes
+    and hinge stencils as Initialize_Discrete_Shell prepares them."""
+    import idp_gb300 as idp
+    from idp_gb300.api import FEM, shell_material
+
+    X0, F, pr, v = pressed_sphere()
+    surf = oracle.shell_surface(X0.shape[0], F)
+    hin, info = oracle.shell_hinges(X0, F, surf["edges"])
+    mem = oracle.membrane_rest(X0, F, pr["thickness"], pr["E"], pr["nu"])
+    k = oracle.hinge_stiffness(pr["E"], pr["nu"], pr["thickness"])
+    # the reference's storages: rest first fundamental form per face (IB), its
+    # P slot of face 0 holding the hinge stiffness, (F, vol, lambda, mu) per face
+    IB = np.stack([np.linalg.inv(np.array([[m[0], m[1]], [m[1], m[2]]])) for m in mem])
+    elemAttr = {"IB": IB, "P": np.zeros_like(IB)}
+    elemAttr["P"][0, 0, 0] = k
+    elasticityAttr = {"vol": mem[:, 4], "lambda": mem[:, 5], "mu": mem[:, 6]}
+    nodeAttr = {"x0": X0.copy(), "v": v.copy(), "g": np.zeros_like(X0), "m": pr["mass"].copy()}
+    kappaVec = [pr["kappa"], pr["kappa_max"], 0.0]
+    X = X0.copy()
+    args = [F, [], [], {}, hin, info, pr["thickness"], 1.0, [], [], [1.0, 0.0], [1.0, 1.0], [0.0, 0.0], None, 0.1, 1e-3,
+            True, pr["dHat2"], kappaVec, 0.0, 1e-10, 0, [], [], False, X, nodeAttr, None, elemAttr, elasticityAttr,
+            np.zeros((0, 4), np.int32), None, None, [], [], [], [], [], [], 0.0, [], ""]
+    its = FEM.DiscreteShell.Advance_One_Step_IE_Hinge(*args)
+    mat = shell_material(F, nodeAttr, elemAttr, elasticityAttr, 1.0)
+    ctx = idp.Context(h=0.1, mode=idp.MODE_MIXED, newton_tol=1e-3)
+    ctx.add_elastic_shell_instance(X0, F, mat["density"], mat["E"], mat["nu"], mat["thickness"], pr["dHat2"],
+                                   pr["kappa"], pr["kappa_max"], bending_mult=mat["bending_mult"], mass=mat["mass"])
+    ctx.set_velocity(0, v)
+    ctx.commit()
+    _, r = ctx.advance(check=False)
+    Xd, vd, kd = ctx.state(0)
+    assert its == r[0]["newton_iters"]
+    assert np.array_equal(X, Xd) and np.array_equal(nodeAttr["v"], vd) and kappaVec[0] == kd[0]
+    assert r[0]["num_constraints"] > 0
+    ctx.close()
