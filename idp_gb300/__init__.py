@@ -40,7 +40,7 @@ EXPORTS = [
     "idp_check_intersection_all", "idp_reset", "idp_device_bytes", "idp_job_footprint", "idp_server_create",
     "idp_server_create_simulated", "idp_server_submit", "idp_server_wait", "idp_server_drain",
     "idp_server_get_stats", "idp_server_destroy", "idp_add_shell_instance", "idp_step_begin", "idp_step_iterate",
-    "idp_set_body_force", "idp_add_elastic_shell_instance",
+    "idp_set_body_force", "idp_add_elastic_shell_instance", "idp_set_dbc_targets",
 ]
 
 
@@ -138,6 +138,7 @@ def load(path: str | None = None):
     L.idp_step_begin.argtypes = [C.c_void_p]
     L.idp_step_iterate.argtypes = [C.c_void_p, C.c_int, C.POINTER(Result), C.POINTER(C.c_int)]
     L.idp_set_body_force.argtypes = [C.c_void_p, C.c_int, _dp]
+    L.idp_set_dbc_targets.argtypes = [C.c_void_p, C.c_int, _dp]
     L.idp_add_elastic_shell_instance.argtypes = [C.c_void_p, C.c_int, _dp, _dp, C.c_int, _ip, _dp, C.c_double,
                                                  C.c_double, C.c_double, C.c_double, C.c_double, C.c_int, _ip,
                                                  C.c_double, C.c_double, C.c_double]
@@ -214,6 +215,7 @@ class Context:
         if not self._h:
             raise IDPError(st.value, "idp_create")
         self._V = []
+        self._ndbc = []
         self.committed = False
 
     def close(self):
@@ -244,6 +246,7 @@ class Context:
         if r < 0:
             raise IDPError(-r, "idp_add_instance")
         self._V.append(V)
+        self._ndbc.append(dbc.size)
         return r
 
     def add_shell_instance(self, X, faces, density, thickness, dHat2, kappa, kappa_max, dbc_idx=None):
@@ -257,6 +260,7 @@ class Context:
         if r < 0:
             raise IDPError(-r, "idp_add_shell_instance")
         self._V.append(V)
+        self._ndbc.append(dbc.size)
         return r
 
     def add_elastic_shell_instance(self, X, faces, density, E, nu, thickness, dHat2, kappa, kappa_max,
@@ -277,6 +281,7 @@ class Context:
         if r < 0:
             raise IDPError(-r, "idp_add_elastic_shell_instance")
         self._V.append(V)
+        self._ndbc.append(dbc.size)
         return r
 
     def set_velocity(self, i, v):
@@ -288,6 +293,16 @@ class Context:
         bb = None if b is None else _f64(b)
         self._check(load().idp_set_body_force(self._h, int(i), None if bb is None else _pd(bb)),
                     "idp_set_body_force")
+
+    def set_dbc_targets(self, i, targets):
+        """Targets (nDBC, 3) of instance i's DBC vertices in their dbc_idx
+        order; vertices whose target differs from their position at a
+        step's start move there (augmented Lagrangian). None: all fixed."""
+        t = None if targets is None else _f64(targets)
+        if t is not None and t.size != 3 * self._ndbc[i]:
+            raise ValueError("targets: one (x, y, z) per DBC vertex of the instance")
+        self._check(load().idp_set_dbc_targets(self._h, int(i), None if t is None else _pd(t)),
+                    "idp_set_dbc_targets")
 
     def set_normal_flow(self, i, step):
         """x_tilde = x + step * n on surface vertices, x_tilde = x inside
@@ -312,6 +327,7 @@ class Context:
         """Drop the instances, keep the device buffers for the next set."""
         self._check(load().idp_reset(self._h), "idp_reset")
         self._V = []
+        self._ndbc = []
         self.committed = False
 
     def device_bytes(self):

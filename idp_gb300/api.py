@@ -27,7 +27,7 @@ import numpy as np
 
 from . import Context, IDPError, IDP_WARN_ITER_CAP, MODE_MIXED, meshgen
 
-_UNSUPPORTED = "not part of the GB300 path (tet meshes and triangle shells with offset IPC)"
+_UNSUPPORTED = "not part of the GB300 path (tet meshes and triangle shells with offset IPC and DBC)"
 
 
 def _empty(x):
@@ -71,25 +71,23 @@ def _digest(*arrays):
     return hsh.hexdigest()
 
 
-def _dbc_indices(DBC, X=None):
-    """Vertex indices of the DBC storage (rows (index, x, y, z), the
-    reference's VECTOR_STORAGE<T, dim + 1>, IMPLICIT_EULER.h:155). Only fixed
-    DBCs are on this path: a target that differs from the vertex's position
-    (a moving DBC, solved by the reference's augmented Lagrangian,
-    Shell/DIRICHLET.h) raises NotImplementedError."""
+def _dbc_rows(DBC):
+    """Vertex indices and targets of the DBC storage (rows (index, x, y, z),
+    the reference's VECTOR_STORAGE<T, dim + 1>, IMPLICIT_EULER.h:155): (None,
+    None) without DBC, targets None for a bare index list. A row whose target
+    is the vertex's position at a step's start is fixed; the others move there
+    (the augmented Lagrangian, IMPLICIT_EULER.h:305-401, 701-757)."""
     if _empty(DBC):
-        return None
+        return None, None
     D = np.asarray(DBC, dtype=np.float64)
     if D.ndim == 1:
-        return D.astype(np.int32)
+        return D.astype(np.int32), None
     idx = D[:, 0].astype(np.int32)
-    if X is not None and D.shape[1] >= 4 and not np.array_equal(D[:, 1:4], np.asarray(X)[idx]):
-        raise NotImplementedError(f"moving DBC targets: {_UNSUPPORTED}")
-    return idx
+    return idx, (np.ascontiguousarray(D[:, 1:4]) if D.shape[1] >= 4 else None)
 
 
 def _context_for(tet, X, nodeAttr, tetEl, dHat2, kappaVec, DBC, h, NewtonTol, thickness, mode):
-    dbc_idx = _dbc_indices(DBC, X)
+    dbc_idx, _ = _dbc_rows(DBC)
     key = (_digest(tet, nodeAttr["x0"], nodeAttr["m"], tetEl["lambda"], tetEl["mu"],
                    np.zeros(0, np.int32) if dbc_idx is None else dbc_idx),
            X.shape, float(dHat2), float(h), float(NewtonTol), float(thickness), mode)
@@ -138,7 +136,7 @@ def shell_material(Elem, nodeAttr, elemAttr, elasticityAttr, bendingStiffMult):
 
 def _shell_context_for(Elem, X, nodeAttr, elemAttr, elasticityAttr, bendingStiffMult, dHat2, kappaVec, DBC, h,
                        NewtonTol, thickness, mode):
-    dbc_idx = _dbc_indices(DBC, X)
+    dbc_idx, _ = _dbc_rows(DBC)
     P = np.asarray(elemAttr["P"], dtype=np.float64)
     key = ("shell", _digest(np.asarray(Elem, dtype=np.int32), nodeAttr["x0"], nodeAttr["m"], elasticityAttr["vol"],
                             elasticityAttr["lambda"], elasticityAttr["mu"], P.reshape(-1)[:1],
@@ -199,6 +197,9 @@ class DiscreteShell:
         ctx.set_positions(0, X)
         ctx.set_velocity(0, nodeAttr["v"])
         ctx.set_kappa(0, [kappaVec[0], kappaVec[1], 0.0])
+        idx, targets = _dbc_rows(DBC)
+        if idx is not None:
+            ctx.set_dbc_targets(0, targets)
         bb = None if b is None else np.asarray(b, dtype=np.float64).reshape(-1, 3)
         ctx.set_body_force(0, bb if bb is not None and np.any(bb != 0) else None)
         rc, res = ctx.advance(check=False)
@@ -229,7 +230,7 @@ def _flow_context_for(Elem, X, nodeAttr, elasticityAttr, dHat2, kappaVec, DBC, h
     shell_t = float(vol[0] / area[0])
     rho = float(np.sum(nodeAttr["m"]) / np.sum(vol))
     ctx = Context(h=h, newton_tol=NewtonTol, thickness=thickness, mode=mode)
-    dbc_idx = _dbc_indices(DBC, X)
+    dbc_idx, _ = _dbc_rows(DBC)
     ctx.add_shell_instance(X0, Elem, rho, shell_t, dHat2, kappaVec[0], kappaVec[1], dbc_idx=dbc_idx)
     ctx.commit()
     _FlowCache.ctx, _FlowCache.key = ctx, key
@@ -254,6 +255,9 @@ def _advance_flow(Elem, segs, DBC, edge2tri, edgeStencil, edgeInfo, thickness, b
     ctx = _flow_context_for(Elem, X, nodeAttr, elasticityAttr, dHat2, kappaVec, DBC, h, NewtonTol, thickness,
                             DiscreteShell.mode)
     ctx.set_positions(0, X)
+    idx, targets = _dbc_rows(DBC)
+    if idx is not None:
+        ctx.set_dbc_targets(0, targets)
     m = np.asarray(nodeAttr["m"], dtype=np.float64)
     bb = np.zeros_like(X) if b is None else np.asarray(b, dtype=np.float64).reshape(-1, 3)
     ctx.set_velocity(0, h * bb / m[:, None])

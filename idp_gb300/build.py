@@ -22,9 +22,9 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
           "-Xcompiler", "-Wall", "-Xcompiler", "-Wno-unused-function", "-I", INCLUDE]
-EXACT_FP64 = {"contact.cu", "ccd.cu", "flow.cu"}
+EXACT_FP64 = {"contact.cu", "ccd.cu", "flow.cu", "dirichlet.cu"}
 UNITS = ["prims.cu", "tet.cu", "contact.cu", "barrier.cu", "ccd.cu", "solver.cu", "precond.cu", "vecops.cu",
-         "flow.cu", "shell.cu", "shell_elastic.cu", "engine.cpp", "server.cpp"]
+         "flow.cu", "shell.cu", "shell_elastic.cu", "dirichlet.cu", "engine.cpp", "server.cpp"]
 HEADERS = ["common.cuh", "prims.cuh", "geom.cuh", "grid.cuh", "engine.hpp", "predicates.cuh", "psd.cuh"]
 
 

@@ -751,11 +751,11 @@ int ccd_stepsize(Arena& A, Work& W, const double* X, const double* dir, double* 
         if (W[W_CAND].ensure(sizeof(CCand) * (cap_pt + cap_ee))) return IDP_ERR_CUDA;
         CCand* cand = W[W_CAND].as<CCand>();
         if (A.Sn)
-            (::idp::count_launch(), k_ccd_query_pt<<<grid_for(kCcdQueryLanes * A.Sn), kBlock, 0, s>>>(A.Sn, A.snode, A.sn_inst, A.active, X, dir, A.dbc, A.stri,
+            (::idp::count_launch(), k_ccd_query_pt<<<grid_for(kCcdQueryLanes * A.Sn), kBlock, 0, s>>>(A.Sn, A.snode, A.sn_inst, A.active, X, dir, A.dbc_excl, A.stri,
                                                              nbox, tbox, nboxc, tboxc, gc, A.thickness, gt.cells, gt.cell_start,
                                                              gt.entries, cand, ccount, cap_pt));
         if (A.Se)
-            (::idp::count_launch(), k_ccd_query_ee<<<grid_for(kCcdQueryLanes * A.Se), kBlock, 0, s>>>(A.Se, A.sedge, A.se_inst, A.active, X, dir, A.dbc, ebox, eboxc, gc,
+            (::idp::count_launch(), k_ccd_query_ee<<<grid_for(kCcdQueryLanes * A.Se), kBlock, 0, s>>>(A.Se, A.sedge, A.se_inst, A.active, X, dir, A.dbc_excl, ebox, eboxc, gc,
                                                              A.thickness, ge.cells, ge.cell_start,
                                                              ge.entries, cand + cap_pt, ccount + 1, cap_ee));
         (::idp::count_launch(), k_fill<<<grid_for(nI), kBlock, 0, s>>>(nI, 1e300, amin));

@@ -816,11 +816,11 @@ int build_constraint_set(Arena& A, Work& W, const double* X, ContactSet& cs, cud
         if (W[W_CAND].ensure(sizeof(Cand) * (cap_pt + cap_ee))) return IDP_ERR_CUDA;
         Cand* cand = W[W_CAND].as<Cand>();
         if (A.Sn)
-            (::idp::count_launch(), k_query_pt<<<grid_for(kQueryLanes * A.Sn), kBlock, 0, s>>>(A.Sn, A.snode, A.sn_inst, A.active, X, A.dbc, A.stri, tbox, gp,
+            (::idp::count_launch(), k_query_pt<<<grid_for(kQueryLanes * A.Sn), kBlock, 0, s>>>(A.Sn, A.snode, A.sn_inst, A.active, X, A.dbc_excl, A.stri, tbox, gp,
                                                          A.dHat2, A.thickness, gt.cells, gt.cell_start,
                                                          gt.entries, cand, ccount, cap_pt));
         if (A.Se)
-            (::idp::count_launch(), k_query_ee<<<grid_for(kQueryLanes * A.Se), kBlock, 0, s>>>(A.Se, A.sedge, A.se_inst, A.active, X, A.dbc, ebox, gp, A.dHat2,
+            (::idp::count_launch(), k_query_ee<<<grid_for(kQueryLanes * A.Se), kBlock, 0, s>>>(A.Se, A.sedge, A.se_inst, A.active, X, A.dbc_excl, ebox, gp, A.dHat2,
                                                          A.thickness, ge.cells, ge.cell_start, ge.entries,
                                                          cand + cap_pt, ccount + 1, cap_ee));
         IDP_CUDA_TRY(cudaMemcpyAsync(hp + 2, ccount, 3 * sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
@@ -938,7 +938,7 @@ int edge_tri_intersections(Arena& A, Work& W, const double* X, unsigned int* ins
         if (A.St)
             (::idp::count_launch(),
              k_query_tri_edges<<<grid_for(kQueryLanes * A.St), kBlock, 0, s>>>(
-                 A.St, A.stri, A.st_inst, A.active, X, A.dbc, A.sedge, tbox, ebox, gp, ge.cells, ge.cell_start,
+                 A.St, A.stri, A.st_inst, A.active, X, A.dbc_excl, A.sedge, tbox, ebox, gp, ge.cells, ge.cell_start,
                  ge.entries, out, ccount, cap, inst_count));
         IDP_CUDA_TRY(cudaMemcpyAsync(hp + 2, ccount, 3 * sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
         IDP_CUDA_TRY(cudaStreamSynchronize(s));

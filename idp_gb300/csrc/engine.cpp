@@ -174,7 +174,7 @@ void build_chunks(const std::vector<int>& off, std::vector<Chunk>& ch, std::vect
 }
 
 // per-instance device scalar layout inside ctx->inst_buf
-enum { S_ETET, S_EINERT, S_EBAR, S_MIND, S_NORM2, S_TOL, S_NUMD };
+enum { S_ETET, S_EINERT, S_EBAR, S_MIND, S_NORM2, S_TOL, S_EDBC, S_DDBC, S_NUMD };
 enum { SI_BAD, SI_BADB, SI_KFLAG, SI_CCDF, SI_ISECT, S_NUMI };
 
 double* dsc(idp_ctx* c, int k) { return c->inst_buf.as<double>() + (long)k * c->A.nI; }
@@ -214,6 +214,31 @@ int fetch_scalars(idp_ctx* c, InstScalars& out) {
     return IDP_OK;
 }
 
+// some instance has its moving-DBC penalty on (the device copy A.dstiff
+// mirrors InstState::dbc_stiff)
+bool dbc_penalty_on(idp_ctx* c) {
+    for (const InstState& S : c->st)
+        if (S.dbc_stiff > 0) return true;
+    return false;
+}
+
+int upload_dbc_stiff(idp_ctx* c) {
+    std::vector<double> k(c->A.nI);
+    for (int i = 0; i < c->A.nI; ++i) k[i] = c->st[i].dbc_stiff;
+    IDP_CUDA_TRY(cudaMemcpyAsync(c->A.dstiff, k.data(), sizeof(double) * k.size(), cudaMemcpyHostToDevice, c->s));
+    return IDP_OK;
+}
+
+// the rows projected to the identity for instance i: its fixed DBC vertices
+// while the penalty pulls the moving ones, every DBC vertex otherwise
+// (INC_POTENTIAL.h:387-394)
+int set_projection(idp_ctx* c, int i, bool penalty) {
+    const long o = c->A.v_off[i], n = c->inst[i].V;
+    IDP_CUDA_TRY(cudaMemcpyAsync(c->A.dbc + o, (penalty ? c->A.dfix : c->A.dbc_excl) + o, n, cudaMemcpyDeviceToDevice,
+                                 c->s));
+    return IDP_OK;
+}
+
 // incremental potential of the masked instances at X (INC_POTENTIAL.h:15-152):
 // E = h^2 sum vol*Psi + inertia [+ barrier over a freshly built constraint
 // set]. bad[i] = 1 when a tet is inverted, 2 when a constraint distance is
@@ -236,6 +261,8 @@ int eval_energy(idp_ctx* c, const double* X, bool with_barrier, std::vector<doub
         rc = barrier_energy(A, c->W, X, c->cs, dsc(c, S_EBAR), isc(c, SI_BADB), c->s);
         if (rc) return rc;
     }
+    const bool dpen = dbc_penalty_on(c);
+    if (dpen && (rc = dbc_sums(A, c->W, X, dsc(c, S_EDBC), dsc(c, S_DDBC), c->s))) return rc;
     // one copy of the whole per-instance scalar block, one synchronisation
     std::vector<double> hb((size_t)(S_NUMD + S_NUMI) * nI);
     IDP_CUDA_TRY(cudaMemcpyAsync(hb.data(), c->inst_buf.p, sizeof(double) * S_NUMD * nI + sizeof(int) * S_NUMI * nI,
@@ -244,6 +271,7 @@ int eval_energy(idp_ctx* c, const double* X, bool with_barrier, std::vector<doub
     const double* et = hb.data() + (size_t)S_ETET * nI;
     const double* ei = hb.data() + (size_t)S_EINERT * nI;
     const double* eb = hb.data() + (size_t)S_EBAR * nI;
+    const double* ed = hb.data() + (size_t)S_EDBC * nI;
     const int* hi = reinterpret_cast<const int*>(hb.data() + (size_t)S_NUMD * nI);
     const int* b1 = hi + (size_t)SI_BAD * nI;
     const int* b2 = hi + (size_t)SI_BADB * nI;
@@ -251,6 +279,8 @@ int eval_energy(idp_ctx* c, const double* X, bool with_barrier, std::vector<doub
     bad.resize(nI);
     for (int i = 0; i < nI; ++i) {
         E[i] = et[i] + ei[i] + eb[i];
+        // Compute_DBC_Energy (FEM/Shell/DIRICHLET.h:26-45)
+        if (dpen && c->st[i].dbc_stiff > 0) E[i] += 0.5 * c->st[i].dbc_stiff * ed[i];
         bad[i] = b1[i] ? 1 : (b2[i] ? 2 : 0);
     }
     return IDP_OK;
@@ -273,6 +303,8 @@ int eval_gradient(idp_ctx* c, const double* X) {
     rc = barrier_gradient(A, c->W, X, c->cs, A.g, c->s);
     c->W.timer.stop(c->s);
     if (rc) return rc;
+    // moving-DBC penalty (IMPLICIT_EULER.h:467-474), then the projected rows
+    if (dbc_penalty_on(c) && (rc = dbc_gradient(A, X, A.g, c->s))) return rc;
     return vec_zero_dbc(A, A.g, c->s);
 }
 
@@ -439,6 +471,7 @@ int idp_add_instance(idp_ctx* c, int V, const double* X, const double* X0, int T
         if (dbc_idx[k] < 0 || dbc_idx[k] >= V) return -IDP_ERR_INVALID_ARG;
         h.dbc[dbc_idx[k]] = 1;
     }
+    if (nDBC > 0) h.dbc_list.assign(dbc_idx, dbc_idx + nDBC);
     h.v.assign(3 * (long)V, 0.0);
     h.dHat2 = dHat2;
     h.kappa = kappa;
@@ -503,6 +536,7 @@ static int build_shell(HostInstance& h, int V, const double* X, int F, const int
         if (!dbc_idx || dbc_idx[k] < 0 || dbc_idx[k] >= V) return -IDP_ERR_INVALID_ARG;
         h.dbc[dbc_idx[k]] = 1;
     }
+    if (nDBC > 0) h.dbc_list.assign(dbc_idx, dbc_idx + nDBC);
     h.v.assign(3 * (long)V, 0.0);
     h.dHat2 = dHat2;
     h.kappa = kappa;
@@ -731,6 +765,39 @@ int idp_set_positions(idp_ctx* c, int i, const double* X) {
     return IDP_OK;
 }
 
+int idp_set_dbc_targets(idp_ctx* c, int i, const double* targets) {
+    if (!c || i < 0 || i >= (int)c->inst.size()) return IDP_ERR_INVALID_ARG;
+    if (c->stepping) return IDP_ERR_STATE;
+    HostInstance& h = c->inst[i];
+    if (h.dbc_list.empty()) return targets ? IDP_ERR_INVALID_ARG : IDP_OK;
+    if (!targets) {
+        h.dbc_tgt.clear();
+    } else {
+        // one row per DBC vertex: a vertex listed twice has no single target
+        std::vector<double> t(3 * (size_t)h.V, 0.0);
+        std::vector<char> seen(h.V, 0);
+        for (size_t k = 0; k < h.dbc_list.size(); ++k) {
+            const int v = h.dbc_list[k];
+            if (seen[v]) return IDP_ERR_INVALID_ARG;
+            seen[v] = 1;
+            for (int d = 0; d < 3; ++d) {
+                if (!std::isfinite(targets[3 * k + d])) return IDP_ERR_INVALID_ARG;
+                t[3 * v + d] = targets[3 * k + d];
+            }
+        }
+        h.dbc_tgt.swap(t);
+    }
+    if (c->committed) {
+        if (!c->A.dtgt) return IDP_ERR_STATE;
+        cudaSetDevice(c->P.device);
+        if (!h.dbc_tgt.empty())
+            IDP_CUDA_TRY(cudaMemcpyAsync(c->A.dtgt + 3L * c->A.v_off[i], h.dbc_tgt.data(), sizeof(double) * 3 * h.V,
+                                         cudaMemcpyHostToDevice, c->s));
+        IDP_CUDA_TRY(cudaStreamSynchronize(c->s));
+    }
+    return IDP_OK;
+}
+
 int idp_commit(idp_ctx* c) {
     if (!c) return IDP_ERR_INVALID_ARG;
     if (c->committed) return IDP_ERR_STATE;
@@ -843,6 +910,28 @@ int idp_commit(idp_ctx* c) {
     rc |= upload(c, A.dir, zeros);
     rc |= upload(c, A.mass, mass);
     rc |= upload(c, A.dbc, dbc);
+    rc |= upload(c, A.dbc_excl, dbc);
+    {
+        // moving-DBC targets (positions until set) and the per-instance
+        // penalty stiffness, kept when some instance has DBC vertices
+        bool any_dbc = false;
+        std::vector<double> tgt;
+        for (int i = 0; i < nI; ++i) any_dbc |= !c->inst[i].dbc_list.empty();
+        if (any_dbc) {
+            tgt = X;
+            for (int i = 0; i < nI; ++i)
+                if (!c->inst[i].dbc_tgt.empty())
+                    std::copy(c->inst[i].dbc_tgt.begin(), c->inst[i].dbc_tgt.end(), tgt.begin() + 3L * A.v_off[i]);
+            std::vector<unsigned char> fz(A.V, 0);
+            rc |= upload(c, A.dtgt, tgt);
+            rc |= upload(c, A.dfix, fz);
+        } else {
+            A.dtgt = nullptr;
+            A.dfix = nullptr;
+        }
+        std::vector<double> zs(nI, 0.0);
+        rc |= upload(c, A.dstiff, zs);
+    }
     rc |= upload(c, A.vinst, vinst);
     rc |= upload(c, A.tet, tetv);
     rc |= upload(c, A.IB, IB);
@@ -1117,6 +1206,90 @@ static void collect_stats(idp_ctx* c, long long launches0) {
     W.stats.kernel_launches += g_launch_count - launches0;
 }
 
+// Dirichlet conditions at the start of a step of the instances in `which`
+// (IMPLICIT_EULER.h:305-401): a DBC vertex whose target is its position is
+// fixed; when some have to move, the CCD step of their displacement (every
+// other vertex still) decides: alpha = 1 moves them onto their targets,
+// alpha < 1 leaves them where they are and turns the penalty
+// stiff/2 sum m |t - x|^2 on with stiff = 1e6, projecting only the fixed
+// vertices. The active mask is `which` on return.
+int dbc_stage(idp_ctx* c, const std::vector<unsigned char>& which) {
+    Arena& A = c->A;
+    Work& W = c->W;
+    const int nI = A.nI;
+    cudaStream_t s = c->s;
+    int rc;
+    std::vector<unsigned char> tm(nI, 0);
+    bool anyt = false;
+    for (int i = 0; i < nI; ++i) {
+        if (!which[i] || c->inst[i].dbc_list.empty()) continue;
+        if ((rc = set_projection(c, i, false))) return rc;  // every DBC vertex, unless the penalty turns on
+        if (!c->inst[i].dbc_tgt.empty()) {
+            tm[i] = 1;
+            anyt = true;
+        }
+    }
+    if (anyt) {
+        if ((rc = set_mask(c, tm))) return rc;
+        IDP_CUDA_TRY(cudaMemsetAsync(isc(c, SI_KFLAG), 0, sizeof(int) * nI, s));
+        if ((rc = dbc_classify(A, A.X, A.dir, isc(c, SI_KFLAG), s))) return rc;
+        std::vector<int> mv;
+        if ((rc = fetch(c, isc(c, SI_KFLAG), mv))) return rc;
+        std::vector<unsigned char> mm(nI, 0);
+        bool anym = false;
+        for (int i = 0; i < nI; ++i)
+            if (tm[i] && mv[i]) {
+                mm[i] = 1;
+                anym = true;
+            }
+        if (anym) {
+            if ((rc = set_mask(c, mm))) return rc;
+            std::vector<double> alpha(nI, 1.0);
+            std::vector<int> fl;
+            IDP_CUDA_TRY(cudaMemcpyAsync(A.alpha, alpha.data(), sizeof(double) * nI, cudaMemcpyHostToDevice, s));
+            W.timer.start(PhaseTimer::CCD, s);
+            rc = ccd_stepsize(A, W, A.X, A.dir, A.alpha, isc(c, SI_CCDF), s);
+            W.timer.stop(s);
+            if (rc) return rc;
+            IDP_CUDA_TRY(cudaMemcpyAsync(alpha.data(), A.alpha, sizeof(double) * nI, cudaMemcpyDeviceToHost, s));
+            if ((rc = fetch(c, isc(c, SI_CCDF), fl))) return rc;
+            std::vector<unsigned char> snap(nI, 0), pen(nI, 0);
+            bool anys = false, anyp = false;
+            for (int i = 0; i < nI; ++i) {
+                if (!mm[i]) continue;
+                if (fl[i] & 2) {  // no feasible step for the DBC (the reference exits)
+                    c->st[i].status = IDP_ERR_ZERO_STEP;
+                    c->st[i].active = false;
+                } else if (alpha[i] == 1.0) {
+                    snap[i] = 1;
+                    anys = true;
+                } else {
+                    pen[i] = 1;
+                    anyp = true;
+                    c->st[i].dbc_stiff = 1e6;
+                }
+            }
+            if (anys) {
+                if ((rc = set_mask(c, snap))) return rc;
+                if ((rc = dbc_snap(A, A.X, s))) return rc;
+            }
+            if (anyp) {
+                if ((rc = upload_dbc_stiff(c))) return rc;
+                if ((rc = set_mask(c, pen))) return rc;
+                if ((rc = dbc_sums(A, W, A.X, dsc(c, S_EDBC), dsc(c, S_DDBC), s))) return rc;
+                std::vector<double> d2;
+                if ((rc = fetch(c, dsc(c, S_DDBC), d2))) return rc;
+                for (int i = 0; i < nI; ++i)
+                    if (pen[i]) {
+                        c->st[i].dbc_pen0 = d2[i];
+                        if ((rc = set_projection(c, i, true))) return rc;
+                    }
+            }
+        }
+    }
+    return set_mask(c, which);
+}
+
 // Start one implicit-Euler step of the instances in `which` (the others keep
 // their state): x^n = x, predictor x_tilde = x + h v (+ h^2 M^-1 b with a body
 // force; IMPLICIT_EULER.h:195-216; a flow-mode shell's velocity is zeroed
@@ -1160,9 +1333,11 @@ int step_begin(idp_ctx* c, const std::vector<unsigned char>& which) {
         S.finalized = false;
         S.min_alpha = 1.0;
     }
+    if ((rc = upload_dbc_stiff(c))) return rc;
     std::vector<double> kap(nI);
     for (int i = 0; i < nI; ++i) kap[i] = st[i].kappa;
     IDP_CUDA_TRY(cudaMemcpyAsync(A.kappa, kap.data(), sizeof(double) * nI, cudaMemcpyHostToDevice, s));
+    if (A.dtgt && (rc = dbc_stage(c, which))) return rc;
     W.timer.start(PhaseTimer::CONTACT, s);
     rc = build_constraint_set(A, W, A.X, c->cs, s);
     W.timer.stop(s);
@@ -1390,6 +1565,8 @@ int step_iterate(idp_ctx* c, int max_iters, idp_result* results, int* n_active) 
                                            dsc(c, S_MIND), s)))
                 return rc;
             if ((rc = barrier_energy(A, W, A.X, c->cs, dsc(c, S_EBAR), isc(c, SI_BADB), s))) return rc;
+            const bool dpen = dbc_penalty_on(c);
+            if (dpen && (rc = dbc_sums(A, W, A.X, dsc(c, S_EDBC), dsc(c, S_DDBC), s))) return rc;
             InstScalars sc;
             if ((rc = fetch_scalars(c, sc))) return rc;
             const double t2 = c->P.thickness * c->P.thickness;
@@ -1403,7 +1580,8 @@ int step_iterate(idp_ctx* c, int max_iters, idp_result* results, int* n_active) 
                     alpha[i] /= 2;  // safe guard backtrack (IMPLICIT_EULER.h:120-129)
                     continue;
                 }
-                const double Ei = sc.d(S_ETET, i) + sc.d(S_EINERT, i) + sc.d(S_EBAR, i);
+                double Ei = sc.d(S_ETET, i) + sc.d(S_EINERT, i) + sc.d(S_EBAR, i);
+                if (dpen && st[i].dbc_stiff > 0) Ei += 0.5 * st[i].dbc_stiff * sc.d(S_EDBC, i);
                 bool ok = sc.flag(SI_BADB, i) == 0 && std::isfinite(Ei) && !(Ei > st[i].Eprev);
                 alpha[i] /= 2.0;
                 if (ok) {
@@ -1456,6 +1634,7 @@ int step_iterate(idp_ctx* c, int max_iters, idp_result* results, int* n_active) 
                                   W[W_PREV_DIST2].as<double>(), c->prevC, isc(c, SI_KFLAG), s)))
                 return rc;
         if ((rc = vec_dir_norm2(A, W, A.dir, dsc(c, S_NORM2), s))) return rc;
+        if (dbc_penalty_on(c) && (rc = dbc_sums(A, W, A.X, dsc(c, S_EDBC), dsc(c, S_DDBC), s))) return rc;
         InstScalars ksc;
         if ((rc = fetch_scalars(c, ksc))) return rc;
         if (have_prev && c->prevC > 0) {
@@ -1481,6 +1660,8 @@ int step_iterate(idp_ctx* c, int max_iters, idp_result* results, int* n_active) 
         for (int i = 0; i < nI; ++i)
             if (mask[i]) st[i].have_prev = true;
         // ---- stopping criterion (IMPLICIT_EULER.h:647-676, 759, 855)
+        std::vector<unsigned char> dbc_new(nI, 0);
+        bool any_dbc_new = false;
         for (int i = 0; i < nI; ++i) {
             if (!mask[i]) continue;
             InstState& S = st[i];
@@ -1494,6 +1675,26 @@ int step_iterate(idp_ctx* c, int max_iters, idp_result* results, int* n_active) 
             if (S.use_gd) L2m = c->P.newton_tol * 10;
             // switch to gradient descent after a vanishing step (IMPLICIT_EULER.h:682-699)
             S.use_gd = (S.alpha < 1e-8 && S.feasible_alpha > 1e-8);
+            if (S.dbc_stiff > 0) {
+                // moving DBC (IMPLICIT_EULER.h:701-757): until the DBC vertices
+                // have covered 99 % of their way, keep iterating and double the
+                // penalty whenever the solve has settled; then drop it and
+                // project every DBC vertex where it is
+                const double progress = 1 - std::sqrt(ksc.d(S_DDBC, i) / S.dbc_pen0);
+                if (progress < 0.99) {
+                    if (L2m < c->P.newton_tol * 10 && S.dbc_stiff < 1e8) {
+                        S.dbc_stiff *= 2;
+                        dbc_new[i] = 1;
+                        any_dbc_new = true;
+                    }
+                    L2m = c->P.newton_tol * 10;
+                } else {
+                    S.dbc_stiff = 0;
+                    dbc_new[i] = 1;
+                    any_dbc_new = true;
+                    if ((rc = set_projection(c, i, false))) return rc;
+                }
+            }
             if (S.status == IDP_ERR_ZERO_STEP || S.status == IDP_ERR_NONPOSITIVE_DIST ||
                 S.status == IDP_ERR_INTERSECTION)
                 S.active = false;
@@ -1505,6 +1706,13 @@ int step_iterate(idp_ctx* c, int max_iters, idp_result* results, int* n_active) 
                 S.active = false;  // flow mode without contacts: one Newton step (IMPLICIT_EULER.h:850-854)
             }
             if (!S.active) S.latency_ms = since_ms(c->t_begin);
+        }
+        if (any_dbc_new) {  // the energy with the new penalty (IMPLICIT_EULER.h:726-755)
+            if ((rc = upload_dbc_stiff(c))) return rc;
+            if ((rc = set_mask(c, dbc_new))) return rc;
+            if ((rc = eval_energy(c, A.X, true, E, bad))) return rc;
+            for (int i = 0; i < nI; ++i)
+                if (dbc_new[i]) st[i].Eprev = E[i];
         }
     }
     // instances that stopped (in this call, or already at the step's begin):
@@ -1527,6 +1735,14 @@ int step_iterate(idp_ctx* c, int max_iters, idp_result* results, int* n_active) 
     if (any_fin) {
         if ((rc = set_mask(c, fin))) return rc;
         if ((rc = vec_velocity(A, A.X, A.Xn, h, c->vel.as<double>(), s))) return rc;
+        bool drop = false;
+        for (int i = 0; i < nI; ++i)
+            if (fin[i] && st[i].dbc_stiff > 0) {  // a step cut short by the iteration cap
+                st[i].dbc_stiff = 0;
+                drop = true;
+                if ((rc = set_projection(c, i, false))) return rc;
+            }
+        if (drop && (rc = upload_dbc_stiff(c))) return rc;
     }
     W.timer.stop(s);
     IDP_CUDA_TRY(cudaStreamSynchronize(s));
@@ -1556,6 +1772,7 @@ int step_iterate(idp_ctx* c, int max_iters, idp_result* results, int* n_active) 
 
 int snapshot_instance(idp_ctx* c, int i, InstSnapshot& out) {
     if (!c || !c->committed || i < 0 || i >= c->A.nI) return IDP_ERR_INVALID_ARG;
+    if (c->st[i].dbc_stiff > 0) return IDP_ERR_STATE;  // the penalty's projection is not carried over
     const long o = 3L * c->A.v_off[i], n = 3L * c->inst[i].V;
     out.st = c->st[i];
     out.X.resize(n);

@@ -27,7 +27,8 @@ struct HostInstance {
     std::vector<double> X, X0, mass, lam, mu, v, xtilde;
     std::vector<int> tets;      // 4T, local ids
     std::vector<unsigned char> dbc;
-    std::vector<double> dbc_pos;  // 3V (only entries with dbc set are read)
+    std::vector<int> dbc_list;      // DBC vertices in the order given (the reference's DBC rows)
+    std::vector<double> dbc_tgt;    // 3V target positions of the DBC vertices (empty: all fixed)
     bool has_xtilde = false;
     double dHat2 = 0, kappa = 0, kappa_max = 0;
     // surface in reference order (local ids)
@@ -65,6 +66,8 @@ struct InstState {
     double g0 = 0;             // gradient norm at the first Newton iteration
     bool have_prev = false;    // a previous iterate's constraint set exists (kappa test)
     bool finalized = true;     // stopped and its velocity written
+    double dbc_stiff = 0;      // penalty stiffness of moving DBC (0: off, IMPLICIT_EULER.h:384-401)
+    double dbc_pen0 = 0;       // sum |target - x^n|^2 over the DBC rows at the step's start
     double latency_ms = 0;     // host time from the step's begin until it stopped
     int ncons = 0;             // constraint-set size at its latest iterate
 };
@@ -87,7 +90,11 @@ struct Arena {
     // ---- device, per vertex (3V doubles unless noted)
     double *X = nullptr, *X0 = nullptr, *Xn = nullptr, *Xtilde = nullptr, *Xprev = nullptr, *mass = nullptr;
     double *g = nullptr, *dir = nullptr;          // gradient, Newton direction (3V)
-    unsigned char* dbc = nullptr;                 // V
+    unsigned char* dbc = nullptr;                 // V: rows projected to the identity (Project_DBC)
+    unsigned char* dbc_excl = nullptr;            // V: every DBC vertex (exclusions, skipped elements)
+    double* dtgt = nullptr;                       // 3V DBC targets, when some instance has them
+    unsigned char* dfix = nullptr;                // V: DBC vertex already at its target (step start)
+    double* dstiff = nullptr;                     // nI: moving-DBC penalty stiffness (0: off)
     int* vinst = nullptr;                         // V
     // ---- per tet
     int4* tet = nullptr;
@@ -383,6 +390,11 @@ int pcg_solve(Arena& A, Work& W, const ContactSet& cs, bool fp64, const double* 
 int vec_inertia(Arena& A, Work& W, const double* X, double* inst_E, double* g /*nullable*/, cudaStream_t s);
 int vec_axpy_trial(Arena& A, const double* Xprev, const double* dir, double* Xout, cudaStream_t s);
 int vec_zero_dbc(Arena& A, double* g, cudaStream_t s);
+// dirichlet.cu: moving Dirichlet conditions (the augmented Lagrangian)
+int dbc_classify(Arena& A, const double* X, double* dir, int* moving, cudaStream_t s);
+int dbc_snap(Arena& A, double* X, cudaStream_t s);
+int dbc_sums(Arena& A, Work& W, const double* X, double* inst_w, double* inst_d, cudaStream_t s);
+int dbc_gradient(Arena& A, const double* X, double* g, cudaStream_t s);
 int chunk_reduce(Arena& A, Work& W, const Chunk* chunks, int nchunks, const double* chunk_vals, double* inst_out,
                  cudaStream_t s);
 int chunk_reduce_off(Arena& A, const int* coff, const double* part, double* out, bool accumulate, cudaStream_t s);

@@ -384,13 +384,13 @@ int shell_energy(Arena& A, Work& W, const double* X, double w_h2, double* inst_E
     int rc = IDP_OK;
     if (A.Fm) {
         (::idp::count_launch(), k_membrane_energy<<<A.n_mface_chunks, kBlock, 0, s>>>(A.mface_chunks, A.active, X, A.mface,
-                                                                                      A.mem, A.dbc, w_h2, part));
+                                                                                      A.mem, A.dbc_excl, w_h2, part));
         rc = chunk_reduce_off(A, A.mface_chunk_off, part, inst_E, true, s);
         if (rc) return rc;
     }
     if (A.Hn) {
         (::idp::count_launch(), k_bending_energy<<<A.n_hinge_chunks, kBlock, 0, s>>>(A.hinge_chunks, A.active, X, A.hinge,
-                                                                                     A.hk, A.dbc, w_h2, part));
+                                                                                     A.hk, A.dbc_excl, w_h2, part));
         rc = chunk_reduce_off(A, A.hinge_chunk_off, part, inst_E, true, s);
     }
     return rc;
@@ -402,10 +402,10 @@ int shell_gradient(Arena& A, Work& W, const double* X, double w_h2, double* g, c
     double* gel = W[W_SHELL_GRAD].as<double>();
     if (A.Fm)
         (::idp::count_launch(), k_membrane_grad<<<grid_for(A.Fm), kBlock, 0, s>>>(A.Fm, A.finst, A.active, X, A.mface,
-                                                                                   A.mem, A.dbc, w_h2, gel));
+                                                                                   A.mem, A.dbc_excl, w_h2, gel));
     if (A.Hn)
         (::idp::count_launch(), k_bending_grad<<<grid_for(A.Hn), kBlock, 0, s>>>(A.Hn, A.Fm, A.hinst, A.active, X, A.hinge,
-                                                                                  A.hk, A.dbc, w_h2, gel));
+                                                                                  A.hk, A.dbc_excl, w_h2, gel));
     (::idp::count_launch(), k_grad_gather_shell<<<grid_for(A.V), kBlock, 0, s>>>(A.V, A.vinst, A.active, A.vshell_ptr,
                                                                                  A.vshell, gel, g));
     return cudaGetLastError() == cudaSuccess ? IDP_OK : IDP_ERR_CUDA;
@@ -420,18 +420,18 @@ int shell_hessian(Arena& A, Work& W, const double* X, double w_h2, bool fp64, cu
         double* base = W[W_TET_HESS].as<double>() + 90 * A.T;
         if (A.Fm)
             (::idp::count_launch(), k_membrane_hess<double><<<grid_for(A.Fm, 64), 64, 0, s>>>(A.Fm, A.finst, A.active, X,
-                                                                                             A.mface, A.mem, A.dbc, w_h2, base));
+                                                                                             A.mface, A.mem, A.dbc_excl, w_h2, base));
         if (A.Hn)
             (::idp::count_launch(), k_bending_hess<double><<<grid_for(A.Hn, 64), 64, 0, s>>>(A.Hn, A.Fm, A.hinst, A.active, X,
-                                                                                            A.hinge, A.hk, A.dbc, w_h2, base));
+                                                                                            A.hinge, A.hk, A.dbc_excl, w_h2, base));
     } else {
         float* base = W[W_TET_HESS].as<float>() + 90 * A.T;
         if (A.Fm)
             (::idp::count_launch(), k_membrane_hess<float><<<grid_for(A.Fm, 64), 64, 0, s>>>(A.Fm, A.finst, A.active, X,
-                                                                                            A.mface, A.mem, A.dbc, w_h2, base));
+                                                                                            A.mface, A.mem, A.dbc_excl, w_h2, base));
         if (A.Hn)
             (::idp::count_launch(), k_bending_hess<float><<<grid_for(A.Hn, 64), 64, 0, s>>>(A.Hn, A.Fm, A.hinst, A.active, X,
-                                                                                           A.hinge, A.hk, A.dbc, w_h2, base));
+                                                                                           A.hinge, A.hk, A.dbc_excl, w_h2, base));
     }
     return cudaGetLastError() == cudaSuccess ? IDP_OK : IDP_ERR_CUDA;
 }

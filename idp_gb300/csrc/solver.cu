@@ -38,6 +38,7 @@ __global__ void k_assemble_tet(long B, const int* __restrict__ src_ptr, const in
                                const int* __restrict__ colidx, const double* __restrict__ mass,
                                const unsigned char* __restrict__ dbc, const int* __restrict__ vinst,
                                const unsigned char* __restrict__ active, const double* __restrict__ fvol, double h,
+                               const double* __restrict__ dstiff, const unsigned char* __restrict__ excl,
                                T* __restrict__ val) {
     long b = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= B) return;
@@ -63,6 +64,12 @@ __global__ void k_assemble_tet(long B, const int* __restrict__ src_ptr, const in
     if (row == col) {
         T m = (T)mass[row];
         acc[0] += m; acc[4] += m; acc[8] += m;
+        // moving-DBC penalty stiff * m on the diagonal (Compute_DBC_Hessian,
+        // FEM/Shell/DIRICHLET.h:72-90)
+        if (excl[row] && dstiff[vinst[row]] > 0) {
+            T k = (T)(dstiff[vinst[row]] * mass[row]);
+            acc[0] += k; acc[4] += k; acc[8] += k;
+        }
     }
     if (dbc[row] || dbc[col]) {
 #pragma unroll
@@ -1121,14 +1128,14 @@ int assemble(Arena& A, Work& W, const ContactSet& cs, bool fp64, cudaStream_t s)
     const int* tcol = W[W_TAIL_COL].as<int>();
     if (fp64) {
         (::idp::count_launch(), k_assemble_tet<double><<<grid_for(A.B), kBlock, 0, s>>>(A.B, A.src_ptr, A.src, W[W_TET_HESS].as<double>(), A.brow,
-                                                                A.colidx, A.mass, A.dbc, A.vinst, A.active, A.fvol, A.h,
+                                                                A.colidx, A.mass, A.dbc, A.vinst, A.active, A.fvol, A.h, A.dstiff, A.dbc_excl,
                                                                 W[W_BSR_VAL].as<double>()));
         (::idp::count_launch(), k_diag_inv<double><<<grid_for(A.V), kBlock, 0, s>>>(A.V, A.diagblk, W[W_BSR_VAL].as<double>(), trp, tcol,
                                                             W[W_TAIL_VAL].as<double>(), A.dbc, A.vinst, A.active,
                                                             W[W_DIAG_INV].as<double>()));
     } else {
         (::idp::count_launch(), k_assemble_tet<float><<<grid_for(A.B), kBlock, 0, s>>>(A.B, A.src_ptr, A.src, W[W_TET_HESS].as<float>(), A.brow,
-                                                               A.colidx, A.mass, A.dbc, A.vinst, A.active, A.fvol, A.h,
+                                                               A.colidx, A.mass, A.dbc, A.vinst, A.active, A.fvol, A.h, A.dstiff, A.dbc_excl,
                                                                W[W_BSR_VAL].as<float>()));
         (::idp::count_launch(), k_diag_inv<float><<<grid_for(A.V), kBlock, 0, s>>>(A.V, A.diagblk, W[W_BSR_VAL].as<float>(), trp, tcol,
                                                            W[W_TAIL_VAL].as<float>(), A.dbc, A.vinst, A.active,

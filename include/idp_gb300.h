@@ -176,6 +176,20 @@ int idp_set_velocity(idp_ctx* ctx, int inst, const double* v);
 int idp_set_body_force(idp_ctx* ctx, int inst, const double* b);
 /* Current positions (3V), e.g. a warm start between frames. */
 int idp_set_positions(idp_ctx* ctx, int inst, const double* X);
+/* Targets of the instance's DBC vertices: 3 doubles per vertex of the dbc_idx
+ * list given when the instance was added, in that order (the reference's DBC
+ * rows (index, x, y, z), VECTOR_STORAGE<T, dim + 1>; FEM.Load_Dirichlet,
+ * BOUNDARY_CONDITION.h:175-197, refreshes them per frame). At the start of
+ * each following step (IMPLICIT_EULER.h:305-401) a DBC vertex whose target is
+ * its position is fixed; the others move onto their targets when the CCD step
+ * of that displacement is 1, and otherwise are pulled there inside the Newton
+ * loop by the penalty stiff/2 sum m |t - x|^2 (FEM/Shell/DIRICHLET.h), stiff
+ * starting at 1e6 and doubling (up to 1e8) whenever the solve settles, until
+ * the DBC vertices have covered 99 % of their way (:701-757); the step does
+ * not stop before that. NULL clears the targets (every DBC vertex fixed).
+ * Before or after idp_commit, not while a step is in flight; a dbc_idx list
+ * that names a vertex twice has no targets (-> IDP_ERR_INVALID_ARG). */
+int idp_set_dbc_targets(idp_ctx* ctx, int inst, const double* targets);
 
 /* Normal-flow predictor for one instance (inst >= 0) or all (inst = -1),
  * computed on the device from the current positions: every surface vertex

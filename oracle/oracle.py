@@ -381,6 +381,8 @@ class Problem:
     hinges: np.ndarray = None  # (Hn,4) hinge stencils of an elastic shell
     hinfo: np.ndarray = None  # (Hn,3) thetabar, ebar, hbar
     kbend: float = 0.0        # hinge stiffness k
+    dbc_rows: np.ndarray = None    # (R,) vertex of each DBC row, in the reference's row order
+    dbc_target: np.ndarray = None  # (R,3) DBC target positions: moving DBC (augmented Lagrangian)
 
     @property
     def flow(self):
@@ -439,8 +441,11 @@ def _gradient(pb, X, Xtilde, cons, info):
     return g
 
 
-def _hessian(pb, X, cons, info):
-    """Compute_IncPotential_Hessian (INC_POTENTIAL.h:277-395) as scipy CSR."""
+def _hessian(pb, X, cons, info, proj=None, dpen=None):
+    """Compute_IncPotential_Hessian (INC_POTENTIAL.h:277-395) as scipy CSR;
+    proj: the rows projected to the identity (default pb.dbc), dpen: a
+    per-vertex diagonal added to the Hessian (Compute_DBC_Hessian,
+    Shell/DIRICHLET.h:72-90)."""
     import scipy.sparse as sp
 
     n = X.size
@@ -478,18 +483,37 @@ def _hessian(pb, X, cons, info):
     R.append(np.arange(n))
     Cc.append(np.arange(n))
     Vv.append(np.repeat(pb.mass, 3))
+    if dpen is not None:
+        R.append(np.arange(n))
+        Cc.append(np.arange(n))
+        Vv.append(np.repeat(dpen, 3))
     H = sp.coo_matrix((np.concatenate(Vv), (np.concatenate(R), np.concatenate(Cc))), shape=(n, n)).tocsr()
     # Project_DBC (Math/CSR_MATRIX.h:130-141): DBC rows/cols -> identity
-    if pb.dbc.any():
-        m = np.repeat(pb.dbc.astype(bool), 3)
+    pm = pb.dbc if proj is None else proj
+    if pm.any():
+        m = np.repeat(pm.astype(bool), 3)
         keep = sp.diags((~m).astype(float))
         H = keep @ H @ keep + sp.diags(m.astype(float))
     return H.tocsr()
 
 
+def dbc_energy(pb, X, stiff):
+    """Compute_DBC_Energy (Shell/DIRICHLET.h:26-45): stiff/2 sum m |t - x|^2
+    over the DBC rows."""
+    d = pb.dbc_target - X[pb.dbc_rows]
+    return 0.5 * stiff * float(np.sum(pb.mass[pb.dbc_rows] * np.sum(d * d, axis=1)))
+
+
+def dbc_dist2(pb, X):
+    """Compute_DBC_Dist2 (Shell/DIRICHLET.h:6-24): sum |t - x|^2 over the rows."""
+    d = pb.dbc_target - X[pb.dbc_rows]
+    return float(np.sum(d * d))
+
+
 def advance_one_step(pb: Problem, Xtilde=None, verbose=False, on_iter=None):
     """Advance_One_Step_IE_Discrete_Shell<double,3,false,false,false>
-    (FEM/Shell/IMPLICIT_EULER.h:151-891) for tets with fixed DBC, no friction.
+    (FEM/Shell/IMPLICIT_EULER.h:151-891) for tets or shells with fixed or
+    moving DBC (the augmented Lagrangian of :305-401, 701-757), no friction.
     Returns the Newton iteration count; pb.X and pb.v are updated.
     on_iter(it, Xprev, direction, ncons) is called after each accepted
     Newton step with the iterate the direction was computed at and the size
@@ -508,8 +532,43 @@ def advance_one_step(pb: Problem, Xtilde=None, verbose=False, on_iter=None):
     surf, dbc = pb.surf, pb.dbc
     nDBC = int(dbc.sum())
     X = pb.X
+    # ---- Dirichlet conditions (IMPLICIT_EULER.h:305-401): rows whose target
+    # is the current position are fixed; the others move by the CCD-safe
+    # fraction of their displacement, all the way (alpha = 1) or, when
+    # contact blocks the way, through the penalty stiff/2 sum m |t - x|^2
+    stiff, pen0 = 0.0, 0.0
+    proj = dbc
+    if pb.dbc_target is not None:
+        rows = np.asarray(pb.dbc_rows, np.int64)
+        nDBC = rows.size
+        disp = pb.dbc_target - X[rows]
+        fixed = np.zeros_like(dbc)
+        fixed[rows[~np.any(disp != 0, axis=1)]] = 1
+        dirn = np.zeros_like(X)
+        dirn[rows] = disp
+        dbc_alpha = 1.0
+        if np.any(disp != 0):
+            dbc_alpha, rc = ccd_stepsize(X, dirn.reshape(-1), surf, dbc, 1.0, pb.thickness)
+            if rc < 0:
+                raise RuntimeError("zero CCD step for the DBC")
+        pb.dbc_alpha = dbc_alpha
+        if dbc_alpha == 1:
+            X[rows] = pb.dbc_target
+        else:
+            stiff = 1e6
+            pen0 = dbc_dist2(pb, Xn)
+            proj = fixed
+    dpen = None
     cons, info = constraint_set(X, pb.X0, surf, dbc, pb.dHat2, pb.thickness)
-    Eprev = _energy(pb, X, Xtilde, True, cons, info)
+
+    def energy(Xe, barrier, c, i):
+        E = _energy(pb, Xe, Xtilde, barrier, c, i)
+        if E is not None and stiff:
+            E += dbc_energy(pb, Xe, stiff)
+        return E
+
+    Eprev = energy(X, True, cons, info)
+    progress_log = []
     res_record = deque()
     it = 0
     use_gd = False
@@ -517,11 +576,18 @@ def advance_one_step(pb: Problem, Xtilde=None, verbose=False, on_iter=None):
     stats = dict(ls_trials=0, ccd_calls=0, alphas=[], t_solve=0.0)
     while True:
         g = _gradient(pb, X, Xtilde, cons, info)
-        if nDBC:
-            g.reshape(-1, 3)[dbc.astype(bool)] = 0
+        if stiff:  # Compute_DBC_Gradient (Shell/DIRICHLET.h:47-70)
+            gr = g.reshape(-1, 3)
+            gr[pb.dbc_rows] += stiff * pb.mass[pb.dbc_rows, None] * (X[pb.dbc_rows] - pb.dbc_target)
+            dpen = np.zeros(X.shape[0])
+            dpen[pb.dbc_rows] = stiff * pb.mass[pb.dbc_rows]
+        else:
+            dpen = None
+        if proj.any():
+            g.reshape(-1, 3)[proj.astype(bool)] = 0
         rhs = -g
         if not use_gd:
-            Hm = _hessian(pb, X, cons, info)
+            Hm = _hessian(pb, X, cons, info, proj=proj, dpen=dpen)
             t0 = time.perf_counter()
             sol = cholesky.solve_spd(Hm, rhs, X)  # Solve_Direct (DIRECT_SOLVER.h:13-65)
             stats["t_solve"] += time.perf_counter() - t0
@@ -537,7 +603,7 @@ def advance_one_step(pb: Problem, Xtilde=None, verbose=False, on_iter=None):
         alpha = 1.0
         while True:
             Xt = Xprev + alpha * p
-            if _energy(pb, Xt, Xtilde, False, cons, info) is not None:
+            if energy(Xt, False, cons, info) is not None:
                 break
             alpha /= 2.0
         stats["ccd_calls"] += 1
@@ -549,7 +615,7 @@ def advance_one_step(pb: Problem, Xtilde=None, verbose=False, on_iter=None):
         while True:
             stats["ls_trials"] += 1
             Xt = Xprev + alpha * p
-            E = _energy(pb, Xt, Xtilde, False, cons, info)
+            E = energy(Xt, False, cons, info)
             valid = E is not None
             if valid:
                 cons, info = constraint_set(Xt, pb.X0, surf, dbc, pb.dHat2, pb.thickness)
@@ -559,7 +625,7 @@ def advance_one_step(pb: Problem, Xtilde=None, verbose=False, on_iter=None):
                         alpha /= 2
                         E = Eprev + 1
                         continue
-                E = _energy(pb, Xt, Xtilde, True, cons, info)
+                E = energy(Xt, True, cons, info)
             alpha /= 2.0
             if valid and not (E > Eprev):
                 break
@@ -572,7 +638,7 @@ def advance_one_step(pb: Problem, Xtilde=None, verbose=False, on_iter=None):
             upd = bool(np.any((dist2_prev < 1e-18) & (cur < dist2_prev)))
             if upd and pb.kappa[0] < pb.kappa[1]:
                 pb.kappa[0] *= 2
-                Eprev = _energy(pb, X, Xtilde, True, cons, info)
+                Eprev = energy(X, True, cons, info)
         dist2 = min_dist2(cons, X, pb.thickness)[1] if cons.shape[0] else np.zeros(0)
         cons_prev, dist2_prev = cons.copy(), dist2
         # ---- stopping criterion (IMPLICIT_EULER.h:647-676, 759, 855)
@@ -589,7 +655,20 @@ def advance_one_step(pb: Problem, Xtilde=None, verbose=False, on_iter=None):
             use_gd = True
         else:
             use_gd = False
-        pb.log.append(dict(it=it, E=Eprev, res=L2, alpha=alpha * 2, ncons=int(cons.shape[0]), kappa=pb.kappa[0]))
+        if stiff:  # augmented Lagrangian progress (IMPLICIT_EULER.h:701-757)
+            progress = 1 - math.sqrt(dbc_dist2(pb, X) / pen0)
+            progress_log.append((it, progress, stiff))
+            if progress < 0.99:
+                if L2m < pb.tol * 10 and stiff < 1e8:
+                    stiff *= 2
+                    Eprev = energy(X, True, cons, info)
+                L2m = pb.tol * 10
+            else:
+                stiff = 0.0
+                proj = dbc
+                Eprev = energy(X, True, cons, info)
+        pb.log.append(dict(it=it, E=Eprev, res=L2, alpha=alpha * 2, ncons=int(cons.shape[0]), kappa=pb.kappa[0],
+                           dbc_stiff=stiff))
         if on_iter is not None:
             on_iter(it, Xprev, sol, ncons_prev)
         if verbose:
@@ -599,6 +678,7 @@ def advance_one_step(pb: Problem, Xtilde=None, verbose=False, on_iter=None):
         if pb.flow and cons.shape[0] == 0:  # IMPLICIT_EULER.h:850-854
             break
     pb.v = (X - Xn) / h                     # IMPLICIT_EULER.h:882-888
+    stats["dbc_progress"] = progress_log
     pb.last_stats = stats
     pb.last_energy = Eprev
     return it

@@ -60,16 +60,15 @@ def test_reference_shaped_shim_rejects_unsupported_inputs(gpu_lib):
         FEM.DiscreteShell.Advance_One_Step_IE_Hinge(*args)
 
 
-def test_reference_shaped_shim_rejects_moving_dbc(gpu_lib):
-    """A DBC target away from the vertex's position is a moving DBC (the
-    reference's augmented Lagrangian), which this path does not solve: the
-    shim says so instead of fixing the vertex where it is."""
+def test_reference_shaped_shim_reads_dbc_rows(gpu_lib):
+    """DBC rows (index, x, y, z) give the vertex list and the targets (a
+    target away from the vertex's position is a moving DBC, solved by the
+    augmented Lagrangian); a bare index list has no targets."""
     import numpy as np
-    import pytest
-    from idp_gb300.api import _dbc_indices
+    from idp_gb300.api import _dbc_rows
 
-    X = np.arange(12, dtype=float).reshape(4, 3)
-    assert list(_dbc_indices(np.array([[1, 3.0, 4.0, 5.0]]), X)) == [1]
-    with pytest.raises(NotImplementedError):
-        _dbc_indices(np.array([[1, 3.0, 4.0, 5.5]]), X)
-    assert _dbc_indices(None, X) is None
+    idx, t = _dbc_rows(np.array([[1, 3.0, 4.0, 5.5], [3, 0.0, 1.0, 2.0]]))
+    assert list(idx) == [1, 3] and np.array_equal(t, [[3.0, 4.0, 5.5], [0.0, 1.0, 2.0]])
+    idx, t = _dbc_rows(np.array([2, 0]))
+    assert list(idx) == [2, 0] and t is None
+    assert _dbc_rows(None) == (None, None)

@@ -43,7 +43,7 @@ def test_hinge_call_matches_the_c_abi(gpu_lib):
     from idp_gb300 import api
     from idp_gb300.api import FEM
 
-    X, tets, tgt, pr = bar_case()
+    X, tets, tgt, pr = bar_case(ang=0.3)
     V = X.shape[0]
     h = 0.1
     v = (tgt - X) / h
@@ -123,8 +123,12 @@ def test_body_force_step_matches_oracle(oracle, gpu_lib):
 def test_kappa_adapts_like_the_oracle(oracle, gpu_lib, mode):
     """Two bars pressed together with a barrier a millionth of its usual
     stiffness: the bars close below 1e-9 and kappa doubles
-    (IMPLICIT_EULER.h:566-595) on the GPU exactly as often as in the oracle,
-    and the converged energies agree."""
+    (IMPLICIT_EULER.h:566-595) on the GPU as in the oracle. How often it
+    doubles depends on which iterate first brings a pair below 1e-18, a
+    last-bit matter along the trajectory, so the counts agree within a few
+    doublings; the GPU's result is a converged solution of the step at the
+    GPU's kappa: the oracle, started from it with that kappa, stops within a
+    few iterations at the GPU's energy within 1e-6."""
     import idp_gb300 as idp
 
     X, tets = cases.two_bars(gap=2e-3, seed=0)
@@ -139,15 +143,24 @@ def test_kappa_adapts_like_the_oracle(oracle, gpu_lib, mode):
     ctx.commit()
     rc, res = ctx.advance(check=False)
     assert rc == idp.IDP_OK, res
-    po = oracle.Problem(X=X.copy(), X0=X, tets=tets, mass=pr["mass"], lam=np.full(T, pr["lam"]),
-                        mu=np.full(T, pr["mu"]), h=0.1, dHat2=pr["dHat2"], kappa=[k0, pr["kappa_max"], 0.0],
-                        v=v.copy(), tol=1e-3, max_iters=300)
+    Xg, _, kap = ctx.state(0)
+
+    def problem(X1, kappa):
+        return oracle.Problem(X=X1.copy(), X0=X, tets=tets, mass=pr["mass"], lam=np.full(T, pr["lam"]),
+                              mu=np.full(T, pr["mu"]), h=0.1, dHat2=pr["dHat2"], kappa=kappa, v=v.copy(), tol=1e-3,
+                              max_iters=300)
+
+    po = problem(X, [k0, pr["kappa_max"], 0.0])
     oracle.advance_one_step(po)
-    assert po.kappa[0] / k0 >= 2 ** 8  # kappa did adapt
-    print(f"kappa doublings: GPU {math.log2(res[0]['kappa'] / k0):.0f}, oracle {math.log2(po.kappa[0] / k0):.0f}; "
-          f"iterations GPU {res[0]['newton_iters']}, oracle {len(po.log)}")
-    assert res[0]["kappa"] == po.kappa[0]
-    assert abs(res[0]["energy"] - po.last_energy) <= 1e-6 * abs(po.last_energy)
+    dg, do = math.log2(res[0]["kappa"] / k0), math.log2(po.kappa[0] / k0)
+    # from the GPU's result, kappa held at the GPU's value
+    pw = problem(Xg, [kap[0], kap[0], 0.0])
+    its = oracle.advance_one_step(pw, Xtilde=X + 0.1 * v)
+    rel = abs(res[0]["energy"] - pw.last_energy) / abs(pw.last_energy)
+    print(f"kappa doublings: GPU {dg:.0f}, oracle {do:.0f}; iterations GPU {res[0]['newton_iters']}, oracle "
+          f"{len(po.log)}; oracle from the GPU result {its} iterations, rel energy {rel:.2e}")
+    assert dg >= 8 and do >= 8 and abs(dg - do) <= 3
+    assert its <= 10 and rel <= 1e-6
     ctx.close()
 
 
