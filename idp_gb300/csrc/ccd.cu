@@ -192,11 +192,23 @@ __device__ double cta_tree_sum(const double* x, long n, double* scratch) {
 // thread, 3 Sn dependent additions) only when a fixed-order estimate of the
 // span is within the two sums' rounding-error bound ((n + 32) u) of 1 or
 // above it.
+// voxel size per instance: the mean surface edge length at X, summed in the
+// reference's order (SPATIAL_HASH.h:455-465, Eigen's mean())
+__global__ void k_mean_edge(int nI, const int* __restrict__ se_off, const double* __restrict__ len,
+                            double* __restrict__ voxel_size) {
+    __shared__ double buf[2][kStageTile];
+    const int i = blockIdx.x;
+    const long e0 = se_off[i], ne = se_off[i + 1] - se_off[i];
+    const double es = cta_eigen_sum(len + e0, ne, buf);
+    if (threadIdx.x == 0) voxel_size[i] = ne ? 1.0 * (es / (double)ne) : 1.0;
+}
+
 __global__ void k_span_cap(int nI, const unsigned char* __restrict__ active, const int* __restrict__ se_off,
                            const int* __restrict__ sn_off, const int* __restrict__ tile_off,
                            const double* __restrict__ tsum, const double* __restrict__ len,
                            const double* __restrict__ absdir, double* __restrict__ scratch,
-                           double* __restrict__ alpha, double* __restrict__ voxel_size) {
+                           double* __restrict__ alpha, double* __restrict__ voxel_size,
+                           const double* __restrict__ voxel_pre) {
     __shared__ double buf[2][kStageTile];
     __shared__ double s_vsz, s_est;
     int i = blockIdx.x;
@@ -206,11 +218,11 @@ __global__ void k_span_cap(int nI, const unsigned char* __restrict__ active, con
     const int tn0 = tile_off[2 * i + 1], tn1 = tile_off[2 * i + 2];
     const int ntn = tn1 - tn0;
     double* sc = scratch + 2 * (long)tile_off[2 * i] + 8 * (long)i;
-    const double es = cta_eigen_sum(len + e0, ne, buf);
+    const double es = voxel_pre ? 0.0 : cta_eigen_sum(len + e0, ne, buf);
     const double ps = ntn == 0 ? 0.0 : (ntn == 1 ? tsum[tn0] : cta_tree_sum(tsum + tn0, ntn, sc));
     const double cnt = (double)(nn * 3);
     if (threadIdx.x == 0) {
-        s_vsz = ne ? 1.0 * (es / (double)ne) : 1.0;
+        s_vsz = voxel_pre ? voxel_pre[i] : (ne ? 1.0 * (es / (double)ne) : 1.0);
         s_est = alpha[i] * (ps / cnt) / s_vsz;
     }
     __syncthreads();
@@ -681,7 +693,23 @@ __global__ void k_fill(int n, double v, double* a) {
 
 }  // namespace
 
-int ccd_stepsize(Arena& A, Work& W, const double* X, const double* dir, double* alpha, int* flags, cudaStream_t s) {
+int ccd_voxel_size(Arena& A, Work& W, const double* X, cudaStream_t s) {
+    const int nI = A.nI;
+    const long Se = A.Se > 0 ? A.Se : 1;
+    if (W[W_CCD_VOX].ensure(sizeof(double) * (Se + nI + 8))) return IDP_ERR_CUDA;
+    double* len = W[W_CCD_VOX].as<double>() + nI;
+    if (A.Se) (::idp::count_launch(), k_edge_len<<<grid_for(A.Se), kBlock, 0, s>>>(A.Se, A.sedge, X, len));
+    (::idp::count_launch(), k_mean_edge<<<nI, 256, 0, s>>>(nI, A.d_se_off, len, W[W_CCD_VOX].as<double>()));
+    return cudaGetLastError() == cudaSuccess ? IDP_OK : IDP_ERR_CUDA;
+}
+
+const double* ccd_voxel_sizes(Arena& A, Work& W) {
+    (void)A;
+    return W[W_CCD_VOX].as<double>();
+}
+
+int ccd_stepsize(Arena& A, Work& W, const double* X, const double* dir, double* alpha, int* flags, cudaStream_t s,
+                 const double* voxel_pre) {
     const int nI = A.nI;
     long Se = A.Se > 0 ? A.Se : 1, Sn = A.Sn > 0 ? A.Sn : 1;
     // scratch layout (doubles): len[Se] | absdir[3Sn] | sum scratch | voxel[nI] | amin[nI]
@@ -694,14 +722,14 @@ int ccd_stepsize(Arena& A, Work& W, const double* X, const double* dir, double* 
     double* amin = vsz + nI;
     const int* d_se_off = A.d_se_off;
     const int* d_sn_off = A.d_sn_off;
-    if (A.Se) (::idp::count_launch(), k_edge_len<<<grid_for(A.Se), kBlock, 0, s>>>(A.Se, A.sedge, X, len));
+    if (A.Se && !voxel_pre) (::idp::count_launch(), k_edge_len<<<grid_for(A.Se), kBlock, 0, s>>>(A.Se, A.sedge, X, len));
     if (A.Sn) (::idp::count_launch(), k_abs_dir<<<grid_for(A.Sn), kBlock, 0, s>>>(A.Sn, A.snode, dir, absdir));
     if (W[W_SPAN].ensure(sizeof(double) * (A.n_span_tiles + 1))) return IDP_ERR_CUDA;
     double* tsum = W[W_SPAN].as<double>();
     if (A.n_span_tiles > 0)
         (::idp::count_launch(), k_span_tiles<<<A.n_span_tiles, 256, 0, s>>>(A.span_tiles, A.active, absdir, tsum));
     (::idp::count_launch(), k_span_cap<<<nI, 256, 0, s>>>(nI, A.active, d_se_off, d_sn_off, A.span_tile_off, tsum,
-                                                          len, absdir, sumsc, alpha, vsz));
+                                                          len, absdir, sumsc, alpha, vsz, voxel_pre));
     // grid
     if (W[W_BBOX].ensure(sizeof(unsigned long long) * 6 * nI) || W[W_GRIDP].ensure(sizeof(GridP) * nI))
         return IDP_ERR_CUDA;

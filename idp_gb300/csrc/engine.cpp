@@ -63,9 +63,14 @@ struct idp_ctx {
     DBuf snap;                // saved X and v (6V)
     std::vector<double> snap_kappa;
     bool has_snap = false;
+    DBuf stage;               // 3V doubles in the caller's vertex order (transfers across the interface)
     DBuf bacc;                // body-force accelerations M^-1 b (3V), when some instance has one
     bool has_bacc = false;
     bool stepping = false;    // a step is in flight (begun, instances still iterating)
+    // side stream: the CCD voxel size of an iteration's positions, computed
+    // while the gradient and Hessian of the same positions are
+    cudaStream_t s2 = nullptr;
+    cudaEvent_t ev_x = nullptr, ev_vox = nullptr;
     std::chrono::steady_clock::time_point t_begin;  // the step's begin (latency origin)
 };
 
@@ -211,6 +216,93 @@ int fetch_scalars(idp_ctx* c, InstScalars& out) {
     IDP_CUDA_TRY(cudaMemcpyAsync(out.buf.data(), c->inst_buf.p, sizeof(double) * S_NUMD * nI + sizeof(int) * S_NUMI * nI,
                                  cudaMemcpyDeviceToHost, c->s));
     IDP_CUDA_TRY(cudaStreamSynchronize(c->s));
+    return IDP_OK;
+}
+
+// Spatial order of an instance's vertices: Morton codes of the rest
+// positions quantized to 10 bits per axis over the instance's bounding box,
+// ties in the caller's order. perm[k] = caller index of device vertex k.
+std::vector<int> morton_order(const HostInstance& h) {
+    const int V = h.V;
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (int v = 0; v < V; ++v)
+        for (int d = 0; d < 3; ++d) {
+            lo[d] = std::min(lo[d], h.X0[3 * v + d]);
+            hi[d] = std::max(hi[d], h.X0[3 * v + d]);
+        }
+    const double ext = std::max(hi[0] - lo[0], std::max(hi[1] - lo[1], hi[2] - lo[2]));
+    const double sc = ext > 0 ? 1023.0 / ext : 0.0;
+    auto spread = [](uint64_t x) {
+        uint64_t r = 0;
+        for (int b = 0; b < 10; ++b) r |= ((x >> b) & 1ull) << (3 * b);
+        return r;
+    };
+    std::vector<std::pair<uint64_t, int>> key(V);
+    for (int v = 0; v < V; ++v) {
+        uint64_t q[3];
+        for (int d = 0; d < 3; ++d) {
+            double t = (h.X0[3 * v + d] - lo[d]) * sc;
+            q[d] = (uint64_t)std::min(1023.0, std::max(0.0, std::floor(t)));
+        }
+        key[v] = {spread(q[0]) | (spread(q[1]) << 1) | (spread(q[2]) << 2), v};
+    }
+    std::sort(key.begin(), key.end());
+    std::vector<int> perm(V);
+    for (int k = 0; k < V; ++k) perm[k] = key[k].second;
+    return perm;
+}
+
+// copy of an instance with its vertices in device order `perm`: per-vertex
+// arrays gathered, vertex ids in element, surface and DBC lists renamed
+// (the lists keep their order)
+HostInstance to_device_order(const HostInstance& h, const std::vector<int>& perm) {
+    HostInstance d = h;
+    const int V = h.V;
+    std::vector<int> ip(V);
+    for (int k = 0; k < V; ++k) ip[perm[k]] = k;
+    auto g3 = [&](const std::vector<double>& a, std::vector<double>& o) {
+        if (a.size() != 3 * (size_t)V) return;
+        for (int k = 0; k < V; ++k)
+            for (int j = 0; j < 3; ++j) o[3 * k + j] = a[3 * (size_t)perm[k] + j];
+    };
+    g3(h.X, d.X);
+    g3(h.X0, d.X0);
+    g3(h.v, d.v);
+    g3(h.xtilde, d.xtilde);
+    g3(h.bacc, d.bacc);
+    g3(h.dbc_tgt, d.dbc_tgt);
+    for (int k = 0; k < V; ++k) {
+        d.mass[k] = h.mass[perm[k]];
+        d.dbc[k] = h.dbc[perm[k]];
+    }
+    for (auto* a : {&d.tets, &d.faces, &d.hinges, &d.tris, &d.edges, &d.nodes, &d.dbc_list})
+        for (int& v : *a) v = ip[v];
+    d.perm = perm;
+    return d;
+}
+
+// 3-vectors of instance i between the caller and the device: in device
+// order at dst (+ the instance's offset) from the caller's host array src
+int upload3(idp_ctx* c, int i, const double* src, double* dst) {
+    const long o = 3L * c->A.v_off[i], n = 3L * c->inst[i].V;
+    if (c->inst[i].perm.empty()) {
+        IDP_CUDA_TRY(cudaMemcpyAsync(dst + o, src, sizeof(double) * n, cudaMemcpyHostToDevice, c->s));
+        return IDP_OK;
+    }
+    IDP_CUDA_TRY(cudaMemcpyAsync(c->stage.as<double>() + o, src, sizeof(double) * n, cudaMemcpyHostToDevice, c->s));
+    return perm_to_device(c->A, c->A.v_off[i], c->inst[i].V, c->stage.as<double>(), dst, c->s);
+}
+
+// ... and back: the caller's host array dst from device-order src
+int download3(idp_ctx* c, int i, const double* src, double* dst) {
+    const long o = 3L * c->A.v_off[i], n = 3L * c->inst[i].V;
+    if (c->inst[i].perm.empty()) {
+        IDP_CUDA_TRY(cudaMemcpyAsync(dst, src + o, sizeof(double) * n, cudaMemcpyDeviceToHost, c->s));
+        return IDP_OK;
+    }
+    int rc = perm_to_caller(c->A, c->A.v_off[i], c->inst[i].V, src, c->stage.as<double>(), c->s);
+    if (rc) return rc;
+    IDP_CUDA_TRY(cudaMemcpyAsync(dst, c->stage.as<double>() + o, sizeof(double) * n, cudaMemcpyDeviceToHost, c->s));
     return IDP_OK;
 }
 
@@ -365,6 +457,7 @@ void idp_default_params(idp_params* p) {
     p->pcg_grid_cta_vertices = 0;
     p->contact_block_vertices = 0;
     p->verify_iterates = 0;
+    p->caller_vertex_order = 0;
 }
 
 const char* idp_status_str(int s) {
@@ -397,7 +490,15 @@ idp_ctx* idp_create(const idp_params* p, int* status) {
     c->W.grid_vper = c->P.pcg_grid_cta_vertices > 0 ? c->P.pcg_grid_cta_vertices : 112;
     c->W.cl_cap = c->P.contact_block_vertices > 0 ? std::max(2, std::min(c->P.contact_block_vertices, kClusterCap))
                                                   : kClusterCap;
-    if (cudaSetDevice(c->P.device) != cudaSuccess || cudaStreamCreateWithFlags(&c->s, cudaStreamNonBlocking) != cudaSuccess) {
+    int prio_lo = 0, prio_hi = 0;
+    if (cudaSetDevice(c->P.device) != cudaSuccess || cudaStreamCreateWithFlags(&c->s, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi) != cudaSuccess ||
+        cudaStreamCreateWithPriority(&c->s2, cudaStreamNonBlocking, prio_hi) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_x, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_vox, cudaEventDisableTiming) != cudaSuccess) {
+        if (c->s) cudaStreamDestroy(c->s);
+        if (c->s2) cudaStreamDestroy(c->s2);
+        if (c->ev_x) cudaEventDestroy(c->ev_x);
         delete c;
         if (status) *status = IDP_ERR_CUDA;
         return nullptr;
@@ -410,12 +511,16 @@ void idp_destroy(idp_ctx* c) {
     if (!c) return;
     cudaSetDevice(c->P.device);
     cudaStreamSynchronize(c->s);
+    cudaStreamSynchronize(c->s2);
     for (auto& b : c->owned) b.release();
     c->W.release();
     c->inst_buf.release();
     c->vel.release();
     c->bacc.release();
     c->snap.release();
+    cudaEventDestroy(c->ev_x);
+    cudaEventDestroy(c->ev_vox);
+    cudaStreamDestroy(c->s2);
     cudaStreamDestroy(c->s);
     delete c;
 }
@@ -700,8 +805,8 @@ int idp_set_velocity(idp_ctx* c, int i, const double* v) {
     h.v.assign(v, v + 3 * (long)h.V);
     h.vel_set = true;
     if (c->committed) {
-        long o = 3L * c->A.v_off[i];
-        IDP_CUDA_TRY(cudaMemcpyAsync(c->vel.as<double>() + o, v, sizeof(double) * 3 * h.V, cudaMemcpyHostToDevice, c->s));
+        int rc = upload3(c, i, v, c->vel.as<double>());
+        if (rc) return rc;
         IDP_CUDA_TRY(cudaStreamSynchronize(c->s));
     }
     return IDP_OK;
@@ -730,10 +835,10 @@ int idp_set_body_force(idp_ctx* c, int i, const double* b) {
             IDP_CUDA_TRY(cudaMemsetAsync(c->bacc.p, 0, sizeof(double) * n, c->s));
             c->has_bacc = true;
         }
-        if (b)
-            IDP_CUDA_TRY(cudaMemcpyAsync(c->bacc.as<double>() + o, h.bacc.data(), sizeof(double) * 3 * h.V,
-                                         cudaMemcpyHostToDevice, c->s));
-        else
+        if (b) {
+            int rc = upload3(c, i, h.bacc.data(), c->bacc.as<double>());
+            if (rc) return rc;
+        } else
             IDP_CUDA_TRY(cudaMemsetAsync(c->bacc.as<double>() + o, 0, sizeof(double) * 3 * h.V, c->s));
         IDP_CUDA_TRY(cudaStreamSynchronize(c->s));
     }
@@ -758,8 +863,8 @@ int idp_set_positions(idp_ctx* c, int i, const double* X) {
     HostInstance& h = c->inst[i];
     h.X.assign(X, X + 3 * (long)h.V);
     if (c->committed) {
-        long o = 3L * c->A.v_off[i];
-        IDP_CUDA_TRY(cudaMemcpyAsync(c->A.X + o, X, sizeof(double) * 3 * h.V, cudaMemcpyHostToDevice, c->s));
+        int rc = upload3(c, i, X, c->A.X);
+        if (rc) return rc;
         IDP_CUDA_TRY(cudaStreamSynchronize(c->s));
     }
     return IDP_OK;
@@ -790,9 +895,10 @@ int idp_set_dbc_targets(idp_ctx* c, int i, const double* targets) {
     if (c->committed) {
         if (!c->A.dtgt) return IDP_ERR_STATE;
         cudaSetDevice(c->P.device);
-        if (!h.dbc_tgt.empty())
-            IDP_CUDA_TRY(cudaMemcpyAsync(c->A.dtgt + 3L * c->A.v_off[i], h.dbc_tgt.data(), sizeof(double) * 3 * h.V,
-                                         cudaMemcpyHostToDevice, c->s));
+        if (!h.dbc_tgt.empty()) {
+            int rc = upload3(c, i, h.dbc_tgt.data(), c->A.dtgt);
+            if (rc) return rc;
+        }
         IDP_CUDA_TRY(cudaStreamSynchronize(c->s));
     }
     return IDP_OK;
@@ -814,8 +920,22 @@ int idp_commit(idp_ctx* c) {
     A.sn_off.assign(nI + 1, 0);
     A.se_off.assign(nI + 1, 0);
     A.st_off.assign(nI + 1, 0);
+    // device order of each instance's vertices (the caller's order is kept
+    // on the host; every transfer across the interface maps between them)
+    std::vector<HostInstance> dview(nI);
+    std::vector<const HostInstance*> hv(nI);
     for (int i = 0; i < nI; ++i) {
-        const HostInstance& h = c->inst[i];
+        c->inst[i].perm.clear();
+        if (!c->P.caller_vertex_order && c->inst[i].V > 1) {
+            dview[i] = to_device_order(c->inst[i], morton_order(c->inst[i]));
+            c->inst[i].perm = dview[i].perm;
+            hv[i] = &dview[i];
+        } else {
+            hv[i] = &c->inst[i];
+        }
+    }
+    for (int i = 0; i < nI; ++i) {
+        const HostInstance& h = *hv[i];
         A.v_off[i + 1] = A.v_off[i] + h.V;
         A.t_off[i + 1] = A.t_off[i] + h.T;
         A.f_off[i + 1] = A.f_off[i] + (int)h.fvol.size();
@@ -840,9 +960,11 @@ int idp_commit(idp_ctx* c) {
     std::vector<double> fvol, mem, hk;
     std::vector<int> mface, finst, hinst;
     std::vector<int4> tet, hinge;
+    std::vector<int> vsrc(A.V);
     for (int i = 0; i < nI; ++i) {
-        const HostInstance& h = c->inst[i];
+        const HostInstance& h = *hv[i];
         int vo = A.v_off[i];
+        for (int k = 0; k < h.V; ++k) vsrc[vo + k] = vo + (h.perm.empty() ? k : h.perm[k]);
         X.insert(X.end(), h.X.begin(), h.X.end());
         X0.insert(X0.end(), h.X0.begin(), h.X0.end());
         mass.insert(mass.end(), h.mass.begin(), h.mass.end());
@@ -916,12 +1038,12 @@ int idp_commit(idp_ctx* c) {
         // penalty stiffness, kept when some instance has DBC vertices
         bool any_dbc = false;
         std::vector<double> tgt;
-        for (int i = 0; i < nI; ++i) any_dbc |= !c->inst[i].dbc_list.empty();
+        for (int i = 0; i < nI; ++i) any_dbc |= !hv[i]->dbc_list.empty();
         if (any_dbc) {
             tgt = X;
             for (int i = 0; i < nI; ++i)
-                if (!c->inst[i].dbc_tgt.empty())
-                    std::copy(c->inst[i].dbc_tgt.begin(), c->inst[i].dbc_tgt.end(), tgt.begin() + 3L * A.v_off[i]);
+                if (!hv[i]->dbc_tgt.empty())
+                    std::copy(hv[i]->dbc_tgt.begin(), hv[i]->dbc_tgt.end(), tgt.begin() + 3L * A.v_off[i]);
             std::vector<unsigned char> fz(A.V, 0);
             rc |= upload(c, A.dtgt, tgt);
             rc |= upload(c, A.dfix, fz);
@@ -933,6 +1055,7 @@ int idp_commit(idp_ctx* c) {
         rc |= upload(c, A.dstiff, zs);
     }
     rc |= upload(c, A.vinst, vinst);
+    rc |= upload(c, A.vsrc, vsrc);
     rc |= upload(c, A.tet, tetv);
     rc |= upload(c, A.IB, IB);
     rc |= upload(c, A.vol, vol);
@@ -1151,11 +1274,12 @@ int idp_commit(idp_ctx* c) {
     // body-force accelerations (only when some instance has one)
     c->has_bacc = false;
     for (const HostInstance& h : c->inst) c->has_bacc |= !h.bacc.empty();
+    if (c->stage.ensure(sizeof(double) * 3 * (A.V + 1))) return IDP_ERR_CUDA;
     if (c->has_bacc) {
         std::vector<double> acc(3 * (size_t)A.V, 0.0);
         for (int i = 0; i < nI; ++i)
-            if (!c->inst[i].bacc.empty())
-                std::copy(c->inst[i].bacc.begin(), c->inst[i].bacc.end(), acc.begin() + 3L * A.v_off[i]);
+            if (!hv[i]->bacc.empty())
+                std::copy(hv[i]->bacc.begin(), hv[i]->bacc.end(), acc.begin() + 3L * A.v_off[i]);
         if (c->bacc.ensure(sizeof(double) * 3 * (A.V + 1)) ||
             cudaMemcpy(c->bacc.p, acc.data(), sizeof(double) * 3 * A.V, cudaMemcpyHostToDevice) != cudaSuccess)
             return IDP_ERR_CUDA;
@@ -1426,6 +1550,12 @@ int step_iterate(idp_ctx* c, int max_iters, idp_result* results, int* n_active) 
         }
         if (!any) break;
         if ((rc = set_mask(c, mask))) return rc;
+        // CCD voxel size at this iterate on the side stream (the CCD of the
+        // line search starts from these positions); joined before the PCG
+        IDP_CUDA_TRY(cudaEventRecord(c->ev_x, s));
+        IDP_CUDA_TRY(cudaStreamWaitEvent(c->s2, c->ev_x, 0));
+        if ((rc = ccd_voxel_size(A, W, A.X, c->s2))) return rc;
+        IDP_CUDA_TRY(cudaEventRecord(c->ev_vox, c->s2));
         // ---- gradient, Hessian, direction
         if ((rc = eval_gradient(c, A.X))) return rc;
         // inexact Newton: PCG tolerance per instance follows |g| / |g_0|
@@ -1458,6 +1588,7 @@ int step_iterate(idp_ctx* c, int max_iters, idp_result* results, int* n_active) 
             if ((rc = eval_hessian(c, A.X))) return rc;
             std::vector<int> its;
             std::vector<double> rel;
+            IDP_CUDA_TRY(cudaStreamWaitEvent(s, c->ev_vox, 0));  // the side stream is idle during the PCG
             if ((rc = pcg_solve(A, W, c->cs, fp64, A.g, A.dir, c->P.pcg_rel_tol, c->P.pcg_max_iters, its, rel, s,
                                  tol.data())))
                 return rc;
@@ -1494,6 +1625,7 @@ int step_iterate(idp_ctx* c, int max_iters, idp_result* results, int* n_active) 
         }
         if ((rc = set_mask(c, mask))) return rc;
         // ---- Line_Search (IMPLICIT_EULER.h:9-149)
+        IDP_CUDA_TRY(cudaStreamWaitEvent(s, c->ev_vox, 0));
         W.timer.start(PhaseTimer::LINESEARCH, s);
         IDP_CUDA_TRY(cudaMemcpyAsync(A.Xprev, A.X, sizeof(double) * 3 * A.V, cudaMemcpyDeviceToDevice, s));
         std::vector<double> alpha(nI, 1.0);
@@ -1519,7 +1651,7 @@ int step_iterate(idp_ctx* c, int max_iters, idp_result* results, int* n_active) 
         if ((rc = set_mask(c, mask))) return rc;
         IDP_CUDA_TRY(cudaMemcpyAsync(A.alpha, alpha.data(), sizeof(double) * nI, cudaMemcpyHostToDevice, s));
         W.timer.start(PhaseTimer::CCD, s);
-        rc = ccd_stepsize(A, W, A.Xprev, A.dir, A.alpha, isc(c, SI_CCDF), s);
+        rc = ccd_stepsize(A, W, A.Xprev, A.dir, A.alpha, isc(c, SI_CCDF), s, ccd_voxel_sizes(A, W));
         W.timer.stop(s);
         if (rc) return rc;
         hi.resize(nI);
@@ -1862,9 +1994,12 @@ int idp_get_state(idp_ctx* c, int i, double* X, double* v, double* kappa3) {
         if (kappa3) { kappa3[0] = h.kappa; kappa3[1] = h.kappa_max; kappa3[2] = 0; }
         return IDP_OK;
     }
-    long o = 3L * c->A.v_off[i], n = 3L * c->inst[i].V;
-    if (X) IDP_CUDA_TRY(cudaMemcpyAsync(X, c->A.X + o, sizeof(double) * n, cudaMemcpyDeviceToHost, c->s));
-    if (v) IDP_CUDA_TRY(cudaMemcpyAsync(v, c->vel.as<double>() + o, sizeof(double) * n, cudaMemcpyDeviceToHost, c->s));
+    int rc;
+    if (X) {
+        if ((rc = download3(c, i, c->A.X, X))) return rc;
+        IDP_CUDA_TRY(cudaStreamSynchronize(c->s));  // the staging buffer is reused below
+    }
+    if (v && (rc = download3(c, i, c->vel.as<double>(), v))) return rc;
     IDP_CUDA_TRY(cudaStreamSynchronize(c->s));
     if (kappa3) {
         kappa3[0] = c->st[i].kappa;
@@ -1920,8 +2055,7 @@ static int prep_one(idp_ctx* c, int i, const double* X) {
     m[i] = 1;
     int rc = set_mask(c, m);
     if (rc) return rc;
-    long o = 3L * c->A.v_off[i];
-    IDP_CUDA_TRY(cudaMemcpyAsync(c->A.Xprev + o, X, sizeof(double) * 3 * c->inst[i].V, cudaMemcpyHostToDevice, c->s));
+    if ((rc = upload3(c, i, X, c->A.Xprev))) return rc;
     // x_tilde from the instance's current positions and velocity
     rc = vec_xtilde(c->A, c->A.X, c->vel.as<double>(), c->P.h, c->A.Xtilde, c->s,
                     c->has_bacc ? c->bacc.as<double>() : nullptr);
@@ -1956,8 +2090,7 @@ int idp_eval_gradient(idp_ctx* c, int i, const double* X, double* g) {
     if (rc) return rc;
     if ((rc = build_constraint_set(c->A, c->W, c->A.Xprev, c->cs, c->s))) return rc;
     if ((rc = eval_gradient(c, c->A.Xprev))) return rc;
-    long o = 3L * c->A.v_off[i];
-    IDP_CUDA_TRY(cudaMemcpyAsync(g, c->A.g + o, sizeof(double) * 3 * c->inst[i].V, cudaMemcpyDeviceToHost, c->s));
+    if ((rc = download3(c, i, c->A.g, g))) return rc;
     IDP_CUDA_TRY(cudaStreamSynchronize(c->s));
     return IDP_OK;
 }
@@ -1975,9 +2108,12 @@ int idp_constraint_set(idp_ctx* c, int i, const double* X, int cap, int32_t* con
         IDP_CUDA_TRY(cudaStreamSynchronize(c->s));
         // device ids are arena-global; return instance-local ids, keeping the
         // sign tags (-v-1), the -1 markers and the -count multiplicity slot
+        // (and the caller's vertex numbering)
         int vo = c->A.v_off[i];
-        auto pos = [vo](int v) { return v - vo; };
-        auto tag = [vo](int v) { return -((-v - 1) - vo) - 1; };
+        const std::vector<int>& pm = c->inst[i].perm;
+        auto loc = [&pm](int k) { return pm.empty() ? k : pm[k]; };
+        auto pos = [vo, &loc](int v) { return loc(v - vo); };
+        auto tag = [vo, &loc](int v) { return -loc((-v - 1) - vo) - 1; };
         for (int k = 0; k < n; ++k) {
             int* q = cons + 4 * k;
             if (q[0] >= 0) {  // edge-edge family: every negative entry is a tagged vertex
@@ -2052,8 +2188,7 @@ int idp_ccd_stepsize(idp_ctx* c, int i, const double* X, const double* dir, doub
     int rc = prep_one(c, i, X);
     if (rc) return rc;
     if (!dir || !alpha) return IDP_ERR_INVALID_ARG;
-    long o = 3L * c->A.v_off[i];
-    IDP_CUDA_TRY(cudaMemcpyAsync(c->A.dir + o, dir, sizeof(double) * 3 * c->inst[i].V, cudaMemcpyHostToDevice, c->s));
+    if ((rc = upload3(c, i, dir, c->A.dir))) return rc;
     std::vector<double> a(c->A.nI, *alpha);
     IDP_CUDA_TRY(cudaMemcpyAsync(c->A.alpha, a.data(), sizeof(double) * c->A.nI, cudaMemcpyHostToDevice, c->s));
     if ((rc = ccd_stepsize(c->A, c->W, c->A.Xprev, c->A.dir, c->A.alpha, isc(c, SI_CCDF), c->s))) return rc;
@@ -2071,11 +2206,10 @@ int idp_hessian_apply(idp_ctx* c, int i, const double* X, const double* x, doubl
     if (rc) return rc;
     if ((rc = build_constraint_set(c->A, c->W, c->A.Xprev, c->cs, c->s))) return rc;
     if ((rc = eval_hessian(c, c->A.Xprev))) return rc;
-    long o = 3L * c->A.v_off[i], n = 3L * c->inst[i].V;
     IDP_CUDA_TRY(cudaMemsetAsync(c->A.dir, 0, sizeof(double) * 3 * c->A.V, c->s));
-    IDP_CUDA_TRY(cudaMemcpyAsync(c->A.dir + o, x, sizeof(double) * n, cudaMemcpyHostToDevice, c->s));
+    if ((rc = upload3(c, i, x, c->A.dir))) return rc;
     if ((rc = hessian_apply(c->A, c->W, c->P.mode == IDP_MODE_FP64, c->A.dir, c->A.g, c->s))) return rc;
-    IDP_CUDA_TRY(cudaMemcpyAsync(y, c->A.g + o, sizeof(double) * n, cudaMemcpyDeviceToHost, c->s));
+    if ((rc = download3(c, i, c->A.g, y))) return rc;
     IDP_CUDA_TRY(cudaStreamSynchronize(c->s));
     return IDP_OK;
 }
@@ -2092,8 +2226,7 @@ int idp_newton_direction(idp_ctx* c, int i, const double* X, double* p, int* ite
     if ((rc = pcg_solve(c->A, c->W, c->cs, c->P.mode == IDP_MODE_FP64, c->A.g, c->A.dir, c->P.pcg_rel_tol,
                         c->P.pcg_max_iters, its, rel, c->s)))
         return rc;
-    long o = 3L * c->A.v_off[i];
-    IDP_CUDA_TRY(cudaMemcpyAsync(p, c->A.dir + o, sizeof(double) * 3 * c->inst[i].V, cudaMemcpyDeviceToHost, c->s));
+    if ((rc = download3(c, i, c->A.dir, p))) return rc;
     IDP_CUDA_TRY(cudaStreamSynchronize(c->s));
     if (iters) *iters = its[i];
     if (relres) *relres = rel[i];

@@ -49,6 +49,9 @@ struct HostInstance {
     std::vector<int> hinges;
     std::vector<double> hk;
     bool flow() const { return shell && !elastic; }
+    // device order: internal local index -> caller's local index (set at
+    // commit; empty = the caller's order)
+    std::vector<int> perm;
 };
 
 // per-instance Newton state kept on the host
@@ -96,6 +99,7 @@ struct Arena {
     unsigned char* dfix = nullptr;                // V: DBC vertex already at its target (step start)
     double* dstiff = nullptr;                     // nI: moving-DBC penalty stiffness (0: off)
     int* vinst = nullptr;                         // V
+    int* vsrc = nullptr;                          // V: caller-order arena index of each device vertex
     // ---- per tet
     int4* tet = nullptr;
     double *IB = nullptr, *vol = nullptr, *lam = nullptr, *mu = nullptr;
@@ -253,7 +257,7 @@ enum WorkSlot {
     W_BH, W_BG, W_GENT_KEY, W_GENT_VAL, W_GENT_KEY2, W_GENT_VAL2, W_GENT_HEAD,
     W_TAIL_ROWPTR, W_TAIL_COL, W_TAIL_VAL, W_TAIL_KEYS,
     W_BSR_VAL, W_DIAG_INV, W_PCG_VEC, W_PCG_GRID, W_SPAN, W_CBASE, W_DENSE0, W_DENSE1, W_PCG_VEC64, W_CCD_TMP, W_CCD_ALPHA, W_MISC, W_MISC2,
-    W_CL_INT, W_CL_DENSE, W_CL_HOSTCONS, W_PSD, W_SHELL_GRAD,
+    W_CL_INT, W_CL_DENSE, W_CL_HOSTCONS, W_PSD, W_SHELL_GRAD, W_CCD_VOX,
     W_NUM
 };
 struct Work {
@@ -376,8 +380,13 @@ int barrier_gradient(Arena& A, Work& W, const double* X, const ContactSet& cs, d
 int barrier_hessian(Arena& A, Work& W, const double* X, const ContactSet& cs, bool fp64, cudaStream_t s);
 
 // ccd.cu
+// voxel size of the CCD hash at X for every instance (the mean surface edge
+// length in the reference's summation order), into W_CCD_VOX; ccd_stepsize
+// takes it instead of computing it when given
+int ccd_voxel_size(Arena& A, Work& W, const double* X, cudaStream_t s);
+const double* ccd_voxel_sizes(Arena& A, Work& W);
 int ccd_stepsize(Arena& A, Work& W, const double* X, const double* dir, double* alpha /*device nI*/, int* flags,
-                 cudaStream_t s);
+                 cudaStream_t s, const double* voxel_pre = nullptr);
 
 // solver.cu
 int assemble(Arena& A, Work& W, const ContactSet& cs, bool fp64, cudaStream_t s);
@@ -390,6 +399,10 @@ int pcg_solve(Arena& A, Work& W, const ContactSet& cs, bool fp64, const double* 
 int vec_inertia(Arena& A, Work& W, const double* X, double* inst_E, double* g /*nullable*/, cudaStream_t s);
 int vec_axpy_trial(Arena& A, const double* Xprev, const double* dir, double* Xout, cudaStream_t s);
 int vec_zero_dbc(Arena& A, double* g, cudaStream_t s);
+// vecops.cu: between the caller's vertex order (in) and the device order
+// (out) for the instance's range [v0, v0 + n) of 3-vectors
+int perm_to_device(Arena& A, long v0, long n, const double* in, double* out, cudaStream_t s);
+int perm_to_caller(Arena& A, long v0, long n, const double* in, double* out, cudaStream_t s);
 // dirichlet.cu: moving Dirichlet conditions (the augmented Lagrangian)
 int dbc_classify(Arena& A, const double* X, double* dir, int* moving, cudaStream_t s);
 int dbc_snap(Arena& A, double* X, cudaStream_t s);

@@ -83,7 +83,36 @@ __global__ void k_kappa_check(long C, const int4* __restrict__ cons, const int* 
     if (cur < prev) flag[inst] = 1;
 }
 
+// out[v] = in[vsrc[v]] (device order from the caller's), or the reverse
+__global__ void k_perm3(long v0, long n, const int* __restrict__ vsrc, const double* __restrict__ in,
+                        double* __restrict__ out, int to_device) {
+    long k = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const long v = v0 + k, src = vsrc[v];
+    if (to_device) {
+        out[3 * v] = in[3 * src];
+        out[3 * v + 1] = in[3 * src + 1];
+        out[3 * v + 2] = in[3 * src + 2];
+    } else {
+        out[3 * src] = in[3 * v];
+        out[3 * src + 1] = in[3 * v + 1];
+        out[3 * src + 2] = in[3 * v + 2];
+    }
+}
+
 }  // namespace
+
+int perm_to_device(Arena& A, long v0, long n, const double* in, double* out, cudaStream_t s) {
+    if (n <= 0) return IDP_OK;
+    (::idp::count_launch(), k_perm3<<<grid_for(n), kBlock, 0, s>>>(v0, n, A.vsrc, in, out, 1));
+    return cudaGetLastError() == cudaSuccess ? IDP_OK : IDP_ERR_CUDA;
+}
+
+int perm_to_caller(Arena& A, long v0, long n, const double* in, double* out, cudaStream_t s) {
+    if (n <= 0) return IDP_OK;
+    (::idp::count_launch(), k_perm3<<<grid_for(n), kBlock, 0, s>>>(v0, n, A.vsrc, in, out, 0));
+    return cudaGetLastError() == cudaSuccess ? IDP_OK : IDP_ERR_CUDA;
+}
 
 int vec_fill(double* a, long n, double v, cudaStream_t s) {
     if (n <= 0) return IDP_OK;

@@ -69,6 +69,12 @@ typedef struct idp_params {
                              diagnostic); an instance that fails stops with
                              IDP_ERR_INTERSECTION. Positive tet volumes are already
                              enforced by the line search. 0 = off (default)          */
+    int caller_vertex_order; /* 0 (default): each instance's vertices are stored on
+                             the device in a spatial (Morton) order of its rest
+                             positions, which keeps the PCG's per-CTA row blocks
+                             compact; every array crossing this interface stays in
+                             the caller's order. Nonzero: stored in the caller's
+                             order.                                                  */
 } idp_params;
 
 typedef struct idp_result {
