@@ -458,6 +458,7 @@ void idp_default_params(idp_params* p) {
     p->contact_block_vertices = 0;
     p->verify_iterates = 0;
     p->caller_vertex_order = 0;
+    p->pcg_local_degree = 2;
 }
 
 const char* idp_status_str(int s) {
@@ -488,6 +489,12 @@ idp_ctx* idp_create(const idp_params* p, int* status) {
     else idp_default_params(&c->P);
     c->W.grid_min_v = c->P.pcg_grid_min_vertices > 0 ? c->P.pcg_grid_min_vertices : 16384;
     c->W.grid_vper = c->P.pcg_grid_cta_vertices > 0 ? c->P.pcg_grid_cta_vertices : 112;
+    if (c->P.pcg_local_degree < 0 || c->P.pcg_local_degree > 8 || (c->P.pcg_local_degree & 1)) {
+        delete c;
+        if (status) *status = IDP_ERR_INVALID_ARG;
+        return nullptr;
+    }
+    c->W.local_deg = c->P.pcg_local_degree;
     c->W.cl_cap = c->P.contact_block_vertices > 0 ? std::max(2, std::min(c->P.contact_block_vertices, kClusterCap))
                                                   : kClusterCap;
     int prio_lo = 0, prio_hi = 0;
@@ -1203,6 +1210,7 @@ int idp_commit(idp_ctx* c) {
         for (long v = 0; v < A.V; ++v)
             if (diag[v] < 0) return IDP_ERR_INVALID_ARG;
         rc |= upload(c, A.rowptr, rowptr);
+        A.rowptr_h = rowptr;
         rc |= upload(c, A.colidx, colidx);
         rc |= upload(c, A.brow, brow);
         rc |= upload(c, A.src_ptr, src_ptr);

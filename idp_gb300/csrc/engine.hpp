@@ -125,6 +125,7 @@ struct Arena {
     // ---- BSR pattern of the tet stencil (3x3 blocks)
     long B = 0;
     int *rowptr = nullptr, *colidx = nullptr, *diagblk = nullptr;
+    std::vector<int> rowptr_h;                    // host copy of rowptr
     int *src_ptr = nullptr, *src = nullptr;       // per BSR block: contributing (tet*10+k)*2+transposed
     int* d_se_off = nullptr;                      // device copies of se_off / sn_off
     int* d_sn_off = nullptr;
@@ -268,6 +269,7 @@ struct Work {
     double* tol_inst = nullptr;              // per-instance PCG tolerance (device)
     long grid_min_v = 16384;                 // grid-wide PCG above this many vertices
     long grid_vper = 112;                    // vertices per CTA in the grid-wide PCG
+    int local_deg = 2;                       // degree of the grid PCG's CTA-local polynomial preconditioner
     int cl_cap = kClusterCap;                // vertices per dense contact block
     long long accd_maxit = 0;                // diagnostics (IDP_PROFILE)
     long long accd_long = 0, accd_total = 0, accd_pairs = 0;

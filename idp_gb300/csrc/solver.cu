@@ -695,9 +695,11 @@ struct GridRows {
     int ncache;
 };
 
-__host__ __device__ inline size_t grid_smem_fixed(int nvmax, size_t tsize) {
+// fixed part of the image: row offsets, the 3x3 inverses and, with the
+// CTA-local polynomial preconditioner, three 3-vectors per row
+__host__ __device__ inline size_t grid_smem_fixed(int nvmax, size_t tsize, bool poly) {
     size_t a = ((size_t)(nvmax + 1) * 4 + 15) & ~size_t(15);
-    return a + tsize * 9 * (size_t)nvmax;
+    return a + tsize * (poly ? 18 : 9) * (size_t)nvmax;
 }
 
 template <class T>
@@ -716,7 +718,7 @@ __global__ void __launch_bounds__(GP_THREADS, 3) k_pcg_grid(
     const T* __restrict__ dinv, ClusterPC<T> pc, const double* __restrict__ b, T* x, T* r, T* z, T* p, T* q,
     T* u, T* w, T* sv, T* m0, T* m1, T* part, T* redbuf, unsigned int* ctlbuf, int* err,
     const double* __restrict__ tol_inst, double rel_tol, int max_iters, int* __restrict__ iters_out,
-    unsigned long long* prof) {
+    unsigned long long* prof, int local_deg) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ T wsh[2 * (GP_THREADS / 32)];
     __shared__ T sh_t[kRed];
@@ -735,8 +737,11 @@ __global__ void __launch_bounds__(GP_THREADS, 3) k_pcg_grid(
     GridRows<T> S;
     S.row = reinterpret_cast<int*>(smem_raw);
     S.dinv = reinterpret_cast<T*>(smem_raw + (((size_t)(nvmax + 1) * 4 + 15) & ~size_t(15)));
-    S.val = reinterpret_cast<T*>(smem_raw + grid_smem_fixed(nvmax, sizeof(T)));
+    S.val = reinterpret_cast<T*>(smem_raw + grid_smem_fixed(nvmax, sizeof(T), local_deg > 0));
     S.col = reinterpret_cast<int*>(S.val + 9L * cap_blocks);
+    T* ya = S.dinv + 9 * nvmax;  // polynomial preconditioner: two iterates and their sum
+    T* yb = ya + 3 * nvmax;
+    T* yz = yb + 3 * nvmax;
     const int kb0 = rowptr[v0];
     const int nbk = rowptr[v1] - kb0;
     S.ncache = min(nbk, cap_blocks);
@@ -799,6 +804,53 @@ __global__ void __launch_bounds__(GP_THREADS, 3) k_pcg_grid(
             a2 += __shfl_xor_sync(0xffffffffu, a2, o);
         }
     };
+    // CTA-local polynomial preconditioner: with y0 = D^-1 v in ya and yz,
+    // y_{k+1} = y_k - D^-1 A_loc y_k, z = y_0 + ... + y_deg, where A_loc is
+    // the matrix's blocks between this CTA's rows (block Jacobi over the CTA
+    // subdomains, each block inverted by a truncated Neumann series). For an
+    // even degree p(S) = sum_k (I - S)^k > 0 for every S = D^-1/2 A_loc D^-1/2
+    // > 0, so M^-1 = p(D^-1 A_loc) D^-1 is symmetric positive definite. The
+    // result z is written to dst (global) for the instance's next SpMV.
+    auto local_poly = [&](T* dst) {
+        __syncthreads();
+        T* yin = ya;
+        T* yout = yb;
+        for (int pass = 0; pass < local_deg; ++pass) {
+            for (int base = kRows * warp; base < nv; base += kRows * nw) {
+                const int lv = base + lane / kRL;
+                const bool act = lv < nv;
+                const int v = v0 + (act ? lv : 0);
+                const bool fixed = act && dbc[v];
+                T a0 = 0, a1 = 0, a2 = 0;
+                if (act && !fixed) {
+                    const int ka = S.row[lv], kz = S.row[lv + 1];
+                    for (int k = ka + l8; k < kz; k += kRL) {
+                        const bool cached = k < S.ncache;
+                        const int c = cached ? S.col[k] : colidx[kb0 + k];
+                        const unsigned lc = (unsigned)(c - v0);
+                        if (lc >= (unsigned)nv) continue;
+                        const T* mm = cached ? S.val + 9 * k : val + 9L * (kb0 + k);
+                        const T x0 = yin[3 * lc], x1 = yin[3 * lc + 1], x2 = yin[3 * lc + 2];
+                        a0 += mm[0] * x0 + mm[1] * x1 + mm[2] * x2;
+                        a1 += mm[3] * x0 + mm[4] * x1 + mm[5] * x2;
+                        a2 += mm[6] * x0 + mm[7] * x1 + mm[8] * x2;
+                    }
+                }
+                group_sum3(a0, a1, a2);
+                if (act && l8 < 3) {
+                    const T* D = S.dinv + 9 * lv;
+                    const T yn = fixed ? T(0) : yin[3 * lv + l8] - (D[3 * l8] * a0 + D[3 * l8 + 1] * a1 + D[3 * l8 + 2] * a2);
+                    yout[3 * lv + l8] = yn;
+                    yz[3 * lv + l8] += yn;
+                }
+            }
+            __syncthreads();
+            T* t = yin;
+            yin = yout;
+            yout = t;
+        }
+        for (int i = threadIdx.x; i < 3 * nv; i += GP_THREADS) dst[3 * v0 + i] = yz[i];
+    };
     if (!has_blocks) {
         // ---- pipelined PCG (Ghysels & Vanroose): one reduction round per
         // iteration, which also publishes the vector the next SpMV gathers.
@@ -819,8 +871,11 @@ __global__ void __launch_bounds__(GP_THREADS, 3) k_pcg_grid(
                 q[i3] = T(0);
                 sv[i3] = T(0);
                 p[i3] = T(0);
+                ya[3 * lv + d] = uv[d];
+                yz[3 * lv + d] = uv[d];
             }
         }
+        if (local_deg > 0) local_poly(u);  // u = M r
         if (!barrier()) return;
         // w = A u, m = M w; partials gamma = r.u, delta = w.u, rho = r.r
         T gam_l = 0, del_l = 0, rho_l = 0;
@@ -847,9 +902,13 @@ __global__ void __launch_bounds__(GP_THREADS, 3) k_pcg_grid(
                     w2 = __shfl_sync(0xffffffffu, wn, gb + 2);
             if (act && l8 < 3) {
                 const T* D = S.dinv + 9 * lv;
-                m0[3 * v + l8] = fixed ? T(0) : D[3 * l8] * w0 + D[3 * l8 + 1] * w1 + D[3 * l8 + 2] * w2;
+                const T mv = fixed ? T(0) : D[3 * l8] * w0 + D[3 * l8 + 1] * w1 + D[3 * l8 + 2] * w2;
+                m0[3 * v + l8] = mv;
+                ya[3 * lv + l8] = mv;
+                yz[3 * lv + l8] = mv;
             }
         }
+        if (local_deg > 0) local_poly(m0);  // m = M w
         T red3[kRed];
         {
             T in[kRed] = {cta_sum1(gam_l, wsh), cta_sum1(del_l, wsh), cta_sum1(rho_l, wsh), T(0)};
@@ -909,9 +968,13 @@ __global__ void __launch_bounds__(GP_THREADS, 3) k_pcg_grid(
                             w2 = __shfl_sync(0xffffffffu, wn, gb + 2);
                     if (act && l8 < 3) {
                         const T* D = S.dinv + 9 * lv;
-                        mn_[3 * v + l8] = fixed ? T(0) : D[3 * l8] * w0 + D[3 * l8 + 1] * w1 + D[3 * l8 + 2] * w2;
+                        const T mv = fixed ? T(0) : D[3 * l8] * w0 + D[3 * l8 + 1] * w1 + D[3 * l8 + 2] * w2;
+                        mn_[3 * v + l8] = mv;
+                        ya[3 * lv + l8] = mv;
+                        yz[3 * lv + l8] = mv;
                     }
                 }
+                if (local_deg > 0) local_poly(mn_);  // m = M w
                 T in[kRed] = {cta_sum1(gam_l, wsh), cta_sum1(del_l, wsh), cta_sum1(rho_l, wsh), T(0)};
                 if (timed) { t1 = gtimer(); prof[0] += t1 - t0; t0 = t1; }
                 if (!inst_round<T>(ctl, red, part, c0, nc, ++round, true, in, red3, err, sh_i, sh_t)) return;
@@ -1336,7 +1399,16 @@ static int pcg_inner(Arena& A, Work& W, const double* b, double rel_tol, int max
         const int G = (int)wv.size();
         int nvmax = 1;
         for (const GridCta& g : wv) nvmax = std::max(nvmax, g.v1 - g.v0);
-        const long fixed = (long)grid_smem_fixed(nvmax, sizeof(T));
+        // the polynomial preconditioner's vectors when they leave room for
+        // at least half of the rows' blocks, else block Jacobi for this wave
+        long nbmax = 0;
+        for (const GridCta& g : wv) nbmax = std::max<long>(nbmax, (long)(A.rowptr_h[g.v1] - A.rowptr_h[g.v0]));
+        int deg = W.local_deg;
+        long fixed = (long)grid_smem_fixed(nvmax, sizeof(T), deg > 0);
+        if (deg > 0 && (kGridSmem - fixed) / (long)(9 * sizeof(T) + 4) < nbmax / 2) {
+            deg = 0;
+            fixed = (long)grid_smem_fixed(nvmax, sizeof(T), false);
+        }
         const int cap_blocks = (int)((kGridSmem - fixed) / (long)(9 * sizeof(T) + 4));
         if (cap_blocks < 0) return IDP_ERR_CAPACITY;  // rows per CTA beyond the shared-memory image
         IDP_CUDA_TRY(cudaMemcpyAsync(d_plan, wv.data(), sizeof(GridCta) * G, cudaMemcpyHostToDevice, s));
@@ -1356,7 +1428,7 @@ static int pcg_inner(Arena& A, Work& W, const double* b, double rel_tol, int max
                                         (const int*)A.rowptr,
                                         (const int*)A.colidx, val, trp, tcol, tval, (const unsigned char*)A.dbc, dinv,
                                         pcb, b, x, r, z, p, Ap, pu, pw, psv, pm0, pm1, d_part, d_red, d_ctl, d_err,
-                                        (const double*)W.tol_inst, rel_tol, max_iters, d_iters, d_prof));
+                                        (const double*)W.tol_inst, rel_tol, max_iters, d_iters, d_prof, deg));
         W.stats.pcg_launches += 1;
     }
     W.timer.stop(s);
