@@ -78,6 +78,10 @@ def parse():
                     help="PCG relative tolerance of the timed arm (0 = library default); the FP64 arm keeps the default")
     ap.add_argument("--pcg-grid-cta-vertices", type=int, default=0,
                     help="vertices per CTA of the grid-wide PCG (0 = library default)")
+    ap.add_argument("--pcg-local-degree", type=int, default=-1,
+                    help="grid PCG's CTA-local polynomial preconditioner degree (-1 = library default, 0 = block Jacobi)")
+    ap.add_argument("--caller-vertex-order", action="store_true",
+                    help="keep the caller's vertex order on the device (default: spatial order)")
     ap.add_argument("--instances", type=int, default=256)
     ap.add_argument("--mode", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--max-newton", type=int, default=2000)
@@ -332,6 +336,10 @@ def run_flow(args):
         kw = {}
         if timed_arm and args.pcg_rel_tol > 0:
             kw["pcg_rel_tol"] = args.pcg_rel_tol
+        if args.pcg_local_degree >= 0:
+            kw["pcg_local_degree"] = args.pcg_local_degree
+        if args.caller_vertex_order:
+            kw["caller_vertex_order"] = 1
         c = idp.Context(h=H, newton_tol=1e-3, max_newton=args.max_newton, mode=m, device=local,
                         pcg_grid_cta_vertices=args.pcg_grid_cta_vertices, **kw)
         c.add_instance(p["X"], p["tets"], p["mass"], p["lam"], p["mu"], p["dHat2"], p["kappa"], p["kappa_max"])
