@@ -433,6 +433,7 @@ def run_flow(args):
                    "l2": "working set larger than L2 (BSR + tet data + vectors > 129 MB); no flush"},
         "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
         "newton_iters": {"mean": float(np.mean(newton)), "max": int(np.max(newton)), "total": int(np.sum(newton))},
+        "pcg_iters_per_newton": float(sum(r["pcg_iters"] for r in results) / max(1, int(np.sum(newton)))),
         "status": sorted({int(r["status"]) for r in results}),
         "phase_ms_per_step": {k: v / args.steps for k, v in phase.items()},
         "fp64": fp64,
