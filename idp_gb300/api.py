@@ -25,7 +25,7 @@ import math
 
 import numpy as np
 
-from . import Context, IDPError, IDP_WARN_ITER_CAP, MODE_MIXED, meshgen
+from . import Context, IDPError, IDP_WARN_ITER_CAP, MODE_MIXED, dirichlet, meshgen
 
 _UNSUPPORTED = "not part of the GB300 path (tet meshes and triangle shells with offset IPC and DBC)"
 
@@ -278,9 +278,54 @@ class FEM:
     DiscreteShell = DiscreteShell
 
 
-class TetIPCSim:
+class _DirichletDriver:
+    """The Dirichlet part of FEMDiscreteShellBase: DBC rows and motions
+    (set_DBC, set_DBC_with_range, load_frame's Reset_Dirichlet) and their
+    update before each step (FEMDiscreteShellBase.py:273-299): the motion
+    runs while MDBC_tmin < t < MDBC_tmax, its velocities reversing every
+    MDBC_period; with seqDBC >= 0 the targets are read from the OBJ sequence
+    seqDBCPath/shell<frame>.obj instead, translated by (0, -0.75, 0)."""
+
+    def _init_dbc(self):
+        self.DBC = dirichlet.DBCStorage()
+        self.DBCMotion = dirichlet.DBCMotion()
+        self.t = 0.0
+        self.MDBC_tmax = 1e10
+        self.MDBC_tmin = -1.0
+        self.MDBC_period = 1e10
+        self.MDBC_periodCounter = 1
+        self.seqDBC = -1
+        self.seqDBCPath = ""
+        self.curFrameNum = 0
+
+    def set_DBC(self, DBCRangeMin, DBCRangeMax, v, rotCenter, rotAxis, angVelDeg):
+        dirichlet.init_dirichlet(self.X, DBCRangeMin, DBCRangeMax, v, rotCenter, rotAxis, angVelDeg, self.DBC,
+                                 self.DBCMotion)
+
+    def set_DBC_with_range(self, DBCRangeMin, DBCRangeMax, v, rotCenter, rotAxis, angVelDeg, vIndRange):
+        dirichlet.init_dirichlet(self.X, DBCRangeMin, DBCRangeMax, v, rotCenter, rotAxis, angVelDeg, self.DBC,
+                                 self.DBCMotion, vIndRange)
+
+    def _step_dbc(self, dt):
+        if self.MDBC_tmin < self.t < self.MDBC_tmax:
+            if self.seqDBC < 0:
+                if self.t - self.MDBC_tmin >= self.MDBC_period * self.MDBC_periodCounter:
+                    self.MDBC_periodCounter += 1
+                    dirichlet.turn_dirichlet(self.DBCMotion)
+                dirichlet.step_dirichlet(self.DBCMotion, dt, self.DBC)
+            else:
+                dirichlet.load_dirichlet(f"{self.seqDBCPath}/shell{self.curFrameNum}.obj", self.seqDBC,
+                                         (0.0, -0.75, 0.0), self.DBC)
+                self.curFrameNum += 1
+
+    def _dbc_arg(self):
+        return self.DBC if len(self.DBC) else None
+
+
+class TetIPCSim(_DirichletDriver):
     """The tet + offset-IPC slice of FEMDiscreteShellBase
-    (Python/Drivers/FEMDiscreteShellBase.py:14-388)."""
+    (Python/Drivers/FEMDiscreteShellBase.py:14-388), with its Dirichlet
+    conditions (fixed, moving by a velocity and an angular velocity)."""
 
     def __init__(self, dt=0.1, PNTol=1e-3, mode=MODE_MIXED):
         self.dt = dt
@@ -292,9 +337,10 @@ class TetIPCSim:
         self.dHat2 = 1e-6
         self.kappa = [1e5, 0.0, 0.0]
         self.thickness = 0.0
-        self.DBC = None
         self.PNIterCount = 0
         self.mode = mode
+        self.bodyForce = None
+        self._init_dbc()
 
     def add_object_3D(self, X, *args):
         """Append a tet mesh and return its mesh counter. Either
@@ -335,23 +381,26 @@ class TetIPCSim:
 
     def advance_one_time_step(self, dt=None):
         DiscreteShell.mode = self.mode
+        h = dt or self.dt
+        self._step_dbc(h)
         it = FEM.DiscreteShell.Advance_One_Step_IE_Hinge(
-            None, None, self.DBC, None, None, None, self.thickness, 0, None, None, None, None, None, None,
-            dt or self.dt, self.PNTol, True, self.dHat2, self.kappa, 0, 1e-6, 1, None, None, False, self.X,
+            None, None, self._dbc_arg(), None, None, None, self.thickness, 0, None, None, None, None, None,
+            self.bodyForce, h, self.PNTol, True, self.dHat2, self.kappa, 0, 1e-6, 1, None, None, False, self.X,
             self.nodeAttr, None, None, None, self.tet, None, self.tetElasticity, None, None, None, None, None, None,
             10, None, "")
         self.PNIterCount += it
+        self.t += h
         return it
 
 
-class ShellFlowSim:
+class ShellFlowSim(_DirichletDriver):
     """The triangle-shell slice of FEMDiscreteShellBase: what the normal-flow
     scripts drive (Projects/FEMShell/12-14_normal_flow.py) — add_shell_3D,
     initialize, initialize_OIPC, the frame loop of SimulationBase
     (Python/Drivers/SimulationBase.py:76-103) and advance_one_time_step with
     Update_Normal_Flow_Neumann (FEMDiscreteShellBase.py:266-276, 332-340) —
-    and, with flow off, the elastic shell's Hinge step with gravity
-    (FEMDiscreteShellBase.py:300-361)."""
+    and, with flow off, the elastic shell's Hinge step with gravity and
+    Dirichlet conditions (FEMDiscreteShellBase.py:255-361)."""
 
     def __init__(self, precision="double", dim=3, mode=MODE_MIXED):
         if dim != 3:
@@ -374,11 +423,11 @@ class ShellFlowSim:
         self.dHat2 = 1e-6
         self.kappa = [1e5, 0.0, 0.0]
         self.thickness = 0.0  # IPC offset
-        self.DBC = None
         self.PNIterCount = 0
         self.mode = mode
         self._ctx = None
         self._ctx_h = None
+        self._init_dbc()
 
     def add_shell_3D(self, filePath, translate, rotCenter, rotAxis, rotDeg):
         from . import meshio
@@ -402,10 +451,7 @@ class ShellFlowSim:
         self.shell_E, self.shell_nu = float(E), float(nu)
         self.thickness = float(thickness)
         if self.flow:
-            e = np.sort(self.Elem[:, [[0, 1], [1, 2], [2, 0]]].reshape(-1, 2), axis=1)
-            uniq, cnt = np.unique(e, axis=0, return_counts=True)
-            bnd = np.unique(uniq[cnt == 1].reshape(-1))
-            self.DBC = bnd.astype(np.int32) if bnd.size else None
+            dirichlet.boundary_dirichlet(self.X, self.Elem, self.DBC)
 
     def initialize_OIPC(self, thickness, offset, stiffMult=1.0):
         """Initialize_OIPC (DISCRETE_SHELL.h:555-577): d-hat = thickness,
@@ -416,6 +462,8 @@ class ShellFlowSim:
         self.thickness = float(offset)
 
     def _context(self, h):
+        if self._ctx is not None and self._dbc_n != len(self.DBC):  # the DBC rows changed: rebuild
+            self._ctx_h = None
         if self._ctx is None or self._ctx_h != h:
             X = self.X.copy()
             v = None
@@ -425,14 +473,16 @@ class ShellFlowSim:
             else:
                 self._X0 = X.copy()
             self._ctx = Context(h=h, newton_tol=self.PNTol, thickness=self.thickness, mode=self.mode)
+            dbc_idx = self.DBC.indices if len(self.DBC) else None
+            self._dbc_n = len(self.DBC)
             if self.flow:
                 self._ctx.add_shell_instance(X, self.Elem, self.shell_density, self.shell_thickness, self.dHat2,
-                                             self.kappa[0], self.kappa[1], dbc_idx=self.DBC)
+                                             self.kappa[0], self.kappa[1], dbc_idx=dbc_idx)
             else:
                 self._ctx.add_elastic_shell_instance(X, self.Elem, self.shell_density, self.shell_E, self.shell_nu,
                                                      self.shell_thickness, self.dHat2, self.kappa[0], self.kappa[1],
                                                      bending_mult=self.bendingStiffMult, X0=self._X0,
-                                                     dbc_idx=self.DBC)
+                                                     dbc_idx=dbc_idx)
                 if v is not None:
                     self._ctx.set_velocity(0, v)
                 if any(g != 0 for g in self.gravity):  # b = M g (Initialize_Discrete_Shell)
@@ -443,10 +493,14 @@ class ShellFlowSim:
 
     def advance_one_time_step(self, dt):
         """Advance_One_Step_IE_Flow with the normal-flow predictor in flow
-        mode, Advance_One_Step_IE_Hinge of the elastic shell otherwise."""
+        mode, Advance_One_Step_IE_Hinge of the elastic shell otherwise; the
+        Dirichlet motion is stepped first."""
+        self._step_dbc(dt)
         ctx = self._context(dt)
         ctx.set_positions(0, self.X)
         ctx.set_kappa(0, self.kappa)
+        if len(self.DBC):
+            ctx.set_dbc_targets(0, self.DBC.targets)
         if self.flow and self.normalFlowMag != 0:
             ctx.set_normal_flow(0, dt * dt * self.normalFlowMag)
         rc, res = ctx.advance(check=False)
@@ -456,6 +510,7 @@ class ShellFlowSim:
         self.X[...] = X
         self.kappa[0] = k[0]
         self.PNIterCount += res[0]["newton_iters"]
+        self.t += dt
         return res[0]["newton_iters"]
 
     def advance_one_frame(self, f):

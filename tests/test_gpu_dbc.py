@@ -121,3 +121,44 @@ def test_hinge_call_with_moving_dbc_rows_matches_c_abi(oracle, gpu_lib):
     FEM.DiscreteShell.Advance_One_Step_IE_Hinge(*list(a.values()))
     assert np.array_equal(a["X"][rows], DBC2[:, 1:])
     ctx.close()
+
+
+def test_twisting_bar_driver_matches_oracle(oracle, gpu_lib):
+    """TetIPCSim with its bottom fixed (set_DBC, zero motion) and its top
+    turning at 90 degrees per second (set_DBC with an angular velocity):
+    Step_Dirichlet moves the top rows before each step and the Newton step
+    puts the top vertices on them; three steps against the oracle fed the
+    same rows."""
+    import idp_gb300 as idp
+    from idp_gb300 import dirichlet, meshgen
+    from idp_gb300.api import TetIPCSim
+
+    X, tets = meshgen.bar(2, 2, 6, size=(1.0, 1.0, 3.0), seed=0)
+    sim = TetIPCSim(dt=0.1, PNTol=1e-5, mode=idp.MODE_FP64)
+    sim.add_object_3D(X, tets)
+    sim.initialize_added_objects((0.0, 0.0, 0.0), 1000.0, 1e4, 0.3)
+    sim.initialize_OIPC(1e-3 * float(np.linalg.norm(X.max(0) - X.min(0))), 0.0)
+    sim.set_DBC((-0.1, -0.1, -0.1), (1.1, 1.1, 0.01), (0, 0, 0), (0, 0, 0), (0, 0, 1), 0.0)
+    sim.set_DBC((-0.1, -0.1, 0.99), (1.1, 1.1, 1.1), (0, 0, 0), (0.5, 0.5, 3.0), (0, 0, 1), 90.0)
+    rows = sim.DBC.indices.copy()
+    assert len(sim.DBCMotion) == 2 and rows.size > 8
+    # the oracle, fed the same rows step by step
+    D, M = dirichlet.DBCStorage(sim.DBC.rows), dirichlet.DBCMotion([list(r) for r in sim.DBCMotion])
+    T = tets.shape[0]
+    mask = np.zeros(X.shape[0], np.uint8)
+    mask[rows] = 1
+    pb = oracle.Problem(X=X.copy(), X0=X, tets=tets, mass=sim.nodeAttr["m"], lam=sim.tetElasticity["lambda"],
+                        mu=sim.tetElasticity["mu"], h=0.1, dHat2=sim.dHat2, kappa=list(sim.kappa), v=np.zeros_like(X),
+                        dbc=mask, dbc_rows=rows, tol=1e-5)
+    for _ in range(3):
+        sim.advance_one_time_step()
+        dirichlet.step_dirichlet(M, 0.1, D)
+        pb.dbc_target = D.targets.copy()
+        oracle.advance_one_step(pb)
+        assert np.array_equal(D.rows, sim.DBC.rows)
+        assert np.array_equal(sim.X[rows], D.targets)  # reached at once (nothing in the way)
+        assert np.max(np.abs(sim.X - pb.X)) <= 1e-5
+    # the top turned by 27 degrees about the bar's axis
+    top = rows[(X[rows, 2] > 2.9) & (np.hypot(X[rows, 0] - 0.5, X[rows, 1] - 0.5) > 0.1)]
+    ang = np.arctan2(sim.X[top, 1] - 0.5, sim.X[top, 0] - 0.5) - np.arctan2(X[top, 1] - 0.5, X[top, 0] - 0.5)
+    assert np.allclose(np.mod(ang, 2 * np.pi), np.deg2rad(27.0), atol=1e-9)

@@ -211,7 +211,7 @@ def test_normal_flow_script_driver(oracle, gpu_lib, tmp_path):
     sim.initialize_OIPC(1e-3, 0)
     X0 = sim.X.copy()
     sim.run()
-    assert sim.DBC is None  # closed surface: nothing fixed
+    assert len(sim.DBC) == 0  # closed surface: nothing fixed
     ctx = idp.Context(h=0.5, mode=idp.MODE_MIXED)
     k0, km0 = idp.api.initialize_oipc(float(sim._mass().mean()), 1e-6)
     ctx.add_shell_instance(X0, F, 1.0, 1.0, 1e-6, k0, km0)
