@@ -71,6 +71,9 @@ def parse():
     ap.add_argument("--serve-batch", type=int, default=8)
     ap.add_argument("--hbm-budget-gb", type=float, default=150.0)
     ap.add_argument("--serve-newton-cap", type=int, default=30)
+    ap.add_argument("--serve-pool", type=int, default=8, help="serve: bars and blobs in the job pool (each)")
+    ap.add_argument("--serve-max-bar-tets", type=int, default=50_000)
+    ap.add_argument("--serve-max-blob-tets", type=int, default=100_000)
     ap.add_argument("--blob-n", type=int, default=64)
     ap.add_argument("--flow-step", type=float, default=0.05)
     ap.add_argument("--no-fp64", action="store_true")
@@ -710,20 +713,20 @@ def fp64_one_at_a_time(idp, probs, results, sample, max_newton, budget, device):
     return out
 
 
-def serve_pool(seed=0):
-    """Config-4 style job pool: 8 bars (tet counts log-uniform in [2k, 50k],
-    bend U[1.5pi, 2.5pi], the config-0 target) and 8 blobs (tet counts
-    log-uniform in [2k, 100k], one normal-flow step of 0.05)."""
+def serve_pool(seed=0, n_each=8, max_bar=50_000, max_blob=100_000):
+    """Config-4 style job pool: n_each bars (tet counts log-uniform in [2k,
+    max_bar], bend U[1.5pi, 2.5pi], the config-0 target) and n_each blobs (tet
+    counts log-uniform in [2k, max_blob], one normal-flow step of 0.05)."""
     import numpy as np
     from idp_gb300 import meshgen
     from idp_gb300.api import initialize_oipc
 
     rng = np.random.default_rng(seed)
     pool = []
-    for it in meshgen.bar_batch(8, 2_000, 50_000, seed=seed):
+    for it in meshgen.bar_batch(n_each, 2_000, max_bar, seed=seed):
         pool.append(dict(kind="bar", X=it["X"], tets=it["tets"], v=(it["target"] - it["X"]) / 0.1, flow=0.0))
-    for k in range(8):
-        t = math.exp(rng.uniform(math.log(2_000), math.log(100_000)))
+    for k in range(n_each):
+        t = math.exp(rng.uniform(math.log(2_000), math.log(max_blob)))
         n = max(8, int(round((t / 0.84) ** (1.0 / 3.0))))
         X, tets, _ = meshgen.blob(n=n, lmax=8, amp=0.3, seed=seed * 100 + k)
         pool.append(dict(kind="blob", X=X, tets=tets, v=None, flow=0.05))
@@ -750,7 +753,8 @@ def run_serve(args):
 
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
-    pool = serve_pool(seed=rank)
+    pool = serve_pool(seed=rank, n_each=args.serve_pool, max_bar=args.serve_max_bar_tets,
+                      max_blob=args.serve_max_blob_tets)
     rng = np.random.default_rng(1000 + rank)
     arr, t = [], 0.0
     while True:
@@ -830,8 +834,10 @@ def run_serve(args):
         "steps": len(infos), "warmup": args.warmup, "ms_per_step": 1000.0 / thr if thr else None,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
         "config": {"workload": f"serve: Poisson arrivals {args.rate:g}/s for {args.duration:g} s, jobs drawn from "
-                               "8 bars (2k-50k tets, bend U[1.5pi,2.5pi]) and 8 blobs (2k-100k tets, one normal-flow "
-                               f"step 0.05), Newton cap {args.serve_newton_cap} per job",
+                               f"{args.serve_pool} bars (2k-{args.serve_max_bar_tets // 1000}k tets, bend "
+                               f"U[1.5pi,2.5pi]) and {args.serve_pool} blobs (2k-{args.serve_max_blob_tets // 1000}k "
+                               f"tets, one normal-flow step 0.05), Newton cap {args.serve_newton_cap} per job",
+                   "pool_tets": sorted(int(p["tets"].shape[0]) for p in pool),
                    "jobs": len(infos), "kinds": kinds, "workers": args.serve_workers, "max_batch": args.serve_batch,
                    "hbm_budget_gb": args.hbm_budget_gb, "l2": "no flush; jobs are independent solves"},
         "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
