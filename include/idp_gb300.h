@@ -431,7 +431,7 @@ int idp_newton_direction(idp_ctx* ctx, int inst, const double* X, double* p, int
  * calls that overlap on the GPU (other streams, other threads) race on it, so
  * order them. The first call on each device looks up that array's device
  * address (again after the device's context is re-created, e.g. by
- * cudaDeviceReset); make it before any stream capture. */
+ * cudaDeviceReset). */
 int idp_tet_energy_noalloc(int T, const int32_t* tets, const double* X, const double* IB, const double* vol,
                            const double* lam, const double* mu, double weight, double* energy, int32_t* inverted,
                            void* stream);
