@@ -85,6 +85,9 @@ def parse():
                     help="grid PCG's CTA-local polynomial preconditioner degree (-1 = library default, 0 = block Jacobi)")
     ap.add_argument("--caller-vertex-order", action="store_true",
                     help="keep the caller's vertex order on the device (default: spatial order)")
+    ap.add_argument("--autotune", action="store_true",
+                    help="pick the PCG tile and preconditioner shapes with idp_gb300.autotune before timing "
+                         "(untimed; cached per workload kind)")
     ap.add_argument("--instances", type=int, default=256)
     ap.add_argument("--mode", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--max-newton", type=int, default=2000)
@@ -335,8 +338,19 @@ def run_flow(args):
     desc = blob_desc(p, args.blob_n, args.flow_step)
     V = p["X"].shape[0]
 
+    tuned = None
+    if args.autotune:
+        from idp_gb300 import autotune
+
+        inst = [dict(p, normal_flow=args.flow_step)]
+        tp, rec = autotune.tune(inst, base=dict(h=H, newton_tol=1e-3, mode=mode), device_name=None)
+        tuned = {k: tp[k] for k in autotune.DEFAULT_SPACE}
+        tuned_rec = {"params": tuned, "step_ms": rec["ms"], "cached": rec["cached"]}
+
     def make_ctx(m, timed_arm=True):
         kw = {}
+        if tuned and timed_arm:
+            kw.update(tuned)
         if timed_arm and args.pcg_rel_tol > 0:
             kw["pcg_rel_tol"] = args.pcg_rel_tol
         if args.pcg_local_degree >= 0:
@@ -437,6 +451,7 @@ def run_flow(args):
         "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
         "newton_iters": {"mean": float(np.mean(newton)), "max": int(np.max(newton)), "total": int(np.sum(newton))},
         "pcg_iters_per_newton": float(sum(r["pcg_iters"] for r in results) / max(1, int(np.sum(newton)))),
+        "autotune": tuned_rec if tuned else None,
         "status": sorted({int(r["status"]) for r in results}),
         "phase_ms_per_step": {k: v / args.steps for k, v in phase.items()},
         "fp64": fp64,
