@@ -137,7 +137,7 @@ def test_kappa_adapts_like_the_oracle(oracle, gpu_lib, mode):
     v = np.zeros_like(X)
     v[V // 2:, 0] = -0.02 / 0.1
     k0 = pr["kappa"] * 1e-6
-    ctx = idp.Context(h=0.1, mode=mode, newton_tol=1e-3, max_newton=300)
+    ctx = idp.Context(h=0.1, mode=mode, newton_tol=1e-5, max_newton=500)
     ctx.add_instance(X, tets, pr["mass"], pr["lam"], pr["mu"], pr["dHat2"], k0, pr["kappa_max"])
     ctx.set_velocity(0, v)
     ctx.commit()
@@ -147,8 +147,8 @@ def test_kappa_adapts_like_the_oracle(oracle, gpu_lib, mode):
 
     def problem(X1, kappa):
         return oracle.Problem(X=X1.copy(), X0=X, tets=tets, mass=pr["mass"], lam=np.full(T, pr["lam"]),
-                              mu=np.full(T, pr["mu"]), h=0.1, dHat2=pr["dHat2"], kappa=kappa, v=v.copy(), tol=1e-3,
-                              max_iters=300)
+                              mu=np.full(T, pr["mu"]), h=0.1, dHat2=pr["dHat2"], kappa=kappa, v=v.copy(), tol=1e-5,
+                              max_iters=500)
 
     po = problem(X, [k0, pr["kappa_max"], 0.0])
     oracle.advance_one_step(po)
