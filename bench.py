@@ -85,6 +85,7 @@ def parse():
                     help="grid PCG's CTA-local polynomial preconditioner degree (-1 = library default, 0 = block Jacobi)")
     ap.add_argument("--caller-vertex-order", action="store_true",
                     help="keep the caller's vertex order on the device (default: spatial order)")
+    ap.add_argument("--progress", action="store_true", help="print progress lines to stderr")
     ap.add_argument("--autotune", action="store_true",
                     help="pick the PCG tile and preconditioner shapes with idp_gb300.autotune before timing "
                          "(untimed; cached per workload kind)")
@@ -589,10 +590,18 @@ def run_gpu(args):
             torch.distributed.barrier()
         torch.cuda.synchronize()
 
+    def progress(msg):
+        if args.progress and rank == 0:
+            print(f"[{time.strftime('%H:%M:%S')}] {msg}", file=sys.stderr, flush=True)
+
     # ---- resident inputs: restore the device snapshot, advance
-    for _ in range(args.warmup):
+    for w in range(args.warmup):
         ctx.restore_state()
-        ctx.advance(check=False)
+        t0 = time.perf_counter()
+        _, rw = ctx.advance(check=False)
+        progress(f"warm-up step {w}: {time.perf_counter() - t0:.1f} s, Newton max "
+                 f"{max(r['newton_iters'] for r in rw)}, converged "
+                 f"{sum(1 for r in rw if r['status'] in (idp.IDP_OK, idp.IDP_WARN_ITER_CAP))}/{len(rw)}")
     barrier()
     dev_ms, wall, lat, results, launches = [], [], [], None, 0
     pcg_ms = pcg_bytes = 0.0
@@ -608,6 +617,7 @@ def run_gpu(args):
             pcg_bytes += st["pcg_bytes"]
             launches += st["kernel_launches"]
             lat += [r["latency_ms"] for r in results]
+            progress(f"timed step: {wall[-1]:.1f} s wall, {dev_ms[-1] / 1000:.1f} s device")
     barrier()
     step_ms = max_over_ranks(statistics.mean(dev_ms), world)
     iters_step = sum(r["newton_iters"] for r in results)
@@ -627,7 +637,7 @@ def run_gpu(args):
     counts = ctx.intersection_counts()
     injective = {"checked": nI, "intersection_free": int((counts == 0).sum()),
                  "inverted": sum(1 for r in results if r["status"] == idp.IDP_ERR_INVERTED)}
-    fp64_single = fp64_one_at_a_time(idp, probs, results, args.fp64_sample, max_newton, budget, local) \
+    fp64_single = fp64_one_at_a_time(idp, probs, results, args.fp64_sample, max_newton, budget, local, progress) \
         if rank == 0 and mode == idp.MODE_MIXED and args.fp64_sample > 0 else None
 
     # ---- end to end with host buffers (pinned), copies inside the timed region
@@ -692,7 +702,7 @@ def run_gpu(args):
     print(json.dumps(out))
 
 
-def fp64_one_at_a_time(idp, probs, results, sample, max_newton, budget, device):
+def fp64_one_at_a_time(idp, probs, results, sample, max_newton, budget, device, progress=None):
     """The plain FP64 path, one instance per context and call, on `sample`
     instances spread evenly over the batch (same start state and Newton
     budget as the batched mixed run); Newton iterations/s and solves/s from
@@ -721,6 +731,9 @@ def fp64_one_at_a_time(idp, probs, results, sample, max_newton, budget, device):
         e64, em = r[0]["energy"], results[i]["energy"]
         rel.append(abs(em - e64) / max(abs(e64), 1e-300))
         c.close()
+        if progress:
+            progress(f"FP64 one at a time: instance {i} ({p['tets'].shape[0]} tets) {r[0]['newton_iters']} iterations, "
+                     f"status {r[0]['status']}, rel energy vs mixed batched {rel[-1]:.2e}")
     out = {"instances": idx if len(idx) <= 32 else len(idx), "newton_iters": int(its), "ms": ms,
            "newton_iters_per_s": its / (ms / 1000.0) if ms > 0 else None,
            "solves_per_s": (solved / (ms / 1000.0)) if budget == 0 and ms > 0 else None,
