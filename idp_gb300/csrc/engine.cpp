@@ -20,6 +20,7 @@
 #include <map>
 #include <numeric>
 #include <set>
+#include <thread>
 #include <vector>
 #include "engine.hpp"
 
@@ -1153,58 +1154,101 @@ int idp_commit(idp_ctx* c) {
     }
     // BSR pattern of the tet stencil + contributor lists (fixed order)
     {
-        std::vector<std::pair<long, int>> keys;  // (row*V + col, code)
-        keys.reserve(16 * A.T + 9 * A.F);
+        // Row by row: the (column, contributor code) entries of a row, in
+        // element order (tets ascending with the row's corner against every
+        // corner, then flow faces, membrane faces and hinges likewise), are
+        // stably sorted by column, so each block lists its contributors in
+        // the order a global stable sort of all (row, column) keys gives.
+        // Rows are independent: threads take contiguous row ranges.
+        const long V = A.V;
+        std::vector<long> roff(V + 1, 0);
         for (long t = 0; t < A.T; ++t) {
-            int v[4] = {tet[t].x, tet[t].y, tet[t].z, tet[t].w};
-            for (int a = 0; a < 4; ++a)
-                for (int b = 0; b < 4; ++b) {
-                    int lo = std::min(a, b), hi = std::max(a, b);
-                    int k = lo * 4 - lo * (lo - 1) / 2 + (hi - lo);
-                    int code = (int)((t * 10 + k) * 2 + (a > b ? 1 : 0));
-                    keys.push_back({(long)v[a] * A.V + v[b], code});
-                }
+            roff[tet[t].x + 1] += 4; roff[tet[t].y + 1] += 4; roff[tet[t].z + 1] += 4; roff[tet[t].w + 1] += 4;
         }
-        // shell faces: -(2 f + diagonal) - 1 (flow Hessian, INC_POTENTIAL.h:323-339)
         for (long f = 0; f < A.F; ++f)
-            for (int a = 0; a < 3; ++a)
-                for (int b = 0; b < 3; ++b)
-                    keys.push_back({(long)face[3 * f + a] * A.V + face[3 * f + b], -(int)(2 * f + (a == b ? 1 : 0)) - 1});
-        // elastic-shell element blocks, stored after the tets' 10 per tet:
-        // 6 per membrane face, 10 per hinge (upper blocks, a <= b)
+            for (int a = 0; a < 3; ++a) roff[face[3 * f + a] + 1] += 3;
         for (long f = 0; f < A.Fm; ++f)
-            for (int a = 0; a < 3; ++a)
-                for (int b = 0; b < 3; ++b) {
-                    const int lo = std::min(a, b), hi = std::max(a, b);
-                    const long k = 10 * A.T + 6 * f + lo * 3 - lo * (lo - 1) / 2 + (hi - lo);
-                    keys.push_back({(long)mface[3 * f + a] * A.V + mface[3 * f + b], (int)(k * 2 + (a > b ? 1 : 0))});
-                }
+            for (int a = 0; a < 3; ++a) roff[mface[3 * f + a] + 1] += 3;
         for (long q = 0; q < A.Hn; ++q) {
-            const int v[4] = {hinge[q].x, hinge[q].y, hinge[q].z, hinge[q].w};
-            for (int a = 0; a < 4; ++a)
-                for (int b = 0; b < 4; ++b) {
-                    const int lo = std::min(a, b), hi = std::max(a, b);
-                    const long k = 10 * A.T + 6 * A.Fm + 10 * q + lo * 4 - lo * (lo - 1) / 2 + (hi - lo);
-                    keys.push_back({(long)v[a] * A.V + v[b], (int)(k * 2 + (a > b ? 1 : 0))});
-                }
+            roff[hinge[q].x + 1] += 4; roff[hinge[q].y + 1] += 4; roff[hinge[q].z + 1] += 4; roff[hinge[q].w + 1] += 4;
         }
-        std::stable_sort(keys.begin(), keys.end(),
-                         [](const std::pair<long, int>& x, const std::pair<long, int>& y) { return x.first < y.first; });
-        std::vector<int> rowptr(A.V + 1, 0), colidx, brow, src_ptr, src, diag(A.V, -1);
-        for (size_t i = 0; i < keys.size();) {
-            size_t j = i;
-            while (j < keys.size() && keys[j].first == keys[i].first) ++j;
-            int r = (int)(keys[i].first / A.V), col = (int)(keys[i].first % A.V);
-            if (r == col) diag[r] = (int)colidx.size();
-            colidx.push_back(col);
-            brow.push_back(r);
-            src_ptr.push_back((int)src.size());
-            for (size_t k = i; k < j; ++k) src.push_back(keys[k].second);
-            rowptr[r + 1]++;
-            i = j;
+        for (long v = 0; v < V; ++v) roff[v + 1] += roff[v];
+        std::vector<std::pair<int, int>> ent(roff[V]);  // (column, code)
+        {
+            std::vector<long> fill(roff.begin(), roff.end() - 1);
+            for (long t = 0; t < A.T; ++t) {
+                const int v[4] = {tet[t].x, tet[t].y, tet[t].z, tet[t].w};
+                for (int a = 0; a < 4; ++a)
+                    for (int b = 0; b < 4; ++b) {
+                        const int lo = std::min(a, b), hi = std::max(a, b);
+                        const int k = lo * 4 - lo * (lo - 1) / 2 + (hi - lo);
+                        ent[fill[v[a]]++] = {v[b], (int)((t * 10 + k) * 2 + (a > b ? 1 : 0))};
+                    }
+            }
+            // shell faces in flow mode: -(2 f + diagonal) - 1 (INC_POTENTIAL.h:323-339)
+            for (long f = 0; f < A.F; ++f)
+                for (int a = 0; a < 3; ++a)
+                    for (int b = 0; b < 3; ++b)
+                        ent[fill[face[3 * f + a]]++] = {face[3 * f + b], -(int)(2 * f + (a == b ? 1 : 0)) - 1};
+            // elastic-shell element blocks, stored after the tets' 10 per tet:
+            // 6 per membrane face, 10 per hinge (upper blocks, a <= b)
+            for (long f = 0; f < A.Fm; ++f)
+                for (int a = 0; a < 3; ++a)
+                    for (int b = 0; b < 3; ++b) {
+                        const int lo = std::min(a, b), hi = std::max(a, b);
+                        const long k = 10 * A.T + 6 * f + lo * 3 - lo * (lo - 1) / 2 + (hi - lo);
+                        ent[fill[mface[3 * f + a]]++] = {mface[3 * f + b], (int)(k * 2 + (a > b ? 1 : 0))};
+                    }
+            for (long q = 0; q < A.Hn; ++q) {
+                const int v[4] = {hinge[q].x, hinge[q].y, hinge[q].z, hinge[q].w};
+                for (int a = 0; a < 4; ++a)
+                    for (int b = 0; b < 4; ++b) {
+                        const int lo = std::min(a, b), hi = std::max(a, b);
+                        const long k = 10 * A.T + 6 * A.Fm + 10 * q + lo * 4 - lo * (lo - 1) / 2 + (hi - lo);
+                        ent[fill[v[a]]++] = {v[b], (int)(k * 2 + (a > b ? 1 : 0))};
+                    }
+            }
+        }
+        std::vector<int> nblk(V, 0);
+        auto sort_rows = [&](long r0, long r1) {
+            for (long r = r0; r < r1; ++r) {
+                auto b0 = ent.begin() + roff[r], b1 = ent.begin() + roff[r + 1];
+                std::stable_sort(b0, b1, [](const std::pair<int, int>& x, const std::pair<int, int>& y) {
+                    return x.first < y.first;
+                });
+                int n = 0;
+                for (auto it = b0; it != b1; ++it)
+                    if (it == b0 || it->first != (it - 1)->first) ++n;
+                nblk[r] = n;
+            }
+        };
+        {
+            const long nth = std::max<long>(1, std::min<long>(std::thread::hardware_concurrency(), V / 4096 + 1));
+            std::vector<std::thread> th;
+            for (long k = 1; k < nth; ++k) th.emplace_back(sort_rows, V * k / nth, V * (k + 1) / nth);
+            sort_rows(0, V / nth);
+            for (auto& x : th) x.join();
+        }
+        std::vector<int> rowptr(V + 1, 0), colidx, brow, src_ptr, src(roff[V]), diag(V, -1);
+        for (long v = 0; v < V; ++v) rowptr[v + 1] = nblk[v];
+        for (long v = 0; v < V; ++v) rowptr[v + 1] += rowptr[v];
+        colidx.resize(rowptr[V]);
+        brow.resize(rowptr[V]);
+        src_ptr.resize(rowptr[V]);
+        for (long r = 0; r < V; ++r) {
+            int bk = rowptr[r] - 1;
+            for (long e = roff[r]; e < roff[r + 1]; ++e) {
+                if (e == roff[r] || ent[e].first != ent[e - 1].first) {
+                    ++bk;
+                    colidx[bk] = ent[e].first;
+                    brow[bk] = (int)r;
+                    src_ptr[bk] = (int)e;
+                    if (ent[e].first == r) diag[r] = bk;
+                }
+                src[e] = ent[e].second;
+            }
         }
         src_ptr.push_back((int)src.size());
-        for (long v = 0; v < A.V; ++v) rowptr[v + 1] += rowptr[v];
         A.B = (long)colidx.size();
         // vertices without tets still need a diagonal block
         for (long v = 0; v < A.V; ++v)
