@@ -119,13 +119,23 @@ void extract_surface(int V, const std::vector<int>& tets, std::vector<int>& tris
         return inv & 1;
     };
     std::vector<long> order(faces.size());
-    std::iota(order.begin(), order.end(), 0);
-    std::sort(order.begin(), order.end(), [&](long a, long b) {
-        const Face &A = faces[a], &B = faces[b];
-        for (int d = 0; d < 3; ++d)
-            if (A.s[d] != B.s[d]) return A.s[d] < B.s[d];
-        return a < b;
-    });
+    if (V <= (1 << 21)) {
+        // the sorted triple packed in 63 bits, ties by face index
+        std::vector<std::pair<uint64_t, long>> key(faces.size());
+        for (size_t i = 0; i < faces.size(); ++i)
+            key[i] = {((uint64_t)faces[i].s[0] << 42) | ((uint64_t)faces[i].s[1] << 21) | (uint64_t)faces[i].s[2],
+                      (long)i};
+        std::sort(key.begin(), key.end());
+        for (size_t i = 0; i < faces.size(); ++i) order[i] = key[i].second;
+    } else {
+        std::iota(order.begin(), order.end(), 0);
+        std::sort(order.begin(), order.end(), [&](long a, long b) {
+            const Face &A = faces[a], &B = faces[b];
+            for (int d = 0; d < 3; ++d)
+                if (A.s[d] != B.s[d]) return A.s[d] < B.s[d];
+            return a < b;
+        });
+    }
     std::vector<std::array<int, 3>> bnd;
     for (size_t i = 0; i < order.size();) {
         size_t j = i;
