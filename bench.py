@@ -358,8 +358,8 @@ def run_flow(args):
             kw["pcg_local_degree"] = args.pcg_local_degree
         if args.caller_vertex_order:
             kw["caller_vertex_order"] = 1
-        c = idp.Context(h=H, newton_tol=1e-3, max_newton=args.max_newton, mode=m, device=local,
-                        pcg_grid_cta_vertices=args.pcg_grid_cta_vertices, **kw)
+        kw.setdefault("pcg_grid_cta_vertices", args.pcg_grid_cta_vertices)
+        c = idp.Context(h=H, newton_tol=1e-3, max_newton=args.max_newton, mode=m, device=local, **kw)
         c.add_instance(p["X"], p["tets"], p["mass"], p["lam"], p["mu"], p["dHat2"], p["kappa"], p["kappa_max"])
         c.commit()
         return c

@@ -739,7 +739,7 @@ __global__ void __launch_bounds__(GP_THREADS, 3) k_pcg_grid(
     S.dinv = reinterpret_cast<T*>(smem_raw + (((size_t)(nvmax + 1) * 4 + 15) & ~size_t(15)));
     S.val = reinterpret_cast<T*>(smem_raw + grid_smem_fixed(nvmax, sizeof(T), local_deg > 0));
     S.col = reinterpret_cast<int*>(S.val + 9L * cap_blocks);
-    T* ya = S.dinv + 9 * nvmax;  // polynomial preconditioner: two iterates and their sum
+    T* ya = S.dinv + 9 * nvmax;  // polynomial preconditioner: two iterates and their sum (local_deg > 0 only)
     T* yb = ya + 3 * nvmax;
     T* yz = yb + 3 * nvmax;
     const int kb0 = rowptr[v0];
@@ -871,8 +871,10 @@ __global__ void __launch_bounds__(GP_THREADS, 3) k_pcg_grid(
                 q[i3] = T(0);
                 sv[i3] = T(0);
                 p[i3] = T(0);
-                ya[3 * lv + d] = uv[d];
-                yz[3 * lv + d] = uv[d];
+                if (local_deg > 0) {  // ya/yz overlay the cached values otherwise
+                    ya[3 * lv + d] = uv[d];
+                    yz[3 * lv + d] = uv[d];
+                }
             }
         }
         if (local_deg > 0) local_poly(u);  // u = M r
@@ -904,8 +906,10 @@ __global__ void __launch_bounds__(GP_THREADS, 3) k_pcg_grid(
                 const T* D = S.dinv + 9 * lv;
                 const T mv = fixed ? T(0) : D[3 * l8] * w0 + D[3 * l8 + 1] * w1 + D[3 * l8 + 2] * w2;
                 m0[3 * v + l8] = mv;
-                ya[3 * lv + l8] = mv;
-                yz[3 * lv + l8] = mv;
+                if (local_deg > 0) {
+                    ya[3 * lv + l8] = mv;
+                    yz[3 * lv + l8] = mv;
+                }
             }
         }
         if (local_deg > 0) local_poly(m0);  // m = M w
@@ -970,8 +974,10 @@ __global__ void __launch_bounds__(GP_THREADS, 3) k_pcg_grid(
                         const T* D = S.dinv + 9 * lv;
                         const T mv = fixed ? T(0) : D[3 * l8] * w0 + D[3 * l8 + 1] * w1 + D[3 * l8 + 2] * w2;
                         mn_[3 * v + l8] = mv;
-                        ya[3 * lv + l8] = mv;
-                        yz[3 * lv + l8] = mv;
+                        if (local_deg > 0) {
+                            ya[3 * lv + l8] = mv;
+                            yz[3 * lv + l8] = mv;
+                        }
                     }
                 }
                 if (local_deg > 0) local_poly(mn_);  // m = M w
