@@ -81,7 +81,7 @@ def test_penalty_stiffness_doubling_ends_at_an_oracle_solution(oracle, gpu_lib):
     ctx, r, Xg, its = run_both(oracle, idp, pb, idp.MODE_FP64)
     prog = pb.last_stats["dbc_progress"]
     assert max(s for _, _, s in prog) >= 2e6  # the oracle did double
-    assert r["status"] == idp.IDP_OK
+    assert r["status"] in (idp.IDP_OK, idp.IDP_WARN_ITER_CAP)  # converged (a capped ACCD loop stays safe)
     assert np.array_equal(Xg[far], X[far])  # fixed rows stay
     d0 = np.linalg.norm(tgt - X[rows])
     assert np.linalg.norm(tgt - Xg[rows]) <= 0.01 * d0 + 1e-15
