@@ -806,11 +806,29 @@ __global__ void __launch_bounds__(GP_THREADS, 3) k_pcg_grid(
     };
     // CTA-local polynomial preconditioner: with y0 = D^-1 v in ya and yz,
     // y_{k+1} = y_k - D^-1 A_loc y_k, z = y_0 + ... + y_deg, where A_loc is
-    // the matrix's blocks between this CTA's rows (block Jacobi over the CTA
-    // subdomains, each block inverted by a truncated Neumann series). For an
+    // the matrix's blocks between this CTA's subdomain rows (block Jacobi over
+    // the CTA subdomains, each block inverted by a truncated Neumann series). For an
     // even degree p(S) = sum_k (I - S)^k > 0 for every S = D^-1/2 A_loc D^-1/2
     // > 0, so M^-1 = p(D^-1 A_loc) D^-1 is symmetric positive definite. The
     // result z is written to dst (global) for the instance's next SpMV.
+    // The subdomain is the CTA's rows whose blocks all sit in shared memory
+    // (a prefix [0, nloc) of its rows); a row past it is its own block
+    // (A_loc = D there, so its Neumann terms vanish and it keeps y0 = D^-1 v).
+    int nloc = 0;
+    if (local_deg > 0) {
+        if (threadIdx.x == 0) {
+            int lo = 0, hi = nv;  // largest r with S.row[r] <= S.ncache
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) / 2;
+                if (S.row[mid] <= S.ncache) lo = mid;
+                else hi = mid - 1;
+            }
+            sh_i[0] = lo;
+        }
+        __syncthreads();
+        nloc = sh_i[0];
+        __syncthreads();
+    }
     auto local_poly = [&](T* dst) {
         __syncthreads();
         T* yin = ya;
@@ -819,17 +837,17 @@ __global__ void __launch_bounds__(GP_THREADS, 3) k_pcg_grid(
             for (int base = kRows * warp; base < nv; base += kRows * nw) {
                 const int lv = base + lane / kRL;
                 const bool act = lv < nv;
+                const bool inside = lv < nloc;
                 const int v = v0 + (act ? lv : 0);
                 const bool fixed = act && dbc[v];
                 T a0 = 0, a1 = 0, a2 = 0;
-                if (act && !fixed) {
+                if (inside && !fixed) {
                     const int ka = S.row[lv], kz = S.row[lv + 1];
+#pragma unroll 4
                     for (int k = ka + l8; k < kz; k += kRL) {
-                        const bool cached = k < S.ncache;
-                        const int c = cached ? S.col[k] : colidx[kb0 + k];
-                        const unsigned lc = (unsigned)(c - v0);
-                        if (lc >= (unsigned)nv) continue;
-                        const T* mm = cached ? S.val + 9 * k : val + 9L * (kb0 + k);
+                        const unsigned lc = (unsigned)(S.col[k] - v0);
+                        if (lc >= (unsigned)nloc) continue;
+                        const T* mm = S.val + 9 * k;
                         const T x0 = yin[3 * lc], x1 = yin[3 * lc + 1], x2 = yin[3 * lc + 2];
                         a0 += mm[0] * x0 + mm[1] * x1 + mm[2] * x2;
                         a1 += mm[3] * x0 + mm[4] * x1 + mm[5] * x2;
@@ -839,7 +857,9 @@ __global__ void __launch_bounds__(GP_THREADS, 3) k_pcg_grid(
                 group_sum3(a0, a1, a2);
                 if (act && l8 < 3) {
                     const T* D = S.dinv + 9 * lv;
-                    const T yn = fixed ? T(0) : yin[3 * lv + l8] - (D[3 * l8] * a0 + D[3 * l8 + 1] * a1 + D[3 * l8 + 2] * a2);
+                    const T yn = (fixed || !inside)
+                                     ? T(0)
+                                     : yin[3 * lv + l8] - (D[3 * l8] * a0 + D[3 * l8 + 1] * a1 + D[3 * l8 + 2] * a2);
                     yout[3 * lv + l8] = yn;
                     yz[3 * lv + l8] += yn;
                 }
