@@ -90,12 +90,13 @@ def _context_for(tet, X, nodeAttr, tetEl, dHat2, kappaVec, DBC, h, NewtonTol, th
     dbc_idx, _ = _dbc_rows(DBC)
     key = (_digest(tet, nodeAttr["x0"], nodeAttr["m"], tetEl["lambda"], tetEl["mu"],
                    np.zeros(0, np.int32) if dbc_idx is None else dbc_idx),
-           X.shape, float(dHat2), float(h), float(NewtonTol), float(thickness), mode)
+           X.shape, float(dHat2), float(h), float(NewtonTol), float(thickness), mode,
+           tuple(sorted(DiscreteShell.params.items())))
     if _Cache.key == key and _Cache.ctx is not None:
         return _Cache.ctx
     if _Cache.ctx is not None:
         _Cache.ctx.close()
-    ctx = Context(h=h, newton_tol=NewtonTol, thickness=thickness, mode=mode)
+    ctx = Context(h=h, newton_tol=NewtonTol, thickness=thickness, mode=mode, **DiscreteShell.params)
     ctx.add_instance(X, tet, nodeAttr["m"], tetEl["lambda"], tetEl["mu"], dHat2, kappaVec[0], kappaVec[1],
                      X0=nodeAttr["x0"], dbc_idx=dbc_idx)
     ctx.commit()
@@ -141,13 +142,14 @@ def _shell_context_for(Elem, X, nodeAttr, elemAttr, elasticityAttr, bendingStiff
     key = ("shell", _digest(np.asarray(Elem, dtype=np.int32), nodeAttr["x0"], nodeAttr["m"], elasticityAttr["vol"],
                             elasticityAttr["lambda"], elasticityAttr["mu"], P.reshape(-1)[:1],
                             np.zeros(0, np.int32) if dbc_idx is None else dbc_idx),
-           float(bendingStiffMult), X.shape, float(dHat2), float(h), float(NewtonTol), float(thickness), mode)
+           float(bendingStiffMult), X.shape, float(dHat2), float(h), float(NewtonTol), float(thickness), mode,
+           tuple(sorted(DiscreteShell.params.items())))
     if _Cache.key == key and _Cache.ctx is not None:
         return _Cache.ctx
     if _Cache.ctx is not None:
         _Cache.ctx.close()
     mat = shell_material(Elem, nodeAttr, elemAttr, elasticityAttr, bendingStiffMult)
-    ctx = Context(h=h, newton_tol=NewtonTol, thickness=thickness, mode=mode)
+    ctx = Context(h=h, newton_tol=NewtonTol, thickness=thickness, mode=mode, **DiscreteShell.params)
     ctx.add_elastic_shell_instance(X, Elem, mat["density"], mat["E"], mat["nu"], mat["thickness"], dHat2,
                                    kappaVec[0], kappaVec[1], bending_mult=mat["bending_mult"], X0=nodeAttr["x0"],
                                    dbc_idx=dbc_idx, mass=mat["mass"])
@@ -158,6 +160,7 @@ def _shell_context_for(Elem, X, nodeAttr, elemAttr, elasticityAttr, bendingStiff
 
 class DiscreteShell:
     mode = MODE_MIXED
+    params: dict = {}  # further idp_params fields for the contexts the calls create
 
     @staticmethod
     def Advance_One_Step_IE_Hinge(Elem, segs, DBC, edge2tri, edgeStencil, edgeInfo, thickness, bendingStiffMult,
