@@ -383,14 +383,17 @@ class TetIPCSim(_DirichletDriver):
         self.thickness = offset
 
     def advance_one_time_step(self, dt=None):
-        DiscreteShell.mode = self.mode
         h = dt or self.dt
         self._step_dbc(h)
-        it = FEM.DiscreteShell.Advance_One_Step_IE_Hinge(
-            None, None, self._dbc_arg(), None, None, None, self.thickness, 0, None, None, None, None, None,
-            self.bodyForce, h, self.PNTol, True, self.dHat2, self.kappa, 0, 1e-6, 1, None, None, False, self.X,
-            self.nodeAttr, None, None, None, self.tet, None, self.tetElasticity, None, None, None, None, None, None,
-            10, None, "")
+        mode, DiscreteShell.mode = DiscreteShell.mode, self.mode  # this driver's precision for its own call only
+        try:
+            it = FEM.DiscreteShell.Advance_One_Step_IE_Hinge(
+                None, None, self._dbc_arg(), None, None, None, self.thickness, 0, None, None, None, None, None,
+                self.bodyForce, h, self.PNTol, True, self.dHat2, self.kappa, 0, 1e-6, 1, None, None, False, self.X,
+                self.nodeAttr, None, None, None, self.tet, None, self.tetElasticity, None, None, None, None, None,
+                None, 10, None, "")
+        finally:
+            DiscreteShell.mode = mode
         self.PNIterCount += it
         self.t += h
         return it

@@ -27,7 +27,7 @@ import os
 
 DEFAULT_SPACE = {
     "pcg_grid_cta_vertices": [112, 80, 144],
-    "pcg_local_degree": [2, 0, 4],
+    "pcg_local_degree": [0, 2, 4],
     "pcg_grid_min_vertices": [16384, 8192, 32768],
     "contact_block_vertices": [192, 96],
 }

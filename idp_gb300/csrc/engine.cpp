@@ -469,7 +469,7 @@ void idp_default_params(idp_params* p) {
     p->contact_block_vertices = 0;
     p->verify_iterates = 0;
     p->caller_vertex_order = 0;
-    p->pcg_local_degree = 2;
+    p->pcg_local_degree = 0;
 }
 
 const char* idp_status_str(int s) {

@@ -269,7 +269,7 @@ struct Work {
     double* tol_inst = nullptr;              // per-instance PCG tolerance (device)
     long grid_min_v = 16384;                 // grid-wide PCG above this many vertices
     long grid_vper = 112;                    // vertices per CTA in the grid-wide PCG
-    int local_deg = 2;                       // degree of the grid PCG's CTA-local polynomial preconditioner
+    int local_deg = 0;                       // degree of the grid PCG's CTA-local polynomial preconditioner
     int cl_cap = kClusterCap;                // vertices per dense contact block
     long long accd_maxit = 0;                // diagnostics (IDP_PROFILE)
     long long accd_long = 0, accd_total = 0, accd_pairs = 0;

@@ -76,11 +76,11 @@ typedef struct idp_params {
                              the caller's order. Nonzero: stored in the caller's
                              order.                                                  */
     int pcg_local_degree; /* grid-wide PCG (pcg_grid_min_vertices) preconditioner:
-                             0 = 3x3 block Jacobi; an even degree d (default 2) =
-                             block Jacobi over each CTA's rows, every block inverted
-                             by d terms of a Neumann series in D^-1 A_loc (symmetric
-                             positive definite for even d). Instances solved with
-                             contact blocks keep 3x3 block Jacobi.                  */
+                             0 (default) = 3x3 block Jacobi; an even degree d =
+                             block Jacobi over each CTA's subdomain rows, every block
+                             inverted by d terms of a Neumann series in D^-1 A_loc
+                             (symmetric positive definite for even d). Instances
+                             solved with contact blocks keep 3x3 block Jacobi.      */
 } idp_params;
 
 typedef struct idp_result {
