@@ -25,3 +25,14 @@ def gpu_lib():
     g.build()
     import idp_gb300
     return idp_gb300.load()
+
+
+@pytest.fixture(autouse=True)
+def reference_call_defaults():
+    """Every test starts the reference-shaped entry points from their
+    defaults (precision mode, extra context parameters)."""
+    from idp_gb300 import api
+
+    mode, params = api.DiscreteShell.mode, dict(api.DiscreteShell.params)
+    yield
+    api.DiscreteShell.mode, api.DiscreteShell.params = mode, params

@@ -43,11 +43,14 @@ def test_hinge_call_matches_the_c_abi(gpu_lib):
     from idp_gb300 import api
     from idp_gb300.api import FEM
 
+    # a cantilever: the base fixed, the bar swung sideways and pulled down
+    # by gravity (no self-contact, a few Newton iterations per step)
     X, tets, tgt, pr = bar_case(ang=0.3)
     V = X.shape[0]
     h = 0.1
-    v = (tgt - X) / h
-    fixed = np.arange(0, V, 7, dtype=np.int32)[:6]
+    v = np.zeros_like(X)
+    v[:, 0] = 0.5 * X[:, 2]
+    fixed = np.nonzero(X[:, 2] < 1e-12)[0].astype(np.int32)
     DBC = np.concatenate([fixed[:, None].astype(np.float64), X[fixed]], axis=1)  # (index, target)
     b = np.zeros_like(X)
     b[:, 1] = -9.8 * pr["mass"]  # gravity
@@ -78,12 +81,13 @@ def test_hinge_call_matches_the_c_abi(gpu_lib):
     assert np.array_equal(a["X"], Xd) and kappaVec[0] == kd[0]
     # a new tet array with the same content reuses the context; different
     # content (a moved rest shape) builds a new one
-    key = api._Cache.key
+    key, c0 = api._Cache.key, api._Cache.ctx
     a2 = dict(a, tet=tets.copy())
-    FEM.DiscreteShell.Advance_One_Step_IE_Hinge(*[a2[k] for k in order])
-    assert api._Cache.key == key
+    assert api._context_for(np.asarray(a2["tet"]), a2["X"], a2["nodeAttr"], a2["tetElasticityAttr"], a2["dHat2"],
+                            kappaVec, DBC, h, 1e-3, 0.0, api.DiscreteShell.mode) is c0
     a3 = dict(a, nodeAttr=dict(a["nodeAttr"], x0=X * 1.01))
-    FEM.DiscreteShell.Advance_One_Step_IE_Hinge(*[a3[k] for k in order])
+    api._context_for(np.asarray(a3["tet"]), a3["X"], a3["nodeAttr"], a3["tetElasticityAttr"], a3["dHat2"], kappaVec,
+                     DBC, h, 1e-3, 0.0, api.DiscreteShell.mode)
     assert api._Cache.key != key
     ctx.close()
 
