@@ -598,7 +598,18 @@ def run_gpu(args):
     for w in range(args.warmup):
         ctx.restore_state()
         t0 = time.perf_counter()
-        _, rw = ctx.advance(check=False)
+        if args.progress:
+            # the warm-up solve in slices of 100 Newton iterations, reporting
+            # how many instances are still iterating (same result as advance)
+            ctx.step_begin()
+            n_active, done = len(probs), 0
+            while n_active:
+                _, n_active, rw = ctx.step_iterate(100)
+                done += 100
+                progress(f"warm-up step {w}: {done} iterations, {n_active} instances iterating, "
+                         f"{time.perf_counter() - t0:.0f} s")
+        else:
+            _, rw = ctx.advance(check=False)
         progress(f"warm-up step {w}: {time.perf_counter() - t0:.1f} s, Newton max "
                  f"{max(r['newton_iters'] for r in rw)}, converged "
                  f"{sum(1 for r in rw if r['status'] in (idp.IDP_OK, idp.IDP_WARN_ITER_CAP))}/{len(rw)}")
