@@ -103,6 +103,16 @@ def parse():
     return ap.parse_args()
 
 
+def extra_params(args):
+    """Library parameters the command line sets for the timed arm."""
+    kw = {}
+    if args.pcg_local_degree >= 0:
+        kw["pcg_local_degree"] = args.pcg_local_degree
+    if args.caller_vertex_order:
+        kw["caller_vertex_order"] = 1
+    return kw
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -575,7 +585,7 @@ def run_gpu(args):
     max_newton = budget if budget > 0 else args.max_newton
     if budget > 0:
         desc += f"; first {budget} Newton iterations of every instance from the rest state"
-    ctx = idp.Context(h=0.1, newton_tol=1e-3, max_newton=max_newton, mode=mode, device=local)
+    ctx = idp.Context(h=0.1, newton_tol=1e-3, max_newton=max_newton, mode=mode, device=local, **extra_params(args))
     for i, p in enumerate(probs):
         ctx.add_instance(p["X"], p["tets"], p["mass"], p["lam"], p["mu"], p["dHat2"], p["kappa"], p["kappa_max"])
         ctx.set_velocity(i, (p["target"] - p["X"]) / 0.1)
@@ -801,7 +811,7 @@ def run_serve(args):
         if t > args.duration:
             break
         arr.append((t, int(rng.integers(len(pool)))))
-    params = dict(h=0.1, newton_tol=1e-3, max_newton=args.serve_newton_cap, device=local)
+    params = dict(h=0.1, newton_tol=1e-3, max_newton=args.serve_newton_cap, device=local, **extra_params(args))
     # FP64 one at a time: service time of every pool job (wall time of one
     # context's add + commit + solve + read back, after a warm-up solve)
     svc, e64 = [], []
