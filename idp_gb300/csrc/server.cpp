@@ -4,10 +4,10 @@
 // context (one CUDA stream and one device arena) holding the jobs it is
 // solving. A worker advances its jobs a few Newton iterations at a time
 // (step_iterate); between those chunks it releases every job that finished
-// (its result is written at once) and admits jobs from the head of the queue
-// into its running arena: the jobs still iterating are snapshotted, the
-// arena is rebuilt with them and the new jobs, and their Newton loops resume
-// where they were. Workers run concurrently on their own streams. The
+// (its result is written at once) and, once half of its slots are free,
+// admits jobs from the head of the queue into its running arena: the jobs
+// still iterating are snapshotted, the arena is rebuilt with them and the new
+// jobs, and their Newton loops resume where they were. Workers run concurrently on their own streams. The
 // reference has no counterpart: its Python driver advances one scene per
 // call (Python/Drivers/FEMDiscreteShellBase.py:333-361).
 //
@@ -61,7 +61,7 @@ struct idp_server {
     idp_params P{};
     double budget = 0;
     int max_batch = 1;
-    int chunk = 4;                // Newton iterations between admission points
+    int chunk = 8;                // Newton iterations between admission points
     bool simulated = false;
     double sim_ms_per_kvertex = 0;
     std::mutex mu;
@@ -241,10 +241,13 @@ void worker(idp_server* S, int w) {
             S->cv_work.notify_all();
             continue;
         }
-        // admission at the queue head, between Newton iterations
+        // admission at the queue head, between Newton iterations; a worker
+        // that is iterating admits once half of its slots are free (each
+        // admission rebuilds its arena, so admissions are batched)
         std::vector<Job*> fresh;
         double fp = 0;
-        while (!S->pending.empty() && S->live[w] + (int)fresh.size() < S->max_batch &&
+        const bool may_admit = S->live[w] == 0 || S->max_batch - S->live[w] >= std::max(1, S->max_batch / 2);
+        while (may_admit && !S->pending.empty() && S->live[w] + (int)fresh.size() < S->max_batch &&
                S->total_with(w, fp + S->pending.front()->footprint) <= S->budget) {
             fp += S->pending.front()->footprint;
             fresh.push_back(S->pending.front());

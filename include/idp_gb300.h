@@ -323,8 +323,9 @@ int idp_check_intersection_all(idp_ctx* ctx, int32_t* counts);
  * of worker threads, each driving its own context and CUDA stream, solves
  * the jobs it holds a few Newton iterations at a time. Between those chunks a
  * worker writes the result of every job that finished (at once, not when the
- * slowest job it holds finishes) and admits jobs from the head of the queue
- * into its running arena (max_batch jobs at most): the jobs still iterating
+ * slowest job it holds finishes) and, once half of its max_batch slots are
+ * free (or it holds none), admits jobs from the head of the queue into its
+ * running arena (max_batch jobs at most): the jobs still iterating
  * are carried over to a rebuilt arena with the new ones and their Newton
  * loops continue where they were. Workers run on the device at the same
  * time. Admission keeps the sum over workers of max(device bytes the worker's
