@@ -943,9 +943,11 @@ int idp_commit(idp_ctx* c) {
     std::vector<HostInstance> dview(nI);
     std::vector<const HostInstance*> hv(nI);
     for (int i = 0; i < nI; ++i) {
-        c->inst[i].perm.clear();
+        if (c->P.caller_vertex_order || c->inst[i].perm.size() != (size_t)c->inst[i].V) c->inst[i].perm.clear();
         if (!c->P.caller_vertex_order && c->inst[i].V > 1) {
-            dview[i] = to_device_order(c->inst[i], morton_order(c->inst[i]));
+            // an instance added from a committed copy keeps its order
+            dview[i] = to_device_order(c->inst[i], c->inst[i].perm.empty() ? morton_order(c->inst[i])
+                                                                           : c->inst[i].perm);
             c->inst[i].perm = dview[i].perm;
             hv[i] = &dview[i];
         } else {
@@ -1962,6 +1964,18 @@ int step_iterate(idp_ctx* c, int max_iters, idp_result* results, int* n_active) 
             worst = st[i].status;
     }
     return worst;
+}
+
+int add_prebuilt(idp_ctx* c, const HostInstance& h) {
+    if (!c) return -IDP_ERR_INVALID_ARG;
+    if (c->committed) return -IDP_ERR_STATE;
+    c->inst.push_back(h);
+    return (int)c->inst.size() - 1;
+}
+
+const HostInstance* instance_host(idp_ctx* c, int i) {
+    if (!c || i < 0 || i >= (int)c->inst.size()) return nullptr;
+    return &c->inst[i];
 }
 
 int snapshot_instance(idp_ctx* c, int i, InstSnapshot& out) {

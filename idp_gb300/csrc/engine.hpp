@@ -337,6 +337,10 @@ struct Params {
 int step_begin(idp_ctx* c, const std::vector<unsigned char>& which);
 int step_iterate(idp_ctx* c, int max_iters, idp_result* results, int* n_active);
 int step_prepare_resumed(idp_ctx* c);
+// an instance taken from another context's committed copy (surface,
+// device order and rest data already built), before idp_commit
+int add_prebuilt(idp_ctx* c, const HostInstance& h);
+const HostInstance* instance_host(idp_ctx* c, int i);
 int snapshot_instance(idp_ctx* c, int i, InstSnapshot& out);
 int resume_instance(idp_ctx* c, int i, const InstSnapshot& in);
 bool instance_active(idp_ctx* c, int i);  // still iterating in the step in flight

@@ -44,6 +44,7 @@ struct Job {
     double* v_out = nullptr;
     double footprint = 0;
     bool done = false;
+    std::shared_ptr<idp::HostInstance> host;  // built at its first admission, reused by later re-packs
     int sim_left = 0;  // simulated mode: Newton iterations still to run
     idp_job_info info{};
 };
@@ -146,13 +147,18 @@ int repack(idp_server* S, Slots& W, const std::vector<Job*>& fresh) {
         return rc;
     }
     for (Job* j : W.job) {
-        int k = idp_add_instance(W.ctx, j->V, j->X.data(), j->X0.data(), j->T, j->tets.data(), j->mass.data(),
-                                 j->lam.data(), j->mu.data(), j->nDBC, j->dbc.empty() ? nullptr : j->dbc.data(),
-                                 j->dHat2, j->kappa, j->kappa_max);
+        // a carried-over job's instance is re-added from its cached copy
+        // (no second surface extraction; its state comes from the snapshot)
+        int k = j->host ? idp::add_prebuilt(W.ctx, *j->host)
+                        : idp_add_instance(W.ctx, j->V, j->X.data(), j->X0.data(), j->T, j->tets.data(),
+                                           j->mass.data(), j->lam.data(), j->mu.data(), j->nDBC,
+                                           j->dbc.empty() ? nullptr : j->dbc.data(), j->dHat2, j->kappa, j->kappa_max);
         if (k < 0) return -k;
         if (k >= (int)keep.size() && j->has_v && (rc = idp_set_velocity(W.ctx, k, j->v.data()))) return rc;
     }
     if ((rc = idp_commit(W.ctx))) return rc;
+    for (size_t k = keep.size(); k < W.job.size(); ++k)
+        if (!W.job[k]->host) W.job[k]->host = std::make_shared<idp::HostInstance>(*idp::instance_host(W.ctx, (int)k));
     for (size_t k = 0; k < keep.size(); ++k)
         if ((rc = idp::resume_instance(W.ctx, (int)k, snaps[k]))) return rc;
     std::vector<unsigned char> which(W.job.size(), 0);
