@@ -49,7 +49,8 @@ class Params(C.Structure):
                 ("pcg_rel_tol", C.c_double), ("pcg_max_iters", C.c_int), ("thickness", C.c_double),
                 ("device", C.c_int), ("pcg_grid_min_vertices", C.c_int), ("pcg_grid_cta_vertices", C.c_int),
                 ("contact_block_vertices", C.c_int), ("verify_iterates", C.c_int),
-                ("caller_vertex_order", C.c_int), ("pcg_local_degree", C.c_int)]
+                ("caller_vertex_order", C.c_int), ("pcg_local_degree", C.c_int),
+                ("surface_device_min_tets", C.c_int)]
 
 
 class Result(C.Structure):

@@ -24,7 +24,7 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relax
           "-Xcompiler", "-Wall", "-Xcompiler", "-Wno-unused-function", "-I", INCLUDE]
 EXACT_FP64 = {"contact.cu", "ccd.cu", "flow.cu", "dirichlet.cu"}
 UNITS = ["prims.cu", "tet.cu", "contact.cu", "barrier.cu", "ccd.cu", "solver.cu", "precond.cu", "vecops.cu",
-         "flow.cu", "shell.cu", "shell_elastic.cu", "dirichlet.cu", "engine.cpp", "server.cpp"]
+         "flow.cu", "shell.cu", "shell_elastic.cu", "dirichlet.cu", "surface.cu", "engine.cpp", "server.cpp"]
 HEADERS = ["common.cuh", "prims.cuh", "geom.cuh", "grid.cuh", "engine.hpp", "predicates.cuh", "psd.cuh"]
 
 

@@ -470,6 +470,7 @@ void idp_default_params(idp_params* p) {
     p->verify_iterates = 0;
     p->caller_vertex_order = 0;
     p->pcg_local_degree = 0;
+    p->surface_device_min_tets = 0;
 }
 
 const char* idp_status_str(int s) {
@@ -599,7 +600,14 @@ int idp_add_instance(idp_ctx* c, int V, const double* X, const double* X0, int T
     h.dHat2 = dHat2;
     h.kappa = kappa;
     h.kappa_max = kappa_max;
-    extract_surface(V, h.tets, h.tris, h.edges, h.nodes);
+    const long dev_min = c->P.surface_device_min_tets == 0 ? 65536 : c->P.surface_device_min_tets;
+    if (dev_min > 0 && T >= dev_min && V <= (1 << 21)) {
+        cudaSetDevice(c->P.device);
+        const int rc = idp::extract_surface_device(V, h.tets, h.tris, h.edges, h.nodes, c->s);
+        if (rc) return -rc;
+    } else {
+        extract_surface(V, h.tets, h.tris, h.edges, h.nodes);
+    }
     double s = 0;
     for (size_t e = 0; e + 1 < h.edges.size(); e += 2) {
         const double* a = &h.X0[3 * h.edges[e]];

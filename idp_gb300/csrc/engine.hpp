@@ -409,6 +409,9 @@ int vec_zero_dbc(Arena& A, double* g, cudaStream_t s);
 // (out) for the instance's range [v0, v0 + n) of 3-vectors
 int perm_to_device(Arena& A, long v0, long n, const double* in, double* out, cudaStream_t s);
 int perm_to_caller(Arena& A, long v0, long n, const double* in, double* out, cudaStream_t s);
+// surface.cu: surface of a tet mesh in the reference's order, on the device
+int extract_surface_device(int V, const std::vector<int>& tets, std::vector<int>& tris, std::vector<int>& edges,
+                           std::vector<int>& nodes, cudaStream_t s);
 // dirichlet.cu: moving Dirichlet conditions (the augmented Lagrangian)
 int dbc_classify(Arena& A, const double* X, double* dir, int* moving, cudaStream_t s);
 int dbc_snap(Arena& A, double* X, cudaStream_t s);

@@ -81,6 +81,11 @@ typedef struct idp_params {
                              inverted by d terms of a Neumann series in D^-1 A_loc
                              (symmetric positive definite for even d). Instances
                              solved with contact blocks keep 3x3 block Jacobi.      */
+    int surface_device_min_tets; /* tet meshes with at least this many tets (and
+                             fewer than 2^21 vertices) extract their surface in
+                             idp_add_instance on the device (same lists, same
+                             order as the host extraction); 0 = default (65536),
+                             negative = always on the host                          */
 } idp_params;
 
 typedef struct idp_result {
