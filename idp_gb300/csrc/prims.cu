@@ -55,7 +55,7 @@ __global__ void rs_scatter(const uint64_t* __restrict__ keys, const uint32_t* __
                 wc[w][t] = run;
                 run += c;
             }
-            // stash this round's total in the slot past the prefix: reuse via register
+            // this pass's total stays in a register (the prefix overwrote the slots)
             __syncthreads();
             if (valid) {
                 uint32_t pos = gbase[d] + running[d] + wc[warp][d] + rank_w;
