@@ -22,6 +22,7 @@ normal-flow scripts drive (``add_shell_3D``, ``initialize``,
 from __future__ import annotations
 
 import math
+import os
 
 import numpy as np
 
@@ -406,7 +407,9 @@ class ShellFlowSim(_DirichletDriver):
     (Python/Drivers/SimulationBase.py:76-103) and advance_one_time_step with
     Update_Normal_Flow_Neumann (FEMDiscreteShellBase.py:266-276, 332-340) —
     and, with flow off, the elastic shell's Hinge step with gravity and
-    Dirichlet conditions (FEMDiscreteShellBase.py:255-361)."""
+    Dirichlet conditions (FEMDiscreteShellBase.py:255-361), including the
+    character sequences of Projects/FEMShell/16_fix_char_seq.py
+    (add_shell_with_scale_3D, lv_fn, seqDBCPath, write)."""
 
     def __init__(self, precision="double", dim=3, mode=MODE_MIXED):
         if dim != 3:
@@ -433,6 +436,9 @@ class ShellFlowSim(_DirichletDriver):
         self.mode = mode
         self._ctx = None
         self._ctx_h = None
+        self._X0 = None
+        self.lv_fn = -1
+        self.output_folder = ""
         self._init_dbc()
 
     def add_shell_3D(self, filePath, translate, rotCenter, rotAxis, rotDeg):
@@ -442,8 +448,23 @@ class ShellFlowSim(_DirichletDriver):
         meshio.transform_points(self.X, translate, rotCenter, rotAxis, rotDeg, (1.0, 1.0, 1.0), counter)
         return counter
 
-    def _mass(self):
-        X, F = self.X, self.Elem
+    def add_shell_with_scale_3D(self, filePath, translate, scale, rotCenter, rotAxis, rotDeg):
+        from . import meshio
+
+        self.X, self.Elem, counter = meshio.read_tri_obj(filePath, self.X, self.Elem)
+        meshio.transform_points(self.X, translate, rotCenter, rotAxis, rotDeg, scale, counter)
+        return counter
+
+    def write(self, frame_idx):
+        """The current shell as <output_folder>/shell<frame>.obj."""
+        from . import meshio
+
+        if self.output_folder:
+            os.makedirs(self.output_folder, exist_ok=True)
+            meshio.write_tri_obj(os.path.join(self.output_folder, f"shell{frame_idx}.obj"), self.X, self.Elem)
+
+    def _mass(self, X=None):
+        X, F = (self.X if X is None else X), self.Elem
         area = np.linalg.norm(np.cross(X[F[:, 1]] - X[F[:, 0]], X[F[:, 2]] - X[F[:, 0]]), axis=1) / 2
         m = np.zeros(X.shape[0])
         np.add.at(m, F.reshape(-1), np.repeat(area * self.shell_thickness * self.shell_density / 3, 3))
@@ -461,11 +482,31 @@ class ShellFlowSim(_DirichletDriver):
 
     def initialize_OIPC(self, thickness, offset, stiffMult=1.0):
         """Initialize_OIPC (DISCRETE_SHELL.h:555-577): d-hat = thickness,
-        kappa from the mean lumped mass."""
+        kappa from the mean lumped mass (of the rest shape in use)."""
         self.dHat2 = float(thickness) ** 2
-        k, km = initialize_oipc(float(self._mass().mean()), self.dHat2, stiffMult)
+        k, km = initialize_oipc(float(self._mass(self._X0).mean()), self.dHat2, stiffMult)
         self.kappa = [k, km, 0.0]
         self.thickness = float(offset)
+
+    def _next_frame_rest_shape(self, dt):
+        """The lv_fn sequence (FEMDiscreteShellBase.py:297-310): frame lv_fn of
+        seqDBCPath becomes the rest shape (masses and kappa follow), the
+        velocity points at it (Load_Velocity_X0, Library/Utils/MESHIO.h:987-1004)
+        and the DBC rows take their targets from it (Load_Dirichlet)."""
+        from . import meshio
+
+        path = f"{self.seqDBCPath}/{self.lv_fn}.obj"
+        newX, _, _ = meshio.read_tri_obj(path)
+        if newX.shape != self.X.shape:
+            raise ValueError(f"{path}: node count does not match")
+        self._X0 = newX
+        self.initialize_OIPC(math.sqrt(self.dHat2), self.thickness)  # default stiffMult, as the reference does
+        dirichlet.load_dirichlet(path, 0, (0.0, 0.0, 0.0), self.DBC)
+        self.lv_fn += 1
+        if self._ctx is not None:
+            self._ctx.close()
+            self._ctx = None
+        return (newX - self.X) / dt
 
     def _context(self, h):
         if self._ctx is not None and self._dbc_n != len(self.DBC):  # the DBC rows changed: rebuild
@@ -476,7 +517,7 @@ class ShellFlowSim(_DirichletDriver):
             if self._ctx is not None:  # a new step size keeps the elastic shell's rest shape and velocity
                 v = self._ctx.state(0)[1]
                 self._ctx.close()
-            else:
+            elif self._X0 is None:
                 self._X0 = X.copy()
             self._ctx = Context(h=h, newton_tol=self.PNTol, thickness=self.thickness, mode=self.mode)
             dbc_idx = self.DBC.indices if len(self.DBC) else None
@@ -492,7 +533,7 @@ class ShellFlowSim(_DirichletDriver):
                 if v is not None:
                     self._ctx.set_velocity(0, v)
                 if any(g != 0 for g in self.gravity):  # b = M g (Initialize_Discrete_Shell)
-                    self._ctx.set_body_force(0, self._mass()[:, None] * np.asarray(self.gravity, float)[None, :])
+                    self._ctx.set_body_force(0, self._mass(self._X0)[:, None] * np.asarray(self.gravity, float)[None, :])
             self._ctx.commit()
             self._ctx_h = h
         return self._ctx
@@ -500,9 +541,17 @@ class ShellFlowSim(_DirichletDriver):
     def advance_one_time_step(self, dt):
         """Advance_One_Step_IE_Flow with the normal-flow predictor in flow
         mode, Advance_One_Step_IE_Hinge of the elastic shell otherwise; the
-        Dirichlet motion is stepped first."""
+        Dirichlet motion is stepped first; with lv_fn >= 0 the next frame of
+        the sequence sets the rest shape, the velocity and the DBC targets."""
         self._step_dbc(dt)
+        v_seq = None
+        if self.lv_fn >= 0:
+            if self.flow:
+                raise ValueError("lv_fn frame sequences drive the elastic shell; set flow = False")
+            v_seq = self._next_frame_rest_shape(dt)
         ctx = self._context(dt)
+        if v_seq is not None:
+            ctx.set_velocity(0, v_seq)
         ctx.set_positions(0, self.X)
         ctx.set_kappa(0, self.kappa)
         if len(self.DBC):
@@ -529,3 +578,4 @@ class ShellFlowSim(_DirichletDriver):
     def run(self):
         for f in range(self.frame_num):
             self.advance_one_frame(f + 1)
+            self.write(f + 1)

@@ -5,7 +5,8 @@ Hessian times a vector within 1e-9 (FP64) / 2e-4 (mixed), constraint sets
 bit for bit, whole steps (two spheres expanding into each other) to the
 oracle's energy within 1e-6, and a buckling sphere pressed flat through
 itself to a converged oracle solution; the reference-shaped Hinge call with
-shell elements gives the direct C-ABI calls' results bit for bit."""
+shell elements gives the direct C-ABI calls' results bit for bit; a character
+sequence (each frame the next rest shape and DBC target) against the oracle."""
 import numpy as np
 import pytest
 
@@ -197,3 +198,50 @@ def test_hinge_call_with_shell_elements_matches_c_abi(oracle, gpu_lib):
     assert np.array_equal(X, Xd) and np.array_equal(nodeAttr["v"], vd) and kappaVec[0] == kd[0]
     assert r[0]["num_constraints"] > 0
     ctx.close()
+
+
+@pytest.mark.parametrize("mode,tol", [(0, 1e-5), (1, 2e-4)], ids=["fp64", "mixed"])
+def test_character_sequence_matches_oracle(oracle, gpu_lib, tmp_path, mode, tol):
+    """The shell driver over a three-frame sequence (lv_fn / seqDBCPath, as
+    the mannequin script drives it): each step takes frame k as the rest
+    shape, points the velocity at it and moves the top cap's DBC rows onto
+    it, under gravity; the oracle is fed the same rest shape, velocity,
+    kappa, body force and targets, step by step."""
+    from idp_gb300 import meshio
+    from idp_gb300.api import ShellFlowSim, initialize_oipc
+    from test_api_shell import rotated_frames
+
+    X, F = cases.sphere_shell(2)
+    meshio.write_tri_obj(tmp_path / "rest.obj", X, F)
+    sim = ShellFlowSim("double", 3, mode=mode)
+    sim.add_shell_with_scale_3D(str(tmp_path / "rest.obj"), (0, 0.75, 0), (0.5, 0.5, 0.5), (0, 0, 0), (1, 0, 0), -90)
+    sim.set_DBC((-0.1, 0.8, -0.1), (1.1, 1.1, 1.1), (0, 0, 0), (0, 0, 0), (1, 0, 0), 0)
+    h, g = 0.1, np.array([0.0, -1.0, 0.0])
+    sim.dt = sim.frame_dt = h
+    sim.gravity = tuple(g)
+    sim.PNTol = 1e-5
+    sim.initialize(1000, 1e4, 0.4, 0.01, 0)
+    sim.initialize_OIPC(1e-3, 0)
+    (tmp_path / "seq").mkdir()
+    for k, Y in enumerate(rotated_frames(sim.X, 3), 1):
+        meshio.write_tri_obj(tmp_path / "seq" / f"{k}.obj", Y, F)
+    sim.lv_fn, sim.seqDBCPath, sim.output_folder = 1, str(tmp_path / "seq"), str(tmp_path / "out")
+    rows = sim.DBC.indices.copy()
+    assert rows.size > 4
+    for f in range(1, 4):
+        Y, _, _ = meshio.read_tri_obj(tmp_path / "seq" / f"{f}.obj")
+        pr = cases.shell_problem(Y, F, density=1000.0, E=1e4, nu=0.4, thickness=0.01, dHat=1e-3)
+        k, km = initialize_oipc(float(pr["mass"].mean()), 1e-6, 1.0)
+        pr["kappa"], pr["kappa_max"] = k, km
+        pb = shell_oracle(oracle, Y, F, pr, (Y - sim.X) / h, X=sim.X, dbc=rows, tol=1e-5)
+        pb.h, pb.b = h, pr["mass"][:, None] * g[None, :]
+        pb.dbc_rows, pb.dbc_target = rows, Y[rows]
+        sim.advance_one_frame(f)
+        sim.write(f)
+        oracle.advance_one_step(pb)
+        assert sim.lv_fn == f + 1
+        assert np.array_equal(sim.X[rows], Y[rows])  # nothing in the way: the rows reach their targets
+        assert np.max(np.abs(sim.X - pb.X)) <= tol
+        Xw, Fw, _ = meshio.read_tri_obj(tmp_path / "out" / f"shell{f}.obj")
+        assert np.array_equal(Fw, F) and np.allclose(Xw, sim.X, rtol=1e-5, atol=1e-6)
+    assert np.max(np.linalg.norm(sim.X - Y, axis=1)) > 1e-3  # gravity pulled the free part off the frame
