@@ -59,7 +59,13 @@ def parse():
     ap.add_argument("--steps", type=int, default=17)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="blob", choices=["blob", "batch256", "bar", "serve", "anim", "shellflow"])
+    ap.add_argument("--workload", default="blob",
+                    choices=["blob", "batch256", "bar", "serve", "anim", "shellflow", "charseq"])
+    ap.add_argument("--charseq-mesh", default="", help="charseq: rest shell (OBJ), e.g. the mannequin wm2_15k.obj; "
+                    "empty: a synthetic bumpy shell")
+    ap.add_argument("--charseq-frames", default="", help="charseq: folder of frame OBJs 1.obj, 2.obj, ... "
+                    "(e.g. Rumba_Dancing_unfixed); empty: synthetic frames")
+    ap.add_argument("--charseq-n", type=int, default=68, help="charseq: background grid of the synthetic shell")
     ap.add_argument("--shell-n", type=int, default=48, help="shellflow: background grid of the blob whose surface is "
                                                             "the shell")
     ap.add_argument("--frames", type=int, default=120, help="anim: keyframes solved")
@@ -512,7 +518,7 @@ def run_reference(args):
     rank, world, local = dist_env()
     if rank != 0:
         return
-    if args.workload in ("serve", "anim", "shellflow"):
+    if args.workload in ("serve", "anim", "shellflow", "charseq"):
         print(json.dumps({"impl": "reference", "unavailable": f"{args.workload}: the reference's CPU path (the "
                           "oracle port) is timed on the blob and batch workloads only"}))
         return
@@ -1089,6 +1095,169 @@ def run_shellflow(args):
     print(json.dumps(out))
 
 
+def charseq_synthetic(n, count, folder):
+    """A synthetic character sequence: the surface of the bumpy blob (lmax 8,
+    amplitude 0.3, seed 0) on an n^3 grid, lifted to stand on y = 0, and
+    frames 1..count written as OBJ files: frame k turns it by k degrees
+    about the vertical axis, leans it by 0.5 k degrees about z and
+    stretches it along y by 1 + 0.003 k."""
+    import numpy as np
+    from idp_gb300 import meshgen, meshio
+
+    Xb, Tb, _ = meshgen.blob(n=n, lmax=8, amp=0.3, seed=0)
+    X, F = meshgen.shell_from_tets(Xb, Tb)
+    X = X - [0.0, X[:, 1].min(), 0.0]
+    rest = os.path.join(folder, "rest.obj")
+    meshio.write_tri_obj(rest, X, F)
+    X, F, _ = meshio.read_tri_obj(rest)
+    for k in range(1, count + 1):
+        a, b = np.deg2rad(1.0 * k), np.deg2rad(0.5 * k)
+        Ry = np.array([[np.cos(a), 0, np.sin(a)], [0, 1, 0], [-np.sin(a), 0, np.cos(a)]])
+        Rz = np.array([[np.cos(b), -np.sin(b), 0], [np.sin(b), np.cos(b), 0], [0, 0, 1]])
+        Y = X * [1.0, 1.0 + 0.003 * k, 1.0]
+        meshio.write_tri_obj(os.path.join(folder, f"{k}.obj"), Y @ (Rz @ Ry).T, F)
+    return rest
+
+
+def oracle_charseq_frames(sim0, F, frames, starts, h, budget_s):
+    """The oracle (FP64, sparse Cholesky) solving frames of the character
+    sequence from the GPU's start states: frame f's rest shape and DBC
+    targets from frames[f], velocity (frame - x)/h, kappa from its masses;
+    at least one frame, more while the time budget lasts."""
+    import numpy as np
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    from idp_gb300.api import initialize_oipc
+
+    O.build()
+    rows = sim0["rows"]
+    out, t_used = [], 0.0
+    for Y, Xs in zip(frames, starts):
+        area = np.linalg.norm(np.cross(Y[F[:, 1]] - Y[F[:, 0]], Y[F[:, 2]] - Y[F[:, 0]]), axis=1) / 2
+        mass = np.zeros(Y.shape[0])
+        np.add.at(mass, F.reshape(-1), np.repeat(area * sim0["thickness"] * sim0["density"] / 3, 3))
+        k, km = initialize_oipc(float(mass.mean()), sim0["dHat2"], 1.0)
+        surf = O.shell_surface(Y.shape[0], F)
+        hin, info = O.shell_hinges(Y, F, surf["edges"])
+        mask = np.zeros(Y.shape[0], np.uint8)
+        mask[rows] = 1
+        pb = O.Problem(X=Xs.copy(), X0=Y, tets=np.zeros((0, 4), np.int32), mass=mass, lam=np.zeros(0),
+                       mu=np.zeros(0), h=h, dHat2=sim0["dHat2"], kappa=[k, km, 0.0], v=(Y - Xs) / h, faces=F,
+                       mem=O.membrane_rest(Y, F, sim0["thickness"], sim0["E"], sim0["nu"]), hinges=hin, hinfo=info,
+                       kbend=O.hinge_stiffness(sim0["E"], sim0["nu"], sim0["thickness"]), dbc=mask, tol=1e-3,
+                       max_iters=500)
+        pb.surf = surf
+        pb.dbc_rows, pb.dbc_target = rows, Y[rows]
+        t0 = time.perf_counter()
+        it = O.advance_one_step(pb)
+        t_used += time.perf_counter() - t0
+        out.append(dict(energy=pb.last_energy, newton_iters=it, X=pb.X))
+        if t_used >= budget_s:
+            break
+    return out, t_used
+
+
+def run_charseq(args):
+    """The character-sequence script (Projects/FEMShell/16_fix_char_seq.py)
+    through the shell driver: the rest shell is loaded turned -90 degrees
+    about x and lifted by 0.75 (add_shell_with_scale_3D), the vertices in
+    the script's box (relative to the bounding box: [-0.1, 0.867, -0.1] to
+    [1.1, 1.1, 1.1]) are DBC rows, dt 0.04, no gravity, density
+    1000, E 100, nu 0.4, thickness 0.01, d-hat 1e-2; every step makes the
+    next frame the rest shape, velocity target and DBC target (lv_fn). W
+    warm-up and K timed frames; value = frames per second of device time
+    of the Newton solves, e2e = frames per second of the whole driver step
+    (frame OBJ read, context rebuild, uploads, solve, readback)."""
+    import tempfile
+
+    import numpy as np
+    import torch
+    import idp_gb300 as idp
+    from idp_gb300 import meshio
+    from idp_gb300.api import ShellFlowSim
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    tmp = tempfile.TemporaryDirectory()
+    nframes = args.warmup + args.steps
+    if args.charseq_mesh:
+        mesh, folder, data = args.charseq_mesh, args.charseq_frames, "reference data files"
+        xf = dict(translate=(0, 0.75, 0), rot=-90)
+    else:
+        folder, data = tmp.name, "synthetic"
+        mesh = charseq_synthetic(args.charseq_n, nframes, folder)
+        xf = dict(translate=(0, 0, 0), rot=0)
+    mode = idp.MODE_MIXED if args.mode == "mixed" else idp.MODE_FP64
+    h = 0.04
+    sim = ShellFlowSim("double", 3, mode=mode)
+    sim.add_shell_with_scale_3D(mesh, xf["translate"], (1, 1, 1), (0, 0, 0), (1, 0, 0), xf["rot"])
+    sim.set_DBC((-0.1, 0.867, -0.1), (1.1, 1.1, 1.1), (0, 0, 0), (0, 0, 0), (1, 0, 0), 0)
+    sim.dt = sim.frame_dt = h
+    sim.gravity = (0.0, 0.0, 0.0)
+    sim.initialize(1000, 100, 0.4, 0.01, 0)
+    sim.initialize_OIPC(1e-2, 0, 1.0)
+    sim.lv_fn, sim.seqDBCPath = 1, folder
+    rows = sim.DBC.indices.copy()
+    V, F = sim.X.shape[0], sim.Elem.copy()
+    for _ in range(args.warmup):
+        sim.advance_one_time_step(h)
+    recs, starts, frames = [], [], []
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            f = sim.lv_fn
+            starts.append(sim.X.copy())
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            it = sim.advance_one_time_step(h)
+            wall = time.perf_counter() - t0
+            st = sim._ctx.stats()
+            Y, _, _ = meshio.read_tri_obj(os.path.join(folder, f"{f}.obj"))
+            frames.append(Y)
+            recs.append(dict(frame=f, ms=st["total_ms"], wall_ms=1000 * wall, newton=it,
+                             pcg=st["pcg_iters"], dbc_gap=float(np.abs(sim.X[rows] - Y[rows]).max()),
+                             launches=st["kernel_launches"]))
+            print(f"frame {f}: {st['total_ms']:.1f} ms device, {1000 * wall:.1f} ms wall, {it} Newton",
+                  file=sys.stderr, flush=True)
+    isect = int(sim._ctx.intersection_counts()[0])
+    if rank != 0:
+        return
+    ms = [r["ms"] for r in recs]
+    wall = [r["wall_ms"] for r in recs]
+    out = {
+        "metric": "per-frame solve time of the character-sequence script (elastic shell, moving DBC rows)",
+        "value": 1000.0 * len(recs) / sum(ms), "unit": "frames/s", "n_gpus": 1, "steps": len(recs),
+        "warmup": args.warmup, "ms_per_step": statistics.mean(ms), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+f64" if mode == idp.MODE_MIXED else "f64", "data": data,
+        "config": {"workload": f"charseq: {os.path.basename(mesh)} ({V} verts, {F.shape[0]} faces, {rows.size} DBC "
+                               f"rows), frames {recs[0]['frame']}..{recs[-1]['frame']} of "
+                               f"{os.path.basename(os.path.normpath(folder)) if args.charseq_mesh else 'synthetic'}"
+                               ", dt 0.04, E 100, nu 0.4, thickness 0.01, d-hat 1e-2, no gravity",
+                   "mode": args.mode, "l2": "working set fits in L2; no flush"},
+        "frame_ms": {"mean": statistics.mean(ms), "p50": float(np.percentile(ms, 50)),
+                     "p99": float(np.percentile(ms, 99)), "max": max(ms)},
+        "newton_iters": [r["newton"] for r in recs],
+        "dbc_gap_max": max(r["dbc_gap"] for r in recs),
+        "final_state_intersections": isect,
+        "e2e": {"value": 1000.0 * len(recs) / sum(wall), "unit": "frames/s", "h2d_bytes_per_step": 3 * V * 8 * 3,
+                "d2h_bytes_per_step": 3 * V * 8 * 2},
+        "gpu_launches": sum(r["launches"] for r in recs),
+        "clocks": clocks.summary(),
+    }
+    if not args.no_cpu_baseline:
+        sim0 = dict(rows=rows, thickness=0.01, density=1000.0, E=100.0, nu=0.4, dHat2=sim.dHat2)
+        ores, t_or = oracle_charseq_frames(sim0, F, frames, starts, h, args.cpu_sample_s)
+        n = len(ores)
+        out["cpu_baseline"] = {"value": n / t_or, "unit": "frames/s", "cores": cpu_cores(), "kind": "port",
+                               "sample": f"oracle (FP64, sparse Cholesky) solving the first {n} timed frame(s) "
+                                         "from the GPU's start states"}
+        out["oracle_check"] = {"newton_iters": [o["newton_iters"] for o in ores],
+                               "max_abs_x_diff": [float(np.abs(o["X"] - s).max()) for o, s in
+                                                  zip(ores, [sim_x for sim_x in starts[1:] + [sim.X]])]}
+    print(json.dumps(out))
+    tmp.cleanup()
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -1099,6 +1268,8 @@ def main():
         run_serve(args)
     elif args.workload == "anim":
         run_anim(args)
+    elif args.workload == "charseq":
+        run_charseq(args)
     elif args.workload == "blob":
         run_flow(args)
     else:

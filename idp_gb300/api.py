@@ -501,7 +501,7 @@ class ShellFlowSim(_DirichletDriver):
             raise ValueError(f"{path}: node count does not match")
         self._X0 = newX
         self.initialize_OIPC(math.sqrt(self.dHat2), self.thickness)  # default stiffMult, as the reference does
-        dirichlet.load_dirichlet(path, 0, (0.0, 0.0, 0.0), self.DBC)
+        dirichlet.targets_from_points(newX, 0, (0.0, 0.0, 0.0), self.DBC)  # Load_Dirichlet of the same file
         self.lv_fn += 1
         if self._ctx is not None:
             self._ctx.close()

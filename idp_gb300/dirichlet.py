@@ -117,7 +117,13 @@ def load_dirichlet(filePath, vIndOffset, translate, DBC):
         Y, _, _ = meshio.read_tri_obj(filePath, np.zeros((0, 3)), np.zeros((0, 3), np.int32))
     except OSError:
         return
-    DBC.rows[:, 1:4] = Y[DBC.indices - int(vIndOffset)] + np.asarray(translate, float)
+    targets_from_points(Y, vIndOffset, translate, DBC)
+
+
+def targets_from_points(Y, vIndOffset, translate, DBC):
+    """What Load_Dirichlet does with the vertices it read: row target =
+    Y[row vertex - vIndOffset] + translate."""
+    DBC.rows[:, 1:4] = np.asarray(Y, float)[DBC.indices - int(vIndOffset)] + np.asarray(translate, float)
 
 
 def pop_back_dirichlet(motion, DBC):

@@ -62,22 +62,39 @@ def read_tri_obj(path, X=None, faces=None):
     X0 = np.zeros((0, 3)) if X is None else np.asarray(X, dtype=np.float64).reshape(-1, 3)
     F0 = np.zeros((0, 3), np.int32) if faces is None else np.asarray(faces, dtype=np.int32).reshape(-1, 3)
     base_v, base_f = X0.shape[0], F0.shape[0]
-    pts, tris = [], []
     with open(path) as f:
-        for line in f:
-            line = line.rstrip("\n")
-            if line.startswith("v "):
-                v = line[2:].split()
-                pts.append([float(v[0]), float(v[1]), float(v[2])])
-            elif line.startswith("f"):
-                tri, quad = _face_indices(line)
-                tri = [t + base_v for t in tri]
-                tris.append(tri)
-                if quad is not None:
-                    tris.append([tri[0], tri[2], quad + base_v])
-    Xn = np.vstack([X0, np.asarray(pts, dtype=np.float64).reshape(-1, 3)])
-    Fn = np.vstack([F0, np.asarray(tris, dtype=np.int32).reshape(-1, 3)])
+        lines = f.read().splitlines()
+    # v lines: the first three numbers after "v " (correctly rounded, as float())
+    vt = [line.split()[1:4] for line in lines if line.startswith("v ")]
+    pts = np.array(vt, dtype=np.float64).reshape(-1, 3)
+    flines = [line for line in lines if line.startswith("f")]
+    tris = _plain_triangles(flines)
+    if tris is None:  # slashes, quads or other forms: the reference's scan, line by line
+        out = []
+        for line in flines:
+            tri, quad = _face_indices(line)
+            out.append(tri)
+            if quad is not None:
+                out.append([tri[0], tri[2], quad])
+        tris = np.asarray(out, dtype=np.int64).reshape(-1, 3)
+    Xn = np.vstack([X0, pts])
+    Fn = np.vstack([F0, (tris + base_v).astype(np.int32)])
     return Xn, Fn, (base_v, base_f, Xn.shape[0], Fn.shape[0])
+
+
+def _plain_triangles(flines):
+    """Zero-based indices of face lines that are all "f i j k", single
+    spaces, positive integers (what _face_indices gives for them), else None."""
+    ft = [line.split() for line in flines]
+    if not all(len(t) == 4 and " ".join(t) == line for t, line in zip(ft, flines)):
+        return None
+    try:
+        tris = np.array([t[1:] for t in ft], dtype=np.int64).reshape(-1, 3)
+    except ValueError:
+        return None
+    if tris.size and tris.min() < 1:
+        return None
+    return tris - 1
 
 
 def read_tet_vtk(path, X=None, tets=None):

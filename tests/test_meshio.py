@@ -22,6 +22,45 @@ def test_obj_reader_faces_quads_and_offsets(tmp_path):
     assert F2[4:].tolist() == (F + 4).tolist()
 
 
+def scan_obj(path):
+    """The reference's OBJ scan line by line: the first three numbers of each
+    "v " line, _face_indices on each "f" line (quads split)."""
+    from idp_gb300 import meshio
+
+    pts, tris = [], []
+    for line in open(path).read().splitlines():
+        if line.startswith("v "):
+            pts.append([float(x) for x in line[2:].split()[:3]])
+        elif line.startswith("f"):
+            tri, quad = meshio._face_indices(line)
+            tris.append(tri)
+            if quad is not None:
+                tris.append([tri[0], tri[2], quad])
+    return np.array(pts, dtype=np.float64).reshape(-1, 3), np.array(tris, dtype=np.int64).reshape(-1, 3)
+
+
+@pytest.mark.parametrize("faces", ["f 1 2 3\nf 3 2 4\n", "f 1 2 3\nf  3 2 4\n", "f 1 2 3\nf 3\t2 4\n",
+                                   "f 1 2 3\nf 3 2 4 1\n", "f 1/7/1 2/8/2 3/9/3\n", "f 1 2 3\nf -1 -2 -3\n",
+                                   "f 1 2 3\nf +3 2 4\n", "f 1 2 3 \n"])
+def test_obj_reader_matches_the_line_scan(tmp_path, faces):
+    """The vectorised reader gives the line-by-line scan's arrays bit for bit:
+    vertex coordinates in shortest-repr, %e and %.17g forms (with and without
+    a w coordinate) and face lines that take the plain-triangle path or fall
+    back to it (extra spaces, tabs, quads, slashes, signs, trailing space)."""
+    from idp_gb300 import meshio
+
+    rng = np.random.default_rng(3)
+    vals = rng.standard_normal((4, 3)) * 10.0 ** rng.integers(-20, 20, (4, 3))
+    fmt = [lambda v: repr(float(v)), lambda v: "%e" % v, lambda v: "%.17g" % v, lambda v: repr(float(v))]
+    body = "".join("v " + " ".join(f(x) for x in row) + (" 1.0" if i == 3 else "") + "\n"
+                   for i, (row, f) in enumerate(zip(vals, fmt)))
+    p = tmp_path / "m.obj"
+    p.write_text(body + faces)
+    X, F, _ = meshio.read_tri_obj(p)
+    Xs, Fs = scan_obj(p)
+    assert np.array_equal(X, Xs) and np.array_equal(F, Fs.astype(np.int32))
+
+
 def test_vtk_round_trip_and_counters(tmp_path):
     from idp_gb300 import meshgen, meshio
 
