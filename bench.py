@@ -1216,7 +1216,8 @@ def run_charseq(args):
             frames.append(Y)
             recs.append(dict(frame=f, ms=st["total_ms"], wall_ms=1000 * wall, newton=it,
                              pcg=st["pcg_iters"], dbc_gap=float(np.abs(sim.X[rows] - Y[rows]).max()),
-                             launches=st["kernel_launches"]))
+                             launches=st["kernel_launches"],
+                             phases={k: st[k + "_ms"] for k in ("pcg", "tet", "contact", "ccd", "barrier", "assembly")}))
             print(f"frame {f}: {st['total_ms']:.1f} ms device, {1000 * wall:.1f} ms wall, {it} Newton",
                   file=sys.stderr, flush=True)
     isect = int(sim._ctx.intersection_counts()[0])
@@ -1237,6 +1238,8 @@ def run_charseq(args):
         "frame_ms": {"mean": statistics.mean(ms), "p50": float(np.percentile(ms, 50)),
                      "p99": float(np.percentile(ms, 99)), "max": max(ms)},
         "newton_iters": [r["newton"] for r in recs],
+        "pcg_iters": [r["pcg"] for r in recs],
+        "phase_ms_mean": {k: statistics.mean(r["phases"][k] for r in recs) for k in recs[0]["phases"]},
         "dbc_gap_max": max(r["dbc_gap"] for r in recs),
         "final_state_intersections": isect,
         "e2e": {"value": 1000.0 * len(recs) / sum(wall), "unit": "frames/s", "h2d_bytes_per_step": 3 * V * 8 * 3,

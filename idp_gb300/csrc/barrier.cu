@@ -337,15 +337,8 @@ __global__ void k_barrier_gh(long C, const int4* __restrict__ cons, const int* _
     write_upper_blocks(H, n, hout + 90 * i);
 }
 
-// The 12x12 PSD projection of makePD (Math/UTILS.h:10-27: eigenvalues below
-// zero set to zero) for the matrices k_barrier_gh found indefinite, one warp
-// per matrix: cyclic Jacobi in round-robin (tournament) order, so each step
-// rotates n/2 disjoint index pairs at once (an odd n gets a dummy index), the
-// rotations' column, row and eigenvector updates spread over the lanes. The
-// rotation formula and the stopping test are those of make_pd; only the
-// order of the rotations differs, so the result agrees with it to rounding.
-constexpr int kPsdWarps = 8;  // warps per CTA
-
+// The 12x12 PSD projection of makePD (Math/UTILS.h:10-27) for the matrices
+// k_barrier_gh found indefinite, one warp per matrix (psd_warp_project).
 template <class T>
 __global__ void __launch_bounds__(32 * kPsdWarps) k_psd_warp(const int* __restrict__ plist,
                                                                const unsigned int* __restrict__ pcount,
@@ -360,88 +353,12 @@ __global__ void __launch_bounds__(32 * kPsdWarps) k_psd_warp(const int* __restri
     for (unsigned int item = blockIdx.x * kPsdWarps + w; item < cnt; item += gridDim.x * kPsdWarps) {
         const int i = plist[item];
         const int n = hn[i];
-        const int m = n + (n & 1);  // players of the tournament
-        const int P = m / 2;         // rotations per step
         for (int k = lane; k < n * n; k += 32) {
             A[k] = hloc[144L * i + k];
             Vm[k] = (k / n == k % n) ? T(1) : T(0);
         }
         __syncwarp();
-        for (int sweep = 0; sweep < 20; ++sweep) {
-            T off = 0, tot = 0;
-            for (int k = lane; k < n * n; k += 32) {
-                const T a = A[k];
-                tot += a * a;
-                if (k / n != k % n) off += a * a;
-            }
-            for (int o = 16; o > 0; o >>= 1) {
-                off += __shfl_xor_sync(0xffffffffu, off, o);
-                tot += __shfl_xor_sync(0xffffffffu, tot, o);
-            }
-            if (off <= (sizeof(T) == 4 ? T(1e-14) : T(1e-30)) * tot || off == T(0)) break;
-            for (int r = 0; r < m - 1; ++r) {
-                if (lane < P) {
-                    int p = lane == 0 ? r : (r + lane) % (m - 1);
-                    int q = lane == 0 ? m - 1 : (r - lane + (m - 1)) % (m - 1);
-                    if (p > q) { const int t = p; p = q; q = t; }
-                    T c = T(1), sn = T(0);
-                    if (q < n) {
-                        const T apq = A[p * n + q];
-                        if (apq != T(0)) {
-                            const T app = A[p * n + p], aqq = A[q * n + q];
-                            const T theta = (aqq - app) / (T(2) * apq);
-                            const T t = (theta >= T(0) ? T(1) : T(-1)) / (fabs(theta) + sqrt(theta * theta + T(1)));
-                            c = T(1) / sqrt(t * t + T(1));
-                            sn = t * c;
-                        }
-                    }
-                    sPQ[w][lane][0] = p;
-                    sPQ[w][lane][1] = q;
-                    sCS[w][lane][0] = c;
-                    sCS[w][lane][1] = sn;
-                }
-                __syncwarp();
-                // columns of A and of V: A <- A J, V <- V J
-                for (int t = lane; t < 2 * P * n; t += 32) {
-                    T* M = t < P * n ? A : Vm;
-                    const int u = t < P * n ? t : t - P * n;
-                    const int j = u / n, k = u % n;
-                    const int p = sPQ[w][j][0], q = sPQ[w][j][1];
-                    if (q >= n) continue;
-                    const T c = sCS[w][j][0], sn = sCS[w][j][1];
-                    const T mp = M[k * n + p], mq = M[k * n + q];
-                    M[k * n + p] = c * mp - sn * mq;
-                    M[k * n + q] = sn * mp + c * mq;
-                }
-                __syncwarp();
-                // rows of A: A <- J^T A
-                for (int t = lane; t < P * n; t += 32) {
-                    const int j = t / n, k = t % n;
-                    const int p = sPQ[w][j][0], q = sPQ[w][j][1];
-                    if (q >= n) continue;
-                    const T c = sCS[w][j][0], sn = sCS[w][j][1];
-                    const T ap = A[p * n + k], aq = A[q * n + k];
-                    A[p * n + k] = c * ap - sn * aq;
-                    A[q * n + k] = sn * ap + c * aq;
-                }
-                __syncwarp();
-            }
-        }
-        if (lane < n) sW[w][lane] = A[lane * n + lane] > T(0) ? A[lane * n + lane] : T(0);
-        __syncwarp();
-        for (int t = lane; t < n * n; t += 32) {
-            const int a = t / n, b = t % n;
-            T acc = 0;
-            for (int k = 0; k < n; ++k) acc += Vm[a * n + k] * sW[w][k] * Vm[b * n + k];
-            A[t] = acc;
-        }
-        __syncwarp();
-        // symmetric by construction up to rounding: mirror the upper triangle
-        for (int t = lane; t < n * n; t += 32) {
-            const int a = t / n, b = t % n;
-            if (a > b) A[t] = A[b * n + a];
-        }
-        __syncwarp();
+        psd_warp_project(A, Vm, n, sCS[w], sPQ[w], sW[w], lane);
         const int nv = n / 3;
         T* ho = hout + 90L * i;
         for (int t = lane; t < 90; t += 32) {

@@ -258,7 +258,7 @@ enum WorkSlot {
     W_BH, W_BG, W_GENT_KEY, W_GENT_VAL, W_GENT_KEY2, W_GENT_VAL2, W_GENT_HEAD,
     W_TAIL_ROWPTR, W_TAIL_COL, W_TAIL_VAL, W_TAIL_KEYS,
     W_BSR_VAL, W_DIAG_INV, W_PCG_VEC, W_PCG_GRID, W_SPAN, W_CBASE, W_DENSE0, W_DENSE1, W_PCG_VEC64, W_CCD_TMP, W_CCD_ALPHA, W_MISC, W_MISC2,
-    W_CL_INT, W_CL_DENSE, W_CL_HOSTCONS, W_PSD, W_SHELL_GRAD, W_CCD_VOX,
+    W_CL_INT, W_CL_DENSE, W_CL_HOSTCONS, W_PSD, W_SHELL_GRAD, W_CCD_VOX, W_SHELL_PSD,
     W_NUM
 };
 struct Work {

@@ -2,7 +2,8 @@
 // reference's makePD (Math/UTILS.h:10-27: eigen-decompose, clamp negative
 // eigenvalues to zero, recompose): a Cholesky test first (a positive definite
 // matrix is left unchanged), else cyclic Jacobi rotations until the
-// off-diagonal part is negligible. One thread per matrix.
+// off-diagonal part is negligible. make_pd takes one thread per matrix,
+// psd_warp_project one warp.
 #pragma once
 #include "common.cuh"
 
@@ -76,6 +77,98 @@ __device__ void make_pd(T* A, int n) {
             A[i * n + j] = s;
             A[j * n + i] = s;
         }
+}
+
+// The cyclic Jacobi sweeps of make_pd run by one warp on an n x n matrix A
+// in shared memory (n <= 12), Vm holding the identity: round-robin
+// (tournament) order, so each step rotates n/2 disjoint index pairs at once
+// (an odd n gets a dummy index), the rotations' column, row and eigenvector
+// updates spread over the lanes. The rotation formula and the stopping test
+// are those of make_pd; only the order of the rotations differs, so the
+// result agrees with it to rounding. On return A holds the projection
+// (eigenvalues below zero set to zero), symmetric. cs, pq and wv are the
+// warp's scratch (6 rotations, 12 eigenvalues).
+constexpr int kPsdWarps = 8;  // warps per CTA of the warp-per-matrix kernels
+
+template <class T>
+__device__ void psd_warp_project(T* A, T* Vm, int n, T (*cs)[2], int (*pq)[2], T* wv, int lane) {
+    const int m = n + (n & 1);  // players of the tournament
+    const int P = m / 2;         // rotations per step
+    for (int sweep = 0; sweep < 20; ++sweep) {
+        T off = 0, tot = 0;
+        for (int k = lane; k < n * n; k += 32) {
+            const T a = A[k];
+            tot += a * a;
+            if (k / n != k % n) off += a * a;
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            off += __shfl_xor_sync(0xffffffffu, off, o);
+            tot += __shfl_xor_sync(0xffffffffu, tot, o);
+        }
+        if (off <= (sizeof(T) == 4 ? T(1e-14) : T(1e-30)) * tot || off == T(0)) break;
+        for (int r = 0; r < m - 1; ++r) {
+            if (lane < P) {
+                int p = lane == 0 ? r : (r + lane) % (m - 1);
+                int q = lane == 0 ? m - 1 : (r - lane + (m - 1)) % (m - 1);
+                if (p > q) { const int t = p; p = q; q = t; }
+                T c = T(1), sn = T(0);
+                if (q < n) {
+                    const T apq = A[p * n + q];
+                    if (apq != T(0)) {
+                        const T app = A[p * n + p], aqq = A[q * n + q];
+                        const T theta = (aqq - app) / (T(2) * apq);
+                        const T t = (theta >= T(0) ? T(1) : T(-1)) / (fabs(theta) + sqrt(theta * theta + T(1)));
+                        c = T(1) / sqrt(t * t + T(1));
+                        sn = t * c;
+                    }
+                }
+                pq[lane][0] = p;
+                pq[lane][1] = q;
+                cs[lane][0] = c;
+                cs[lane][1] = sn;
+            }
+            __syncwarp();
+            // columns of A and of V: A <- A J, V <- V J
+            for (int t = lane; t < 2 * P * n; t += 32) {
+                T* M = t < P * n ? A : Vm;
+                const int u = t < P * n ? t : t - P * n;
+                const int j = u / n, k = u % n;
+                const int p = pq[j][0], q = pq[j][1];
+                if (q >= n) continue;
+                const T c = cs[j][0], sn = cs[j][1];
+                const T mp = M[k * n + p], mq = M[k * n + q];
+                M[k * n + p] = c * mp - sn * mq;
+                M[k * n + q] = sn * mp + c * mq;
+            }
+            __syncwarp();
+            // rows of A: A <- J^T A
+            for (int t = lane; t < P * n; t += 32) {
+                const int j = t / n, k = t % n;
+                const int p = pq[j][0], q = pq[j][1];
+                if (q >= n) continue;
+                const T c = cs[j][0], sn = cs[j][1];
+                const T ap = A[p * n + k], aq = A[q * n + k];
+                A[p * n + k] = c * ap - sn * aq;
+                A[q * n + k] = sn * ap + c * aq;
+            }
+            __syncwarp();
+        }
+    }
+    if (lane < n) wv[lane] = A[lane * n + lane] > T(0) ? A[lane * n + lane] : T(0);
+    __syncwarp();
+    for (int t = lane; t < n * n; t += 32) {
+        const int a = t / n, b = t % n;
+        T acc = 0;
+        for (int k = 0; k < n; ++k) acc += Vm[a * n + k] * wv[k] * Vm[b * n + k];
+        A[t] = acc;
+    }
+    __syncwarp();
+    // symmetric by construction up to rounding: mirror the upper triangle
+    for (int t = lane; t < n * n; t += 32) {
+        const int a = t / n, b = t % n;
+        if (a > b) A[t] = A[b * n + a];
+    }
+    __syncwarp();
 }
 
 }  // namespace

@@ -12,8 +12,9 @@
 // reference. Energies per element are summed per chunk in a fixed tree and
 // chunk sums per instance in order; gradients go to per-element slots that a
 // per-vertex gather sums in a fixed order; element Hessians are evaluated in
-// FP64, projected to PSD (make_pd) and stored as upper 3x3 blocks after the
-// tets' blocks, where the BSR assembly gathers them.
+// FP64, rounded to the working precision, projected to PSD (make_pd, one
+// warp per matrix) and stored as upper 3x3 blocks after the tets' blocks,
+// where the BSR assembly gathers them.
 #include "engine.hpp"
 #include "psd.cuh"
 
@@ -326,8 +327,8 @@ __global__ void k_grad_gather_shell(long V, const int* __restrict__ vinst, const
 }
 
 // the upper 3x3 blocks (a <= b) of an nv-vertex element's 3nv x 3nv matrix
-template <class T>
-__device__ __forceinline__ void store_blocks(const double* H, int nv, T* ho) {
+template <class S, class T>
+__device__ __forceinline__ void store_blocks(const S* H, int nv, T* ho) {
     const int n = 3 * nv;
     int k = 0;
     for (int a = 0; a < nv; ++a)
@@ -336,41 +337,106 @@ __device__ __forceinline__ void store_blocks(const double* H, int nv, T* ho) {
                 for (int e = 0; e < 3; ++e) ho[k * 9 + d * 3 + e] = (T)H[(3 * a + d) * n + 3 * b + e];
 }
 
+// blocks of shell element e: faces e < Fm (6 blocks at 54 e), then hinges
+// (10 blocks at 54 Fm + 90 (e - Fm))
+__device__ __forceinline__ long shell_block_off(long e, long Fm) { return e < Fm ? 54 * e : 54 * Fm + 90 * (e - Fm); }
+
+// an element Hessian (n x n, FP64) in the working precision T: stored as it
+// is when the Cholesky test finds it positive definite, else queued for the
+// warp projection (an element Hessian is singular along its rigid motions,
+// so nearly all are queued)
+template <class T>
+__device__ void shell_element_out(const double* H, int n, long e, long Fm, T* __restrict__ hout,
+                                  T* __restrict__ hloc, int* __restrict__ hn, int* __restrict__ plist,
+                                  unsigned int* __restrict__ pcount) {
+    T Ht[144];
+    for (int k = 0; k < n * n; ++k) Ht[k] = (T)H[k];
+    if (chol_pd(Ht, n)) {
+        store_blocks(Ht, n / 3, hout + shell_block_off(e, Fm));
+        return;
+    }
+    T* hl = hloc + 144 * e;
+    for (int k = 0; k < n * n; ++k) hl[k] = Ht[k];
+    hn[e] = n;
+    plist[atomicAdd(pcount, 1u)] = (int)e;
+}
+
 template <class T>
 __global__ void k_membrane_hess(long Fm, const int* __restrict__ finst, const unsigned char* __restrict__ active,
                                 const double* __restrict__ X, const int* __restrict__ mface,
                                 const double* __restrict__ mem, const unsigned char* __restrict__ dbc, double w,
-                                T* __restrict__ hout) {
+                                T* __restrict__ hout, T* __restrict__ hloc, int* __restrict__ hn,
+                                int* __restrict__ plist, unsigned int* __restrict__ pcount) {
     const long f = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= Fm || !active[finst[f]]) return;
     const int* t = mface + 3 * f;
-    double H[144];
     if (all_fixed(dbc, t, 3)) {
-        for (int i = 0; i < 81; ++i) H[i] = 0.0;
-    } else {
-        membrane_face(ld(X, t[0]), ld(X, t[1]), ld(X, t[2]), mem + 7 * f, w, nullptr, H);
-        make_pd(H, 9);
+        for (int k = 0; k < 54; ++k) hout[54 * f + k] = T(0);
+        return;
     }
-    store_blocks(H, 3, hout + 54 * f);
+    double H[81];
+    membrane_face(ld(X, t[0]), ld(X, t[1]), ld(X, t[2]), mem + 7 * f, w, nullptr, H);
+    shell_element_out(H, 9, f, Fm, hout, hloc, hn, plist, pcount);
 }
 
 template <class T>
 __global__ void k_bending_hess(long Hn, long Fm, const int* __restrict__ hinst, const unsigned char* __restrict__ active,
                                const double* __restrict__ X, const int4* __restrict__ hinge,
                                const double* __restrict__ hk, const unsigned char* __restrict__ dbc, double w,
-                               T* __restrict__ hout) {
+                               T* __restrict__ hout, T* __restrict__ hloc, int* __restrict__ hn,
+                               int* __restrict__ plist, unsigned int* __restrict__ pcount) {
     const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= Hn || !active[hinst[i]]) return;
     const int4 hh = hinge[i];
     const int v[4] = {hh.x, hh.y, hh.z, hh.w};
-    double H[144];
     if (all_fixed(dbc, v, 4)) {
-        for (int q = 0; q < 144; ++q) H[q] = 0.0;
-    } else {
-        bending_hinge(ld(X, v[0]), ld(X, v[1]), ld(X, v[2]), ld(X, v[3]), hk + 2 * i, w, nullptr, H);
-        make_pd(H, 12);
+        for (int q = 0; q < 90; ++q) hout[54 * Fm + 90 * i + q] = T(0);
+        return;
     }
-    store_blocks(H, 4, hout + 54 * Fm + 90 * i);
+    double H[144];
+    bending_hinge(ld(X, v[0]), ld(X, v[1]), ld(X, v[2]), ld(X, v[3]), hk + 2 * i, w, nullptr, H);
+    shell_element_out(H, 12, Fm + i, Fm, hout, hloc, hn, plist, pcount);
+}
+
+// make_pd of the queued element Hessians, one warp per matrix
+// (psd_warp_project), written to the element's blocks
+template <class T>
+__global__ void __launch_bounds__(32 * kPsdWarps) k_shell_psd_warp(const int* __restrict__ plist,
+                                                                     const unsigned int* __restrict__ pcount,
+                                                                     const T* __restrict__ hloc,
+                                                                     const int* __restrict__ hn, long Fm,
+                                                                     T* __restrict__ hout) {
+    __shared__ T sA[kPsdWarps][144], sV[kPsdWarps][144], sCS[kPsdWarps][6][2], sW[kPsdWarps][12];
+    __shared__ int sPQ[kPsdWarps][6][2];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    T* A = sA[w];
+    T* Vm = sV[w];
+    const unsigned int cnt = *pcount;
+    for (unsigned int item = blockIdx.x * kPsdWarps + w; item < cnt; item += gridDim.x * kPsdWarps) {
+        const long e = plist[item];
+        const int n = hn[e];
+        for (int k = lane; k < n * n; k += 32) {
+            A[k] = hloc[144 * e + k];
+            Vm[k] = (k / n == k % n) ? T(1) : T(0);
+        }
+        __syncwarp();
+        psd_warp_project(A, Vm, n, sCS[w], sPQ[w], sW[w], lane);
+        const int nv = n / 3, nb = nv * (nv + 1) / 2;
+        T* ho = hout + shell_block_off(e, Fm);
+        for (int t = lane; t < 9 * nb; t += 32) {
+            const int blk = t / 9, d = (t % 9) / 3, c = t % 3;
+            int a = 0, b = 0, kk = blk;
+            for (a = 0; a < nv; ++a) {
+                if (kk < nv - a) {
+                    b = a + kk;
+                    break;
+                }
+                kk -= nv - a;
+            }
+            ho[t] = A[(3 * a + d) * n + 3 * b + c];
+        }
+        __syncwarp();
+    }
 }
 
 }  // namespace
@@ -412,28 +478,39 @@ int shell_gradient(Arena& A, Work& W, const double* X, double w_h2, double* g, c
 }
 
 // element blocks after the tets' (10 per tet): 6 per face, 10 per hinge
+template <class T>
+static int shell_hessian_t(Arena& A, Work& W, const double* X, double w_h2, T* base, cudaStream_t s) {
+    // PSD queue: local matrices (144 per element) | sizes | list | count
+    const long Ne = A.Fm + A.Hn;
+    const size_t o_n = ((sizeof(T) * 144 * (size_t)Ne) + 255) & ~size_t(255);
+    const size_t o_l = o_n + ((sizeof(int) * (size_t)Ne + 255) & ~size_t(255));
+    const size_t o_c = o_l + ((sizeof(int) * (size_t)Ne + 255) & ~size_t(255));
+    if (W[W_SHELL_PSD].ensure(o_c + 256)) return IDP_ERR_CUDA;
+    char* pb = W[W_SHELL_PSD].as<char>();
+    T* hloc = reinterpret_cast<T*>(pb);
+    int* hn = reinterpret_cast<int*>(pb + o_n);
+    int* plist = reinterpret_cast<int*>(pb + o_l);
+    unsigned int* pcount = reinterpret_cast<unsigned int*>(pb + o_c);
+    IDP_CUDA_TRY(cudaMemsetAsync(pcount, 0, sizeof(unsigned int), s));
+    if (A.Fm)
+        (::idp::count_launch(), k_membrane_hess<T><<<grid_for(A.Fm, 64), 64, 0, s>>>(
+                                    A.Fm, A.finst, A.active, X, A.mface, A.mem, A.dbc_excl, w_h2, base, hloc, hn, plist,
+                                    pcount));
+    if (A.Hn)
+        (::idp::count_launch(), k_bending_hess<T><<<grid_for(A.Hn, 64), 64, 0, s>>>(
+                                    A.Hn, A.Fm, A.hinst, A.active, X, A.hinge, A.hk, A.dbc_excl, w_h2, base, hloc, hn,
+                                    plist, pcount));
+    const int pgrid = (int)std::min<long>((Ne + kPsdWarps - 1) / kPsdWarps, 8L * 152);
+    (::idp::count_launch(), k_shell_psd_warp<T><<<pgrid, 32 * kPsdWarps, 0, s>>>(plist, pcount, hloc, hn, A.Fm, base));
+    return cudaGetLastError() == cudaSuccess ? IDP_OK : IDP_ERR_CUDA;
+}
+
 int shell_hessian(Arena& A, Work& W, const double* X, double w_h2, bool fp64, cudaStream_t s) {
     if (A.Fm == 0 && A.Hn == 0) return IDP_OK;
     const size_t el = fp64 ? sizeof(double) : sizeof(float);
     if (W[W_TET_HESS].ensure(el * 9 * (10 * (A.T + 1) + 6 * A.Fm + 10 * A.Hn))) return IDP_ERR_CUDA;
-    if (fp64) {
-        double* base = W[W_TET_HESS].as<double>() + 90 * A.T;
-        if (A.Fm)
-            (::idp::count_launch(), k_membrane_hess<double><<<grid_for(A.Fm, 64), 64, 0, s>>>(A.Fm, A.finst, A.active, X,
-                                                                                             A.mface, A.mem, A.dbc_excl, w_h2, base));
-        if (A.Hn)
-            (::idp::count_launch(), k_bending_hess<double><<<grid_for(A.Hn, 64), 64, 0, s>>>(A.Hn, A.Fm, A.hinst, A.active, X,
-                                                                                            A.hinge, A.hk, A.dbc_excl, w_h2, base));
-    } else {
-        float* base = W[W_TET_HESS].as<float>() + 90 * A.T;
-        if (A.Fm)
-            (::idp::count_launch(), k_membrane_hess<float><<<grid_for(A.Fm, 64), 64, 0, s>>>(A.Fm, A.finst, A.active, X,
-                                                                                            A.mface, A.mem, A.dbc_excl, w_h2, base));
-        if (A.Hn)
-            (::idp::count_launch(), k_bending_hess<float><<<grid_for(A.Hn, 64), 64, 0, s>>>(A.Hn, A.Fm, A.hinst, A.active, X,
-                                                                                           A.hinge, A.hk, A.dbc_excl, w_h2, base));
-    }
-    return cudaGetLastError() == cudaSuccess ? IDP_OK : IDP_ERR_CUDA;
+    if (fp64) return shell_hessian_t(A, W, X, w_h2, W[W_TET_HESS].as<double>() + 90 * A.T, s);
+    return shell_hessian_t(A, W, X, w_h2, W[W_TET_HESS].as<float>() + 90 * A.T, s);
 }
 
 }  // namespace idp
