@@ -27,7 +27,11 @@ steps and K timed steps continue one flow sequence (20 steps for K=17, W=3).
 
 ``--workload batch256`` (256 bars, tet counts log-uniform in [1k, 50k]) and
 ``--workload bar`` (6x6x24 bar, bend 2.2pi) time one batched solve per step
-from a restored device snapshot instead.
+from a restored device snapshot instead. ``--workload serve`` drives the
+request server with Poisson arrivals, ``anim`` the animation-fix cylinder,
+``shellflow`` flow mode on a triangle shell, and ``charseq`` the
+character-sequence script on an elastic shell (frames/s; the mesh and
+frames by path, or a synthetic turning shell).
 
 ``--impl reference`` times the reference's CPU path (the oracle port: the
 reference does not build in this environment) on the same metric: on the
