@@ -301,6 +301,20 @@ class _DirichletDriver:
         self.seqDBC = -1
         self.seqDBCPath = ""
         self.curFrameNum = 0
+        # rows removed from the back of the motion list over time
+        self.DBCPopBackCounter = 0
+        self.DBCPopBackFrameCounter = 0
+        self.DBCPopBackAmt = 0
+        self.DBCPopBackTStart = 0.0
+        self.DBCPopBackTEnd = -1.0
+        self.DBCPopBackStep = 1
+        self.DBCPopBackBatch = 1
+        # a second motion list over the same rows, with its own time window
+        self.DBCMotion2 = dirichlet.DBCMotion()
+        self.MDBC_tmax2 = -1.0
+        self.MDBC_tmin2 = 0.0
+        self.MDBC_period2 = 1e10
+        self.MDBC_periodCounter2 = 1
 
     def set_DBC(self, DBCRangeMin, DBCRangeMax, v, rotCenter, rotAxis, angVelDeg):
         dirichlet.init_dirichlet(self.X, DBCRangeMin, DBCRangeMax, v, rotCenter, rotAxis, angVelDeg, self.DBC,
@@ -310,7 +324,37 @@ class _DirichletDriver:
         dirichlet.init_dirichlet(self.X, DBCRangeMin, DBCRangeMax, v, rotCenter, rotAxis, angVelDeg, self.DBC,
                                  self.DBCMotion, vIndRange)
 
+    def set_DBC2_with_range(self, DBCRangeMin, DBCRangeMax, v, rotCenter, rotAxis, angVelDeg, vIndRange):
+        dirichlet.init_dirichlet(self.X, DBCRangeMin, DBCRangeMax, v, rotCenter, rotAxis, angVelDeg, self.DBC,
+                                 self.DBCMotion2, vIndRange)
+
+    def load_frame(self, filePath):
+        """Positions from an OBJ file, DBC targets reset to them
+        (FEMDiscreteShellBase.py:244-250)."""
+        from . import meshio
+
+        X, _, _ = meshio.read_tri_obj(filePath)
+        if X.shape != self.X.shape:
+            raise ValueError(f"{filePath}: node count does not match")
+        self.X = X
+        dirichlet.reset_dirichlet(self.X, self.DBC)
+
+    def load_velocity(self, folderPath, lastFrame, h):
+        """Velocity (frame lastFrame - frame lastFrame-1) / h of an OBJ
+        sequence (Load_Velocity, Library/Utils/MESHIO.h:967-984), applied
+        at the next step."""
+        from . import meshio
+
+        X0, _, _ = meshio.read_tri_obj(f"{folderPath}/{lastFrame - 1}.obj")
+        X1, _, _ = meshio.read_tri_obj(f"{folderPath}/{lastFrame}.obj")
+        if X0.shape != self.X.shape or X1.shape != self.X.shape:
+            raise ValueError(f"{folderPath}: node count does not match")
+        self._set_velocity((X1 - X0) / h)
+
     def _step_dbc(self, dt):
+        """The DBC updates before a step (FEMDiscreteShellBase.py:275-299):
+        the first motion list (or the OBJ sequence), pop-backs, the second
+        motion list."""
         if self.MDBC_tmin < self.t < self.MDBC_tmax:
             if self.seqDBC < 0:
                 if self.t - self.MDBC_tmin >= self.MDBC_period * self.MDBC_periodCounter:
@@ -321,6 +365,17 @@ class _DirichletDriver:
                 dirichlet.load_dirichlet(f"{self.seqDBCPath}/shell{self.curFrameNum}.obj", self.seqDBC,
                                          (0.0, -0.75, 0.0), self.DBC)
                 self.curFrameNum += 1
+        if (self.DBCPopBackCounter < self.DBCPopBackAmt and self.DBCPopBackTStart < self.t < self.DBCPopBackTEnd):
+            if self.DBCPopBackFrameCounter % self.DBCPopBackBatch == 0:
+                for _ in range(self.DBCPopBackStep):
+                    dirichlet.pop_back_dirichlet(self.DBCMotion, self.DBC)
+                self.DBCPopBackCounter += 1
+            self.DBCPopBackFrameCounter += 1
+        if self.MDBC_tmin2 < self.t < self.MDBC_tmax2:
+            if self.t - self.MDBC_tmin2 >= self.MDBC_period2 * self.MDBC_periodCounter2:
+                self.MDBC_periodCounter2 += 1
+                dirichlet.turn_dirichlet(self.DBCMotion2)
+            dirichlet.step_dirichlet(self.DBCMotion2, dt, self.DBC)
 
     def _dbc_arg(self):
         return self.DBC if len(self.DBC) else None
@@ -343,6 +398,7 @@ class TetIPCSim(_DirichletDriver):
         self.thickness = 0.0
         self.PNIterCount = 0
         self.mode = mode
+        self.gravity = (0.0, -9.81, 0.0)
         self.bodyForce = None
         self._init_dbc()
 
@@ -371,11 +427,31 @@ class TetIPCSim(_DirichletDriver):
         return counter
 
     def initialize_added_objects(self, velocity, p_density, E, nu):
+        """Masses, velocity, Lame parameters and the gravity body force of the
+        added tets (FEMDiscreteShellBase.py:214-221)."""
         m = meshgen.lumped_mass(self.X, self.tet, p_density)
         lam, mu = meshgen.lame(E, nu)
         T = self.tet.shape[0]
         self.nodeAttr = dict(x0=self.X.copy(), v=np.tile(np.asarray(velocity, float), (self.X.shape[0], 1)), m=m)
         self.tetElasticity = {"lambda": np.full(T, lam), "mu": np.full(T, mu)}
+        self.bodyForce = meshgen.tet_body_force(self.X, self.tet, p_density, self.gravity)
+
+    def adjust_material(self, meshCounter, densityMult, YoungsMult):
+        """Adjust_Material (FEM/Shell/DISCRETE_SHELL.h:532-553): masses and
+        body force of the mesh's vertices scaled by densityMult, its tets'
+        Lame parameters by YoungsMult."""
+        v0, t0, v1, t1 = (int(c) for c in meshCounter)
+        self.nodeAttr["m"][v0:v1] *= densityMult
+        if self.bodyForce is not None:
+            self.bodyForce[v0:v1] *= densityMult
+        self.tetElasticity["lambda"][t0:t1] *= YoungsMult
+        self.tetElasticity["mu"][t0:t1] *= YoungsMult
+
+    def magnify_body_force(self, DBCRangeMin, DBCRangeMax, magnifyFactor):
+        dirichlet.magnify_body_force(self.X, DBCRangeMin, DBCRangeMax, magnifyFactor, self.bodyForce)
+
+    def _set_velocity(self, v):
+        self.nodeAttr["v"][:] = v
 
     def initialize_OIPC(self, dhat, offset, stiffMult=1.0):
         self.dHat2 = dhat * dhat
@@ -423,7 +499,10 @@ class ShellFlowSim(_DirichletDriver):
         self.flow = False
         self.normalFlowMag = 0.0
         self.withCollision = True
-        self.gravity = (0.0, 0.0, 0.0)
+        self.gravity = (0.0, -9.81, 0.0)
+        self.bodyForce = None  # set by initialize: lumped mass x gravity
+        self._bf_dirty = False
+        self._v_next = None
         self.bendingStiffMult = 1.0
         self.shell_density = 1000.0
         self.shell_E = 1e5
@@ -472,13 +551,44 @@ class ShellFlowSim(_DirichletDriver):
 
     def initialize(self, p_density, E, nu, thickness, caseI):
         """Shell material (Initialize_Shell_Hinge_EIPC's density, E, nu and
-        thickness; E and nu do not enter the flow energy); in flow mode the
-        open boundary's vertices are fixed (FEM.Boundary_Dirichlet)."""
+        thickness; E and nu do not enter the flow energy), gravity off when
+        caseI is nonzero, the body force lumped mass x gravity
+        (FEMDiscreteShellBase.py:190-203); in flow mode the open boundary's
+        vertices are fixed (FEM.Boundary_Dirichlet)."""
         self.shell_density, self.shell_thickness = float(p_density), float(thickness)
         self.shell_E, self.shell_nu = float(E), float(nu)
         self.thickness = float(thickness)
+        if caseI != 0:
+            self.gravity = (0.0, 0.0, 0.0)
+        self.bodyForce = self._gravity_force(self.X)
         if self.flow:
             dirichlet.boundary_dirichlet(self.X, self.Elem, self.DBC)
+
+    def _gravity_force(self, X):
+        return self._mass(X)[:, None] * np.asarray(self.gravity, float)[None, :]
+
+    def add_mannequin(self, filePath, translate, scale, rotCenter, rotAxis, rotDeg):
+        """A shell whose every vertex is a fixed DBC row
+        (FEMDiscreteShellBase.py:152-157: moved 1e6 along x so that the box
+        x >= 0.5 of the bounding box holds exactly its vertices, set_DBC,
+        moved back, targets reset to the positions)."""
+        from . import meshio
+
+        counter = self.add_shell_with_scale_3D(filePath, translate, scale, rotCenter, rotAxis, rotDeg)
+        meshio.transform_points(self.X, (1e6, 0, 0), (0, 0, 0), (1, 0, 0), 0, (1, 1, 1), counter)
+        self.set_DBC((0.5, -1, -1), (1.1, 1.1, 1.1), (0, 0, 0), (0, 0, 0), (1, 0, 0), 0)
+        meshio.transform_points(self.X, (-1e6, 0, 0), (0, 0, 0), (1, 0, 0), 0, (1, 1, 1), counter)
+        dirichlet.reset_dirichlet(self.X, self.DBC)
+        return counter
+
+    def magnify_body_force(self, DBCRangeMin, DBCRangeMax, magnifyFactor):
+        if self.bodyForce is None:
+            self.bodyForce = self._gravity_force(self.X if self._X0 is None else self._X0)
+        dirichlet.magnify_body_force(self.X, DBCRangeMin, DBCRangeMax, magnifyFactor, self.bodyForce)
+        self._bf_dirty = True
+
+    def _set_velocity(self, v):
+        self._v_next = np.array(v, dtype=np.float64).reshape(-1, 3)
 
     def initialize_OIPC(self, thickness, offset, stiffMult=1.0):
         """Initialize_OIPC (DISCRETE_SHELL.h:555-577): d-hat = thickness,
@@ -500,6 +610,7 @@ class ShellFlowSim(_DirichletDriver):
         if newX.shape != self.X.shape:
             raise ValueError(f"{path}: node count does not match")
         self._X0 = newX
+        self.bodyForce = self._gravity_force(newX)
         self.initialize_OIPC(math.sqrt(self.dHat2), self.thickness)  # default stiffMult, as the reference does
         dirichlet.targets_from_points(newX, 0, (0.0, 0.0, 0.0), self.DBC)  # Load_Dirichlet of the same file
         self.lv_fn += 1
@@ -532,8 +643,10 @@ class ShellFlowSim(_DirichletDriver):
                                                      dbc_idx=dbc_idx)
                 if v is not None:
                     self._ctx.set_velocity(0, v)
-                if any(g != 0 for g in self.gravity):  # b = M g (Initialize_Discrete_Shell)
-                    self._ctx.set_body_force(0, self._mass(self._X0)[:, None] * np.asarray(self.gravity, float)[None, :])
+                b = self._gravity_force(self._X0) if self.bodyForce is None else self.bodyForce
+                if np.any(b != 0):  # b = M g (Initialize_Discrete_Shell)
+                    self._ctx.set_body_force(0, b)
+                self._bf_dirty = False
             self._ctx.commit()
             self._ctx_h = h
         return self._ctx
@@ -550,6 +663,12 @@ class ShellFlowSim(_DirichletDriver):
                 raise ValueError("lv_fn frame sequences drive the elastic shell; set flow = False")
             v_seq = self._next_frame_rest_shape(dt)
         ctx = self._context(dt)
+        if self._v_next is not None:  # load_velocity
+            ctx.set_velocity(0, self._v_next)
+            self._v_next = None
+        if self._bf_dirty and not self.flow:  # magnify_body_force after the context was built
+            ctx.set_body_force(0, self.bodyForce)
+            self._bf_dirty = False
         if v_seq is not None:
             ctx.set_velocity(0, v_seq)
         ctx.set_positions(0, self.X)

@@ -246,14 +246,27 @@ def bar_batch(count=256, tmin=1_000, tmax=50_000, seed=0):
     return out
 
 
+def _tet_volumes(X, tets):
+    d = X[tets[:, 1:]] - X[tets[:, :1]]
+    return np.einsum("ti,ti->t", d[:, 0], np.cross(d[:, 1], d[:, 2])) / 6.0
+
+
 def lumped_mass(X, tets, density):
     """Per-vertex lumped mass, vol * density / 4 per tet corner
     (FEM/ELEM_TO_NODE.h:11-46)."""
-    d = X[tets[:, 1:]] - X[tets[:, :1]]
-    vol = np.einsum("ti,ti->t", d[:, 0], np.cross(d[:, 1], d[:, 2])) / 6.0
     m = np.zeros(X.shape[0])
-    np.add.at(m, tets.reshape(-1), np.repeat(vol * density / 4.0, 4))
+    np.add.at(m, tets.reshape(-1), np.repeat(_tet_volumes(X, tets) * density / 4.0, 4))
     return m
+
+
+def tet_body_force(X, tets, density, acc):
+    """Body force of a body acceleration acc (V x 3): (vol * density / 4) acc
+    added per tet corner, tets in order (Augment_Mass_Matrix_And_Body_Force,
+    FEM/ELEM_TO_NODE.h:49-87)."""
+    each = _tet_volumes(X, tets) * density / 4.0
+    b = np.zeros((X.shape[0], 3))
+    np.add.at(b, tets.reshape(-1), np.repeat(each, 4)[:, None] * np.asarray(acc, float)[None, :])
+    return b
 
 
 def lame(E, nu):

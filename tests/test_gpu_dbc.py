@@ -151,6 +151,7 @@ def test_twisting_bar_driver_matches_oracle(oracle, gpu_lib):
 
     X, tets = meshgen.bar(2, 2, 6, size=(1.0, 1.0, 3.0), seed=0)
     sim = TetIPCSim(dt=0.1, PNTol=1e-5, mode=idp.MODE_FP64)
+    sim.gravity = (0.0, 0.0, 0.0)  # Dirichlet motion only
     sim.add_object_3D(X, tets)
     sim.initialize_added_objects((0.0, 0.0, 0.0), 1000.0, 1e4, 0.3)
     sim.initialize_OIPC(1e-3 * float(np.linalg.norm(X.max(0) - X.min(0))), 0.0)
