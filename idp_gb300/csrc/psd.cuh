@@ -1,9 +1,9 @@
 // PSD projection of a small symmetric matrix (n <= 12), following the
 // reference's makePD (Math/UTILS.h:10-27: eigen-decompose, clamp negative
-// eigenvalues to zero, recompose): a Cholesky test first (a positive definite
-// matrix is left unchanged), else cyclic Jacobi rotations until the
-// off-diagonal part is negligible. make_pd takes one thread per matrix,
-// psd_warp_project one warp.
+// eigenvalues to zero, recompose): a per-thread Cholesky test first (a
+// positive definite matrix is left unchanged, chol_pd), else cyclic Jacobi
+// rotations by one warp until the off-diagonal part is negligible
+// (psd_warp_project).
 #pragma once
 #include "common.cuh"
 
@@ -28,66 +28,17 @@ __device__ bool chol_pd(const T* A, int n) {
     return true;
 }
 
-template <class T>
-__device__ void make_pd(T* A, int n) {
-    if (chol_pd(A, n)) return;
-    T V[144];
-    for (int i = 0; i < n * n; ++i) V[i] = T(0);
-    for (int i = 0; i < n; ++i) V[i * n + i] = T(1);
-    for (int sweep = 0; sweep < 20; ++sweep) {
-        T off = 0, tot = 0;
-        for (int i = 0; i < n; ++i)
-            for (int j = 0; j < n; ++j) {
-                T a = A[i * n + j];
-                tot += a * a;
-                if (i != j) off += a * a;
-            }
-        if (off <= (sizeof(T) == 4 ? T(1e-14) : T(1e-30)) * tot || off == T(0)) break;
-        for (int p = 0; p < n - 1; ++p)
-            for (int q = p + 1; q < n; ++q) {
-                T apq = A[p * n + q];
-                if (apq == T(0)) continue;
-                T app = A[p * n + p], aqq = A[q * n + q];
-                T theta = (aqq - app) / (T(2) * apq);
-                T t = (theta >= T(0) ? T(1) : T(-1)) / (fabs(theta) + sqrt(theta * theta + T(1)));
-                T c = T(1) / sqrt(t * t + T(1)), s = t * c;
-                for (int k = 0; k < n; ++k) {
-                    T akp = A[k * n + p], akq = A[k * n + q];
-                    A[k * n + p] = c * akp - s * akq;
-                    A[k * n + q] = s * akp + c * akq;
-                }
-                for (int k = 0; k < n; ++k) {
-                    T apk = A[p * n + k], aqk = A[q * n + k];
-                    A[p * n + k] = c * apk - s * aqk;
-                    A[q * n + k] = s * apk + c * aqk;
-                }
-                for (int k = 0; k < n; ++k) {
-                    T vkp = V[k * n + p], vkq = V[k * n + q];
-                    V[k * n + p] = c * vkp - s * vkq;
-                    V[k * n + q] = s * vkp + c * vkq;
-                }
-            }
-    }
-    T w[12];
-    for (int i = 0; i < n; ++i) w[i] = A[i * n + i] > T(0) ? A[i * n + i] : T(0);
-    for (int i = 0; i < n; ++i)
-        for (int j = i; j < n; ++j) {
-            T s = 0;
-            for (int k = 0; k < n; ++k) s += V[i * n + k] * w[k] * V[j * n + k];
-            A[i * n + j] = s;
-            A[j * n + i] = s;
-        }
-}
-
-// The cyclic Jacobi sweeps of make_pd run by one warp on an n x n matrix A
-// in shared memory (n <= 12), Vm holding the identity: round-robin
-// (tournament) order, so each step rotates n/2 disjoint index pairs at once
-// (an odd n gets a dummy index), the rotations' column, row and eigenvector
-// updates spread over the lanes. The rotation formula and the stopping test
-// are those of make_pd; only the order of the rotations differs, so the
-// result agrees with it to rounding. On return A holds the projection
-// (eigenvalues below zero set to zero), symmetric. cs, pq and wv are the
-// warp's scratch (6 rotations, 12 eigenvalues).
+// Cyclic Jacobi sweeps run by one warp on an n x n matrix A in shared
+// memory (n <= 12), Vm holding the identity. Each rotation of a pair (p, q)
+// uses theta = (a_qq - a_pp) / (2 a_pq), t = sign(theta) / (|theta| +
+// sqrt(theta^2 + 1)), c = 1 / sqrt(t^2 + 1), s = t c; a sweep visits every
+// pair in round-robin (tournament) order, so each step rotates n/2 disjoint
+// pairs at once (an odd n gets a dummy index), the rotations' column, row
+// and eigenvector updates spread over the lanes. Sweeps stop once the
+// squared off-diagonal part is at most 1e-14 (FP32) or 1e-30 (FP64) of the
+// squared total, after 20 at most. On return A holds the projection
+// V max(Lambda, 0) V^T, symmetric. cs, pq and wv are the warp's scratch (6
+// rotations, 12 eigenvalues).
 constexpr int kPsdWarps = 8;  // warps per CTA of the warp-per-matrix kernels
 
 template <class T>

@@ -12,7 +12,7 @@
 // reference. Energies per element are summed per chunk in a fixed tree and
 // chunk sums per instance in order; gradients go to per-element slots that a
 // per-vertex gather sums in a fixed order; element Hessians are evaluated in
-// FP64, rounded to the working precision, projected to PSD (make_pd, one
+// FP64, rounded to the working precision, projected to PSD (makePD, one
 // warp per matrix) and stored as upper 3x3 blocks after the tets' blocks,
 // where the BSR assembly gathers them.
 #include "engine.hpp"
@@ -398,7 +398,7 @@ __global__ void k_bending_hess(long Hn, long Fm, const int* __restrict__ hinst, 
     shell_element_out(H, 12, Fm + i, Fm, hout, hloc, hn, plist, pcount);
 }
 
-// make_pd of the queued element Hessians, one warp per matrix
+// makePD of the queued element Hessians, one warp per matrix
 // (psd_warp_project), written to the element's blocks
 template <class T>
 __global__ void __launch_bounds__(32 * kPsdWarps) k_shell_psd_warp(const int* __restrict__ plist,
