@@ -1123,7 +1123,7 @@ def charseq_synthetic(n, count, folder):
     return rest
 
 
-def oracle_charseq_frames(sim0, F, frames, starts, h, budget_s):
+def oracle_charseq_frames(shell, F, frames, starts, h, budget_s):
     """The oracle (FP64, sparse Cholesky) solving frames of the character
     sequence from the GPU's start states: frame f's rest shape and DBC
     targets from frames[f], velocity (frame - x)/h, kappa from its masses;
@@ -1135,21 +1135,21 @@ def oracle_charseq_frames(sim0, F, frames, starts, h, budget_s):
     from idp_gb300.api import initialize_oipc
 
     O.build()
-    rows = sim0["rows"]
+    rows = shell["rows"]
     out, t_used = [], 0.0
     for Y, Xs in zip(frames, starts):
         area = np.linalg.norm(np.cross(Y[F[:, 1]] - Y[F[:, 0]], Y[F[:, 2]] - Y[F[:, 0]]), axis=1) / 2
         mass = np.zeros(Y.shape[0])
-        np.add.at(mass, F.reshape(-1), np.repeat(area * sim0["thickness"] * sim0["density"] / 3, 3))
-        k, km = initialize_oipc(float(mass.mean()), sim0["dHat2"], 1.0)
+        np.add.at(mass, F.reshape(-1), np.repeat(area * shell["thickness"] * shell["density"] / 3, 3))
+        k, km = initialize_oipc(float(mass.mean()), shell["dHat2"], 1.0)
         surf = O.shell_surface(Y.shape[0], F)
         hin, info = O.shell_hinges(Y, F, surf["edges"])
         mask = np.zeros(Y.shape[0], np.uint8)
         mask[rows] = 1
         pb = O.Problem(X=Xs.copy(), X0=Y, tets=np.zeros((0, 4), np.int32), mass=mass, lam=np.zeros(0),
-                       mu=np.zeros(0), h=h, dHat2=sim0["dHat2"], kappa=[k, km, 0.0], v=(Y - Xs) / h, faces=F,
-                       mem=O.membrane_rest(Y, F, sim0["thickness"], sim0["E"], sim0["nu"]), hinges=hin, hinfo=info,
-                       kbend=O.hinge_stiffness(sim0["E"], sim0["nu"], sim0["thickness"]), dbc=mask, tol=1e-3,
+                       mu=np.zeros(0), h=h, dHat2=shell["dHat2"], kappa=[k, km, 0.0], v=(Y - Xs) / h, faces=F,
+                       mem=O.membrane_rest(Y, F, shell["thickness"], shell["E"], shell["nu"]), hinges=hin, hinfo=info,
+                       kbend=O.hinge_stiffness(shell["E"], shell["nu"], shell["thickness"]), dbc=mask, tol=1e-3,
                        max_iters=500)
         pb.surf = surf
         pb.dbc_rows, pb.dbc_target = rows, Y[rows]
@@ -1215,7 +1215,7 @@ def run_charseq(args):
             t0 = time.perf_counter()
             it = sim.advance_one_time_step(h)
             wall = time.perf_counter() - t0
-            st = sim._ctx.stats()
+            st = sim.context.stats()
             Y, _, _ = meshio.read_tri_obj(os.path.join(folder, f"{f}.obj"))
             frames.append(Y)
             recs.append(dict(frame=f, ms=st["total_ms"], wall_ms=1000 * wall, newton=it,
@@ -1224,7 +1224,7 @@ def run_charseq(args):
                              phases={k: st[k + "_ms"] for k in ("pcg", "tet", "contact", "ccd", "barrier", "assembly")}))
             print(f"frame {f}: {st['total_ms']:.1f} ms device, {1000 * wall:.1f} ms wall, {it} Newton",
                   file=sys.stderr, flush=True)
-    isect = int(sim._ctx.intersection_counts()[0])
+    isect = int(sim.context.intersection_counts()[0])
     if rank != 0:
         return
     ms = [r["ms"] for r in recs]
@@ -1252,8 +1252,8 @@ def run_charseq(args):
         "clocks": clocks.summary(),
     }
     if not args.no_cpu_baseline:
-        sim0 = dict(rows=rows, thickness=0.01, density=1000.0, E=100.0, nu=0.4, dHat2=sim.dHat2)
-        ores, t_or = oracle_charseq_frames(sim0, F, frames, starts, h, args.cpu_sample_s)
+        shell = dict(rows=rows, thickness=0.01, density=1000.0, E=100.0, nu=0.4, dHat2=sim.dHat2)
+        ores, t_or = oracle_charseq_frames(shell, F, frames, starts, h, args.cpu_sample_s)
         n = len(ores)
         out["cpu_baseline"] = {"value": n / t_or, "unit": "frames/s", "cores": cpu_cores(), "kind": "port",
                                "sample": f"oracle (FP64, sparse Cholesky) solving the first {n} timed frame(s) "

@@ -619,6 +619,12 @@ class ShellFlowSim(_DirichletDriver):
             self._ctx = None
         return (newX - self.X) / dt
 
+    @property
+    def context(self):
+        """The device context of the last step (None before the first): its
+        stats(), state() and intersection_counts()."""
+        return self._ctx
+
     def _context(self, h):
         if self._ctx is not None and self._dbc_n != len(self.DBC):  # the DBC rows changed: rebuild
             self._ctx_h = None
