@@ -121,3 +121,35 @@ def test_tet_sim_reads_vtk(tmp_path):
     assert cnt2[0] == X.shape[0] and sim.tet.shape[0] == 2 * T.shape[0]
     assert np.allclose(sim.X[: X.shape[0]], X + [1.0, 0.0, 0.0])
     assert np.allclose(sim.X[X.shape[0]:], X + [0.0, 5.0, 0.0])
+
+
+def test_obj_reader_matches_the_line_scan_on_random_faces(tmp_path):
+    """Random face lines (index forms i, i/j, i//k, i/j/k; one or two spaces,
+    tabs, trailing blanks, signs, quads) and plain ones: the reader's arrays
+    equal the line scan's."""
+    hyp = pytest.importorskip("hypothesis")
+    st = pytest.importorskip("hypothesis.strategies")
+    from idp_gb300 import meshio
+
+    idx = st.integers(1, 9)
+    token = st.one_of(idx.map(str), st.tuples(idx, idx).map(lambda t: f"{t[0]}/{t[1]}"),
+                      st.tuples(idx, idx).map(lambda t: f"{t[0]}//{t[1]}"), idx.map(lambda i: f"+{i}"),
+                      st.tuples(idx, idx, idx).map(lambda t: f"{t[0]}/{t[1]}/{t[2]}"))
+    sep = st.sampled_from([" ", " ", " ", "  ", "\t"])
+    face = st.tuples(st.lists(st.tuples(sep, token), min_size=3, max_size=4), st.sampled_from(["", " ", "\t"])).map(
+        lambda t: "f" + "".join(a + b for a, b in t[0]) + t[1])
+    plain = st.lists(idx, min_size=3, max_size=3).map(lambda t: "f " + " ".join(map(str, t)))
+    body = "".join(f"v {i} {2 * i} {3 * i}\n" for i in range(9))
+    n = [0]
+
+    @hyp.settings(max_examples=150, deadline=None)
+    @hyp.given(st.lists(st.one_of(face, plain), min_size=1, max_size=6))
+    def check(lines):
+        n[0] += 1
+        p = tmp_path / f"r{n[0]}.obj"
+        p.write_text(body + "\n".join(lines) + "\n")
+        X, F, _ = meshio.read_tri_obj(p)
+        Xs, Fs = scan_obj(p)
+        assert np.array_equal(X, Xs) and np.array_equal(F, Fs.astype(np.int32))
+
+    check()
